@@ -1,0 +1,315 @@
+"""Benchmark: exciton hops/s of the Green-Kubo hot path on GB300.
+
+Workload (one "step" = all excitons advanced by one MSD bin of 1 ps):
+  film: 100 straight tubes x 200 nm, uniform centres in a 500 x 500 x 10 nm box, azimuth U[0, pi),
+        z-tilt U[-5, 5] deg, 1 nm segments (20,000 sites), 10 nm hopping cutoff, 2-D
+        (distance 0.5-10 nm x angle 0-90 deg) Förster-form rate table;
+  1,000,000 excitons injected uniformly at random sites, Philox seed 1, MSD sampled every 1 ps,
+  exciton velocity 2e5 m/s.  Synthetic film (the reference's meshes are not available).
+value: hops/s of the mixed-precision kernel, device time from CUDA events on the launching
+stream, max over ranks; e2e: the same metric through the public API from host buffers (film and
+table uploaded, neighbour lists built, excitons created, K steps run, MSD read back).
+Multi-GPU (torchrun): independent replicas (seed + rank), weak scaling, no collective on the
+data path.  --impl reference times the reference's algorithm (the oracle's restatement, which
+recomputes every neighbour list on every hop like src/monte_carlo/scatterer.cpp:9-31) on the host
+cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FILM = dict(n_tubes=100, length_nm=200.0, box_nm=(500.0, 500.0, 10.0), tilt_deg=5.0, film_seed=1234)
+R_MAX, VEL, BIN = 10e-9, 2e5, 1e-12
+N_EXC, SEED = 1_000_000, 1
+METRIC = "exciton hops/s (Green-Kubo hop kernel)"
+UNIT = "hops/s"
+
+
+def workload():
+    from cnt_film_monte_carlo_gb300 import film as F
+    from cnt_film_monte_carlo_gb300 import tables
+
+    f = F.straight_tubes(FILM["n_tubes"], FILM["length_nm"], box_nm=FILM["box_nm"], max_tilt_deg=FILM["tilt_deg"],
+                         seed=FILM["film_seed"])
+    return f, tables.forster_2d(1e15)
+
+
+def config(n_exc, bins_per_step, extra=None):
+    c = {"workload": "cfg2 film: 100 tubes x 200 nm, 500x500x10 nm, 1 nm segments, 10 nm cutoff, 2-D rate table; "
+                     f"{n_exc} excitons uniform injection; MSD bin 1 ps; {bins_per_step} bin(s) per step",
+         "n_sites": FILM["n_tubes"] * int(FILM["length_nm"]), "n_excitons": n_exc, "bin_s": BIN,
+         "bins_per_step": bins_per_step, "precision": "mixed (FP32 cumulative rates, exact FP64 re-resolve)",
+         "l2": "256 MB buffer written between timed steps (working set ~15 MB CSR is L2-resident by size)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.p is None:
+            return
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def bytes_per_hop(k_mean, fp32=True):
+    """Algorithmic bytes of one hop: the destination's 32-byte site record, one 32-byte sector of
+    the neighbour index, and one sector per bisection probe that leaves the previous sector
+    (8 FP32 or 4 FP64 cumulative entries per sector)."""
+    lg = math.ceil(math.log2(max(k_mean, 2.0)))
+    s = max(1, lg - (3 if fp32 else 2))
+    return 32 + 32 + 32 * s
+
+
+def cpu_sample(f, tab, target_cpu_s=15.0, threads=None, steps=1):
+    """The reference's algorithm on the host cores: the oracle restatement with a fresh neighbour
+    search on every hop (scatterer.cpp:9-31), OpenMP over excitons."""
+    from oracle import oracle as O
+
+    threads = threads or os.cpu_count() or 1
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, R_MAX, VEL, n_threads=threads)
+    n = max(threads * 4, 64)
+    sim.create_excitons(1, 0, n, SEED, use_csr=False)
+    t0 = time.perf_counter()
+    sim.step(BIN / 20, 1)
+    dt = time.perf_counter() - t0
+    rate = sim.total_hops() / max(dt, 1e-9)
+    hops_per_exc_bin = max(sim.total_hops() / n * 20, 1.0)
+    n = int(max(threads, min(N_EXC, target_cpu_s / threads * rate / hops_per_exc_bin / steps)))
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, R_MAX, VEL, n_threads=threads)
+    sim.create_excitons(1, 0, n, SEED, use_csr=False)
+    t0 = time.perf_counter()
+    sim.step(BIN, steps)
+    dt = time.perf_counter() - t0
+    return sim.total_hops() / dt, threads, f"{n} excitons x {steps} x 1 ps bins of the same film ({sim.total_hops()} hops, {dt:.2f} s)"
+
+
+def reference_arm(args):
+    f, tab = workload()
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, cores, sample = cpu_sample(f, tab, target_cpu_s=args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(N_EXC, 1, {"sample": sample}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-exc", type=int, default=N_EXC)
+    ap.add_argument("--bins-per-step", type=int, default=1)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        return
+
+    import torch
+
+    from cnt_film_monte_carlo_gb300 import _lib as L
+    from cnt_film_monte_carlo_gb300 import build as B
+    from cnt_film_monte_carlo_gb300 import engine as E
+
+    B.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    f, tab = workload()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    e = E.Engine(local)
+    e.load_films(f)
+    e.set_table(tab)
+    st = e.build(R_MAX)
+    e.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+    bins = args.bins_per_step
+    for _ in range(args.warmup):
+        e.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
+    h0 = e.stats()["hops"]
+    dev_ms, launches = 0.0, 0
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
+            s = e.stats()
+            dev_ms += s["last_run_ms"]
+            launches += s["last_launches"]
+        barrier()
+        wall = time.perf_counter() - t0
+    hops = e.stats()["hops"] - h0
+    msd = e.msd(0, e.stats()["steps_done"])[0]
+    t_end = e.stats()["steps_done"] * BIN
+    d_eff = (msd[-1] / args.n_exc / (2 * t_end)).tolist()
+    e.close()
+    dev_s = dev_ms / 1e3
+    if dist is not None:
+        t = torch.tensor([dev_s, wall, float(hops)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        dev_s_max, wall_max, hops_all = mx[0].item(), mx[1].item(), t[2].item()
+    else:
+        dev_s_max, wall_max, hops_all = dev_s, wall, float(hops)
+    value = hops_all / dev_s_max
+
+    # plain FP64 kernel on the same workload (same seeds; same hop sequence)
+    fp64 = None
+    if args.fp64_steps > 0:
+        e2 = E.Engine(local)
+        e2.load_films(f)
+        e2.set_table(tab)
+        e2.build(R_MAX)
+        e2.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+        e2.run(args.warmup * bins, BIN, VEL, L.KMC_PREC_FP64)
+        h1 = e2.stats()["hops"]
+        ms = 0.0
+        for _ in range(args.fp64_steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e2.run(bins, BIN, VEL, L.KMC_PREC_FP64)
+            ms += e2.stats()["last_run_ms"]
+        fp64 = (e2.stats()["hops"] - h1) / (ms / 1e3)
+        e2.close()
+
+    # end to end through the public API from host buffers
+    e2e = None
+    if not args.no_e2e:
+        barrier()
+        t0 = time.perf_counter()
+        e3 = E.Engine(local)
+        e3.load_films(f)
+        e3.set_table(tab)
+        e3.build(R_MAX)
+        e3.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+        for _ in range(args.steps):
+            e3.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
+        out = e3.msd(0, args.steps * bins)
+        h3 = e3.stats()["hops"]
+        e3.close()
+        barrier()
+        w3 = time.perf_counter() - t0
+        h2d = f.n_sites * (3 * 8 * 2 + 2 * 4) + 8 * 2 + tab["rate"].nbytes + sum(g.nbytes for g in tab["grids"]) + 16
+        e2e = {"value": h3 * world / w3, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": int(out.nbytes / args.steps), "seconds": w3,
+               "includes": "film+table upload, neighbour build, exciton creation, K steps, MSD read-back"}
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    bph = bytes_per_hop(st["k_mean"], fp32=True)
+    achieved = hops / dev_s * bph / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "hop_mixed_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            pj = json.load(fh)
+        traffic = pj.get("dram_bytes_per_hop", 0) * hops / max(launches, 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+f32", "data": "synthetic",
+        "config": config(args.n_exc, bins, {"k_mean": st["k_mean"], "nnz": st["nnz"], "hops_timed": hops}),
+        "fp64_plain_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
+        "d_eff_m2_per_s": d_eff,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "bytes_per_hop": bph,
+                     "note": "algorithmic bytes per hop x hops / hop-kernel device time; CSR is L2-resident"},
+        "gpu_launches": launches,
+        "e2e": e2e,
+        "clocks": clk.summary(),
+    }
+    if world == 1 and not args.no_cpu:
+        v, cores, sample = cpu_sample(f, tab, target_cpu_s=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

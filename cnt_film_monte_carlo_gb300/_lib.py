@@ -1,0 +1,113 @@
+"""ctypes bindings of libcntkmc.so (include/cntkmc.h).
+
+The shared library is built in-tree by ``cnt_film_monte_carlo_gb300.build``.  Loading fails
+loudly when it is missing: there is no CPU fallback for any engine call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcntkmc.so")
+
+KMC_OK = 0
+KMC_ERR_ARG = -1
+KMC_ERR_CUDA = -2
+KMC_ERR_STATE = -3
+KMC_ERR_IO = -4
+KMC_ERR_HOP_CAP = -5
+KMC_ERR_NOMEM = -6
+KMC_ERR_NO_DEVICE = -7
+KMC_TABLE_4D = 4
+KMC_TABLE_2D = 2
+KMC_INJECT_REGION = 0
+KMC_INJECT_UNIFORM = 1
+KMC_PREC_FP64 = 0
+KMC_PREC_MIXED = 1
+
+PD = C.POINTER(C.c_double)
+PI32 = C.POINTER(C.c_int32)
+PI64 = C.POINTER(C.c_int64)
+PU64 = C.POINTER(C.c_uint64)
+
+
+class kmc_film(C.Structure):
+    _fields_ = [("n_films", C.c_int32), ("film_site_offsets", PI64), ("pos", PD), ("orient", PD), ("left", PI32),
+                ("right", PI32)]
+
+
+class kmc_table(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("n", C.c_int32 * 4), ("grid", PD * 4), ("rate", PD)]
+
+
+class kmc_inject(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("n_sections", C.c_int32), ("n_excitons", PI64), ("seeds", PU64)]
+
+
+class kmc_nbr_stats(C.Structure):
+    _fields_ = [("n_sites", C.c_int64), ("nnz", C.c_int64), ("k_mean", C.c_double), ("k_max", C.c_int32),
+                ("n_cells", C.c_int64), ("isolated", C.c_int64), ("exact_only", C.c_int64), ("build_ms", C.c_double)]
+
+
+class kmc_run_stats(C.Structure):
+    _fields_ = [("hops", C.c_int64), ("crossings", C.c_int64), ("exact_resolves", C.c_int64),
+                ("steps_done", C.c_int64), ("last_run_ms", C.c_double), ("last_launches", C.c_int32)]
+
+
+# every symbol include/cntkmc.h declares, with (restype, argtypes)
+SIGNATURES = {
+    "kmc_create": (C.c_void_p, [C.c_int, C.POINTER(C.c_int)]),
+    "kmc_destroy": (None, [C.c_void_p]),
+    "kmc_last_error": (C.c_char_p, [C.c_void_p]),
+    "kmc_load_film": (C.c_int, [C.c_void_p, C.POINTER(kmc_film)]),
+    "kmc_set_rate_table": (C.c_int, [C.c_void_p, C.POINTER(kmc_table)]),
+    "kmc_build_neighbors": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(kmc_nbr_stats)]),
+    "kmc_init_excitons": (C.c_int, [C.c_void_p, C.POINTER(kmc_inject)]),
+    "kmc_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32]),
+    "kmc_get_msd": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, PD]),
+    "kmc_get_excitons": (C.c_int, [C.c_void_p, PI32, PD, PD, PD, PI32, PU64, PI64]),
+    "kmc_num_excitons": (C.c_int64, [C.c_void_p]),
+    "kmc_get_run_stats": (C.c_int, [C.c_void_p, C.POINTER(kmc_run_stats)]),
+    "kmc_get_neighbors": (C.c_int, [C.c_void_p, PI64, PI32, PD, PD]),
+    "kmc_set_trace": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64]),
+    "kmc_get_trace": (C.c_int64, [C.c_void_p, C.c_int64, PI32, C.c_int64]),
+    "kmc_set_hop_cap": (C.c_int, [C.c_void_p, C.c_int64]),
+    "kmc_trim_sites": (C.c_int, [C.c_int64, PD, PD, PI32, PI32, PD, PI64]),
+    "kmc_domain": (C.c_int, [C.c_int64, PD, PD, PD]),
+    "kmc_forster_table": (C.c_int, [C.c_double, PD, PD, PD, PD, PD, PD, PD, PD, PD]),
+    "kmc_read_mesh": (C.c_int, [C.c_char_p, PI64, PI64, PD, PD, PI32, PI32]),
+    "kmc_selftest_uniform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, PU64]),
+    "kmc_math_probe": (C.c_int, [C.c_void_p, PD, C.c_int64, PD, PD]),
+    "kmc_set_launch_config": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "kmc_version": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+def load():
+    """Load libcntkmc.so (fails loudly if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run cnt_film_monte_carlo_gb300.build.build() first")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+class KmcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"cntkmc error {code}: {msg}")
+        self.code = code

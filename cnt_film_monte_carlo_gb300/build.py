@@ -1,0 +1,88 @@
+"""Build the engine's native code in-tree: libcntkmc.so (CUDA, sm_103a) and the drop-in driver.
+
+nvcc cross-compiles sm_103a on a machine without a GPU.  Objects go to ``_build/`` next to
+this file; the shared library and the ``cntkmc_run`` driver land in this package directory.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+LIB = os.path.join(HERE, "libcntkmc.so")
+DRIVER = os.path.join(HERE, "cntkmc_run")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+              f"-I{INCLUDE}", f"-I{CSRC}"]
+CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall", f"-I{INCLUDE}",
+             f"-I{CSRC}"]
+
+CU_SOURCES = ["kmc_kernels.cu", "cntkmc_api.cu"]
+CXX_SOURCES = ["kmc_host.cpp"]
+DRIVER_SOURCES = ["driver.cpp"]
+
+
+def nvcc() -> str:
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found")
+    return p
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stdout + r.stderr
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
+    """Compile (when sources changed) and return the path of libcntkmc.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers.append(os.path.join(INCLUDE, "cntkmc.h"))
+    jobs, objs = [], []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            extra = ["-Xptxas", "-v"] if ptxas_info else []
+            jobs.append([nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
+    for src in CXX_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append(["g++"] + CXX_FLAGS + ["-c", s, "-o", o])
+    out = []
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+        for text in ex.map(_run, jobs):
+            out.append(text)
+    if force or jobs or _stale(LIB, objs):
+        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]))
+    drv_src = [os.path.join(CSRC, s) for s in DRIVER_SOURCES]
+    if all(os.path.exists(s) for s in drv_src) and (force or _stale(DRIVER, drv_src + headers + [LIB])):
+        out.append(_run(["g++"] + CXX_FLAGS + ["-o", DRIVER] + drv_src + ["-L" + HERE, "-lcntkmc",
+                                                                         "-Wl,-rpath,$ORIGIN"]))
+    if verbose:
+        print("\n".join(t for t in out if t.strip()))
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, force="--force" in sys.argv, ptxas_info="--ptxas" in sys.argv)

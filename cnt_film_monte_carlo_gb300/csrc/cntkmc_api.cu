@@ -1,0 +1,718 @@
+// cntkmc_api.cu -- implementation of the C ABI in include/cntkmc.h (context, device memory,
+// launch sequencing).  The kernels are in kmc_kernels.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cntkmc.h"
+#include "kmc_internal.h"
+
+using kmc::FilmDev;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    release();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+const double kLogTab[1 << KMC_LOG_TABLE_BITS][3] = KMC_LOG_TAB_INIT;
+
+}  // namespace
+
+struct kmc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  // films (host copies)
+  int32_t n_films = 0;
+  int64_t n_sites = 0;
+  std::vector<int64_t> film_off;
+  std::vector<double> pos;  // [n][3]
+  std::vector<FilmDev> films;
+  std::vector<std::array<double, 6>> domains;
+  bool film_loaded = false;
+  DevBuf<double4_32a> d_pos4;
+  DevBuf<double> d_orient;
+  DevBuf<int32_t> d_left, d_right, d_site_film;
+  DevBuf<FilmDev> d_films;
+  // table
+  bool has_table = false;
+  kmc::TableDev table{};
+  DevBuf<double> d_grid[4], d_rate;
+  // neighbours
+  bool built = false;
+  double r_max = 0;
+  int64_t nnz = 0, n_cells = 0;
+  DevBuf<int64_t> d_cell_of, d_cell_start, d_cell_cursor, d_rowptr, d_scan;
+  DevBuf<int32_t> d_cell_members, d_col;
+  DevBuf<double> d_cum, d_total, d_inv_total;
+  DevBuf<float> d_cumn;
+  DevBuf<kmc::SiteRec> d_rec;
+  DevBuf<double2> d_lt64;
+  double lt_v = -1;
+  // excitons
+  bool inited = false;
+  int64_t n_slots = 0, n_exc_total = 0;
+  std::vector<int64_t> n_exc;
+  DevBuf<int32_t> d_warp_film, d_inject, d_e_site;
+  DevBuf<uint32_t> d_e_flags;
+  DevBuf<double> d_e_pos, d_e_delta, d_e_ff;
+  DevBuf<uint64_t> d_e_draws, d_e_hops;
+  // msd and trace
+  DevBuf<double> d_msd;
+  int64_t msd_cap = 0, steps_done = 0;
+  int64_t n_trace = 0, trace_cap = 0;
+  DevBuf<int32_t> d_trace;
+  DevBuf<int64_t> d_trace_cnt;
+  // misc
+  DevBuf<kmc::LogTab> d_logtab;
+  DevBuf<unsigned long long> d_counters, d_stats;
+  DevBuf<int32_t> d_err;
+  int64_t hop_cap = 100000000LL;
+  int steps_per_launch = 32;
+  int block = 128;
+  kmc_run_stats stats{};
+};
+
+#define FAIL(ctx, code, ...)                                          \
+  do {                                                                \
+    char _b[512];                                                     \
+    std::snprintf(_b, sizeof _b, __VA_ARGS__);                        \
+    (ctx)->err = _b;                                                  \
+    return (code);                                                    \
+  } while (0)
+#define CK(ctx, call)                                                                              \
+  do {                                                                                             \
+    cudaError_t _e = (call);                                                                       \
+    if (_e != cudaSuccess) FAIL(ctx, _e == cudaErrorMemoryAllocation ? KMC_ERR_NOMEM : KMC_ERR_CUDA, \
+                                "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+  } while (0)
+
+template <typename T>
+static cudaError_t upload(DevBuf<T>& b, const T* h, size_t n, cudaStream_t s) {
+  cudaError_t e = b.alloc(n);
+  if (e != cudaSuccess) return e;
+  if (n) e = cudaMemcpyAsync(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s);
+  return e;
+}
+
+extern "C" {
+
+kmc_ctx* kmc_create(int device, int* status) {
+  auto set = [&](int v) {
+    if (status) *status = v;
+  };
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+    set(KMC_ERR_NO_DEVICE);
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    set(KMC_ERR_NO_DEVICE);
+    return nullptr;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess || prop.major != 10) {
+    set(KMC_ERR_NO_DEVICE);
+    return nullptr;
+  }
+  kmc_ctx* c = new kmc_ctx();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
+      upload(c->d_logtab, reinterpret_cast<const kmc::LogTab*>(kLogTab), 1, c->stream) != cudaSuccess ||
+      c->d_counters.alloc(4) != cudaSuccess || c->d_stats.alloc(4) != cudaSuccess || c->d_err.alloc(1) != cudaSuccess ||
+      cudaMemsetAsync(c->d_counters.p, 0, 4 * sizeof(unsigned long long), c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    set(KMC_ERR_CUDA);
+    kmc_destroy(c);
+    return nullptr;
+  }
+  set(KMC_OK);
+  return c;
+}
+
+void kmc_destroy(kmc_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto* b : {&c->d_orient, &c->d_cum, &c->d_total, &c->d_inv_total, &c->d_rate, &c->d_e_pos, &c->d_e_delta,
+                  &c->d_e_ff, &c->d_msd})
+    b->release();
+  for (auto& g : c->d_grid) g.release();
+  for (auto* b : {&c->d_left, &c->d_right, &c->d_site_film, &c->d_cell_members, &c->d_col, &c->d_warp_film,
+                  &c->d_inject, &c->d_e_site, &c->d_trace, &c->d_err})
+    b->release();
+  for (auto* b : {&c->d_cell_of, &c->d_cell_start, &c->d_cell_cursor, &c->d_rowptr, &c->d_scan, &c->d_trace_cnt})
+    b->release();
+  c->d_pos4.release();
+  c->d_films.release();
+  c->d_cumn.release();
+  c->d_rec.release();
+  c->d_lt64.release();
+  c->d_e_flags.release();
+  c->d_e_draws.release();
+  c->d_e_hops.release();
+  c->d_logtab.release();
+  c->d_counters.release();
+  c->d_stats.release();
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* kmc_last_error(const kmc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
+  if (!c) return KMC_ERR_ARG;
+  if (!f || f->n_films < 1 || !f->film_site_offsets || !f->pos || !f->orient || !f->left || !f->right)
+    FAIL(c, KMC_ERR_ARG, "kmc_load_film: missing arrays");
+  CK(c, cudaSetDevice(c->device));
+  const int32_t nf = f->n_films;
+  const int64_t n = f->film_site_offsets[nf];
+  if (f->film_site_offsets[0] != 0 || n <= 0 || n >= (1LL << 31)) FAIL(c, KMC_ERR_ARG, "kmc_load_film: bad offsets");
+  std::vector<int32_t> L(n), R(n), sf(n);
+  std::vector<double4_32a> p4(n);
+  c->films.assign(nf, FilmDev{});
+  c->domains.assign(nf, {});
+  for (int32_t i = 0; i < nf; ++i) {
+    int64_t s0 = f->film_site_offsets[i], s1 = f->film_site_offsets[i + 1];
+    if (s1 <= s0) FAIL(c, KMC_ERR_ARG, "kmc_load_film: film %d has no sites", i);
+    FilmDev& fd = c->films[i];
+    fd.site0 = s0;
+    fd.n_sites = s1 - s0;
+    double mn[3], mx[3];
+    kmc_domain(s1 - s0, f->pos + 3 * s0, mn, mx);
+    for (int k = 0; k < 3; ++k) {
+      c->domains[i][k] = mn[k];
+      c->domains[i][3 + k] = mx[k];
+      fd.mn[k] = mn[k];
+    }
+    for (int64_t s = s0; s < s1; ++s) {
+      int32_t l = f->left[s], r = f->right[s];
+      if (l >= fd.n_sites || r >= fd.n_sites || l < -1 || r < -1) FAIL(c, KMC_ERR_ARG, "kmc_load_film: bad link at %lld", (long long)s);
+      L[s] = l < 0 ? -1 : (int32_t)(s0 + l);
+      R[s] = r < 0 ? -1 : (int32_t)(s0 + r);
+      sf[s] = i;
+      p4[s] = make_double4_32a(f->pos[3 * s], f->pos[3 * s + 1], f->pos[3 * s + 2], 0.0);
+    }
+  }
+  c->n_films = nf;
+  c->n_sites = n;
+  c->film_off.assign(f->film_site_offsets, f->film_site_offsets + nf + 1);
+  c->pos.assign(f->pos, f->pos + 3 * n);
+  CK(c, upload(c->d_pos4, p4.data(), n, c->stream));
+  CK(c, upload(c->d_orient, f->orient, 3 * n, c->stream));
+  CK(c, upload(c->d_left, L.data(), n, c->stream));
+  CK(c, upload(c->d_right, R.data(), n, c->stream));
+  CK(c, upload(c->d_site_film, sf.data(), n, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->film_loaded = true;
+  c->built = false;
+  c->inited = false;
+  return KMC_OK;
+}
+
+int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
+  if (!c) return KMC_ERR_ARG;
+  if (!t || (t->kind != KMC_TABLE_4D && t->kind != KMC_TABLE_2D) || !t->rate)
+    FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: kind must be 4 or 2");
+  CK(c, cudaSetDevice(c->device));
+  int dims = t->kind == KMC_TABLE_4D ? 4 : 2;
+  int64_t nr = 1;
+  c->table = kmc::TableDev{};
+  c->table.kind = t->kind;
+  for (int d = 0; d < dims; ++d) {
+    if (t->n[d] < 1 || !t->grid[d]) FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: grid %d empty", d);
+    nr *= t->n[d];
+    CK(c, upload(c->d_grid[d], t->grid[d], t->n[d], c->stream));
+    c->table.n[d] = t->n[d];
+    c->table.grid[d] = c->d_grid[d].p;
+  }
+  CK(c, upload(c->d_rate, t->rate, nr, c->stream));
+  c->table.rate = c->d_rate.p;
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->has_table = true;
+  c->built = false;
+  c->inited = false;
+  return KMC_OK;
+}
+
+int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->film_loaded || !c->has_table) FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: load a film and a rate table first");
+  if (!(r_max > 0)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: radius must be positive");
+  CK(c, cudaSetDevice(c->device));
+  const int64_t n = c->n_sites;
+  // cell grids, monte_carlo.h:375-387: n_d = ceil((max - min) / r) + 1
+  int64_t ncell = 0;
+  for (int32_t i = 0; i < c->n_films; ++i) {
+    FilmDev& fd = c->films[i];
+    const auto& d = c->domains[i];
+    double nd[3];
+    for (int k = 0; k < 3; ++k) nd[k] = std::ceil((d[3 + k] - d[k]) / r_max) + 1;
+    if (!(nd[0] * nd[1] * nd[2] < 4e9)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: cell grid too large");
+    fd.nx = (int32_t)nd[0];
+    fd.ny = (int32_t)nd[1];
+    fd.nz = (int32_t)nd[2];
+    fd.r = r_max;
+    fd.cell0 = ncell;
+    fd.n_cells = (int64_t)fd.nx * fd.ny * fd.nz;
+    ncell += fd.n_cells;
+  }
+  c->n_cells = ncell;
+  CK(c, upload(c->d_films, c->films.data(), c->films.size(), c->stream));
+  CK(c, c->d_cell_of.alloc(n));
+  CK(c, c->d_cell_start.alloc(ncell + 1));
+  CK(c, c->d_cell_cursor.alloc(ncell));
+  CK(c, c->d_cell_members.alloc(n));
+  CK(c, c->d_rowptr.alloc(n + 1));
+  int64_t sl = std::max(kmc::scan_scratch_len(ncell + 1), kmc::scan_scratch_len(n + 1));
+  CK(c, c->d_scan.alloc(sl));
+  CK(c, cudaMemsetAsync(c->d_cell_start.p, 0, (ncell + 1) * sizeof(int64_t), c->stream));
+  CK(c, cudaMemsetAsync(c->d_cell_cursor.p, 0, ncell * sizeof(int64_t), c->stream));
+  CK(c, cudaMemsetAsync(c->d_rowptr.p, 0, (n + 1) * sizeof(int64_t), c->stream));
+  CK(c, cudaMemsetAsync(c->d_stats.p, 0, 4 * sizeof(unsigned long long), c->stream));
+  CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
+  kmc::BuildArgs a{};
+  a.pos4 = c->d_pos4.p;
+  a.orient = c->d_orient.p;
+  a.site_film = c->d_site_film.p;
+  a.films = c->d_films.p;
+  a.n_sites = n;
+  a.cell_of = c->d_cell_of.p;
+  a.cell_start = c->d_cell_start.p;
+  a.cell_cursor = c->d_cell_cursor.p;
+  a.cell_members = c->d_cell_members.p;
+  a.n_cells = ncell;
+  a.table = c->table;
+  a.r_max = r_max;
+  a.counts = c->d_rowptr.p;
+  a.rowptr = c->d_rowptr.p;
+  a.left = c->d_left.p;
+  a.right = c->d_right.p;
+  a.err = c->d_err.p;
+  a.stats = c->d_stats.p;
+  CK(c, cudaEventRecord(c->ev0, c->stream));
+  CK(c, kmc::launch_cell_ids(a, c->stream));
+  CK(c, kmc::exclusive_scan_i64(c->d_cell_start.p, ncell + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
+  CK(c, kmc::launch_cell_fill(a, c->stream));
+  CK(c, kmc::launch_nbr_count(a, c->stream));
+  CK(c, kmc::exclusive_scan_i64(c->d_rowptr.p, n + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
+  std::vector<int64_t> nnz0(c->n_films + 1);
+  for (int32_t i = 0; i <= c->n_films; ++i)
+    CK(c, cudaMemcpyAsync(&nnz0[i], c->d_rowptr.p + c->film_off[i], sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  int32_t herr = 0;
+  CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
+  if (herr) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: a site lies outside its film's cell grid (non-finite position?)");
+  c->nnz = nnz0[c->n_films];
+  for (int32_t i = 0; i < c->n_films; ++i) {
+    c->films[i].nnz0 = nnz0[i];
+    c->films[i].nnz = nnz0[i + 1] - nnz0[i];
+    if (c->films[i].nnz >= (1LL << 32)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: film %d has >= 2^32 neighbour entries", i);
+  }
+  CK(c, cudaMemcpyAsync(c->d_films.p, c->films.data(), c->films.size() * sizeof(FilmDev), cudaMemcpyHostToDevice, c->stream));
+  CK(c, c->d_col.alloc(c->nnz));
+  CK(c, c->d_cum.alloc(c->nnz));
+  CK(c, c->d_cumn.alloc(c->nnz));
+  CK(c, c->d_total.alloc(n));
+  CK(c, c->d_inv_total.alloc(n));
+  CK(c, c->d_rec.alloc(n));
+  CK(c, c->d_lt64.alloc(n));
+  a.col = c->d_col.p;
+  a.cum = c->d_cum.p;
+  a.cumn = c->d_cumn.p;
+  a.total = c->d_total.p;
+  a.inv_total = c->d_inv_total.p;
+  a.rec = c->d_rec.p;
+  CK(c, kmc::launch_nbr_fill(a, c->stream));
+  CK(c, cudaEventRecord(c->ev1, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  unsigned long long hs[4];
+  CK(c, cudaMemcpy(hs, c->d_stats.p, sizeof hs, cudaMemcpyDeviceToHost));
+  c->r_max = r_max;
+  c->lt_v = -1;
+  c->built = true;
+  c->inited = false;
+  if (st) {
+    st->n_sites = n;
+    st->nnz = c->nnz;
+    st->k_mean = (double)c->nnz / (double)n;
+    st->k_max = (int32_t)hs[0];
+    st->n_cells = ncell;
+    st->isolated = (int64_t)hs[1];
+    st->exact_only = (int64_t)hs[2];
+    st->build_ms = ms;
+  }
+  return KMC_OK;
+}
+
+int kmc_set_trace(kmc_ctx* c, int64_t n_trace, int64_t cap) {
+  if (!c) return KMC_ERR_ARG;
+  if (n_trace < 0 || cap < 0 || (n_trace > 0 && cap == 0)) FAIL(c, KMC_ERR_ARG, "kmc_set_trace: bad sizes");
+  c->n_trace = n_trace;
+  c->trace_cap = cap;
+  c->inited = false;
+  return KMC_OK;
+}
+
+int kmc_set_hop_cap(kmc_ctx* c, int64_t cap) {
+  if (!c) return KMC_ERR_ARG;
+  if (cap < 1) FAIL(c, KMC_ERR_ARG, "kmc_set_hop_cap: cap must be >= 1");
+  c->hop_cap = cap;
+  return KMC_OK;
+}
+
+int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_init_excitons: build the neighbour lists first");
+  if (!inj || !inj->n_excitons || !inj->seeds) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: missing arrays");
+  if (inj->mode != KMC_INJECT_REGION && inj->mode != KMC_INJECT_UNIFORM) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: bad mode");
+  CK(c, cudaSetDevice(c->device));
+  const int nsec = inj->n_sections;
+  if (inj->mode == KMC_INJECT_REGION && !(nsec > 1 && nsec % 2 == 1 && nsec < 1000))
+    FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: number of sections must be odd and > 1");
+  std::vector<int32_t> inject;
+  std::vector<int32_t> warp_film;
+  int64_t slot = 0, total = 0;
+  c->n_exc.assign(c->n_films, 0);
+  for (int32_t i = 0; i < c->n_films; ++i) {
+    FilmDev& fd = c->films[i];
+    int64_t ne = inj->n_excitons[i];
+    if (ne < 0) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: negative exciton count");
+    fd.mode = inj->mode;
+    fd.seed = inj->seeds[i];
+    fd.inj0 = (int64_t)inject.size();
+    if (inj->mode == KMC_INJECT_REGION) {
+      // injection_region / get_removal_domain, monte_carlo.cpp:203-251
+      const auto& d = c->domains[i];
+      std::vector<double> g[3];
+      for (int k = 0; k < 3; ++k) {
+        double step = (d[3 + k] - d[k]) / double(nsec);
+        for (int q = 0; q <= nsec; ++q) g[k].push_back(double(q) * step + d[k]);
+      }
+      for (int64_t s = fd.site0; s < fd.site0 + fd.n_sites; ++s) {
+        const double* p = &c->pos[3 * s];
+        if (g[0][nsec / 2] <= p[0] && p[0] <= g[0][nsec / 2 + 1] && g[1][nsec / 2] <= p[1] && p[1] <= g[1][nsec / 2 + 1] &&
+            g[2][nsec / 2] <= p[2] && p[2] <= g[2][nsec / 2 + 1])
+          inject.push_back((int32_t)s);
+      }
+      for (int k = 0; k < 3; ++k) {
+        fd.rmin[k] = g[k][1];
+        fd.rmax[k] = g[k][nsec - 1];
+      }
+      fd.n_inj = (int64_t)inject.size() - fd.inj0;
+    } else {
+      fd.n_inj = fd.n_sites;
+    }
+    if (ne > 0 && fd.n_inj == 0) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: film %d has no injection site", i);
+    if (fd.n_inj >= (1LL << 31)) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: too many injection sites");
+    fd.slot0 = slot;
+    fd.n_exc = ne;
+    int64_t padded = (ne + 31) / 32 * 32;
+    for (int64_t w = 0; w < padded / 32; ++w) warp_film.push_back(i);
+    slot += padded;
+    total += ne;
+    c->n_exc[i] = ne;
+  }
+  if (slot == 0) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: no excitons");
+  c->n_slots = slot;
+  c->n_exc_total = total;
+  CK(c, cudaMemcpyAsync(c->d_films.p, c->films.data(), c->films.size() * sizeof(FilmDev), cudaMemcpyHostToDevice, c->stream));
+  CK(c, upload(c->d_inject, inject.data(), inject.size(), c->stream));
+  CK(c, upload(c->d_warp_film, warp_film.data(), warp_film.size(), c->stream));
+  CK(c, c->d_e_site.alloc(slot));
+  CK(c, c->d_e_flags.alloc(slot));
+  CK(c, c->d_e_pos.alloc(3 * slot));
+  CK(c, c->d_e_delta.alloc(3 * slot));
+  CK(c, c->d_e_ff.alloc(slot));
+  CK(c, c->d_e_draws.alloc(slot));
+  CK(c, c->d_e_hops.alloc(slot));
+  if (c->n_trace > 0) {
+    CK(c, c->d_trace.alloc((size_t)(c->n_trace * c->trace_cap)));
+    CK(c, c->d_trace_cnt.alloc(c->n_trace));
+    CK(c, cudaMemsetAsync(c->d_trace_cnt.p, 0, c->n_trace * sizeof(int64_t), c->stream));
+  }
+  c->steps_done = 0;
+  c->msd_cap = 0;
+  c->d_msd.release();
+  CK(c, cudaMemsetAsync(c->d_counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+  kmc::HopArgs a{};
+  a.pos4 = c->d_pos4.p;
+  a.inv_total = c->d_inv_total.p;
+  a.films = c->d_films.p;
+  a.warp_film = c->d_warp_film.p;
+  a.inject = c->d_inject.p;
+  a.e_site = c->d_e_site.p;
+  a.e_flags = c->d_e_flags.p;
+  a.e_pos = c->d_e_pos.p;
+  a.e_delta = c->d_e_delta.p;
+  a.e_ff = c->d_e_ff.p;
+  a.e_draws = c->d_e_draws.p;
+  a.e_hops = c->d_e_hops.p;
+  a.n_slots = slot;
+  a.logtab = c->d_logtab.p;
+  CK(c, kmc::launch_init_excitons(a, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->stats = kmc_run_stats{};
+  c->inited = true;
+  return KMC_OK;
+}
+
+static int ensure_msd(kmc_ctx* c, int64_t need) {
+  if (need <= c->msd_cap) return KMC_OK;
+  int64_t cap = std::max<int64_t>(need, std::max<int64_t>(64, 2 * c->msd_cap));
+  DevBuf<double> nb;
+  CK(c, nb.alloc((size_t)(c->n_films * cap * 3)));
+  CK(c, cudaMemsetAsync(nb.p, 0, (size_t)c->n_films * cap * 3 * sizeof(double), c->stream));
+  if (c->msd_cap > 0 && c->steps_done > 0)
+    CK(c, cudaMemcpy2DAsync(nb.p, cap * 3 * sizeof(double), c->d_msd.p, c->msd_cap * 3 * sizeof(double),
+                            c->steps_done * 3 * sizeof(double), c->n_films, cudaMemcpyDeviceToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->d_msd.release();
+  c->d_msd = nb;
+  nb.p = nullptr;
+  c->msd_cap = cap;
+  return KMC_OK;
+}
+
+int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_run: create the excitons first");
+  if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_run: bad step count, time step or velocity");
+  if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_run: bad precision");
+  CK(c, cudaSetDevice(c->device));
+  if (n_steps == 0) return KMC_OK;
+  int rc = ensure_msd(c, c->steps_done + n_steps);
+  if (rc) return rc;
+  if (precision == KMC_PREC_MIXED && c->lt_v != v) {
+    CK(c, kmc::launch_link_times(c->d_pos4.p, c->d_left.p, c->d_right.p, c->d_rec.p, c->d_lt64.p, c->n_sites, v, c->stream));
+    c->lt_v = v;
+  }
+  kmc::HopArgs a{};
+  a.pos4 = c->d_pos4.p;
+  a.left = c->d_left.p;
+  a.right = c->d_right.p;
+  a.rowptr = c->d_rowptr.p;
+  a.col = c->d_col.p;
+  a.cum = c->d_cum.p;
+  a.total = c->d_total.p;
+  a.inv_total = c->d_inv_total.p;
+  a.rec = c->d_rec.p;
+  a.cumn = c->d_cumn.p;
+  a.lt64 = c->d_lt64.p;
+  a.films = c->d_films.p;
+  a.warp_film = c->d_warp_film.p;
+  a.inject = c->d_inject.p;
+  a.e_site = c->d_e_site.p;
+  a.e_flags = c->d_e_flags.p;
+  a.e_pos = c->d_e_pos.p;
+  a.e_delta = c->d_e_delta.p;
+  a.e_ff = c->d_e_ff.p;
+  a.e_draws = c->d_e_draws.p;
+  a.e_hops = c->d_e_hops.p;
+  a.n_slots = c->n_slots;
+  a.msd = c->d_msd.p;
+  a.msd_cap = c->msd_cap;
+  a.trace = c->d_trace.p;
+  a.trace_cnt = c->d_trace_cnt.p;
+  a.n_trace = c->n_trace;
+  a.trace_cap = c->trace_cap;
+  a.logtab = c->d_logtab.p;
+  a.counters = c->d_counters.p;
+  a.err = c->d_err.p;
+  a.hop_cap = c->hop_cap;
+  a.dt = dt;
+  a.v = v;
+  unsigned long long before[4];
+  CK(c, cudaMemcpyAsync(before, c->d_counters.p, sizeof before, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
+  CK(c, cudaEventRecord(c->ev0, c->stream));
+  int launches = 0;
+  for (int64_t s = 0; s < n_steps; s += c->steps_per_launch) {
+    int64_t k = std::min<int64_t>(c->steps_per_launch, n_steps - s);
+    a.step0 = c->steps_done + s;
+    if (precision == KMC_PREC_FP64)
+      CK(c, kmc::launch_hop_fp64(a, k, c->block, c->stream));
+    else
+      CK(c, kmc::launch_hop_mixed(a, k, c->block, c->stream));
+    ++launches;
+  }
+  CK(c, cudaEventRecord(c->ev1, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  int32_t herr = 0;
+  unsigned long long after[4];
+  CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
+  c->steps_done += n_steps;
+  c->stats.hops = (int64_t)after[0];
+  c->stats.crossings = (int64_t)after[1];
+  c->stats.exact_resolves = (int64_t)after[2];
+  c->stats.steps_done = c->steps_done;
+  c->stats.last_run_ms = ms;
+  c->stats.last_launches = launches;
+  (void)before;
+  if (herr & 1) FAIL(c, KMC_ERR_HOP_CAP, "kmc_run: an exciton exceeded %lld hops in one step", (long long)c->hop_cap);
+  if (herr) FAIL(c, KMC_ERR_ARG, "kmc_run: a free flight crossed more than 2^22 links (zero-length tube links?)");
+  return KMC_OK;
+}
+
+int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) {
+  if (!c) return KMC_ERR_ARG;
+  if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
+  if (count == 0) return KMC_OK;
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpy2DAsync(out, count * 3 * sizeof(double), c->d_msd.p + first * 3, c->msd_cap * 3 * sizeof(double),
+                          count * 3 * sizeof(double), c->n_films, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return KMC_OK;
+}
+
+int64_t kmc_num_excitons(const kmc_ctx* c) { return c && c->inited ? c->n_exc_total : 0; }
+
+int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,
+                     uint64_t* draws, int64_t* hops) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_get_excitons: no excitons");
+  CK(c, cudaSetDevice(c->device));
+  const int64_t ns = c->n_slots;
+  std::vector<int32_t> hs(ns);
+  std::vector<uint32_t> hf(ns);
+  std::vector<double> hp(3 * ns), hd(3 * ns), hff(ns);
+  std::vector<uint64_t> hdr(ns), hh(ns);
+  CK(c, cudaMemcpyAsync(hs.data(), c->d_e_site.p, ns * 4, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(hf.data(), c->d_e_flags.p, ns * 4, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(hp.data(), c->d_e_pos.p, 3 * ns * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(hd.data(), c->d_e_delta.p, 3 * ns * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(hff.data(), c->d_e_ff.p, ns * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(hdr.data(), c->d_e_draws.p, ns * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(hh.data(), c->d_e_hops.p, ns * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  int64_t o = 0;
+  for (int32_t f = 0; f < c->n_films; ++f) {
+    const FilmDev& fd = c->films[f];
+    for (int64_t i = 0; i < fd.n_exc; ++i, ++o) {
+      int64_t s = fd.slot0 + i;
+      if (site) site[o] = hs[s] < 0 ? -1 : (int32_t)(hs[s] - fd.site0);
+      for (int k = 0; k < 3; ++k) {
+        if (pos) pos[3 * o + k] = hp[k * ns + s];
+        if (delta) delta[3 * o + k] = hd[k * ns + s];
+      }
+      if (ff) ff[o] = hff[s];
+      if (heading) heading[o] = (hf[s] & kmc::kExHeading) ? 1 : 0;
+      if (draws) draws[o] = hdr[s];
+      if (hops) hops[o] = (int64_t)hh[s];
+    }
+  }
+  return KMC_OK;
+}
+
+int kmc_get_run_stats(kmc_ctx* c, kmc_run_stats* st) {
+  if (!c || !st) return KMC_ERR_ARG;
+  *st = c->stats;
+  return KMC_OK;
+}
+
+int kmc_get_neighbors(kmc_ctx* c, int64_t* rowptr, int32_t* col, double* cum, double* total) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_get_neighbors: not built");
+  CK(c, cudaSetDevice(c->device));
+  const int64_t n = c->n_sites;
+  if (rowptr) CK(c, cudaMemcpy(rowptr, c->d_rowptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
+  if (cum) CK(c, cudaMemcpy(cum, c->d_cum.p, c->nnz * 8, cudaMemcpyDeviceToHost));
+  if (total) CK(c, cudaMemcpy(total, c->d_total.p, n * 8, cudaMemcpyDeviceToHost));
+  if (col) {
+    CK(c, cudaMemcpy(col, c->d_col.p, c->nnz * 4, cudaMemcpyDeviceToHost));
+    for (int32_t f = 0; f < c->n_films; ++f) {
+      const FilmDev& fd = c->films[f];
+      for (int64_t i = fd.nnz0; i < fd.nnz0 + fd.nnz; ++i) col[i] -= (int32_t)fd.site0;
+    }
+  }
+  return KMC_OK;
+}
+
+int64_t kmc_get_trace(kmc_ctx* c, int64_t e, int32_t* out, int64_t cap) {
+  if (!c || !c->inited || e < 0 || e >= c->n_trace || !out) return KMC_ERR_ARG;
+  if (cudaSetDevice(c->device) != cudaSuccess) return KMC_ERR_CUDA;
+  int64_t cnt = 0;
+  if (cudaMemcpy(&cnt, c->d_trace_cnt.p + e, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return KMC_ERR_CUDA;
+  int64_t k = std::min(std::min(cnt, c->trace_cap), cap);
+  if (k > 0 && cudaMemcpy(out, c->d_trace.p + e * c->trace_cap, k * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return KMC_ERR_CUDA;
+  return cnt;
+}
+
+int kmc_selftest_uniform(kmc_ctx* c, uint32_t r0, uint64_t count, uint64_t* mismatches) {
+  if (!c || !mismatches) return KMC_ERR_ARG;
+  CK(c, cudaSetDevice(c->device));
+  DevBuf<unsigned long long> m;
+  CK(c, m.alloc(1));
+  CK(c, cudaMemsetAsync(m.p, 0, 8, c->stream));
+  CK(c, kmc::launch_u_check(r0, count, m.p, c->stream));
+  unsigned long long h = 0;
+  CK(c, cudaMemcpyAsync(&h, m.p, 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  m.release();
+  *mismatches = h;
+  return KMC_OK;
+}
+
+int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, double* acos_out) {
+  if (!c || !x || !log_out || !acos_out || n < 0) return KMC_ERR_ARG;
+  if (n == 0) return KMC_OK;
+  CK(c, cudaSetDevice(c->device));
+  DevBuf<double> dx, dl, da;
+  CK(c, upload(dx, x, n, c->stream));
+  CK(c, dl.alloc(n));
+  CK(c, da.alloc(n));
+  CK(c, kmc::launch_math_probe(dx.p, dl.p, da.p, n, c->d_logtab.p, c->stream));
+  CK(c, cudaMemcpyAsync(log_out, dl.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(acos_out, da.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  dx.release();
+  dl.release();
+  da.release();
+  return KMC_OK;
+}
+
+int kmc_set_launch_config(kmc_ctx* c, int32_t block, int32_t steps_per_launch) {
+  if (!c) return KMC_ERR_ARG;
+  if (block < 32 || block > 256 || block % 32 || steps_per_launch < 1) FAIL(c, KMC_ERR_ARG, "kmc_set_launch_config: bad values");
+  c->block = block;
+  c->steps_per_launch = steps_per_launch;
+  return KMC_OK;
+}
+
+}  // extern "C"

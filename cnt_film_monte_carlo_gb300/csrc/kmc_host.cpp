@@ -1,0 +1,186 @@
+// kmc_host.cpp -- host-side reference algorithms of the C ABI (no device code).
+// Compiled with -ffp-contract=off so every expression rounds as written.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/cntkmc.h"
+
+namespace {
+
+constexpr double kRefPi = 3.141592;  // src/helper/constants.h:10
+
+inline double dot3(const double* a, const double* b) {
+  double acc1 = 0.0, acc2 = 0.0;
+  acc1 += a[0] * b[0];
+  acc2 += a[1] * b[1];
+  acc1 += a[2] * b[2];
+  return acc1 + acc2;
+}
+inline double norm3(const double* a) { return std::sqrt(dot3(a, a)); }
+
+// arma::linspace (used by monte_carlo.cpp:66-75,158-167): s + i (e - s)/(n - 1), last = e
+void linspace(double start, double end, int64_t num, double* out) {
+  if (num == 1) {
+    out[0] = end;
+    return;
+  }
+  if (num < 2) return;
+  const double delta = (end - start) / double(num - 1);
+  for (int64_t i = 0; i < num - 1; ++i) out[i] = start + double(i) * delta;
+  out[num - 1] = end;
+}
+
+bool read_matrix(const std::string& path, std::vector<double>& v, int64_t& rows, int64_t& cols) {
+  std::ifstream f(path);
+  if (!f) return false;
+  v.clear();
+  rows = 0;
+  cols = -1;
+  std::string line;
+  while (std::getline(f, line)) {
+    for (auto& ch : line)
+      if (ch == ',') ch = ' ';
+    const char* s = line.c_str();
+    int64_t c = 0;
+    for (;;) {
+      char* e;
+      double x = std::strtod(s, &e);
+      if (e == s) break;
+      v.push_back(x);
+      ++c;
+      s = e;
+    }
+    if (c == 0) continue;
+    if (cols < 0) cols = c;
+    if (c != cols) return false;
+    ++rows;
+  }
+  if (cols < 0) cols = 0;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_t* right, const double lim[6],
+                   int64_t* n_out) {
+  if (n < 0 || (n > 0 && (!pos || !orient || !left || !right)) || !lim || !n_out) return KMC_ERR_ARG;
+  // monte_carlo.h:730-750: exchange sites i and j, first pointing their tube neighbours at the new slots
+  auto swap_sites = [&](int64_t i, int64_t j) {
+    int32_t iL = left[i], iR = right[i], jL = left[j], jR = right[j];
+    int32_t new_i = (int32_t)j, new_j = (int32_t)i;
+    if (iL > -1) right[iL] = new_i;
+    if (iR > -1) left[iR] = new_i;
+    if (jL > -1) right[jL] = new_j;
+    if (jR > -1) left[jR] = new_j;
+    for (int c = 0; c < 3; ++c) {
+      std::swap(pos[3 * i + c], pos[3 * j + c]);
+      std::swap(orient[3 * i + c], orient[3 * j + c]);
+    }
+    std::swap(left[i], left[j]);
+    std::swap(right[i], right[j]);
+  };
+  // monte_carlo.h:752-771: out-of-limit sites go to the end; their neighbours lose the link
+  int64_t j = n;
+  for (int64_t i = 0; i < j;) {
+    const double* p = pos + 3 * i;
+    if (p[0] < lim[0] || p[1] < lim[2] || p[2] < lim[4] || p[0] > lim[1] || p[1] > lim[3] || p[2] > lim[5]) {
+      --j;
+      swap_sites(i, j);
+      if (left[j] > -1) right[left[j]] = -1;
+      if (right[j] > -1) left[right[j]] = -1;
+    } else {
+      ++i;
+    }
+  }
+  *n_out = j;
+  return KMC_OK;
+}
+
+int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]) {
+  if (n <= 0 || !pos || !mn || !mx) return KMC_ERR_ARG;
+  // find_simulation_domain, monte_carlo.h:328-340
+  for (int c = 0; c < 3; ++c) mn[c] = mx[c] = pos[c];
+  for (int64_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) {
+      double p = pos[3 * i + c];
+      mn[c] = mn[c] > p ? p : mn[c];
+      mx[c] = mx[c] < p ? p : mx[c];
+    }
+  return KMC_OK;
+}
+
+int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
+                      const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate) {
+  if (!theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh || !a1 || !a2 || !rate) return KMC_ERR_ARG;
+  int64_t nt = (int64_t)theta_deg[2], nz = (int64_t)zshift[2], n1 = (int64_t)ash1[2], n2 = (int64_t)ash2[2];
+  if (nt < 1 || nz < 1 || n1 < 1 || n2 < 1) return KMC_ERR_ARG;
+  linspace(zshift[0], zshift[1], nz, zsh);
+  linspace(ash1[0], ash1[1], n1, a1);
+  linspace(ash2[0], ash2[1], n2, a2);
+  linspace(theta_deg[0], theta_deg[1], nt, theta);
+  const double scale = kRefPi / 180;
+  for (int64_t i = 0; i < nt; ++i) theta[i] = theta[i] * scale;
+  // monte_carlo.cpp:174-195: point dipoles on two axes at angle th, separated by zsh
+  for (int64_t it = 0; it < nt; ++it) {
+    const double th = theta[it];
+    for (int64_t iz = 0; iz < nz; ++iz)
+      for (int64_t i1 = 0; i1 < n1; ++i1)
+        for (int64_t i2 = 0; i2 < n2; ++i2) {
+          double r1[3] = {a1[i1], 0, 0};
+          double r2[3] = {a2[i2] * std::cos(th), a2[i2] * std::sin(th), zsh[iz]};
+          double dR[3] = {r1[0] - r2[0], r1[1] - r2[1], r1[2] - r2[2]};
+          double n_r1 = norm3(r1), n_r2 = norm3(r2), n_dR = norm3(dR);
+          double d1 = n_r1 != 0 ? n_r1 : 1.0, d2 = n_r2 != 0 ? n_r2 : 1.0, dd = n_dR != 0 ? n_dR : 1.0;
+          double u1[3] = {r1[0] / d1, r1[1] / d1, r1[2] / d1};
+          double u2[3] = {r2[0] / d2, r2[1] / d2, r2[2] / d2};
+          double ud[3] = {dR[0] / dd, dR[1] / dd, dR[2] / dd};
+          double af = std::cos(th) - 3 * dot3(u1, ud) * dot3(u2, ud);
+          rate[((it * nz + iz) * n1 + i1) * n2 + i2] = gamma_0 * (af * af) * std::pow(1.e-9 / n_dR, 6);
+        }
+  }
+  return KMC_OK;
+}
+
+int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* pos, double* orient, int32_t* left,
+                  int32_t* right) {
+  if (!dir || !n_tubes || !n_points) return KMC_ERR_ARG;
+  static const char* names[6] = {"single_cnt.pos.x.dat",    "single_cnt.pos.y.dat",    "single_cnt.pos.z.dat",
+                                 "single_cnt.orient.x.dat", "single_cnt.orient.y.dat", "single_cnt.orient.z.dat"};
+  std::vector<double> m[6];
+  int64_t rows = -1, cols = -1;
+  for (int k = 0; k < 6; ++k) {
+    int64_t r = 0, c = 0;
+    if (!read_matrix(std::string(dir) + "/" + names[k], m[k], r, c)) return KMC_ERR_IO;
+    if (rows >= 0 && (r != rows || c != cols)) return KMC_ERR_IO;
+    rows = r;
+    cols = c;
+  }
+  *n_tubes = rows;
+  *n_points = cols;
+  if (!pos && !orient && !left && !right) return KMC_OK;
+  if (!pos || !orient || !left || !right) return KMC_ERR_ARG;
+  // monte_carlo.h:249-262; positions scaled by 1e-9 (:211,225,239)
+  for (int64_t i = 0; i < rows; ++i)
+    for (int64_t j = 0; j < cols; ++j) {
+      int64_t s = i * cols + j;
+      for (int c = 0; c < 3; ++c) {
+        pos[3 * s + c] = m[c][s] * 1.e-9;
+        orient[3 * s + c] = m[3 + c][s];
+      }
+      left[s] = j > 0 ? (int32_t)(s - 1) : -1;
+      right[s] = j + 1 < cols ? (int32_t)(s + 1) : -1;
+    }
+  return KMC_OK;
+}
+
+const char* kmc_version(void) { return "cntkmc 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// kmc_internal.h -- device data layout and kernel launchers of the engine (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kmc_device.cuh"
+
+namespace kmc {
+
+// Per-film constants (device copy).
+struct FilmDev {
+  int64_t site0, n_sites;   // film's sites in the global site arrays
+  int64_t cell0, n_cells;   // film's cells in the global cell arrays
+  int64_t nnz0, nnz;        // film's neighbour entries in the global CSR arrays
+  int32_t nx, ny, nz, mode; // cell grid; injection mode
+  double mn[3];             // domain minimum (cell origin)
+  double r;                 // cell side = max hopping radius
+  int64_t inj0, n_inj;      // injection sites (global ids) in the inject array
+  double rmin[3], rmax[3];  // removal domain (mode 0)
+  uint64_t seed;            // Philox key
+  int64_t slot0, n_exc;     // exciton slots (padded to whole warps)
+};
+
+// Per-site record read once per hop by the mixed kernel (one 32-byte sector).
+struct __align__(32) SiteRec {
+  double inv_total;   // 1 / total rate (inf for an empty list)
+  uint32_t row;       // film-local offset of the neighbour row
+  uint32_t len_flags; // row length (low 24 bits) | flags << 24
+  int32_t left, right;// global site ids or -1
+  uint32_t lt_hi_l;   // high 32 bits of the FP64 link time to the left / right neighbour
+  uint32_t lt_hi_r;
+};
+constexpr uint32_t kRecExact = 1u << 24;  // row resolved in FP64 only (non-finite/zero total, negative rate)
+constexpr uint32_t kLenMask = (1u << 24) - 1;
+
+struct TableDev {
+  int32_t kind;
+  int32_t n[4];
+  const double* grid[4];
+  const double* rate;
+};
+
+// Exciton flags
+constexpr uint32_t kExHeading = 1u;  // heading right
+constexpr uint32_t kExAtSite = 2u;   // position equals the current site's position (mixed kernel)
+constexpr uint32_t kExActive = 4u;   // slot holds an exciton (not warp padding)
+
+struct HopArgs {
+  // sites
+  const double4_32a* pos4;
+  const int32_t* left;
+  const int32_t* right;
+  const int64_t* rowptr;  // global
+  const int32_t* col;     // global site ids
+  const double* cum;
+  const double* total;
+  const double* inv_total;
+  const SiteRec* rec;
+  const float* cumn;      // cum / total in FP32
+  const double2* lt64;    // exact link times (left, right)
+  // films and excitons
+  const FilmDev* films;
+  const int32_t* warp_film;
+  const int32_t* inject;
+  int32_t* e_site;
+  uint32_t* e_flags;
+  double* e_pos;    // [3][n_slots]
+  double* e_delta;  // [3][n_slots]
+  double* e_ff;
+  uint64_t* e_draws;
+  uint64_t* e_hops;
+  int64_t n_slots;
+  // output
+  double* msd;      // [n_films][msd_cap][3]
+  int64_t msd_cap;
+  int64_t step0;
+  int32_t* trace;
+  int64_t* trace_cnt;
+  int64_t n_trace, trace_cap;
+  const LogTab* logtab;
+  unsigned long long* counters;  // [0] hops [1] crossings [2] exact re-resolves
+  int32_t* err;
+  int64_t hop_cap;
+  double dt, v;
+};
+
+struct BuildArgs {
+  const double4_32a* pos4;
+  const double* orient;    // [n][3]
+  const int32_t* site_film;
+  const FilmDev* films;
+  int64_t n_sites;
+  int64_t* cell_of;        // [n]
+  int64_t* cell_start;     // [n_cells + 1]
+  int64_t* cell_cursor;    // [n_cells]
+  int32_t* cell_members;   // [n]
+  int64_t n_cells;
+  TableDev table;
+  double r_max;
+  int64_t* counts;         // [n + 1] -> rowptr
+  int64_t* rowptr;
+  int32_t* col;
+  double* cum;
+  double* total;
+  double* inv_total;
+  float* cumn;
+  SiteRec* rec;
+  const int32_t* left;
+  const int32_t* right;
+  int32_t* err;
+  unsigned long long* stats;  // [0] longest row [1] empty rows [2] rows resolved in FP64 only
+};
+
+// launchers (kmc_kernels.cu); all return cudaError_t of the launch
+cudaError_t launch_cell_ids(const BuildArgs& a, cudaStream_t s);
+cudaError_t launch_cell_fill(const BuildArgs& a, cudaStream_t s);
+cudaError_t launch_nbr_count(const BuildArgs& a, cudaStream_t s);
+cudaError_t launch_nbr_fill(const BuildArgs& a, cudaStream_t s);
+cudaError_t exclusive_scan_i64(int64_t* data, int64_t n, int64_t* scratch, int64_t scratch_len, cudaStream_t s);
+int64_t scan_scratch_len(int64_t n);
+cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, const int32_t* right, SiteRec* rec,
+                              double2* lt64, int64_t n, double v, cudaStream_t s);
+cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s);
+cudaError_t launch_hop_fp64(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
+cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
+cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, cudaStream_t s);
+cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,
+                              cudaStream_t s);
+
+}  // namespace kmc

@@ -1,0 +1,209 @@
+"""Python handle on one engine context (a thin layer over the C ABI in include/cntkmc.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .film import Film
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Engine:
+    """Owns a kmc_ctx on one CUDA device.  Every method maps to one C-ABI call and raises
+    ``KmcError`` with the library's message when the call fails."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        st = C.c_int(0)
+        self.h = self.lib.kmc_create(device, C.byref(st))
+        if not self.h:
+            raise L.KmcError(st.value, "kmc_create failed (no sm_10x CUDA device?)")
+        self._keep = []
+        self.n_films = 0
+        self.n_exc = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.kmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != L.KMC_OK:
+            raise L.KmcError(rc, self.lib.kmc_last_error(self.h).decode())
+
+    # ------------------------------------------------------------------ set-up
+    def load_films(self, films, positions_m=None):
+        """Load one or more films.  ``films`` is a Film or a list of Films; positions are the
+        films' nm coordinates scaled by 1e-9 unless ``positions_m`` gives them in metres."""
+        if isinstance(films, Film):
+            films = [films]
+        pos = [(_f64(positions_m[i]) if positions_m is not None else f.pos_m()) for i, f in enumerate(films)]
+        off = np.zeros(len(films) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([f.n_sites for f in films])
+        P = _f64(np.concatenate(pos))
+        O = _f64(np.concatenate([f.orient for f in films]))
+        Lk = np.ascontiguousarray(np.concatenate([f.left for f in films]), dtype=np.int32)
+        R = np.ascontiguousarray(np.concatenate([f.right for f in films]), dtype=np.int32)
+        return self.load_arrays(off, P, O, Lk, R)
+
+    def load_arrays(self, offsets, pos_m, orient, left, right):
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        pos_m = _f64(pos_m)
+        orient = _f64(orient)
+        left = np.ascontiguousarray(left, dtype=np.int32)
+        right = np.ascontiguousarray(right, dtype=np.int32)
+        f = L.kmc_film(len(offsets) - 1, L.ptr(offsets, C.c_int64), L.ptr(pos_m, C.c_double),
+                       L.ptr(orient, C.c_double), L.ptr(left, C.c_int32), L.ptr(right, C.c_int32))
+        self._check(self.lib.kmc_load_film(self.h, C.byref(f)))
+        self.n_films = len(offsets) - 1
+        self.offsets = offsets
+        return self
+
+    def set_table(self, table: dict):
+        """``table = {"kind": 4|2, "grids": [...], "rate": ndarray}``."""
+        grids = [_f64(g) for g in table["grids"]]
+        rate = _f64(table["rate"]).ravel()
+        t = L.kmc_table()
+        t.kind = int(table["kind"])
+        for d, g in enumerate(grids):
+            t.n[d] = len(g)
+            t.grid[d] = L.ptr(g, C.c_double)
+        t.rate = L.ptr(rate, C.c_double)
+        self._check(self.lib.kmc_set_rate_table(self.h, C.byref(t)))
+        return self
+
+    def build(self, r_max: float) -> dict:
+        st = L.kmc_nbr_stats()
+        self._check(self.lib.kmc_build_neighbors(self.h, float(r_max), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in L.kmc_nbr_stats._fields_}
+
+    def set_trace(self, n_trace: int, cap: int):
+        self._check(self.lib.kmc_set_trace(self.h, n_trace, cap))
+
+    def set_hop_cap(self, cap: int):
+        self._check(self.lib.kmc_set_hop_cap(self.h, cap))
+
+    def set_launch_config(self, block: int, steps_per_launch: int):
+        self._check(self.lib.kmc_set_launch_config(self.h, block, steps_per_launch))
+
+    def init_excitons(self, n_excitons, seeds, mode=L.KMC_INJECT_UNIFORM, n_sections=5):
+        ne = np.ascontiguousarray(np.broadcast_to(np.asarray(n_excitons, dtype=np.int64), (self.n_films,)))
+        sd = np.ascontiguousarray(np.broadcast_to(np.asarray(seeds, dtype=np.uint64), (self.n_films,)))
+        inj = L.kmc_inject(int(mode), int(n_sections), L.ptr(ne, C.c_int64), L.ptr(sd, C.c_uint64))
+        self._check(self.lib.kmc_init_excitons(self.h, C.byref(inj)))
+        self.n_exc = ne
+        return self
+
+    # ------------------------------------------------------------------ run and read
+    def run(self, n_steps: int, dt: float, velocity: float, precision=L.KMC_PREC_MIXED):
+        self._check(self.lib.kmc_run(self.h, int(n_steps), float(dt), float(velocity), int(precision)))
+
+    def msd(self, first: int, count: int) -> np.ndarray:
+        out = np.zeros((self.n_films, count, 3))
+        self._check(self.lib.kmc_get_msd(self.h, first, count, L.ptr(out, C.c_double)))
+        return out
+
+    def stats(self) -> dict:
+        st = L.kmc_run_stats()
+        self._check(self.lib.kmc_get_run_stats(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in L.kmc_run_stats._fields_}
+
+    def excitons(self) -> dict:
+        n = int(self.lib.kmc_num_excitons(self.h))
+        out = {"site": np.zeros(n, np.int32), "pos": np.zeros((n, 3)), "delta": np.zeros((n, 3)),
+               "ff": np.zeros(n), "heading": np.zeros(n, np.int32), "draws": np.zeros(n, np.uint64),
+               "hops": np.zeros(n, np.int64)}
+        self._check(self.lib.kmc_get_excitons(self.h, L.ptr(out["site"], C.c_int32), L.ptr(out["pos"], C.c_double),
+                                              L.ptr(out["delta"], C.c_double), L.ptr(out["ff"], C.c_double),
+                                              L.ptr(out["heading"], C.c_int32), L.ptr(out["draws"], C.c_uint64),
+                                              L.ptr(out["hops"], C.c_int64)))
+        return out
+
+    def neighbors(self, n_sites: int, nnz: int) -> dict:
+        rowptr = np.zeros(n_sites + 1, np.int64)
+        col = np.zeros(max(nnz, 1), np.int32)
+        cum = np.zeros(max(nnz, 1))
+        total = np.zeros(n_sites)
+        self._check(self.lib.kmc_get_neighbors(self.h, L.ptr(rowptr, C.c_int64), L.ptr(col, C.c_int32),
+                                               L.ptr(cum, C.c_double), L.ptr(total, C.c_double)))
+        return {"rowptr": rowptr, "col": col[:nnz], "cum": cum[:nnz], "total": total}
+
+    def trace(self, e: int, cap: int = 1 << 20):
+        buf = np.zeros(cap, np.int32)
+        n = self.lib.kmc_get_trace(self.h, e, L.ptr(buf, C.c_int32), cap)
+        if n < 0:
+            raise L.KmcError(int(n), "kmc_get_trace failed")
+        return buf[: min(n, cap)].copy(), int(n)
+
+    def selftest_uniform(self, r0: int, count: int) -> int:
+        m = C.c_uint64(0)
+        self._check(self.lib.kmc_selftest_uniform(self.h, r0, count, C.byref(m)))
+        return int(m.value)
+
+    def math_probe(self, x):
+        x = _f64(x)
+        lo = np.zeros_like(x)
+        ao = np.zeros_like(x)
+        self._check(self.lib.kmc_math_probe(self.h, L.ptr(x, C.c_double), len(x), L.ptr(lo, C.c_double),
+                                            L.ptr(ao, C.c_double)))
+        return lo, ao
+
+
+# ---------------------------------------------------------------------- host-side algorithms
+def trim_sites(pos_m, orient, left, right, lim):
+    """trim_scats on copies; returns the kept (pos, orient, left, right)."""
+    lib = L.load()
+    pos = _f64(pos_m).copy()
+    ori = _f64(orient).copy()
+    lk = np.ascontiguousarray(left, dtype=np.int32).copy()
+    rk = np.ascontiguousarray(right, dtype=np.int32).copy()
+    lim = _f64(lim)
+    n_out = C.c_int64(0)
+    rc = lib.kmc_trim_sites(len(lk), L.ptr(pos, C.c_double), L.ptr(ori, C.c_double), L.ptr(lk, C.c_int32),
+                            L.ptr(rk, C.c_int32), L.ptr(lim, C.c_double), C.byref(n_out))
+    if rc != L.KMC_OK:
+        raise L.KmcError(rc, "kmc_trim_sites failed")
+    n = n_out.value
+    return pos[:n].copy(), ori[:n].copy(), lk[:n].copy(), rk[:n].copy()
+
+
+def forster_table(gamma_0, theta_deg, zshift, ash1, ash2) -> dict:
+    """The reference's Förster table on its 4-D grid (monte_carlo.cpp:156-200)."""
+    lib = L.load()
+    th, z, a1, a2 = (_f64(v) for v in (theta_deg, zshift, ash1, ash2))
+    n = [int(th[2]), int(z[2]), int(a1[2]), int(a2[2])]
+    g = [np.zeros(k) for k in n]
+    rate = np.zeros(n)
+    rc = lib.kmc_forster_table(float(gamma_0), L.ptr(th, C.c_double), L.ptr(z, C.c_double), L.ptr(a1, C.c_double),
+                               L.ptr(a2, C.c_double), L.ptr(g[0], C.c_double), L.ptr(g[1], C.c_double),
+                               L.ptr(g[2], C.c_double), L.ptr(g[3], C.c_double), L.ptr(rate, C.c_double))
+    if rc != L.KMC_OK:
+        raise L.KmcError(rc, "kmc_forster_table failed")
+    return {"kind": 4, "grids": g, "rate": rate}
+
+
+def read_mesh(directory: str):
+    """Mesh directory -> (pos_m, orient, left, right) exactly as create_scatterers reads it."""
+    lib = L.load()
+    nt, npnt = C.c_int64(0), C.c_int64(0)
+    rc = lib.kmc_read_mesh(directory.encode(), C.byref(nt), C.byref(npnt), None, None, None, None)
+    if rc != L.KMC_OK:
+        raise L.KmcError(rc, f"cannot read mesh in {directory}")
+    n = nt.value * npnt.value
+    pos = np.zeros((n, 3))
+    ori = np.zeros((n, 3))
+    lk = np.zeros(n, np.int32)
+    rk = np.zeros(n, np.int32)
+    rc = lib.kmc_read_mesh(directory.encode(), C.byref(nt), C.byref(npnt), L.ptr(pos, C.c_double),
+                           L.ptr(ori, C.c_double), L.ptr(lk, C.c_int32), L.ptr(rk, C.c_int32))
+    if rc != L.KMC_OK:
+        raise L.KmcError(rc, f"cannot read mesh in {directory}")
+    return pos, ori, lk, rk

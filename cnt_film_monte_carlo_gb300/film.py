@@ -80,21 +80,25 @@ def unit_axes(phi: np.ndarray, tilt: np.ndarray) -> np.ndarray:
             break
         a[bad] = a[bad] / np.sqrt(_dot3(a[bad]))[:, None]
     bad = np.nonzero(_dot3(a) != 1.0)[0]
-    for i in bad:  # rare: walk one component by ulps until the rounded dot product is 1
+    for i in bad:  # walk one component by ulps (smallest first: finest steps) until the dot product is 1
         v = a[i].copy()
-        c = int(np.argmax(np.abs(v)))
-        for step in range(1, 64):
-            for sgn in (1.0, -1.0):
-                w = v.copy()
-                w[c] = v[c]
-                for _ in range(step):
-                    w[c] = np.nextafter(w[c], sgn * np.inf)
-                if _dot3(w[None, :])[0] == 1.0:
-                    a[i] = w
+        done = False
+        for c in np.argsort(np.abs(v)):
+            for step in range(1, 256):
+                for sgn in (1.0, -1.0):
+                    w = v.copy()
+                    for _ in range(step):
+                        w[c] = np.nextafter(w[c], sgn * np.inf)
+                    if _dot3(w[None, :])[0] == 1.0:
+                        a[i] = w
+                        done = True
+                        break
+                if done:
                     break
-            else:
-                continue
-            break
+            if done:
+                break
+        if not done:
+            raise RuntimeError("could not make a unit axis with dot(a, a) == 1")
     return a
 
 

@@ -1,0 +1,186 @@
+"""Host-side mirror of the reference's ``mc::monte_carlo`` Green-Kubo interface.
+
+Same method names, argument meaning, JSON keys and output file as
+src/monte_carlo/monte_carlo.{h,cpp} and the driver loop of src/main.cpp:62-76, so a caller of
+the reference switches by changing the import.  Every step runs on the GPU engine through the
+C ABI (include/cntkmc.h).
+
+Keys read from the "exciton monte carlo" JSON section (input.json:40-68):
+  mesh input directory, output directory, keep old results, rate type ("forster", "wong";
+  "davoody" needs "rate table directory" with a table saved by the reference),
+  zshift [m], axis shift 1 [m], axis shift 2 [m], theta [degrees], max hopping radius [m],
+  trim limits, exciton velocity [m/s], monte carlo time step,
+  number of sections for injection region, maximum time for kubo simulation [seconds],
+  number of particles for kubo simulation.
+Extensions: "philox seed" (default 100, the reference's srand(100) of main.cpp:30),
+  "injection": "region" (default) | "uniform", "precision": "mixed" (default) | "fp64",
+  "rate type": "forster2d" with "distance [m]" and "theta 2d [degrees]" grids.
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+
+import numpy as np
+
+from . import _lib as L
+from . import tables
+from .engine import Engine, read_mesh, trim_sites
+
+
+def _expand(path: str) -> str:
+    return os.path.expanduser(path) if path.startswith("~") else path
+
+
+def prepare_directory(path: str, keep_old_files: bool = True) -> str:
+    """prepare_directory (src/helper/prepare_directory.hpp:8-65): create the output directory;
+    an existing non-empty one is renamed to <dir>.N (keep) or emptied."""
+    path = _expand(path)
+    if not os.path.exists(path):
+        os.makedirs(path)
+        return path
+    if not os.path.isdir(path):
+        raise ValueError("The input value for output directory is not acceptable.")
+    if os.listdir(path):
+        if keep_old_files:
+            n = 1
+            while os.path.exists(f"{path}.{n}"):
+                n += 1
+            os.rename(path, f"{path}.{n}")
+        else:
+            shutil.rmtree(path)
+        os.makedirs(path)
+    return path
+
+
+def check_directory(path: str, should_be_empty: bool = False) -> str:
+    """check_directory (prepare_directory.hpp:68-105)."""
+    path = _expand(path)
+    if not os.path.exists(path):
+        raise ValueError("directory does NOT exists!!!")
+    if not os.path.isdir(path):
+        raise ValueError("input path is NOT a directory!!!")
+    if not os.listdir(path) and not should_be_empty:
+        raise ValueError("directory is empty!!!")
+    return path
+
+
+class monte_carlo:  # noqa: N801  (the reference's class name)
+    def __init__(self, j: dict, device: int = 0):
+        self._json_prop = dict(j)
+        keep = bool(j.get("keep old results", True))
+        self._output_directory = prepare_directory(j["output directory"], keep)
+        self._input_directory = check_directory(j["mesh input directory"], False)
+        self._time = 0.0  # the reference leaves _time uninitialised (monte_carlo.h:45)
+        self._engine = Engine(device)
+        self._max_time = 0.0
+        self._msd_file = None
+        self._n_particles = 0
+
+    # -- monte_carlo.h:139
+    def time(self) -> float:
+        return self._time
+
+    def kubo_max_time(self) -> float:
+        return self._max_time
+
+    def output_path(self) -> str:
+        return self._output_directory
+
+    def number_of_particles(self) -> int:
+        return self._n_particles
+
+    def create_scattering_table(self, j: dict) -> dict:
+        """monte_carlo.cpp:24-61."""
+        rt = j["rate type"]
+        grids = (j["theta [degrees]"], j["zshift [m]"], j["axis shift 1 [m]"], j["axis shift 2 [m]"])
+        if rt == "forster":
+            return tables.forster_4d(tables.FORSTER_GAMMA, *grids)
+        if rt == "wong":
+            return tables.forster_4d(tables.WONG_GAMMA, *grids)
+        if rt == "forster2d":
+            return tables.forster_2d(tables.FORSTER_GAMMA, j.get("distance [m]", (0.5e-9, 10e-9, 96)),
+                                     j.get("theta 2d [degrees]", (0.0, 90.0, 91)))
+        if rt == "davoody":
+            if "rate table directory" not in j:
+                raise ValueError("rate type davoody needs \"rate table directory\" (a table saved by the reference)")
+            return tables.read_reference_table(_expand(j["rate table directory"]))
+        raise ValueError('rate type must be one of the following: "davoody", "forster", "wong", "forster2d"')
+
+    def kubo_init(self):
+        """monte_carlo.cpp:254-305."""
+        j = self._json_prop
+        self._max_hopping_radius = float(j["max hopping radius [m]"])
+        self._particle_velocity = float(j["exciton velocity [m/s]"])
+        self._scat_table = self.create_scattering_table(j)
+        pos, ori, lk, rk = read_mesh(self._input_directory)
+        tl = j["trim limits"]
+        lim = [*tl["xlim"], *tl["ylim"], *tl["zlim"]]
+        pos, ori, lk, rk = trim_sites(pos, ori, lk, rk, lim)
+        self._sites = (pos, ori, lk, rk)
+        e = self._engine
+        e.load_arrays(np.array([0, len(lk)], np.int64), pos, ori, lk, rk)
+        e.set_table(self._scat_table)
+        self._nbr_stats = e.build(self._max_hopping_radius)
+        self._n_sections = int(j["number of sections for injection region"])
+        self._max_time = float(j["maximum time for kubo simulation [seconds]"])
+
+    def save_json_properties(self):
+        """monte_carlo.h:319-324."""
+        with open(os.path.join(self._output_directory, "input.json"), "w") as f:
+            json.dump(self._json_prop, f, indent=4)
+
+    def kubo_create_particles(self):
+        """monte_carlo.cpp:308-316 (exciton i draws from Philox stream i of "philox seed")."""
+        j = self._json_prop
+        n = int(j["number of particles for kubo simulation"])
+        mode = L.KMC_INJECT_UNIFORM if j.get("injection", "region") == "uniform" else L.KMC_INJECT_REGION
+        self._engine.init_excitons(n, int(j.get("philox seed", 100)), mode, self._n_sections)
+        self._n_particles = n
+        self._step = 0
+
+    def kubo_step(self, dt: float):
+        """monte_carlo.cpp:319-342."""
+        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
+        self._engine.run(1, dt, self._particle_velocity, prec)
+        self._step += 1
+        self._time += dt
+
+    def kubo_save_avg_dispalcement_squared(self):
+        """monte_carlo.cpp:382-409: one row "time,<dx^2>,<dy^2>,<dz^2>" (showpos, scientific)."""
+        if self._msd_file is None:
+            self._msd_file = open(os.path.join(self._output_directory, "particle_dispalcement.avg.squared.dat"), "w")
+            self._msd_file.write("# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble "
+                                 "over time\n")
+            self._msd_file.write(f"# number of particles: {self._n_particles}\n\n")
+            self._msd_file.write("time,x,y,z\n")
+        s = self._engine.msd(self._step - 1, 1)[0, 0] / float(self._n_particles)
+        self._msd_file.write(f"{self._time:+.6e},{s[0]:+.6e},{s[1]:+.6e},{s[2]:+.6e}\n")
+        self._msd_file.flush()
+
+    def close(self):
+        if self._msd_file is not None:
+            self._msd_file.close()
+            self._msd_file = None
+        self._engine.close()
+
+
+def run(input_json: str, device: int = 0) -> str:
+    """src/main.cpp:32-80: read input.json, run the Green-Kubo loop, return the output directory."""
+    with open(input_json) as f:
+        j = json.load(f)
+    if "exciton monte carlo" not in j:
+        raise ValueError('json input file does not contain "exciton monte carlo"')
+    jm = dict(j["exciton monte carlo"])
+    dt = float(jm["monte carlo time step"])
+    sim = monte_carlo(jm, device)
+    sim.kubo_init()
+    sim.save_json_properties()
+    sim.kubo_create_particles()
+    while sim.time() < sim.kubo_max_time():
+        sim.kubo_step(dt)
+        sim.kubo_save_avg_dispalcement_squared()
+    out = sim.output_path()
+    sim.close()
+    return out

@@ -1,0 +1,183 @@
+/* cntkmc.h -- C ABI of the GB300 exciton-hopping kinetic Monte Carlo engine.
+ *
+ * The reference (amirhosseindavoody/cnt_film_monte_carlo) has no plugin or FFI layer; its
+ * boundary is the C++ class mc::monte_carlo driven by src/main.cpp:62-76.  Each entry point
+ * below names the reference code it replaces.  Conventions:
+ *   - every call returns int: KMC_OK (0) or a negative KMC_ERR_* code; kmc_last_error()
+ *     gives the message of the last failure on that context; nothing throws across the ABI;
+ *   - plain pointers and sizes only; host buffers are copied in (the caller keeps them),
+ *     device memory belongs to the context;
+ *   - SI units (m, s, 1/s); positions [n][3] row-major;
+ *   - one context per host thread; calls on one context are not reentrant.
+ */
+#ifndef CNTKMC_H
+#define CNTKMC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KMC_OK 0
+#define KMC_ERR_ARG (-1)       /* invalid argument or size */
+#define KMC_ERR_CUDA (-2)      /* CUDA runtime failure (message has the CUDA error) */
+#define KMC_ERR_STATE (-3)     /* call out of order (e.g. run before build) */
+#define KMC_ERR_IO (-4)        /* file missing or malformed */
+#define KMC_ERR_HOP_CAP (-5)   /* an exciton exceeded the per-step hop cap (device error word) */
+#define KMC_ERR_NOMEM (-6)     /* device or host allocation failed */
+#define KMC_ERR_NO_DEVICE (-7) /* no CUDA device / wrong architecture */
+
+#define KMC_TABLE_4D 4 /* rate(theta)(z_shift, axis_shift_1, axis_shift_2), nearest grid point */
+#define KMC_TABLE_2D 2 /* rate(centre distance, folded angle in [0, pi/2]), nearest grid point */
+
+#define KMC_INJECT_REGION 0  /* reference Green-Kubo set-up: central cell of an n^3 split, removal slab */
+#define KMC_INJECT_UNIFORM 1 /* every site is an injection site, nothing is removed */
+
+#define KMC_PREC_FP64 0  /* plain FP64 hop kernel */
+#define KMC_PREC_MIXED 1 /* FP32 cumulative rates with exact FP64 re-resolve; same hop sequence */
+
+typedef struct kmc_ctx kmc_ctx;
+
+/* One or more films (batched).  Sites of film f are [film_site_offsets[f], [f+1]); left/right
+ * are film-local site indices or -1. */
+typedef struct {
+  int32_t n_films;
+  const int64_t* film_site_offsets; /* [n_films + 1] */
+  const double* pos;                /* [n_sites][3], metres */
+  const double* orient;             /* [n_sites][3], unit tube axes */
+  const int32_t* left;              /* [n_sites] */
+  const int32_t* right;             /* [n_sites] */
+} kmc_film;
+
+/* Rate table (scattering_struct, src/monte_carlo/scattering_struct.h:21-52).  grid[d] has n[d]
+ * points; rate is row-major [n0][n1][n2][n3] (4-D) or [n0][n1] (2-D). */
+typedef struct {
+  int32_t kind;
+  int32_t n[4];
+  const double* grid[4];
+  const double* rate;
+} kmc_table;
+
+typedef struct {
+  int32_t mode;               /* KMC_INJECT_* */
+  int32_t n_sections;         /* KMC_INJECT_REGION: odd n > 1 ("number of sections for injection region") */
+  const int64_t* n_excitons;  /* [n_films] */
+  const uint64_t* seeds;      /* [n_films] Philox key per film; exciton i of a film uses stream i */
+} kmc_inject;
+
+typedef struct {
+  int64_t n_sites;
+  int64_t nnz;           /* neighbour entries */
+  double k_mean;         /* nnz / n_sites */
+  int32_t k_max;
+  int64_t n_cells;
+  int64_t isolated;      /* sites with an empty neighbour list */
+  int64_t exact_only;    /* sites whose row the mixed kernel always resolves in FP64 */
+  double build_ms;       /* device time of cell binning + neighbour/rate build */
+} kmc_nbr_stats;
+
+typedef struct {
+  int64_t hops;          /* update_state calls (dwell draws + cumulative-rate selections) */
+  int64_t crossings;     /* moves onto the next segment by free flight along the tube */
+  int64_t exact_resolves;/* mixed kernel: selections/comparisons re-resolved in FP64 */
+  int64_t steps_done;    /* global time steps run so far */
+  double last_run_ms;    /* device time of the last kmc_run (CUDA events) */
+  int32_t last_launches; /* kernels launched by the last kmc_run */
+} kmc_run_stats;
+
+/* Context on CUDA device `device` (replaces mc::monte_carlo's constructor,
+ * src/monte_carlo/monte_carlo.h:116-136, minus file-system work). status may be NULL. */
+kmc_ctx* kmc_create(int device, int* status);
+void kmc_destroy(kmc_ctx* ctx);
+const char* kmc_last_error(const kmc_ctx* ctx);
+
+/* Copy the film(s) to the device (replaces create_scatterers, monte_carlo.h:199-271, after
+ * trim_scats :722-782, which the host applies with kmc_trim_sites). */
+int kmc_load_film(kmc_ctx* ctx, const kmc_film* film);
+
+/* Copy a rate table to the device (replaces set_scat_table, monte_carlo.h:419-423). */
+int kmc_set_rate_table(kmc_ctx* ctx, const kmc_table* table);
+
+/* Cell binning and the per-site neighbour/rate CSR, built once on the device (replaces
+ * create_scatterer_buckets monte_carlo.h:368-416, set_max_rate :426-440, and the per-hop
+ * find_neighbors scatterer.cpp:34-83).  Neighbour order, rates and cumulative sums are those of
+ * find_neighbors.  stats may be NULL. */
+int kmc_build_neighbors(kmc_ctx* ctx, double max_hopping_radius, kmc_nbr_stats* stats);
+
+/* Create the excitons (replaces injection_region / get_removal_domain / kubo_create_particles,
+ * monte_carlo.cpp:203-251,308-316, and the particle constructor particle.h:48-52). */
+int kmc_init_excitons(kmc_ctx* ctx, const kmc_inject* inject);
+
+/* n_steps calls of kubo_step(dt) (monte_carlo.cpp:319-342; particle::step particle.cpp:57-80;
+ * update_state scatterer.cpp:9-31; fly particle.cpp:9-54), velocity in m/s.  After each step the
+ * sums sum_i dx_i^2, dy_i^2, dz_i^2 of every film are recorded (the numerators of
+ * kubo_save_avg_dispalcement_squared, monte_carlo.cpp:382-409). */
+int kmc_run(kmc_ctx* ctx, int64_t n_steps, double dt, double velocity, int32_t precision);
+
+/* MSD sums of steps [first, first + count) for every film: out[f][s][3]. */
+int kmc_get_msd(kmc_ctx* ctx, int64_t first, int64_t count, double* out);
+
+/* Exciton state (film-major, exciton order).  Any pointer may be NULL.  pos/delta are [n][3]. */
+int kmc_get_excitons(kmc_ctx* ctx, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,
+                     uint64_t* draws, int64_t* hops);
+int64_t kmc_num_excitons(const kmc_ctx* ctx);
+int kmc_get_run_stats(kmc_ctx* ctx, kmc_run_stats* stats);
+
+/* Device CSR copied out for inspection: rowptr [n_sites+1] (film-global), col (film-local site),
+ * cum (FP64 cumulative rate), total [n_sites].  Any pointer may be NULL. */
+int kmc_get_neighbors(kmc_ctx* ctx, int64_t* rowptr, int32_t* col, double* cum, double* total);
+
+/* Hop trace of excitons [0, n_trace) of film 0, cap entries each (must be set before
+ * kmc_init_excitons): update_state result -> site; free-flight crossing -> -1 - site;
+ * reinjection -> INT32_MIN then the new site.  get returns the number of events recorded. */
+int kmc_set_trace(kmc_ctx* ctx, int64_t n_trace, int64_t cap);
+int64_t kmc_get_trace(kmc_ctx* ctx, int64_t exciton, int32_t* out, int64_t cap);
+
+/* Per-step hop cap per exciton (default 1e8); exceeding it makes kmc_run return KMC_ERR_HOP_CAP. */
+int kmc_set_hop_cap(kmc_ctx* ctx, int64_t cap);
+
+/* ---- host-side reference algorithms (no device needed) ---- */
+
+/* trim_scats (monte_carlo.h:722-782): remove sites outside lim = {xmin,xmax,ymin,ymax,zmin,zmax}
+ * by swapping them to the end and repairing tube links; arrays are permuted in place and
+ * *n_out gets the number kept. */
+int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_t* right, const double lim[6],
+                   int64_t* n_out);
+
+/* Domain of a site set (find_simulation_domain, monte_carlo.h:328-340): mn[3], mx[3]. */
+int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]);
+
+/* create_forster_scatt_table (monte_carlo.cpp:156-200) on arma::linspace grids {start, end, n};
+ * the theta grid is in degrees and scaled by pi/180 with pi = 3.141592 (helper/constants.h:10).
+ * Outputs: grids theta[nt], zsh[nz], ash1[n1], ash2[n2]; rate[nt][nz][n1][n2]. */
+int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
+                      const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate);
+
+/* Mesh directory (single_cnt.{pos,orient}.{x,y,z}.dat, monte_carlo.h:199-271): first call with
+ * NULL arrays returns *n_tubes and *n_points; second call fills pos/orient [n][3] (pos in m)
+ * and left/right. */
+int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* pos, double* orient,
+                  int32_t* left, int32_t* right);
+
+/* ---- diagnostics and tuning (no counterpart in the reference) ---- */
+
+/* Check the division-free dwell uniform RN(r / RAND_MAX) of the mixed kernel against IEEE
+ * division on the device for r in [r0, r0 + count); *mismatches gets the number of differences. */
+int kmc_selftest_uniform(kmc_ctx* ctx, uint32_t r0, uint64_t count, uint64_t* mismatches);
+
+/* Evaluate the engine's device log and acos on x[n] (for accuracy tests). */
+int kmc_math_probe(kmc_ctx* ctx, const double* x, int64_t n, double* log_out, double* acos_out);
+
+/* Hop-kernel launch shape: threads per block (multiple of 32, <= 256) and Green-Kubo steps per
+ * launch (the kernel keeps excitons in registers across the steps of one launch). */
+int kmc_set_launch_config(kmc_ctx* ctx, int32_t block, int32_t steps_per_launch);
+
+/* Library version string. */
+const char* kmc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CNTKMC_H */

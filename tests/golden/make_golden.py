@@ -1,0 +1,81 @@
+"""Regenerate the golden fixtures in tests/golden/ from the reference's own code.
+
+The reference ships no tests or golden vectors, so the fixtures are outputs of the reference's
+Green-Kubo engine itself: src/monte_carlo/{particle,scatterer,monte_carlo}.cpp compiled unchanged
+against the project's Armadillo shim (oracle/_ref/ref_kubo, built by ``make -C oracle ref``
+from the reference sources), with the per-exciton Philox rand() and the project log/acos
+interposed.  Each case stores the generated film, the config and everything the reference
+produced (trimmed sites, rate table, neighbour lists, per-step MSD sums, exciton states, hop
+traces).
+
+Needs the reference sources (REF_SRC, default /root/reference); the fixtures themselves are
+self-contained.  Run: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from cnt_film_monte_carlo_gb300 import film as F  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+CASES = {
+    # reference Green-Kubo set-up: trimmed film, central injection cell, removal slab, Förster table
+    "ref_forster_region": dict(tubes=12, length=40.0, box=(60, 60, 6), film_seed=3, rate="forster",
+                               trim=([5e-9, 55e-9], [-1e-6, 1e-6], [-1e-6, 1e-6]), r_max=10e-9, sections=3,
+                               n_exc=200, dt=1e-14, steps=40, seed=1234, n_trace=16),
+    # slower "wong" rates, longer steps (more free-flight crossings), wider cutoff
+    "ref_wong_region": dict(tubes=10, length=30.0, box=(40, 40, 8), film_seed=11, rate="wong",
+                            trim=([-1e-6, 1e-6], [2e-9, 38e-9], [-1e-6, 1e-6]), r_max=12e-9, sections=5,
+                            n_exc=150, dt=2e-13, steps=30, seed=7, n_trace=16),
+}
+
+
+def make_case(name, c, tmp):
+    f = F.straight_tubes(c["tubes"], c["length"], box_nm=c["box"], seed=c["film_seed"])
+    mesh = os.path.join(tmp, name, "mesh")
+    F.write_mesh(f, mesh)
+    mc = {
+        "mesh input directory": mesh, "output directory": os.path.join(tmp, name, "out"), "keep old results": False,
+        "rate type": c["rate"], "zshift [m]": [1.5e-9, 10e-9, 11], "axis shift 1 [m]": [-10e-9, 10e-9, 11],
+        "axis shift 2 [m]": [-10e-9, 10e-9, 11], "theta [degrees]": [0, 180, 21], "temperature [kelvin]": 300,
+        "max hopping radius [m]": c["r_max"],
+        "trim limits": {"xlim": c["trim"][0], "ylim": c["trim"][1], "zlim": c["trim"][2]},
+        "exciton velocity [m/s]": 2e5, "monte carlo time step": c["dt"],
+        "number of sections for injection region": c["sections"],
+        "maximum time for kubo simulation [seconds]": c["dt"] * c["steps"],
+        "number of particles for kubo simulation": c["n_exc"],
+    }
+    cfg_path = os.path.join(tmp, name, "input.json")
+    with open(cfg_path, "w") as fh:
+        json.dump({"exciton monte carlo": mc}, fh)
+    info, R = O.run_reference(cfg_path, os.path.join(tmp, name, "ref.bin"), c["steps"], c["seed"],
+                              n_trace=c["n_trace"], trace_cap=1 << 16, dump_csr=True)
+    out = {
+        "film_pos_nm": f.pos_nm, "film_orient": f.orient, "film_left": f.left, "film_right": f.right,
+        "config": np.frombuffer(json.dumps({k: v for k, v in mc.items() if "directory" not in k}).encode(), np.uint8),
+        "seed": np.uint64(c["seed"]), "steps": np.int64(c["steps"]),
+    }
+    for k, v in R.items():
+        out["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, info, {k: v.shape for k, v in out.items() if hasattr(v, "shape") and v.size > 1000})
+
+
+def main():
+    O.build(ref=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, c in CASES.items():
+            make_case(name, c, tmp)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,254 @@
+"""GPU parity: the CUDA engine through the C ABI against the oracle and the reference's golden
+outputs.  Hop-site sequences, exciton states, dwell clocks and positions are compared bit for bit;
+per-step MSD sums (accumulated with device atomics in a different order) to 1e-12 relative."""
+import numpy as np
+import pytest
+
+from cnt_film_monte_carlo_gb300 import _lib as L
+from cnt_film_monte_carlo_gb300 import engine as E
+from cnt_film_monte_carlo_gb300 import film as F
+from cnt_film_monte_carlo_gb300 import tables
+from helpers import CASES, case_inputs, hop_events, load_case, ref_traces
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+MSD_RTOL = 1e-12
+PRECISIONS = [L.KMC_PREC_FP64, L.KMC_PREC_MIXED]
+
+
+def assert_msd_close(a, b):
+    a = np.asarray(a, dtype=np.float64).ravel()
+    b = np.asarray(b, dtype=np.float64).ravel()
+    np.testing.assert_allclose(a, b, rtol=MSD_RTOL, atol=0)
+
+
+def assert_states_equal(g, o, n=None):
+    n = n if n is not None else len(o["site"])
+    for k in ("site", "pos", "delta", "ff", "heading", "draws"):
+        assert np.array_equal(g[k][:n], o[k][:n]), k
+
+
+@pytest.fixture(scope="module")
+def eng():
+    e = E.Engine(0)
+    yield e
+    e.close()
+
+
+def test_dwell_uniform_exact_for_every_rand_value(eng):
+    # the division-free RN(r / RAND_MAX) of the mixed kernel equals IEEE division for all r
+    assert eng.selftest_uniform(0, 1 << 31) == 0
+
+
+def test_device_log_acos_match_oracle(eng):
+    rng = np.random.default_rng(3)
+    x = np.concatenate([rng.uniform(0, 1, 20000), [r / 2147483647.0 for r in rng.integers(1, 2**31 - 1, 20000)],
+                        np.exp(rng.uniform(-700, 700, 5000)), [1.0, 0.5, 2.0, 5e-324]])
+    lo, _ = eng.math_probe(x)
+    assert np.array_equal(lo, np.array([O.log(v) for v in x]))
+    c = np.concatenate([rng.uniform(-1, 1, 20000), [1.0, -1.0, 0.5, -0.5, 0.0, 0.9999999999]])
+    _, ac = eng.math_probe(c)
+    assert np.array_equal(ac, np.array([O.acos(v) for v in c]))
+
+
+def golden_engine(d):
+    ci = case_inputs(d)
+    pos, ori, lk, rk = E.trim_sites(ci["pos"], ci["orient"], ci["left"], ci["right"], ci["lim"])
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, len(lk)], np.int64), pos, ori, lk, rk)
+    e.set_table(E.forster_table(ci["gamma"], *ci["grids"]))
+    st = e.build(ci["r_max"])
+    return e, ci, st, len(lk)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_golden_neighbor_csr(name):
+    d = load_case(name)
+    e, ci, st, n = golden_engine(d)
+    nb = e.neighbors(n, st["nnz"])
+    assert np.array_equal(nb["rowptr"], d["ref_csr_rowptr"])
+    assert np.array_equal(nb["col"], d["ref_csr_col"])
+    assert np.array_equal(nb["cum"], d["ref_csr_cum"])
+    assert np.array_equal(nb["total"], d["ref_total"])
+    assert st["k_max"] == int(np.max(np.diff(d["ref_csr_rowptr"])))
+    e.close()
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("name", CASES)
+def test_golden_green_kubo(name, precision):
+    d = load_case(name)
+    e, ci, st, n = golden_engine(d)
+    n_tr = len(d["ref_trace_len"])
+    e.set_trace(n_tr, 1 << 16)
+    e.init_excitons(ci["n_exc"], int(d["seed"]), L.KMC_INJECT_REGION, ci["sections"])
+    g0 = e.excitons()
+    assert np.array_equal(g0["site"], d["ref_site_init"])
+    assert np.array_equal(g0["ff"], d["ref_ff_init"])
+    assert np.array_equal(g0["heading"], d["ref_heading_init"])
+    steps = int(d["steps"])
+    half = steps // 2
+    e.run(half, ci["dt"], ci["v"], precision)  # two calls: state carried across launches
+    e.run(steps - half, ci["dt"], ci["v"], precision)
+    g = e.excitons()
+    assert np.array_equal(g["site"], d["ref_site"])
+    assert np.array_equal(g["pos"].ravel(), d["ref_xpos"])
+    assert np.array_equal(g["delta"].ravel(), d["ref_delta"])
+    assert np.array_equal(g["ff"], d["ref_ff"])
+    assert np.array_equal(g["heading"], d["ref_heading"])
+    assert np.array_equal(g["draws"], d["ref_draws"])
+    assert e.stats()["hops"] == int(d["ref_hops"][0])
+    assert_msd_close(e.msd(0, steps), d["ref_msd"])
+    for i, rt in enumerate(ref_traces(d)):
+        tr, _ = e.trace(i)
+        assert np.array_equal(hop_events(tr)[: len(rt)], rt)
+    e.close()
+
+
+def synthetic_case(table_kind=2, n_tubes=40, length=60.0, box=(120.0, 120.0, 8.0), seed=5, r_max=10e-9):
+    f = F.straight_tubes(n_tubes, length, box_nm=box, seed=seed)
+    if table_kind == 2:
+        tab = tables.forster_2d(1e15)
+    else:
+        tab = E.forster_table(1e15, (0, 180, 21), (1.5e-9, 10e-9, 11), (-10e-9, 10e-9, 11), (-10e-9, 10e-9, 11))
+    return f, tab, r_max
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("table_kind", [2, 4])
+def test_uniform_injection_vs_oracle(precision, table_kind):
+    f, tab, r_max = synthetic_case(table_kind)
+    n_exc, seed, dt, v, steps = 500, 1234, 2e-13, 2e5, 12
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, r_max, v)
+    sim.set_trace(8, 1 << 18)
+    sim.create_excitons(1, 0, n_exc, seed)
+    om = sim.step(dt, steps)
+    o = sim.excitons()
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_table(tab)
+    st = e.build(r_max)
+    csr = sim.build_csr()
+    nb = e.neighbors(f.n_sites, st["nnz"])
+    assert np.array_equal(nb["col"], csr["col"]) and np.array_equal(nb["cum"], csr["cum"])
+    e.set_trace(8, 1 << 18)
+    e.init_excitons(n_exc, seed, L.KMC_INJECT_UNIFORM)
+    e.run(steps, dt, v, precision)
+    assert_states_equal(e.excitons(), o)
+    assert_msd_close(e.msd(0, steps), om)
+    for i in range(8):
+        a, na = e.trace(i)
+        b, nb_ = sim.trace(i)
+        assert na == nb_ and np.array_equal(a, b)  # hops and free-flight crossings, in order
+    assert e.stats()["hops"] == sim.total_hops()
+    assert e.stats()["crossings"] == sim.total_crossings()
+    e.close()
+
+
+def test_batched_films_equal_single_films():
+    films = [F.straight_tubes(n, 40.0, box_nm=(80, 80, 6), seed=s) for n, s in ((12, 1), (30, 2), (7, 3))]
+    tab = tables.forster_2d(1e15)
+    n_exc, seeds, dt, v, steps = [70, 200, 33], [11, 22, 33], 1e-13, 2e5, 6
+    b = E.Engine(0)
+    b.load_films(films)
+    b.set_table(tab)
+    b.build(10e-9)
+    b.init_excitons(n_exc, seeds, L.KMC_INJECT_UNIFORM)
+    b.run(steps, dt, v, L.KMC_PREC_MIXED)
+    gb = b.excitons()
+    mb = b.msd(0, steps)
+    off = 0
+    for i, f in enumerate(films):
+        s = E.Engine(0)
+        s.load_films(f)
+        s.set_table(tab)
+        s.build(10e-9)
+        s.init_excitons(n_exc[i], seeds[i], L.KMC_INJECT_UNIFORM)
+        s.run(steps, dt, v, L.KMC_PREC_FP64)
+        gs = s.excitons()
+        for k in ("site", "pos", "delta", "ff", "draws"):
+            assert np.array_equal(gb[k][off:off + n_exc[i]], gs[k]), (i, k)
+        assert_msd_close(mb[i], s.msd(0, steps)[0])
+        off += n_exc[i]
+        s.close()
+    b.close()
+
+
+def test_isolated_sites_and_far_tube():
+    # a tube far from the rest: its sites have no neighbours inside the cutoff (empty lists;
+    # undefined in the reference, defined here as "stay, fly along the tube")
+    f = F.straight_tubes(6, 20.0, box_nm=(30, 30, 4), seed=8)
+    far = F.straight_tubes(1, 5.0, box_nm=(1, 1, 1), seed=9)
+    n0 = f.n_sites
+    pos = np.vstack([f.pos_m(), (far.pos_nm + 500.0) * 1e-9])
+    ori = np.vstack([f.orient, far.orient])
+    lk = np.concatenate([f.left, np.where(far.left >= 0, far.left + n0, -1)]).astype(np.int32)
+    rk = np.concatenate([f.right, np.where(far.right >= 0, far.right + n0, -1)]).astype(np.int32)
+    tab = tables.forster_2d(1e15)
+    sim = O.Sim(pos, ori, lk, rk, tab, 3e-9, 2e5)
+    sim.create_excitons(1, 0, 300, 5)
+    om = sim.step(1e-13, 5)
+    for prec in PRECISIONS:
+        e = E.Engine(0)
+        e.load_arrays(np.array([0, len(lk)], np.int64), pos, ori, lk, rk)
+        e.set_table(tab)
+        st = e.build(3e-9)
+        assert st["isolated"] >= 5
+        e.init_excitons(300, 5, L.KMC_INJECT_UNIFORM)
+        e.run(5, 1e-13, 2e5, prec)
+        assert_states_equal(e.excitons(), sim.excitons())
+        assert_msd_close(e.msd(0, 5), om)
+        e.close()
+
+
+def test_hop_cap_reports_error_and_context_recovers():
+    f, tab, r_max = synthetic_case(2, n_tubes=10, length=20.0, box=(40, 40, 4))
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_table(tab)
+    e.build(r_max)
+    e.init_excitons(64, 1, L.KMC_INJECT_UNIFORM)
+    e.set_hop_cap(3)
+    with pytest.raises(L.KmcError) as ex:
+        e.run(1, 1e-12, 2e5, L.KMC_PREC_MIXED)
+    assert ex.value.code == L.KMC_ERR_HOP_CAP
+    e.set_hop_cap(10**9)
+    e.init_excitons(64, 1, L.KMC_INJECT_UNIFORM)
+    e.run(2, 1e-13, 2e5, L.KMC_PREC_MIXED)
+    assert e.stats()["hops"] > 0
+    e.close()
+
+
+def test_argument_errors():
+    e = E.Engine(0)
+    with pytest.raises(L.KmcError) as ex:
+        e.run(1, 1e-13, 2e5)
+    assert ex.value.code == L.KMC_ERR_STATE
+    f, tab, r_max = synthetic_case(2, n_tubes=4, length=10.0, box=(20, 20, 2))
+    e.load_films(f)
+    with pytest.raises(L.KmcError):
+        e.build(r_max)  # no table yet
+    e.set_table(tab)
+    with pytest.raises(L.KmcError):
+        e.build(-1.0)
+    e.build(r_max)
+    with pytest.raises(L.KmcError):
+        e.init_excitons(10, 1, L.KMC_INJECT_REGION, 4)  # even number of sections
+    e.close()
+
+
+def test_launch_shape_does_not_change_results():
+    f, tab, r_max = synthetic_case(2, n_tubes=20, length=40.0, box=(80, 80, 6))
+    out = []
+    for block, spl in ((128, 32), (64, 1), (256, 5)):
+        e = E.Engine(0)
+        e.load_films(f)
+        e.set_table(tab)
+        e.build(r_max)
+        e.set_launch_config(block, spl)
+        e.init_excitons(1000, 3, L.KMC_INJECT_UNIFORM)
+        e.run(7, 1e-13, 2e5, L.KMC_PREC_MIXED)
+        out.append(e.excitons())
+        e.close()
+    for o in out[1:]:
+        assert_states_equal(o, out[0])

@@ -1,0 +1,95 @@
+"""The oracle against golden outputs of the reference's own code (CPU).
+
+tests/golden/*.npz were produced by the reference's src/monte_carlo sources compiled unchanged
+(oracle/_ref, see tests/golden/make_golden.py).  Everything must match bit for bit.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import CASES, case_inputs, hop_events, load_case, ref_traces
+from oracle import oracle as O
+
+
+@pytest.fixture(params=CASES, scope="module")
+def case(request):
+    return load_case(request.param)
+
+
+def test_trim_table_csr(case):
+    ci = case_inputs(case)
+    pos, ori, lk, rk = O.trim(ci["pos"], ci["orient"], ci["left"], ci["right"], ci["lim"])
+    assert np.array_equal(pos.ravel(), case["ref_pos"])
+    assert np.array_equal(ori.ravel(), case["ref_orient"])
+    assert np.array_equal(lk, case["ref_left"]) and np.array_equal(rk, case["ref_right"])
+    tab = O.forster_table(ci["gamma"], *ci["grids"])
+    assert np.array_equal(tab["rate"].ravel(), case["ref_table_rate"])
+    assert np.array_equal(tab["grids"][0], case["ref_table_theta"])
+    sim = O.Sim(pos, ori, lk, rk, tab, ci["r_max"], ci["v"])
+    csr = sim.build_csr()
+    assert np.array_equal(csr["rowptr"], case["ref_csr_rowptr"])
+    assert np.array_equal(csr["col"], case["ref_csr_col"])
+    assert np.array_equal(csr["cum"], case["ref_csr_cum"])
+    assert np.array_equal(csr["total"], case["ref_total"])
+    assert np.array_equal(csr["inv_total"], case["ref_inv_total"])
+    mn, mx, _ = sim.domain()
+    assert np.array_equal(np.r_[mn, mx], case["ref_domain"])
+
+
+@pytest.mark.parametrize("use_csr", [True, False])
+def test_green_kubo_run(case, use_csr):
+    ci = case_inputs(case)
+    pos, ori, lk, rk = O.trim(ci["pos"], ci["orient"], ci["left"], ci["right"], ci["lim"])
+    tab = O.forster_table(ci["gamma"], *ci["grids"])
+    sim = O.Sim(pos, ori, lk, rk, tab, ci["r_max"], ci["v"])
+    n_tr = len(case["ref_trace_len"])
+    sim.set_trace(n_tr, 1 << 16)
+    sim.create_excitons(0, ci["sections"], ci["n_exc"], int(case["seed"]), use_csr=use_csr)
+    assert sim.n_inject() == len(case["ref_inject"])
+    e0 = sim.excitons()
+    assert np.array_equal(e0["site"], case["ref_site_init"])
+    assert np.array_equal(e0["ff"], case["ref_ff_init"])
+    assert np.array_equal(e0["heading"], case["ref_heading_init"])
+    msd = sim.step(ci["dt"], int(case["steps"]))
+    assert np.array_equal(msd.ravel(), case["ref_msd"])
+    e = sim.excitons()
+    assert np.array_equal(e["site"], case["ref_site"])
+    assert np.array_equal(e["pos"].ravel(), case["ref_xpos"])
+    assert np.array_equal(e["delta"].ravel(), case["ref_delta"])
+    assert np.array_equal(e["ff"], case["ref_ff"])
+    assert np.array_equal(e["heading"], case["ref_heading"])
+    assert np.array_equal(e["draws"], case["ref_draws"])
+    assert sim.total_hops() == int(case["ref_hops"][0])
+    for i, rt in enumerate(ref_traces(case)):
+        tr, _ = sim.trace(i)
+        assert np.array_equal(hop_events(tr)[: len(rt)], rt)
+
+
+def test_live_reference_matches_oracle(tmp_path):
+    """A fresh seed against the reference run right now (needs the reference sources)."""
+    if not os.path.exists(O.REF_BIN):
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    import json
+
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    f = F.straight_tubes(9, 35.0, box_nm=(45, 45, 5), seed=21)
+    F.write_mesh(f, str(tmp_path / "mesh"))
+    mc = {"mesh input directory": str(tmp_path / "mesh"), "output directory": str(tmp_path / "out"),
+          "keep old results": False, "rate type": "forster", "zshift [m]": [1.5e-9, 10e-9, 11],
+          "axis shift 1 [m]": [-10e-9, 10e-9, 11], "axis shift 2 [m]": [-10e-9, 10e-9, 11],
+          "theta [degrees]": [0, 180, 21], "max hopping radius [m]": 9e-9,
+          "trim limits": {"xlim": [-1, 1], "ylim": [-1, 1], "zlim": [-1, 1]}, "exciton velocity [m/s]": 2e5,
+          "monte carlo time step": 5e-14, "number of sections for injection region": 3,
+          "maximum time for kubo simulation [seconds]": 1e-12, "number of particles for kubo simulation": 64}
+    p = tmp_path / "in.json"
+    p.write_text(json.dumps({"exciton monte carlo": mc}))
+    _, R = O.run_reference(str(p), str(tmp_path / "r.bin"), 12, 99, n_trace=4, trace_cap=4096)
+    pos, ori, lk, rk = O.trim(f.pos_m(), f.orient, f.left, f.right, [-1, 1, -1, 1, -1, 1])
+    sim = O.Sim(pos, ori, lk, rk, O.forster_table(1e15, *[mc[k] for k in (
+        "theta [degrees]", "zshift [m]", "axis shift 1 [m]", "axis shift 2 [m]")]), 9e-9, 2e5)
+    sim.create_excitons(0, 3, 64, 99)
+    msd = sim.step(5e-14, 12)
+    assert np.array_equal(msd.ravel(), R["msd"])
+    assert np.array_equal(sim.excitons()["pos"].ravel(), R["xpos"])

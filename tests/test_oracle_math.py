@@ -1,0 +1,103 @@
+"""Known-answer tests of the oracle's RNG and math (CPU)."""
+import os
+import re
+import struct
+
+import mpmath
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+mpmath.mp.prec = 120
+
+
+def ulp_err(x, exact):
+    x = float(x)
+    e = mpmath.mpf(exact)
+    if e == 0:
+        return 0.0 if x == 0 else float("inf")
+    u = np.spacing(abs(float(e)))
+    return float(abs(mpmath.mpf(x) - e) / u)
+
+
+def test_philox_published_vectors():
+    # Random123 known-answer vectors for philox4x32-10 (Salmon et al., SC'11)
+    assert list(O.philox([0, 0, 0, 0], [0, 0])) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert list(O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2)) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+    assert list(O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0])) == [
+        0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_rand_stream_layout():
+    # draw n of stream s: word n%4 of philox(ctr={n/4, 0, s, 0}, key=seed) >> 1
+    seed, s = 0x1234567890ABCDEF, 77
+    for n in range(9):
+        w = O.philox([n // 4, 0, s, 0], [seed & 0xFFFFFFFF, seed >> 32])[n % 4]
+        assert O.rand(seed, s, n) == int(w) >> 1
+    vals = [O.rand(1, 0, n) for n in range(4000)]
+    assert 0 <= min(vals) and max(vals) <= 2**31 - 1
+    assert len(set(vals)) > 3990
+    assert O.rand(1, 0, 5) != O.rand(1, 1, 5)
+
+
+def test_log_accuracy():
+    rng = np.random.default_rng(0)
+    xs = list(rng.uniform(0, 1, 3000)) + list(np.exp(rng.uniform(-700, 700, 2000)))
+    xs += [(r / 2147483647.0) for r in rng.integers(1, 2**31 - 1, 2000)]
+    xs += [1 - 2.0**-k for k in range(1, 53)] + [1 + 2.0**-k for k in range(1, 53)] + [5e-324, 2.2250738585072014e-308]
+    worst = max(ulp_err(O.log(x), mpmath.log(mpmath.mpf(x))) for x in xs)
+    assert worst < 1.0, worst
+    assert O.log(1.0) == 0.0
+    assert O.log(0.0) == -np.inf and np.isnan(O.log(-1.0)) and O.log(np.inf) == np.inf
+
+
+def test_acos_accuracy():
+    rng = np.random.default_rng(1)
+    cs = list(rng.uniform(-1, 1, 4000)) + [1 - 2.0**-k for k in range(1, 53)] + [-1 + 2.0**-k for k in range(1, 53)]
+    cs += [0.5, -0.5, 0.0, -0.0, 1.0, -1.0, np.nextafter(0.5, 1), np.nextafter(-0.5, -1)]
+    worst = max(ulp_err(O.acos(c), mpmath.acos(mpmath.mpf(c))) for c in cs)
+    assert worst < 2.0, worst
+    assert O.acos(1.0) == 0.0 and np.isnan(O.acos(1.0000000000000002)) and np.isnan(O.acos(np.nan))
+
+
+def _header_doubles(path, pattern):
+    txt = open(path).read()
+    return [float.fromhex(h) for h in re.findall(pattern, txt)]
+
+
+def test_oracle_and_engine_tables_agree():
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hexnum = r"(-?0x[0-9a-f]\.[0-9a-f]+p[+-]\d+)"
+    a = _header_doubles(os.path.join(root, "oracle", "kmc_math_tables.h"), hexnum)
+    b = _header_doubles(os.path.join(root, "cnt_film_monte_carlo_gb300", "csrc", "kmc_math_tables.h"), hexnum)
+    assert len(a) > 400 and sorted(a) == sorted(b)
+
+
+@pytest.mark.parametrize("dice,expect", [(0.0, 1), (1.0, 1), (2.0, 3), (2.5, 3), (3.0, 4), (9.0, 4), (-1.0, 0)])
+def test_select_semantics(dice, expect):
+    # cumulative row with zero-rate runs: the first index whose cum > dice, clamped to n-1 (scatterer.cpp:17-30)
+    cum = np.array([0.0, 2.0, 2.0, 3.0, 3.0])
+    assert O.select(cum, dice) == expect
+
+
+def test_select_single_and_pair():
+    assert O.select(np.array([5.0]), 7.0) == 0
+    assert O.select(np.array([1.0, 2.0]), 0.5) == 0
+    assert O.select(np.array([1.0, 2.0]), 1.0) == 1
+
+
+def test_index_min_semantics():
+    g = np.array([0.0, 1.0, 2.0, 3.0])
+    assert O.index_min(g, 1.5) == 1  # tie -> first
+    assert O.index_min(g, 2.6) == 3
+    assert O.index_min(g, -5) == 0
+    assert O.index_min(g, np.nan) == 0
+
+
+def test_linspace_semantics():
+    x = O.linspace(-10e-9, 10e-9, 11)
+    assert x[-1] == 10e-9 and x[0] == -10e-9
+    d = (10e-9 - (-10e-9)) / 10
+    assert all(x[i] == -10e-9 + i * d for i in range(10))
+    assert list(O.linspace(3.0, 7.0, 1)) == [7.0]
