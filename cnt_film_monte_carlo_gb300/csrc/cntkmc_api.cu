@@ -513,6 +513,7 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_run: bad precision");
   CK(c, cudaSetDevice(c->device));
   if (n_steps == 0) return KMC_OK;
+  dt = dt + 0.0;  // a zero time step is +0 (the kernels compare non-negative doubles bitwise)
   int rc = ensure_msd(c, c->steps_done + n_steps);
   if (rc) return rc;
   if (precision == KMC_PREC_MIXED && c->lt_v != v) {
@@ -709,7 +710,7 @@ int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, doub
 
 int kmc_set_launch_config(kmc_ctx* c, int32_t block, int32_t steps_per_launch) {
   if (!c) return KMC_ERR_ARG;
-  if (block < 32 || block > 256 || block % 32 || steps_per_launch < 1) FAIL(c, KMC_ERR_ARG, "kmc_set_launch_config: bad values");
+  if (block < 32 || block > 256 || block % 32 || steps_per_launch < 1 || steps_per_launch > 1024) FAIL(c, KMC_ERR_ARG, "kmc_set_launch_config: bad values");
   c->block = block;
   c->steps_per_launch = steps_per_launch;
   return KMC_OK;

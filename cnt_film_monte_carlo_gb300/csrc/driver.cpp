@@ -1,0 +1,53 @@
+// driver.cpp -- cntkmc_run: drop-in replacement for the reference's src/main.cpp Green-Kubo run.
+//
+//   cntkmc_run [input.json]
+//
+// Reads the "exciton monte carlo" section of input.json (default file name as main.cpp:34-38),
+// then runs the same loop as main.cpp:64-76: kubo_init, save_json_properties,
+// kubo_create_particles, and while time < max time: kubo_step(dt), kubo_save_avg_dispalcement_squared.
+#include <chrono>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <string>
+
+#include "monte_carlo.hpp"
+
+int main(int argc, char** argv) {
+  try {
+    std::string filename = argc <= 1 ? "input.json" : argv[1];
+    std::ifstream in(filename);
+    if (!in) throw std::invalid_argument("cannot open " + filename);
+    std::stringstream ss;
+    ss << in.rdbuf();
+    jl::Value j = jl::parse(ss.str());
+    if (!j.has("exciton monte carlo"))
+      throw std::invalid_argument("json input file does not contain \"exciton monte carlo\"");
+    const jl::Value& jm = j["exciton monte carlo"];
+    double time_step = jm["monte carlo time step"].as_double();
+    auto t0 = std::chrono::steady_clock::now();
+    cntkmc::monte_carlo sim(jm);
+    sim.kubo_init();
+    sim.save_json_properties();
+    sim.kubo_create_particles();
+    const kmc_nbr_stats& nb = sim.neighbor_stats();
+    std::printf("sites: %lld  neighbour entries: %lld (mean %.2f, max %d)  build: %.3f ms\n", (long long)nb.n_sites,
+                (long long)nb.nnz, nb.k_mean, nb.k_max, nb.build_ms);
+    double dev_ms = 0;
+    while (sim.time() < sim.kubo_max_time()) {
+      sim.kubo_step(time_step);
+      sim.kubo_save_avg_dispalcement_squared();
+      dev_ms += sim.run_stats().last_run_ms;
+    }
+    kmc_run_stats rs = sim.run_stats();
+    double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf("Green-Kubo simulation finished: %lld steps, %lld hops, %lld crossings, device %.3f s, wall %.3f s\n",
+                (long long)rs.steps_done, (long long)rs.hops, (long long)rs.crossings, dev_ms / 1e3, wall);
+    std::printf("output: %s\n", sim.output_path().c_str());
+    return 0;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "cntkmc_run: %s\n", e.what());
+    return 1;
+  }
+}

@@ -6,11 +6,11 @@ acos(a1 . a2) (scatterer.cpp:51).  The engine evaluates both with functions of i
 that every build (CUDA device code, host code) produces the same bits:
 
 * log: P. T. P. Tang's table-driven method (ACM TOMS 16(4), 1990).  x = 2^k z with
-  z in [0.701171875, 1.40234375), split into 128 intervals of equal width in the bit
+  z in [a, 2a), a ~ 0.7012, split into 1024 intervals of equal width in the bit
   pattern; interval i has c_i = 1/midpoint (c = 1 exactly on the interval holding 1.0)
   and -log(c_i) as hi (a multiple of 2^-42, so k ln2_hi + hi is exact) + lo;
   log x = (k ln2_hi + hi) + (r + ((k ln2_lo + lo) + r^2 P(r))), r = fma(z, c_i, -1),
-  P(r) = -1/2 + r/3 - ... - r^6/8 (Taylor series of log1p).
+  P(r) = -1/2 + r/3 - r^2/4 + r^3/5 (Taylor series of log1p; |r| <= 2^-11).
 * acos: pi/2 - asin(c) for |c| <= 1/2, 2 asin(sqrt((1-c)/2)) above and
   pi - 2 asin(sqrt((1+c)/2)) below, asin(x) = x + x z Q(z), z = x^2, Q from the Taylor
   series (2n)!/(4^n (n!)^2 (2n+1)), 24 terms.
@@ -25,11 +25,11 @@ import mpmath
 
 mpmath.mp.prec = 200
 
-BITS = 7
+BITS = 10
 N = 1 << BITS
 ONE = 0x3FF0000000000000
 STEP = 1 << (52 - BITS)
-CENTER = 76
+CENTER = 76 * 8 + 4  # the interval that holds 1.0 in its middle
 OFF = ONE - STEP // 2 - CENTER * STEP
 N_ASIN = 24
 
@@ -67,7 +67,7 @@ def main():
         "KMC_PI_HI": nearest(mpmath.pi),
         "KMC_PI_LO": nearest(mpmath.pi - mpmath.mpf(nearest(mpmath.pi))),
     }
-    log1p = [nearest(mpmath.mpf((-1) ** (j + 1)) / j) for j in range(2, 9)]
+    log1p = [nearest(mpmath.mpf((-1) ** (j + 1)) / j) for j in range(2, 6)]
     asin = [
         nearest(mpmath.factorial(2 * n) / (mpmath.mpf(4) ** n * mpmath.factorial(n) ** 2 * (2 * n + 1)))
         for n in range(1, N_ASIN + 1)

@@ -1,0 +1,194 @@
+// json_lite.hpp -- a small JSON reader/writer for the drop-in driver's input.json.
+// Supports objects, arrays, numbers, strings (with \" \\ \/ \b \f \n \r \t \uXXXX escapes for
+// ASCII), true/false/null.  Object key order is kept for writing the file back.
+#pragma once
+#include <cstdlib>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace jl {
+
+struct Value {
+  enum Kind { Null, Bool, Number, String, Array, Object } kind = Null;
+  bool b = false;
+  double num = 0;
+  std::string str;
+  std::vector<Value> arr;
+  std::vector<std::pair<std::string, Value>> obj;
+
+  bool has(const std::string& k) const {
+    for (auto& kv : obj)
+      if (kv.first == k) return true;
+    return false;
+  }
+  const Value& operator[](const std::string& k) const {
+    for (auto& kv : obj)
+      if (kv.first == k) return kv.second;
+    throw std::invalid_argument("json: missing key \"" + k + "\"");
+  }
+  const Value& operator[](size_t i) const {
+    if (kind != Array || i >= arr.size()) throw std::invalid_argument("json: index out of range");
+    return arr[i];
+  }
+  double as_double() const {
+    if (kind != Number) throw std::invalid_argument("json: number expected");
+    return num;
+  }
+  long long as_int() const { return (long long)as_double(); }
+  bool as_bool() const {
+    if (kind != Bool) throw std::invalid_argument("json: bool expected");
+    return b;
+  }
+  const std::string& as_string() const {
+    if (kind != String) throw std::invalid_argument("json: string expected");
+    return str;
+  }
+};
+
+class Parser {
+ public:
+  explicit Parser(const std::string& s) : s_(s) {}
+  Value parse() {
+    Value v = value();
+    ws();
+    if (i_ != s_.size()) fail("trailing characters");
+    return v;
+  }
+
+ private:
+  const std::string& s_;
+  size_t i_ = 0;
+  [[noreturn]] void fail(const char* what) {
+    throw std::invalid_argument(std::string("json: ") + what + " at offset " + std::to_string(i_));
+  }
+  void ws() {
+    while (i_ < s_.size() && (s_[i_] == ' ' || s_[i_] == '\n' || s_[i_] == '\t' || s_[i_] == '\r')) ++i_;
+  }
+  bool eat(char c) {
+    ws();
+    if (i_ < s_.size() && s_[i_] == c) {
+      ++i_;
+      return true;
+    }
+    return false;
+  }
+  Value value() {
+    ws();
+    if (i_ >= s_.size()) fail("unexpected end");
+    char c = s_[i_];
+    Value v;
+    if (c == '{') {
+      ++i_;
+      v.kind = Value::Object;
+      if (eat('}')) return v;
+      do {
+        ws();
+        std::string k = string();
+        if (!eat(':')) fail("':' expected");
+        v.obj.emplace_back(k, value());
+      } while (eat(','));
+      if (!eat('}')) fail("'}' expected");
+    } else if (c == '[') {
+      ++i_;
+      v.kind = Value::Array;
+      if (eat(']')) return v;
+      do {
+        v.arr.push_back(value());
+      } while (eat(','));
+      if (!eat(']')) fail("']' expected");
+    } else if (c == '"') {
+      v.kind = Value::String;
+      v.str = string();
+    } else if (s_.compare(i_, 4, "true") == 0) {
+      i_ += 4;
+      v.kind = Value::Bool;
+      v.b = true;
+    } else if (s_.compare(i_, 5, "false") == 0) {
+      i_ += 5;
+      v.kind = Value::Bool;
+    } else if (s_.compare(i_, 4, "null") == 0) {
+      i_ += 4;
+    } else {
+      const char* p = s_.c_str() + i_;
+      char* e;
+      v.num = std::strtod(p, &e);
+      if (e == p) fail("value expected");
+      v.kind = Value::Number;
+      i_ += (size_t)(e - p);
+    }
+    return v;
+  }
+  std::string string() {
+    if (i_ >= s_.size() || s_[i_] != '"') fail("string expected");
+    ++i_;
+    std::string out;
+    while (i_ < s_.size() && s_[i_] != '"') {
+      char c = s_[i_++];
+      if (c == '\\') {
+        if (i_ >= s_.size()) fail("bad escape");
+        char e = s_[i_++];
+        switch (e) {
+          case 'n': out += '\n'; break;
+          case 't': out += '\t'; break;
+          case 'r': out += '\r'; break;
+          case 'b': out += '\b'; break;
+          case 'f': out += '\f'; break;
+          case 'u': {
+            if (i_ + 4 > s_.size()) fail("bad \\u escape");
+            out += (char)std::strtol(s_.substr(i_, 4).c_str(), nullptr, 16);
+            i_ += 4;
+            break;
+          }
+          default: out += e;
+        }
+      } else {
+        out += c;
+      }
+    }
+    if (i_ >= s_.size()) fail("unterminated string");
+    ++i_;
+    return out;
+  }
+};
+
+inline Value parse(const std::string& text) { return Parser(text).parse(); }
+
+inline void write(std::ostream& o, const Value& v, int indent = 0) {
+  std::string pad(indent, ' '), pad2(indent + 4, ' ');
+  switch (v.kind) {
+    case Value::Null: o << "null"; break;
+    case Value::Bool: o << (v.b ? "true" : "false"); break;
+    case Value::Number: {
+      std::ostringstream t;
+      t.precision(17);
+      t << v.num;
+      o << t.str();
+      break;
+    }
+    case Value::String: o << '"' << v.str << '"'; break;
+    case Value::Array:
+      o << "[";
+      for (size_t i = 0; i < v.arr.size(); ++i) {
+        if (i) o << ", ";
+        write(o, v.arr[i], indent + 4);
+      }
+      o << "]";
+      break;
+    case Value::Object:
+      o << "{\n";
+      for (size_t i = 0; i < v.obj.size(); ++i) {
+        o << pad2 << '"' << v.obj[i].first << "\": ";
+        write(o, v.obj[i].second, indent + 4);
+        o << (i + 1 < v.obj.size() ? ",\n" : "\n");
+      }
+      o << pad << "}";
+      break;
+  }
+}
+
+}  // namespace jl

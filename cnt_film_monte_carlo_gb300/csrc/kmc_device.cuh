@@ -126,8 +126,27 @@ struct LogTab {
   double t[1 << KMC_LOG_TABLE_BITS][3];
 };
 
+// log(z 2^k) from the reduced argument: the common tail of kmc_log and kmc_log_unit.
+__device__ __forceinline__ double log_tail(uint64_t ix, uint64_t tmp, double kf, const LogTab* __restrict__ tab) {
+  int i = (int)((tmp >> (52 - KMC_LOG_TABLE_BITS)) & ((1u << KMC_LOG_TABLE_BITS) - 1));
+  double z = __longlong_as_double((long long)(ix - (tmp & 0xFFF0000000000000ull)));
+  double invc = __ldg(&tab->t[i][0]);
+  double lhi = __ldg(&tab->t[i][1]);
+  double llo = __ldg(&tab->t[i][2]);
+  const double c[4] = KMC_LOG1P_INIT;
+  double r = fma(z, invc, -1.0);
+  double t1 = fma(kf, KMC_LN2_HI, lhi);
+  double p = c[3];
+  p = fma(p, r, c[2]);
+  p = fma(p, r, c[1]);
+  p = fma(p, r, c[0]);
+  double r2 = r * r;
+  double q = r2 * p;
+  double s = fma(kf, KMC_LN2_LO, llo) + q;
+  return t1 + (r + s);
+}
+
 __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ tab) {
-  // Inputs here are dwell-time uniforms in (0, 1]; the general cases are still handled.
   uint64_t ix = (uint64_t)__double_as_longlong(x);
   if (!(x > 0.0)) return x == 0.0 ? -__longlong_as_double(0x7FF0000000000000ll) : __longlong_as_double(0x7FF8000000000000ll);
   if (ix >= 0x7FF0000000000000ull) return x;
@@ -138,27 +157,21 @@ __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ t
     kadj = -52;
   }
   uint64_t tmp = ix - KMC_LOG_OFF;
-  int i = (int)((tmp >> (52 - KMC_LOG_TABLE_BITS)) & ((1u << KMC_LOG_TABLE_BITS) - 1));
   int k = (int)((int64_t)tmp >> 52) + kadj;
-  double z = __longlong_as_double((long long)(ix - (tmp & 0xFFF0000000000000ull)));
-  double invc = __ldg(&tab->t[i][0]);
-  double lhi = __ldg(&tab->t[i][1]);
-  double llo = __ldg(&tab->t[i][2]);
-  const double c[7] = KMC_LOG1P_INIT;
-  double kf = (double)k;
-  double r = fma(z, invc, -1.0);
-  double t1 = fma(kf, KMC_LN2_HI, lhi);
-  double p = c[6];
-  p = fma(p, r, c[5]);
-  p = fma(p, r, c[4]);
-  p = fma(p, r, c[3]);
-  p = fma(p, r, c[2]);
-  p = fma(p, r, c[1]);
-  p = fma(p, r, c[0]);
-  double r2 = r * r;
-  double q = r2 * p;
-  double s = fma(kf, KMC_LN2_LO, llo) + q;
-  return t1 + (r + s);
+  return log_tail(ix, tmp, (double)k, tab);
+}
+
+// kmc_log for a normal x in (0, 1] (the dwell-time uniforms): no special cases, and the exponent
+// k in [-1022, 0] is turned into a double with integer operations (same exact value as (double)k).
+__device__ __forceinline__ double kmc_log_unit(double x, const LogTab* __restrict__ tab) {
+  uint64_t ix = (uint64_t)__double_as_longlong(x);
+  uint64_t tmp = ix - KMC_LOG_OFF;
+  int k = (int)((int64_t)tmp >> 52);
+  uint32_t m = (uint32_t)(-k);
+  int e = 31 - __clz((int)m);
+  uint64_t kb = m ? ((1ull << 63) | ((uint64_t)(1023 + e) << 52) | (((uint64_t)m << (52 - e)) & ((1ull << 52) - 1)))
+                  : 0ull;
+  return log_tail(ix, tmp, __longlong_as_double((long long)kb), tab);
 }
 
 // ---------------------------------------------------------------- acos (asin Taylor series)

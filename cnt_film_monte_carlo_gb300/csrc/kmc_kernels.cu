@@ -605,9 +605,24 @@ __device__ __forceinline__ bool link_time_less(uint32_t lt_hi, const double2* lt
   return lt < dtf;
 }
 
+// Exact ff <= rem for rem >= +0 and ff not a NaN with the sign bit set (device NaNs are
+// positive): non-negative doubles order like their bit patterns, and a negative ff (or -0.0)
+// is below every non-negative rem in both orders.
+__device__ __forceinline__ bool dwell_fits(double ff, double rem) {
+  return __double_as_longlong(ff) <= __double_as_longlong(rem);
+}
+
+// Each lane advances its exciton through all n_steps steps of the launch on its own (a lane
+// whose step ends early starts its next step instead of waiting for the warp); the MSD sums of
+// a warp's lanes go to per-warp shared-memory bins and are added to global memory once at the end.
 __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
+  extern __shared__ double s_bins[];  // [warps in block][n_steps][3]
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  double* bins = s_bins + (size_t)wib * n_steps * 3;
+  for (int64_t i = lane; i < n_steps * 3; i += 32) bins[i] = 0.0;
+  __syncwarp();
   int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (slot >= a.n_slots) return;
+  if (slot >= a.n_slots) return;  // whole warps (n_slots is a multiple of 32)
   int32_t film = a.warp_film[slot >> 5];
   const FilmDev& f = a.films[film];
   const float* __restrict__ cumn = a.cumn + f.nnz0;
@@ -618,159 +633,183 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
   e.trace_i = (film == 0 && local < a.n_trace) ? local : -1;
   if (e.active) e.g.init(f.seed, (uint64_t)local, a.e_draws[slot]);
   uint64_t exact = 0;
-  bool dead = false;
   const float lo_m = 1.0f - 0x1p-20f, hi_m = 1.0f + 0x1p-20f;
-  for (int64_t s = 0; s < n_steps; ++s) {
-    if (e.active && e.at_site) {
+  int64_t s = 0;
+  double ox = 0, oy = 0, oz = 0, rem = a.dt;
+  int64_t hs = 0;
+  SiteRec rr;
+  if (e.active) {
+    if (e.at_site) {
       double4_32a p = a.pos4[e.site];
       e.px = p.x;
       e.py = p.y;
       e.pz = p.z;
     }
-    double ox = e.px, oy = e.py, oz = e.pz;
-    if (e.active && !dead) {
-      double rem = a.dt;
-      int64_t hs = 0;
-      SiteRec rr = a.rec[e.site];
-      while (e.ff <= rem) {
-        rem -= e.ff;
-        // ---- fly(ff)
-        double dtf = e.ff;
-        if (rr.left >= 0 || rr.right >= 0) {
-          for (int guard = 0;; ++guard) {
-            if (guard >= kMaxCrossings) {
-              atomicOr(a.err, KMC_ERR_FLIGHT_CODE);
-              break;
-            }
-            int32_t next = e.heading ? (rr.right > -1 ? rr.right : rr.left) : (rr.left > -1 ? rr.left : rr.right);
-            bool to_right = (next == rr.right);
-            e.heading = to_right;
-            bool cross;
-            double lt;
-            if (e.at_site) {
-              cross = link_time_less(to_right ? rr.lt_hi_r : rr.lt_hi_l, a.lt64, e.site, to_right, dtf, exact);
-              if (cross) {
-                double2 l = a.lt64[e.site];
-                lt = to_right ? l.y : l.x;
-              }
-            } else {
-              double4_32a t = a.pos4[next];
-              double dist = norm3(e.px - t.x, e.py - t.y, e.pz - t.z);
-              lt = dist / a.v;
-              cross = lt < dtf;
-            }
-            if (cross) {
-              e.site = next;
-              e.at_site = true;
-              dtf -= lt;
-              e.crossings++;
-              trace_push(a, e, -1 - next);
-              rr = a.rec[next];
-              continue;
-            }
-            // partial flight: observed only if no hop follows (empty neighbour list)
-            if ((rr.len_flags & kLenMask) == 0) {
-              if (e.at_site) {
-                double4_32a p = a.pos4[e.site];
-                e.px = p.x;
-                e.py = p.y;
-                e.pz = p.z;
-              }
-              double4_32a t = a.pos4[next];
-              double e0 = t.x - e.px, e1 = t.y - e.py, e2 = t.z - e.pz;
-              double nn = norm3(e0, e1, e2);
-              double den = nn != 0 ? nn : 1.0;
-              double u0 = e0 / den, u1 = e1 / den, u2 = e2 / den;
-              double k = a.v * dtf;
-              e.px = e.px + k * u0;
-              e.py = e.py + k * u1;
-              e.pz = e.pz + k * u2;
-              e.at_site = false;
-            }
+    ox = e.px;
+    oy = e.py;
+    oz = e.pz;
+    rr = a.rec[e.site];
+  } else {
+    s = n_steps;
+  }
+  while (s < n_steps) {
+    if (dwell_fits(e.ff, rem)) {
+      // ------------------------------------------------ one event of particle::step (particle.cpp:71-84)
+      rem -= e.ff;
+      double dtf = e.ff;
+      if (rr.left >= 0 || rr.right >= 0) {  // fly(ff)
+        for (int guard = 0;; ++guard) {
+          if (guard >= kMaxCrossings) {
+            atomicOr(a.err, KMC_ERR_FLIGHT_CODE);
             break;
           }
-        }
-        // ---- update_state
-        uint32_t n = rr.len_flags & kLenMask;
-        int32_t ns = e.site;
-        if (n > 0) {
-          uint32_t r = e.g.next();
-          const uint32_t row = rr.row;
-          bool resolved = false;
-          if (!(rr.len_flags & kRecExact)) {
-            float u = __uint2float_rn(r) * (1.0f / 2147483647.0f);
-            unsigned left = (unsigned)-1, right = n - 1;
-            float cl = 0.f, cr = 0.f;
-            while (left + 1 < right) {
-              unsigned mid = (left + right) / 2;
-              float c = __ldg(cumn + row + mid);
-              if (c <= u) {
-                left = mid;
-                cl = c;
-              } else {
-                right = mid;
-                cr = c;
-              }
+          int32_t next = e.heading ? (rr.right > -1 ? rr.right : rr.left) : (rr.left > -1 ? rr.left : rr.right);
+          bool to_right = (next == rr.right);
+          e.heading = to_right;
+          bool cross;
+          double lt;
+          if (e.at_site) {
+            cross = link_time_less(to_right ? rr.lt_hi_r : rr.lt_hi_l, a.lt64, e.site, to_right, dtf, exact);
+            if (cross) {
+              double2 l = a.lt64[e.site];
+              lt = to_right ? l.y : l.x;
             }
-            bool ok = (left == (unsigned)-1 || cl < u * lo_m) && (right == n - 1 || cr > u * hi_m);
-            if (ok) {
-              ns = __ldg(col + row + right);
-              resolved = true;
-            }
+          } else {
+            double4_32a t = a.pos4[next];
+            double dist = norm3(e.px - t.x, e.py - t.y, e.pz - t.z);
+            lt = dist / a.v;
+            cross = lt < dtf;
           }
-          if (!resolved) {  // exact FP64 update_state on the site's FP64 row
-            ++exact;
-            const double* cum = a.cum + f.nnz0 + row;
-            double dice = a.total[e.site] * (double)r / (double)kRandMax;
-            unsigned left = (unsigned)-1, right = n - 1;
-            while (left + 1 < right) {
-              unsigned mid = (left + right) / 2;
-              if (cum[mid] <= dice)
-                left = mid;
-              else
-                right = mid;
-            }
-            ns = col[row + right];
+          if (cross) {
+            e.site = next;
+            e.at_site = true;
+            dtf -= lt;
+            e.crossings++;
+            trace_push(a, e, -1 - next);
+            rr = a.rec[next];
+            continue;
           }
-        }
-        e.hops++;
-        trace_push(a, e, ns);
-        if (ns != e.site) {
-          e.site = ns;
-          e.at_site = true;
-          rr = a.rec[ns];
-        }
-        uint32_t r;
-        while ((r = e.g.next()) == 0) {
-        }
-        e.ff = -rr.inv_total * kmc_log(u_from_rand(r), a.logtab);
-        if (++hs > a.hop_cap) {
-          atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
-          dead = true;
+          // the partial flight is observed only when no hop follows (empty neighbour list)
+          if ((rr.len_flags & kLenMask) == 0) {
+            if (e.at_site) {
+              double4_32a p = a.pos4[e.site];
+              e.px = p.x;
+              e.py = p.y;
+              e.pz = p.z;
+            }
+            double4_32a t = a.pos4[next];
+            double e0 = t.x - e.px, e1 = t.y - e.py, e2 = t.z - e.pz;
+            double nn = norm3(e0, e1, e2);
+            double den = nn != 0 ? nn : 1.0;
+            double u0 = e0 / den, u1 = e1 / den, u2 = e2 / den;
+            double k = a.v * dtf;
+            e.px = e.px + k * u0;
+            e.py = e.py + k * u1;
+            e.pz = e.pz + k * u2;
+            e.at_site = false;
+          }
           break;
         }
       }
-      if (!dead) {
-        if (e.at_site) {
-          double4_32a p = a.pos4[e.site];
-          e.px = p.x;
-          e.py = p.y;
-          e.pz = p.z;
+      // update_state (scatterer.cpp:9-31)
+      uint32_t n = rr.len_flags & kLenMask;
+      int32_t ns = e.site;
+      if (n > 0) {
+        uint32_t r = e.g.next();
+        const uint32_t row = rr.row;
+        bool resolved = false;
+        if (!(rr.len_flags & kRecExact)) {
+          float u = __uint2float_rn(r) * (1.0f / 2147483647.0f);
+          unsigned left = (unsigned)-1, right = n - 1;
+          float cl = 0.f, cr = 0.f;
+          while (left + 1 < right) {
+            unsigned mid = (left + right) / 2;
+            float c = __ldg(cumn + row + mid);
+            if (c <= u) {
+              left = mid;
+              cl = c;
+            } else {
+              right = mid;
+              cr = c;
+            }
+          }
+          if ((left == (unsigned)-1 || cl < u * lo_m) && (right == n - 1 || cr > u * hi_m)) {
+            ns = __ldg(col + row + right);
+            resolved = true;
+          }
         }
-        fly_full(a, e, rem);
-        e.at_site = false;
-        e.ff -= rem;
+        if (!resolved) {  // exact FP64 selection on the site's FP64 row
+          ++exact;
+          const double* cum = a.cum + f.nnz0 + row;
+          double dice = a.total[e.site] * (double)r / (double)kRandMax;
+          unsigned left = (unsigned)-1, right = n - 1;
+          while (left + 1 < right) {
+            unsigned mid = (left + right) / 2;
+            if (cum[mid] <= dice)
+              left = mid;
+            else
+              right = mid;
+          }
+          ns = col[row + right];
+        }
       }
+      e.hops++;
+      trace_push(a, e, ns);
+      if (ns != e.site) {
+        e.site = ns;
+        e.at_site = true;
+        rr = a.rec[ns];
+      }
+      uint32_t r;
+      while ((r = e.g.next()) == 0) {
+      }
+      e.ff = -rr.inv_total * kmc_log_unit(u_from_rand(r), a.logtab);
+      if (++hs > a.hop_cap) {
+        atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
+        break;
+      }
+    } else {
+      // ------------------------------------------------ end of step s: fly(rem), ff -= rem, kubo_step tail
+      if (e.at_site) {
+        double4_32a p = a.pos4[e.site];
+        e.px = p.x;
+        e.py = p.y;
+        e.pz = p.z;
+      }
+      fly_full(a, e, rem);
+      e.at_site = false;
+      e.ff -= rem;
+      e.dx += e.px - ox;
+      e.dy += e.py - oy;
+      e.dz += e.pz - oz;
+      maybe_reinject(a, f, e);
+      atomicAdd(&bins[s * 3 + 0], e.dx * e.dx);
+      atomicAdd(&bins[s * 3 + 1], e.dy * e.dy);
+      atomicAdd(&bins[s * 3 + 2], e.dz * e.dz);
+      ++s;
+      ox = e.px;
+      oy = e.py;
+      oz = e.pz;
+      rem = a.dt;
+      hs = 0;
+      rr = a.rec[e.site];
     }
-    step_epilogue(a, f, film, e, ox, oy, oz, s);
   }
+  __syncwarp();
+  double* m = a.msd + ((int64_t)film * a.msd_cap + a.step0) * 3;
+  for (int64_t i = lane; i < n_steps * 3; i += 32) atomicAdd(m + i, bins[i]);
   store_exciton(a, slot, e);
   flush_counters(a, e, exact);
 }
 
 cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s) {
   int64_t nb = (a.n_slots + block - 1) / block;
-  if (nb) k_hop_mixed<<<(unsigned)nb, block, 0, s>>>(a, n_steps);
+  size_t smem = (size_t)(block / 32) * n_steps * 3 * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_hop_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  if (nb) k_hop_mixed<<<(unsigned)nb, block, smem, s>>>(a, n_steps);
   return cudaGetLastError();
 }
 

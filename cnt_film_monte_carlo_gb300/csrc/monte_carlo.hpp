@@ -1,0 +1,269 @@
+// monte_carlo.hpp -- C++ mirror of the reference's mc::monte_carlo Green-Kubo interface
+// (src/monte_carlo/monte_carlo.h:35-844, monte_carlo.cpp:254-409) on top of the C ABI.
+//
+// Same method names, JSON keys ("exciton monte carlo" section of input.json) and output file
+// (particle_dispalcement.avg.squared.dat).  Every step runs on the GPU engine.  Errors are
+// thrown as std::runtime_error / std::invalid_argument, as the reference throws.
+// Extensions: "philox seed" (default 100), "injection": "region" | "uniform",
+// "precision": "mixed" | "fp64", "rate type": "forster2d" with "distance [m]" and
+// "theta 2d [degrees]" grids, "rate table directory" for a table saved by the reference.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <filesystem>
+#include <fstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cntkmc.h"
+#include "json_lite.hpp"
+
+namespace cntkmc {
+
+namespace fs = std::filesystem;
+
+inline std::string expand_home(std::string p) {
+  if (!p.empty() && p[0] == '~') {
+    const char* h = std::getenv("HOME");
+    p = std::string(h ? h : "") + p.substr(1);
+  }
+  return p;
+}
+
+// prepare_directory (src/helper/prepare_directory.hpp:8-65)
+inline std::string prepare_directory(std::string path, bool keep_old_files = true) {
+  path = expand_home(path);
+  if (!fs::exists(path)) {
+    fs::create_directories(path);
+    return path;
+  }
+  if (!fs::is_directory(path)) throw std::invalid_argument("The input value for output directory is not acceptable.");
+  if (!fs::is_empty(path)) {
+    if (keep_old_files) {
+      int n = 1;
+      while (fs::exists(path + "." + std::to_string(n))) ++n;
+      fs::rename(path, path + "." + std::to_string(n));
+    } else {
+      fs::remove_all(path);
+    }
+    fs::create_directories(path);
+  }
+  return path;
+}
+
+// check_directory (prepare_directory.hpp:68-105)
+inline std::string check_directory(std::string path, bool should_be_empty = false) {
+  path = expand_home(path);
+  if (!fs::exists(path)) throw std::invalid_argument("directory does NOT exists!!!");
+  if (!fs::is_directory(path)) throw std::invalid_argument("input path is NOT a directory!!!");
+  if (fs::is_empty(path) && !should_be_empty) throw std::invalid_argument("directory is empty!!!");
+  return path;
+}
+
+class monte_carlo {
+ public:
+  explicit monte_carlo(const jl::Value& j, int device = 0) : j_(j) {
+    bool keep = j.has("keep old results") ? j["keep old results"].as_bool() : true;
+    out_dir_ = prepare_directory(j["output directory"].as_string(), keep);
+    in_dir_ = check_directory(j["mesh input directory"].as_string(), false);
+    int st = 0;
+    ctx_ = kmc_create(device, &st);
+    if (!ctx_) throw std::runtime_error("cntkmc: no usable CUDA device (status " + std::to_string(st) + ")");
+  }
+  ~monte_carlo() {
+    if (msd_) std::fclose(msd_);
+    kmc_destroy(ctx_);
+  }
+  monte_carlo(const monte_carlo&) = delete;
+  monte_carlo& operator=(const monte_carlo&) = delete;
+
+  const double& time() const { return time_; }
+  const double& kubo_max_time() const { return max_time_; }
+  const std::string& output_path() const { return out_dir_; }
+  unsigned number_of_particles() const { return (unsigned)n_particles_; }
+
+  // monte_carlo.cpp:254-305
+  void kubo_init() {
+    r_max_ = j_["max hopping radius [m]"].as_double();
+    velocity_ = j_["exciton velocity [m/s]"].as_double();
+    create_scattering_table();
+    int64_t nt = 0, np = 0;
+    check(kmc_read_mesh(in_dir_.c_str(), &nt, &np, nullptr, nullptr, nullptr, nullptr), "kmc_read_mesh");
+    int64_t n = nt * np;
+    pos_.resize(3 * n);
+    orient_.resize(3 * n);
+    left_.resize(n);
+    right_.resize(n);
+    check(kmc_read_mesh(in_dir_.c_str(), &nt, &np, pos_.data(), orient_.data(), left_.data(), right_.data()),
+          "kmc_read_mesh");
+    const jl::Value& tl = j_["trim limits"];
+    double lim[6] = {tl["xlim"][0].as_double(), tl["xlim"][1].as_double(), tl["ylim"][0].as_double(),
+                     tl["ylim"][1].as_double(), tl["zlim"][0].as_double(), tl["zlim"][1].as_double()};
+    int64_t kept = 0;
+    check(kmc_trim_sites(n, pos_.data(), orient_.data(), left_.data(), right_.data(), lim, &kept), "kmc_trim_sites");
+    if (kept == 0) throw std::invalid_argument("no site left inside the trim limits");
+    int64_t off[2] = {0, kept};
+    kmc_film f{1, off, pos_.data(), orient_.data(), left_.data(), right_.data()};
+    check(kmc_load_film(ctx_, &f), "kmc_load_film");
+    kmc_table t{};
+    t.kind = table_kind_;
+    for (size_t d = 0; d < grids_.size(); ++d) {
+      t.n[d] = (int32_t)grids_[d].size();
+      t.grid[d] = grids_[d].data();
+    }
+    t.rate = rates_.data();
+    check(kmc_set_rate_table(ctx_, &t), "kmc_set_rate_table");
+    check(kmc_build_neighbors(ctx_, r_max_, &nbr_), "kmc_build_neighbors");
+    n_sections_ = (int)j_["number of sections for injection region"].as_int();
+    max_time_ = j_["maximum time for kubo simulation [seconds]"].as_double();
+  }
+
+  // monte_carlo.h:319-324
+  void save_json_properties() const {
+    std::ofstream f(fs::path(out_dir_) / "input.json");
+    jl::write(f, j_);
+    f << "\n";
+  }
+
+  // monte_carlo.cpp:308-316
+  void kubo_create_particles() {
+    n_particles_ = j_["number of particles for kubo simulation"].as_int();
+    uint64_t seed = j_.has("philox seed") ? (uint64_t)j_["philox seed"].as_int() : 100u;
+    bool uniform = j_.has("injection") && j_["injection"].as_string() == "uniform";
+    int64_t ne = n_particles_;
+    kmc_inject inj{uniform ? KMC_INJECT_UNIFORM : KMC_INJECT_REGION, n_sections_, &ne, &seed};
+    check(kmc_init_excitons(ctx_, &inj), "kmc_init_excitons");
+    steps_ = 0;
+  }
+
+  // monte_carlo.cpp:319-342
+  void kubo_step(double dt) {
+    int prec = (j_.has("precision") && j_["precision"].as_string() == "fp64") ? KMC_PREC_FP64 : KMC_PREC_MIXED;
+    check(kmc_run(ctx_, 1, dt, velocity_, prec), "kmc_run");
+    ++steps_;
+    time_ += dt;
+  }
+
+  // monte_carlo.cpp:382-409
+  void kubo_save_avg_dispalcement_squared() {
+    if (!msd_) {
+      msd_ = std::fopen((fs::path(out_dir_) / "particle_dispalcement.avg.squared.dat").c_str(), "w");
+      if (!msd_) throw std::runtime_error("cannot open the MSD file");
+      std::fprintf(msd_, "# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble over time\n");
+      std::fprintf(msd_, "# number of particles: %lld\n\ntime,x,y,z\n", (long long)n_particles_);
+    }
+    double s[3];
+    check(kmc_get_msd(ctx_, steps_ - 1, 1, s), "kmc_get_msd");
+    double n = double(n_particles_);
+    std::fprintf(msd_, "%+e,%+e,%+e,%+e\n", time_, s[0] / n, s[1] / n, s[2] / n);
+    std::fflush(msd_);
+  }
+
+  const kmc_nbr_stats& neighbor_stats() const { return nbr_; }
+  kmc_run_stats run_stats() const {
+    kmc_run_stats s{};
+    kmc_get_run_stats(ctx_, &s);
+    return s;
+  }
+
+ private:
+  void check(int rc, const char* what) const {
+    if (rc != KMC_OK) throw std::runtime_error(std::string(what) + ": " + kmc_last_error(ctx_));
+  }
+  static std::vector<double> lin(const jl::Value& g) { return lin3(g[0].as_double(), g[1].as_double(), g[2].as_int()); }
+  // arma::linspace as the engine defines it: a + i (b - a)/(n - 1), last element b
+  static std::vector<double> lin3(double a, double b, int64_t n) {
+    std::vector<double> x((size_t)std::max<int64_t>(n, 0));
+    if (n == 1) x[0] = b;
+    if (n >= 2) {
+      const double delta = (b - a) / double(n - 1);
+      for (int64_t i = 0; i < n - 1; ++i) x[i] = a + double(i) * delta;
+      x[n - 1] = b;
+    }
+    return x;
+  }
+  // monte_carlo.cpp:24-61
+  void create_scattering_table() {
+    std::string rt = j_["rate type"].as_string();
+    if (rt == "forster" || rt == "wong") {
+      double g0 = rt == "forster" ? 1.e15 : 1.e13;
+      const jl::Value *th = &j_["theta [degrees]"], *z = &j_["zshift [m]"], *a1 = &j_["axis shift 1 [m]"],
+                      *a2 = &j_["axis shift 2 [m]"];
+      double gt[3] = {(*th)[0].as_double(), (*th)[1].as_double(), (*th)[2].as_double()};
+      double gz[3] = {(*z)[0].as_double(), (*z)[1].as_double(), (*z)[2].as_double()};
+      double g1[3] = {(*a1)[0].as_double(), (*a1)[1].as_double(), (*a1)[2].as_double()};
+      double g2[3] = {(*a2)[0].as_double(), (*a2)[1].as_double(), (*a2)[2].as_double()};
+      grids_.assign(4, {});
+      grids_[0].resize((size_t)gt[2]);
+      grids_[1].resize((size_t)gz[2]);
+      grids_[2].resize((size_t)g1[2]);
+      grids_[3].resize((size_t)g2[2]);
+      rates_.resize(grids_[0].size() * grids_[1].size() * grids_[2].size() * grids_[3].size());
+      if (kmc_forster_table(g0, gt, gz, g1, g2, grids_[0].data(), grids_[1].data(), grids_[2].data(), grids_[3].data(),
+                            rates_.data()) != KMC_OK)
+        throw std::invalid_argument("bad rate-table grids");
+      table_kind_ = KMC_TABLE_4D;
+      return;
+    }
+    if (rt == "forster2d") {
+      grids_ = {j_.has("distance [m]") ? lin(j_["distance [m]"]) : lin3(0.5e-9, 10e-9, 96),
+                j_.has("theta 2d [degrees]") ? lin(j_["theta 2d [degrees]"]) : lin3(0, 90, 91)};
+      for (auto& t : grids_[1]) t = t * (3.141592 / 180);
+      rates_.resize(grids_[0].size() * grids_[1].size());
+      for (size_t i = 0; i < grids_[0].size(); ++i)
+        for (size_t k = 0; k < grids_[1].size(); ++k) {
+          double c = std::cos(grids_[1][k]);
+          rates_[i * grids_[1].size() + k] = 1.e15 * (c * c) * std::pow(1.e-9 / grids_[0][i], 6);
+        }
+      table_kind_ = KMC_TABLE_2D;
+      return;
+    }
+    if (rt == "davoody") {
+      if (!j_.has("rate table directory"))
+        throw std::invalid_argument("rate type davoody needs \"rate table directory\" (a table saved by the reference)");
+      read_reference_table(expand_home(j_["rate table directory"].as_string()));
+      return;
+    }
+    throw std::invalid_argument("rate type must be one of the following: \"davoody\", \"forster\", \"wong\", \"forster2d\"");
+  }
+  // scat_table.*.dat written by scattering_struct::save (scattering_struct.h:56-94)
+  void read_reference_table(const std::string& dir) {
+    auto col = [&](const char* name) {
+      std::ifstream f(fs::path(dir) / (std::string("scat_table.") + name + ".dat"));
+      if (!f) throw std::runtime_error(std::string("missing scat_table.") + name + ".dat");
+      std::vector<double> v;
+      double x;
+      while (f >> x) v.push_back(x);
+      return v;
+    };
+    grids_ = {col("theta"), col("z_shift"), col("axis_shift_1"), col("axis_shift_2")};
+    std::ifstream f(fs::path(dir) / "scat_table.rates.dat");
+    std::string line;
+    for (int i = 0; i < 4 && std::getline(f, line); ++i) {
+    }
+    rates_.clear();
+    double x;
+    while (f >> x) rates_.push_back(x);
+    if (rates_.size() != grids_[0].size() * grids_[1].size() * grids_[2].size() * grids_[3].size())
+      throw std::runtime_error("scat_table.rates.dat does not match its grids");
+    table_kind_ = KMC_TABLE_4D;
+  }
+
+  jl::Value j_;
+  std::string out_dir_, in_dir_;
+  kmc_ctx* ctx_ = nullptr;
+  double time_ = 0, max_time_ = 0, r_max_ = 0, velocity_ = 0;
+  int n_sections_ = 5;
+  int64_t n_particles_ = 0, steps_ = 0;
+  int table_kind_ = KMC_TABLE_4D;
+  std::vector<std::vector<double>> grids_;
+  std::vector<double> rates_, pos_, orient_;
+  std::vector<int32_t> left_, right_;
+  kmc_nbr_stats nbr_{};
+  std::FILE* msd_ = nullptr;
+};
+
+}  // namespace cntkmc

@@ -8,11 +8,12 @@ one project-defined log and acos, written from the mathematics:
 
 * log: table-driven method of P. T. P. Tang, "Table-driven implementation of the
   logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990.
-  x = 2^k z with z in [a, 2a), a = 0.701171875; z falls into one of 128 intervals
-  (equal width in the bit pattern), each with a reciprocal c_i of its midpoint.
-  log x = k ln2 - log c_i + log1p(z c_i - 1), log1p by its Taylor series
-  r - r^2/2 + ... - r^8/8.  The interval holding 1.0 has c = 1 exactly, so
-  the result keeps full relative accuracy near x = 1.
+  x = 2^k z with z in [a, 2a), a ~ 0.7012; z falls into one of 1024 intervals
+  (equal width in the bit pattern), each with a reciprocal c_i of its midpoint, so that
+  |r| = |z c_i - 1| <= 2^-11.  log x = k ln2 - log c_i + log1p(r), log1p by its Taylor
+  series r - r^2/2 + r^3/3 - r^4/4 + r^5/5 (the first omitted term is below 2^-55 |r|).
+  The interval holding 1.0 has c = 1 exactly, so the result keeps full relative
+  accuracy near x = 1.
 * acos: acos(c) = pi/2 - asin(c) for |c| <= 1/2, 2 asin(sqrt((1-c)/2)) above,
   pi - 2 asin(sqrt((1+c)/2)) below; asin by its Taylor series
   x + sum_n (2n)!/(4^n (n!)^2 (2n+1)) x^(2n+1), 24 terms (|x| <= 1/2).
@@ -27,12 +28,12 @@ import mpmath
 
 mpmath.mp.prec = 200
 
-LOG_TABLE_BITS = 7
+LOG_TABLE_BITS = 10
 LOG_N = 1 << LOG_TABLE_BITS
 ONE_BITS = 0x3FF0000000000000
 STEP = 1 << (52 - LOG_TABLE_BITS)
-CENTER_INDEX = 76
-LOG_OFF = ONE_BITS - STEP // 2 - CENTER_INDEX * STEP  # 0x3FE6700000000000 = 0.701171875
+CENTER_INDEX = 76 * 8 + 4  # the interval that holds 1.0 in its middle
+LOG_OFF = ONE_BITS - STEP // 2 - CENTER_INDEX * STEP  # bit pattern of a
 ASIN_TERMS = 24
 
 
@@ -82,7 +83,7 @@ def main():
     for n in range(1, ASIN_TERMS + 1):
         a = mpmath.factorial(2 * n) / (mpmath.mpf(4) ** n * mpmath.factorial(n) ** 2 * (2 * n + 1))
         asin_c.append(rn(a))
-    log1p_c = [rn(mpmath.mpf((-1) ** (j + 1)) / j) for j in range(2, 9)]  # -1/2, 1/3, ..., -1/8
+    log1p_c = [rn(mpmath.mpf((-1) ** (j + 1)) / j) for j in range(2, 6)]  # -1/2, 1/3, -1/4, 1/5
     invc, lhi, llo = log_tables()
 
     out = []
@@ -100,8 +101,8 @@ def main():
     out.append(f"static const double ORC_PIO2_LO = {pio2_lo.hex()};")
     out.append(f"static const double ORC_PI_HI = {pi_hi.hex()};")
     out.append(f"static const double ORC_PI_LO = {pi_lo.hex()};")
-    out.append("/* log1p(r) = r + r^2 * P(r), P(r) = c[0] + c[1] r + ... + c[6] r^6 */")
-    out.append("static const double ORC_LOG1P_C[7] = {" + ", ".join(c.hex() for c in log1p_c) + "};")
+    out.append("/* log1p(r) = r + r^2 * P(r), P(r) = c[0] + c[1] r + c[2] r^2 + c[3] r^3 */")
+    out.append("static const double ORC_LOG1P_C[4] = {" + ", ".join(c.hex() for c in log1p_c) + "};")
     out.append(f"/* asin(x) = x + x z Q(z), z = x^2, Q(z) = a[0] + a[1] z + ... + a[{ASIN_TERMS - 1}] z^{ASIN_TERMS - 1} */")
     out.append(f"static const double ORC_ASIN_C[{ASIN_TERMS}] = {{")
     for c in asin_c:

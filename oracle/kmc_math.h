@@ -118,10 +118,7 @@ static inline double orc_log(double x) {
   double kf = (double)k;
   double r = fma(z, invc, -1.0);
   double t1 = fma(kf, ORC_LN2_HI, lhi); /* exact: both terms are multiples of 2^-42 below 2^11 */
-  double p = ORC_LOG1P_C[6];
-  p = fma(p, r, ORC_LOG1P_C[5]);
-  p = fma(p, r, ORC_LOG1P_C[4]);
-  p = fma(p, r, ORC_LOG1P_C[3]);
+  double p = ORC_LOG1P_C[3];
   p = fma(p, r, ORC_LOG1P_C[2]);
   p = fma(p, r, ORC_LOG1P_C[1]);
   p = fma(p, r, ORC_LOG1P_C[0]);

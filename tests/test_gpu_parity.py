@@ -174,30 +174,45 @@ def test_batched_films_equal_single_films():
     b.close()
 
 
-def test_isolated_sites_and_far_tube():
-    # a tube far from the rest: its sites have no neighbours inside the cutoff (empty lists;
-    # undefined in the reference, defined here as "stay, fly along the tube")
-    f = F.straight_tubes(6, 20.0, box_nm=(30, 30, 4), seed=8)
-    far = F.straight_tubes(1, 5.0, box_nm=(1, 1, 1), seed=9)
-    n0 = f.n_sites
-    pos = np.vstack([f.pos_m(), (far.pos_nm + 500.0) * 1e-9])
-    ori = np.vstack([f.orient, far.orient])
-    lk = np.concatenate([f.left, np.where(far.left >= 0, far.left + n0, -1)]).astype(np.int32)
-    rk = np.concatenate([f.right, np.where(far.right >= 0, far.right + n0, -1)]).astype(np.int32)
-    tab = tables.forster_2d(1e15)
+def isolated_film():
+    """Tube A: sites at x = 0, 1, 2, 7, 12 nm (the last two have no neighbour within 3 nm but keep
+    their tube links); tube B: x = 0..4 nm at y = 1.5 nm; three single sites far away (no links,
+    no neighbours).  Empty neighbour lists are undefined behaviour in the reference; here an
+    exciton there stays (update_state returns the site) and keeps flying along its tube."""
+    xa = [0.0, 1.0, 2.0, 7.0, 12.0]
+    pos = [[x, 0.0, 0.0] for x in xa] + [[x, 1.5, 0.0] for x in range(5)] + [[100.0 + 20 * k, 50.0, 0.0] for k in range(3)]
+    n = len(pos)
+    left = np.full(n, -1, np.int32)
+    right = np.full(n, -1, np.int32)
+    for a, b in ((0, 5), (5, 10)):
+        for i in range(a, b):
+            left[i] = i - 1 if i > a else -1
+            right[i] = i + 1 if i + 1 < b else -1
+    ori = np.tile([1.0, 0.0, 0.0], (n, 1))
+    return np.asarray(pos) * 1e-9, ori, left, right
+
+
+def test_isolated_sites_and_empty_lists():
+    pos, ori, lk, rk = isolated_film()
+    tab = tables.forster_2d(1e13)  # slow rates: dwell times longer than the 5 nm link flight
     sim = O.Sim(pos, ori, lk, rk, tab, 3e-9, 2e5)
+    sim.set_trace(32, 1 << 16)
     sim.create_excitons(1, 0, 300, 5)
-    om = sim.step(1e-13, 5)
+    om = sim.step(1e-13, 6)
+    assert sim.total_crossings() > 0
     for prec in PRECISIONS:
         e = E.Engine(0)
         e.load_arrays(np.array([0, len(lk)], np.int64), pos, ori, lk, rk)
         e.set_table(tab)
         st = e.build(3e-9)
-        assert st["isolated"] >= 5
+        assert st["isolated"] == 5
+        e.set_trace(32, 1 << 16)
         e.init_excitons(300, 5, L.KMC_INJECT_UNIFORM)
-        e.run(5, 1e-13, 2e5, prec)
+        e.run(6, 1e-13, 2e5, prec)
         assert_states_equal(e.excitons(), sim.excitons())
-        assert_msd_close(e.msd(0, 5), om)
+        assert_msd_close(e.msd(0, 6), om)
+        for i in range(32):
+            assert np.array_equal(e.trace(i)[0], sim.trace(i)[0])
         e.close()
 
 
