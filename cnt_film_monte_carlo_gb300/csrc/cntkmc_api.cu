@@ -71,7 +71,11 @@ struct kmc_ctx {
   DevBuf<int64_t> d_cell_of, d_cell_start, d_cell_cursor, d_rowptr, d_scan;
   DevBuf<int32_t> d_cell_members, d_col;
   DevBuf<double> d_cum, d_total, d_inv_total;
-  DevBuf<float> d_cumn;
+  DevBuf<int64_t> d_blkptr;
+  DevBuf<kmc::RowBlock> d_blocks;
+  DevBuf<float> d_blast;
+  DevBuf<double> d_cump;
+  int64_t nblk = 0;
   DevBuf<kmc::SiteRec> d_rec;
   DevBuf<double2> d_lt64;
   double lt_v = -1;
@@ -91,7 +95,8 @@ struct kmc_ctx {
   DevBuf<int64_t> d_trace_cnt;
   // misc
   DevBuf<kmc::LogTab> d_logtab;
-  DevBuf<unsigned long long> d_counters, d_stats;
+  DevBuf<unsigned long long> d_counters, d_stats, d_queue;
+  int n_sms = 0;
   DevBuf<int32_t> d_err;
   int64_t hop_cap = 100000000LL;
   int steps_per_launch = 32;
@@ -143,10 +148,12 @@ kmc_ctx* kmc_create(int device, int* status) {
   }
   kmc_ctx* c = new kmc_ctx();
   c->device = device;
+  c->n_sms = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       upload(c->d_logtab, reinterpret_cast<const kmc::LogTab*>(kLogTab), 1, c->stream) != cudaSuccess ||
       c->d_counters.alloc(4) != cudaSuccess || c->d_stats.alloc(4) != cudaSuccess || c->d_err.alloc(1) != cudaSuccess ||
+      c->d_queue.alloc(1) != cudaSuccess ||
       cudaMemsetAsync(c->d_counters.p, 0, 4 * sizeof(unsigned long long), c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess) {
@@ -173,7 +180,10 @@ void kmc_destroy(kmc_ctx* c) {
     b->release();
   c->d_pos4.release();
   c->d_films.release();
-  c->d_cumn.release();
+  c->d_blkptr.release();
+  c->d_blocks.release();
+  c->d_blast.release();
+  c->d_cump.release();
   c->d_rec.release();
   c->d_lt64.release();
   c->d_e_flags.release();
@@ -182,6 +192,7 @@ void kmc_destroy(kmc_ctx* c) {
   c->d_logtab.release();
   c->d_counters.release();
   c->d_stats.release();
+  c->d_queue.release();
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -326,30 +337,43 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, kmc::launch_cell_fill(a, c->stream));
   CK(c, kmc::launch_nbr_count(a, c->stream));
   CK(c, kmc::exclusive_scan_i64(c->d_rowptr.p, n + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
-  std::vector<int64_t> nnz0(c->n_films + 1);
-  for (int32_t i = 0; i <= c->n_films; ++i)
+  CK(c, c->d_blkptr.alloc(n + 1));
+  a.blkptr = c->d_blkptr.p;
+  CK(c, kmc::launch_blk_counts(a, c->stream));
+  CK(c, kmc::exclusive_scan_i64(c->d_blkptr.p, n + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
+  std::vector<int64_t> nnz0(c->n_films + 1), blk0(c->n_films + 1);
+  for (int32_t i = 0; i <= c->n_films; ++i) {
     CK(c, cudaMemcpyAsync(&nnz0[i], c->d_rowptr.p + c->film_off[i], sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaMemcpyAsync(&blk0[i], c->d_blkptr.p + c->film_off[i], sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  }
   CK(c, cudaStreamSynchronize(c->stream));
   int32_t herr = 0;
   CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
   if (herr) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: a site lies outside its film's cell grid (non-finite position?)");
   c->nnz = nnz0[c->n_films];
+  c->nblk = blk0[c->n_films];
   for (int32_t i = 0; i < c->n_films; ++i) {
     c->films[i].nnz0 = nnz0[i];
     c->films[i].nnz = nnz0[i + 1] - nnz0[i];
+    c->films[i].blk0 = blk0[i];
+    c->films[i].nblk = blk0[i + 1] - blk0[i];
     if (c->films[i].nnz >= (1LL << 32)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: film %d has >= 2^32 neighbour entries", i);
   }
   CK(c, cudaMemcpyAsync(c->d_films.p, c->films.data(), c->films.size() * sizeof(FilmDev), cudaMemcpyHostToDevice, c->stream));
   CK(c, c->d_col.alloc(c->nnz));
   CK(c, c->d_cum.alloc(c->nnz));
-  CK(c, c->d_cumn.alloc(c->nnz));
+  CK(c, c->d_blocks.alloc(c->nblk));
+  CK(c, c->d_blast.alloc(c->nblk));
+  CK(c, c->d_cump.alloc(c->nblk * 8));
   CK(c, c->d_total.alloc(n));
   CK(c, c->d_inv_total.alloc(n));
   CK(c, c->d_rec.alloc(n));
   CK(c, c->d_lt64.alloc(n));
   a.col = c->d_col.p;
   a.cum = c->d_cum.p;
-  a.cumn = c->d_cumn.p;
+  a.blocks = c->d_blocks.p;
+  a.blast = c->d_blast.p;
+  a.cump = c->d_cump.p;
   a.total = c->d_total.p;
   a.inv_total = c->d_inv_total.p;
   a.rec = c->d_rec.p;
@@ -530,7 +554,9 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   a.total = c->d_total.p;
   a.inv_total = c->d_inv_total.p;
   a.rec = c->d_rec.p;
-  a.cumn = c->d_cumn.p;
+  a.blocks = c->d_blocks.p;
+  a.blast = c->d_blast.p;
+  a.cump = c->d_cump.p;
   a.lt64 = c->d_lt64.p;
   a.films = c->d_films.p;
   a.warp_film = c->d_warp_film.p;
@@ -560,13 +586,16 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
   CK(c, cudaEventRecord(c->ev0, c->stream));
   int launches = 0;
+  const int single_film = c->n_films == 1 ? 1 : 0;
+  const int grid_blocks =
+      c->n_sms * kmc::hop_mixed_blocks_per_sm(c->block, std::min<int64_t>(c->steps_per_launch, n_steps), single_film);
   for (int64_t s = 0; s < n_steps; s += c->steps_per_launch) {
     int64_t k = std::min<int64_t>(c->steps_per_launch, n_steps - s);
     a.step0 = c->steps_done + s;
     if (precision == KMC_PREC_FP64)
       CK(c, kmc::launch_hop_fp64(a, k, c->block, c->stream));
     else
-      CK(c, kmc::launch_hop_mixed(a, k, c->block, c->stream));
+      CK(c, kmc::launch_hop_mixed(a, k, c->block, grid_blocks, single_film, c->d_queue.p, c->stream));
     ++launches;
   }
   CK(c, cudaEventRecord(c->ev1, c->stream));

@@ -13,6 +13,7 @@ struct FilmDev {
   int64_t site0, n_sites;   // film's sites in the global site arrays
   int64_t cell0, n_cells;   // film's cells in the global cell arrays
   int64_t nnz0, nnz;        // film's neighbour entries in the global CSR arrays
+  int64_t blk0, nblk;       // film's 8-entry blocks in the blocked (mixed-precision) row arrays
   int32_t nx, ny, nz, mode; // cell grid; injection mode
   double mn[3];             // domain minimum (cell origin)
   double r;                 // cell side = max hopping radius
@@ -22,16 +23,27 @@ struct FilmDev {
   int64_t slot0, n_exc;     // exciton slots (padded to whole warps)
 };
 
-// Per-site record read once per hop by the mixed kernel (one 32-byte sector).
-struct __align__(32) SiteRec {
+// Per-site record read once per hop by the mixed kernel: one 64-byte line.  coarse[] is the
+// first level of the row search: the FP32 normalised cumulative rate at the end of each group
+// of G blocks (G = 1 for rows of up to 64 entries, ceil(blocks/8) up to 512 entries), +inf
+// past the row end.
+struct __align__(64) SiteRec {
   double inv_total;   // 1 / total rate (inf for an empty list)
-  uint32_t row;       // film-local offset of the neighbour row
-  uint32_t len_flags; // row length (low 24 bits) | flags << 24
+  uint32_t blk;       // film-local index of the row's first 8-entry block
+  uint32_t len_flags; // row length (low 24 bits) | flags
   int32_t left, right;// global site ids or -1
   uint32_t lt_hi_l;   // high 32 bits of the FP64 link time to the left / right neighbour
   uint32_t lt_hi_r;
+  float coarse[8];
+};
+// One 64-byte block of a neighbour row: 8 FP32 values of cum/total and the 8 neighbour ids
+// (global site ids); entries past the row end hold +inf and -1.
+struct __align__(64) RowBlock {
+  float c[8];
+  int32_t col[8];
 };
 constexpr uint32_t kRecExact = 1u << 24;  // row resolved in FP64 only (non-finite/zero total, negative rate)
+constexpr uint32_t kRecLong = 1u << 25;   // row longer than 512 entries: FP32 bisection over the blocks
 constexpr uint32_t kLenMask = (1u << 24) - 1;
 
 struct TableDev {
@@ -57,7 +69,9 @@ struct HopArgs {
   const double* total;
   const double* inv_total;
   const SiteRec* rec;
-  const float* cumn;      // cum / total in FP32
+  const RowBlock* blocks; // blocked rows (global block index)
+  const float* blast;     // last FP32 value of every block (second search level of long rows)
+  const double* cump;     // FP64 cumulative rates in the blocked layout (8 per block)
   const double2* lt64;    // exact link times (left, right)
   // films and excitons
   const FilmDev* films;
@@ -104,7 +118,10 @@ struct BuildArgs {
   double* cum;
   double* total;
   double* inv_total;
-  float* cumn;
+  int64_t* blkptr;         // [n + 1] first block of each row (global)
+  RowBlock* blocks;
+  float* blast;
+  double* cump;
   SiteRec* rec;
   const int32_t* left;
   const int32_t* right;
@@ -117,13 +134,16 @@ cudaError_t launch_cell_ids(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_cell_fill(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_nbr_count(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_nbr_fill(const BuildArgs& a, cudaStream_t s);
+cudaError_t launch_blk_counts(const BuildArgs& a, cudaStream_t s);
 cudaError_t exclusive_scan_i64(int64_t* data, int64_t n, int64_t* scratch, int64_t scratch_len, cudaStream_t s);
 int64_t scan_scratch_len(int64_t n);
 cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, const int32_t* right, SiteRec* rec,
                               double2* lt64, int64_t n, double v, cudaStream_t s);
 cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s);
 cudaError_t launch_hop_fp64(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
-cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
+cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, int grid_blocks, int single_film,
+                             unsigned long long* queue, cudaStream_t s);
+int hop_mixed_blocks_per_sm(int block, int64_t n_steps, int single_film);
 cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,
                               cudaStream_t s);

@@ -187,16 +187,60 @@ __global__ void k_nbr_fill(BuildArgs a) {
   a.inv_total[s] = inv;
   bool exact = negative || !(tot > 0.0) || !(tot < __longlong_as_double(0x7FF0000000000000ll));
   if (exact && k > 0) atomicAdd(&a.stats[2], 1ull);
-  for (int64_t i = 0; i < k; ++i) a.cumn[b + i] = exact ? 0.0f : (float)(a.cum[b + i] / tot);
+  // blocked copy of the row for the mixed kernel: 8 entries per 64-byte block
+  const float kInf = __int_as_float(0x7f800000);
+  const int64_t bo = a.blkptr[s];
+  const int64_t nb = (k + 7) / 8;
+  for (int64_t j = 0; j < nb; ++j) {
+    RowBlock blk;
+    for (int i = 0; i < 8; ++i) {
+      int64_t q = 8 * j + i;
+      if (q < k) {
+        double cv = a.cum[b + q];
+        blk.c[i] = exact ? 0.0f : (float)(cv / tot);
+        blk.col[i] = a.col[b + q];
+        a.cump[(bo + j) * 8 + i] = cv;
+      } else {
+        blk.c[i] = kInf;
+        blk.col[i] = -1;
+        a.cump[(bo + j) * 8 + i] = __longlong_as_double(0x7FF0000000000000ll);
+      }
+    }
+    a.blocks[bo + j] = blk;
+    int64_t last = min(8 * j + 7, k - 1);
+    a.blast[bo + j] = exact ? 0.0f : (float)(a.cum[b + last] / tot);
+  }
   SiteRec r;
   r.inv_total = inv;
-  r.row = (uint32_t)(b - f.nnz0);
-  r.len_flags = (uint32_t)k | (exact ? kRecExact : 0u);
+  r.blk = (uint32_t)(bo - f.blk0);
+  r.len_flags = (uint32_t)k | (exact ? kRecExact : 0u) | (nb > 64 ? kRecLong : 0u);
   r.left = a.left[s];
   r.right = a.right[s];
   r.lt_hi_l = 0;
   r.lt_hi_r = 0;
+  const int64_t G = nb <= 8 ? 1 : (nb + 7) / 8;
+  for (int i = 0; i < 8; ++i) {
+    if (i * G < nb && !exact) {
+      int64_t last = min(8 * G * (i + 1) - 1, k - 1);
+      r.coarse[i] = (float)(a.cum[b + last] / tot);
+    } else {
+      r.coarse[i] = kInf;
+    }
+  }
   a.rec[s] = r;
+}
+
+// blocks per row, from the row pointers: blkptr[s] = ceil(len / 8) (scanned afterwards)
+__global__ void k_blk_counts(BuildArgs a) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s > a.n_sites) return;
+  a.blkptr[s] = s < a.n_sites ? (a.rowptr[s + 1] - a.rowptr[s] + 7) / 8 : 0;
+}
+
+cudaError_t launch_blk_counts(const BuildArgs& a, cudaStream_t s) {
+  int64_t nb = (a.n_sites + 1 + 255) / 256;
+  k_blk_counts<<<(unsigned)nb, 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_nbr_count(const BuildArgs& a, cudaStream_t s) {
@@ -612,47 +656,63 @@ __device__ __forceinline__ bool dwell_fits(double ff, double rem) {
   return __double_as_longlong(ff) <= __double_as_longlong(rem);
 }
 
-// Each lane advances its exciton through all n_steps steps of the launch on its own (a lane
-// whose step ends early starts its next step instead of waiting for the warp); the MSD sums of
-// a warp's lanes go to per-warp shared-memory bins and are added to global memory once at the end.
-__global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
-  extern __shared__ double s_bins[];  // [warps in block][n_steps][3]
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  double* bins = s_bins + (size_t)wib * n_steps * 3;
-  for (int64_t i = lane; i < n_steps * 3; i += 32) bins[i] = 0.0;
-  __syncwarp();
-  int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (slot >= a.n_slots) return;  // whole warps (n_slots is a multiple of 32)
-  int32_t film = a.warp_film[slot >> 5];
-  const FilmDev& f = a.films[film];
-  const float* __restrict__ cumn = a.cumn + f.nnz0;
-  const int32_t* __restrict__ col = a.col + f.nnz0;
-  Exciton e;
-  load_exciton(a, slot, e);
-  int64_t local = slot - f.slot0;
-  e.trace_i = (film == 0 && local < a.n_trace) ? local : -1;
-  if (e.active) e.g.init(f.seed, (uint64_t)local, a.e_draws[slot]);
-  uint64_t exact = 0;
-  const float lo_m = 1.0f - 0x1p-20f, hi_m = 1.0f + 0x1p-20f;
-  int64_t s = 0;
-  double ox = 0, oy = 0, oz = 0, rem = a.dt;
-  int64_t hs = 0;
-  SiteRec rr;
-  if (e.active) {
-    if (e.at_site) {
-      double4_32a p = a.pos4[e.site];
-      e.px = p.x;
-      e.py = p.y;
-      e.pz = p.z;
-    }
-    ox = e.px;
-    oy = e.py;
-    oz = e.pz;
-    rr = a.rec[e.site];
-  } else {
-    s = n_steps;
+// Persistent work queue: the grid holds as many threads as the GPU keeps resident; each lane
+// takes the next exciton slot from a global counter (warp-aggregated atomics), advances it
+// through all n_steps steps of the launch on its own, stores it and takes the next one, so no
+// lane waits for another lane's exciton.  MSD sums of a single-film run go to block-shared bins
+// (added to global memory once per block); batched films add to global memory directly.
+__global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps, unsigned long long* queue,
+                                                   int single_film) {
+  extern __shared__ double s_bins[];  // [n_steps][3]
+  const int lane = threadIdx.x & 31;
+  if (single_film) {
+    for (int64_t i = threadIdx.x; i < n_steps * 3; i += blockDim.x) s_bins[i] = 0.0;
+    __syncthreads();
   }
-  while (s < n_steps) {
+  const float lo_m = 1.0f - 0x1p-20f, hi_m = 1.0f + 0x1p-20f;
+  uint64_t exact = 0, lane_hops = 0, lane_cross = 0;
+  Exciton e;
+  e.active = false;
+  int64_t cur = -1, s = 0, hs = 0;
+  int32_t film = 0;
+  const FilmDev* fp = a.films;
+  double ox = 0, oy = 0, oz = 0, rem = 0;
+  SiteRec rr;
+  for (;;) {
+    if (cur < 0) {
+      // ---- take the next exciton slot
+      unsigned m = __activemask();
+      int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(m));
+      base = __shfl_sync(m, base, leader);
+      cur = (int64_t)base + __popc(m & ((1u << lane) - 1));
+      if (cur >= a.n_slots) break;
+      film = a.warp_film[cur >> 5];
+      fp = a.films + film;
+      load_exciton(a, cur, e);
+      if (!e.active) {
+        cur = -1;
+        continue;
+      }
+      int64_t local = cur - fp->slot0;
+      e.trace_i = (film == 0 && local < a.n_trace) ? local : -1;
+      e.g.init(fp->seed, (uint64_t)local, a.e_draws[cur]);
+      if (e.at_site) {
+        double4_32a p = a.pos4[e.site];
+        e.px = p.x;
+        e.py = p.y;
+        e.pz = p.z;
+      }
+      ox = e.px;
+      oy = e.py;
+      oz = e.pz;
+      rem = a.dt;
+      s = 0;
+      hs = 0;
+      rr = a.rec[e.site];
+    }
+    const FilmDev& f = *fp;
     if (dwell_fits(e.ff, rem)) {
       // ------------------------------------------------ one event of particle::step (particle.cpp:71-84)
       rem -= e.ff;
@@ -716,31 +776,82 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
       int32_t ns = e.site;
       if (n > 0) {
         uint32_t r = e.g.next();
-        const uint32_t row = rr.row;
+        const RowBlock* __restrict__ rb = a.blocks + f.blk0 + rr.blk;
         bool resolved = false;
-        if (!(rr.len_flags & kRecExact)) {
+        if (!(rr.len_flags & (kRecExact | kRecLong))) {
+          // two- or three-level search for the first FP32 value > u (count of values <= u)
+          float u = __uint2float_rn(r) * (1.0f / 2147483647.0f);
+          int j1 = 0;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) j1 += (rr.coarse[i] <= u);
+          float prev = rr.coarse[0];
+#pragma unroll
+          for (int i = 1; i < 8; ++i)
+            if (j1 == i + 1) prev = rr.coarse[i];  // value before the group: coarse[j1 - 1]
+          uint32_t nb = (n + 7) >> 3;
+          uint32_t bsel;
+          if (nb <= 8) {
+            bsel = (uint32_t)j1;
+          } else {
+            uint32_t G = (nb + 7) >> 3, g0 = (uint32_t)j1 * G;
+            const float* __restrict__ bl = a.blast + f.blk0 + rr.blk + g0;
+            float v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = ((uint32_t)i < G && g0 + i < nb) ? __ldg(bl + i) : __int_as_float(0x7f800000);
+            int j2 = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) j2 += (v[i] <= u);
+#pragma unroll
+            for (int i = 0; i < 7; ++i)
+              if (j2 == i + 1) prev = v[i];
+            bsel = g0 + (uint32_t)j2;
+          }
+          const float4* bp = reinterpret_cast<const float4*>(rb + bsel);
+          float4 c0 = __ldg(bp), c1 = __ldg(bp + 1);
+          int4 k0 = __ldg(reinterpret_cast<const int4*>(bp + 2)), k1 = __ldg(reinterpret_cast<const int4*>(bp + 3));
+          float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+          int32_t cl[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+          int kk = 0;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) kk += (c[i] <= u);
+          float ck = c[0], ckm = prev;
+          int32_t colk = cl[0];
+#pragma unroll
+          for (int i = 1; i < 8; ++i)
+            if (kk == i) {
+              ck = c[i];
+              ckm = c[i - 1];
+              colk = cl[i];
+            }
+          uint32_t R = bsel * 8 + (uint32_t)kk;
+          if ((R == 0 || ckm < u * lo_m) && (R == n - 1 || ck > u * hi_m)) {
+            ns = colk;
+            resolved = true;
+          }
+        } else if (rr.len_flags & kRecLong && !(rr.len_flags & kRecExact)) {
+          // rows beyond 512 entries: the reference bisection on the blocked FP32 values
           float u = __uint2float_rn(r) * (1.0f / 2147483647.0f);
           unsigned left = (unsigned)-1, right = n - 1;
           float cl = 0.f, cr = 0.f;
           while (left + 1 < right) {
             unsigned mid = (left + right) / 2;
-            float c = __ldg(cumn + row + mid);
-            if (c <= u) {
+            float cv = __ldg(&rb[mid >> 3].c[mid & 7]);
+            if (cv <= u) {
               left = mid;
-              cl = c;
+              cl = cv;
             } else {
               right = mid;
-              cr = c;
+              cr = cv;
             }
           }
           if ((left == (unsigned)-1 || cl < u * lo_m) && (right == n - 1 || cr > u * hi_m)) {
-            ns = __ldg(col + row + right);
+            ns = __ldg(&rb[right >> 3].col[right & 7]);
             resolved = true;
           }
         }
-        if (!resolved) {  // exact FP64 selection on the site's FP64 row
+        if (!resolved) {  // exact FP64 selection on the site's FP64 row (update_state, scatterer.cpp:17-30)
           ++exact;
-          const double* cum = a.cum + f.nnz0 + row;
+          const double* cum = a.cump + (f.blk0 + rr.blk) * 8;
           double dice = a.total[e.site] * (double)r / (double)kRandMax;
           unsigned left = (unsigned)-1, right = n - 1;
           while (left + 1 < right) {
@@ -750,7 +861,7 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
             else
               right = mid;
           }
-          ns = col[row + right];
+          ns = rb[right >> 3].col[right & 7];
         }
       }
       e.hops++;
@@ -764,9 +875,10 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
       while ((r = e.g.next()) == 0) {
       }
       e.ff = -rr.inv_total * kmc_log_unit(u_from_rand(r), a.logtab);
-      if (++hs > a.hop_cap) {
+      if (++hs > a.hop_cap) {  // leave this exciton where it is and report
         atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
-        break;
+        store_exciton(a, cur, e);
+        cur = -1;
       }
     } else {
       // ------------------------------------------------ end of step s: fly(rem), ff -= rem, kubo_step tail
@@ -783,10 +895,24 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
       e.dy += e.py - oy;
       e.dz += e.pz - oz;
       maybe_reinject(a, f, e);
-      atomicAdd(&bins[s * 3 + 0], e.dx * e.dx);
-      atomicAdd(&bins[s * 3 + 1], e.dy * e.dy);
-      atomicAdd(&bins[s * 3 + 2], e.dz * e.dz);
+      if (single_film) {
+        atomicAdd(&s_bins[s * 3 + 0], e.dx * e.dx);
+        atomicAdd(&s_bins[s * 3 + 1], e.dy * e.dy);
+        atomicAdd(&s_bins[s * 3 + 2], e.dz * e.dz);
+      } else {
+        double* m = a.msd + ((int64_t)film * a.msd_cap + a.step0 + s) * 3;
+        atomicAdd(m, e.dx * e.dx);
+        atomicAdd(m + 1, e.dy * e.dy);
+        atomicAdd(m + 2, e.dz * e.dz);
+      }
       ++s;
+      if (s == n_steps) {
+        store_exciton(a, cur, e);
+        lane_hops += e.hops;
+        lane_cross += e.crossings;
+        cur = -1;
+        continue;
+      }
       ox = e.px;
       oy = e.py;
       oz = e.pz;
@@ -795,22 +921,37 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps) {
       rr = a.rec[e.site];
     }
   }
+  if (single_film) {
+    __syncthreads();
+    double* m = a.msd + a.step0 * 3;
+    for (int64_t i = threadIdx.x; i < n_steps * 3; i += blockDim.x) atomicAdd(m + i, s_bins[i]);
+  }
+  e.hops = lane_hops;
+  e.crossings = lane_cross;
   __syncwarp();
-  double* m = a.msd + ((int64_t)film * a.msd_cap + a.step0) * 3;
-  for (int64_t i = lane; i < n_steps * 3; i += 32) atomicAdd(m + i, bins[i]);
-  store_exciton(a, slot, e);
   flush_counters(a, e, exact);
 }
 
-cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s) {
-  int64_t nb = (a.n_slots + block - 1) / block;
-  size_t smem = (size_t)(block / 32) * n_steps * 3 * sizeof(double);
+cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, int grid_blocks, int single_film,
+                             unsigned long long* queue, cudaStream_t s) {
+  size_t smem = single_film ? (size_t)n_steps * 3 * sizeof(double) : 0;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_hop_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
-  if (nb) k_hop_mixed<<<(unsigned)nb, block, smem, s>>>(a, n_steps);
+  int64_t need = (a.n_slots + block - 1) / block;
+  int64_t nb = need < grid_blocks ? need : grid_blocks;
+  cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  if (nb) k_hop_mixed<<<(unsigned)nb, block, smem, s>>>(a, n_steps, queue, single_film);
   return cudaGetLastError();
+}
+
+int hop_mixed_blocks_per_sm(int block, int64_t n_steps, int single_film) {
+  int nb = 0;
+  size_t smem = single_film ? (size_t)n_steps * 3 * sizeof(double) : 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_hop_mixed, block, smem) != cudaSuccess) return 1;
+  return nb > 0 ? nb : 1;
 }
 
 // ============================================================================ self-checks

@@ -267,3 +267,24 @@ def test_launch_shape_does_not_change_results():
         e.close()
     for o in out[1:]:
         assert_states_equal(o, out[0])
+
+
+@pytest.mark.parametrize("box,n_tubes,r_max,kmin", [((60, 60, 4), 40, 12e-9, 65), ((40, 40, 4), 60, 20e-9, 513)])
+def test_long_rows_match_oracle(box, n_tubes, r_max, kmin):
+    # neighbour rows beyond 64 entries (three-level search) and beyond 512 (FP32 bisection)
+    f = F.straight_tubes(n_tubes, 40.0, box_nm=box, seed=3)
+    tab = tables.forster_2d(1e15)
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, r_max, 2e5, n_threads=4)
+    sim.create_excitons(1, 0, 400, 9)
+    om = sim.step(2e-14, 4)
+    for prec in PRECISIONS:
+        e = E.Engine(0)
+        e.load_films(f)
+        e.set_table(tab)
+        st = e.build(r_max)
+        assert st["k_max"] >= kmin
+        e.init_excitons(400, 9, L.KMC_INJECT_UNIFORM)
+        e.run(4, 2e-14, 2e5, prec)
+        assert_states_equal(e.excitons(), sim.excitons())
+        assert_msd_close(e.msd(0, 4), om)
+        e.close()
