@@ -108,13 +108,12 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def bytes_per_hop(k_mean, fp32=True):
-    """Algorithmic bytes of one hop: the destination's 32-byte site record, one 32-byte sector of
-    the neighbour index, and one sector per bisection probe that leaves the previous sector
-    (8 FP32 or 4 FP64 cumulative entries per sector)."""
-    lg = math.ceil(math.log2(max(k_mean, 2.0)))
-    s = max(1, lg - (3 if fp32 else 2))
-    return 32 + 32 + 32 * s
+def bytes_per_hop(k_mean):
+    """Algorithmic bytes of one hop of the mixed kernel: the destination site's 64-byte record
+    (1/total, links, link times, first search level) and the one 64-byte row block holding the
+    chosen entry (8 FP32 cumulative values + 8 neighbour ids); rows of 65-512 entries add the
+    32-byte second level."""
+    return 128 if k_mean <= 64 else 160
 
 
 def cpu_sample(f, tab, target_cpu_s=15.0, threads=None, steps=1):
@@ -281,7 +280,7 @@ def main():
     if rank != 0:
         return
     peak, peak_kind = measured_peak()
-    bph = bytes_per_hop(st["k_mean"], fp32=True)
+    bph = bytes_per_hop(st["k_mean"])
     achieved = hops / dev_s * bph / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "hop_mixed_traffic.json")
@@ -293,7 +292,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32", "data": "synthetic",
-        "config": config(args.n_exc, bins, {"k_mean": st["k_mean"], "nnz": st["nnz"], "hops_timed": hops}),
+        "config": config(args.n_exc, bins, {"k_mean": st["k_mean"], "k_max": st["k_max"], "nnz": st["nnz"], "hops_timed": hops}),
         "fp64_plain_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "d_eff_m2_per_s": d_eff,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -14,6 +14,7 @@
 #include <cstdio>
 
 #include "kmc_internal.h"
+#include "kmc_pair.cuh"
 
 namespace kmc {
 
@@ -83,47 +84,6 @@ cudaError_t launch_cell_fill(const BuildArgs& a, cudaStream_t s) {
 }
 
 // ============================================================================ K2: neighbour + rate CSR
-__device__ __forceinline__ double table_rate(const TableDev& t, double th, double zsh, double a1, double a2,
-                                             double dist) {
-  if (t.kind == 4) {
-    int i0 = index_min_abs(t.grid[0], t.n[0], th);
-    int i1 = index_min_abs(t.grid[1], t.n[1], zsh);
-    int i2 = index_min_abs(t.grid[2], t.n[2], a1);
-    int i3 = index_min_abs(t.grid[3], t.n[3], a2);
-    return t.rate[(((int64_t)i0 * t.n[1] + i1) * t.n[2] + i2) * t.n[3] + i3];
-  }
-  int i0 = index_min_abs(t.grid[0], t.n[0], dist);
-  int i1 = index_min_abs(t.grid[1], t.n[1], th);
-  return t.rate[(int64_t)i0 * t.n[1] + i1];
-}
-
-// Pair rate of find_neighbors (scatterer.cpp:40-68) for a pair already inside the window.
-__device__ __forceinline__ double pair_rate(const TableDev& t, const double4_32a& p1, const double* a1v, const double4_32a& p2,
-                                            const double* a2v, double dR0, double dR1, double dR2, double distance) {
-  double cosT = dot3(a1v[0], a1v[1], a1v[2], a2v[0], a2v[1], a2v[2]);
-  double theta, ash1 = 0, ash2 = 0, zsh = 0;
-  if (t.kind == 2) {
-    double ac = fabs(cosT);
-    theta = ac >= 1.0 ? 0.0 : kmc_acos(ac);
-  } else if (cosT == 1) {
-    ash1 = 0;
-    ash2 = dot3(dR0, dR1, dR2, a1v[0], a1v[1], a1v[2]);
-    theta = 0;
-    double tt = dot3(dR0, dR1, dR2, a1v[0], a1v[1], a1v[2]);
-    zsh = norm3(dR0 - tt * a1v[0], dR1 - tt * a1v[1], dR2 - tt * a1v[2]);
-  } else {
-    theta = kmc_acos(cosT);
-    double y1 = dot3(a1v[0], a1v[1], a1v[2], dR0, dR1, dR2);
-    double y2 = dot3(a2v[0], a2v[1], a2v[2], dR0, dR1, dR2);
-    double sin2 = 1 - cosT * cosT;
-    ash1 = (y1 + y2 * cosT) / sin2;
-    ash2 = (y2 + y1 * cosT) / sin2;
-    zsh = norm3((ash1 * a1v[0] + p1.x) - (ash2 * a2v[0] + p2.x), (ash1 * a1v[1] + p1.y) - (ash2 * a2v[1] + p2.y),
-                (ash1 * a1v[2] + p1.z) - (ash2 * a2v[2] + p2.z));
-  }
-  return table_rate(t, theta, zsh, ash1, ash2, distance);
-}
-
 // Visit the neighbours of site s in find_neighbors order; fn(j, p2, dR, distance) per neighbour.
 template <typename F>
 __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s, F fn) {
@@ -678,7 +638,11 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps, u
   const FilmDev* fp = a.films;
   double ox = 0, oy = 0, oz = 0, rem = 0;
   SiteRec rr;
+  bool alive = true;
   for (;;) {
+    // all 32 lanes meet here once per event, so every event starts with the warp converged
+    if (!__any_sync(0xffffffffu, alive)) break;
+    if (!alive) continue;
     if (cur < 0) {
       // ---- take the next exciton slot
       unsigned m = __activemask();
@@ -687,7 +651,10 @@ __global__ void __launch_bounds__(256) k_hop_mixed(HopArgs a, int64_t n_steps, u
       if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(m));
       base = __shfl_sync(m, base, leader);
       cur = (int64_t)base + __popc(m & ((1u << lane) - 1));
-      if (cur >= a.n_slots) break;
+      if (cur >= a.n_slots) {
+        alive = false;
+        continue;
+      }
       film = a.warp_film[cur >> 5];
       fp = a.films + film;
       load_exciton(a, cur, e);
