@@ -27,6 +27,8 @@ KMC_INJECT_REGION = 0
 KMC_INJECT_UNIFORM = 1
 KMC_PREC_FP64 = 0
 KMC_PREC_MIXED = 1
+KMC_NOALLOC_MAX_SITES = 65536
+KMC_NOALLOC_MAX_CELLS = 65536
 
 PD = C.POINTER(C.c_double)
 PI32 = C.POINTER(C.c_int32)
@@ -82,6 +84,8 @@ SIGNATURES = {
     "kmc_selftest_uniform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, PU64]),
     "kmc_math_probe": (C.c_int, [C.c_void_p, PD, C.c_int64, PD, PD]),
     "kmc_set_launch_config": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "kmc_build_neighbors_noalloc": (C.c_int, [PD, PD, C.c_int64, C.POINTER(kmc_table), C.c_double, PI64, PI32, PD, PD,
+                                              C.c_int64, PI64, C.c_void_p, C.c_char_p, C.c_int64]),
     "kmc_version": (C.c_char_p, []),
 }
 

@@ -173,6 +173,32 @@ int kmc_math_probe(kmc_ctx* ctx, const double* x, int64_t n, double* log_out, do
  * launch (the kernel keeps excitons in registers across the steps of one launch). */
 int kmc_set_launch_config(kmc_ctx* ctx, int32_t block, int32_t steps_per_launch);
 
+/* ---- neighbour lists without device allocation (no counterpart in the reference) ----
+ *
+ * For callers that cannot call cudaMalloc: applications whose device memory is handed out by
+ * their own pool or a pre-reserved arena, or hosts that forbid allocation (which synchronises
+ * the device) while they run.  Builds the neighbour/rate CSR of ONE film exactly as
+ * kmc_build_neighbors does (same order, rates and FP64 cumulative sums), into the caller's
+ * device buffers, and allocates nothing: no cudaMalloc/cudaFree, no allocating library call.
+ *   inputs  (device): pos [n][3] in m, orient [n][3]; table->grid[d] and table->rate are device
+ *                     pointers (same layout as kmc_table);
+ *   outputs (device): rowptr [n+1], col [capacity] (site ids), cum [capacity], total [n];
+ *   *nnz (host) receives the number of neighbour entries; if it exceeds `capacity` the call
+ *   returns KMC_ERR_ARG after writing rowptr, so a caller can size col/cum and call again.
+ *   stream: a cudaStream_t (NULL: the default stream); the call returns after the stream has
+ *   finished its work.  err/err_len: optional buffer for a message.
+ * Limits: n_sites <= KMC_NOALLOC_MAX_SITES and the film's cell grid (cells of side
+ * max_hopping_radius) <= KMC_NOALLOC_MAX_CELLS; larger inputs are rejected with KMC_ERR_ARG.
+ * Intermediate storage is one fixed device array (about 1 MB) that every GPU loading this
+ * library keeps until exit.  The first call on a device looks up that array's address with the
+ * device current; make it before any stream capture.  All calls share the array (each clears
+ * what must start at zero); calls that overlap on the GPU race and must be serialised. */
+#define KMC_NOALLOC_MAX_SITES 65536
+#define KMC_NOALLOC_MAX_CELLS 65536
+int kmc_build_neighbors_noalloc(const double* pos, const double* orient, int64_t n_sites, const kmc_table* table,
+                                double max_hopping_radius, int64_t* rowptr, int32_t* col, double* cum, double* total,
+                                int64_t capacity, int64_t* nnz, void* stream, char* err, int64_t err_len);
+
 /* Library version string. */
 const char* kmc_version(void);
 
