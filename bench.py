@@ -168,6 +168,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--variant", type=int, default=None)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -204,6 +206,9 @@ def main():
     st = e.build(R_MAX)
     e.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
     bins = args.bins_per_step
+    if args.variant is not None:
+        e.set_mixed_variant(args.variant)
+    tune = e.autotune(BIN, VEL, trial_steps=1) if not (args.no_tune or args.variant is not None) else None
     for _ in range(args.warmup):
         e.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
     h0 = e.stats()["hops"]
@@ -265,6 +270,11 @@ def main():
         e3.set_table(tab)
         e3.build(R_MAX)
         e3.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+        if tune:
+            e3.set_mixed_variant(tune["variant"])
+            e3.set_launch_config(128, tune["steps_per_launch"])
+        elif args.variant is not None:
+            e3.set_mixed_variant(args.variant)
         for _ in range(args.steps):
             e3.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
         out = e3.msd(0, args.steps * bins)
@@ -299,6 +309,7 @@ def main():
                      "traffic": traffic, "peak_kind": peak_kind, "bytes_per_hop": bph,
                      "note": "algorithmic bytes per hop x hops / hop-kernel device time; CSR is L2-resident"},
         "gpu_launches": launches,
+        "autotune": tune,
         "e2e": e2e,
         "clocks": clk.summary(),
     }

@@ -59,6 +59,10 @@ class kmc_run_stats(C.Structure):
                 ("steps_done", C.c_int64), ("last_run_ms", C.c_double), ("last_launches", C.c_int32)]
 
 
+class kmc_tune_result(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("steps_per_launch", C.c_int32), ("hops_per_s", C.c_double)]
+
+
 # every symbol include/cntkmc.h declares, with (restype, argtypes)
 SIGNATURES = {
     "kmc_create": (C.c_void_p, [C.c_int, C.POINTER(C.c_int)]),
@@ -70,6 +74,9 @@ SIGNATURES = {
     "kmc_init_excitons": (C.c_int, [C.c_void_p, C.POINTER(kmc_inject)]),
     "kmc_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32]),
     "kmc_get_msd": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, PD]),
+    "kmc_set_msd_batches": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kmc_get_msd_batches": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, PD]),
+    "kmc_fit_diffusion": (C.c_int, [PD, PI64, PD, C.c_int64, C.c_int32, C.c_double, PD, PD]),
     "kmc_get_excitons": (C.c_int, [C.c_void_p, PI32, PD, PD, PD, PI32, PU64, PI64]),
     "kmc_num_excitons": (C.c_int64, [C.c_void_p]),
     "kmc_get_run_stats": (C.c_int, [C.c_void_p, C.POINTER(kmc_run_stats)]),
@@ -84,6 +91,8 @@ SIGNATURES = {
     "kmc_selftest_uniform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, PU64]),
     "kmc_math_probe": (C.c_int, [C.c_void_p, PD, C.c_int64, PD, PD]),
     "kmc_set_launch_config": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "kmc_set_mixed_variant": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kmc_autotune": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_void_p]),
     "kmc_build_neighbors_noalloc": (C.c_int, [PD, PD, C.c_int64, C.POINTER(kmc_table), C.c_double, PI64, PI32, PD, PD,
                                               C.c_int64, PI64, C.c_void_p, C.c_char_p, C.c_int64]),
     "kmc_version": (C.c_char_p, []),

@@ -90,6 +90,7 @@ struct kmc_ctx {
   // msd and trace
   DevBuf<double> d_msd;
   int64_t msd_cap = 0, steps_done = 0;
+  int32_t msd_batches = 1;
   int64_t n_trace = 0, trace_cap = 0;
   DevBuf<int32_t> d_trace;
   DevBuf<int64_t> d_trace_cnt;
@@ -101,6 +102,7 @@ struct kmc_ctx {
   int64_t hop_cap = 100000000LL;
   int steps_per_launch = 32;
   int block = 128;
+  int mixed_variant = 1;
   kmc_run_stats stats{};
 };
 
@@ -516,12 +518,13 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
 static int ensure_msd(kmc_ctx* c, int64_t need) {
   if (need <= c->msd_cap) return KMC_OK;
   int64_t cap = std::max<int64_t>(need, std::max<int64_t>(64, 2 * c->msd_cap));
+  const size_t row = (size_t)c->msd_batches * 3;  // doubles per (film, step)
   DevBuf<double> nb;
-  CK(c, nb.alloc((size_t)(c->n_films * cap * 3)));
-  CK(c, cudaMemsetAsync(nb.p, 0, (size_t)c->n_films * cap * 3 * sizeof(double), c->stream));
+  CK(c, nb.alloc((size_t)c->n_films * cap * row));
+  CK(c, cudaMemsetAsync(nb.p, 0, (size_t)c->n_films * cap * row * sizeof(double), c->stream));
   if (c->msd_cap > 0 && c->steps_done > 0)
-    CK(c, cudaMemcpy2DAsync(nb.p, cap * 3 * sizeof(double), c->d_msd.p, c->msd_cap * 3 * sizeof(double),
-                            c->steps_done * 3 * sizeof(double), c->n_films, cudaMemcpyDeviceToDevice, c->stream));
+    CK(c, cudaMemcpy2DAsync(nb.p, cap * row * sizeof(double), c->d_msd.p, c->msd_cap * row * sizeof(double),
+                            c->steps_done * row * sizeof(double), c->n_films, cudaMemcpyDeviceToDevice, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   c->d_msd.release();
   c->d_msd = nb;
@@ -530,20 +533,7 @@ static int ensure_msd(kmc_ctx* c, int64_t need) {
   return KMC_OK;
 }
 
-int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision) {
-  if (!c) return KMC_ERR_ARG;
-  if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_run: create the excitons first");
-  if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_run: bad step count, time step or velocity");
-  if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_run: bad precision");
-  CK(c, cudaSetDevice(c->device));
-  if (n_steps == 0) return KMC_OK;
-  dt = dt + 0.0;  // a zero time step is +0 (the kernels compare non-negative doubles bitwise)
-  int rc = ensure_msd(c, c->steps_done + n_steps);
-  if (rc) return rc;
-  if (precision == KMC_PREC_MIXED && c->lt_v != v) {
-    CK(c, kmc::launch_link_times(c->d_pos4.p, c->d_left.p, c->d_right.p, c->d_rec.p, c->d_lt64.p, c->n_sites, v, c->stream));
-    c->lt_v = v;
-  }
+static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   kmc::HopArgs a{};
   a.pos4 = c->d_pos4.p;
   a.left = c->d_left.p;
@@ -571,6 +561,7 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   a.n_slots = c->n_slots;
   a.msd = c->d_msd.p;
   a.msd_cap = c->msd_cap;
+  a.msd_batches = c->msd_batches;
   a.trace = c->d_trace.p;
   a.trace_cnt = c->d_trace_cnt.p;
   a.n_trace = c->n_trace;
@@ -581,30 +572,57 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   a.hop_cap = c->hop_cap;
   a.dt = dt;
   a.v = v;
-  unsigned long long before[4];
-  CK(c, cudaMemcpyAsync(before, c->d_counters.p, sizeof before, cudaMemcpyDeviceToHost, c->stream));
+  return a;
+}
+
+// Launch n_steps steps (step indices step0.. in a.msd) with the given shape; device time in *ms.
+static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0, int32_t precision, int variant,
+                     int spl, float* ms, int* launches) {
+  if (precision == KMC_PREC_MIXED && c->lt_v != a.v) {
+    CK(c, kmc::launch_link_times(c->d_pos4.p, c->d_left.p, c->d_right.p, c->d_rec.p, c->d_lt64.p, c->n_sites, a.v,
+                                 c->stream));
+    c->lt_v = a.v;
+  }
   CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
   CK(c, cudaEventRecord(c->ev0, c->stream));
-  int launches = 0;
-  const int single_film = c->n_films == 1 ? 1 : 0;
-  const int grid_blocks =
-      c->n_sms * kmc::hop_mixed_blocks_per_sm(c->block, std::min<int64_t>(c->steps_per_launch, n_steps), single_film);
-  for (int64_t s = 0; s < n_steps; s += c->steps_per_launch) {
-    int64_t k = std::min<int64_t>(c->steps_per_launch, n_steps - s);
-    a.step0 = c->steps_done + s;
+  const int single_film = (c->n_films == 1 && c->msd_batches == 1) ? 1 : 0;
+  const int grid_blocks = c->n_sms * kmc::hop_mixed_blocks_per_sm(variant, std::min<int64_t>(spl, n_steps), single_film);
+  int nl = 0;
+  for (int64_t s = 0; s < n_steps; s += spl) {
+    int64_t k = std::min<int64_t>(spl, n_steps - s);
+    a.step0 = step0 + s;
     if (precision == KMC_PREC_FP64)
       CK(c, kmc::launch_hop_fp64(a, k, c->block, c->stream));
     else
-      CK(c, kmc::launch_hop_mixed(a, k, c->block, grid_blocks, single_film, c->d_queue.p, c->stream));
-    ++launches;
+      CK(c, kmc::launch_hop_mixed(a, k, variant, grid_blocks, single_film, c->d_queue.p, c->stream));
+    ++nl;
   }
   CK(c, cudaEventRecord(c->ev1, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
-  float ms = 0;
-  CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  CK(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
+  *launches = nl;
   int32_t herr = 0;
-  unsigned long long after[4];
   CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
+  if (herr & 1) FAIL(c, KMC_ERR_HOP_CAP, "kmc_run: an exciton exceeded %lld hops in one step", (long long)c->hop_cap);
+  if (herr) FAIL(c, KMC_ERR_ARG, "kmc_run: a free flight crossed more than 2^22 links (zero-length tube links?)");
+  return KMC_OK;
+}
+
+int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_run: create the excitons first");
+  if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_run: bad step count, time step or velocity");
+  if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_run: bad precision");
+  CK(c, cudaSetDevice(c->device));
+  if (n_steps == 0) return KMC_OK;
+  dt = dt + 0.0;  // a zero time step is +0 (the kernels compare non-negative doubles bitwise)
+  int rc = ensure_msd(c, c->steps_done + n_steps);
+  if (rc) return rc;
+  kmc::HopArgs a = hop_args(c, dt, v);
+  float ms = 0;
+  int launches = 0;
+  rc = run_steps(c, a, n_steps, c->steps_done, precision, c->mixed_variant, c->steps_per_launch, &ms, &launches);
+  unsigned long long after[4];
   CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
   c->steps_done += n_steps;
   c->stats.hops = (int64_t)after[0];
@@ -613,20 +631,147 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   c->stats.steps_done = c->steps_done;
   c->stats.last_run_ms = ms;
   c->stats.last_launches = launches;
-  (void)before;
-  if (herr & 1) FAIL(c, KMC_ERR_HOP_CAP, "kmc_run: an exciton exceeded %lld hops in one step", (long long)c->hop_cap);
-  if (herr) FAIL(c, KMC_ERR_ARG, "kmc_run: a free flight crossed more than 2^22 links (zero-length tube links?)");
+  return rc;
+}
+
+int kmc_set_mixed_variant(kmc_ctx* c, int32_t variant) {
+  if (!c) return KMC_ERR_ARG;
+  if (variant < 0 || variant >= kmc::kMixedVariants) FAIL(c, KMC_ERR_ARG, "kmc_set_mixed_variant: 0..%d", kmc::kMixedVariants - 1);
+  c->mixed_variant = variant;
+  return KMC_OK;
+}
+
+int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_result* out) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_autotune: create the excitons first");
+  if (trial_steps < 1 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_autotune: bad arguments");
+  CK(c, cudaSetDevice(c->device));
+  dt = dt + 0.0;
+  const int64_t ns = c->n_slots;
+  // save the exciton state and counters; trials run into a scratch MSD buffer
+  DevBuf<int32_t> b_site;
+  DevBuf<uint32_t> b_flags;
+  DevBuf<double> b_pos, b_delta, b_ff, t_msd;
+  DevBuf<uint64_t> b_draws, b_hops;
+  DevBuf<int64_t> b_tcnt;
+  CK(c, b_site.alloc(ns));
+  CK(c, b_flags.alloc(ns));
+  CK(c, b_pos.alloc(3 * ns));
+  CK(c, b_delta.alloc(3 * ns));
+  CK(c, b_ff.alloc(ns));
+  CK(c, b_draws.alloc(ns));
+  CK(c, b_hops.alloc(ns));
+  CK(c, t_msd.alloc((size_t)c->n_films * trial_steps * c->msd_batches * 3));
+  auto copy_state = [&](bool save) -> cudaError_t {
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+      return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->stream);
+    };
+    cudaError_t e = cudaSuccess;
+    if (save) {
+      if ((e = cp(b_site.p, c->d_e_site.p, ns * 4)) || (e = cp(b_flags.p, c->d_e_flags.p, ns * 4)) ||
+          (e = cp(b_pos.p, c->d_e_pos.p, 3 * ns * 8)) || (e = cp(b_delta.p, c->d_e_delta.p, 3 * ns * 8)) ||
+          (e = cp(b_ff.p, c->d_e_ff.p, ns * 8)) || (e = cp(b_draws.p, c->d_e_draws.p, ns * 8)) ||
+          (e = cp(b_hops.p, c->d_e_hops.p, ns * 8)))
+        return e;
+    } else {
+      if ((e = cp(c->d_e_site.p, b_site.p, ns * 4)) || (e = cp(c->d_e_flags.p, b_flags.p, ns * 4)) ||
+          (e = cp(c->d_e_pos.p, b_pos.p, 3 * ns * 8)) || (e = cp(c->d_e_delta.p, b_delta.p, 3 * ns * 8)) ||
+          (e = cp(c->d_e_ff.p, b_ff.p, ns * 8)) || (e = cp(c->d_e_draws.p, b_draws.p, ns * 8)) ||
+          (e = cp(c->d_e_hops.p, b_hops.p, ns * 8)))
+        return e;
+    }
+    return cudaSuccess;
+  };
+  unsigned long long counters[4];
+  CK(c, cudaMemcpy(counters, c->d_counters.p, sizeof counters, cudaMemcpyDeviceToHost));
+  CK(c, copy_state(true));
+  int64_t saved_trace = c->n_trace;
+  c->n_trace = 0;  // trials record no trace
+  kmc::HopArgs a = hop_args(c, dt, v);
+  a.msd = t_msd.p;
+  a.msd_cap = trial_steps;
+  a.n_trace = 0;
+  const int spl_options[3] = {1, 8, 32};
+  double best = -1;
+  int best_v = c->mixed_variant, best_spl = c->steps_per_launch;
+  int rc = KMC_OK;
+  for (int variant = 0; variant < kmc::kMixedVariants && rc == KMC_OK; ++variant)
+    for (int spl : spl_options) {
+      if (spl > trial_steps && spl != 1) continue;
+      CK(c, copy_state(false));
+      CK(c, cudaMemcpyAsync(c->d_counters.p, counters, sizeof counters, cudaMemcpyHostToDevice, c->stream));
+      CK(c, cudaMemsetAsync(t_msd.p, 0, t_msd.n * sizeof(double), c->stream));
+      float ms = 0;
+      int nl = 0;
+      rc = run_steps(c, a, trial_steps, 0, KMC_PREC_MIXED, variant, spl, &ms, &nl);
+      if (rc) break;
+      unsigned long long after[4];
+      CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
+      double rate = (double)(after[0] - counters[0]) / (ms * 1e-3);
+      if (rate > best) {
+        best = rate;
+        best_v = variant;
+        best_spl = spl;
+      }
+    }
+  c->n_trace = saved_trace;
+  CK(c, copy_state(false));
+  CK(c, cudaMemcpyAsync(c->d_counters.p, counters, sizeof counters, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  b_site.release();
+  b_flags.release();
+  b_pos.release();
+  b_delta.release();
+  b_ff.release();
+  b_draws.release();
+  b_hops.release();
+  t_msd.release();
+  if (rc) return rc;
+  c->mixed_variant = best_v;
+  c->steps_per_launch = best_spl;
+  if (out) {
+    out->variant = best_v;
+    out->steps_per_launch = best_spl;
+    out->hops_per_s = best;
+  }
+  return KMC_OK;
+}
+
+int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) {
+  if (!c) return KMC_ERR_ARG;
+  if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
+  if (count == 0) return KMC_OK;
+  CK(c, cudaSetDevice(c->device));
+  const size_t row = (size_t)c->msd_batches * 3;
+  CK(c, cudaMemcpy2DAsync(out, count * row * sizeof(double), c->d_msd.p + first * row, c->msd_cap * row * sizeof(double),
+                          count * row * sizeof(double), c->n_films, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
   return KMC_OK;
 }
 
 int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) {
   if (!c) return KMC_ERR_ARG;
+  if (c->msd_batches == 1) return kmc_get_msd_batches(c, first, count, out);
   if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
-  if (count == 0) return KMC_OK;
-  CK(c, cudaSetDevice(c->device));
-  CK(c, cudaMemcpy2DAsync(out, count * 3 * sizeof(double), c->d_msd.p + first * 3, c->msd_cap * 3 * sizeof(double),
-                          count * 3 * sizeof(double), c->n_films, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));
+  const int64_t B = c->msd_batches;
+  std::vector<double> tmp((size_t)c->n_films * count * B * 3);
+  int rc = kmc_get_msd_batches(c, first, count, tmp.data());
+  if (rc) return rc;
+  for (int64_t f = 0; f < c->n_films; ++f)
+    for (int64_t s = 0; s < count; ++s)
+      for (int k = 0; k < 3; ++k) {
+        double acc = 0;  // batch order
+        for (int64_t b = 0; b < B; ++b) acc += tmp[((f * count + s) * B + b) * 3 + k];
+        out[(f * count + s) * 3 + k] = acc;
+      }
+  return KMC_OK;
+}
+
+int kmc_set_msd_batches(kmc_ctx* c, int32_t batches) {
+  if (!c) return KMC_ERR_ARG;
+  if (batches < 1 || batches > 4096) FAIL(c, KMC_ERR_ARG, "kmc_set_msd_batches: 1..4096 batches");
+  c->msd_batches = batches;
+  c->inited = false;
   return KMC_OK;
 }
 

@@ -181,6 +181,59 @@ int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* 
   return KMC_OK;
 }
 
+// Two-sided 95% quantile of Student's t with nu degrees of freedom: exact values for nu <= 4,
+// otherwise the Cornish-Fisher expansion about the normal quantile (Abramowitz & Stegun 26.7.5).
+static double t975(int nu) {
+  static const double small[5] = {0, 12.706204736174707, 4.302652729749464, 3.182446305284263, 2.776445105197793};
+  if (nu < 1) return NAN;
+  if (nu <= 4) return small[nu];
+  const double z = 1.959963984540054, v = nu;
+  const double z3 = z * z * z, z5 = z3 * z * z, z7 = z5 * z * z, z9 = z7 * z * z;
+  return z + (z3 + z) / (4 * v) + (5 * z5 + 16 * z3 + 3 * z) / (96 * v * v) +
+         (3 * z7 + 19 * z5 + 17 * z3 - 15 * z) / (384 * v * v * v) +
+         (79 * z9 + 776 * z7 + 1482 * z5 - 1920 * z3 - 945 * z) / (92160 * v * v * v * v);
+}
+
+int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* times, int64_t n_steps, int32_t batches,
+                      double fit_fraction, double D[3], double ci95[3]) {
+  if (!msd || !counts || !times || !D || !ci95 || n_steps < 2 || batches < 1 || !(fit_fraction > 0) ||
+      fit_fraction > 1)
+    return KMC_ERR_ARG;
+  int64_t s0 = n_steps - (int64_t)std::ceil(fit_fraction * (double)n_steps);
+  if (s0 < 0) s0 = 0;
+  if (n_steps - s0 < 2) s0 = n_steps - 2;
+  const int64_t m = n_steps - s0;
+  double tm = 0;
+  for (int64_t s = s0; s < n_steps; ++s) tm += times[s];
+  tm /= (double)m;
+  double sxx = 0;
+  for (int64_t s = s0; s < n_steps; ++s) sxx += (times[s] - tm) * (times[s] - tm);
+  if (!(sxx > 0)) return KMC_ERR_ARG;
+  for (int k = 0; k < 3; ++k) {
+    std::vector<double> db;
+    for (int32_t b = 0; b < batches; ++b) {
+      if (counts[b] <= 0) continue;
+      double ym = 0;
+      for (int64_t s = s0; s < n_steps; ++s) ym += msd[(s * batches + b) * 3 + k] / (double)counts[b];
+      ym /= (double)m;
+      double sxy = 0;
+      for (int64_t s = s0; s < n_steps; ++s)
+        sxy += (times[s] - tm) * (msd[(s * batches + b) * 3 + k] / (double)counts[b] - ym);
+      db.push_back(sxy / sxx / 2.0);
+    }
+    if (db.empty()) return KMC_ERR_ARG;
+    double mean = 0;
+    for (double x : db) mean += x;
+    mean /= (double)db.size();
+    double var = 0;
+    for (double x : db) var += (x - mean) * (x - mean);
+    D[k] = mean;
+    ci95[k] = db.size() > 1 ? t975((int)db.size() - 1) * std::sqrt(var / (double)(db.size() - 1)) / std::sqrt((double)db.size())
+                            : NAN;
+  }
+  return KMC_OK;
+}
+
 const char* kmc_version(void) { return "cntkmc 0.1 (sm_103a)"; }
 
 }  // extern "C"

@@ -86,8 +86,9 @@ struct HopArgs {
   uint64_t* e_hops;
   int64_t n_slots;
   // output
-  double* msd;      // [n_films][msd_cap][3]
+  double* msd;      // [n_films][msd_cap][msd_batches][3]
   int64_t msd_cap;
+  int32_t msd_batches; // excitons of a film are split into batches by warp: ((local / 32) mod batches)
   int64_t step0;
   int32_t* trace;
   int64_t* trace_cnt;
@@ -141,9 +142,10 @@ cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, cons
                               double2* lt64, int64_t n, double v, cudaStream_t s);
 cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s);
 cudaError_t launch_hop_fp64(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
-cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int block, int grid_blocks, int single_film,
+cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int variant, int grid_blocks, int single_film,
                              unsigned long long* queue, cudaStream_t s);
-int hop_mixed_blocks_per_sm(int block, int64_t n_steps, int single_film);
+int hop_mixed_blocks_per_sm(int variant, int64_t n_steps, int single_film);
+constexpr int kMixedVariants = 3;
 cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,
                               cudaStream_t s);

@@ -91,8 +91,26 @@ class Engine:
     def set_hop_cap(self, cap: int):
         self._check(self.lib.kmc_set_hop_cap(self.h, cap))
 
+    def set_msd_batches(self, batches: int):
+        self._check(self.lib.kmc_set_msd_batches(self.h, batches))
+        self.batches = batches
+
+    def msd_batches(self, first: int, count: int) -> np.ndarray:
+        b = getattr(self, "batches", 1)
+        out = np.zeros((self.n_films, count, b, 3))
+        self._check(self.lib.kmc_get_msd_batches(self.h, first, count, L.ptr(out, C.c_double)))
+        return out
+
     def set_launch_config(self, block: int, steps_per_launch: int):
         self._check(self.lib.kmc_set_launch_config(self.h, block, steps_per_launch))
+
+    def set_mixed_variant(self, variant: int):
+        self._check(self.lib.kmc_set_mixed_variant(self.h, variant))
+
+    def autotune(self, dt: float, velocity: float, trial_steps: int = 2) -> dict:
+        r = L.kmc_tune_result()
+        self._check(self.lib.kmc_autotune(self.h, float(dt), float(velocity), int(trial_steps), C.byref(r)))
+        return {"variant": r.variant, "steps_per_launch": r.steps_per_launch, "hops_per_s": r.hops_per_s}
 
     def init_excitons(self, n_excitons, seeds, mode=L.KMC_INJECT_UNIFORM, n_sections=5):
         ne = np.ascontiguousarray(np.broadcast_to(np.asarray(n_excitons, dtype=np.int64), (self.n_films,)))

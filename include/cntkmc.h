@@ -118,6 +118,21 @@ int kmc_run(kmc_ctx* ctx, int64_t n_steps, double dt, double velocity, int32_t p
 /* MSD sums of steps [first, first + count) for every film: out[f][s][3]. */
 int kmc_get_msd(kmc_ctx* ctx, int64_t first, int64_t count, double* out);
 
+/* MSD sums per exciton batch (no counterpart in the reference; used for the confidence interval
+ * of D).  Exciton i of a film belongs to batch (i / 32) mod batches.  Set before
+ * kmc_init_excitons (default 1).  out[f][s][batch][3]. */
+int kmc_set_msd_batches(kmc_ctx* ctx, int32_t batches);
+int kmc_get_msd_batches(kmc_ctx* ctx, int64_t first, int64_t count, double* out);
+
+/* Diffusion coefficient from batch MSD curves (the reference plots MSD/t,
+ * visualization/monte_carlo_results.py:478-500, and reports no fit): per batch and axis the
+ * least-squares slope of <dx^2>(t) over the last `fit_fraction` of the steps, D = slope/2;
+ * D[axis] = mean over batches, ci95[axis] = t(0.975, B-1) sd / sqrt(B).  msd is
+ * [n_steps][batches][3] sums, counts[batch] the excitons per batch, times[n_steps] the step
+ * end times.  Host-only. */
+int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* times, int64_t n_steps,
+                      int32_t batches, double fit_fraction, double D[3], double ci95[3]);
+
 /* Exciton state (film-major, exciton order).  Any pointer may be NULL.  pos/delta are [n][3]. */
 int kmc_get_excitons(kmc_ctx* ctx, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,
                      uint64_t* draws, int64_t* hops);
@@ -172,6 +187,21 @@ int kmc_math_probe(kmc_ctx* ctx, const double* x, int64_t n, double* log_out, do
 /* Hop-kernel launch shape: threads per block (multiple of 32, <= 256) and Green-Kubo steps per
  * launch (the kernel keeps excitons in registers across the steps of one launch). */
 int kmc_set_launch_config(kmc_ctx* ctx, int32_t block, int32_t steps_per_launch);
+
+/* Mixed kernel variant: 0, 1, 2 = compiled for at least 4, 6, 8 resident blocks of 128
+ * threads per SM (fewer registers per thread, more warps resident). */
+int kmc_set_mixed_variant(kmc_ctx* ctx, int32_t variant);
+
+typedef struct {
+  int32_t variant;
+  int32_t steps_per_launch;
+  double hops_per_s;
+} kmc_tune_result;
+
+/* Time every mixed-kernel variant with 1, 8 and 32 steps per launch for trial_steps steps of dt
+ * on the current excitons (their state is saved and restored; no MSD step is recorded) and keep
+ * the fastest.  Results never depend on the choice. */
+int kmc_autotune(kmc_ctx* ctx, double dt, double velocity, int64_t trial_steps, kmc_tune_result* out);
 
 /* ---- neighbour lists without device allocation (no counterpart in the reference) ----
  *

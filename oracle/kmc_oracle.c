@@ -678,6 +678,11 @@ int64_t orc_sim_get_trace(const orc_sim* s, int64_t e, int32_t* buf, int64_t cap
 
 /* kubo_step, monte_carlo.cpp:319-342, then the sums of kubo_save_avg_dispalcement_squared :398-402 */
 int orc_sim_step(orc_sim* s, double dt, int64_t n_steps, double* msd_sums) {
+  return orc_sim_step_batches(s, dt, n_steps, 1, msd_sums);
+}
+
+int orc_sim_step_batches(orc_sim* s, double dt, int64_t n_steps, int batches, double* msd_sums) {
+  if (batches < 1) return -1;
   for (int64_t st = 0; st < n_steps; ++st) {
 #pragma omp parallel num_threads(s->n_threads)
     {
@@ -708,17 +713,16 @@ int orc_sim_step(orc_sim* s, double dt, int64_t n_steps, double* msd_sums) {
       free(cum);
       free(col);
     }
-    double sx = 0, sy = 0, sz = 0;
-    for (int64_t e = 0; e < s->n_exc; ++e) {
-      const orc_exc* p = s->exc + e;
-      sx += p->delta[0] * p->delta[0];
-      sy += p->delta[1] * p->delta[1];
-      sz += p->delta[2] * p->delta[2];
-    }
     if (msd_sums) {
-      msd_sums[3 * st + 0] = sx;
-      msd_sums[3 * st + 1] = sy;
-      msd_sums[3 * st + 2] = sz;
+      double* row = msd_sums + (size_t)st * batches * 3;
+      for (int b = 0; b < 3 * batches; ++b) row[b] = 0.0;
+      for (int64_t e = 0; e < s->n_exc; ++e) {
+        const orc_exc* p = s->exc + e;
+        double* m = row + 3 * ((e / 32) % batches);
+        m[0] += p->delta[0] * p->delta[0];
+        m[1] += p->delta[1] * p->delta[1];
+        m[2] += p->delta[2] * p->delta[2];
+      }
     }
   }
   return 0;

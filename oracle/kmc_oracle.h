@@ -90,6 +90,9 @@ int64_t orc_sim_get_trace(const orc_sim* s, int64_t e, int32_t* buf, int64_t cap
  * sum_i dx_i^2, dy^2, dz^2 in exciton order (kubo_save_avg_dispalcement_squared
  * :382-409 before its division) go to msd_sums[step][3]. */
 int orc_sim_step(orc_sim* s, double dt, int64_t n_steps, double* msd_sums);
+/* As orc_sim_step, with the sums split by exciton batch: exciton i adds to batch
+ * (i / 32) % batches; out[step][batch][3], each batch summed in exciton order. */
+int orc_sim_step_batches(orc_sim* s, double dt, int64_t n_steps, int batches, double* out);
 
 /* Per-exciton state: site, pos[3], old_pos[3], delta[3], ff, heading, draws, hops. */
 void orc_sim_get_excitons(const orc_sim* s, int32_t* site, double* pos, double* old_pos, double* delta, double* ff,

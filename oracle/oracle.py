@@ -71,6 +71,8 @@ def lib():
         L.orc_sim_get_trace.restype = I64
         L.orc_sim_step.argtypes = [C.c_void_p, D, I64, PD]
         L.orc_sim_step.restype = C.c_int
+        L.orc_sim_step_batches.argtypes = [C.c_void_p, D, I64, C.c_int, PD]
+        L.orc_sim_step_batches.restype = C.c_int
         L.orc_sim_get_excitons.argtypes = [C.c_void_p, PI32, PD, PD, PD, PD, PI32, PU64, PI64]
         L.orc_sim_total_hops.argtypes = [C.c_void_p]
         L.orc_sim_total_hops.restype = I64
@@ -225,6 +227,11 @@ class Sim:
         msd = np.zeros((max(n_steps, 1), 3))
         lib().orc_sim_step(self.h, dt, n_steps, _p(msd, D))
         return msd[:n_steps]
+
+    def step_batches(self, dt, n_steps, batches):
+        out = np.zeros((max(n_steps, 1), batches, 3))
+        lib().orc_sim_step_batches(self.h, dt, n_steps, batches, _p(out, D))
+        return out[:n_steps]
 
     def excitons(self):
         n = self.n_exc

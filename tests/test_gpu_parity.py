@@ -288,3 +288,61 @@ def test_long_rows_match_oracle(box, n_tubes, r_max, kmin):
         assert_states_equal(e.excitons(), sim.excitons())
         assert_msd_close(e.msd(0, 4), om)
         e.close()
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_msd_batches_and_diffusion_fit_match_oracle(precision):
+    from cnt_film_monte_carlo_gb300 import diffusion
+
+    f, tab, r_max = synthetic_case(2, n_tubes=30, length=50.0, box=(100, 100, 6))
+    n_exc, seed, dt, v, steps, B = 2000, 17, 1e-13, 2e5, 10, 8
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, r_max, v)
+    sim.create_excitons(1, 0, n_exc, seed)
+    ob = sim.step_batches(dt, steps, B)
+    for films in ([f], [f, f]):  # single film (shared bins off: batches > 1) and two films (global atomics)
+        e = E.Engine(0)
+        e.load_films(films)
+        e.set_table(tab)
+        e.build(r_max)
+        e.set_msd_batches(B)
+        e.init_excitons(n_exc, seed, L.KMC_INJECT_UNIFORM)
+        e.run(steps, dt, v, precision)
+        gb = e.msd_batches(0, steps)
+        for k in range(len(films)):
+            np.testing.assert_allclose(gb[k], ob, rtol=MSD_RTOL)
+            np.testing.assert_allclose(e.msd(0, steps)[k], ob.sum(axis=1), rtol=MSD_RTOL)
+        t = np.arange(1, steps + 1) * dt
+        dg, cg = diffusion.fit(gb[0], n_exc, t)
+        do, co = diffusion.fit(ob, n_exc, t)
+        np.testing.assert_allclose(dg, do, rtol=1e-9)
+        np.testing.assert_allclose(cg, co, rtol=1e-6)
+        e.close()
+
+
+def test_mixed_variants_and_autotune_do_not_change_results():
+    f, tab, r_max = synthetic_case(2, n_tubes=20, length=40.0, box=(80, 80, 6))
+    states = []
+    for variant in (0, 1, 2):
+        e = E.Engine(0)
+        e.load_films(f)
+        e.set_table(tab)
+        e.build(r_max)
+        e.set_mixed_variant(variant)
+        e.init_excitons(3000, 4, L.KMC_INJECT_UNIFORM)
+        e.run(5, 1e-13, 2e5, L.KMC_PREC_MIXED)
+        states.append((e.excitons(), e.msd(0, 5), e.stats()["hops"]))
+        e.close()
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_table(tab)
+    e.build(r_max)
+    e.init_excitons(3000, 4, L.KMC_INJECT_UNIFORM)
+    choice = e.autotune(1e-13, 2e5, trial_steps=2)
+    assert choice["variant"] in (0, 1, 2) and choice["hops_per_s"] > 0
+    e.run(5, 1e-13, 2e5, L.KMC_PREC_MIXED)
+    states.append((e.excitons(), e.msd(0, 5), e.stats()["hops"]))
+    e.close()
+    for g, m, h in states[1:]:
+        assert_states_equal(g, states[0][0])
+        assert_msd_close(m, states[0][1])
+        assert h == states[0][2]
