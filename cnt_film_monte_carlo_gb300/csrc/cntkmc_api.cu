@@ -39,7 +39,7 @@ struct DevBuf {
   }
 };
 
-const double kLogTab[1 << KMC_LOG_TABLE_BITS][3] = KMC_LOG_TAB_INIT;
+const uint64_t kLogTab[1 << KMC_LOG_TABLE_BITS][3] = KMC_FX_TAB_INIT;
 
 }  // namespace
 
@@ -268,6 +268,11 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
     CK(c, upload(c->d_grid[d], t->grid[d], t->n[d], c->stream));
     c->table.n[d] = t->n[d];
     c->table.grid[d] = c->d_grid[d].p;
+    // windowed nearest-point search only for strictly ascending grids
+    bool asc = t->n[d] >= 8;
+    for (int32_t i = 1; i < t->n[d] && asc; ++i) asc = t->grid[d][i] > t->grid[d][i - 1];
+    double span = t->grid[d][t->n[d] - 1] - t->grid[d][0];
+    c->table.inv_h[d] = (asc && span > 0) ? (double)(t->n[d] - 1) / span : 0.0;
   }
   CK(c, upload(c->d_rate, t->rate, nr, c->stream));
   c->table.rate = c->d_rate.p;

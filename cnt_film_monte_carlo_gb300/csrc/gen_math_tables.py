@@ -1,21 +1,25 @@
-"""Generate kmc_math_tables.h: constants of the engine's FP64 log and acos.
+"""Generate kmc_math_tables.h: constants of the engine's log and acos.
 
 The hop kernels draw dwell times -log(u)/Gamma (the reference's scatterer::ff_time,
 src/monte_carlo/scatterer.h:74-80) and the neighbour build needs the pair angle
 acos(a1 . a2) (scatterer.cpp:51).  The engine evaluates both with functions of its own so
 that every build (CUDA device code, host code) produces the same bits:
 
-* log: P. T. P. Tang's table-driven method (ACM TOMS 16(4), 1990).  x = 2^k z with
-  z in [a, 2a), a ~ 0.7012, split into 1024 intervals of equal width in the bit
-  pattern; interval i has c_i = 1/midpoint (c = 1 exactly on the interval holding 1.0)
-  and -log(c_i) as hi (a multiple of 2^-42, so k ln2_hi + hi is exact) + lo;
-  log x = (k ln2_hi + hi) + (r + ((k ln2_lo + lo) + r^2 P(r))), r = fma(z, c_i, -1),
-  P(r) = -1/2 + r/3 - r^2/4 + r^3/5 (Taylor series of log1p; |r| <= 2^-11).
+* log, fixed point (after the table-driven method of P. T. P. Tang, "Table-driven
+  implementation of the logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4),
+  1990): x = 2^k z with z in [a, 2a), a ~ 0.7012, z in one of 1024 intervals of equal width in
+  the bit pattern (the interval holding 1.0 has it in its middle).  Interval i has a 24-bit
+  integer reciprocal C_i = round(2^23 / midpoint) (C = 2^23 on the interval holding 1.0), so
+  r = z C_i 2^-23 - 1 is an exact integer multiple of 2^-76 (z < 1) or 2^-75 with
+  |r| <= 2^-11.  log1p(r) = r S(r), S = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 - r^5/6 evaluated in
+  Q1.62 integers; log x = k ln2 - log(C_i 2^-23) + r S is summed in a signed 128-bit integer with
+  116 fraction bits (ln2 and -log(C_i 2^-23) rounded to 2^-116) and rounded once to double
+  (nearest, ties to even).  Error below 0.52 ulp.
 * acos: pi/2 - asin(c) for |c| <= 1/2, 2 asin(sqrt((1-c)/2)) above and
   pi - 2 asin(sqrt((1+c)/2)) below, asin(x) = x + x z Q(z), z = x^2, Q from the Taylor
   series (2n)!/(4^n (n!)^2 (2n+1)), 24 terms.
 
-Values are mpmath results at 200 bits rounded once to double.
+Values are mpmath results at 200 bits, rounded once.
 Run: python cnt_film_monte_carlo_gb300/csrc/gen_math_tables.py
 """
 import os
@@ -42,52 +46,49 @@ def nearest(x):
     return float(mpmath.mpf(x))
 
 
-def to_grid(x, e):
-    """Nearest multiple of 2**e."""
-    s = mpmath.mpf(2) ** e
-    return float(mpmath.nint(mpmath.mpf(x) / s) * s)
-
-
 def main():
     ln2 = mpmath.log(2)
-    ln2_hi = to_grid(ln2, -42)
-    rows = []
-    for i in range(N):
-        a = mpmath.mpf(bits_to_double(OFF + i * STEP))
-        b = mpmath.mpf(bits_to_double(OFF + (i + 1) * STEP))
-        c = 1.0 if i == CENTER else nearest(2 / (a + b))
-        neg_log_c = -mpmath.log(mpmath.mpf(c))
-        hi = to_grid(neg_log_c, -42)
-        rows.append((c, hi, nearest(neg_log_c - mpmath.mpf(hi))))
     consts = {
-        "KMC_LN2_HI": ln2_hi,
-        "KMC_LN2_LO": nearest(ln2 - mpmath.mpf(ln2_hi)),
         "KMC_PIO2_HI": nearest(mpmath.pi / 2),
         "KMC_PIO2_LO": nearest(mpmath.pi / 2 - mpmath.mpf(nearest(mpmath.pi / 2))),
         "KMC_PI_HI": nearest(mpmath.pi),
         "KMC_PI_LO": nearest(mpmath.pi - mpmath.mpf(nearest(mpmath.pi))),
     }
-    log1p = [nearest(mpmath.mpf((-1) ** (j + 1)) / j) for j in range(2, 6)]
     asin = [
         nearest(mpmath.factorial(2 * n) / (mpmath.mpf(4) ** n * mpmath.factorial(n) ** 2 * (2 * n + 1)))
         for n in range(1, N_ASIN + 1)
     ]
     lines = [
         "/* kmc_math_tables.h -- generated by gen_math_tables.py; do not edit.",
-        " * Constants of the engine's FP64 log (Tang's table-driven method) and acos (asin Taylor",
-        " * series).  Initialiser macros, so host and device code can each instantiate them. */",
+        " * Constants of the engine's fixed-point log and of acos (asin Taylor series).",
+        " * Initialiser macros, so host and device code can each instantiate them. */",
         "#pragma once",
         f"#define KMC_LOG_TABLE_BITS {BITS}",
         f"#define KMC_LOG_OFF 0x{OFF:016X}ULL",
     ]
     for k, v in consts.items():
         lines.append(f"#define {k} ({v.hex()})")
-    lines.append("#define KMC_LOG1P_INIT {" + ", ".join(c.hex() for c in log1p) + "}")
     lines.append("#define KMC_ASIN_INIT {" + ", ".join(c.hex() for c in asin) + "}")
     lines.append(f"#define KMC_ASIN_TERMS {N_ASIN}")
-    lines.append("#define KMC_LOG_TAB_INIT { \\")
-    for c, hi, lo in rows:
-        lines.append(f"  {{{c.hex()}, {hi.hex()}, {lo.hex()}}}, \\")
+    Q = 116
+    ln2q = int(mpmath.nint(ln2 * mpmath.mpf(2) ** Q))
+    lines.append(f"#define KMC_FX_LN2_HI 0x{ln2q >> 64:016X}ULL")
+    lines.append(f"#define KMC_FX_LN2_LO 0x{ln2q & ((1 << 64) - 1):016X}ULL")
+    s62 = [int(mpmath.nint(mpmath.mpf(v) * mpmath.mpf(2) ** 62)) for v in
+           (1, mpmath.mpf(-1) / 2, mpmath.mpf(1) / 3, mpmath.mpf(-1) / 4, mpmath.mpf(1) / 5, mpmath.mpf(-1) / 6)]
+    lines.append("#define KMC_FX_S_INIT {" + ", ".join(f"{v}LL" for v in s62) + "}")
+    cs, lcs = [], []
+    for i in range(N):
+        a = mpmath.mpf(bits_to_double(OFF + i * STEP))
+        b = mpmath.mpf(bits_to_double(OFF + (i + 1) * STEP))
+        C = 1 << 23 if i == CENTER else int(mpmath.nint(mpmath.mpf(2) ** 24 / (a + b)))
+        lc = int(mpmath.nint(-mpmath.log(mpmath.mpf(C) / mpmath.mpf(2) ** 23) * mpmath.mpf(2) ** Q))
+        cs.append(C)
+        lcs.append(lc & ((1 << 128) - 1))
+    lines.append("/* per interval: {C_i (24-bit reciprocal), hi, lo of -log(C_i 2^-23) in Q116 (two's complement)} */")
+    lines.append("#define KMC_FX_TAB_INIT { \\")
+    for c, v in zip(cs, lcs):
+        lines.append(f"  {{{c}ull, 0x{v >> 64:016X}ull, 0x{v & ((1 << 64) - 1):016X}ull}}, \\")
     lines.append("}")
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kmc_math_tables.h")
     with open(out, "w") as f:

@@ -121,29 +121,122 @@ __device__ __forceinline__ double u_from_rand(uint32_t r) {
   return __longlong_as_double((long long)bits);
 }
 
-// ---------------------------------------------------------------- log (Tang's table-driven method)
+// ---------------------------------------------------------------- log (fixed point, integer pipes)
+// x = 2^k z (z in [a, 2a), one of 1024 intervals); c = C 2^-23 with a 24-bit reciprocal C, so
+// r = z c - 1 = R 2^(ez - 75) is exact; log1p(r) = r S(r) with S evaluated in Q1.62 integers;
+// k ln2 - log c + r S is summed in a signed 128-bit Q116 integer and rounded once to double
+// (nearest, ties to even).  No floating-point instruction is used: the FP64 pipe of sm_103a is
+// the scarce resource of the hop kernels.  Error < 0.52 ulp.
 struct LogTab {
-  double t[1 << KMC_LOG_TABLE_BITS][3];
+  uint64_t t[1 << KMC_LOG_TABLE_BITS][3];  // C, hi and lo of -log(C 2^-23) in Q116
 };
 
-// log(z 2^k) from the reduced argument: the common tail of kmc_log and kmc_log_unit.
-__device__ __forceinline__ double log_tail(uint64_t ix, uint64_t tmp, double kf, const LogTab* __restrict__ tab) {
-  int i = (int)((tmp >> (52 - KMC_LOG_TABLE_BITS)) & ((1u << KMC_LOG_TABLE_BITS) - 1));
-  double z = __longlong_as_double((long long)(ix - (tmp & 0xFFF0000000000000ull)));
-  double invc = __ldg(&tab->t[i][0]);
-  double lhi = __ldg(&tab->t[i][1]);
-  double llo = __ldg(&tab->t[i][2]);
-  const double c[4] = KMC_LOG1P_INIT;
-  double r = fma(z, invc, -1.0);
-  double t1 = fma(kf, KMC_LN2_HI, lhi);
-  double p = c[3];
-  p = fma(p, r, c[2]);
-  p = fma(p, r, c[1]);
-  p = fma(p, r, c[0]);
-  double r2 = r * r;
-  double q = r2 * p;
-  double s = fma(kf, KMC_LN2_LO, llo) + q;
-  return t1 + (r + s);
+struct I128 {
+  uint64_t lo;
+  int64_t hi;
+};
+
+__device__ __forceinline__ I128 add128(I128 a, I128 b) {
+  I128 r;
+  r.lo = a.lo + b.lo;
+  r.hi = a.hi + b.hi + (r.lo < a.lo ? 1 : 0);
+  return r;
+}
+// arithmetic shift right by 1 <= s <= 63
+__device__ __forceinline__ I128 sar128(I128 a, int s) {
+  I128 r;
+  r.lo = (a.lo >> s) | ((uint64_t)a.hi << (64 - s));
+  r.hi = a.hi >> s;
+  return r;
+}
+__device__ __forceinline__ I128 neg128(I128 a) {
+  I128 r;
+  r.lo = ~a.lo + 1;
+  r.hi = ~a.hi + (r.lo == 0 ? 1 : 0);
+  return r;
+}
+__device__ __forceinline__ I128 mul64s(int64_t a, int64_t b) {
+  I128 r;
+  r.lo = (uint64_t)a * (uint64_t)b;
+  r.hi = __mul64hi((long long)a, (long long)b);
+  return r;
+}
+__device__ __forceinline__ int bitlen128(uint64_t hi, uint64_t lo) {
+  return hi ? 128 - __clzll((long long)hi) : (lo ? 64 - __clzll((long long)lo) : 0);
+}
+
+// T 2^-116 rounded to the nearest double (ties to even); T != 0
+__device__ __forceinline__ double q116_to_double(I128 T) {
+  uint64_t sign = 0;
+  if (T.hi < 0) {
+    sign = 1ull << 63;
+    T = neg128(T);
+  }
+  const uint64_t hi = (uint64_t)T.hi, lo = T.lo;
+  const int L = bitlen128(hi, lo);
+  uint64_t mant;
+  int e2;
+  if (L <= 53) {
+    mant = lo << (53 - L);
+    e2 = L - 53 - 116;
+  } else {
+    int sh = L - 53;  // 1..74
+    uint64_t keep = sh < 64 ? ((lo >> sh) | (sh ? hi << (64 - sh) : 0)) : (hi >> (sh - 64));
+    int g = sh - 1;  // guard bit position
+    uint64_t guard = g < 64 ? (lo >> g) & 1ull : (hi >> (g - 64)) & 1ull;
+    bool sticky = g <= 64 ? (g == 64 ? lo != 0 : (lo & ((1ull << g) - 1)) != 0)
+                          : (lo != 0 || (hi & ((1ull << (g - 64)) - 1)) != 0);
+    mant = keep;
+    if (guard && (sticky || (mant & 1ull))) {
+      ++mant;
+      if (mant == (1ull << 53)) {
+        mant >>= 1;
+        ++sh;
+      }
+    }
+    e2 = sh - 116;
+  }
+  return __longlong_as_double((long long)(sign | ((uint64_t)(e2 + 52 + 1023) << 52) | (mant & ((1ull << 52) - 1))));
+}
+
+// log(x) for a normal x > 0 (kadj: exponent correction of a pre-scaled subnormal)
+__device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const LogTab* __restrict__ tab) {
+  const uint64_t tmp = ix - KMC_LOG_OFF;
+  const int i = (int)((tmp >> (52 - KMC_LOG_TABLE_BITS)) & ((1u << KMC_LOG_TABLE_BITS) - 1));
+  const int k = (int)((int64_t)tmp >> 52) + kadj;
+  const uint64_t iz = ix - (tmp & 0xFFF0000000000000ull);
+  const int ez = (int)(iz >> 52) - 1023;  // -1 or 0
+  const uint64_t Z = (iz & ((1ull << 52) - 1)) | (1ull << 52);
+  const uint64_t C = __ldg(&tab->t[i][0]);
+  // R = Z C - 2^(75 - ez): the subtrahend is 2^(11 - ez) in the high word
+  I128 R;
+  R.lo = Z * C;
+  R.hi = (int64_t)__umul64hi(Z, C) - (1ll << (11 - ez));
+  const int64_t r62 = (int64_t)sar128(R, 13 - ez).lo;  // r in Q1.62
+  const int64_t sc[6] = KMC_FX_S_INIT;
+  int64_t t = sc[5];
+#pragma unroll
+  for (int j = 4; j >= 0; --j) {
+    I128 m = mul64s(t, r62);
+    t = (int64_t)((m.lo >> 62) | ((uint64_t)m.hi << 2)) + sc[j];
+  }
+  I128 aR = R.hi < 0 ? neg128(R) : R;
+  const int bl = bitlen128((uint64_t)aR.hi, aR.lo);
+  const int sh = bl > 62 ? bl - 62 : 0;
+  const int64_t R64 = sh ? (int64_t)sar128(R, sh).lo : (int64_t)R.lo;
+  const I128 L1 = sar128(mul64s(R64, t), 21 - ez - sh);  // r S in Q116
+  // k ln2 in Q116
+  const uint64_t ka = (uint64_t)(k < 0 ? -k : k);
+  I128 kl;
+  kl.lo = ka * KMC_FX_LN2_LO;
+  kl.hi = (int64_t)(ka * KMC_FX_LN2_HI + __umul64hi(ka, KMC_FX_LN2_LO));
+  if (k < 0) kl = neg128(kl);
+  I128 lc;
+  lc.lo = __ldg(&tab->t[i][2]);
+  lc.hi = (int64_t)__ldg(&tab->t[i][1]);
+  const I128 T = add128(add128(kl, lc), L1);
+  if (T.hi == 0 && T.lo == 0) return 0.0;
+  return q116_to_double(T);
 }
 
 __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ tab) {
@@ -156,22 +249,12 @@ __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ t
     ix = (uint64_t)__double_as_longlong(x);
     kadj = -52;
   }
-  uint64_t tmp = ix - KMC_LOG_OFF;
-  int k = (int)((int64_t)tmp >> 52) + kadj;
-  return log_tail(ix, tmp, (double)k, tab);
+  return log_fx_normal(ix, kadj, tab);
 }
 
-// kmc_log for a normal x in (0, 1] (the dwell-time uniforms): no special cases, and the exponent
-// k in [-1022, 0] is turned into a double with integer operations (same exact value as (double)k).
+// kmc_log for the dwell-time uniforms, which are normal numbers in (0, 1]: no special cases.
 __device__ __forceinline__ double kmc_log_unit(double x, const LogTab* __restrict__ tab) {
-  uint64_t ix = (uint64_t)__double_as_longlong(x);
-  uint64_t tmp = ix - KMC_LOG_OFF;
-  int k = (int)((int64_t)tmp >> 52);
-  uint32_t m = (uint32_t)(-k);
-  int e = 31 - __clz((int)m);
-  uint64_t kb = m ? ((1ull << 63) | ((uint64_t)(1023 + e) << 52) | (((uint64_t)m << (52 - e)) & ((1ull << 52) - 1)))
-                  : 0ull;
-  return log_tail(ix, tmp, __longlong_as_double((long long)kb), tab);
+  return log_fx_normal((uint64_t)__double_as_longlong(x), 0, tab);
 }
 
 // ---------------------------------------------------------------- acos (asin Taylor series)
@@ -220,6 +303,33 @@ __device__ __forceinline__ int index_min_abs(const double* __restrict__ g, int n
       idx = i;
     }
   }
+  return idx;
+}
+
+// index_min_abs for an ascending grid with (roughly) uniform spacing: the scan is restricted to
+// a window around the estimate (x - g[0]) * inv_h and gives the same index as the full scan,
+// which is used whenever that cannot be guaranteed.  The computed differences fl(g[i] - x) are
+// non-decreasing in i, so |g[i] - x| falls, then rises: its first minimum is the last index left
+// of the sign change or the first one right of it.  The window result stands when the sign
+// change lies strictly inside the window (or at a grid end) and no tie reaches the window's
+// left edge.
+__device__ __forceinline__ int index_min_abs_fast(const double* __restrict__ g, int n, double x, double inv_h) {
+  if (!(fabs(x) < __longlong_as_double(0x7FF0000000000000ll)) || n < 8) return index_min_abs(g, n, x);
+  double e = (x - g[0]) * inv_h;
+  int c = e < 0.0 ? 0 : (e > (double)(n - 1) ? n - 1 : (int)(e + 0.5));
+  int lo = c - 2 < 0 ? 0 : c - 2, hi = c + 2 > n - 1 ? n - 1 : c + 2;
+  double dlo = g[lo] - x, dhi = g[hi] - x;
+  if ((lo > 0 && !(dlo < 0.0)) || (hi < n - 1 && !(dhi >= 0.0))) return index_min_abs(g, n, x);
+  double best = __longlong_as_double(0x7FF0000000000000ll);
+  int idx = lo;
+  for (int i = lo; i <= hi; ++i) {
+    double t = fabs(g[i] - x);
+    if (t < best) {
+      best = t;
+      idx = i;
+    }
+  }
+  if (idx == lo && lo > 0) return index_min_abs(g, n, x);  // a tie could extend left of the window
   return idx;
 }
 

@@ -51,6 +51,7 @@ struct TableDev {
   int32_t n[4];
   const double* grid[4];
   const double* rate;
+  double inv_h[4];  // (n - 1) / (grid[n-1] - grid[0]) for ascending grids, 0: always scan in full
 };
 
 // Exciton flags

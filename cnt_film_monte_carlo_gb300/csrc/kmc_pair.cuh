@@ -8,15 +8,18 @@ namespace kmc {
 
 __device__ __forceinline__ double table_rate(const TableDev& t, double th, double zsh, double a1, double a2,
                                              double dist) {
+  auto idx = [&](int d, double x) {
+    return t.inv_h[d] > 0 ? index_min_abs_fast(t.grid[d], t.n[d], x, t.inv_h[d]) : index_min_abs(t.grid[d], t.n[d], x);
+  };
   if (t.kind == 4) {
-    int i0 = index_min_abs(t.grid[0], t.n[0], th);
-    int i1 = index_min_abs(t.grid[1], t.n[1], zsh);
-    int i2 = index_min_abs(t.grid[2], t.n[2], a1);
-    int i3 = index_min_abs(t.grid[3], t.n[3], a2);
+    int i0 = idx(0, th);
+    int i1 = idx(1, zsh);
+    int i2 = idx(2, a1);
+    int i3 = idx(3, a2);
     return t.rate[(((int64_t)i0 * t.n[1] + i1) * t.n[2] + i2) * t.n[3] + i3];
   }
-  int i0 = index_min_abs(t.grid[0], t.n[0], dist);
-  int i1 = index_min_abs(t.grid[1], t.n[1], th);
+  int i0 = idx(0, dist);
+  int i1 = idx(1, th);
   return t.rate[(int64_t)i0 * t.n[1] + i1];
 }
 

@@ -1,4 +1,4 @@
-"""Generate oracle/kmc_math_tables.h: constants for the oracle's FP64 log and acos.
+"""Generate oracle/kmc_math_tables.h: constants for the oracle's log and acos.
 
 TEST INFRASTRUCTURE (oracle). The oracle restates the reference's hot path on the
 CPU; the reference calls glibc ``std::log`` (src/monte_carlo/scatterer.h:79) and
@@ -6,14 +6,16 @@ CPU; the reference calls glibc ``std::log`` (src/monte_carlo/scatterer.h:79) and
 oracle, the shim-compiled reference (oracle/_ref) and the CUDA kernels all evaluate
 one project-defined log and acos, written from the mathematics:
 
-* log: table-driven method of P. T. P. Tang, "Table-driven implementation of the
-  logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990.
-  x = 2^k z with z in [a, 2a), a ~ 0.7012; z falls into one of 1024 intervals
-  (equal width in the bit pattern), each with a reciprocal c_i of its midpoint, so that
-  |r| = |z c_i - 1| <= 2^-11.  log x = k ln2 - log c_i + log1p(r), log1p by its Taylor
-  series r - r^2/2 + r^3/3 - r^4/4 + r^5/5 (the first omitted term is below 2^-55 |r|).
-  The interval holding 1.0 has c = 1 exactly, so the result keeps full relative
-  accuracy near x = 1.
+* log, fixed point (after the table-driven method of P. T. P. Tang, "Table-driven
+  implementation of the logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4),
+  1990): x = 2^k z with z in [a, 2a), a ~ 0.7012, z in one of 1024 intervals of equal width in
+  the bit pattern (the interval holding 1.0 has it in its middle).  Interval i has a 24-bit
+  integer reciprocal C_i = round(2^23 / midpoint) (C = 2^23 on the interval holding 1.0), so
+  r = z C_i 2^-23 - 1 is an exact integer multiple of 2^-76 (z < 1) or 2^-75 with
+  |r| <= 2^-11.  log1p(r) = r S(r), S = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 - r^5/6 evaluated in
+  Q1.62 integers; log x = k ln2 - log(C_i 2^-23) + r S is summed in a signed 128-bit integer with
+  116 fraction bits (ln2 and -log(C_i 2^-23) rounded to 2^-116) and rounded once to double
+  (nearest, ties to even).  Error below 0.52 ulp.
 * acos: acos(c) = pi/2 - asin(c) for |c| <= 1/2, 2 asin(sqrt((1-c)/2)) above,
   pi - 2 asin(sqrt((1+c)/2)) below; asin by its Taylor series
   x + sum_n (2n)!/(4^n (n!)^2 (2n+1)) x^(2n+1), 24 terms (|x| <= 1/2).
@@ -46,34 +48,8 @@ def rn(x):
     return float(mpmath.mpf(x))
 
 
-def round_to_multiple(x, ulp_exp):
-    """Round x to the nearest multiple of 2**ulp_exp (returned as a double)."""
-    q = mpmath.nint(mpmath.mpf(x) * mpmath.mpf(2) ** (-ulp_exp))
-    return float(q * mpmath.mpf(2) ** ulp_exp)
-
-
-def log_tables():
-    invc, logc_hi, logc_lo = [], [], []
-    for i in range(LOG_N):
-        lo = mpmath.mpf(b2d(LOG_OFF + i * STEP))
-        hi = mpmath.mpf(b2d(LOG_OFF + (i + 1) * STEP))
-        if i == CENTER_INDEX:
-            c = 1.0
-        else:
-            c = rn(2 / (lo + hi))
-        lc = -mpmath.log(mpmath.mpf(c))  # log(x) = k ln2 + (-log c) + log1p(z c - 1)
-        h = round_to_multiple(lc, -42)
-        invc.append(c)
-        logc_hi.append(h)
-        logc_lo.append(rn(lc - mpmath.mpf(h)))
-    assert invc[CENTER_INDEX] == 1.0 and logc_hi[CENTER_INDEX] == 0.0 and logc_lo[CENTER_INDEX] == 0.0
-    return invc, logc_hi, logc_lo
-
-
 def main():
     ln2 = mpmath.log(2)
-    ln2_hi = round_to_multiple(ln2, -42)
-    ln2_lo = rn(ln2 - mpmath.mpf(ln2_hi))
     pi = mpmath.pi
     pio2_hi = rn(pi / 2)
     pio2_lo = rn(pi / 2 - mpmath.mpf(pio2_hi))
@@ -83,35 +59,50 @@ def main():
     for n in range(1, ASIN_TERMS + 1):
         a = mpmath.factorial(2 * n) / (mpmath.mpf(4) ** n * mpmath.factorial(n) ** 2 * (2 * n + 1))
         asin_c.append(rn(a))
-    log1p_c = [rn(mpmath.mpf((-1) ** (j + 1)) / j) for j in range(2, 6)]  # -1/2, 1/3, -1/4, 1/5
-    invc, lhi, llo = log_tables()
 
     out = []
     out.append("/* Generated by oracle/gen_math_tables.py -- do not edit.")
-    out.append(" * TEST INFRASTRUCTURE (oracle): constants of the oracle's FP64 log and acos.")
+    out.append(" * TEST INFRASTRUCTURE (oracle): constants of the oracle's log and acos.")
     out.append(" * Every value is an mpmath (200-bit) result rounded once to double. */")
     out.append("#ifndef ORC_MATH_TABLES_H")
     out.append("#define ORC_MATH_TABLES_H")
     out.append("#include <stdint.h>")
     out.append(f"#define ORC_LOG_TABLE_BITS {LOG_TABLE_BITS}")
     out.append(f"#define ORC_LOG_OFF 0x{LOG_OFF:016X}ULL")
-    out.append(f"static const double ORC_LN2_HI = {ln2_hi.hex()};")
-    out.append(f"static const double ORC_LN2_LO = {ln2_lo.hex()};")
     out.append(f"static const double ORC_PIO2_HI = {pio2_hi.hex()};")
     out.append(f"static const double ORC_PIO2_LO = {pio2_lo.hex()};")
     out.append(f"static const double ORC_PI_HI = {pi_hi.hex()};")
     out.append(f"static const double ORC_PI_LO = {pi_lo.hex()};")
-    out.append("/* log1p(r) = r + r^2 * P(r), P(r) = c[0] + c[1] r + c[2] r^2 + c[3] r^3 */")
-    out.append("static const double ORC_LOG1P_C[4] = {" + ", ".join(c.hex() for c in log1p_c) + "};")
     out.append(f"/* asin(x) = x + x z Q(z), z = x^2, Q(z) = a[0] + a[1] z + ... + a[{ASIN_TERMS - 1}] z^{ASIN_TERMS - 1} */")
     out.append(f"static const double ORC_ASIN_C[{ASIN_TERMS}] = {{")
     for c in asin_c:
         out.append(f"  {c.hex()},")
     out.append("};")
-    out.append("/* per interval i: {1/c_i, hi(-log c_i) (multiple of 2^-42), lo(-log c_i)} */")
-    out.append(f"static const double ORC_LOG_TAB[{LOG_N}][3] = {{")
+    # fixed-point log tables
+    Q = 116
+    ln2q = int(mpmath.nint(ln2 * mpmath.mpf(2) ** Q))
+    out.append(f"#define ORC_FX_LN2_HI 0x{ln2q >> 64:016X}ULL")
+    out.append(f"#define ORC_FX_LN2_LO 0x{ln2q & ((1 << 64) - 1):016X}ULL")
+    s62 = [int(mpmath.nint(mpmath.mpf(v) * mpmath.mpf(2) ** 62)) for v in
+           (1, mpmath.mpf(-1) / 2, mpmath.mpf(1) / 3, mpmath.mpf(-1) / 4, mpmath.mpf(1) / 5, mpmath.mpf(-1) / 6)]
+    out.append("/* S(r) = s[0] + s[1] r + ... + s[5] r^5 in Q1.62 */")
+    out.append("static const int64_t ORC_FX_S[6] = {" + ", ".join(f"{v}LL" for v in s62) + "};")
+    out.append(f"/* per interval i: C_i (24-bit reciprocal), -log(C_i 2^-23) in Q{Q} as (hi, lo) two's complement */")
+    out.append(f"static const uint32_t ORC_FX_C[{LOG_N}] = {{")
+    cs, lcs = [], []
     for i in range(LOG_N):
-        out.append(f"  {{{invc[i].hex()}, {lhi[i].hex()}, {llo[i].hex()}}},")
+        lo_ = mpmath.mpf(b2d(LOG_OFF + i * STEP))
+        hi_ = mpmath.mpf(b2d(LOG_OFF + (i + 1) * STEP))
+        C = 1 << 23 if i == CENTER_INDEX else int(mpmath.nint(mpmath.mpf(2) ** 23 * 2 / (lo_ + hi_)))
+        lc = int(mpmath.nint(-mpmath.log(mpmath.mpf(C) / mpmath.mpf(2) ** 23) * mpmath.mpf(2) ** Q))
+        cs.append(C)
+        lcs.append(lc & ((1 << 128) - 1))
+    for i in range(0, LOG_N, 8):
+        out.append("  " + ", ".join(f"{c}u" for c in cs[i:i + 8]) + ",")
+    out.append("};")
+    out.append(f"static const uint64_t ORC_FX_LC[{LOG_N}][2] = {{")
+    for v in lcs:
+        out.append(f"  {{0x{v >> 64:016X}ULL, 0x{v & ((1 << 64) - 1):016X}ULL}},")
     out.append("};")
     out.append("#endif")
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kmc_math_tables.h")

@@ -10,10 +10,11 @@
  *    seed S is word (n mod 4) of Philox(counter = {n/4 lo, n/4 hi, s lo, s hi},
  *    key = {S lo, S hi}), shifted right by one bit, so a draw lies in [0, 2^31 - 1],
  *    the range of glibc rand() (RAND_MAX = 2^31 - 1).
- * 2. orc_log / orc_acos: the project's FP64 log and acos, which replace std::log and
- *    std::acos on every side of the parity comparison.  Method and constants:
- *    oracle/gen_math_tables.py.  Every step is an IEEE operation written out (fma() where
- *    fused), so the value is the same on any IEEE machine built with -ffp-contract=off.
+ * 2. orc_log / orc_acos: the project's log and acos, which replace std::log and std::acos on
+ *    every side of the parity comparison.  Method and constants: oracle/gen_math_tables.py.
+ *    log is integer (fixed-point) arithmetic with one final rounding; acos is IEEE operations
+ *    written out (fma() where fused); both give the same value on any machine built with
+ *    -ffp-contract=off.
  */
 #ifndef ORC_KMC_MATH_H
 #define ORC_KMC_MATH_H
@@ -96,7 +97,52 @@ static inline double orc_b2d(uint64_t b) {
   return x;
 }
 
-/* Natural logarithm (Tang's table-driven method; see oracle/gen_math_tables.py). */
+typedef __int128 orc_i128;
+typedef unsigned __int128 orc_u128;
+
+static inline int orc_bitlen128(orc_u128 m) {
+  uint64_t hi = (uint64_t)(m >> 64), lo = (uint64_t)m;
+  if (hi) return 128 - __builtin_clzll(hi);
+  return lo ? 64 - __builtin_clzll(lo) : 0;
+}
+
+/* T * 2^-116 rounded to the nearest double (ties to even); T != 0, |T| < 2^127. */
+static inline double orc_q116_to_double(orc_i128 T) {
+  uint64_t sign = 0;
+  orc_u128 m;
+  if (T < 0) {
+    sign = 1ULL << 63;
+    m = (orc_u128)(-T);
+  } else {
+    m = (orc_u128)T;
+  }
+  int L = orc_bitlen128(m);
+  uint64_t mant;
+  int e2;
+  if (L <= 53) {
+    mant = (uint64_t)m << (53 - L);
+    e2 = L - 53 - 116;
+  } else {
+    int sh = L - 53;
+    orc_u128 keep = m >> sh;
+    orc_u128 rem = m & ((((orc_u128)1) << sh) - 1);
+    orc_u128 half = ((orc_u128)1) << (sh - 1);
+    mant = (uint64_t)keep;
+    if (rem > half || (rem == half && (mant & 1))) {
+      mant++;
+      if (mant == (1ULL << 53)) {
+        mant >>= 1;
+        sh++;
+      }
+    }
+    e2 = sh - 116;
+  }
+  return orc_b2d(sign | ((uint64_t)(e2 + 52 + 1023) << 52) | (mant & ((1ULL << 52) - 1)));
+}
+
+/* Natural logarithm, fixed-point table method (constants and method: oracle/gen_math_tables.py).
+ * Every step is integer arithmetic except the final rounding, so the value is the same on any
+ * machine; error below 0.52 ulp. */
 static inline double orc_log(double x) {
   uint64_t ix = orc_d2b(x);
   if (!(x > 0.0)) {
@@ -113,19 +159,25 @@ static inline double orc_log(double x) {
   uint64_t tmp = ix - ORC_LOG_OFF;
   int i = (int)((tmp >> (52 - ORC_LOG_TABLE_BITS)) & ((1u << ORC_LOG_TABLE_BITS) - 1));
   int k = (int)((int64_t)tmp >> 52) + kadj;
-  double z = orc_b2d(ix - (tmp & 0xFFF0000000000000ULL));
-  double invc = ORC_LOG_TAB[i][0], lhi = ORC_LOG_TAB[i][1], llo = ORC_LOG_TAB[i][2];
-  double kf = (double)k;
-  double r = fma(z, invc, -1.0);
-  double t1 = fma(kf, ORC_LN2_HI, lhi); /* exact: both terms are multiples of 2^-42 below 2^11 */
-  double p = ORC_LOG1P_C[3];
-  p = fma(p, r, ORC_LOG1P_C[2]);
-  p = fma(p, r, ORC_LOG1P_C[1]);
-  p = fma(p, r, ORC_LOG1P_C[0]);
-  double r2 = r * r;
-  double q = r2 * p;
-  double s = fma(kf, ORC_LN2_LO, llo) + q;
-  return t1 + (r + s);
+  uint64_t iz = ix - (tmp & 0xFFF0000000000000ULL);
+  int ez = (int)(iz >> 52) - 1023; /* -1 or 0 */
+  uint64_t Z = (iz & ((1ULL << 52) - 1)) | (1ULL << 52);
+  /* r = z c - 1 = R 2^(ez - 75) exactly */
+  orc_i128 R = (orc_i128)((orc_u128)Z * ORC_FX_C[i]) - (((orc_i128)1) << (75 - ez));
+  int64_t r62 = (int64_t)(R >> (13 - ez)); /* r in Q1.62 */
+  int64_t t = ORC_FX_S[5];
+  for (int j = 4; j >= 0; --j) t = (int64_t)(((orc_i128)t * r62) >> 62) + ORC_FX_S[j];
+  orc_u128 aR = R < 0 ? (orc_u128)(-R) : (orc_u128)R;
+  int bl = orc_bitlen128(aR);
+  int sh = bl > 62 ? bl - 62 : 0;
+  int64_t R64 = (int64_t)(R >> sh);
+  orc_i128 P = (orc_i128)R64 * t; /* r S = P 2^(ez + sh - 137) */
+  orc_i128 L1 = P >> (21 - ez - sh);
+  orc_i128 ln2 = (orc_i128)((((orc_u128)ORC_FX_LN2_HI) << 64) | ORC_FX_LN2_LO);
+  orc_i128 lc = (orc_i128)((((orc_u128)ORC_FX_LC[i][0]) << 64) | ORC_FX_LC[i][1]);
+  orc_i128 T = (orc_i128)k * ln2 + lc + L1;
+  if (T == 0) return 0.0;
+  return orc_q116_to_double(T);
 }
 
 /* asin on |x| <= 1/2 by its Taylor series. */

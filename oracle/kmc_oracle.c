@@ -780,6 +780,9 @@ void orc_sim_destroy(orc_sim* s) {
 }
 
 double orc_log_export(double x) { return orc_log(x); }
+void orc_log_array(const double* x, double* out, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) out[i] = orc_log(x[i]);
+}
 double orc_acos_export(double x) { return orc_acos(x); }
 void orc_philox_export(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { orc_philox4x32_10(ctr, key, out); }
 int orc_rand_export(uint64_t seed, uint64_t stream, uint64_t n) {

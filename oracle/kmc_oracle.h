@@ -102,6 +102,7 @@ int64_t orc_sim_total_crossings(const orc_sim* s);
 
 /* Exposed pieces for known-answer tests. */
 double orc_log_export(double x);
+void orc_log_array(const double* x, double* out, int64_t n);
 double orc_acos_export(double x);
 void orc_philox_export(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 int orc_rand_export(uint64_t seed, uint64_t stream, uint64_t n);

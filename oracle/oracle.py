@@ -80,6 +80,7 @@ def lib():
         L.orc_sim_total_crossings.restype = I64
         L.orc_log_export.argtypes = [D]
         L.orc_log_export.restype = D
+        L.orc_log_array.argtypes = [PD, PD, I64]
         L.orc_acos_export.argtypes = [D]
         L.orc_acos_export.restype = D
         L.orc_philox_export.argtypes = [PU32, PU32, PU32]
@@ -99,6 +100,13 @@ def _p(a, t):
 
 def log(x: float) -> float:
     return lib().orc_log_export(float(x))
+
+
+def log_array(x):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros_like(x)
+    lib().orc_log_array(_p(x, D), _p(out, D), len(x))
+    return out
 
 
 def acos(x: float) -> float:

@@ -42,10 +42,11 @@ def test_dwell_uniform_exact_for_every_rand_value(eng):
 
 def test_device_log_acos_match_oracle(eng):
     rng = np.random.default_rng(3)
-    x = np.concatenate([rng.uniform(0, 1, 20000), [r / 2147483647.0 for r in rng.integers(1, 2**31 - 1, 20000)],
-                        np.exp(rng.uniform(-700, 700, 5000)), [1.0, 0.5, 2.0, 5e-324]])
+    r = rng.integers(1, 2**31, 400000)
+    x = np.concatenate([r / 2147483647.0, rng.uniform(0, 1, 100000), np.exp(rng.uniform(-700, 700, 50000)),
+                        [1.0, 0.5, 2.0, 5e-324, 2.2250738585072014e-308, 1 - 2.0**-53, 1 + 2.0**-52]])
     lo, _ = eng.math_probe(x)
-    assert np.array_equal(lo, np.array([O.log(v) for v in x]))
+    assert np.array_equal(lo.view(np.uint64), O.log_array(x).view(np.uint64))
     c = np.concatenate([rng.uniform(-1, 1, 20000), [1.0, -1.0, 0.5, -0.5, 0.0, 0.9999999999]])
     _, ac = eng.math_probe(c)
     assert np.array_equal(ac, np.array([O.acos(v) for v in c]))
@@ -346,3 +347,30 @@ def test_mixed_variants_and_autotune_do_not_change_results():
         assert_states_equal(g, states[0][0])
         assert_msd_close(m, states[0][1])
         assert h == states[0][2]
+
+
+@pytest.mark.parametrize("table_kind", [2, 4])
+def test_random_geometry_csr_matches_oracle(table_kind):
+    # sites at random points with random axes (each a one-site tube): pair distances and angles
+    # sweep the table grids densely, so every nearest-grid tie and window edge is exercised
+    rng = np.random.default_rng(11)
+    n = 3000
+    pos = rng.uniform(0, 40e-9, size=(n, 3))
+    ax = rng.normal(size=(n, 3))
+    ax /= np.linalg.norm(ax, axis=1)[:, None]
+    lk = np.full(n, -1, np.int32)
+    rk = np.full(n, -1, np.int32)
+    if table_kind == 2:
+        tab = tables.forster_2d(1e15)
+    else:
+        tab = E.forster_table(1e15, (0, 180, 21), (1.5e-9, 10e-9, 11), (-10e-9, 10e-9, 11), (-10e-9, 10e-9, 11))
+    sim = O.Sim(pos, ax, lk, rk, tab, 8e-9, 2e5, n_threads=4)
+    csr = sim.build_csr()
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, n], np.int64), pos, ax, lk, rk)
+    e.set_table(tab)
+    st = e.build(8e-9)
+    nb = e.neighbors(n, st["nnz"])
+    for k in ("rowptr", "col", "cum", "total"):
+        assert np.array_equal(nb[k], csr[k]), k
+    e.close()
