@@ -69,8 +69,8 @@ struct kmc_ctx {
   double r_max = 0;
   int64_t nnz = 0, n_cells = 0;
   DevBuf<int64_t> d_cell_of, d_cell_start, d_cell_cursor, d_rowptr, d_scan;
-  DevBuf<int32_t> d_cell_members, d_col;
-  DevBuf<double> d_cum, d_total, d_inv_total;
+  DevBuf<int32_t> d_cell_members;
+  DevBuf<double> d_total, d_inv_total;
   DevBuf<int64_t> d_blkptr;
   DevBuf<kmc::RowBlock> d_blocks;
   DevBuf<float> d_blast;
@@ -171,11 +171,11 @@ void kmc_destroy(kmc_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (auto* b : {&c->d_orient, &c->d_cum, &c->d_total, &c->d_inv_total, &c->d_rate, &c->d_e_pos, &c->d_e_delta,
+  for (auto* b : {&c->d_orient, &c->d_total, &c->d_inv_total, &c->d_rate, &c->d_e_pos, &c->d_e_delta,
                   &c->d_e_ff, &c->d_msd})
     b->release();
   for (auto& g : c->d_grid) g.release();
-  for (auto* b : {&c->d_left, &c->d_right, &c->d_site_film, &c->d_cell_members, &c->d_col, &c->d_warp_film,
+  for (auto* b : {&c->d_left, &c->d_right, &c->d_site_film, &c->d_cell_members, &c->d_warp_film,
                   &c->d_inject, &c->d_e_site, &c->d_trace, &c->d_err})
     b->release();
   for (auto* b : {&c->d_cell_of, &c->d_cell_start, &c->d_cell_cursor, &c->d_rowptr, &c->d_scan, &c->d_trace_cnt})
@@ -367,8 +367,6 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
     if (c->films[i].nnz >= (1LL << 32)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: film %d has >= 2^32 neighbour entries", i);
   }
   CK(c, cudaMemcpyAsync(c->d_films.p, c->films.data(), c->films.size() * sizeof(FilmDev), cudaMemcpyHostToDevice, c->stream));
-  CK(c, c->d_col.alloc(c->nnz));
-  CK(c, c->d_cum.alloc(c->nnz));
   CK(c, c->d_blocks.alloc(c->nblk));
   CK(c, c->d_blast.alloc(c->nblk));
   CK(c, c->d_cump.alloc(c->nblk * 8));
@@ -376,8 +374,6 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, c->d_inv_total.alloc(n));
   CK(c, c->d_rec.alloc(n));
   CK(c, c->d_lt64.alloc(n));
-  a.col = c->d_col.p;
-  a.cum = c->d_cum.p;
   a.blocks = c->d_blocks.p;
   a.blast = c->d_blast.p;
   a.cump = c->d_cump.p;
@@ -544,8 +540,7 @@ static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   a.left = c->d_left.p;
   a.right = c->d_right.p;
   a.rowptr = c->d_rowptr.p;
-  a.col = c->d_col.p;
-  a.cum = c->d_cum.p;
+  a.blkptr = c->d_blkptr.p;
   a.total = c->d_total.p;
   a.inv_total = c->d_inv_total.p;
   a.rec = c->d_rec.p;
@@ -830,15 +825,24 @@ int kmc_get_neighbors(kmc_ctx* c, int64_t* rowptr, int32_t* col, double* cum, do
   if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_get_neighbors: not built");
   CK(c, cudaSetDevice(c->device));
   const int64_t n = c->n_sites;
-  if (rowptr) CK(c, cudaMemcpy(rowptr, c->d_rowptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
-  if (cum) CK(c, cudaMemcpy(cum, c->d_cum.p, c->nnz * 8, cudaMemcpyDeviceToHost));
+  std::vector<int64_t> rp(n + 1), bp(n + 1);
+  CK(c, cudaMemcpy(rp.data(), c->d_rowptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
+  if (rowptr) std::copy(rp.begin(), rp.end(), rowptr);
   if (total) CK(c, cudaMemcpy(total, c->d_total.p, n * 8, cudaMemcpyDeviceToHost));
-  if (col) {
-    CK(c, cudaMemcpy(col, c->d_col.p, c->nnz * 4, cudaMemcpyDeviceToHost));
-    for (int32_t f = 0; f < c->n_films; ++f) {
-      const FilmDev& fd = c->films[f];
-      for (int64_t i = fd.nnz0; i < fd.nnz0 + fd.nnz; ++i) col[i] -= (int32_t)fd.site0;
-    }
+  if (!col && !cum) return KMC_OK;
+  CK(c, cudaMemcpy(bp.data(), c->d_blkptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
+  // rows are stored in 8-entry blocks; gather them back into the reference's CSR layout
+  std::vector<kmc::RowBlock> blocks(c->nblk);
+  std::vector<double> cump(c->nblk * 8);
+  CK(c, cudaMemcpy(blocks.data(), c->d_blocks.p, c->nblk * sizeof(kmc::RowBlock), cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(cump.data(), c->d_cump.p, c->nblk * 8 * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int32_t f = 0; f < c->n_films; ++f) {
+    const FilmDev& fd = c->films[f];
+    for (int64_t s = fd.site0; s < fd.site0 + fd.n_sites; ++s)
+      for (int64_t k = 0; k < rp[s + 1] - rp[s]; ++k) {
+        if (col) col[rp[s] + k] = blocks[bp[s] + (k >> 3)].col[k & 7] - (int32_t)fd.site0;
+        if (cum) cum[rp[s] + k] = cump[bp[s] * 8 + k];
+      }
   }
   return KMC_OK;
 }

@@ -200,14 +200,14 @@ __device__ __forceinline__ double q116_to_double(I128 T) {
 }
 
 // log(x) for a normal x > 0 (kadj: exponent correction of a pre-scaled subnormal)
-__device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const LogTab* __restrict__ tab) {
+__device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const LogTab* tab) {
   const uint64_t tmp = ix - KMC_LOG_OFF;
   const int i = (int)((tmp >> (52 - KMC_LOG_TABLE_BITS)) & ((1u << KMC_LOG_TABLE_BITS) - 1));
   const int k = (int)((int64_t)tmp >> 52) + kadj;
   const uint64_t iz = ix - (tmp & 0xFFF0000000000000ull);
   const int ez = (int)(iz >> 52) - 1023;  // -1 or 0
   const uint64_t Z = (iz & ((1ull << 52) - 1)) | (1ull << 52);
-  const uint64_t C = __ldg(&tab->t[i][0]);
+  const uint64_t C = tab->t[i][0];
   // R = Z C - 2^(75 - ez): the subtrahend is 2^(11 - ez) in the high word
   I128 R;
   R.lo = Z * C;
@@ -232,8 +232,8 @@ __device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const Log
   kl.hi = (int64_t)(ka * KMC_FX_LN2_HI + __umul64hi(ka, KMC_FX_LN2_LO));
   if (k < 0) kl = neg128(kl);
   I128 lc;
-  lc.lo = __ldg(&tab->t[i][2]);
-  lc.hi = (int64_t)__ldg(&tab->t[i][1]);
+  lc.lo = tab->t[i][2];
+  lc.hi = (int64_t)tab->t[i][1];
   const I128 T = add128(add128(kl, lc), L1);
   if (T.hi == 0 && T.lo == 0) return 0.0;
   return q116_to_double(T);
@@ -253,7 +253,7 @@ __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ t
 }
 
 // kmc_log for the dwell-time uniforms, which are normal numbers in (0, 1]: no special cases.
-__device__ __forceinline__ double kmc_log_unit(double x, const LogTab* __restrict__ tab) {
+__device__ __forceinline__ double kmc_log_unit(double x, const LogTab* tab) {
   return log_fx_normal((uint64_t)__double_as_longlong(x), 0, tab);
 }
 

@@ -65,8 +65,7 @@ struct HopArgs {
   const int32_t* left;
   const int32_t* right;
   const int64_t* rowptr;  // global
-  const int32_t* col;     // global site ids
-  const double* cum;
+  const int64_t* blkptr;  // first row block of each site (global)
   const double* total;
   const double* inv_total;
   const SiteRec* rec;
@@ -116,8 +115,6 @@ struct BuildArgs {
   double r_max;
   int64_t* counts;         // [n + 1] -> rowptr
   int64_t* rowptr;
-  int32_t* col;
-  double* cum;
   double* total;
   double* inv_total;
   int64_t* blkptr;         // [n + 1] first block of each row (global)

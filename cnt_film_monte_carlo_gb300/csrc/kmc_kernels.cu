@@ -128,7 +128,8 @@ __global__ void k_nbr_fill(BuildArgs a) {
   const FilmDev& f = a.films[a.site_film[s]];
   double4_32a p1 = a.pos4[s];
   double a1v[3] = {a.orient[3 * s], a.orient[3 * s + 1], a.orient[3 * s + 2]};
-  int64_t b = a.rowptr[s];
+  const int64_t bo = a.blkptr[s];
+  double* cump = a.cump + bo * 8;  // this row's FP64 cumulative rates (8 per block)
   int64_t k = 0;
   double run = 0.0;
   bool negative = false;
@@ -137,8 +138,8 @@ __global__ void k_nbr_fill(BuildArgs a) {
     double rate = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance);
     negative |= rate < 0;
     run = (k == 0) ? rate : run + rate;  // in-place inclusive prefix sum, scatterer.cpp:78-80
-    a.col[b + k] = q;
-    a.cum[b + k] = run;
+    cump[k] = run;
+    a.blocks[bo + (k >> 3)].col[k & 7] = q;
     ++k;
   });
   double tot = k > 0 ? run : 0.0;
@@ -147,28 +148,23 @@ __global__ void k_nbr_fill(BuildArgs a) {
   a.inv_total[s] = inv;
   bool exact = negative || !(tot > 0.0) || !(tot < __longlong_as_double(0x7FF0000000000000ll));
   if (exact && k > 0) atomicAdd(&a.stats[2], 1ull);
-  // blocked copy of the row for the mixed kernel: 8 entries per 64-byte block
+  // FP32 normalised values, padding, second and first search levels
   const float kInf = __int_as_float(0x7f800000);
-  const int64_t bo = a.blkptr[s];
   const int64_t nb = (k + 7) / 8;
   for (int64_t j = 0; j < nb; ++j) {
-    RowBlock blk;
+    RowBlock& blk = a.blocks[bo + j];
     for (int i = 0; i < 8; ++i) {
       int64_t q = 8 * j + i;
       if (q < k) {
-        double cv = a.cum[b + q];
-        blk.c[i] = exact ? 0.0f : (float)(cv / tot);
-        blk.col[i] = a.col[b + q];
-        a.cump[(bo + j) * 8 + i] = cv;
+        blk.c[i] = exact ? 0.0f : (float)(cump[q] / tot);
       } else {
         blk.c[i] = kInf;
         blk.col[i] = -1;
-        a.cump[(bo + j) * 8 + i] = __longlong_as_double(0x7FF0000000000000ll);
+        cump[q] = __longlong_as_double(0x7FF0000000000000ll);
       }
     }
-    a.blocks[bo + j] = blk;
     int64_t last = min(8 * j + 7, k - 1);
-    a.blast[bo + j] = exact ? 0.0f : (float)(a.cum[b + last] / tot);
+    a.blast[bo + j] = exact ? 0.0f : (float)(cump[last] / tot);
   }
   SiteRec r;
   r.inv_total = inv;
@@ -182,7 +178,7 @@ __global__ void k_nbr_fill(BuildArgs a) {
   for (int i = 0; i < 8; ++i) {
     if (i * G < nb && !exact) {
       int64_t last = min(8 * G * (i + 1) - 1, k - 1);
-      r.coarse[i] = (float)(a.cum[b + last] / tot);
+      r.coarse[i] = (float)(cump[last] / tot);
     } else {
       r.coarse[i] = kInf;
     }
@@ -537,20 +533,21 @@ __global__ void __launch_bounds__(256) k_hop_fp64(HopArgs a, int64_t n_steps) {
         rem -= e.ff;
         fly_full(a, e, e.ff);
         int32_t ns = e.site;
-        int64_t b = a.rowptr[e.site];
-        int64_t n = a.rowptr[e.site + 1] - b;
+        int64_t n = a.rowptr[e.site + 1] - a.rowptr[e.site];
         if (n > 0) {  // update_state, scatterer.cpp:14-30
+          const int64_t bo = a.blkptr[e.site];
+          const double* cum = a.cump + bo * 8;
           uint32_t r = e.g.next();
           double dice = a.total[e.site] * (double)r / (double)kRandMax;
           unsigned left = (unsigned)-1, right = (unsigned)(n - 1);
           while (left + 1 < right) {
             unsigned mid = (left + right) / 2;
-            if (a.cum[b + mid] <= dice)
+            if (cum[mid] <= dice)
               left = mid;
             else
               right = mid;
           }
-          ns = a.col[b + right];
+          ns = a.blocks[bo + (right >> 3)].col[right & 7];
         }
         e.hops++;
         trace_push(a, e, ns);
@@ -677,13 +674,18 @@ template <int MINB>
 __global__ void __launch_bounds__(128, MINB) k_hop_mixed(HopArgs a, int64_t n_steps, unsigned long long* queue,
                                                          int single_film) {
   extern __shared__ double s_mem[];
-  double* s_bins = s_mem;  // [n_steps][3] when single_film
-  ColdState* cs = reinterpret_cast<ColdState*>(s_mem + (single_film ? n_steps * 3 : 0)) + threadIdx.x;
+  LogTab* s_log = reinterpret_cast<LogTab*>(s_mem);  // the log table, read once per hop
+  double* s_bins = s_mem + sizeof(LogTab) / sizeof(double);  // [n_steps][3] when single_film
+  ColdState* cs = reinterpret_cast<ColdState*>(s_bins + (single_film ? n_steps * 3 : 0)) + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  if (single_film) {
-    for (int64_t i = threadIdx.x; i < n_steps * 3; i += blockDim.x) s_bins[i] = 0.0;
-    __syncthreads();
+  {
+    const uint64_t* src = &a.logtab->t[0][0];
+    uint64_t* dst = &s_log->t[0][0];
+    for (int i = threadIdx.x; i < (int)(sizeof(LogTab) / 8); i += blockDim.x) dst[i] = __ldg(src + i);
   }
+  if (single_film)
+    for (int64_t i = threadIdx.x; i < n_steps * 3; i += blockDim.x) s_bins[i] = 0.0;
+  __syncthreads();
   const float lo_m = 1.0f - 0x1p-20f, hi_m = 1.0f + 0x1p-20f;
   uint64_t exact = 0, lane_hops = 0, lane_cross = 0;
   // hot state
@@ -936,7 +938,7 @@ __global__ void __launch_bounds__(128, MINB) k_hop_mixed(HopArgs a, int64_t n_st
       uint32_t r;
       while ((r = cold_next(rn, cs, w0, w1, w2, w3)) == 0) {
       }
-      ff = -inv * kmc_log_unit(u_from_rand(r), a.logtab);
+      ff = -inv * kmc_log_unit(u_from_rand(r), s_log);
       if (++hs > a.hop_cap) {  // leave this exciton where it is and report
         atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
         Exciton e;
@@ -1048,7 +1050,7 @@ template <int MINB>
 static cudaError_t launch_mixed_t(const HopArgs& a, int64_t n_steps, int grid_blocks, int single_film,
                                   unsigned long long* queue, cudaStream_t s) {
   const int block = 128;
-  size_t smem = (single_film ? (size_t)n_steps * 3 * sizeof(double) : 0) + block * sizeof(ColdState);
+  size_t smem = sizeof(LogTab) + (single_film ? (size_t)n_steps * 3 * sizeof(double) : 0) + block * sizeof(ColdState);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_hop_mixed<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1064,7 +1066,7 @@ static cudaError_t launch_mixed_t(const HopArgs& a, int64_t n_steps, int grid_bl
 template <int MINB>
 static int blocks_per_sm_t(int64_t n_steps, int single_film) {
   int nb = 0;
-  size_t smem = (single_film ? (size_t)n_steps * 3 * sizeof(double) : 0) + 128 * sizeof(ColdState);
+  size_t smem = sizeof(LogTab) + (single_film ? (size_t)n_steps * 3 * sizeof(double) : 0) + 128 * sizeof(ColdState);
   if (smem > 48 * 1024) cudaFuncSetAttribute(k_hop_mixed<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_hop_mixed<MINB>, 128, smem) != cudaSuccess) return 1;
   return nb > 0 ? nb : 1;
