@@ -36,21 +36,37 @@ METRIC = "exciton hops/s (Green-Kubo hop kernel)"
 UNIT = "hops/s"
 
 
-def workload():
+def workload(name="cfg2", films=256):
+    """(list of films, rate table, excitons per film, description)."""
     from cnt_film_monte_carlo_gb300 import film as F
     from cnt_film_monte_carlo_gb300 import tables
 
+    tab = tables.forster_2d(1e15)
+    if name == "cfg4":
+        f = F.lognormal_tubes(20000, 500.0, 0.4, (5000.0, 5000.0, 50.0), seed=7)
+        return [f], tab, [10_000_000], ("cfg4 film: 20,000 tubes, lognormal length (median 500 nm, sigma 0.4), "
+                                          "5x5 um x 50 nm box, 1 nm segments, 10 nm cutoff, 2-D rate table")
+    if name == "cfg3":
+        out, ne = [], []
+        for i in range(films):
+            rng = np.random.default_rng(i)
+            n_t = int(rng.integers(50, 2001))
+            out.append(F.lognormal_tubes(n_t, 300.0, 0.5, (1000.0, 1000.0, 20.0), seed=i))
+            ne.append(100 * n_t)
+        return out, tab, ne, (f"cfg3 batch: {films} films, tubes U{{50..2000}}, lognormal length (median 300 nm, "
+                               "sigma 0.5), 1000x1000x20 nm boxes, 1 nm segments, 10 nm cutoff, 100 excitons per tube, "
+                               "one persistent launch")
     f = F.straight_tubes(FILM["n_tubes"], FILM["length_nm"], box_nm=FILM["box_nm"], max_tilt_deg=FILM["tilt_deg"],
                          seed=FILM["film_seed"])
-    return f, tables.forster_2d(1e15)
+    return [f], tab, [N_EXC], ("cfg2 film: 100 tubes x 200 nm, 500x500x10 nm, 1 nm segments, 10 nm cutoff, "
+                               "2-D rate table")
 
 
-def config(n_exc, bins_per_step, extra=None):
-    c = {"workload": "cfg2 film: 100 tubes x 200 nm, 500x500x10 nm, 1 nm segments, 10 nm cutoff, 2-D rate table; "
-                     f"{n_exc} excitons uniform injection; MSD bin 1 ps; {bins_per_step} bin(s) per step",
-         "n_sites": FILM["n_tubes"] * int(FILM["length_nm"]), "n_excitons": n_exc, "bin_s": BIN,
+def config(desc, n_sites, n_exc, bins_per_step, extra=None):
+    c = {"workload": f"{desc}; {n_exc} excitons uniform injection; MSD bin 1 ps; {bins_per_step} bin(s) per step",
+         "n_sites": n_sites, "n_excitons": n_exc, "bin_s": BIN,
          "bins_per_step": bins_per_step, "precision": "mixed (FP32 cumulative rates, exact FP64 re-resolve)",
-         "l2": "256 MB buffer written between timed steps (working set ~15 MB CSR is L2-resident by size)"}
+         "l2": "256 MB buffer written between timed steps"}
     if extra:
         c.update(extra)
     return c
@@ -116,42 +132,58 @@ def bytes_per_hop(k_mean):
     return 128 if k_mean <= 64 else 160
 
 
-def cpu_sample(f, tab, target_cpu_s=15.0, threads=None, steps=1):
+class CpuSample:
     """The reference's algorithm on the host cores: the oracle restatement with a fresh neighbour
-    search on every hop (scatterer.cpp:9-31), OpenMP over excitons."""
-    from oracle import oracle as O
+    search on every hop (scatterer.cpp:9-31), OpenMP over excitons.  A short pilot fixes the number
+    of excitons so that one sample (all of them advanced by one 1 ps bin from their injection) takes
+    about `seconds` of wall time."""
 
-    threads = threads or os.cpu_count() or 1
-    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, R_MAX, VEL, n_threads=threads)
-    n = max(threads * 4, 64)
-    sim.create_excitons(1, 0, n, SEED, use_csr=False)
-    t0 = time.perf_counter()
-    sim.step(BIN / 20, 1)
-    dt = time.perf_counter() - t0
-    rate = sim.total_hops() / max(dt, 1e-9)
-    hops_per_exc_bin = max(sim.total_hops() / n * 20, 1.0)
-    n = int(max(threads, min(N_EXC, target_cpu_s / threads * rate / hops_per_exc_bin / steps)))
-    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, R_MAX, VEL, n_threads=threads)
-    sim.create_excitons(1, 0, n, SEED, use_csr=False)
-    t0 = time.perf_counter()
-    sim.step(BIN, steps)
-    dt = time.perf_counter() - t0
-    return sim.total_hops() / dt, threads, f"{n} excitons x {steps} x 1 ps bins of the same film ({sim.total_hops()} hops, {dt:.2f} s)"
+    def __init__(self, f, tab, seconds=10.0, threads=None):
+        from oracle import oracle as O
+
+        self.O, self.f, self.tab = O, f, tab
+        self.threads = threads or os.cpu_count() or 1
+        n = max(self.threads * 16, 128)
+        sim = self._sim(n)
+        t0 = time.perf_counter()
+        sim.step(BIN / 20, 1)
+        dt = time.perf_counter() - t0
+        rate = max(sim.total_hops(), 1) / max(dt, 1e-9)
+        hops_per_exc_bin = max(sim.total_hops() / n * 20, 1.0)
+        self.n = int(max(self.threads, min(N_EXC, seconds * rate / hops_per_exc_bin)))
+
+    def _sim(self, n):
+        f = self.f
+        sim = self.O.Sim(f.pos_m(), f.orient, f.left, f.right, self.tab, R_MAX, VEL, n_threads=self.threads)
+        sim.create_excitons(1, 0, n, SEED, use_csr=False)
+        return sim
+
+    def run(self):
+        sim = self._sim(self.n)
+        t0 = time.perf_counter()
+        sim.step(BIN, 1)
+        dt = time.perf_counter() - t0
+        hops = sim.total_hops()
+        return hops / dt, f"{self.n} excitons x one 1 ps bin of the same film ({hops} hops, {dt:.2f} s)"
 
 
 def reference_arm(args):
-    f, tab = workload()
-    vals = []
+    films, tab, _, desc = workload(args.workload, args.films)
+    f = films[0]
+    # whole run within a few minutes: every step gets an equal share of ~150 s
+    per_step = min(args.cpu_seconds, 150.0 / max(args.steps + args.warmup, 1))
+    cs = CpuSample(f, tab, seconds=per_step)
+    vals, sample = [], ""
     for i in range(args.warmup + args.steps):
-        v, cores, sample = cpu_sample(f, tab, target_cpu_s=args.cpu_seconds)
+        v, sample = cs.run()
         if i >= args.warmup:
             vals.append(v)
     value = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config(N_EXC, 1, {"sample": sample}),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "config": config(desc, films[0].n_sites, N_EXC, 1, {"sample": sample}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cs.threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -162,10 +194,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n-exc", type=int, default=N_EXC)
+    ap.add_argument("--n-exc", type=int, default=None, help="excitons per film (default: the workload's)")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4"])
+    ap.add_argument("--films", type=int, default=256, help="films of the cfg3 batch")
     ap.add_argument("--bins-per-step", type=int, default=1)
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall seconds of one CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
@@ -198,13 +232,17 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    f, tab = workload()
+    films, tab, n_exc, desc = workload(args.workload, args.films)
+    if args.n_exc is not None:
+        n_exc = [args.n_exc] * len(films)
+    n_exc_total = int(sum(n_exc))
+    f = films[0]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     e = E.Engine(local)
-    e.load_films(f)
+    e.load_films(films)
     e.set_table(tab)
     st = e.build(R_MAX)
-    e.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+    e.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
     bins = args.bins_per_step
     if args.variant is not None:
         e.set_mixed_variant(args.variant)
@@ -226,9 +264,8 @@ def main():
         barrier()
         wall = time.perf_counter() - t0
     hops = e.stats()["hops"] - h0
-    msd = e.msd(0, e.stats()["steps_done"])[0]
     t_end = e.stats()["steps_done"] * BIN
-    d_eff = (msd[-1] / args.n_exc / (2 * t_end)).tolist()
+    d_eff = (e.msd(0, e.stats()["steps_done"])[:, -1].sum(axis=0) / n_exc_total / (2 * t_end)).tolist()
     e.close()
     dev_s = dev_ms / 1e3
     if dist is not None:
@@ -245,10 +282,10 @@ def main():
     fp64 = None
     if args.fp64_steps > 0:
         e2 = E.Engine(local)
-        e2.load_films(f)
+        e2.load_films(films)
         e2.set_table(tab)
         e2.build(R_MAX)
-        e2.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+        e2.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
         e2.run(args.warmup * bins, BIN, VEL, L.KMC_PREC_FP64)
         h1 = e2.stats()["hops"]
         ms = 0.0
@@ -266,10 +303,10 @@ def main():
         barrier()
         t0 = time.perf_counter()
         e3 = E.Engine(local)
-        e3.load_films(f)
+        e3.load_films(films)
         e3.set_table(tab)
         e3.build(R_MAX)
-        e3.init_excitons(args.n_exc, SEED + rank, L.KMC_INJECT_UNIFORM)
+        e3.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
         if tune:
             e3.set_mixed_variant(tune["variant"])
             e3.set_launch_config(128, tune["steps_per_launch"])
@@ -282,7 +319,8 @@ def main():
         e3.close()
         barrier()
         w3 = time.perf_counter() - t0
-        h2d = f.n_sites * (3 * 8 * 2 + 2 * 4) + 8 * 2 + tab["rate"].nbytes + sum(g.nbytes for g in tab["grids"]) + 16
+        n_all = sum(x.n_sites for x in films)
+        h2d = n_all * (3 * 8 * 2 + 2 * 4) + 8 * (len(films) + 1) + tab["rate"].nbytes + sum(g.nbytes for g in tab["grids"])
         e2e = {"value": h3 * world / w3, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                "d2h_bytes_per_step": int(out.nbytes / args.steps), "seconds": w3,
                "includes": "film+table upload, neighbour build, exciton creation, K steps, MSD read-back"}
@@ -302,7 +340,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64+f32", "data": "synthetic",
-        "config": config(args.n_exc, bins, {"k_mean": st["k_mean"], "k_max": st["k_max"], "nnz": st["nnz"], "hops_timed": hops}),
+        "config": config(desc, st["n_sites"], n_exc_total, bins,
+                         {"films": len(films), "k_mean": st["k_mean"], "k_max": st["k_max"], "nnz": st["nnz"],
+                          "hops_timed": hops, "build_ms": st["build_ms"]}),
         "fp64_plain_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "d_eff_m2_per_s": d_eff,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -314,8 +354,9 @@ def main():
         "clocks": clk.summary(),
     }
     if world == 1 and not args.no_cpu:
-        v, cores, sample = cpu_sample(f, tab, target_cpu_s=args.cpu_seconds)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cs = CpuSample(f, tab, seconds=args.cpu_seconds)
+        v, sample = cs.run()
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cs.threads, "kind": "port", "sample": sample}
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
