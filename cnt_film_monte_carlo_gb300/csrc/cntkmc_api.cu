@@ -653,7 +653,6 @@ int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_
   DevBuf<uint32_t> b_flags;
   DevBuf<double> b_pos, b_delta, b_ff, t_msd;
   DevBuf<uint64_t> b_draws, b_hops;
-  DevBuf<int64_t> b_tcnt;
   CK(c, b_site.alloc(ns));
   CK(c, b_flags.alloc(ns));
   CK(c, b_pos.alloc(3 * ns));

@@ -1,0 +1,165 @@
+// kmc_hop_common.cuh -- device pieces shared by the hop kernels: exciton state in registers,
+// fly from a materialised position, load/store of the slot arrays, removal and reinjection,
+// counters.  Included by kmc_kernels.cu and the two translation units of the mixed kernel.
+#pragma once
+
+#include "kmc_internal.h"
+
+namespace kmc {
+
+#define KMC_ERR_HOP_CAP_CODE 1
+#define KMC_ERR_CELL_CODE 2
+#define KMC_ERR_FLIGHT_CODE 4
+// Upper bound of link crossings in one free flight: a flight of length v*dt over links of
+// positive length ends long before; only zero-length links (coincident sites) could loop.
+constexpr int kMaxCrossings = 1 << 22;
+
+struct Exciton {
+  int32_t site;
+  bool heading, at_site, active;
+  double px, py, pz, dx, dy, dz, ff;
+  Rng g;
+  uint64_t hops, crossings;
+  int64_t trace_i;
+};
+
+__device__ __forceinline__ void trace_push(const HopArgs& a, const Exciton& e, int32_t v) {
+  if (e.trace_i >= 0) {
+    int64_t c = a.trace_cnt[e.trace_i];
+    if (c < a.trace_cap) a.trace[e.trace_i * a.trace_cap + c] = v;
+    a.trace_cnt[e.trace_i] = c + 1;
+  }
+}
+
+// particle::fly (particle.cpp:9-54) in FP64 from a materialised position.
+__device__ __forceinline__ void fly_full(const HopArgs& a, Exciton& e, double dtf) {
+  if (a.left[e.site] < 0 && a.right[e.site] < 0) return;
+  for (int guard = 0;; ++guard) {
+    if (guard >= kMaxCrossings) {
+      atomicOr(a.err, KMC_ERR_FLIGHT_CODE);
+      return;
+    }
+    int32_t l = a.left[e.site], r = a.right[e.site];
+    int32_t next = e.heading ? (r > -1 ? r : l) : (l > -1 ? l : r);
+    e.heading = (next == r);
+    double4_32a t = a.pos4[next];
+    double dist = norm3(e.px - t.x, e.py - t.y, e.pz - t.z);
+    if (dist / a.v < dtf) {
+      e.px = t.x;
+      e.py = t.y;
+      e.pz = t.z;
+      e.site = next;
+      dtf -= dist / a.v;
+      e.crossings++;
+      trace_push(a, e, -1 - next);
+    } else {
+      double e0 = t.x - e.px, e1 = t.y - e.py, e2 = t.z - e.pz;
+      double nn = norm3(e0, e1, e2);
+      double den = nn != 0 ? nn : 1.0;
+      double u0 = e0 / den, u1 = e1 / den, u2 = e2 / den;
+      double k = a.v * dtf;
+      e.px = e.px + k * u0;
+      e.py = e.py + k * u1;
+      e.pz = e.pz + k * u2;
+      return;
+    }
+  }
+}
+
+__device__ __forceinline__ void load_exciton(const HopArgs& a, int64_t slot, Exciton& e) {
+  const int64_t ns = a.n_slots;
+  uint32_t fl = a.e_flags[slot];
+  e.active = (fl & kExActive) != 0;
+  e.heading = (fl & kExHeading) != 0;
+  e.at_site = (fl & kExAtSite) != 0;
+  e.site = a.e_site[slot];
+  e.px = a.e_pos[slot];
+  e.py = a.e_pos[ns + slot];
+  e.pz = a.e_pos[2 * ns + slot];
+  e.dx = a.e_delta[slot];
+  e.dy = a.e_delta[ns + slot];
+  e.dz = a.e_delta[2 * ns + slot];
+  e.ff = a.e_ff[slot];
+  e.hops = 0;
+  e.crossings = 0;
+}
+
+__device__ __forceinline__ void store_exciton(const HopArgs& a, int64_t slot, const Exciton& e) {
+  const int64_t ns = a.n_slots;
+  if (!e.active) return;
+  a.e_flags[slot] = kExActive | (e.heading ? kExHeading : 0u) | (e.at_site ? kExAtSite : 0u);
+  a.e_site[slot] = e.site;
+  a.e_pos[slot] = e.px;
+  a.e_pos[ns + slot] = e.py;
+  a.e_pos[2 * ns + slot] = e.pz;
+  a.e_delta[slot] = e.dx;
+  a.e_delta[ns + slot] = e.dy;
+  a.e_delta[2 * ns + slot] = e.dz;
+  a.e_ff[slot] = e.ff;
+  a.e_draws[slot] = e.g.n;
+  a.e_hops[slot] += e.hops;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Removal and reinjection (monte_carlo.cpp:330-336); position must be materialised.
+__device__ __forceinline__ void maybe_reinject(const HopArgs& a, const FilmDev& f, Exciton& e) {
+  if (f.mode != 0) return;
+  bool out = (e.px < f.rmin[0]) | (e.py < f.rmin[1]) | (e.pz < f.rmin[2]) | (f.rmax[0] < e.px) |
+             (f.rmax[1] < e.py) | (f.rmax[2] < e.pz);
+  if (!out) return;
+  uint32_t dice = e.g.next() % (uint32_t)f.n_inj;
+  int32_t site = a.inject[f.inj0 + dice];
+  double4_32a p = a.pos4[site];
+  e.px = p.x;
+  e.py = p.y;
+  e.pz = p.z;
+  e.site = site;
+  e.at_site = true;
+  trace_push(a, e, INT32_MIN);
+  trace_push(a, e, site);
+}
+
+__device__ __forceinline__ void step_epilogue(const HopArgs& a, const FilmDev& f, int32_t film, Exciton& e,
+                                              double ox, double oy, double oz, int64_t s) {
+  if (e.active) {
+    e.dx += e.px - ox;
+    e.dy += e.py - oy;
+    e.dz += e.pz - oz;
+    maybe_reinject(a, f, e);
+  }
+  double sx = e.active ? e.dx * e.dx : 0.0;
+  double sy = e.active ? e.dy * e.dy : 0.0;
+  double sz = e.active ? e.dz * e.dz : 0.0;
+  sx = warp_sum(sx);
+  sy = warp_sum(sy);
+  sz = warp_sum(sz);
+  if ((threadIdx.x & 31) == 0) {
+    const int64_t batch = ((int64_t)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x - f.slot0) >> 5) % a.msd_batches;
+    double* m = a.msd + (((int64_t)film * a.msd_cap + a.step0 + s) * a.msd_batches + batch) * 3;
+    atomicAdd(m, sx);
+    atomicAdd(m + 1, sy);
+    atomicAdd(m + 2, sz);
+  }
+}
+
+__device__ __forceinline__ void flush_counters(const HopArgs& a, const Exciton& e, uint64_t exact) {
+  uint64_t h = e.hops, c = e.crossings, x = exact;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    h += __shfl_xor_sync(0xffffffffu, h, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+    x += __shfl_xor_sync(0xffffffffu, x, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&a.counters[0], (unsigned long long)h);
+    atomicAdd(&a.counters[1], (unsigned long long)c);
+    if (x) atomicAdd(&a.counters[2], (unsigned long long)x);
+  }
+}
+
+}  // namespace kmc

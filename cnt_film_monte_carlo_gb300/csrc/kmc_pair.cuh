@@ -6,7 +6,9 @@
 
 namespace kmc {
 
-__device__ __forceinline__ double table_rate(const TableDev& t, double th, double zsh, double a1, double a2,
+// not inlined: six inlined grid lookups made this translation unit take minutes to compile,
+// and the neighbour build is not on the hop path
+static __device__ __noinline__ double table_rate(const TableDev& t, double th, double zsh, double a1, double a2,
                                              double dist) {
   auto idx = [&](int d, double x) {
     return t.inv_h[d] > 0 ? index_min_abs_fast(t.grid[d], t.n[d], x, t.inv_h[d]) : index_min_abs(t.grid[d], t.n[d], x);

@@ -188,8 +188,9 @@ int kmc_math_probe(kmc_ctx* ctx, const double* x, int64_t n, double* log_out, do
  * launch (the kernel keeps excitons in registers across the steps of one launch). */
 int kmc_set_launch_config(kmc_ctx* ctx, int32_t block, int32_t steps_per_launch);
 
-/* Mixed kernel variant: 0, 1, 2 = compiled for at least 4, 6, 8 resident blocks of 128
- * threads per SM (fewer registers per thread, more warps resident). */
+/* Mixed kernel variant (threads per block x resident blocks per SM the kernel's registers are
+ * budgeted for): 0 = 128 x 4, 1 = 128 x 6, 2 = 128 x 8, 3 = 256 x 3, 4 = 768 x 1.  Larger
+ * blocks stage the log table fewer times per SM and leave more L1 cache. */
 int kmc_set_mixed_variant(kmc_ctx* ctx, int32_t variant);
 
 typedef struct {
