@@ -204,6 +204,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--variant", type=int, default=None)
+    ap.add_argument("--order", default="auto", choices=["auto", "slots", "spatial"],
+                    help="order in which the mixed kernel takes excitons")
+    ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -244,6 +247,9 @@ def main():
     st = e.build(R_MAX)
     e.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
     bins = args.bins_per_step
+    order = {"auto": L.KMC_ORDER_AUTO, "slots": L.KMC_ORDER_SLOTS, "spatial": L.KMC_ORDER_SPATIAL}[args.order]
+    e.set_work_order(order)
+    e.set_graph(not args.no_graph)
     if args.variant is not None:
         e.set_mixed_variant(args.variant)
     tune = e.autotune(BIN, VEL, trial_steps=1) if not (args.no_tune or args.variant is not None) else None
@@ -263,6 +269,7 @@ def main():
             launches += s["last_launches"]
         barrier()
         wall = time.perf_counter() - t0
+    order_used = "spatial" if e.work_order() == L.KMC_ORDER_SPATIAL else "slots"
     hops = e.stats()["hops"] - h0
     t_end = e.stats()["steps_done"] * BIN
     d_eff = (e.msd(0, e.stats()["steps_done"])[:, -1].sum(axis=0) / n_exc_total / (2 * t_end)).tolist()
@@ -307,6 +314,8 @@ def main():
         e3.set_table(tab)
         e3.build(R_MAX)
         e3.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+        e3.set_work_order(order)
+        e3.set_graph(not args.no_graph)
         if tune:
             e3.set_mixed_variant(tune["variant"])
             e3.set_launch_config(128, tune["steps_per_launch"])
@@ -342,7 +351,8 @@ def main():
         "dtype": "f64+f32", "data": "synthetic",
         "config": config(desc, st["n_sites"], n_exc_total, bins,
                          {"films": len(films), "k_mean": st["k_mean"], "k_max": st["k_max"], "nnz": st["nnz"],
-                          "hops_timed": hops, "build_ms": st["build_ms"]}),
+                          "hops_timed": hops, "build_ms": st["build_ms"], "work_order": order_used,
+                          "cuda_graph": not args.no_graph}),
         "fp64_plain_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "d_eff_m2_per_s": d_eff,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

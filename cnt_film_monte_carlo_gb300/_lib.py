@@ -27,6 +27,9 @@ KMC_INJECT_REGION = 0
 KMC_INJECT_UNIFORM = 1
 KMC_PREC_FP64 = 0
 KMC_PREC_MIXED = 1
+KMC_ORDER_AUTO = -1
+KMC_ORDER_SLOTS = 0
+KMC_ORDER_SPATIAL = 1
 KMC_NOALLOC_MAX_SITES = 65536
 KMC_NOALLOC_MAX_CELLS = 65536
 
@@ -92,6 +95,9 @@ SIGNATURES = {
     "kmc_math_probe": (C.c_int, [C.c_void_p, PD, C.c_int64, PD, PD]),
     "kmc_set_launch_config": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "kmc_set_mixed_variant": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kmc_set_work_order": (C.c_int, [C.c_void_p, C.c_int32]),
+    "kmc_get_work_order": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "kmc_set_graph": (C.c_int, [C.c_void_p, C.c_int32]),
     "kmc_autotune": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_void_p]),
     "kmc_build_neighbors_noalloc": (C.c_int, [PD, PD, C.c_int64, C.POINTER(kmc_table), C.c_double, PI64, PI32, PD, PD,
                                               C.c_int64, PI64, C.c_void_p, C.c_char_p, C.c_int64]),

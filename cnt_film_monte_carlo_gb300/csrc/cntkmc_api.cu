@@ -39,7 +39,7 @@ struct DevBuf {
   }
 };
 
-const uint64_t kLogTab[1 << KMC_LOG_TABLE_BITS][3] = KMC_FX_TAB_INIT;
+const uint64_t kLogTab[1 << KMC_LOG_TABLE_BITS][2] = KMC_FX_TAB_INIT;
 
 }  // namespace
 
@@ -104,6 +104,16 @@ struct kmc_ctx {
   int block = 128;
   int mixed_variant = 1;
   kmc_run_stats stats{};
+  size_t l2_bytes = 0;
+  // spatial work order of the mixed kernel (built per launch when in effect)
+  int32_t work_order = KMC_ORDER_AUTO;
+  int64_t n_obuckets = 0;
+  std::vector<int64_t> ord0;
+  DevBuf<int64_t> d_ord0, d_obucket, d_ocount, d_oscan;
+  DevBuf<int32_t> d_order;
+  // the launch sequence of a run is captured into a CUDA graph and replayed
+  bool use_graph = true;
+  cudaGraphExec_t gexec = nullptr;
 };
 
 #define FAIL(ctx, code, ...)                                          \
@@ -151,6 +161,7 @@ kmc_ctx* kmc_create(int device, int* status) {
   kmc_ctx* c = new kmc_ctx();
   c->device = device;
   c->n_sms = prop.multiProcessorCount;
+  c->l2_bytes = (size_t)prop.l2CacheSize;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       upload(c->d_logtab, reinterpret_cast<const kmc::LogTab*>(kLogTab), 1, c->stream) != cudaSuccess ||
@@ -195,6 +206,9 @@ void kmc_destroy(kmc_ctx* c) {
   c->d_counters.release();
   c->d_stats.release();
   c->d_queue.release();
+  for (auto* b : {&c->d_ord0, &c->d_obucket, &c->d_ocount, &c->d_oscan}) b->release();
+  c->d_order.release();
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -575,7 +589,38 @@ static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   return a;
 }
 
+// Whether the mixed kernel takes the excitons in spatial order: on request, or (auto) when the
+// neighbour rows, site records and link times outgrow half of the L2 cache and there are more
+// excitons than resident lanes.
+static bool order_in_effect(const kmc_ctx* c) {
+  if (c->work_order == KMC_ORDER_SLOTS || !c->built || c->n_slots >= (int64_t)INT32_MAX) return false;
+  if (c->work_order == KMC_ORDER_SPATIAL) return true;
+  const double bytes = (double)c->nblk * (sizeof(kmc::RowBlock) + 8 * sizeof(double)) +
+                       (double)c->n_sites * (sizeof(kmc::SiteRec) + sizeof(double2));
+  return bytes > 0.5 * (double)c->l2_bytes && c->n_slots > (int64_t)c->n_sms * 2048;
+}
+
+static int ensure_order_buffers(kmc_ctx* c) {
+  int64_t nb = 0;
+  std::vector<int64_t> o0(c->n_films);
+  for (int32_t i = 0; i < c->n_films; ++i) {
+    o0[i] = nb;
+    nb += kmc::order_buckets(c->films[i]);
+  }
+  if (c->d_order.p && c->d_order.n == (size_t)c->n_slots && nb == c->n_obuckets && o0 == c->ord0) return KMC_OK;
+  CK(c, upload(c->d_ord0, o0.data(), o0.size(), c->stream));
+  CK(c, c->d_obucket.alloc(c->n_slots));
+  CK(c, c->d_ocount.alloc(nb + 1));
+  CK(c, c->d_oscan.alloc(kmc::scan_scratch_len(nb + 1)));
+  CK(c, c->d_order.alloc(c->n_slots));
+  c->ord0 = o0;
+  c->n_obuckets = nb;
+  return KMC_OK;
+}
+
 // Launch n_steps steps (step indices step0.. in a.msd) with the given shape; device time in *ms.
+// The launches (and the work-order rebuild before each mixed launch) are captured into a CUDA
+// graph; the graph of the previous run is updated in place when its topology matches.
 static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0, int32_t precision, int variant,
                      int spl, float* ms, int* launches) {
   if (precision == KMC_PREC_MIXED && c->lt_v != a.v) {
@@ -583,19 +628,69 @@ static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0,
                                  c->stream));
     c->lt_v = a.v;
   }
-  CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
-  CK(c, cudaEventRecord(c->ev0, c->stream));
+  const bool ordered = precision == KMC_PREC_MIXED && order_in_effect(c);
+  if (ordered) {
+    int rc = ensure_order_buffers(c);
+    if (rc) return rc;
+  }
   const int single_film = (c->n_films == 1 && c->msd_batches == 1) ? 1 : 0;
   const int grid_blocks = c->n_sms * kmc::hop_mixed_blocks_per_sm(variant, std::min<int64_t>(spl, n_steps), single_film);
   int nl = 0;
-  for (int64_t s = 0; s < n_steps; s += spl) {
-    int64_t k = std::min<int64_t>(spl, n_steps - s);
-    a.step0 = step0 + s;
-    if (precision == KMC_PREC_FP64)
-      CK(c, kmc::launch_hop_fp64(a, k, c->block, c->stream));
-    else
-      CK(c, kmc::launch_hop_mixed(a, k, variant, grid_blocks, single_film, c->d_queue.p, c->stream));
-    ++nl;
+  auto enqueue = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream);
+    for (int64_t s = 0; s < n_steps && e == cudaSuccess; s += spl) {
+      int64_t k = std::min<int64_t>(spl, n_steps - s);
+      a.step0 = step0 + s;
+      if (precision == KMC_PREC_FP64) {
+        a.order = nullptr;
+        e = kmc::launch_hop_fp64(a, k, c->block, c->stream);
+      } else {
+        a.order = nullptr;
+        if (ordered) {
+          e = kmc::build_work_order(a, c->d_cell_of.p, c->d_ord0.p, c->n_obuckets, c->d_obucket.p, c->d_ocount.p,
+                                    c->d_oscan.p, (int64_t)c->d_oscan.n, c->d_order.p, c->stream);
+          a.order = c->d_order.p;
+          nl += 2 + kmc::scan_kernel_count(c->n_obuckets + 1);
+        }
+        if (e == cudaSuccess) e = kmc::launch_hop_mixed(a, k, variant, grid_blocks, single_film, c->d_queue.p, c->stream);
+      }
+      ++nl;
+    }
+    return e;
+  };
+  if (c->use_graph) {
+    cudaGraph_t g = nullptr;
+    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    cudaError_t e = enqueue();
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      CK(c, e != cudaSuccess ? e : e2);
+    }
+    bool updated = false;
+    if (c->gexec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(c->gexec, g, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();  // clear the update's error state
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+      }
+    }
+    if (!updated) {
+      e = cudaGraphInstantiate(&c->gexec, g, 0);
+      if (e != cudaSuccess) {
+        c->gexec = nullptr;
+        cudaGraphDestroy(g);
+        CK(c, e);
+      }
+    }
+    cudaGraphDestroy(g);
+    CK(c, cudaEventRecord(c->ev0, c->stream));
+    CK(c, cudaGraphLaunch(c->gexec, c->stream));
+  } else {
+    CK(c, cudaEventRecord(c->ev0, c->stream));
+    CK(c, enqueue());
   }
   CK(c, cudaEventRecord(c->ev1, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
@@ -632,6 +727,26 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   c->stats.last_run_ms = ms;
   c->stats.last_launches = launches;
   return rc;
+}
+
+int kmc_set_work_order(kmc_ctx* c, int32_t mode) {
+  if (!c) return KMC_ERR_ARG;
+  if (mode != KMC_ORDER_AUTO && mode != KMC_ORDER_SLOTS && mode != KMC_ORDER_SPATIAL)
+    FAIL(c, KMC_ERR_ARG, "kmc_set_work_order: mode must be KMC_ORDER_AUTO, _SLOTS or _SPATIAL");
+  c->work_order = mode;
+  return KMC_OK;
+}
+
+int kmc_get_work_order(kmc_ctx* c, int32_t* in_effect) {
+  if (!c || !in_effect) return KMC_ERR_ARG;
+  *in_effect = order_in_effect(c) ? KMC_ORDER_SPATIAL : KMC_ORDER_SLOTS;
+  return KMC_OK;
+}
+
+int kmc_set_graph(kmc_ctx* c, int32_t on) {
+  if (!c) return KMC_ERR_ARG;
+  c->use_graph = on != 0;
+  return KMC_OK;
 }
 
 int kmc_set_mixed_variant(kmc_ctx* c, int32_t variant) {
@@ -863,7 +978,7 @@ int kmc_selftest_uniform(kmc_ctx* c, uint32_t r0, uint64_t count, uint64_t* mism
   DevBuf<unsigned long long> m;
   CK(c, m.alloc(1));
   CK(c, cudaMemsetAsync(m.p, 0, 8, c->stream));
-  CK(c, kmc::launch_u_check(r0, count, m.p, c->stream));
+  CK(c, kmc::launch_u_check(r0, count, m.p, c->d_logtab.p, c->stream));
   unsigned long long h = 0;
   CK(c, cudaMemcpyAsync(&h, m.p, 8, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));

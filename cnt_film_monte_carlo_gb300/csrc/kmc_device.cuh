@@ -122,13 +122,14 @@ __device__ __forceinline__ double u_from_rand(uint32_t r) {
 }
 
 // ---------------------------------------------------------------- log (fixed point, integer pipes)
-// x = 2^k z (z in [a, 2a), one of 1024 intervals); c = C 2^-23 with a 24-bit reciprocal C, so
-// r = z c - 1 = R 2^(ez - 75) is exact; log1p(r) = r S(r) with S evaluated in Q1.62 integers;
+// x = 2^k z (z in [a, 2a), one of 1024 intervals); c = C 2^-20 with a 21-bit reciprocal C, so
+// r = z c - 1 = R 2^(ez - 72) is exact and |R| < 2^62 (R is the low word of Z C);
+// log1p(r) = r S(r) with S evaluated in Q1.30 (inner terms) and Q1.62 integers;
 // k ln2 - log c + r S is summed in a signed 128-bit Q116 integer and rounded once to double
 // (nearest, ties to even).  No floating-point instruction is used: the FP64 pipe of sm_103a is
-// the scarce resource of the hop kernels.  Error < 0.52 ulp.
+// the scarce resource of the hop kernels.  Error < 0.501 ulp.
 struct LogTab {
-  uint64_t t[1 << KMC_LOG_TABLE_BITS][3];  // C, hi and lo of -log(C 2^-23) in Q116
+  uint64_t t[1 << KMC_LOG_TABLE_BITS][2];  // hi, lo | C of -log(C 2^-20) in Q116 (low 21 bits: C)
 };
 
 struct I128 {
@@ -199,32 +200,48 @@ __device__ __forceinline__ double q116_to_double(I128 T) {
   return __longlong_as_double((long long)(sign | ((uint64_t)(e2 + 52 + 1023) << 52) | (mant & ((1ull << 52) - 1))));
 }
 
-// log(x) for a normal x > 0 (kadj: exponent correction of a pre-scaled subnormal)
-__device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const LogTab* tab) {
+// The same rounding for |T| >= 2^64 (high word non-zero): normalise to 64 bits with the
+// dropped bits folded into a sticky bit, then round the 64-bit significand to 53 bits.
+__device__ __forceinline__ double q116_to_double_big(I128 T) {
+  uint64_t sign = 0;
+  if (T.hi < 0) {
+    sign = 1ull << 63;
+    T = neg128(T);
+  }
+  const uint64_t hi = (uint64_t)T.hi, lo = T.lo;
+  const int s = __clzll((long long)hi);  // 0..63
+  const uint64_t m = s ? ((hi << s) | (lo >> (64 - s))) : hi;
+  const uint64_t sticky = (s ? (lo << s) : lo) != 0 ? 1ull : 0ull;
+  uint64_t mant = m >> 11;  // 53 bits, top bit set
+  const uint64_t guard = (m >> 10) & 1ull;
+  const uint64_t rest = (m & 0x3FFull) | sticky;
+  mant += guard & ((rest != 0 ? 1ull : 0ull) | (mant & 1ull));
+  // |T| 2^-116 = mant 2^(11 - s - 116 + 64) = (mant 2^-52) 2^(11 - s); a carry into bit 53 adds one
+  // to the exponent field
+  return __longlong_as_double((long long)(sign | (((uint64_t)(1033 - s) << 52) + mant)));
+}
+
+// -log(c) + r S for a normal x (bit pattern ix); k = the binary exponent part of log x
+__device__ __forceinline__ I128 log_fx_core(uint64_t ix, int kadj, const LogTab* tab) {
   const uint64_t tmp = ix - KMC_LOG_OFF;
   const int i = (int)((tmp >> (52 - KMC_LOG_TABLE_BITS)) & ((1u << KMC_LOG_TABLE_BITS) - 1));
   const int k = (int)((int64_t)tmp >> 52) + kadj;
   const uint64_t iz = ix - (tmp & 0xFFF0000000000000ull);
   const int ez = (int)(iz >> 52) - 1023;  // -1 or 0
   const uint64_t Z = (iz & ((1ull << 52) - 1)) | (1ull << 52);
-  const uint64_t C = tab->t[i][0];
-  // R = Z C - 2^(75 - ez): the subtrahend is 2^(11 - ez) in the high word
-  I128 R;
-  R.lo = Z * C;
-  R.hi = (int64_t)__umul64hi(Z, C) - (1ll << (11 - ez));
-  const int64_t r62 = (int64_t)sar128(R, 13 - ez).lo;  // r in Q1.62
-  const int64_t sc[6] = KMC_FX_S_INIT;
-  int64_t t = sc[5];
-#pragma unroll
-  for (int j = 4; j >= 0; --j) {
-    I128 m = mul64s(t, r62);
-    t = (int64_t)((m.lo >> 62) | ((uint64_t)m.hi << 2)) + sc[j];
-  }
-  I128 aR = R.hi < 0 ? neg128(R) : R;
-  const int bl = bitlen128((uint64_t)aR.hi, aR.lo);
-  const int sh = bl > 62 ? bl - 62 : 0;
-  const int64_t R64 = sh ? (int64_t)sar128(R, sh).lo : (int64_t)R.lo;
-  const I128 L1 = sar128(mul64s(R64, t), 21 - ez - sh);  // r S in Q116
+  const uint4 w = *reinterpret_cast<const uint4*>(&tab->t[i][0]);  // one 16-byte load: hi, lo | C
+  const uint64_t whi = ((uint64_t)w.y << 32) | w.x;
+  const uint64_t wlo = ((uint64_t)w.w << 32) | w.z;
+  const uint64_t C = wlo & ((1ull << 21) - 1);
+  const int64_t R = (int64_t)(Z * C);        // z c - 1 = R 2^(ez - 72), |R| < 2^62
+  const int64_t rq = R >> (8 - ez);          // r 2^64
+  const int32_t r30 = (int32_t)(rq >> 34);   // r 2^30
+  const int32_t t4 = (int32_t)KMC_FX_S30_4 + (int32_t)(((int64_t)r30 * KMC_FX_S30_5) >> 30);
+  const int32_t t3 = (int32_t)KMC_FX_S30_3 + (int32_t)(((int64_t)r30 * t4) >> 30);
+  const int64_t t2 = KMC_FX_S62_2 + __mul64hi((long long)rq, (long long)((uint64_t)(int64_t)t3 << 32));
+  const int64_t t1 = KMC_FX_S62_1 + __mul64hi((long long)rq, (long long)t2);
+  const int64_t S = KMC_FX_S62_0 + __mul64hi((long long)rq, (long long)t1);
+  const I128 L1 = sar128(mul64s(R, S), 18 - ez);  // r S in Q116
   // k ln2 in Q116
   const uint64_t ka = (uint64_t)(k < 0 ? -k : k);
   I128 kl;
@@ -232,9 +249,14 @@ __device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const Log
   kl.hi = (int64_t)(ka * KMC_FX_LN2_HI + __umul64hi(ka, KMC_FX_LN2_LO));
   if (k < 0) kl = neg128(kl);
   I128 lc;
-  lc.lo = tab->t[i][2];
-  lc.hi = (int64_t)tab->t[i][1];
-  const I128 T = add128(add128(kl, lc), L1);
+  lc.lo = wlo & ~((1ull << 21) - 1);
+  lc.hi = (int64_t)whi;
+  return add128(add128(kl, lc), L1);
+}
+
+// log(x) for a normal x > 0 (kadj: exponent correction of a pre-scaled subnormal)
+__device__ __forceinline__ double log_fx_normal(uint64_t ix, int kadj, const LogTab* tab) {
+  const I128 T = log_fx_core(ix, kadj, tab);
   if (T.hi == 0 && T.lo == 0) return 0.0;
   return q116_to_double(T);
 }
@@ -252,9 +274,12 @@ __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ t
   return log_fx_normal(ix, kadj, tab);
 }
 
-// kmc_log for the dwell-time uniforms, which are normal numbers in (0, 1]: no special cases.
+// kmc_log for the dwell-time uniforms u = RN(r / RAND_MAX), 1 <= r <= RAND_MAX: u = 1 gives 0,
+// and every other u lies in [2^-31, 1 - 2^-32], where |log u| >= 2^-32 and T >= 2^84 has a
+// non-zero high word.
 __device__ __forceinline__ double kmc_log_unit(double x, const LogTab* tab) {
-  return log_fx_normal((uint64_t)__double_as_longlong(x), 0, tab);
+  if (x == 1.0) return 0.0;
+  return q116_to_double_big(log_fx_core((uint64_t)__double_as_longlong(x), 0, tab));
 }
 
 // ---------------------------------------------------------------- acos (asin Taylor series)

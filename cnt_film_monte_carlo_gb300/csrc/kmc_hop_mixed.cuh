@@ -78,6 +78,39 @@ __device__ __forceinline__ uint32_t cold_next(uint64_t& n, const ColdState* c, u
   return v;
 }
 
+// Two draws in a row (the selection's and the dwell time's) with a single refill point: the warp
+// runs Philox once per hop for the lanes that cross a block boundary, instead of once per draw.
+// Same values and order as two cold_next calls.  Buffer invariant: w0.. hold words n%4 .. 3 of
+// block n/4 (refilled eagerly when n%4 becomes 0).
+__device__ __forceinline__ void cold_next2(uint64_t& n, const ColdState* c, uint32_t& w0, uint32_t& w1, uint32_t& w2,
+                                           uint32_t& w3, uint32_t& first, uint32_t& second) {
+  const uint32_t ph = (uint32_t)n & 3u;
+  first = w0 >> 1;
+  if (ph >= 2) {  // the block runs out within these two draws: next block
+    const uint64_t b = (n >> 2) + 1;
+    uint32_t o[4];
+    philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), (uint32_t)c->stream, (uint32_t)(c->stream >> 32),
+                  (uint32_t)c->seed, (uint32_t)(c->seed >> 32), o);
+    if (ph == 3) {
+      second = o[0] >> 1;
+      w0 = o[1];
+      w1 = o[2];
+      w2 = o[3];
+    } else {
+      second = w1 >> 1;
+      w0 = o[0];
+      w1 = o[1];
+      w2 = o[2];
+      w3 = o[3];
+    }
+  } else {
+    second = w1 >> 1;
+    w0 = w2;
+    w1 = w3;
+  }
+  n += 2;
+}
+
 __device__ __forceinline__ void cold_trace(const HopArgs& a, const ColdState* c, int32_t v) {
   int64_t t = c->trace_i;
   int64_t k = a.trace_cnt[t];
@@ -150,6 +183,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         alive = false;
         continue;
       }
+      if (a.order) cur = a.order[cur];
       film = a.warp_film[cur >> 5];
       fp = a.films + film;
       const int64_t ns = a.n_slots;
@@ -255,8 +289,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       // update_state (scatterer.cpp:9-31)
       uint32_t n = lenf & kLenMask;
       int32_t nsite = site;
+      uint32_t rf;  // the dwell-time draw of this hop (drawn after the selection's)
       if (n > 0) {
-        uint32_t r = cold_next(rn, cs, w0, w1, w2, w3);
+        uint32_t r;
+        cold_next2(rn, cs, w0, w1, w2, w3, r, rf);
         const RowBlock* __restrict__ rb = a.blocks + f.blk0 + blk;
         bool resolved = false;
         if (!(lenf & (kRecExact | kRecLong))) {
@@ -347,6 +383,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
           }
           nsite = rb[right >> 3].col[right & 7];
         }
+      } else {
+        rf = cold_next(rn, cs, w0, w1, w2, w3);
       }
       ehops++;
       if (tracing) cold_trace(a, cs, nsite);
@@ -355,10 +393,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         at_site = true;
         load_rec(nsite);
       }
-      uint32_t r;
-      while ((r = cold_next(rn, cs, w0, w1, w2, w3)) == 0) {
-      }
-      ff = -inv * kmc_log_unit(u_from_rand(r), s_log);
+      while (rf == 0) rf = cold_next(rn, cs, w0, w1, w2, w3);  // ff_time rejects r == 0
+      ff = -inv * kmc_log_unit(u_from_rand(rf), s_log);
       if (++hs > a.hop_cap) {  // leave this exciton where it is and report
         atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
         Exciton e;

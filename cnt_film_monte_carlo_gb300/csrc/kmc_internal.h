@@ -85,6 +85,7 @@ struct HopArgs {
   uint64_t* e_draws;
   uint64_t* e_hops;
   int64_t n_slots;
+  const int32_t* order;  // mixed kernel: slot handed out at queue position q (nullptr: q itself)
   // output
   double* msd;      // [n_films][msd_cap][msd_batches][3]
   int64_t msd_cap;
@@ -139,6 +140,14 @@ int64_t scan_scratch_len(int64_t n);
 cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, const int32_t* right, SiteRec* rec,
                               double2* lt64, int64_t n, double v, cudaStream_t s);
 cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s);
+// spatial work order of the exciton slots (see k_order_count): per-film bucket counts, and the
+// rebuild of order[] from the slots' current sites (bucket[n_slots], count[n_buckets + 1])
+constexpr int kOrderTile = 16;
+int64_t order_buckets(const FilmDev& f);
+int scan_kernel_count(int64_t n);  // kernels exclusive_scan_i64 launches for n elements
+cudaError_t build_work_order(const HopArgs& a, const int64_t* cell_of, const int64_t* ord0, int64_t n_buckets,
+                             int64_t* bucket, int64_t* count, int64_t* scan_scratch, int64_t scratch_len,
+                             int32_t* order, cudaStream_t s);
 cudaError_t launch_hop_fp64(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
 cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int variant, int grid_blocks, int single_film,
                              unsigned long long* queue, cudaStream_t s);
@@ -152,7 +161,8 @@ cudaError_t launch_hop_mixed_large(const HopArgs& a, int64_t n_steps, int varian
 int hop_mixed_blocks_per_sm_small(int variant, int64_t n_steps, int single_film);
 int hop_mixed_blocks_per_sm_large(int variant, int64_t n_steps, int single_film);
 constexpr int kMixedVariants = 5;
-cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, cudaStream_t s);
+cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, const LogTab* tab,
+                           cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,
                               cudaStream_t s);
 

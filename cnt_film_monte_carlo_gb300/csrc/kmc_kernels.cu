@@ -357,6 +357,64 @@ cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ============================================================================ work order
+// Spatial order in which the mixed kernel's work queue hands out exciton slots: slots are
+// bucketed by the cell of their current site, cells taken film by film in tiles of
+// kOrderTile x kOrderTile columns (x fastest inside a tile, tiles row by row) with z innermost.
+// The excitons in flight at one time then hop over a compact part of the film whose rows stay
+// in L2.  The order decides only which exciton a lane takes next, never a result.
+__global__ void k_order_count(HopArgs a, const int64_t* __restrict__ cell_of, const int64_t* __restrict__ ord0,
+                              int64_t n_buckets, int64_t* __restrict__ bucket, unsigned long long* __restrict__ count) {
+  int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (slot >= a.n_slots) return;
+  int64_t b = n_buckets;  // empty slots go last
+  if (a.e_flags[slot] & kExActive) {
+    const int32_t film = a.warp_film[slot >> 5];
+    const FilmDev& f = a.films[film];
+    const int64_t local = cell_of[a.e_site[slot]] - f.cell0;
+    const int64_t ix = local % f.nx, iy = (local / f.nx) % f.ny, iz = local / ((int64_t)f.nx * f.ny);
+    const int64_t ntx = (f.nx + kOrderTile - 1) / kOrderTile;
+    const int64_t tile = (iy / kOrderTile) * ntx + ix / kOrderTile;
+    b = ord0[film] + ((tile * kOrderTile + iy % kOrderTile) * kOrderTile + ix % kOrderTile) * f.nz + iz;
+  }
+  bucket[slot] = b;
+  atomicAdd(&count[b], 1ull);
+}
+
+__global__ void k_order_fill(int64_t n_slots, const int64_t* __restrict__ bucket, unsigned long long* __restrict__ start,
+                             int32_t* __restrict__ order) {
+  int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (slot >= n_slots) return;
+  unsigned long long at = atomicAdd(&start[bucket[slot]], 1ull);
+  order[at] = (int32_t)slot;
+}
+
+int scan_kernel_count(int64_t n) {
+  if (n <= 0) return 0;
+  int64_t tiles = (n + kScanTile - 1) / kScanTile;
+  return tiles == 1 ? 1 : 2 + scan_kernel_count(tiles);
+}
+
+int64_t order_buckets(const FilmDev& f) {
+  const int64_t ntx = (f.nx + kOrderTile - 1) / kOrderTile, nty = (f.ny + kOrderTile - 1) / kOrderTile;
+  return ntx * nty * kOrderTile * kOrderTile * f.nz;
+}
+
+cudaError_t build_work_order(const HopArgs& a, const int64_t* cell_of, const int64_t* ord0, int64_t n_buckets,
+                             int64_t* bucket, int64_t* count, int64_t* scan_scratch, int64_t scratch_len,
+                             int32_t* order, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(count, 0, (n_buckets + 1) * sizeof(int64_t), s);
+  if (e != cudaSuccess) return e;
+  const int64_t nb = (a.n_slots + 255) / 256;
+  if (nb == 0) return cudaSuccess;
+  auto* cnt = reinterpret_cast<unsigned long long*>(count);
+  k_order_count<<<(unsigned)nb, 256, 0, s>>>(a, cell_of, ord0, n_buckets, bucket, cnt);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = exclusive_scan_i64(count, n_buckets + 1, scan_scratch, scratch_len, s)) != cudaSuccess) return e;
+  k_order_fill<<<(unsigned)nb, 256, 0, s>>>(a.n_slots, bucket, cnt, order);
+  return cudaGetLastError();
+}
+
 // ============================================================================ plain FP64 hop kernel
 __global__ void __launch_bounds__(256) k_hop_fp64(HopArgs a, int64_t n_steps) {
   int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -449,7 +507,8 @@ int hop_mixed_blocks_per_sm(int variant, int64_t n_steps, int single_film) {
 
 // ============================================================================ self-checks
 // u_from_rand against IEEE division for r in [r0, r0 + count)
-__global__ void k_u_check(uint32_t r0, uint64_t count, unsigned long long* mism) {
+// and the dwell-time log kmc_log_unit against the general kmc_log on the same uniform
+__global__ void k_u_check(uint32_t r0, uint64_t count, unsigned long long* mism, const LogTab* tab) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   unsigned long long bad = 0;
   for (; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -457,12 +516,14 @@ __global__ void k_u_check(uint32_t r0, uint64_t count, unsigned long long* mism)
     if (r == 0) continue;
     double a = u_from_rand(r), b = (double)r / (double)kRandMax;
     bad += (__double_as_longlong(a) != __double_as_longlong(b));
+    bad += (__double_as_longlong(kmc_log_unit(a, tab)) != __double_as_longlong(kmc_log(b, tab)));
   }
   if (bad) atomicAdd(mism, bad);
 }
 
-cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, cudaStream_t s) {
-  k_u_check<<<152 * 8, 256, 0, s>>>(r0, count, mismatches);
+cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, const LogTab* tab,
+                           cudaStream_t s) {
+  k_u_check<<<152 * 8, 256, 0, s>>>(r0, count, mismatches, tab);
   return cudaGetLastError();
 }
 

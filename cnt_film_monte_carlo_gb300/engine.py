@@ -107,6 +107,18 @@ class Engine:
     def set_mixed_variant(self, variant: int):
         self._check(self.lib.kmc_set_mixed_variant(self.h, variant))
 
+    def set_work_order(self, mode: int):
+        """KMC_ORDER_AUTO, KMC_ORDER_SLOTS or KMC_ORDER_SPATIAL (order the mixed kernel takes excitons)."""
+        self._check(self.lib.kmc_set_work_order(self.h, int(mode)))
+
+    def work_order(self) -> int:
+        v = C.c_int32()
+        self._check(self.lib.kmc_get_work_order(self.h, C.byref(v)))
+        return int(v.value)
+
+    def set_graph(self, on: bool):
+        self._check(self.lib.kmc_set_graph(self.h, 1 if on else 0))
+
     def autotune(self, dt: float, velocity: float, trial_steps: int = 2) -> dict:
         r = L.kmc_tune_result()
         self._check(self.lib.kmc_autotune(self.h, float(dt), float(velocity), int(trial_steps), C.byref(r)))

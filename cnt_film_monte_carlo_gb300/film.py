@@ -73,32 +73,45 @@ def unit_axes(phi: np.ndarray, tilt: np.ndarray) -> np.ndarray:
     exactly (src/monte_carlo/scatterer.cpp:46); an axis whose rounded self dot product is
     not exactly 1 would send same-tube pairs down the general branch with sin^2 ~ 1e-16.
     """
+    phi = np.asarray(phi, dtype=np.float64)
+    tilt = np.asarray(tilt, dtype=np.float64)
     a = np.stack([np.cos(phi) * np.cos(tilt), np.sin(phi) * np.cos(tilt), np.sin(tilt)], axis=1)
     for _ in range(4):
         bad = _dot3(a) != 1.0
         if not bad.any():
             break
         a[bad] = a[bad] / np.sqrt(_dot3(a[bad]))[:, None]
-    bad = np.nonzero(_dot3(a) != 1.0)[0]
-    for i in bad:  # walk one component by ulps (smallest first: finest steps) until the dot product is 1
-        v = a[i].copy()
-        done = False
-        for c in np.argsort(np.abs(v)):
-            for step in range(1, 256):
-                for sgn in (1.0, -1.0):
-                    w = v.copy()
-                    for _ in range(step):
-                        w[c] = np.nextafter(w[c], sgn * np.inf)
-                    if _dot3(w[None, :])[0] == 1.0:
-                        a[i] = w
-                        done = True
-                        break
-                if done:
+    todo = np.nonzero(_dot3(a) != 1.0)[0]
+    # The rest: a1 enters the rounded sum last, so keep a2, move a0 by a few ulps and solve
+    # a1 = +-sqrt(1 - fl(a0^2 + a2^2)), trying the nearby doubles.  Directions that admit no
+    # such a1 are turned by up to 1e-12 rad (a fixed pseudo-random turn per attempt) and tried
+    # again.
+    for attempt in range(128):
+        if todo.size == 0:
+            break
+        jit = np.random.default_rng(attempt).uniform(-1.0, 1.0, (2, todo.size)) * (1e-12 if attempt else 0.0)
+        p = phi[todo] + jit[0]
+        t = tilt[todo] + jit[1]
+        v = np.stack([np.cos(p) * np.cos(t), np.sin(p) * np.cos(t), np.sin(t)], axis=1)
+        v /= np.sqrt(_dot3(v))[:, None]
+        sgn = np.where(v[:, 1] < 0, -1.0, 1.0)
+        left = np.ones(len(todo), dtype=bool)
+        for k0 in sorted(range(-4, 5), key=abs):
+            for k1 in sorted(range(-4, 5), key=abs):
+                idx = np.nonzero(left)[0]
+                if idx.size == 0:
                     break
-            if done:
-                break
-        if not done:
-            raise RuntimeError("could not make a unit axis with dot(a, a) == 1")
+                w = v[idx].copy()
+                w[:, 0] += k0 * np.spacing(np.abs(w[:, 0]))
+                s02 = w[:, 0] * w[:, 0] + w[:, 2] * w[:, 2]
+                a1 = np.sqrt(np.maximum(1.0 - s02, 0.0))
+                w[:, 1] = sgn[idx] * (a1 + k1 * np.spacing(a1))
+                ok = (_dot3(w) == 1.0) & (s02 <= 1.0)
+                a[todo[idx[ok]]] = w[ok]
+                left[idx[ok]] = False
+        todo = todo[left]
+    if todo.size:
+        raise RuntimeError("could not make a unit axis with dot(a, a) == 1")
     return a
 
 

@@ -37,6 +37,10 @@ extern "C" {
 #define KMC_PREC_FP64 0  /* plain FP64 hop kernel */
 #define KMC_PREC_MIXED 1 /* FP32 cumulative rates with exact FP64 re-resolve; same hop sequence */
 
+#define KMC_ORDER_AUTO (-1)  /* spatial order when the neighbour data outgrows half of the L2 cache */
+#define KMC_ORDER_SLOTS 0    /* excitons taken in slot order */
+#define KMC_ORDER_SPATIAL 1  /* excitons taken in order of the cell of their current site */
+
 typedef struct kmc_ctx kmc_ctx;
 
 /* One or more films (batched).  Sites of film f are [film_site_offsets[f], [f+1]); left/right
@@ -178,7 +182,8 @@ int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* 
 /* ---- diagnostics and tuning (no counterpart in the reference) ---- */
 
 /* Check the division-free dwell uniform RN(r / RAND_MAX) of the mixed kernel against IEEE
- * division on the device for r in [r0, r0 + count); *mismatches gets the number of differences. */
+ * division, and its dwell-time log (specialised to these uniforms) against the general device
+ * log, on the device for r in [r0, r0 + count); *mismatches gets the number of differences. */
 int kmc_selftest_uniform(kmc_ctx* ctx, uint32_t r0, uint64_t count, uint64_t* mismatches);
 
 /* Evaluate the engine's device log and acos on x[n] (for accuracy tests). */
@@ -192,6 +197,19 @@ int kmc_set_launch_config(kmc_ctx* ctx, int32_t block, int32_t steps_per_launch)
  * budgeted for): 0 = 128 x 4, 1 = 128 x 6, 2 = 128 x 8, 3 = 256 x 3, 4 = 768 x 1.  Larger
  * blocks stage the log table fewer times per SM and leave more L1 cache. */
 int kmc_set_mixed_variant(kmc_ctx* ctx, int32_t variant);
+
+/* Order in which the mixed kernel takes excitons (no counterpart in the reference, whose OpenMP
+ * loop runs the particles in index order): KMC_ORDER_AUTO (default), _SLOTS or _SPATIAL.  In
+ * spatial order the slots are re-sorted before every launch by the cell of their current site
+ * (tiles of 16 x 16 cell columns, z innermost, film by film), so excitons in flight together
+ * hop over a compact region whose neighbour rows stay in L2.  Results never depend on it. */
+int kmc_set_work_order(kmc_ctx* ctx, int32_t mode);
+/* The order the next mixed run will use: KMC_ORDER_SLOTS or KMC_ORDER_SPATIAL. */
+int kmc_get_work_order(kmc_ctx* ctx, int32_t* in_effect);
+
+/* Capture each kmc_run's launch sequence into a CUDA graph and replay it (default on; the graph
+ * of the previous run is updated in place when its shape matches).  on = 0 launches directly. */
+int kmc_set_graph(kmc_ctx* ctx, int32_t on);
 
 typedef struct {
   int32_t variant;

@@ -9,13 +9,15 @@ one project-defined log and acos, written from the mathematics:
 * log, fixed point (after the table-driven method of P. T. P. Tang, "Table-driven
   implementation of the logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4),
   1990): x = 2^k z with z in [a, 2a), a ~ 0.7012, z in one of 1024 intervals of equal width in
-  the bit pattern (the interval holding 1.0 has it in its middle).  Interval i has a 24-bit
-  integer reciprocal C_i = round(2^23 / midpoint) (C = 2^23 on the interval holding 1.0), so
-  r = z C_i 2^-23 - 1 is an exact integer multiple of 2^-76 (z < 1) or 2^-75 with
-  |r| <= 2^-11.  log1p(r) = r S(r), S = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 - r^5/6 evaluated in
-  Q1.62 integers; log x = k ln2 - log(C_i 2^-23) + r S is summed in a signed 128-bit integer with
-  116 fraction bits (ln2 and -log(C_i 2^-23) rounded to 2^-116) and rounded once to double
-  (nearest, ties to even).  Error below 0.52 ulp.
+  the bit pattern (the interval holding 1.0 has it in its middle).  Interval i has a 21-bit
+  integer reciprocal C_i = round(2^20 / midpoint) (C = 2^20 on the interval holding 1.0), so
+  r = z C_i 2^-20 - 1 = R 2^(ez - 72) exactly, with ez the exponent of z (-1 or 0), |r| < 2^-11
+  and |R| < 2^62: R is the low 64 bits of the product Z C_i of the 53-bit significand and C_i.
+  log1p(r) = r S(r), S = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 - r^5/6, evaluated from the inside
+  with r^3 .. r^5 in Q1.30 (32-bit) and the outer terms in Q1.62 (64-bit high products of
+  r 2^64); log x = k ln2 - log(C_i 2^-20) + r S is summed in a signed 128-bit integer with 116
+  fraction bits (ln2 rounded to 2^-116, -log(C_i 2^-20) to 2^-95) and rounded once to double
+  (nearest, ties to even).  Error below 0.501 ulp.
 * acos: acos(c) = pi/2 - asin(c) for |c| <= 1/2, 2 asin(sqrt((1-c)/2)) above,
   pi - 2 asin(sqrt((1+c)/2)) below; asin by its Taylor series
   x + sum_n (2n)!/(4^n (n!)^2 (2n+1)) x^(2n+1), 24 terms (|x| <= 1/2).
@@ -83,26 +85,22 @@ def main():
     ln2q = int(mpmath.nint(ln2 * mpmath.mpf(2) ** Q))
     out.append(f"#define ORC_FX_LN2_HI 0x{ln2q >> 64:016X}ULL")
     out.append(f"#define ORC_FX_LN2_LO 0x{ln2q & ((1 << 64) - 1):016X}ULL")
-    s62 = [int(mpmath.nint(mpmath.mpf(v) * mpmath.mpf(2) ** 62)) for v in
-           (1, mpmath.mpf(-1) / 2, mpmath.mpf(1) / 3, mpmath.mpf(-1) / 4, mpmath.mpf(1) / 5, mpmath.mpf(-1) / 6)]
-    out.append("/* S(r) = s[0] + s[1] r + ... + s[5] r^5 in Q1.62 */")
-    out.append("static const int64_t ORC_FX_S[6] = {" + ", ".join(f"{v}LL" for v in s62) + "};")
-    out.append(f"/* per interval i: C_i (24-bit reciprocal), -log(C_i 2^-23) in Q{Q} as (hi, lo) two's complement */")
-    out.append(f"static const uint32_t ORC_FX_C[{LOG_N}] = {{")
-    cs, lcs = [], []
+    two = mpmath.mpf(2)
+    s62 = [int(mpmath.nint(v * two ** 62)) for v in (mpmath.mpf(1), mpmath.mpf(-1) / 2, mpmath.mpf(1) / 3)]
+    s30 = [int(mpmath.nint(v * two ** 30)) for v in (mpmath.mpf(-1) / 4, mpmath.mpf(1) / 5, mpmath.mpf(-1) / 6)]
+    out.append("/* S(r) = 1 - r/2 + r^2/3 - r^3/4 + r^4/5 - r^5/6: s62 = 1, -1/2, 1/3 in Q1.62; s30 = -1/4, 1/5, -1/6 in Q1.30 */")
+    out.append("static const int64_t ORC_FX_S62[3] = {" + ", ".join(f"{v}LL" for v in s62) + "};")
+    out.append("static const int32_t ORC_FX_S30[3] = {" + ", ".join(f"{v}LL" for v in s30) + "};")
+    out.append(f"/* per interval i: {{hi, lo | C_i}} with -log(C_i 2^-20) in Q{Q} (two's complement, a multiple of")
+    out.append(" * 2^21, so its low 21 bits carry the 21-bit reciprocal C_i) */")
+    out.append(f"static const uint64_t ORC_FX_TAB[{LOG_N}][2] = {{")
     for i in range(LOG_N):
         lo_ = mpmath.mpf(b2d(LOG_OFF + i * STEP))
         hi_ = mpmath.mpf(b2d(LOG_OFF + (i + 1) * STEP))
-        C = 1 << 23 if i == CENTER_INDEX else int(mpmath.nint(mpmath.mpf(2) ** 23 * 2 / (lo_ + hi_)))
-        lc = int(mpmath.nint(-mpmath.log(mpmath.mpf(C) / mpmath.mpf(2) ** 23) * mpmath.mpf(2) ** Q))
-        cs.append(C)
-        lcs.append(lc & ((1 << 128) - 1))
-    for i in range(0, LOG_N, 8):
-        out.append("  " + ", ".join(f"{c}u" for c in cs[i:i + 8]) + ",")
-    out.append("};")
-    out.append(f"static const uint64_t ORC_FX_LC[{LOG_N}][2] = {{")
-    for v in lcs:
-        out.append(f"  {{0x{v >> 64:016X}ULL, 0x{v & ((1 << 64) - 1):016X}ULL}},")
+        C = 1 << 20 if i == CENTER_INDEX else int(mpmath.nint(two ** 21 / (lo_ + hi_)))
+        assert 0 < C < (1 << 21)
+        lc = (int(mpmath.nint(-mpmath.log(mpmath.mpf(C) / two ** 20) * two ** 95)) << 21) & ((1 << 128) - 1)
+        out.append(f"  {{0x{lc >> 64:016X}ULL, 0x{(lc & ((1 << 64) - 1)) | C:016X}ULL}},")
     out.append("};")
     out.append("#endif")
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "kmc_math_tables.h")

@@ -162,19 +162,19 @@ static inline double orc_log(double x) {
   uint64_t iz = ix - (tmp & 0xFFF0000000000000ULL);
   int ez = (int)(iz >> 52) - 1023; /* -1 or 0 */
   uint64_t Z = (iz & ((1ULL << 52) - 1)) | (1ULL << 52);
-  /* r = z c - 1 = R 2^(ez - 75) exactly */
-  orc_i128 R = (orc_i128)((orc_u128)Z * ORC_FX_C[i]) - (((orc_i128)1) << (75 - ez));
-  int64_t r62 = (int64_t)(R >> (13 - ez)); /* r in Q1.62 */
-  int64_t t = ORC_FX_S[5];
-  for (int j = 4; j >= 0; --j) t = (int64_t)(((orc_i128)t * r62) >> 62) + ORC_FX_S[j];
-  orc_u128 aR = R < 0 ? (orc_u128)(-R) : (orc_u128)R;
-  int bl = orc_bitlen128(aR);
-  int sh = bl > 62 ? bl - 62 : 0;
-  int64_t R64 = (int64_t)(R >> sh);
-  orc_i128 P = (orc_i128)R64 * t; /* r S = P 2^(ez + sh - 137) */
-  orc_i128 L1 = P >> (21 - ez - sh);
+  uint64_t C = ORC_FX_TAB[i][1] & ((1ULL << 21) - 1);
+  /* r = z c - 1 = R 2^(ez - 72) exactly; |R| < 2^62, so R is the low word of Z C */
+  int64_t R = (int64_t)(Z * C);
+  int64_t rq = R >> (8 - ez);            /* r 2^64 */
+  int32_t r30 = (int32_t)(rq >> 34);     /* r 2^30 */
+  int32_t t4 = ORC_FX_S30[1] + (int32_t)(((int64_t)r30 * ORC_FX_S30[2]) >> 30);
+  int32_t t3 = ORC_FX_S30[0] + (int32_t)(((int64_t)r30 * t4) >> 30);
+  int64_t t2 = ORC_FX_S62[2] + (int64_t)(((orc_i128)rq * (orc_i128)((int64_t)t3 * 4294967296LL)) >> 64);
+  int64_t t1 = ORC_FX_S62[1] + (int64_t)(((orc_i128)rq * t2) >> 64);
+  int64_t S = ORC_FX_S62[0] + (int64_t)(((orc_i128)rq * t1) >> 64);
+  orc_i128 L1 = ((orc_i128)R * S) >> (18 - ez); /* r S in Q116 */
   orc_i128 ln2 = (orc_i128)((((orc_u128)ORC_FX_LN2_HI) << 64) | ORC_FX_LN2_LO);
-  orc_i128 lc = (orc_i128)((((orc_u128)ORC_FX_LC[i][0]) << 64) | ORC_FX_LC[i][1]);
+  orc_i128 lc = (orc_i128)((((orc_u128)ORC_FX_TAB[i][0]) << 64) | (ORC_FX_TAB[i][1] & ~((1ULL << 21) - 1)));
   orc_i128 T = (orc_i128)k * ln2 + lc + L1;
   if (T == 0) return 0.0;
   return orc_q116_to_double(T);

@@ -349,6 +349,34 @@ def test_mixed_variants_and_autotune_do_not_change_results():
         assert h == states[0][2]
 
 
+def test_work_order_and_graph_do_not_change_results():
+    # two films so that the spatial order interleaves nothing across films; region injection so
+    # that removal/reinjection moves excitons between cells between launches
+    films = [F.straight_tubes(n, 40.0, box_nm=(80, 80, 6), seed=s) for n, s in ((24, 5), (9, 6))]
+    tab = tables.forster_2d(1e15)
+    runs = []
+    for order, graph, spl in ((L.KMC_ORDER_SLOTS, False, 1), (L.KMC_ORDER_SPATIAL, False, 1),
+                              (L.KMC_ORDER_SPATIAL, True, 2), (L.KMC_ORDER_AUTO, True, 1)):
+        e = E.Engine(0)
+        e.load_films(films)
+        e.set_table(tab)
+        e.build(10e-9)
+        e.set_work_order(order)
+        e.set_graph(graph)
+        e.set_launch_config(128, spl)
+        e.init_excitons([4000, 1500], [3, 4], L.KMC_INJECT_REGION, n_sections=3)
+        if order == L.KMC_ORDER_SPATIAL:
+            assert e.work_order() == L.KMC_ORDER_SPATIAL
+        e.run(3, 1e-13, 2e5, L.KMC_PREC_MIXED)
+        e.run(2, 1e-13, 2e5, L.KMC_PREC_MIXED)  # second run: the cached graph is updated in place
+        runs.append((e.excitons(), e.msd(0, 5), e.stats()["hops"]))
+        e.close()
+    for g, m, h in runs[1:]:
+        assert_states_equal(g, runs[0][0])
+        assert_msd_close(m, runs[0][1])
+        assert h == runs[0][2]
+
+
 @pytest.mark.parametrize("table_kind", [2, 4])
 def test_random_geometry_csr_matches_oracle(table_kind):
     # sites at random points with random axes (each a one-site tube): pair distances and angles

@@ -47,7 +47,7 @@ def test_log_accuracy():
     xs += [(r / 2147483647.0) for r in rng.integers(1, 2**31 - 1, 2000)]
     xs += [1 - 2.0**-k for k in range(1, 53)] + [1 + 2.0**-k for k in range(1, 53)] + [5e-324, 2.2250738585072014e-308]
     worst = max(ulp_err(O.log(x), mpmath.log(mpmath.mpf(x))) for x in xs)
-    assert worst < 1.0, worst
+    assert worst < 0.52, worst
     assert O.log(1.0) == 0.0
     assert O.log(0.0) == -np.inf and np.isnan(O.log(-1.0)) and O.log(np.inf) == np.inf
 
@@ -73,7 +73,7 @@ def test_oracle_and_engine_tables_agree():
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     a = _header_numbers(os.path.join(root, "oracle", "kmc_math_tables.h"))
     b = _header_numbers(os.path.join(root, "cnt_film_monte_carlo_gb300", "csrc", "kmc_math_tables.h"))
-    assert len(a[0]) > 20 and len(a[1]) > 2000 and len(a[2]) > 1000
+    assert len(a[0]) > 20 and len(a[1]) > 2000 and len(a[2]) >= 6
     assert a == b
 
 
