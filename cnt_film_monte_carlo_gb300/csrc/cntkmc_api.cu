@@ -78,6 +78,11 @@ struct kmc_ctx {
   int64_t nblk = 0;
   DevBuf<kmc::SiteRec> d_rec;
   DevBuf<double2> d_lt64;
+  // spatial storage order of the sites: perm[slot] = reference id, rank[id] = slot; the
+  // hop kernels read positions and links per slot
+  DevBuf<int32_t> d_perm, d_rank, d_left_i, d_right_i;
+  DevBuf<double4_32a> d_pos4i;
+  std::vector<int32_t> h_perm;
   double lt_v = -1;
   // excitons
   bool inited = false;
@@ -108,8 +113,7 @@ struct kmc_ctx {
   // spatial work order of the mixed kernel (built per launch when in effect)
   int32_t work_order = KMC_ORDER_AUTO;
   int64_t n_obuckets = 0;
-  std::vector<int64_t> ord0;
-  DevBuf<int64_t> d_ord0, d_obucket, d_ocount, d_oscan;
+  DevBuf<int64_t> d_obucket, d_ocount, d_oscan;
   DevBuf<int32_t> d_order;
   // the launch sequence of a run is captured into a CUDA graph and replayed
   bool use_graph = true;
@@ -206,8 +210,9 @@ void kmc_destroy(kmc_ctx* c) {
   c->d_counters.release();
   c->d_stats.release();
   c->d_queue.release();
-  for (auto* b : {&c->d_ord0, &c->d_obucket, &c->d_ocount, &c->d_oscan}) b->release();
-  c->d_order.release();
+  for (auto* b : {&c->d_obucket, &c->d_ocount, &c->d_oscan}) b->release();
+  for (auto* b : {&c->d_order, &c->d_perm, &c->d_rank, &c->d_left_i, &c->d_right_i}) b->release();
+  c->d_pos4i.release();
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -326,14 +331,30 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, c->d_cell_cursor.alloc(ncell));
   CK(c, c->d_cell_members.alloc(n));
   CK(c, c->d_rowptr.alloc(n + 1));
-  int64_t sl = std::max(kmc::scan_scratch_len(ncell + 1), kmc::scan_scratch_len(n + 1));
+  // buckets of the spatial storage order (tiles of cell columns, film by film)
+  std::vector<int64_t> ord0(c->n_films);
+  int64_t n_tb = 0;
+  for (int32_t i = 0; i < c->n_films; ++i) {
+    ord0[i] = n_tb;
+    n_tb += kmc::order_buckets(c->films[i]);
+  }
+  DevBuf<int64_t> d_ord0, d_tsizes;
+  CK(c, upload(d_ord0, ord0.data(), ord0.size(), c->stream));
+  CK(c, d_tsizes.alloc(n_tb + 1));
+  int64_t sl = std::max(std::max(kmc::scan_scratch_len(ncell + 1), kmc::scan_scratch_len(n + 1)),
+                        kmc::scan_scratch_len(n_tb + 1));
   CK(c, c->d_scan.alloc(sl));
+  CK(c, c->d_perm.alloc(n));
+  CK(c, c->d_rank.alloc(n));
   CK(c, cudaMemsetAsync(c->d_cell_start.p, 0, (ncell + 1) * sizeof(int64_t), c->stream));
   CK(c, cudaMemsetAsync(c->d_cell_cursor.p, 0, ncell * sizeof(int64_t), c->stream));
   CK(c, cudaMemsetAsync(c->d_rowptr.p, 0, (n + 1) * sizeof(int64_t), c->stream));
   CK(c, cudaMemsetAsync(c->d_stats.p, 0, 4 * sizeof(unsigned long long), c->stream));
   CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
   kmc::BuildArgs a{};
+  a.n_films = c->n_films;
+  a.perm = c->d_perm.p;
+  a.rank = c->d_rank.p;
   a.pos4 = c->d_pos4.p;
   a.orient = c->d_orient.p;
   a.site_film = c->d_site_film.p;
@@ -356,6 +377,7 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, kmc::launch_cell_ids(a, c->stream));
   CK(c, kmc::exclusive_scan_i64(c->d_cell_start.p, ncell + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
   CK(c, kmc::launch_cell_fill(a, c->stream));
+  CK(c, kmc::build_site_order(a, d_ord0.p, n_tb, d_tsizes.p, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
   CK(c, kmc::launch_nbr_count(a, c->stream));
   CK(c, kmc::exclusive_scan_i64(c->d_rowptr.p, n + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
   CK(c, c->d_blkptr.alloc(n + 1));
@@ -388,6 +410,12 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, c->d_inv_total.alloc(n));
   CK(c, c->d_rec.alloc(n));
   CK(c, c->d_lt64.alloc(n));
+  CK(c, c->d_pos4i.alloc(n));
+  CK(c, c->d_left_i.alloc(n));
+  CK(c, c->d_right_i.alloc(n));
+  a.pos4i = c->d_pos4i.p;
+  a.left_i = c->d_left_i.p;
+  a.right_i = c->d_right_i.p;
   a.blocks = c->d_blocks.p;
   a.blast = c->d_blast.p;
   a.cump = c->d_cump.p;
@@ -401,6 +429,8 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   unsigned long long hs[4];
   CK(c, cudaMemcpy(hs, c->d_stats.p, sizeof hs, cudaMemcpyDeviceToHost));
+  c->h_perm.resize(n);
+  CK(c, cudaMemcpy(c->h_perm.data(), c->d_perm.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost));
   c->r_max = r_max;
   c->lt_v = -1;
   c->built = true;
@@ -491,6 +521,7 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
   c->n_exc_total = total;
   CK(c, cudaMemcpyAsync(c->d_films.p, c->films.data(), c->films.size() * sizeof(FilmDev), cudaMemcpyHostToDevice, c->stream));
   CK(c, upload(c->d_inject, inject.data(), inject.size(), c->stream));
+  CK(c, kmc::ids_to_slots(c->d_inject.p, (int64_t)inject.size(), c->d_rank.p, c->stream));
   CK(c, upload(c->d_warp_film, warp_film.data(), warp_film.size(), c->stream));
   CK(c, c->d_e_site.alloc(slot));
   CK(c, c->d_e_flags.alloc(slot));
@@ -509,7 +540,8 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
   c->d_msd.release();
   CK(c, cudaMemsetAsync(c->d_counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
   kmc::HopArgs a{};
-  a.pos4 = c->d_pos4.p;
+  a.pos4 = c->d_pos4i.p;
+  a.rank = c->d_rank.p;
   a.inv_total = c->d_inv_total.p;
   a.films = c->d_films.p;
   a.warp_film = c->d_warp_film.p;
@@ -550,9 +582,10 @@ static int ensure_msd(kmc_ctx* c, int64_t need) {
 
 static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   kmc::HopArgs a{};
-  a.pos4 = c->d_pos4.p;
-  a.left = c->d_left.p;
-  a.right = c->d_right.p;
+  a.pos4 = c->d_pos4i.p;
+  a.left = c->d_left_i.p;
+  a.right = c->d_right_i.p;
+  a.rank = c->d_rank.p;
   a.rowptr = c->d_rowptr.p;
   a.blkptr = c->d_blkptr.p;
   a.total = c->d_total.p;
@@ -601,19 +634,12 @@ static bool order_in_effect(const kmc_ctx* c) {
 }
 
 static int ensure_order_buffers(kmc_ctx* c) {
-  int64_t nb = 0;
-  std::vector<int64_t> o0(c->n_films);
-  for (int32_t i = 0; i < c->n_films; ++i) {
-    o0[i] = nb;
-    nb += kmc::order_buckets(c->films[i]);
-  }
-  if (c->d_order.p && c->d_order.n == (size_t)c->n_slots && nb == c->n_obuckets && o0 == c->ord0) return KMC_OK;
-  CK(c, upload(c->d_ord0, o0.data(), o0.size(), c->stream));
+  const int64_t nb = (c->n_sites + kmc::kOrderSpan - 1) / kmc::kOrderSpan;
+  if (c->d_order.p && c->d_order.n == (size_t)c->n_slots && nb == c->n_obuckets) return KMC_OK;
   CK(c, c->d_obucket.alloc(c->n_slots));
   CK(c, c->d_ocount.alloc(nb + 1));
   CK(c, c->d_oscan.alloc(kmc::scan_scratch_len(nb + 1)));
   CK(c, c->d_order.alloc(c->n_slots));
-  c->ord0 = o0;
   c->n_obuckets = nb;
   return KMC_OK;
 }
@@ -624,8 +650,8 @@ static int ensure_order_buffers(kmc_ctx* c) {
 static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0, int32_t precision, int variant,
                      int spl, float* ms, int* launches) {
   if (precision == KMC_PREC_MIXED && c->lt_v != a.v) {
-    CK(c, kmc::launch_link_times(c->d_pos4.p, c->d_left.p, c->d_right.p, c->d_rec.p, c->d_lt64.p, c->n_sites, a.v,
-                                 c->stream));
+    CK(c, kmc::launch_link_times(c->d_pos4i.p, c->d_left_i.p, c->d_right_i.p, c->d_rec.p, c->d_lt64.p, c->n_sites,
+                                 a.v, c->stream));
     c->lt_v = a.v;
   }
   const bool ordered = precision == KMC_PREC_MIXED && order_in_effect(c);
@@ -647,8 +673,8 @@ static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0,
       } else {
         a.order = nullptr;
         if (ordered) {
-          e = kmc::build_work_order(a, c->d_cell_of.p, c->d_ord0.p, c->n_obuckets, c->d_obucket.p, c->d_ocount.p,
-                                    c->d_oscan.p, (int64_t)c->d_oscan.n, c->d_order.p, c->stream);
+          e = kmc::build_work_order(a, c->n_obuckets, c->d_obucket.p, c->d_ocount.p, c->d_oscan.p,
+                                    (int64_t)c->d_oscan.n, c->d_order.p, c->stream);
           a.order = c->d_order.p;
           nl += 2 + kmc::scan_kernel_count(c->n_obuckets + 1);
         }
@@ -914,7 +940,7 @@ int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, doub
     const FilmDev& fd = c->films[f];
     for (int64_t i = 0; i < fd.n_exc; ++i, ++o) {
       int64_t s = fd.slot0 + i;
-      if (site) site[o] = hs[s] < 0 ? -1 : (int32_t)(hs[s] - fd.site0);
+      if (site) site[o] = hs[s] < 0 ? -1 : (int32_t)(c->h_perm[hs[s]] - fd.site0);
       for (int k = 0; k < 3; ++k) {
         if (pos) pos[3 * o + k] = hp[k * ns + s];
         if (delta) delta[3 * o + k] = hd[k * ns + s];
@@ -942,21 +968,28 @@ int kmc_get_neighbors(kmc_ctx* c, int64_t* rowptr, int32_t* col, double* cum, do
   std::vector<int64_t> rp(n + 1), bp(n + 1);
   CK(c, cudaMemcpy(rp.data(), c->d_rowptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
   if (rowptr) std::copy(rp.begin(), rp.end(), rowptr);
-  if (total) CK(c, cudaMemcpy(total, c->d_total.p, n * 8, cudaMemcpyDeviceToHost));
+  if (total) {  // stored per slot
+    std::vector<double> t(n);
+    CK(c, cudaMemcpy(t.data(), c->d_total.p, n * 8, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < n; ++i) total[c->h_perm[i]] = t[i];
+  }
   if (!col && !cum) return KMC_OK;
   CK(c, cudaMemcpy(bp.data(), c->d_blkptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
-  // rows are stored in 8-entry blocks; gather them back into the reference's CSR layout
+  // rows are stored per slot in 8-entry blocks, with neighbours as slots; gather them back into
+  // the reference's CSR layout and ids
   std::vector<kmc::RowBlock> blocks(c->nblk);
   std::vector<double> cump(c->nblk * 8);
   CK(c, cudaMemcpy(blocks.data(), c->d_blocks.p, c->nblk * sizeof(kmc::RowBlock), cudaMemcpyDeviceToHost));
   CK(c, cudaMemcpy(cump.data(), c->d_cump.p, c->nblk * 8 * sizeof(double), cudaMemcpyDeviceToHost));
   for (int32_t f = 0; f < c->n_films; ++f) {
     const FilmDev& fd = c->films[f];
-    for (int64_t s = fd.site0; s < fd.site0 + fd.n_sites; ++s)
+    for (int64_t i = fd.site0; i < fd.site0 + fd.n_sites; ++i) {
+      const int64_t s = c->h_perm[i];
       for (int64_t k = 0; k < rp[s + 1] - rp[s]; ++k) {
-        if (col) col[rp[s] + k] = blocks[bp[s] + (k >> 3)].col[k & 7] - (int32_t)fd.site0;
-        if (cum) cum[rp[s] + k] = cump[bp[s] * 8 + k];
+        if (col) col[rp[s] + k] = c->h_perm[blocks[bp[i] + (k >> 3)].col[k & 7]] - (int32_t)fd.site0;
+        if (cum) cum[rp[s] + k] = cump[bp[i] * 8 + k];
       }
+    }
   }
   return KMC_OK;
 }
@@ -969,6 +1002,12 @@ int64_t kmc_get_trace(kmc_ctx* c, int64_t e, int32_t* out, int64_t cap) {
   int64_t k = std::min(std::min(cnt, c->trace_cap), cap);
   if (k > 0 && cudaMemcpy(out, c->d_trace.p + e * c->trace_cap, k * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
     return KMC_ERR_CUDA;
+  // storage slots back to site ids: v (hop), -1 - v (link crossing); INT32_MIN marks a reinjection
+  for (int64_t j = 0; j < k; ++j) {
+    const int32_t v = out[j];
+    if (v >= 0) out[j] = c->h_perm[v];
+    else if (v != INT32_MIN) out[j] = -1 - c->h_perm[-1 - v];
+  }
   return cnt;
 }
 

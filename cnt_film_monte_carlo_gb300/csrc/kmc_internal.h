@@ -86,6 +86,7 @@ struct HopArgs {
   uint64_t* e_hops;
   int64_t n_slots;
   const int32_t* order;  // mixed kernel: slot handed out at queue position q (nullptr: q itself)
+  const int32_t* rank;   // reference site id -> storage slot (exciton creation)
   // output
   double* msd;      // [n_films][msd_cap][msd_batches][3]
   int64_t msd_cap;
@@ -102,6 +103,7 @@ struct HopArgs {
 };
 
 struct BuildArgs {
+  int32_t n_films;
   const double4_32a* pos4;
   const double* orient;    // [n][3]
   const int32_t* site_film;
@@ -127,6 +129,12 @@ struct BuildArgs {
   const int32_t* right;
   int32_t* err;
   unsigned long long* stats;  // [0] longest row [1] empty rows [2] rows resolved in FP64 only
+  // storage order: perm[slot] = reference id, rank[id] = slot; per-slot copies for the hop kernels
+  int32_t* perm;
+  int32_t* rank;
+  double4_32a* pos4i;
+  int32_t* left_i;   // links as storage slots (-1: tube end)
+  int32_t* right_i;
 };
 
 // launchers (kmc_kernels.cu); all return cudaError_t of the launch
@@ -140,14 +148,19 @@ int64_t scan_scratch_len(int64_t n);
 cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, const int32_t* right, SiteRec* rec,
                               double2* lt64, int64_t n, double v, cudaStream_t s);
 cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s);
-// spatial work order of the exciton slots (see k_order_count): per-film bucket counts, and the
-// rebuild of order[] from the slots' current sites (bucket[n_slots], count[n_buckets + 1])
+// spatial storage order of the sites (see tile_bucket): tiles of kOrderTile x kOrderTile cell
+// columns; order_buckets(f) = tiled cell buckets of one film (with padding)
 constexpr int kOrderTile = 16;
 int64_t order_buckets(const FilmDev& f);
+cudaError_t build_site_order(const BuildArgs& a, const int64_t* ord0, int64_t n_buckets, int64_t* sizes,
+                             int64_t* scan_scratch, int64_t scratch_len, cudaStream_t s);
+cudaError_t ids_to_slots(int32_t* ids, int64_t n, const int32_t* rank, cudaStream_t s);
+// work order of the exciton slots: rebuilt before every mixed launch from the slots' current
+// sites (bucket = storage slot / kOrderSpan; bucket[n_slots], count[n_buckets + 1])
+constexpr int kOrderSpan = 16;
 int scan_kernel_count(int64_t n);  // kernels exclusive_scan_i64 launches for n elements
-cudaError_t build_work_order(const HopArgs& a, const int64_t* cell_of, const int64_t* ord0, int64_t n_buckets,
-                             int64_t* bucket, int64_t* count, int64_t* scan_scratch, int64_t scratch_len,
-                             int32_t* order, cudaStream_t s);
+cudaError_t build_work_order(const HopArgs& a, int64_t n_buckets, int64_t* bucket, int64_t* count,
+                             int64_t* scan_scratch, int64_t scratch_len, int32_t* order, cudaStream_t s);
 cudaError_t launch_hop_fp64(const HopArgs& a, int64_t n_steps, int block, cudaStream_t s);
 cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int variant, int grid_blocks, int single_film,
                              unsigned long long* queue, cudaStream_t s);

@@ -77,6 +77,75 @@ cudaError_t launch_cell_fill(const BuildArgs& a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// ============================================================================ storage order of the sites
+// Sites are stored in spatial order: cells of each film in tiles of kOrderTile x kOrderTile
+// columns (x fastest inside a tile, tiles row by row), z innermost, the members of a cell in
+// reference order.  Every site-indexed array the hop kernels read (records, row blocks, positions,
+// links) is laid out in this order, so a compact region of the film is a compact range of
+// memory; reference ids are translated at the boundary (perm: slot -> id, rank: id -> slot).
+__device__ __forceinline__ int64_t tile_bucket(const FilmDev& f, int64_t local_cell) {
+  const int64_t ix = local_cell % f.nx, iy = (local_cell / f.nx) % f.ny, iz = local_cell / ((int64_t)f.nx * f.ny);
+  const int64_t ntx = (f.nx + kOrderTile - 1) / kOrderTile;
+  const int64_t tile = (iy / kOrderTile) * ntx + ix / kOrderTile;
+  return ((tile * kOrderTile + iy % kOrderTile) * kOrderTile + ix % kOrderTile) * f.nz + iz;
+}
+
+__device__ __forceinline__ int32_t film_of_cell(const FilmDev* films, int32_t n_films, int64_t c) {
+  int32_t lo = 0, hi = n_films - 1;
+  while (lo < hi) {
+    int32_t mid = (lo + hi + 1) / 2;
+    if (films[mid].cell0 <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_site_order_sizes(BuildArgs a, const int64_t* __restrict__ ord0, int64_t* __restrict__ sizes) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int32_t film = film_of_cell(a.films, a.n_films, c);
+  const FilmDev& f = a.films[film];
+  sizes[ord0[film] + tile_bucket(f, c - f.cell0)] = a.cell_start[c + 1] - a.cell_start[c];
+}
+
+__global__ void k_site_order_fill(BuildArgs a, const int64_t* __restrict__ ord0, const int64_t* __restrict__ start) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= a.n_cells) return;
+  const int32_t film = film_of_cell(a.films, a.n_films, c);
+  const FilmDev& f = a.films[film];
+  int64_t at = start[ord0[film] + tile_bucket(f, c - f.cell0)];
+  for (int64_t m = a.cell_start[c], e = a.cell_start[c + 1]; m < e; ++m, ++at) {
+    const int32_t s = a.cell_members[m];
+    a.perm[at] = s;
+    a.rank[s] = (int32_t)at;
+  }
+}
+
+cudaError_t build_site_order(const BuildArgs& a, const int64_t* ord0, int64_t n_buckets, int64_t* sizes,
+                             int64_t* scan_scratch, int64_t scratch_len, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(sizes, 0, (n_buckets + 1) * sizeof(int64_t), s);
+  if (e != cudaSuccess) return e;
+  const int64_t nb = (a.n_cells + 255) / 256;
+  if (nb == 0) return cudaSuccess;
+  k_site_order_sizes<<<(unsigned)nb, 256, 0, s>>>(a, ord0, sizes);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = exclusive_scan_i64(sizes, n_buckets + 1, scan_scratch, scratch_len, s)) != cudaSuccess) return e;
+  k_site_order_fill<<<(unsigned)nb, 256, 0, s>>>(a, ord0, sizes);
+  return cudaGetLastError();
+}
+
+// ids[k] <- rank[ids[k]] (reference ids to storage slots)
+__global__ void k_ids_to_slots(int32_t* ids, int64_t n, const int32_t* __restrict__ rank) {
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k < n) ids[k] = rank[ids[k]];
+}
+
+cudaError_t ids_to_slots(int32_t* ids, int64_t n, const int32_t* rank, cudaStream_t s) {
+  const int64_t nb = (n + 255) / 256;
+  if (nb) k_ids_to_slots<<<(unsigned)nb, 256, 0, s>>>(ids, n, rank);
+  return cudaGetLastError();
+}
+
 // ============================================================================ K2: neighbour + rate CSR
 // Visit the neighbours of site s in find_neighbors order; fn(j, p2, dR, distance) per neighbour.
 template <typename F>
@@ -116,13 +185,16 @@ __global__ void k_nbr_count(BuildArgs a) {
   if (n == 0) atomicAdd(&a.stats[1], 1ull);
 }
 
+// Row of site s (reference id) into storage slot rank[s]; neighbour ids and links are stored as
+// storage slots, so the hop kernels never translate ids.
 __global__ void k_nbr_fill(BuildArgs a) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= a.n_sites) return;
   const FilmDev& f = a.films[a.site_film[s]];
   double4_32a p1 = a.pos4[s];
   double a1v[3] = {a.orient[3 * s], a.orient[3 * s + 1], a.orient[3 * s + 2]};
-  const int64_t bo = a.blkptr[s];
+  const int64_t si = a.rank[s];
+  const int64_t bo = a.blkptr[si];
   double* cump = a.cump + bo * 8;  // this row's FP64 cumulative rates (8 per block)
   int64_t k = 0;
   double run = 0.0;
@@ -133,13 +205,13 @@ __global__ void k_nbr_fill(BuildArgs a) {
     negative |= rate < 0;
     run = (k == 0) ? rate : run + rate;  // in-place inclusive prefix sum, scatterer.cpp:78-80
     cump[k] = run;
-    a.blocks[bo + (k >> 3)].col[k & 7] = q;
+    a.blocks[bo + (k >> 3)].col[k & 7] = a.rank[q];
     ++k;
   });
   double tot = k > 0 ? run : 0.0;
   double inv = 1. / tot;
-  a.total[s] = tot;
-  a.inv_total[s] = inv;
+  a.total[si] = tot;
+  a.inv_total[si] = inv;
   bool exact = negative || !(tot > 0.0) || !(tot < __longlong_as_double(0x7FF0000000000000ll));
   if (exact && k > 0) atomicAdd(&a.stats[2], 1ull);
   // FP32 normalised values, padding, second and first search levels
@@ -164,8 +236,8 @@ __global__ void k_nbr_fill(BuildArgs a) {
   r.inv_total = inv;
   r.blk = (uint32_t)(bo - f.blk0);
   r.len_flags = (uint32_t)k | (exact ? kRecExact : 0u) | (nb > 64 ? kRecLong : 0u);
-  r.left = a.left[s];
-  r.right = a.right[s];
+  r.left = a.left[s] >= 0 ? a.rank[a.left[s]] : -1;
+  r.right = a.right[s] >= 0 ? a.rank[a.right[s]] : -1;
   r.lt_hi_l = 0;
   r.lt_hi_r = 0;
   const int64_t G = nb <= 8 ? 1 : (nb + 7) / 8;
@@ -177,14 +249,23 @@ __global__ void k_nbr_fill(BuildArgs a) {
       r.coarse[i] = kInf;
     }
   }
-  a.rec[s] = r;
+  a.rec[si] = r;
+  a.pos4i[si] = p1;
+  a.left_i[si] = r.left;
+  a.right_i[si] = r.right;
 }
 
-// blocks per row, from the row pointers: blkptr[s] = ceil(len / 8) (scanned afterwards)
+// blocks per row in storage order, from the row pointers (reference order):
+// blkptr[i] = ceil(len(perm[i]) / 8), scanned afterwards
 __global__ void k_blk_counts(BuildArgs a) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s > a.n_sites) return;
-  a.blkptr[s] = s < a.n_sites ? (a.rowptr[s + 1] - a.rowptr[s] + 7) / 8 : 0;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i > a.n_sites) return;
+  if (i == a.n_sites) {
+    a.blkptr[i] = 0;
+    return;
+  }
+  const int64_t s = a.perm[i];
+  a.blkptr[i] = (a.rowptr[s + 1] - a.rowptr[s] + 7) / 8;
 }
 
 cudaError_t launch_blk_counts(const BuildArgs& a, cudaStream_t s) {
@@ -332,7 +413,7 @@ __global__ void k_init_excitons(HopArgs a) {
   g.init(f.seed, (uint64_t)local, 0);
   // kubo_create_particles: dice = rand() % n_inject (monte_carlo.cpp:311)
   uint32_t dice = g.next() % (uint32_t)f.n_inj;
-  int32_t site = (f.mode == 1) ? (int32_t)(f.site0 + dice) : a.inject[f.inj0 + dice];
+  int32_t site = (f.mode == 1) ? a.rank[f.site0 + dice] : a.inject[f.inj0 + dice];  // storage slot
   // particle(pos, s, v): ff_time() then heading = rand() % 2 (particle.h:48-52)
   uint32_t r;
   while ((r = g.next()) == 0) {
@@ -358,25 +439,15 @@ cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s) {
 }
 
 // ============================================================================ work order
-// Spatial order in which the mixed kernel's work queue hands out exciton slots: slots are
-// bucketed by the cell of their current site, cells taken film by film in tiles of
-// kOrderTile x kOrderTile columns (x fastest inside a tile, tiles row by row) with z innermost.
-// The excitons in flight at one time then hop over a compact part of the film whose rows stay
-// in L2.  The order decides only which exciton a lane takes next, never a result.
-__global__ void k_order_count(HopArgs a, const int64_t* __restrict__ cell_of, const int64_t* __restrict__ ord0,
-                              int64_t n_buckets, int64_t* __restrict__ bucket, unsigned long long* __restrict__ count) {
+// Order in which the mixed kernel's work queue hands out exciton slots: by the storage slot of
+// the exciton's current site (sites are stored in spatial order), in buckets of kOrderSpan slots.
+// The excitons in flight at one time then hop over a compact part of the film whose rows stay in
+// L2.  The order decides only which exciton a lane takes next, never a result.
+__global__ void k_order_count(HopArgs a, int64_t n_buckets, int64_t* __restrict__ bucket,
+                              unsigned long long* __restrict__ count) {
   int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (slot >= a.n_slots) return;
-  int64_t b = n_buckets;  // empty slots go last
-  if (a.e_flags[slot] & kExActive) {
-    const int32_t film = a.warp_film[slot >> 5];
-    const FilmDev& f = a.films[film];
-    const int64_t local = cell_of[a.e_site[slot]] - f.cell0;
-    const int64_t ix = local % f.nx, iy = (local / f.nx) % f.ny, iz = local / ((int64_t)f.nx * f.ny);
-    const int64_t ntx = (f.nx + kOrderTile - 1) / kOrderTile;
-    const int64_t tile = (iy / kOrderTile) * ntx + ix / kOrderTile;
-    b = ord0[film] + ((tile * kOrderTile + iy % kOrderTile) * kOrderTile + ix % kOrderTile) * f.nz + iz;
-  }
+  const int64_t b = (a.e_flags[slot] & kExActive) ? (int64_t)(a.e_site[slot] / kOrderSpan) : n_buckets;  // empty slots last
   bucket[slot] = b;
   atomicAdd(&count[b], 1ull);
 }
@@ -400,15 +471,14 @@ int64_t order_buckets(const FilmDev& f) {
   return ntx * nty * kOrderTile * kOrderTile * f.nz;
 }
 
-cudaError_t build_work_order(const HopArgs& a, const int64_t* cell_of, const int64_t* ord0, int64_t n_buckets,
-                             int64_t* bucket, int64_t* count, int64_t* scan_scratch, int64_t scratch_len,
-                             int32_t* order, cudaStream_t s) {
+cudaError_t build_work_order(const HopArgs& a, int64_t n_buckets, int64_t* bucket, int64_t* count,
+                             int64_t* scan_scratch, int64_t scratch_len, int32_t* order, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(count, 0, (n_buckets + 1) * sizeof(int64_t), s);
   if (e != cudaSuccess) return e;
   const int64_t nb = (a.n_slots + 255) / 256;
   if (nb == 0) return cudaSuccess;
   auto* cnt = reinterpret_cast<unsigned long long*>(count);
-  k_order_count<<<(unsigned)nb, 256, 0, s>>>(a, cell_of, ord0, n_buckets, bucket, cnt);
+  k_order_count<<<(unsigned)nb, 256, 0, s>>>(a, n_buckets, bucket, cnt);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if ((e = exclusive_scan_i64(count, n_buckets + 1, scan_scratch, scratch_len, s)) != cudaSuccess) return e;
   k_order_fill<<<(unsigned)nb, 256, 0, s>>>(a.n_slots, bucket, cnt, order);
@@ -436,7 +506,7 @@ __global__ void __launch_bounds__(256) k_hop_fp64(HopArgs a, int64_t n_steps) {
         rem -= e.ff;
         fly_full(a, e, e.ff);
         int32_t ns = e.site;
-        int64_t n = a.rowptr[e.site + 1] - a.rowptr[e.site];
+        int64_t n = a.rec[e.site].len_flags & kLenMask;  // row length (rows are stored per slot)
         if (n > 0) {  // update_state, scatterer.cpp:14-30
           const int64_t bo = a.blkptr[e.site];
           const double* cum = a.cump + bo * 8;
