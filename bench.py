@@ -339,12 +339,15 @@ def main():
     peak, peak_kind = measured_peak()
     bph = bytes_per_hop(st["k_mean"])
     achieved = hops / dev_s * bph / 1e9
-    traffic = None
+    spl = tune["steps_per_launch"] if tune else 32  # the engine's default steps per launch
+    hop_launches = args.steps * math.ceil(bins / spl)
+    traffic = None  # DRAM bytes per hop-kernel launch, from the ncu capture of this workload
     prof = os.path.join(ROOT, "profiles", "hop_mixed_traffic.json")
     if os.path.exists(prof):
         with open(prof) as fh:
-            pj = json.load(fh)
-        traffic = pj.get("dram_bytes_per_hop", 0) * hops / max(launches, 1)
+            pj = json.load(fh).get(args.workload)
+        if pj:
+            traffic = pj["dram_bytes_per_hop"] * hops / max(hop_launches, 1)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
