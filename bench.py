@@ -255,7 +255,8 @@ def main():
     tune = e.autotune(BIN, VEL, trial_steps=1) if not (args.no_tune or args.variant is not None) else None
     for _ in range(args.warmup):
         e.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
-    h0 = e.stats()["hops"]
+    s0 = e.stats()
+    h0 = s0["hops"]
     dev_ms, launches = 0.0, 0
     barrier()
     with ClockSampler(local) as clk:
@@ -270,7 +271,10 @@ def main():
         barrier()
         wall = time.perf_counter() - t0
     order_used = "spatial" if e.work_order() == L.KMC_ORDER_SPATIAL else "slots"
-    hops = e.stats()["hops"] - h0
+    s1 = e.stats()
+    hops = s1["hops"] - h0
+    crossings = s1["crossings"] - s0["crossings"]
+    exact = s1["exact_resolves"] - s0["exact_resolves"]
     t_end = e.stats()["steps_done"] * BIN
     d_eff = (e.msd(0, e.stats()["steps_done"])[:, -1].sum(axis=0) / n_exc_total / (2 * t_end)).tolist()
     e.close()
@@ -354,7 +358,9 @@ def main():
         "dtype": "f64+f32", "data": "synthetic",
         "config": config(desc, st["n_sites"], n_exc_total, bins,
                          {"films": len(films), "k_mean": st["k_mean"], "k_max": st["k_max"], "nnz": st["nnz"],
-                          "hops_timed": hops, "build_ms": st["build_ms"], "work_order": order_used,
+                          "hops_timed": hops, "crossings_per_hop": crossings / max(hops, 1),
+                          "fp64_resolves_per_hop": exact / max(hops, 1),
+                          "build_ms": st["build_ms"], "work_order": order_used,
                           "cuda_graph": not args.no_graph}),
         "fp64_plain_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "d_eff_m2_per_s": d_eff,

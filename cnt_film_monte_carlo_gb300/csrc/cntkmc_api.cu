@@ -109,7 +109,6 @@ struct kmc_ctx {
   int block = 128;
   int mixed_variant = 1;
   kmc_run_stats stats{};
-  size_t l2_bytes = 0;
   // spatial work order of the mixed kernel (built per launch when in effect)
   int32_t work_order = KMC_ORDER_AUTO;
   int64_t n_obuckets = 0;
@@ -165,7 +164,6 @@ kmc_ctx* kmc_create(int device, int* status) {
   kmc_ctx* c = new kmc_ctx();
   c->device = device;
   c->n_sms = prop.multiProcessorCount;
-  c->l2_bytes = (size_t)prop.l2CacheSize;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess ||
       upload(c->d_logtab, reinterpret_cast<const kmc::LogTab*>(kLogTab), 1, c->stream) != cudaSuccess ||
@@ -622,15 +620,14 @@ static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   return a;
 }
 
-// Whether the mixed kernel takes the excitons in spatial order: on request, or (auto) when the
-// neighbour rows, site records and link times outgrow half of the L2 cache and there are more
-// excitons than resident lanes.
+// Whether the mixed kernel takes the excitons in spatial order: on request, or (auto) when there
+// are several excitons per resident lane, so that the lanes of an SM work on neighbouring sites
+// (L1 and L2 reuse; on large films also TLB reach) and the per-launch sort is cheap against the
+// launch.
 static bool order_in_effect(const kmc_ctx* c) {
   if (c->work_order == KMC_ORDER_SLOTS || !c->built || c->n_slots >= (int64_t)INT32_MAX) return false;
   if (c->work_order == KMC_ORDER_SPATIAL) return true;
-  const double bytes = (double)c->nblk * (sizeof(kmc::RowBlock) + 8 * sizeof(double)) +
-                       (double)c->n_sites * (sizeof(kmc::SiteRec) + sizeof(double2));
-  return bytes > 0.5 * (double)c->l2_bytes && c->n_slots > (int64_t)c->n_sms * 2048;
+  return c->n_slots > (int64_t)c->n_sms * 2048;
 }
 
 static int ensure_order_buffers(kmc_ctx* c) {

@@ -326,27 +326,31 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
               if (j2 == i + 1) prev = v[i];
             bsel = g0 + (uint32_t)j2;
           }
-          const float4* bp = reinterpret_cast<const float4*>(rb + bsel);
-          float4 c0 = __ldg(bp), c1 = __ldg(bp + 1);
-          int4 k0 = __ldg(reinterpret_cast<const int4*>(bp + 2)), k1 = __ldg(reinterpret_cast<const int4*>(bp + 3));
-          float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-          int32_t cl[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
-          int kk = 0;
+          // u at or above the row's last FP32 value (u == 1.0f: r >= 2^31 - 64) selects no block of the
+          // row; such draws are resolved in FP64 below
+          if (bsel < nb) {
+            const float4* bp = reinterpret_cast<const float4*>(rb + bsel);
+            float4 c0 = __ldg(bp), c1 = __ldg(bp + 1);
+            int4 k0 = __ldg(reinterpret_cast<const int4*>(bp + 2)), k1 = __ldg(reinterpret_cast<const int4*>(bp + 3));
+            float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+            int32_t cl[8] = {k0.x, k0.y, k0.z, k0.w, k1.x, k1.y, k1.z, k1.w};
+            int kk = 0;
 #pragma unroll
-          for (int i = 0; i < 8; ++i) kk += (c[i] <= u);
-          float ck = c[0], ckm = prev;
-          int32_t colk = cl[0];
+            for (int i = 0; i < 8; ++i) kk += (c[i] <= u);
+            float ck = c[0], ckm = prev;
+            int32_t colk = cl[0];
 #pragma unroll
-          for (int i = 1; i < 8; ++i)
-            if (kk == i) {
-              ck = c[i];
-              ckm = c[i - 1];
-              colk = cl[i];
+            for (int i = 1; i < 8; ++i)
+              if (kk == i) {
+                ck = c[i];
+                ckm = c[i - 1];
+                colk = cl[i];
+              }
+            uint32_t R = bsel * 8 + (uint32_t)kk;
+            if ((R == 0 || ckm < u * lo_m) && (R == n - 1 || ck > u * hi_m)) {
+              nsite = colk;
+              resolved = true;
             }
-          uint32_t R = bsel * 8 + (uint32_t)kk;
-          if ((R == 0 || ckm < u * lo_m) && (R == n - 1 || ck > u * hi_m)) {
-            nsite = colk;
-            resolved = true;
           }
         } else if ((lenf & kRecLong) && !(lenf & kRecExact)) {
           // rows beyond 512 entries: the reference bisection on the blocked FP32 values

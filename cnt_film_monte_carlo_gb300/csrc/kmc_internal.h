@@ -166,14 +166,14 @@ cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int variant, int
                              unsigned long long* queue, cudaStream_t s);
 int hop_mixed_blocks_per_sm(int variant, int64_t n_steps, int single_film);
 // per-translation-unit halves of the two above (kmc_mixed_small.cu: variants 0-2,
-// kmc_mixed_large.cu: variants 3-4)
+// kmc_mixed_large.cu: variants 3-5)
 cudaError_t launch_hop_mixed_small(const HopArgs& a, int64_t n_steps, int variant, int grid_blocks, int single_film,
                                    unsigned long long* queue, cudaStream_t s);
 cudaError_t launch_hop_mixed_large(const HopArgs& a, int64_t n_steps, int variant, int grid_blocks, int single_film,
                                    unsigned long long* queue, cudaStream_t s);
 int hop_mixed_blocks_per_sm_small(int variant, int64_t n_steps, int single_film);
 int hop_mixed_blocks_per_sm_large(int variant, int64_t n_steps, int single_film);
-constexpr int kMixedVariants = 5;
+constexpr int kMixedVariants = 6;
 cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, const LogTab* tab,
                            cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,

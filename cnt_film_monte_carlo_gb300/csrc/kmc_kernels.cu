@@ -563,7 +563,7 @@ cudaError_t launch_hop_fp64(const HopArgs& a, int64_t n_steps, int block, cudaSt
 // Variants of the mixed kernel: (threads per block, resident blocks per SM the registers are
 // budgeted for).  The log table is staged once per block, so fewer, larger blocks leave more of
 // the SM's shared-memory/L1 array to the L1 cache.
-//   0: 128 x 4   1: 128 x 6   2: 128 x 8   3: 256 x 3   4: 768 x 1
+//   0: 128 x 4   1: 128 x 6   2: 128 x 8   3: 256 x 3   4: 768 x 1   5: 1024 x 1
 cudaError_t launch_hop_mixed(const HopArgs& a, int64_t n_steps, int variant, int grid_blocks, int single_film,
                              unsigned long long* queue, cudaStream_t s) {
   if (variant >= 3) return launch_hop_mixed_large(a, n_steps, variant, grid_blocks, single_film, queue, s);

@@ -37,7 +37,7 @@ extern "C" {
 #define KMC_PREC_FP64 0  /* plain FP64 hop kernel */
 #define KMC_PREC_MIXED 1 /* FP32 cumulative rates with exact FP64 re-resolve; same hop sequence */
 
-#define KMC_ORDER_AUTO (-1)  /* spatial order when the neighbour data outgrows half of the L2 cache */
+#define KMC_ORDER_AUTO (-1)  /* spatial order when there are several excitons per resident lane */
 #define KMC_ORDER_SLOTS 0    /* excitons taken in slot order */
 #define KMC_ORDER_SPATIAL 1  /* excitons taken in order of the cell of their current site */
 
@@ -194,15 +194,16 @@ int kmc_math_probe(kmc_ctx* ctx, const double* x, int64_t n, double* log_out, do
 int kmc_set_launch_config(kmc_ctx* ctx, int32_t block, int32_t steps_per_launch);
 
 /* Mixed kernel variant (threads per block x resident blocks per SM the kernel's registers are
- * budgeted for): 0 = 128 x 4, 1 = 128 x 6, 2 = 128 x 8, 3 = 256 x 3, 4 = 768 x 1.  Larger
- * blocks stage the log table fewer times per SM and leave more L1 cache. */
+ * budgeted for): 0 = 128 x 4, 1 = 128 x 6, 2 = 128 x 8, 3 = 256 x 3, 4 = 768 x 1,
+ * 5 = 1024 x 1.  Larger blocks stage the log table fewer times per SM and leave more L1 cache. */
 int kmc_set_mixed_variant(kmc_ctx* ctx, int32_t variant);
 
 /* Order in which the mixed kernel takes excitons (no counterpart in the reference, whose OpenMP
  * loop runs the particles in index order): KMC_ORDER_AUTO (default), _SLOTS or _SPATIAL.  In
- * spatial order the slots are re-sorted before every launch by the cell of their current site
- * (tiles of 16 x 16 cell columns, z innermost, film by film), so excitons in flight together
- * hop over a compact region whose neighbour rows stay in L2.  Results never depend on it. */
+ * spatial order the slots are re-sorted before every launch by the storage slot of their current
+ * site (sites are stored in tiles of 16 x 16 cell columns, z innermost, film by film), so the
+ * excitons in flight together hop over a compact region whose rows stay in L1/L2.  Results never
+ * depend on it. */
 int kmc_set_work_order(kmc_ctx* ctx, int32_t mode);
 /* The order the next mixed run will use: KMC_ORDER_SLOTS or KMC_ORDER_SPATIAL. */
 int kmc_get_work_order(kmc_ctx* ctx, int32_t* in_effect);

@@ -323,7 +323,7 @@ def test_msd_batches_and_diffusion_fit_match_oracle(precision):
 def test_mixed_variants_and_autotune_do_not_change_results():
     f, tab, r_max = synthetic_case(2, n_tubes=20, length=40.0, box=(80, 80, 6))
     states = []
-    for variant in (0, 1, 2, 3, 4):
+    for variant in range(6):
         e = E.Engine(0)
         e.load_films(f)
         e.set_table(tab)
@@ -339,7 +339,7 @@ def test_mixed_variants_and_autotune_do_not_change_results():
     e.build(r_max)
     e.init_excitons(3000, 4, L.KMC_INJECT_UNIFORM)
     choice = e.autotune(1e-13, 2e5, trial_steps=2)
-    assert choice["variant"] in (0, 1, 2, 3, 4) and choice["hops_per_s"] > 0
+    assert choice["variant"] in range(6) and choice["hops_per_s"] > 0
     e.run(5, 1e-13, 2e5, L.KMC_PREC_MIXED)
     states.append((e.excitons(), e.msd(0, 5), e.stats()["hops"]))
     e.close()
