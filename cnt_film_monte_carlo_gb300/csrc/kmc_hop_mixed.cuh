@@ -44,72 +44,24 @@ struct ColdState {
   int64_t trace_i;
 };
 
-__device__ __forceinline__ void cold_refill(uint64_t n, const ColdState* c, uint32_t& w0, uint32_t& w1, uint32_t& w2,
-                                            uint32_t& w3) {
-  uint64_t b = n >> 2;
-  uint32_t o[4];
-  philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), (uint32_t)c->stream, (uint32_t)(c->stream >> 32), (uint32_t)c->seed,
-                (uint32_t)(c->seed >> 32), o);
-  w0 = o[0];
-  w1 = o[1];
-  w2 = o[2];
-  w3 = o[3];
-  for (uint32_t i = 0; i < (uint32_t)(n & 3); ++i) {
-    uint32_t t = w0;
-    w0 = w1;
-    w1 = w2;
-    w2 = w3;
-    w3 = t;
-  }
-}
-
-// one draw of the exciton's stream (same sequence as Rng::next)
-__device__ __forceinline__ uint32_t cold_next(uint64_t& n, const ColdState* c, uint32_t& w0, uint32_t& w1, uint32_t& w2,
-                                              uint32_t& w3) {
-  uint32_t v = w0 >> 1;
-  ++n;
-  if ((n & 3) == 0) {
-    cold_refill(n, c, w0, w1, w2, w3);
-  } else {
-    w0 = w1;
-    w1 = w2;
-    w2 = w3;
-  }
-  return v;
-}
-
-// Two draws in a row (the selection's and the dwell time's) with a single refill point: the warp
-// runs Philox once per hop for the lanes that cross a block boundary, instead of once per draw.
-// Same values and order as two cold_next calls.  Buffer invariant: w0.. hold words n%4 .. 3 of
-// block n/4 (refilled eagerly when n%4 becomes 0).
-__device__ __forceinline__ void cold_next2(uint64_t& n, const ColdState* c, uint32_t& w0, uint32_t& w1, uint32_t& w2,
-                                           uint32_t& w3, uint32_t& first, uint32_t& second) {
-  const uint32_t ph = (uint32_t)n & 3u;
-  first = w0 >> 1;
-  if (ph >= 2) {  // the block runs out within these two draws: next block
-    const uint64_t b = (n >> 2) + 1;
+// Draw buffer of a lane: a ring of 8 Philox words in shared memory (word k of the lane at
+// ring[k * BLOCK + tid], so a warp's accesses hit 32 banks), holding `avail` words from draw index
+// n on.  The ring holds whole blocks: block b occupies words 4(b mod 2) .. +3.
+struct DrawRing {
+  uint32_t* r;  // this lane's word 0
+  int stride;   // BLOCK
+  __device__ __forceinline__ uint32_t word(uint64_t i) const { return r[(int)(i & 7) * stride]; }
+  // Philox block b = d / 4 (d a multiple of 4) into its ring words
+  __device__ __forceinline__ void fill(uint64_t d, const ColdState* c) const {
+    const uint64_t b = d >> 2;
     uint32_t o[4];
     philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), (uint32_t)c->stream, (uint32_t)(c->stream >> 32),
                   (uint32_t)c->seed, (uint32_t)(c->seed >> 32), o);
-    if (ph == 3) {
-      second = o[0] >> 1;
-      w0 = o[1];
-      w1 = o[2];
-      w2 = o[3];
-    } else {
-      second = w1 >> 1;
-      w0 = o[0];
-      w1 = o[1];
-      w2 = o[2];
-      w3 = o[3];
-    }
-  } else {
-    second = w1 >> 1;
-    w0 = w2;
-    w1 = w3;
+    const int k = (int)(d & 4);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) r[(k + j) * stride] = o[j];
   }
-  n += 2;
-}
+};
 
 __device__ __forceinline__ void cold_trace(const HopArgs& a, const ColdState* c, int32_t v) {
   int64_t t = c->trace_i;
@@ -129,7 +81,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
   extern __shared__ double s_mem[];
   LogTab* s_log = reinterpret_cast<LogTab*>(s_mem);  // the log table, read once per hop
   double* s_bins = s_mem + sizeof(LogTab) / sizeof(double);  // [n_steps][3] when single_film
-  ColdState* cs = reinterpret_cast<ColdState*>(s_bins + (single_film ? n_steps * 3 : 0)) + threadIdx.x;
+  ColdState* cs0 = reinterpret_cast<ColdState*>(s_bins + (single_film ? (n_steps * 3 + 15) / 16 * 16 : 0));
+  ColdState* cs = cs0 + threadIdx.x;
+  const DrawRing ring{reinterpret_cast<uint32_t*>(cs0 + BLOCK) + threadIdx.x, BLOCK};
   const int lane = threadIdx.x & 31;
   {
     const uint64_t* src = &a.logtab->t[0][0];
@@ -148,7 +102,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
   bool heading = false, at_site = false, tracing = false;
   double ff = 0, rem = 0;
   uint64_t rn = 0;
-  uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+  uint32_t avail = 0;  // draws buffered in the ring from rn on
   double inv = 0;
   uint32_t blk = 0, lenf = 0, lth_l = 0, lth_r = 0;
   int32_t lnk_l = -1, lnk_r = -1;
@@ -170,6 +124,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
   for (;;) {
     // all 32 lanes meet here once per event, so every event starts with the warp converged
     if (!__any_sync(0xffffffffu, alive)) break;
+    // When any lane of the warp is short of a hop's two draws, every lane with room in its ring
+    // adds the next Philox block: the warp runs Philox together about every other hop instead
+    // of once per hop for half of its lanes.
+    if (__any_sync(0xffffffffu, alive && cur >= 0 && avail < 2)) {
+      if (alive && cur >= 0 && avail <= 4) {
+        ring.fill(rn + avail, cs);
+        avail += 4;
+      }
+    }
     if (!alive) continue;
     if (cur < 0) {
       // ---- take the next exciton slot
@@ -202,7 +165,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       cs->seed = fp->seed;
       cs->stream = (uint64_t)local;
       rn = a.e_draws[cur];
-      cold_refill(rn, cs, w0, w1, w2, w3);
+      ring.fill(rn & ~3ull, cs);
+      avail = 4 - (uint32_t)(rn & 3);
       double px, py, pz;
       if (at_site) {
         double4_32a p = a.pos4[site];
@@ -291,8 +255,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       int32_t nsite = site;
       uint32_t rf;  // the dwell-time draw of this hop (drawn after the selection's)
       if (n > 0) {
-        uint32_t r;
-        cold_next2(rn, cs, w0, w1, w2, w3, r, rf);
+        if (avail < 2) {  // first hop after taking an exciton
+          ring.fill(rn + avail, cs);
+          avail += 4;
+        }
+        const uint32_t r = ring.word(rn) >> 1;
+        rf = ring.word(rn + 1) >> 1;
+        rn += 2;
+        avail -= 2;
         const RowBlock* __restrict__ rb = a.blocks + f.blk0 + blk;
         bool resolved = false;
         if (!(lenf & (kRecExact | kRecLong))) {
@@ -388,7 +358,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
           nsite = rb[right >> 3].col[right & 7];
         }
       } else {
-        rf = cold_next(rn, cs, w0, w1, w2, w3);
+        if (avail == 0) {
+          ring.fill(rn, cs);
+          avail = 4;
+        }
+        rf = ring.word(rn) >> 1;
+        ++rn;
+        --avail;
       }
       ehops++;
       if (tracing) cold_trace(a, cs, nsite);
@@ -397,7 +373,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         at_site = true;
         load_rec(nsite);
       }
-      while (rf == 0) rf = cold_next(rn, cs, w0, w1, w2, w3);  // ff_time rejects r == 0
+      while (rf == 0) {  // ff_time rejects r == 0
+        if (avail == 0) {
+          ring.fill(rn, cs);
+          avail = 4;
+        }
+        rf = ring.word(rn) >> 1;
+        ++rn;
+        --avail;
+      }
       ff = -inv * kmc_log_unit(u_from_rand(rf), s_log);
       if (++hs > a.hop_cap) {  // leave this exciton where it is and report
         atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
@@ -448,17 +432,21 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       e.at_site = false;
       e.g.seed = cs->seed;
       e.g.stream = cs->stream;
+      if (avail == 0) {  // the Rng below holds the rest of the current block
+        ring.fill(rn, cs);
+        avail = 4;
+      }
       e.g.n = rn;
-      e.g.w0 = w0;
-      e.g.w1 = w1;
-      e.g.w2 = w2;
-      e.g.w3 = w3;
+      e.g.w0 = ring.word(rn);
+      e.g.w1 = ring.word(rn + 1);
+      e.g.w2 = ring.word(rn + 2);
+      e.g.w3 = ring.word(rn + 3);
       maybe_reinject(a, f, e);
-      rn = e.g.n;
-      w0 = e.g.w0;
-      w1 = e.g.w1;
-      w2 = e.g.w2;
-      w3 = e.g.w3;
+      if (e.g.n != rn) {  // the reinjection drew: restart the ring at the new draw index
+        rn = e.g.n;
+        ring.fill(rn & ~3ull, cs);
+        avail = 4 - (uint32_t)(rn & 3);
+      }
       site = e.site;
       heading = e.heading;
       at_site = e.at_site;
@@ -508,7 +496,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
 
 template <int BLOCK>
 static size_t mixed_smem(int64_t n_steps, int single_film) {
-  return sizeof(LogTab) + (single_film ? (size_t)n_steps * 3 * sizeof(double) : 0) + BLOCK * sizeof(ColdState);
+  return sizeof(LogTab) + (single_film ? (size_t)(n_steps * 3 + 15) / 16 * 16 * sizeof(double) : 0) +
+         BLOCK * (sizeof(ColdState) + 8 * sizeof(uint32_t));
 }
 
 template <int BLOCK, int MINB>
