@@ -222,6 +222,7 @@ def main():
     from cnt_film_monte_carlo_gb300 import _lib as L
     from cnt_film_monte_carlo_gb300 import build as B
     from cnt_film_monte_carlo_gb300 import engine as E
+    from cnt_film_monte_carlo_gb300 import replicas as R
 
     B.build()
     torch.cuda.set_device(local)
@@ -246,7 +247,7 @@ def main():
     e.load_films(films)
     e.set_table(tab)
     st = e.build(R_MAX)
-    e.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+    e.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
     bins = args.bins_per_step
     order = {"auto": L.KMC_ORDER_AUTO, "slots": L.KMC_ORDER_SLOTS, "spatial": L.KMC_ORDER_SPATIAL}[args.order]
     e.set_work_order(order)
@@ -277,17 +278,12 @@ def main():
     crossings = s1["crossings"] - s0["crossings"]
     exact = s1["exact_resolves"] - s0["exact_resolves"]
     t_end = e.stats()["steps_done"] * BIN
-    d_eff = (e.msd(0, e.stats()["steps_done"])[:, -1].sum(axis=0) / n_exc_total / (2 * t_end)).tolist()
+    # MSD of the last step over every replica's excitons (the path's only exchange)
+    last = R.sum_msd(e.msd(0, e.stats()["steps_done"])[:, -1].sum(axis=0))
+    d_eff = (last / (n_exc_total * world) / (2 * t_end)).tolist()
     e.close()
     dev_s = dev_ms / 1e3
-    if dist is not None:
-        t = torch.tensor([dev_s, wall, float(hops)], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        dev_s_max, wall_max, hops_all = mx[0].item(), mx[1].item(), t[2].item()
-    else:
-        dev_s_max, wall_max, hops_all = dev_s, wall, float(hops)
+    dev_s_max, wall_max, hops_all = R.job_timing(dev_s, wall, hops)
     value = hops_all / dev_s_max
 
     # plain FP64 kernel on the same workload (same seeds; same hop sequence)
@@ -297,7 +293,7 @@ def main():
         e2.load_films(films)
         e2.set_table(tab)
         e2.build(R_MAX)
-        e2.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+        e2.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
         e2.run(args.warmup * bins, BIN, VEL, L.KMC_PREC_FP64)
         h1 = e2.stats()["hops"]
         ms = 0.0
@@ -318,7 +314,7 @@ def main():
         e3.load_films(films)
         e3.set_table(tab)
         e3.build(R_MAX)
-        e3.init_excitons(n_exc, [SEED + rank + i for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+        e3.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
         e3.set_work_order(order)
         e3.set_graph(not args.no_graph)
         if tune:

@@ -23,8 +23,16 @@ def batch_counts(n_excitons: int, batches: int) -> np.ndarray:
 def fit(msd_batches: np.ndarray, n_excitons: int, times: np.ndarray, fit_fraction: float = 0.8):
     """msd_batches: [n_steps][batches][3] sums of one film; returns (D[3], ci95[3]) in m^2/s."""
     m = np.ascontiguousarray(msd_batches, dtype=np.float64)
+    return fit_counts(m, batch_counts(n_excitons, m.shape[1]), times, fit_fraction)
+
+
+def fit_counts(msd_batches: np.ndarray, counts: np.ndarray, times: np.ndarray, fit_fraction: float = 0.8):
+    """As fit, with the excitons of every batch given (e.g. batches gathered from replicas)."""
+    m = np.ascontiguousarray(msd_batches, dtype=np.float64)
     n_steps, batches = m.shape[0], m.shape[1]
-    counts = batch_counts(n_excitons, batches)
+    counts = np.ascontiguousarray(counts, dtype=np.int64)
+    if counts.shape != (batches,):
+        raise ValueError("one exciton count per batch")
     t = np.ascontiguousarray(times, dtype=np.float64)
     D = np.zeros(3)
     ci = np.zeros(3)
