@@ -254,22 +254,47 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       uint32_t n = lenf & kLenMask;
       int32_t nsite = site;
       uint32_t rf;  // the dwell-time draw of this hop (drawn after the selection's)
+      uint32_t r = 0;
+      float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
       if (n > 0) {
         if (avail < 2) {  // first hop after taking an exciton
           ring.fill(rn + avail, cs);
           avail += 4;
         }
-        const uint32_t r = ring.word(rn) >> 1;
+        r = ring.word(rn) >> 1;
         rf = ring.word(rn + 1) >> 1;
         rn += 2;
         avail -= 2;
+        const float4* cq = reinterpret_cast<const float4*>(recp->coarse);  // first search level
+        q0 = __ldg(cq);
+        q1 = __ldg(cq + 1);
+      } else {
+        if (avail == 0) {
+          ring.fill(rn, cs);
+          avail = 4;
+        }
+        rf = ring.word(rn) >> 1;
+        ++rn;
+        --avail;
+      }
+      while (rf == 0) {  // ff_time rejects r == 0
+        if (avail == 0) {
+          ring.fill(rn, cs);
+          avail = 4;
+        }
+        rf = ring.word(rn) >> 1;
+        ++rn;
+        --avail;
+      }
+      // the dwell time's log does not depend on the row: computed here, it covers the latency of
+      // the row loads
+      const double dlog = kmc_log_unit(u_from_rand(rf), s_log);
+      if (n > 0) {
         const RowBlock* __restrict__ rb = a.blocks + f.blk0 + blk;
         bool resolved = false;
         if (!(lenf & (kRecExact | kRecLong))) {
           // two- or three-level search for the first FP32 value > u (count of values <= u)
           float u = __uint2float_rn(r) * (1.0f / 2147483647.0f);
-          const float4* cq = reinterpret_cast<const float4*>(recp->coarse);
-          float4 q0 = __ldg(cq), q1 = __ldg(cq + 1);
           float co[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
           int j1 = 0;
 #pragma unroll
@@ -357,14 +382,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
           }
           nsite = rb[right >> 3].col[right & 7];
         }
-      } else {
-        if (avail == 0) {
-          ring.fill(rn, cs);
-          avail = 4;
-        }
-        rf = ring.word(rn) >> 1;
-        ++rn;
-        --avail;
       }
       ehops++;
       if (tracing) cold_trace(a, cs, nsite);
@@ -373,16 +390,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         at_site = true;
         load_rec(nsite);
       }
-      while (rf == 0) {  // ff_time rejects r == 0
-        if (avail == 0) {
-          ring.fill(rn, cs);
-          avail = 4;
-        }
-        rf = ring.word(rn) >> 1;
-        ++rn;
-        --avail;
-      }
-      ff = -inv * kmc_log_unit(u_from_rand(rf), s_log);
+      ff = -inv * dlog;
       if (++hs > a.hop_cap) {  // leave this exciton where it is and report
         atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
         Exciton e;
