@@ -1,0 +1,85 @@
+"""The drop-in surfaces end to end on the GPU: `cntkmc_run input.json` (the reference's main) and
+the Python `monte_carlo` class, each driven by an input.json built from a golden case, must
+write the reference's MSD file with the reference's numbers (the golden fixtures are outputs of
+the reference's own code under the same Philox streams).
+"""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from cnt_film_monte_carlo_gb300 import build as B
+from cnt_film_monte_carlo_gb300 import film as F
+from cnt_film_monte_carlo_gb300 import monte_carlo as MC
+from helpers import CASES, load_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _film_from_case(d):
+    left = d["film_left"]
+    starts = np.nonzero(left < 0)[0]
+    offsets = np.append(starts, len(left)).astype(np.int64)
+    return F.Film(d["film_pos_nm"], d["film_orient"], left, d["film_right"], offsets)
+
+
+def _input_json(d, tmp, precision):
+    mesh = os.path.join(tmp, "mesh")
+    F.write_mesh(_film_from_case(d), mesh)
+    mc = dict(d["config"])
+    mc.update({"mesh input directory": mesh, "output directory": os.path.join(tmp, "out"),
+               "keep old results": False, "philox seed": int(d["seed"]), "precision": precision})
+    path = os.path.join(tmp, "input.json")
+    with open(path, "w") as f:
+        json.dump({"exciton monte carlo": mc}, f)
+    return path
+
+
+def _read_msd_file(out_dir):
+    rows = []
+    with open(os.path.join(out_dir, "particle_dispalcement.avg.squared.dat")) as f:
+        for line in f:
+            if line[:1] in ("+", "-"):
+                rows.append([float(v) for v in line.split(",")])
+    return np.array(rows)
+
+
+def _expected(d):
+    n = d["config"]["number of particles for kubo simulation"]
+    return d["ref_time"], d["ref_msd"].reshape(-1, 3) / n
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_driver_writes_reference_msd(name, precision, tmp_path):
+    d = load_case(name)
+    cfg = _input_json(d, str(tmp_path), precision)
+    B.build()
+    r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    got = _read_msd_file(os.path.join(str(tmp_path), "out"))
+    t, msd = _expected(d)
+    # main's loop runs while time < max time: accumulated rounding can add a step past the
+    # fixture's (the reference's main does the same)
+    assert got.shape[0] in (len(t), len(t) + 1) and got.shape[1] == 4
+    got = got[:len(t)]
+    np.testing.assert_allclose(got[:, 0], t, rtol=1e-6)   # the file holds %+e (7 significant digits)
+    np.testing.assert_allclose(got[:, 1:], msd, rtol=1e-6, atol=1e-30)
+    with open(os.path.join(str(tmp_path), "out", "input.json")) as f:  # save_json_properties
+        assert json.load(f)["number of particles for kubo simulation"] == d["config"][
+            "number of particles for kubo simulation"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_python_class_writes_reference_msd(name, tmp_path):
+    d = load_case(name)
+    cfg = _input_json(d, str(tmp_path), "mixed")
+    out = MC.run(cfg)
+    got = _read_msd_file(out)
+    t, msd = _expected(d)
+    assert got.shape[0] in (len(t), len(t) + 1)
+    got = got[:len(t)]
+    np.testing.assert_allclose(got[:, 0], t, rtol=1e-6)
+    np.testing.assert_allclose(got[:, 1:], msd, rtol=1e-6, atol=1e-30)
