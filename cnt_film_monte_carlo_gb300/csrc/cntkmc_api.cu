@@ -57,6 +57,7 @@ struct kmc_ctx {
   std::vector<std::array<double, 6>> domains;
   bool film_loaded = false;
   DevBuf<double4_32a> d_pos4;
+  DevBuf<float4> d_pos4f;  // FP32 copy for the neighbour screen
   DevBuf<double> d_orient;
   DevBuf<int32_t> d_left, d_right, d_site_film;
   DevBuf<FilmDev> d_films;
@@ -194,6 +195,7 @@ void kmc_destroy(kmc_ctx* c) {
   for (auto* b : {&c->d_cell_of, &c->d_cell_start, &c->d_cell_cursor, &c->d_rowptr, &c->d_scan, &c->d_trace_cnt})
     b->release();
   c->d_pos4.release();
+  c->d_pos4f.release();
   c->d_films.release();
   c->d_blkptr.release();
   c->d_blocks.release();
@@ -300,6 +302,31 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   return KMC_OK;
 }
 
+// Bounds of the FP32 pair screen.  With M the largest coordinate magnitude, the FP32 distance of
+// a pair differs from the FP64 one by at most sqrt(3) 2^-23 M + 5 2^-24 d (rounding of the
+// coordinates, the difference, the squares and the sum); the margin m = 2^-20 (M + r) is eight
+// times that, and each squared bound is rounded outward, so "surely outside / inside" never
+// disagrees with the FP64 test.
+static kmc::PairScreen pair_screen(double r, double M) {
+  const double m = std::ldexp(M, -20) + std::ldexp(r, -20);
+  auto up = [](double v) {
+    float f = (float)v;
+    return (double)f < v ? std::nextafterf(f, INFINITY) : f;
+  };
+  auto dn = [](double v) {
+    float f = (float)v;
+    return (double)f > v ? std::nextafterf(f, -INFINITY) : f;
+  };
+  const double lo = kmc::kMinHopDist;
+  kmc::PairScreen sc;
+  sc.out_hi2 = up((r + m) * (r + m));
+  sc.out_lo2 = lo > m ? dn((lo - m) * (lo - m)) : 0.f;
+  sc.in_lo2 = up((lo + m) * (lo + m));
+  sc.in_hi2 = r > m ? dn((r - m) * (r - m)) : 0.f;
+  if (!(sc.in_lo2 < sc.in_hi2)) sc.in_lo2 = sc.in_hi2 = 0.f;  // no pair is surely inside
+  return sc;
+}
+
 int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   if (!c) return KMC_ERR_ARG;
   if (!c->film_loaded || !c->has_table) FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: load a film and a rate table first");
@@ -349,8 +376,14 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, cudaMemsetAsync(c->d_rowptr.p, 0, (n + 1) * sizeof(int64_t), c->stream));
   CK(c, cudaMemsetAsync(c->d_stats.p, 0, 4 * sizeof(unsigned long long), c->stream));
   CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
+  double max_coord = 0;
+  for (double v : c->pos) max_coord = std::max(max_coord, std::fabs(v));
+  CK(c, c->d_pos4f.alloc(n));
+  CK(c, kmc::launch_pos_f32(c->d_pos4.p, c->d_pos4f.p, n, c->stream));
   kmc::BuildArgs a{};
   a.n_films = c->n_films;
+  a.pos4f = c->d_pos4f.p;
+  a.scr = pair_screen(r_max, max_coord);
   a.perm = c->d_perm.p;
   a.rank = c->d_rank.p;
   a.pos4 = c->d_pos4.p;

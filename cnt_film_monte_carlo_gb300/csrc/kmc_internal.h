@@ -102,9 +102,18 @@ struct HopArgs {
   double dt, v;
 };
 
+// FP32 screen of candidate pairs: squared-distance bounds (m^2) outside of which a pair is
+// surely out of / surely inside the window (kMinHopDist, r_max), whatever the FP32 rounding
+struct PairScreen {
+  float out_lo2, out_hi2;  // d2 <= out_lo2 or d2 >= out_hi2: outside
+  float in_lo2, in_hi2;    // in_lo2 < d2 < in_hi2: inside
+};
+
 struct BuildArgs {
   int32_t n_films;
   const double4_32a* pos4;
+  const float4* pos4f;     // FP32 copy of pos4
+  PairScreen scr;
   const double* orient;    // [n][3]
   const int32_t* site_film;
   const FilmDev* films;
@@ -138,6 +147,7 @@ struct BuildArgs {
 };
 
 // launchers (kmc_kernels.cu); all return cudaError_t of the launch
+cudaError_t launch_pos_f32(const double4_32a* p, float4* out, int64_t n, cudaStream_t s);
 cudaError_t launch_cell_ids(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_cell_fill(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_nbr_count(const BuildArgs& a, cudaStream_t s);

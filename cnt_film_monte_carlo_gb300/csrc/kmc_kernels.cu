@@ -64,6 +64,20 @@ __global__ void k_cell_sort(BuildArgs a) {
   }
 }
 
+// FP32 copy of the positions for the neighbour screen
+__global__ void k_pos_f32(const double4_32a* __restrict__ p, float4* __restrict__ out, int64_t n) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double4_32a v = p[s];
+  out[s] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+}
+
+cudaError_t launch_pos_f32(const double4_32a* p, float4* out, int64_t n, cudaStream_t s) {
+  int64_t nb = (n + 255) / 256;
+  if (nb) k_pos_f32<<<(unsigned)nb, 256, 0, s>>>(p, out, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_cell_ids(const BuildArgs& a, cudaStream_t s) {
   int64_t nb = (a.n_sites + 255) / 256;
   if (nb) k_cell_ids<<<(unsigned)nb, 256, 0, s>>>(a);
@@ -148,10 +162,15 @@ cudaError_t ids_to_slots(int32_t* ids, int64_t n, const int32_t* rank, cudaStrea
 
 // ============================================================================ K2: neighbour + rate CSR
 // Visit the neighbours of site s in find_neighbors order; fn(j, p2, dR, distance) per neighbour.
-template <typename F>
+// Candidates are screened with FP32 squared distances: a candidate clear of both window edges
+// (0.4 nm, r) by the screen's error bound is in or out without FP64 work; only those within
+// the bound of an edge take the reference's FP64 test, so the neighbour set is exact.  With
+// kGeom false (counting) accepted candidates get no FP64 geometry either.
+template <bool kGeom, typename F>
 __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s, F fn) {
   const FilmDev& f = a.films[a.site_film[s]];
   double4_32a p1 = a.pos4[s];
+  const float4 p1f = a.pos4f[s];
   int64_t local = a.cell_of[s] - f.cell0;
   int ix = (int)(local % f.nx);
   int iy = (int)((local / f.nx) % f.ny);
@@ -165,10 +184,19 @@ __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s,
         int64_t c = f.cell0 + i + (int64_t)j * f.nx + (int64_t)k * f.nx * f.ny;
         for (int64_t m = a.cell_start[c], e = a.cell_start[c + 1]; m < e; ++m) {
           int32_t q = a.cell_members[m];
+          const float4 p2f = a.pos4f[q];
+          const float fx = p1f.x - p2f.x, fy = p1f.y - p2f.y, fz = p1f.z - p2f.z;
+          const float d2 = fx * fx + fy * fy + fz * fz;
+          if (d2 >= a.scr.out_hi2 || d2 <= a.scr.out_lo2) continue;  // surely outside the window
+          const bool inside = d2 < a.scr.in_hi2 && d2 > a.scr.in_lo2;  // surely inside
+          if (!kGeom && inside) {
+            fn(q, p1, 0.0, 0.0, 0.0, 0.0);
+            continue;
+          }
           double4_32a p2 = a.pos4[q];
           double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
           double distance = norm3(dR0, dR1, dR2);
-          if ((distance < a.r_max) && (distance > kMinHopDist)) fn(q, p2, dR0, dR1, dR2, distance);
+          if (inside || ((distance < a.r_max) && (distance > kMinHopDist))) fn(q, p2, dR0, dR1, dR2, distance);
         }
       }
     }
@@ -179,7 +207,7 @@ __global__ void k_nbr_count(BuildArgs a) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= a.n_sites) return;
   int64_t n = 0;
-  for_each_neighbor(a, s, [&](int32_t, const double4_32a&, double, double, double, double) { ++n; });
+  for_each_neighbor<false>(a, s, [&](int32_t, const double4_32a&, double, double, double, double) { ++n; });
   a.counts[s] = n;
   atomicMax(&a.stats[0], (unsigned long long)n);
   if (n == 0) atomicAdd(&a.stats[1], 1ull);
@@ -199,7 +227,7 @@ __global__ void k_nbr_fill(BuildArgs a) {
   int64_t k = 0;
   double run = 0.0;
   bool negative = false;
-  for_each_neighbor(a, s, [&](int32_t q, const double4_32a& p2, double dR0, double dR1, double dR2, double distance) {
+  for_each_neighbor<true>(a, s, [&](int32_t q, const double4_32a& p2, double dR0, double dR1, double dR2, double distance) {
     double a2v[3] = {a.orient[3 * (int64_t)q], a.orient[3 * (int64_t)q + 1], a.orient[3 * (int64_t)q + 2]};
     double rate = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance);
     negative |= rate < 0;

@@ -402,3 +402,38 @@ def test_random_geometry_csr_matches_oracle(table_kind):
     for k in ("rowptr", "col", "cum", "total"):
         assert np.array_equal(nb[k], csr[k]), k
     e.close()
+
+
+@pytest.mark.parametrize("offset", [0.0, 2.5e-6])
+def test_window_edges_match_oracle(offset):
+    # pairs at distances within a few ulps of the window edges (0.4 nm and the cutoff) in every
+    # direction: the FP32 screen must hand all of them to the FP64 test, whose verdict decides
+    r = 8e-9
+    rng = np.random.default_rng(5)
+    centres = offset + rng.uniform(20e-9, 60e-9, size=(60, 3))
+    pos = [centres]
+    for edge in (r, 0.4e-9):
+        for ulps in (-3, -1, 0, 1, 3):
+            d = np.full(len(centres), edge)
+            for _ in range(abs(ulps)):
+                d = np.nextafter(d, np.inf if ulps > 0 else -np.inf)
+            u = rng.normal(size=(len(centres), 3))
+            u /= np.linalg.norm(u, axis=1)[:, None]
+            pos.append(centres + d[:, None] * u)
+    pos = np.concatenate(pos)
+    n = len(pos)
+    ax = rng.normal(size=(n, 3))
+    ax /= np.linalg.norm(ax, axis=1)[:, None]
+    lk = np.full(n, -1, np.int32)
+    rk = np.full(n, -1, np.int32)
+    tab = tables.forster_2d(1e15)
+    sim = O.Sim(pos, ax, lk, rk, tab, r, 2e5, n_threads=4)
+    csr = sim.build_csr()
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, n], np.int64), pos, ax, lk, rk)
+    e.set_table(tab)
+    st = e.build(r)
+    nb = e.neighbors(n, st["nnz"])
+    for k in ("rowptr", "col", "cum", "total"):
+        assert np.array_equal(nb[k], csr[k]), k
+    e.close()
