@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/cntkmc.h"
@@ -17,10 +18,30 @@ using kmc::FilmDev;
 
 namespace {
 
+// Owning device buffer (freed on destruction; movable, not copyable), so early error returns
+// leak nothing.
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
   cudaError_t alloc(size_t count) {
     release();
     if (count == 0) count = 1;
@@ -605,8 +626,7 @@ static int ensure_msd(kmc_ctx* c, int64_t need) {
                             c->steps_done * row * sizeof(double), c->n_films, cudaMemcpyDeviceToDevice, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   c->d_msd.release();
-  c->d_msd = nb;
-  nb.p = nullptr;
+  c->d_msd = std::move(nb);
   c->msd_cap = cap;
   return KMC_OK;
 }

@@ -203,9 +203,12 @@ __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s,
   }
 }
 
+// Both passes take the sites in storage order (thread i: site perm[i]), so the threads of a warp
+// scan the same cells and write neighbouring rows.
 __global__ void k_nbr_count(BuildArgs a) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= a.n_sites) return;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= a.n_sites) return;
+  const int64_t s = a.perm[i];
   int64_t n = 0;
   for_each_neighbor<false>(a, s, [&](int32_t, const double4_32a&, double, double, double, double) { ++n; });
   a.counts[s] = n;
@@ -216,12 +219,13 @@ __global__ void k_nbr_count(BuildArgs a) {
 // Row of site s (reference id) into storage slot rank[s]; neighbour ids and links are stored as
 // storage slots, so the hop kernels never translate ids.
 __global__ void k_nbr_fill(BuildArgs a) {
-  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s >= a.n_sites) return;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= a.n_sites) return;
+  const int64_t s = a.perm[i];
   const FilmDev& f = a.films[a.site_film[s]];
   double4_32a p1 = a.pos4[s];
   double a1v[3] = {a.orient[3 * s], a.orient[3 * s + 1], a.orient[3 * s + 2]};
-  const int64_t si = a.rank[s];
+  const int64_t si = i;  // the row's storage slot (rank[s])
   const int64_t bo = a.blkptr[si];
   double* cump = a.cump + bo * 8;  // this row's FP64 cumulative rates (8 per block)
   int64_t k = 0;
