@@ -1,6 +1,7 @@
 // kmc_hop_mixed.cuh -- the mixed-precision hop kernel, a template over (threads per block,
 // resident blocks per SM).  Instantiated in kmc_mixed_small.cu (128-thread blocks) and
-// kmc_mixed_large.cu (256- and 768-thread blocks) so that the variants compile in parallel.
+// kmc_mixed_large.cu (256-, 768- and 1024-thread blocks) so that the variants compile in
+// parallel.
 #pragma once
 
 #include "kmc_hop_common.cuh"

@@ -39,7 +39,7 @@ extern "C" {
 
 #define KMC_ORDER_AUTO (-1)  /* spatial order when there are several excitons per resident lane */
 #define KMC_ORDER_SLOTS 0    /* excitons taken in slot order */
-#define KMC_ORDER_SPATIAL 1  /* excitons taken in order of the cell of their current site */
+#define KMC_ORDER_SPATIAL 1  /* excitons taken in spatial order of their current site */
 
 typedef struct kmc_ctx kmc_ctx;
 
