@@ -1,7 +1,7 @@
 /* kmc_oracle.h -- TEST INFRASTRUCTURE: CPU restatement of the reference's exciton-hopping
  * hot path (amirhosseindavoody/cnt_film_monte_carlo, src/monte_carlo/).
  *
- * This is the checker for the CUDA engine and the "port" CPU baseline of the benchmark.
+ * It is what the tests compare the CUDA engine with, and the "port" CPU baseline of the benchmark.
  * Only tests/, __graft_entry__.smoke() and bench.py (its CPU-baseline and reference legs)
  * load it; the product never does.
  *

@@ -2,7 +2,7 @@
 
 The oracle is the CPU restatement of the reference's hot path (oracle/kmc_oracle.c).  Only
 tests/, __graft_entry__.smoke() and bench.py (CPU baseline / reference leg) import this
-module, and only as the checker or the timed CPU path -- never inside the product.
+module, and only as the test oracle or the timed CPU path -- never inside the product.
 """
 from __future__ import annotations
 

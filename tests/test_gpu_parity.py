@@ -407,7 +407,7 @@ def test_random_geometry_csr_matches_oracle(table_kind):
 @pytest.mark.parametrize("offset", [0.0, 2.5e-6])
 def test_window_edges_match_oracle(offset):
     # pairs at distances within a few ulps of the window edges (0.4 nm and the cutoff) in every
-    # direction: the FP32 screen must hand all of them to the FP64 test, whose verdict decides
+    # direction: the FP32 screen must hand all of them to the FP64 test, whose answer decides
     r = 8e-9
     rng = np.random.default_rng(5)
     centres = offset + rng.uniform(20e-9, 60e-9, size=(60, 3))
