@@ -254,7 +254,7 @@ def main():
     e.set_graph(not args.no_graph)
     if args.variant is not None:
         e.set_mixed_variant(args.variant)
-    tune = e.autotune(BIN, VEL, trial_steps=1) if not (args.no_tune or args.variant is not None) else None
+    tune = e.autotune(BIN, VEL, trial_steps=2) if not (args.no_tune or args.variant is not None) else None
     for _ in range(args.warmup):
         e.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
     s0 = e.stats()

@@ -96,3 +96,38 @@ def test_cfg3_batch_orders_and_precisions_agree():
     assert ss["hops"] == so["hops"] == sf["hops"]
     np.testing.assert_allclose(ms, mf, rtol=1e-12)
     np.testing.assert_allclose(mo, mf, rtol=1e-12)
+
+
+def test_region_injection_with_removal_at_scale():
+    # the reference's own set-up (central injection cell, removal slab, reinjection): many
+    # excitons leave the removal domain, so the reinjection draw and the per-lane draw ring
+    # restart are exercised thousands of times; spatial order and multi-step launches included
+    f = F.straight_tubes(100, 200.0, box_nm=(500.0, 500.0, 10.0), max_tilt_deg=5.0, seed=1234)
+    tab = tables.forster_2d(1e15)
+    n_exc, seed, dt, steps = 400_000, 99, 2e-12, 6
+    out = []
+    for precision, order, spl in ((L.KMC_PREC_MIXED, L.KMC_ORDER_SPATIAL, 1), (L.KMC_PREC_MIXED, L.KMC_ORDER_SLOTS, 3),
+                                  (L.KMC_PREC_FP64, L.KMC_ORDER_AUTO, 1)):
+        e = E.Engine(0)
+        e.load_films([f])
+        e.set_table(tab)
+        e.build(10e-9)
+        e.set_work_order(order)
+        e.set_launch_config(128, spl)
+        e.init_excitons([n_exc], [seed], L.KMC_INJECT_REGION, n_sections=3)
+        e.run(steps, dt, V, precision)
+        out.append((e.excitons(), e.msd(0, steps), e.stats()))
+        e.close()
+    g0 = out[0][0]
+    assert (g0["draws"] > 0).all()
+    for g, m, st in out[1:]:
+        assert_same(g0, g)
+        np.testing.assert_allclose(m, out[0][1], rtol=1e-12)
+        assert st["hops"] == out[0][2]["hops"]
+    n = 64
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, 10e-9, V, n_threads=8)
+    sim.create_excitons(0, 3, n, seed)
+    sim.step(dt, steps)
+    o = sim.excitons()
+    for k in ("site", "pos", "delta", "ff", "heading", "draws"):
+        assert np.array_equal(g0[k][:n], o[k]), k
