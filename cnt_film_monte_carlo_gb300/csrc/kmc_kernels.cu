@@ -217,7 +217,10 @@ __global__ void k_nbr_count(BuildArgs a) {
 }
 
 // Row of site s (reference id) into storage slot rank[s]; neighbour ids and links are stored as
-// storage slots, so the hop kernels never translate ids.
+// storage slots, so the hop kernels never translate ids.  Two phases: the screen collects the
+// neighbours' reference ids in list order into the row's id slots, then the FP64 pair geometry
+// runs over that list, so the lanes of a warp do their FP64 work together instead of only on
+// the candidates each happens to accept.
 __global__ void k_nbr_fill(BuildArgs a) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= a.n_sites) return;
@@ -229,17 +232,24 @@ __global__ void k_nbr_fill(BuildArgs a) {
   const int64_t bo = a.blkptr[si];
   double* cump = a.cump + bo * 8;  // this row's FP64 cumulative rates (8 per block)
   int64_t k = 0;
+  for_each_neighbor<false>(a, s, [&](int32_t q, const double4_32a&, double, double, double, double) {
+    a.blocks[bo + (k >> 3)].col[k & 7] = q;
+    ++k;
+  });
   double run = 0.0;
   bool negative = false;
-  for_each_neighbor<true>(a, s, [&](int32_t q, const double4_32a& p2, double dR0, double dR1, double dR2, double distance) {
+  for (int64_t j = 0; j < k; ++j) {
+    const int32_t q = a.blocks[bo + (j >> 3)].col[j & 7];
+    const double4_32a p2 = a.pos4[q];
+    const double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
+    const double distance = norm3(dR0, dR1, dR2);
     double a2v[3] = {a.orient[3 * (int64_t)q], a.orient[3 * (int64_t)q + 1], a.orient[3 * (int64_t)q + 2]};
     double rate = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance);
     negative |= rate < 0;
-    run = (k == 0) ? rate : run + rate;  // in-place inclusive prefix sum, scatterer.cpp:78-80
-    cump[k] = run;
-    a.blocks[bo + (k >> 3)].col[k & 7] = a.rank[q];
-    ++k;
-  });
+    run = (j == 0) ? rate : run + rate;  // in-place inclusive prefix sum, scatterer.cpp:78-80
+    cump[j] = run;
+    a.blocks[bo + (j >> 3)].col[j & 7] = a.rank[q];
+  }
   double tot = k > 0 ? run : 0.0;
   double inv = 1. / tot;
   a.total[si] = tot;
