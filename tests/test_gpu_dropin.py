@@ -46,6 +46,14 @@ def _read_msd_file(out_dir):
     return np.array(rows)
 
 
+def _header_ok(out_dir, n):
+    # the reference's header (monte_carlo.cpp:384-392; showpos leaves the unsigned count bare)
+    with open(os.path.join(out_dir, "particle_dispalcement.avg.squared.dat")) as f:
+        head = [f.readline() for _ in range(4)]
+    assert head == ["# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble over time\n",
+                    f"# number of particles: {n}\n", "\n", "time,x,y,z\n"]
+
+
 def _expected(d):
     n = d["config"]["number of particles for kubo simulation"]
     return d["ref_time"], d["ref_msd"].reshape(-1, 3) / n
@@ -60,6 +68,7 @@ def test_driver_writes_reference_msd(name, precision, tmp_path):
     r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     got = _read_msd_file(os.path.join(str(tmp_path), "out"))
+    _header_ok(os.path.join(str(tmp_path), "out"), d["config"]["number of particles for kubo simulation"])
     t, msd = _expected(d)
     # main's loop runs while time < max time: accumulated rounding can add a step past the
     # fixture's (the reference's main does the same)
@@ -78,6 +87,7 @@ def test_python_class_writes_reference_msd(name, tmp_path):
     cfg = _input_json(d, str(tmp_path), "mixed")
     out = MC.run(cfg)
     got = _read_msd_file(out)
+    _header_ok(out, d["config"]["number of particles for kubo simulation"])
     t, msd = _expected(d)
     assert got.shape[0] in (len(t), len(t) + 1)
     got = got[:len(t)]
