@@ -36,13 +36,13 @@ __device__ __forceinline__ bool dwell_fits(double ff, double rem) {
 }
 
 // Step-boundary state of one lane's exciton, kept in shared memory (one slot per thread): only
-// the event loop's hot values stay in registers, which lets more warps stay resident.
+// the event loop's hot values stay in registers, which lets more warps stay resident.  The
+// exciton's Philox key and stream (film seed, index in the film) are re-derived from the slot
+// when needed, leaving more of the SM's shared-memory/L1 array to the L1 cache.
 struct ColdState {
   double p[3];   // position (valid when not at the site)
   double o[3];   // position at the start of the step
   double d[3];   // Green-Kubo displacement
-  uint64_t seed, stream;
-  int64_t trace_i;
 };
 
 // Draw buffer of a lane: a ring of 8 Philox words in shared memory (word k of the lane at
@@ -53,19 +53,18 @@ struct DrawRing {
   int stride;   // BLOCK
   __device__ __forceinline__ uint32_t word(uint64_t i) const { return r[(int)(i & 7) * stride]; }
   // Philox block b = d / 4 (d a multiple of 4) into its ring words
-  __device__ __forceinline__ void fill(uint64_t d, const ColdState* c) const {
+  __device__ __forceinline__ void fill(uint64_t d, uint64_t seed, uint64_t stream) const {
     const uint64_t b = d >> 2;
     uint32_t o[4];
-    philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), (uint32_t)c->stream, (uint32_t)(c->stream >> 32),
-                  (uint32_t)c->seed, (uint32_t)(c->seed >> 32), o);
+    philox4x32_10((uint32_t)b, (uint32_t)(b >> 32), (uint32_t)stream, (uint32_t)(stream >> 32), (uint32_t)seed,
+                  (uint32_t)(seed >> 32), o);
     const int k = (int)(d & 4);
 #pragma unroll
     for (int j = 0; j < 4; ++j) r[(k + j) * stride] = o[j];
   }
 };
 
-__device__ __forceinline__ void cold_trace(const HopArgs& a, const ColdState* c, int32_t v) {
-  int64_t t = c->trace_i;
+__device__ __forceinline__ void cold_trace(const HopArgs& a, int64_t t, int32_t v) {
   int64_t k = a.trace_cnt[t];
   if (k < a.trace_cap) a.trace[t * a.trace_cap + k] = v;
   a.trace_cnt[t] = k + 1;
@@ -130,7 +129,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
     // of once per hop for half of its lanes.
     if (__any_sync(0xffffffffu, alive && cur >= 0 && avail < 2)) {
       if (alive && cur >= 0 && avail <= 4) {
-        ring.fill(rn + avail, cs);
+        ring.fill(rn + avail, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
         avail += 4;
       }
     }
@@ -161,12 +160,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       site = a.e_site[cur];
       ff = a.e_ff[cur];
       int64_t local = cur - fp->slot0;
-      cs->trace_i = (film == 0 && local < a.n_trace) ? local : -1;
-      tracing = cs->trace_i >= 0;
-      cs->seed = fp->seed;
-      cs->stream = (uint64_t)local;
+      tracing = film == 0 && local < a.n_trace;
       rn = a.e_draws[cur];
-      ring.fill(rn & ~3ull, cs);
+      ring.fill(rn & ~3ull, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
       avail = 4 - (uint32_t)(rn & 3);
       double px, py, pz;
       if (at_site) {
@@ -225,7 +221,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
             at_site = true;
             dtf -= lt;
             ecross++;
-            if (tracing) cold_trace(a, cs, -1 - next);
+            if (tracing) cold_trace(a, cur - a.films[film].slot0, -1 - next);
             load_rec(next);
             continue;
           }
@@ -259,7 +255,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), q1 = q0;
       if (n > 0) {
         if (avail < 2) {  // first hop after taking an exciton
-          ring.fill(rn + avail, cs);
+          ring.fill(rn + avail, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
           avail += 4;
         }
         r = ring.word(rn) >> 1;
@@ -271,7 +267,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         q1 = __ldg(cq + 1);
       } else {
         if (avail == 0) {
-          ring.fill(rn, cs);
+          ring.fill(rn, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
           avail = 4;
         }
         rf = ring.word(rn) >> 1;
@@ -280,7 +276,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       }
       while (rf == 0) {  // ff_time rejects r == 0
         if (avail == 0) {
-          ring.fill(rn, cs);
+          ring.fill(rn, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
           avail = 4;
         }
         rf = ring.word(rn) >> 1;
@@ -385,7 +381,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         }
       }
       ehops++;
-      if (tracing) cold_trace(a, cs, nsite);
+      if (tracing) cold_trace(a, cur - a.films[film].slot0, nsite);
       if (nsite != site) {
         site = nsite;
         at_site = true;
@@ -427,7 +423,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         e.py = cs->p[1];
         e.pz = cs->p[2];
       }
-      e.trace_i = cs->trace_i;
+      e.trace_i = tracing ? cur - f.slot0 : -1;
       e.crossings = 0;
       fly_full(a, e, rem);
       ecross += (uint32_t)e.crossings;
@@ -439,10 +435,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       e.dy = dy;
       e.dz = dz;
       e.at_site = false;
-      e.g.seed = cs->seed;
-      e.g.stream = cs->stream;
+      e.g.seed = f.seed;
+      e.g.stream = (uint64_t)(cur - f.slot0);
       if (avail == 0) {  // the Rng below holds the rest of the current block
-        ring.fill(rn, cs);
+        ring.fill(rn, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
         avail = 4;
       }
       e.g.n = rn;
@@ -453,7 +449,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       maybe_reinject(a, f, e);
       if (e.g.n != rn) {  // the reinjection drew: restart the ring at the new draw index
         rn = e.g.n;
-        ring.fill(rn & ~3ull, cs);
+        ring.fill(rn & ~3ull, a.films[film].seed, (uint64_t)(cur - a.films[film].slot0));
         avail = 4 - (uint32_t)(rn & 3);
       }
       site = e.site;
