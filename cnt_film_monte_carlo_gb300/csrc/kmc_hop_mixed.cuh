@@ -37,12 +37,11 @@ __device__ __forceinline__ bool dwell_fits(double ff, double rem) {
 
 // Step-boundary state of one lane's exciton, kept in shared memory (one slot per thread): only
 // the event loop's hot values stay in registers, which lets more warps stay resident.  The
-// exciton's Philox key and stream (film seed, index in the film) are re-derived from the slot
-// when needed, leaving more of the SM's shared-memory/L1 array to the L1 cache.
+// exciton's Philox key and stream (film seed, index in the film) are re-derived from the slot,
+// and the step's starting point and displacement stay in the slot arrays until the step ends,
+// leaving more of the SM's shared-memory/L1 array to the L1 cache.
 struct ColdState {
   double p[3];   // position (valid when not at the site)
-  double o[3];   // position at the start of the step
-  double d[3];   // Green-Kubo displacement
 };
 
 // Draw buffer of a lane: a ring of 8 Philox words in shared memory (word k of the lane at
@@ -170,17 +169,18 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         px = p.x;
         py = p.y;
         pz = p.z;
+        // the slot's position array holds the step's starting point until the step ends
+        a.e_pos[cur] = px;
+        a.e_pos[ns + cur] = py;
+        a.e_pos[2 * ns + cur] = pz;
       } else {
         px = a.e_pos[cur];
         py = a.e_pos[ns + cur];
         pz = a.e_pos[2 * ns + cur];
       }
-      cs->p[0] = cs->o[0] = px;
-      cs->p[1] = cs->o[1] = py;
-      cs->p[2] = cs->o[2] = pz;
-      cs->d[0] = a.e_delta[cur];
-      cs->d[1] = a.e_delta[ns + cur];
-      cs->d[2] = a.e_delta[2 * ns + cur];
+      cs->p[0] = px;
+      cs->p[1] = py;
+      cs->p[2] = pz;
       rem = a.dt;
       s = 0;
       hs = 0;
@@ -398,9 +398,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         e.px = cs->p[0];
         e.py = cs->p[1];
         e.pz = cs->p[2];
-        e.dx = cs->d[0];
-        e.dy = cs->d[1];
-        e.dz = cs->d[2];
+        e.dx = a.e_delta[cur];
+        e.dy = a.e_delta[a.n_slots + cur];
+        e.dz = a.e_delta[2 * a.n_slots + cur];
         e.ff = ff;
         e.g.n = rn;
         e.hops = ehops;
@@ -428,9 +428,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       fly_full(a, e, rem);
       ecross += (uint32_t)e.crossings;
       ff -= rem;
-      double dx = cs->d[0] + (e.px - cs->o[0]);
-      double dy = cs->d[1] + (e.py - cs->o[1]);
-      double dz = cs->d[2] + (e.pz - cs->o[2]);
+      // update_delta_pos: delta += pos - old_pos, with the step's start in the slot arrays
+      const int64_t nsl = a.n_slots;
+      double dx = a.e_delta[cur] + (e.px - a.e_pos[cur]);
+      double dy = a.e_delta[nsl + cur] + (e.py - a.e_pos[nsl + cur]);
+      double dz = a.e_delta[2 * nsl + cur] + (e.pz - a.e_pos[2 * nsl + cur]);
       e.dx = dx;
       e.dy = dy;
       e.dz = dz;
@@ -476,12 +478,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         cur = -1;
         continue;
       }
-      cs->p[0] = cs->o[0] = e.px;
-      cs->p[1] = cs->o[1] = e.py;
-      cs->p[2] = cs->o[2] = e.pz;
-      cs->d[0] = dx;
-      cs->d[1] = dy;
-      cs->d[2] = dz;
+      cs->p[0] = e.px;
+      cs->p[1] = e.py;
+      cs->p[2] = e.pz;
+      a.e_pos[cur] = e.px;  // the next step's start
+      a.e_pos[nsl + cur] = e.py;
+      a.e_pos[2 * nsl + cur] = e.pz;
+      a.e_delta[cur] = dx;
+      a.e_delta[nsl + cur] = dy;
+      a.e_delta[2 * nsl + cur] = dz;
       rem = a.dt;
       hs = 0;
       load_rec(site);
