@@ -17,7 +17,7 @@ struct FilmDev {
   int32_t nx, ny, nz, mode; // cell grid; injection mode
   double mn[3];             // domain minimum (cell origin)
   double r;                 // cell side = max hopping radius
-  int64_t inj0, n_inj;      // injection sites (global ids) in the inject array
+  int64_t inj0, n_inj;      // injection sites (storage slots) in the inject array
   double rmin[3], rmax[3];  // removal domain (mode 0)
   uint64_t seed;            // Philox key
   int64_t slot0, n_exc;     // exciton slots (padded to whole warps)
@@ -31,13 +31,13 @@ struct __align__(64) SiteRec {
   double inv_total;   // 1 / total rate (inf for an empty list)
   uint32_t blk;       // film-local index of the row's first 8-entry block
   uint32_t len_flags; // row length (low 24 bits) | flags
-  int32_t left, right;// global site ids or -1
+  int32_t left, right;// tube neighbours (storage slots) or -1
   uint32_t lt_hi_l;   // high 32 bits of the FP64 link time to the left / right neighbour
   uint32_t lt_hi_r;
   float coarse[8];
 };
-// One 64-byte block of a neighbour row: 8 FP32 values of cum/total and the 8 neighbour ids
-// (global site ids); entries past the row end hold +inf and -1.
+// One 64-byte block of a neighbour row: 8 FP32 values of cum/total and the 8 neighbours
+// (storage slots); entries past the row end hold +inf and -1.
 struct __align__(64) RowBlock {
   float c[8];
   int32_t col[8];
@@ -60,11 +60,11 @@ constexpr uint32_t kExAtSite = 2u;   // position equals the current site's posit
 constexpr uint32_t kExActive = 4u;   // slot holds an exciton (not warp padding)
 
 struct HopArgs {
-  // sites
+  // sites: every array indexed by storage slot (spatial order), except rowptr
   const double4_32a* pos4;
   const int32_t* left;
   const int32_t* right;
-  const int64_t* rowptr;  // global
+  const int64_t* rowptr;  // reference-order CSR offsets (read-back)
   const int64_t* blkptr;  // first row block of each site (global)
   const double* total;
   const double* inv_total;
