@@ -437,3 +437,29 @@ def test_window_edges_match_oracle(offset):
     for k in ("rowptr", "col", "cum", "total"):
         assert np.array_equal(nb[k], csr[k]), k
     e.close()
+
+
+@pytest.mark.parametrize("precision", [L.KMC_PREC_FP64, L.KMC_PREC_MIXED])
+def test_zero_rate_entries_match_oracle(precision):
+    # a table with zero rates in whole bands: rows get runs of equal cumulative values, which
+    # update_state skips (first cum > dice); the FP32 search must agree on every tie
+    f, tab, r_max = synthetic_case(2)
+    rate = tab["rate"].copy()
+    rate[:, 30:60] = 0.0        # angles 30-59 deg
+    rate[40:70, :] = 0.0        # distances ~4.4-7.6 nm
+    tab = {"kind": 2, "grids": tab["grids"], "rate": rate}
+    n_exc, seed, dt, v, steps = 800, 77, 2e-13, 2e5, 8
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, r_max, v)
+    sim.create_excitons(1, 0, n_exc, seed)
+    om = sim.step(dt, steps)
+    o = sim.excitons()
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_table(tab)
+    e.build(r_max)
+    e.init_excitons(n_exc, seed, L.KMC_INJECT_UNIFORM)
+    e.run(steps, dt, v, precision)
+    assert_states_equal(e.excitons(), o)
+    assert_msd_close(e.msd(0, steps), om)
+    assert e.stats()["hops"] == sim.total_hops()
+    e.close()
