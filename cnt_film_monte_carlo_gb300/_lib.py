@@ -21,6 +21,7 @@ KMC_ERR_IO = -4
 KMC_ERR_HOP_CAP = -5
 KMC_ERR_NOMEM = -6
 KMC_ERR_NO_DEVICE = -7
+KMC_ERR_CAPACITY = -8
 KMC_TABLE_4D = 4
 KMC_TABLE_2D = 2
 KMC_INJECT_REGION = 0
@@ -66,6 +67,16 @@ class kmc_tune_result(C.Structure):
     _fields_ = [("variant", C.c_int32), ("steps_per_launch", C.c_int32), ("hops_per_s", C.c_double)]
 
 
+class kmc_contacts(C.Structure):
+    _fields_ = [("n_segments", C.c_int32), ("contact_pop", C.c_int64 * 2), ("seed", C.c_uint64),
+                ("capacity", C.c_int64)]
+
+
+class kmc_contacts_info(C.Structure):
+    _fields_ = [("ymin", C.c_double), ("ymax", C.c_double), ("dy", C.c_double), ("n_initial", C.c_int64),
+                ("n_contact", C.c_int64 * 2), ("capacity", C.c_int64)]
+
+
 # every symbol include/cntkmc.h declares, with (restype, argtypes)
 SIGNATURES = {
     "kmc_create": (C.c_void_p, [C.c_int, C.POINTER(C.c_int)]),
@@ -80,6 +91,8 @@ SIGNATURES = {
     "kmc_set_msd_batches": (C.c_int, [C.c_void_p, C.c_int32]),
     "kmc_get_msd_batches": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, PD]),
     "kmc_fit_diffusion": (C.c_int, [PD, PI64, PD, C.c_int64, C.c_int32, C.c_double, PD, PD]),
+    "kmc_contacts_init": (C.c_int, [C.c_void_p, C.POINTER(kmc_contacts), C.POINTER(kmc_contacts_info), PD, PI64]),
+    "kmc_contacts_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32, PI64, PI64, PI64]),
     "kmc_get_excitons": (C.c_int, [C.c_void_p, PI32, PD, PD, PD, PI32, PU64, PI64]),
     "kmc_num_excitons": (C.c_int64, [C.c_void_p]),
     "kmc_get_run_stats": (C.c_int, [C.c_void_p, C.POINTER(kmc_run_stats)]),

@@ -1,0 +1,86 @@
+"""Output files of the contacts (steady-state flux) mode in the reference's formats.
+
+* ``scatterer_statistics.dat``: get_scatterer_statistics (src/monte_carlo/monte_carlo.h:691-710),
+  written once by init.
+* ``population_profile.dat``: save_population_profile (:528-575), one row per step with the
+  exciton density count / (area dy) of every y slab.
+* ``region_current.dat``: save_currents (:578-625), one row per step with the current
+  count / (interface area dt) through every slab interface.
+
+The reference writes them with iostreams in std::scientific (precision 6), the last two also with
+std::showpos, which prints a sign on every signed value -- also on the interface numbers of the
+current-file header ("interface+0"), but not on the unsigned section numbers ("section0").
+Densities and currents are formed from integer counts here exactly as there (one FP64 division
+by one FP64 product), so the files agree character for character.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _div(a: float, b: float) -> float:
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return float(np.float64(a) / np.float64(b))
+
+
+def _e(x: float, plus: bool) -> str:
+    """iostream std::scientific (with std::showpos when plus) of a double."""
+    if math.isnan(x):
+        s = "nan"
+        return ("-" if math.copysign(1.0, x) < 0 else ("+" if plus else "")) + s
+    return f"{x:+e}" if plus else f"{x:e}"
+
+
+def slab_positions(ymin: float, dy: float, n: int) -> np.ndarray:
+    """Slab centres ymin + (i + 0.5) dy (monte_carlo.h:545-547, 704-706)."""
+    return np.array([ymin + (float(i) + 0.5) * dy for i in range(n)])
+
+
+def interface_positions(ymin: float, dy: float, n: int) -> np.ndarray:
+    """Interfaces ymin + dy i, i = 1..n-1 (save_currents :585-589)."""
+    return np.array([ymin + dy * float(i) for i in range(1, n)])
+
+
+def interface_areas(area) -> np.ndarray:
+    """(area[i-1] + area[i]) / 2 (save_currents :588)."""
+    a = np.asarray(area, dtype=np.float64)
+    return np.array([(a[i - 1] + a[i]) / 2 for i in range(1, len(a))])
+
+
+def scatterer_statistics_text(ymin: float, dy: float, stat_pop, n_sites: int, area) -> str:
+    out = ["position,distribution,population,density\n"]
+    pos = slab_positions(ymin, dy, len(stat_pop))
+    for i, p in enumerate(stat_pop):
+        p = int(p)
+        out.append(f"{_e(pos[i], False)},{_e(_div(float(p), float(n_sites)), False)},{p},"
+                   f"{_e(_div(float(p), float(area[i]) * dy), False)}\n")
+    return "".join(out)
+
+
+def population_header(area, ymin: float, dy: float) -> str:
+    n = len(area)
+    pos = slab_positions(ymin, dy, n)
+    return ("area" + "".join("," + _e(float(a), True) for a in area) + "\n\n"
+            + "dy" + ("," + _e(dy, True)) * n + "\n\n"
+            + "section pos" + "".join("," + _e(float(p), True) for p in pos) + "\n\n"
+            + "time" + "".join(f",section{i}" for i in range(n)) + "\n")
+
+
+def population_row(time: float, counts, area, dy: float) -> str:
+    return _e(time, True) + "".join("," + _e(_div(float(c), float(a) * dy), True) for c, a in zip(counts, area)) + "\n"
+
+
+def current_header(area, ymin: float, dy: float) -> str:
+    n = len(area)
+    aif = interface_areas(area)
+    y = interface_positions(ymin, dy, n)
+    return ("interface area" + "".join("," + _e(float(a), True) for a in aif) + "\n\n"
+            + "interface pos" + "".join("," + _e(float(v), True) for v in y) + "\n\n"
+            + "time" + "".join(f",interface{i:+d}" for i in range(n - 1)) + "\n")
+
+
+def current_row(time: float, counts, area, dt: float) -> str:
+    aif = interface_areas(area)
+    return _e(time, True) + "".join("," + _e(_div(float(c), float(a) * dt), True) for c, a in zip(counts, aif)) + "\n"

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <utility>
 #include <vector>
@@ -139,6 +140,15 @@ struct kmc_ctx {
   // the launch sequence of a run is captured into a CUDA graph and replayed
   bool use_graph = true;
   cudaGraphExec_t gexec = nullptr;
+  // contacts (steady-state flux) mode
+  bool contacts = false;
+  kmc::ContactArgs cargs{};
+  int64_t c_steps = 0;
+  DevBuf<int32_t> d_c_list;  // contact-1 sites then contact-n sites (storage slots)
+  DevBuf<double> d_c_yif, d_y_old;
+  DevBuf<int64_t> d_c_blk_a, d_c_blk_b, d_c_scan, d_c_step;
+  DevBuf<unsigned long long> d_c_pop, d_c_diff, d_c_live;
+  cudaGraphExec_t cgexec = nullptr;  // one contacts step, replayed
 };
 
 #define FAIL(ctx, code, ...)                                          \
@@ -235,6 +245,7 @@ void kmc_destroy(kmc_ctx* c) {
   for (auto* b : {&c->d_order, &c->d_perm, &c->d_rank, &c->d_left_i, &c->d_right_i}) b->release();
   c->d_pos4i.release();
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->cgexec) cudaGraphExecDestroy(c->cgexec);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -610,6 +621,7 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
   CK(c, kmc::launch_init_excitons(a, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   c->stats = kmc_run_stats{};
+  c->contacts = false;
   c->inited = true;
   return KMC_OK;
 }
@@ -694,74 +706,118 @@ static int ensure_order_buffers(kmc_ctx* c) {
   return KMC_OK;
 }
 
+// What a hop launch needs besides its arguments: exact link times for the velocity (mixed), the
+// work-order buffers, the grid of the persistent mixed kernel.
+struct HopPlan {
+  bool ordered = false;
+  int single_film = 0;
+  int grid_blocks = 0;
+};
+
+static int prepare_hops(kmc_ctx* c, double v, int32_t precision, int variant, int64_t steps_per_launch, HopPlan* p) {
+  if (precision == KMC_PREC_MIXED && c->lt_v != v) {
+    CK(c, kmc::launch_link_times(c->d_pos4i.p, c->d_left_i.p, c->d_right_i.p, c->d_rec.p, c->d_lt64.p, c->n_sites, v,
+                                 c->stream));
+    c->lt_v = v;
+  }
+  p->ordered = precision == KMC_PREC_MIXED && order_in_effect(c);
+  if (p->ordered) {
+    int rc = ensure_order_buffers(c);
+    if (rc) return rc;
+  }
+  p->single_film = (c->n_films == 1 && c->msd_batches == 1) ? 1 : 0;
+  p->grid_blocks = c->n_sms * kmc::hop_mixed_blocks_per_sm(variant, steps_per_launch, p->single_film);
+  return KMC_OK;
+}
+
+// The launches of n_steps steps (step indices step0.. in a.msd), spl steps per launch, with the
+// work-order rebuild before each mixed launch; *nl += kernels launched.
+static cudaError_t enqueue_hops(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0, int32_t precision,
+                                int variant, int spl, const HopPlan& p, int* nl) {
+  cudaError_t e = cudaSuccess;
+  for (int64_t s = 0; s < n_steps && e == cudaSuccess; s += spl) {
+    int64_t k = std::min<int64_t>(spl, n_steps - s);
+    a.step0 = step0 + s;
+    a.order = nullptr;
+    if (precision == KMC_PREC_FP64) {
+      e = kmc::launch_hop_fp64(a, k, c->block, c->stream);
+    } else {
+      if (p.ordered) {
+        e = kmc::build_work_order(a, c->n_obuckets, c->d_obucket.p, c->d_ocount.p, c->d_oscan.p, (int64_t)c->d_oscan.n,
+                                  c->d_order.p, c->stream);
+        a.order = c->d_order.p;
+        *nl += 2 + kmc::scan_kernel_count(c->n_obuckets + 1);
+      }
+      if (e == cudaSuccess)
+        e = kmc::launch_hop_mixed(a, k, variant, p.grid_blocks, p.single_film, c->d_queue.p, c->stream);
+    }
+    ++*nl;
+  }
+  return e;
+}
+
+// Capture what enqueue() puts on the context's stream into *exec (updated in place when the
+// topology of the previous capture matches, else re-instantiated).
+static int capture_graph(kmc_ctx* c, cudaGraphExec_t* exec, const std::function<cudaError_t()>& enqueue) {
+  cudaGraph_t g = nullptr;
+  CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  cudaError_t e = enqueue();
+  cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    CK(c, e != cudaSuccess ? e : e2);
+  }
+  bool updated = false;
+  if (*exec) {
+    cudaGraphExecUpdateResultInfo info;
+    updated = cudaGraphExecUpdate(*exec, g, &info) == cudaSuccess;
+    if (!updated) {
+      cudaGetLastError();  // clear the update's error state
+      cudaGraphExecDestroy(*exec);
+      *exec = nullptr;
+    }
+  }
+  if (!updated) {
+    e = cudaGraphInstantiate(exec, g, 0);
+    if (e != cudaSuccess) {
+      *exec = nullptr;
+      cudaGraphDestroy(g);
+      CK(c, e);
+    }
+  }
+  cudaGraphDestroy(g);
+  return KMC_OK;
+}
+
+// Device error word after a run: the failure it records, or KMC_OK.
+static int check_device_error(kmc_ctx* c, const char* who) {
+  int32_t herr = 0;
+  CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
+  if (herr & KMC_ERR_HOP_CAP_CODE)
+    FAIL(c, KMC_ERR_HOP_CAP, "%s: an exciton exceeded %lld hops in one step", who, (long long)c->hop_cap);
+  if (herr & KMC_ERR_CAPACITY_CODE)
+    FAIL(c, KMC_ERR_CAPACITY, "%s: more excitons than the %lld slots of the contacts set-up", who, (long long)c->n_slots);
+  if (herr) FAIL(c, KMC_ERR_ARG, "%s: a free flight crossed more than 2^22 links (zero-length tube links?)", who);
+  return KMC_OK;
+}
+
 // Launch n_steps steps (step indices step0.. in a.msd) with the given shape; device time in *ms.
 // The launches (and the work-order rebuild before each mixed launch) are captured into a CUDA
 // graph; the graph of the previous run is updated in place when its topology matches.
 static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0, int32_t precision, int variant,
                      int spl, float* ms, int* launches) {
-  if (precision == KMC_PREC_MIXED && c->lt_v != a.v) {
-    CK(c, kmc::launch_link_times(c->d_pos4i.p, c->d_left_i.p, c->d_right_i.p, c->d_rec.p, c->d_lt64.p, c->n_sites,
-                                 a.v, c->stream));
-    c->lt_v = a.v;
-  }
-  const bool ordered = precision == KMC_PREC_MIXED && order_in_effect(c);
-  if (ordered) {
-    int rc = ensure_order_buffers(c);
-    if (rc) return rc;
-  }
-  const int single_film = (c->n_films == 1 && c->msd_batches == 1) ? 1 : 0;
-  const int grid_blocks = c->n_sms * kmc::hop_mixed_blocks_per_sm(variant, std::min<int64_t>(spl, n_steps), single_film);
+  HopPlan plan;
+  int rc = prepare_hops(c, a.v, precision, variant, std::min<int64_t>(spl, n_steps), &plan);
+  if (rc) return rc;
   int nl = 0;
   auto enqueue = [&]() -> cudaError_t {
     cudaError_t e = cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream);
-    for (int64_t s = 0; s < n_steps && e == cudaSuccess; s += spl) {
-      int64_t k = std::min<int64_t>(spl, n_steps - s);
-      a.step0 = step0 + s;
-      if (precision == KMC_PREC_FP64) {
-        a.order = nullptr;
-        e = kmc::launch_hop_fp64(a, k, c->block, c->stream);
-      } else {
-        a.order = nullptr;
-        if (ordered) {
-          e = kmc::build_work_order(a, c->n_obuckets, c->d_obucket.p, c->d_ocount.p, c->d_oscan.p,
-                                    (int64_t)c->d_oscan.n, c->d_order.p, c->stream);
-          a.order = c->d_order.p;
-          nl += 2 + kmc::scan_kernel_count(c->n_obuckets + 1);
-        }
-        if (e == cudaSuccess) e = kmc::launch_hop_mixed(a, k, variant, grid_blocks, single_film, c->d_queue.p, c->stream);
-      }
-      ++nl;
-    }
+    if (e == cudaSuccess) e = enqueue_hops(c, a, n_steps, step0, precision, variant, spl, plan, &nl);
     return e;
   };
   if (c->use_graph) {
-    cudaGraph_t g = nullptr;
-    CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
-    cudaError_t e = enqueue();
-    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
-    if (e != cudaSuccess || e2 != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      CK(c, e != cudaSuccess ? e : e2);
-    }
-    bool updated = false;
-    if (c->gexec) {
-      cudaGraphExecUpdateResultInfo info;
-      updated = cudaGraphExecUpdate(c->gexec, g, &info) == cudaSuccess;
-      if (!updated) {
-        cudaGetLastError();  // clear the update's error state
-        cudaGraphExecDestroy(c->gexec);
-        c->gexec = nullptr;
-      }
-    }
-    if (!updated) {
-      e = cudaGraphInstantiate(&c->gexec, g, 0);
-      if (e != cudaSuccess) {
-        c->gexec = nullptr;
-        cudaGraphDestroy(g);
-        CK(c, e);
-      }
-    }
-    cudaGraphDestroy(g);
+    rc = capture_graph(c, &c->gexec, enqueue);
+    if (rc) return rc;
     CK(c, cudaEventRecord(c->ev0, c->stream));
     CK(c, cudaGraphLaunch(c->gexec, c->stream));
   } else {
@@ -772,16 +828,13 @@ static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0,
   CK(c, cudaStreamSynchronize(c->stream));
   CK(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
   *launches = nl;
-  int32_t herr = 0;
-  CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
-  if (herr & 1) FAIL(c, KMC_ERR_HOP_CAP, "kmc_run: an exciton exceeded %lld hops in one step", (long long)c->hop_cap);
-  if (herr) FAIL(c, KMC_ERR_ARG, "kmc_run: a free flight crossed more than 2^22 links (zero-length tube links?)");
-  return KMC_OK;
+  return check_device_error(c, "kmc_run");
 }
 
 int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision) {
   if (!c) return KMC_ERR_ARG;
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_run: create the excitons first");
+  if (c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_run: the excitons are in contacts mode (kmc_contacts_run)");
   if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_run: bad step count, time step or velocity");
   if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_run: bad precision");
   CK(c, cudaSetDevice(c->device));
@@ -803,6 +856,263 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   c->stats.last_run_ms = ms;
   c->stats.last_launches = launches;
   return rc;
+}
+
+// ---------------------------------------------------------------- contacts mode
+int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* info, double* area, int64_t* stat_pop) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_contacts_init: build the neighbour lists first");
+  if (!cfg) FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: missing configuration");
+  if (c->n_films != 1) FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: contacts mode runs one film");
+  const int32_t n_seg = cfg->n_segments;
+  if (n_seg < 2 || n_seg > 4096) FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: number of segments must be in [2, 4096]");
+  for (int k = 0; k < 2; ++k)
+    if (cfg->contact_pop[k] < 0 || cfg->contact_pop[k] > INT32_MAX)
+      FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: contact population out of range");
+  CK(c, cudaSetDevice(c->device));
+  const int64_t n = c->n_sites;
+  const auto& dom = c->domains[0];
+  const double ymin = dom[1], ymax = dom[4];
+  const double dy = (ymax - ymin) / double(n_seg);
+  std::vector<int32_t> rank(n);
+  for (int64_t k = 0; k < n; ++k) rank[c->h_perm[k]] = (int32_t)k;
+  auto y_of = [&](int64_t k) { return c->pos[3 * k + 1]; };
+  // get_area (monte_carlo.h:628-688): per slab the x and z extents, starting from the opposite
+  // domain bounds; the else-if leaves a maximum unset while the minimum moves
+  std::vector<double> xmn(n_seg, dom[3]), xmx(n_seg, dom[0]), zmn(n_seg, dom[5]), zmx(n_seg, dom[2]);
+  for (int64_t k = 0; k < n; ++k) {
+    const double* q = &c->pos[3 * k];
+    int i = (int)((q[1] - ymin) / dy);
+    i = i < 0 ? 0 : (i < n_seg ? i : n_seg - 1);
+    if (xmn[i] > q[0])
+      xmn[i] = q[0];
+    else if (xmx[i] < q[0])
+      xmx[i] = q[0];
+    if (zmn[i] > q[2])
+      zmn[i] = q[2];
+    else if (zmx[i] < q[2])
+      zmx[i] = q[2];
+  }
+  if (area)
+    for (int i = 0; i < n_seg; ++i) area[i] = (zmx[i] - zmn[i]) * (xmx[i] - xmn[i]);
+  // get_scatterer_statistics (:691-710)
+  if (stat_pop) {
+    std::fill(stat_pop, stat_pop + n_seg, 0);
+    for (int64_t k = 0; k < n; ++k) stat_pop[(int)(std::fabs(y_of(k) - ymin) / dy) % n_seg]++;
+  }
+  // contact_scats(1) and contact_scats(n_seg) (:496-517), in site order
+  std::vector<int32_t> clist;
+  int64_t cn[2];
+  for (int k = 0; k < 2; ++k) {
+    const int i = k == 0 ? 1 : n_seg;
+    const double y1 = ymin + double(i - 1) * dy, y2 = ymin + double(i) * dy;
+    const size_t before = clist.size();
+    for (int64_t q = 0; q < n; ++q)
+      if (y_of(q) >= y1 && y_of(q) <= y2) clist.push_back(rank[q]);
+    cn[k] = (int64_t)(clist.size() - before);
+    if (cfg->contact_pop[k] > 0 && cn[k] == 0)
+      FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: contact %d has no site to place excitons at", k == 0 ? 1 : n_seg);
+  }
+  // create_particles (:274-309): slab i gets round(pop1 + i dp) excitons at its sites
+  // [y1, y1 + dy), in site order
+  std::vector<int32_t> seg_sites;
+  std::vector<int64_t> seg_off(1, 0), part_first(1, 0);
+  const double dp = double(cfg->contact_pop[1] - cfg->contact_pop[0]) / (double(n_seg) - 1);
+  for (int i = 0; i < n_seg; ++i) {
+    const int n_particle = (int)std::round(double(cfg->contact_pop[0]) + double(i) * dp);
+    const double y1 = ymin + double(i) * dy;
+    const double y2 = y1 + dy;
+    for (int64_t q = 0; q < n; ++q)
+      if (y1 <= y_of(q) && y_of(q) < y2) seg_sites.push_back(rank[q]);
+    seg_off.push_back((int64_t)seg_sites.size());
+    const int64_t np = std::max(n_particle, 0);
+    if (np > 0 && seg_off[i + 1] == seg_off[i])
+      FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: segment %d has no site for its %lld excitons", i, (long long)np);
+    part_first.push_back(part_first.back() + np);
+  }
+  const int64_t n_initial = part_first.back();
+  int64_t cap = cfg->capacity > 0 ? cfg->capacity
+                                  : std::max<int64_t>(1024, 2 * (n_initial + cfg->contact_pop[0] + cfg->contact_pop[1]));
+  cap = (cap + 31) / 32 * 32;
+  if (cap < n_initial) FAIL(c, KMC_ERR_CAPACITY, "kmc_contacts_init: %lld slots for %lld initial excitons", (long long)cap,
+                            (long long)n_initial);
+  if (cap >= (1LL << 31)) FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: capacity too large");
+  // slots and film
+  FilmDev& fd = c->films[0];
+  fd.mode = 2;  // no Green-Kubo removal
+  fd.seed = cfg->seed;
+  fd.slot0 = 0;
+  fd.n_exc = cap;
+  fd.inj0 = 0;
+  fd.n_inj = 0;
+  c->n_exc.assign(1, cap);
+  c->n_slots = cap;
+  c->n_exc_total = cap;
+  std::vector<int32_t> warp_film((size_t)(cap / 32), 0);
+  CK(c, cudaMemcpyAsync(c->d_films.p, c->films.data(), sizeof(FilmDev), cudaMemcpyHostToDevice, c->stream));
+  CK(c, upload(c->d_warp_film, warp_film.data(), warp_film.size(), c->stream));
+  CK(c, c->d_e_site.alloc(cap));
+  CK(c, c->d_e_flags.alloc(cap));
+  CK(c, c->d_e_pos.alloc(3 * cap));
+  CK(c, c->d_e_delta.alloc(3 * cap));
+  CK(c, c->d_e_ff.alloc(cap));
+  CK(c, c->d_e_draws.alloc(cap));
+  CK(c, c->d_e_hops.alloc(cap));
+  CK(c, c->d_y_old.alloc(cap));
+  CK(c, upload(c->d_c_list, clist.data(), clist.size(), c->stream));
+  std::vector<double> yif(n_seg - 1);
+  for (int i = 1; i < n_seg; ++i) yif[i - 1] = ymin + dy * double(i);  // save_currents :585-589
+  CK(c, upload(c->d_c_yif, yif.data(), yif.size(), c->stream));
+  const int64_t nb = kmc::contacts_blocks(cap);
+  CK(c, c->d_c_blk_a.alloc(nb + 1));
+  CK(c, c->d_c_blk_b.alloc(nb + 1));
+  CK(c, c->d_c_scan.alloc(kmc::scan_scratch_len(nb + 1)));
+  CK(c, c->d_c_step.alloc(1));
+  if (c->n_trace > 0) {
+    CK(c, c->d_trace.alloc((size_t)(c->n_trace * c->trace_cap)));
+    CK(c, c->d_trace_cnt.alloc(c->n_trace));
+    CK(c, cudaMemsetAsync(c->d_trace_cnt.p, 0, c->n_trace * sizeof(int64_t), c->stream));
+  }
+  kmc::ContactArgs& a = c->cargs;
+  a = kmc::ContactArgs{};
+  a.e_site = c->d_e_site.p;
+  a.e_flags = c->d_e_flags.p;
+  a.e_pos = c->d_e_pos.p;
+  a.e_delta = c->d_e_delta.p;
+  a.e_ff = c->d_e_ff.p;
+  a.e_draws = c->d_e_draws.p;
+  a.e_hops = c->d_e_hops.p;
+  a.y_old = c->d_y_old.p;
+  a.n_slots = cap;
+  a.pos4 = c->d_pos4i.p;
+  a.inv_total = c->d_inv_total.p;
+  a.logtab = c->d_logtab.p;
+  a.seed = cfg->seed;
+  a.n_seg = n_seg;
+  a.ymin = ymin;
+  a.dy = dy;
+  a.y_if = c->d_c_yif.p;
+  // repopulate_contacts (:443-455): slab 1 = [ymin, ymin + dy], slab n = [ymin + (n-1) dy, ymax]
+  a.rem_y1[0] = ymin;
+  a.rem_y2[0] = ymin + dy;
+  a.rem_y1[1] = ymin + double(n_seg - 1) * dy;
+  a.rem_y2[1] = ymax;
+  a.c_list[0] = c->d_c_list.p;
+  a.c_list[1] = c->d_c_list.p + cn[0];
+  for (int k = 0; k < 2; ++k) {
+    a.c_n[k] = cn[k];
+    a.c_pop[k] = cfg->contact_pop[k];
+  }
+  a.blk_a = c->d_c_blk_a.p;
+  a.blk_b = c->d_c_blk_b.p;
+  a.step = c->d_c_step.p;
+  a.err = c->d_err.p;
+  {
+    DevBuf<int32_t> d_seg;
+    DevBuf<int64_t> d_off, d_first;
+    CK(c, upload(d_seg, seg_sites.data(), seg_sites.size(), c->stream));
+    CK(c, upload(d_off, seg_off.data(), seg_off.size(), c->stream));
+    CK(c, upload(d_first, part_first.data(), part_first.size(), c->stream));
+    CK(c, kmc::launch_contacts_init(a, d_seg.p, d_off.p, d_first.p, n_initial, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
+  c->steps_done = 0;
+  c->msd_cap = 0;
+  c->d_msd.release();
+  CK(c, cudaMemsetAsync(c->d_counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->stats = kmc_run_stats{};
+  c->c_steps = 0;
+  c->contacts = true;
+  c->inited = true;
+  if (info) {
+    info->ymin = ymin;
+    info->ymax = ymax;
+    info->dy = dy;
+    info->n_initial = n_initial;
+    info->n_contact[0] = cn[0];
+    info->n_contact[1] = cn[1];
+    info->capacity = cap;
+  }
+  return KMC_OK;
+}
+
+int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision, int64_t* population,
+                     int64_t* current, int64_t* n_live) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_contacts_run: set up contacts mode first (kmc_contacts_init)");
+  if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_contacts_run: bad step count, time step or velocity");
+  if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_contacts_run: bad precision");
+  CK(c, cudaSetDevice(c->device));
+  if (n_steps == 0) return KMC_OK;
+  dt = dt + 0.0;
+  int rc = ensure_msd(c, 1);  // the hop kernels' MSD sums land in one scratch row
+  if (rc) return rc;
+  const int32_t n_seg = c->cargs.n_seg;
+  CK(c, c->d_c_pop.alloc((size_t)n_steps * n_seg));
+  CK(c, c->d_c_diff.alloc((size_t)n_steps * n_seg));
+  CK(c, c->d_c_live.alloc((size_t)n_steps));
+  CK(c, cudaMemsetAsync(c->d_c_pop.p, 0, (size_t)n_steps * n_seg * 8, c->stream));
+  CK(c, cudaMemsetAsync(c->d_c_diff.p, 0, (size_t)n_steps * n_seg * 8, c->stream));
+  CK(c, cudaMemsetAsync(c->d_c_live.p, 0, (size_t)n_steps * 8, c->stream));
+  CK(c, cudaMemsetAsync(c->d_c_step.p, 0, sizeof(int64_t), c->stream));
+  CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
+  kmc::ContactArgs ca = c->cargs;
+  ca.pop = c->d_c_pop.p;
+  ca.diff = c->d_c_diff.p;
+  ca.n_live = c->d_c_live.p;
+  kmc::HopArgs a = hop_args(c, dt, v);
+  HopPlan plan;
+  rc = prepare_hops(c, v, precision, c->mixed_variant, 1, &plan);
+  if (rc) return rc;
+  int nl = 0;
+  auto enqueue = [&]() -> cudaError_t {
+    nl = 0;
+    cudaError_t e = enqueue_hops(c, a, 1, 0, precision, c->mixed_variant, 1, plan, &nl);
+    if (e == cudaSuccess) e = kmc::enqueue_contacts_step(ca, c->d_c_scan.p, (int64_t)c->d_c_scan.n, c->stream);
+    nl += kmc::contacts_kernel_count(c->n_slots);
+    return e;
+  };
+  if (c->use_graph) {
+    rc = capture_graph(c, &c->cgexec, enqueue);
+    if (rc) return rc;
+    CK(c, cudaEventRecord(c->ev0, c->stream));
+    for (int64_t s = 0; s < n_steps; ++s) CK(c, cudaGraphLaunch(c->cgexec, c->stream));
+  } else {
+    CK(c, cudaEventRecord(c->ev0, c->stream));
+    for (int64_t s = 0; s < n_steps; ++s) CK(c, enqueue());
+  }
+  CK(c, cudaEventRecord(c->ev1, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  rc = check_device_error(c, "kmc_contacts_run");
+  unsigned long long after[4];
+  CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
+  c->c_steps += n_steps;
+  c->stats.hops = (int64_t)after[0];
+  c->stats.crossings = (int64_t)after[1];
+  c->stats.exact_resolves = (int64_t)after[2];
+  c->stats.steps_done = c->c_steps;
+  c->stats.last_run_ms = ms;
+  c->stats.last_launches = (int32_t)(nl * n_steps);
+  if (rc) return rc;
+  std::vector<unsigned long long> hp((size_t)n_steps * n_seg), hd((size_t)n_steps * n_seg), hl((size_t)n_steps);
+  CK(c, cudaMemcpy(hp.data(), c->d_c_pop.p, hp.size() * 8, cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(hd.data(), c->d_c_diff.p, hd.size() * 8, cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(hl.data(), c->d_c_live.p, hl.size() * 8, cudaMemcpyDeviceToHost));
+  for (int64_t s = 0; s < n_steps; ++s) {
+    long long run = 0;
+    for (int32_t i = 0; i < n_seg; ++i) {
+      if (population) population[s * n_seg + i] = (int64_t)hp[s * n_seg + i];
+      if (i < n_seg - 1) {
+        run += (long long)hd[s * n_seg + i];
+        if (current) current[s * (n_seg - 1) + i] = run;
+      }
+    }
+    if (n_live) n_live[s] = (int64_t)hl[s];
+  }
+  return KMC_OK;
 }
 
 int kmc_set_work_order(kmc_ctx* c, int32_t mode) {

@@ -1,10 +1,11 @@
-// driver.cpp -- cntkmc_run: drop-in replacement for the reference's src/main.cpp Green-Kubo run.
+// driver.cpp -- cntkmc_run: drop-in replacement for the reference's src/main.cpp.
 //
 //   cntkmc_run [input.json]
 //
 // Reads the "exciton monte carlo" section of input.json (default file name as main.cpp:34-38),
 // then runs the same loop as main.cpp:64-76: kubo_init, save_json_properties,
 // kubo_create_particles, and while time < max time: kubo_step(dt), kubo_save_avg_dispalcement_squared.
+// With "mode": "contacts" it runs the reference's contacts loop instead (main.cpp:86-105).
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -27,6 +28,27 @@ int main(int argc, char** argv) {
     const jl::Value& jm = j["exciton monte carlo"];
     double time_step = jm["monte carlo time step"].as_double();
     auto t0 = std::chrono::steady_clock::now();
+    if (jm.has("mode") && jm["mode"].as_string() == "contacts") {
+      // main.cpp:86-105: init, save_json_properties, then step / save_metrics /
+      // repopulate_contacts -- until "maximum time for contacts simulation [seconds]" (the
+      // reference's loop has no end)
+      if (!jm.has("maximum time for contacts simulation [seconds]"))
+        throw std::invalid_argument("contacts mode needs \"maximum time for contacts simulation [seconds]\"");
+      cntkmc::monte_carlo sim(jm);
+      sim.init();
+      sim.save_json_properties();
+      while (sim.time() < sim.contacts_max_time()) {
+        sim.step(time_step);
+        sim.save_metrics(time_step);
+        sim.repopulate_contacts();
+      }
+      kmc_run_stats rs = sim.run_stats();
+      double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      std::printf("contacts simulation finished: %lld steps, %lld hops, %u particles, wall %.3f s\n",
+                  (long long)rs.steps_done, (long long)rs.hops, sim.number_of_particles(), wall);
+      std::printf("output: %s\n", sim.output_path().c_str());
+      return 0;
+    }
     cntkmc::monte_carlo sim(jm);
     sim.kubo_init();
     sim.save_json_properties();

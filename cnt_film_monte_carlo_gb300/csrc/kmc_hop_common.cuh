@@ -7,9 +7,6 @@
 
 namespace kmc {
 
-#define KMC_ERR_HOP_CAP_CODE 1
-#define KMC_ERR_CELL_CODE 2
-#define KMC_ERR_FLIGHT_CODE 4
 // Upper bound of link crossings in one free flight: a flight of length v*dt over links of
 // positive length ends long before; only zero-length links (coincident sites) could loop.
 constexpr int kMaxCrossings = 1 << 22;
@@ -22,6 +19,11 @@ struct Exciton {
   uint64_t hops, crossings;
   int64_t trace_i;
 };
+
+__device__ __forceinline__ double dwell(double inv_total, uint32_t r, const LogTab* tab) {
+  // ff_time: -(1/Gamma) log(r / RAND_MAX), r != 0 (scatterer.h:74-80)
+  return -inv_total * kmc_log((double)r / (double)kRandMax, tab);
+}
 
 __device__ __forceinline__ void trace_push(const HopArgs& a, const Exciton& e, int32_t v) {
   if (e.trace_i >= 0) {

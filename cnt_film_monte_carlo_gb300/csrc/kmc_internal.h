@@ -6,6 +6,12 @@
 
 #include "kmc_device.cuh"
 
+// bits of the device error word
+#define KMC_ERR_HOP_CAP_CODE 1   // an exciton exceeded the hop cap of one step
+#define KMC_ERR_CELL_CODE 2      // a site fell outside the cell grid
+#define KMC_ERR_FLIGHT_CODE 4    // a free flight crossed more than kMaxCrossings links
+#define KMC_ERR_CAPACITY_CODE 8  // contacts mode: fewer empty slots than new excitons
+
 namespace kmc {
 
 // Per-film constants (device copy).
@@ -184,6 +190,43 @@ cudaError_t launch_hop_mixed_large(const HopArgs& a, int64_t n_steps, int varian
 int hop_mixed_blocks_per_sm_small(int variant, int64_t n_steps, int single_film);
 int hop_mixed_blocks_per_sm_large(int variant, int64_t n_steps, int single_film);
 constexpr int kMixedVariants = 6;
+// Contacts (steady-state flux) mode: the exciton slots, the y slabs and the per-step outputs.
+struct ContactArgs {
+  int32_t* e_site;
+  uint32_t* e_flags;
+  double* e_pos;     // [3][n_slots]
+  double* e_delta;   // [3][n_slots]
+  double* e_ff;
+  uint64_t* e_draws;
+  uint64_t* e_hops;
+  double* y_old;     // y at the start of the step (particle::step's _old_pos(1))
+  int64_t n_slots;
+  const double4_32a* pos4;  // sites (storage order)
+  const double* inv_total;
+  const LogTab* logtab;
+  uint64_t seed;            // Philox key; slot k draws from stream k
+  int32_t n_seg;
+  double ymin, dy;
+  const double* y_if;       // [n_seg - 1] interface positions (save_currents)
+  double rem_y1[2], rem_y2[2];  // repopulation slabs of contact 1 and contact n_seg
+  const int32_t* c_list[2];     // contact sites (storage slots), in site order
+  int64_t c_n[2], c_pop[2];
+  int64_t* blk_a;           // [blocks + 1] empty slots per block, then their exclusive scan
+  int64_t* blk_b;
+  int64_t* step;            // index of the step being run (device counter)
+  unsigned long long* pop;  // [steps][n_seg] excitons per segment
+  unsigned long long* diff; // [steps][n_seg] interface crossings as a difference array
+  unsigned long long* n_live;  // [steps] excitons after repopulation
+  int32_t* err;
+};
+int64_t contacts_blocks(int64_t n_slots);
+// slots [0, n_initial) get create_particles' excitons (part_first[n_seg + 1]: first exciton of
+// each segment; seg_off[n_seg + 1] into seg_sites), the rest are emptied
+cudaError_t launch_contacts_init(const ContactArgs& a, const int32_t* seg_sites, const int64_t* seg_off,
+                                 const int64_t* part_first, int64_t n_initial, cudaStream_t s);
+// after a hop launch of one step: the metrics, both repopulations, the step counter
+cudaError_t enqueue_contacts_step(const ContactArgs& a, int64_t* scan_scratch, int64_t scratch_len, cudaStream_t s);
+int contacts_kernel_count(int64_t n_slots);
 cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, const LogTab* tab,
                            cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,

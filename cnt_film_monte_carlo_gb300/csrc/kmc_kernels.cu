@@ -431,10 +431,6 @@ cudaError_t exclusive_scan_i64(int64_t* data, int64_t n, int64_t* scratch, int64
 }
 
 // ============================================================================ excitons
-__device__ __forceinline__ double dwell(double inv_total, uint32_t r, const LogTab* tab) {
-  // ff_time: -(1/Gamma) log(r / RAND_MAX), r != 0 (scatterer.h:74-80)
-  return -inv_total * kmc_log((double)r / (double)kRandMax, tab);
-}
 
 __global__ void k_init_excitons(HopArgs a) {
   int64_t slot = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;

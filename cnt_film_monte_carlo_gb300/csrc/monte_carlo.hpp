@@ -1,8 +1,11 @@
-// monte_carlo.hpp -- C++ mirror of the reference's mc::monte_carlo Green-Kubo interface
-// (src/monte_carlo/monte_carlo.h:35-844, monte_carlo.cpp:254-409) on top of the C ABI.
+// monte_carlo.hpp -- C++ mirror of the reference's mc::monte_carlo interface
+// (src/monte_carlo/monte_carlo.h:35-844, monte_carlo.cpp:254-409) on top of the C ABI: the
+// Green-Kubo driver (kubo_*) and the contacts / steady-state flux driver (init, step,
+// save_metrics, repopulate_contacts).
 //
-// Same method names, JSON keys ("exciton monte carlo" section of input.json) and output file
-// (particle_dispalcement.avg.squared.dat).  Every step runs on the GPU engine.  Errors are
+// Same method names, JSON keys ("exciton monte carlo" section of input.json) and output files
+// (particle_dispalcement.avg.squared.dat; scatterer_statistics.dat, population_profile.dat,
+// region_current.dat).  Every step runs on the GPU engine.  Errors are
 // thrown as std::runtime_error / std::invalid_argument, as the reference throws.
 // Extensions: "philox seed" (default 100), "injection": "region" | "uniform",
 // "precision": "mixed" | "fp64", "rate type": "forster2d" with "distance [m]" and
@@ -75,6 +78,8 @@ class monte_carlo {
   }
   ~monte_carlo() {
     if (msd_) std::fclose(msd_);
+    if (pop_f_) std::fclose(pop_f_);
+    if (cur_f_) std::fclose(cur_f_);
     kmc_destroy(ctx_);
   }
   monte_carlo(const monte_carlo&) = delete;
@@ -87,6 +92,158 @@ class monte_carlo {
 
   // monte_carlo.cpp:254-305
   void kubo_init() {
+    setup_film();
+    n_sections_ = (int)j_["number of sections for injection region"].as_int();
+    max_time_ = j_["maximum time for kubo simulation [seconds]"].as_double();
+  }
+
+  // Contacts (steady-state flux) mode, monte_carlo.h:157-195: the film as kubo_init builds it, the
+  // y slabs ("number of segments"), scatterer_statistics.dat, the contact sites and the initial
+  // linear profile of excitons.  Extensions: "contact populations" (default [1100, 0], the
+  // reference's hard-coded _c1_pop/_c2_pop), "contacts capacity" (exciton slots),
+  // "maximum time for contacts simulation [seconds]" (the reference's loop never ends).
+  void init() {
+    setup_film();
+    n_seg_ = (int32_t)j_["number of segments"].as_int();
+    int64_t pops[2] = {1100, 0};
+    if (j_.has("contact populations"))
+      for (int k = 0; k < 2; ++k) pops[k] = j_["contact populations"][k].as_int();
+    kmc_contacts cfg{};
+    cfg.n_segments = n_seg_;
+    cfg.contact_pop[0] = pops[0];
+    cfg.contact_pop[1] = pops[1];
+    cfg.seed = seed();
+    cfg.capacity = j_.has("contacts capacity") ? j_["contacts capacity"].as_int() : 0;
+    area_.assign((size_t)std::max(n_seg_, 0), 0.0);
+    std::vector<int64_t> stat(area_.size(), 0);
+    check(kmc_contacts_init(ctx_, &cfg, &cinfo_, area_.data(), stat.data()), "kmc_contacts_init");
+    pop_.assign((size_t)n_seg_, 0);
+    cur_.assign((size_t)n_seg_ - 1, 0);
+    n_particles_ = cinfo_.n_initial;
+    max_time_ = j_.has("maximum time for contacts simulation [seconds]")
+                    ? j_["maximum time for contacts simulation [seconds]"].as_double()
+                    : 0.0;
+    // get_scatterer_statistics, monte_carlo.h:691-710
+    std::FILE* f = std::fopen((fs::path(out_dir_) / "scatterer_statistics.dat").c_str(), "w");
+    if (!f) throw std::runtime_error("cannot open scatterer_statistics.dat");
+    std::fprintf(f, "position,distribution,population,density\n");
+    const double n_sites = double(nbr_.n_sites);
+    for (int32_t i = 0; i < n_seg_; ++i)
+      std::fprintf(f, "%e,%e,%lld,%e\n", cinfo_.ymin + (double(i) + 0.5) * cinfo_.dy, double(stat[i]) / n_sites,
+                   (long long)stat[i], double(stat[i]) / (area_[i] * cinfo_.dy));
+    std::fclose(f);
+  }
+
+  // step (monte_carlo.h:343-354).  The engine runs the step, the counts behind save_metrics and
+  // repopulate_contacts as one unit, in the order of src/main.cpp:98-102.
+  void step(double dt) {
+    if (!cinfo_.capacity) throw std::logic_error("step: call init() first");
+    int64_t live = 0;
+    check(kmc_contacts_run(ctx_, 1, dt, velocity_, precision(), pop_.data(), cur_.data(), &live), "kmc_contacts_run");
+    live_ = live;
+    time_ += dt;
+    ++steps_;
+  }
+
+  // save_metrics (monte_carlo.h:519-625): population_profile.dat and region_current.dat rows of
+  // the last step
+  void save_metrics(double dt) {
+    const double dy = cinfo_.dy, ymin = cinfo_.ymin;
+    const int32_t n = n_seg_;
+    if (!pop_f_) {
+      pop_f_ = std::fopen((fs::path(out_dir_) / "population_profile.dat").c_str(), "w");
+      cur_f_ = std::fopen((fs::path(out_dir_) / "region_current.dat").c_str(), "w");
+      if (!pop_f_ || !cur_f_) throw std::runtime_error("cannot open the contacts output files");
+      std::fprintf(pop_f_, "area");
+      for (int32_t i = 0; i < n; ++i) std::fprintf(pop_f_, ",%+e", area_[i]);
+      std::fprintf(pop_f_, "\n\ndy");
+      for (int32_t i = 0; i < n; ++i) std::fprintf(pop_f_, ",%+e", dy);
+      std::fprintf(pop_f_, "\n\nsection pos");
+      for (int32_t i = 0; i < n; ++i) std::fprintf(pop_f_, ",%+e", ymin + (double(i) + 0.5) * dy);
+      std::fprintf(pop_f_, "\n\ntime");
+      for (int32_t i = 0; i < n; ++i) std::fprintf(pop_f_, ",section%d", i);
+      std::fprintf(pop_f_, "\n");
+      // showpos prints the sign of the (signed) interface numbers too
+      std::fprintf(cur_f_, "interface area");
+      for (int32_t i = 1; i < n; ++i) std::fprintf(cur_f_, ",%+e", (area_[i - 1] + area_[i]) / 2);
+      std::fprintf(cur_f_, "\n\ninterface pos");
+      for (int32_t i = 1; i < n; ++i) std::fprintf(cur_f_, ",%+e", ymin + dy * double(i));
+      std::fprintf(cur_f_, "\n\ntime");
+      for (int32_t i = 1; i < n; ++i) std::fprintf(cur_f_, ",interface%+d", i - 1);
+      std::fprintf(cur_f_, "\n");
+    }
+    std::fprintf(pop_f_, "%+e", time_);
+    for (int32_t i = 0; i < n; ++i) std::fprintf(pop_f_, ",%+e", double(pop_[i]) / (area_[i] * dy));
+    std::fprintf(pop_f_, "\n");
+    std::fprintf(cur_f_, "%+e", time_);
+    for (int32_t i = 1; i < n; ++i)
+      std::fprintf(cur_f_, ",%+e", double(cur_[i - 1]) / (((area_[i - 1] + area_[i]) / 2) * dt));
+    std::fprintf(cur_f_, "\n");
+    std::fflush(pop_f_);
+    std::fflush(cur_f_);
+  }
+
+  // repopulate_contacts (monte_carlo.h:443-455): done by the engine at the end of step(); the
+  // particle count is updated here, where the reference's list changes size
+  void repopulate_contacts() { n_particles_ = live_; }
+
+  double contacts_max_time() const { return max_time_; }
+  const kmc_contacts_info& contacts_info() const { return cinfo_; }
+
+  // monte_carlo.h:319-324
+  void save_json_properties() const {
+    std::ofstream f(fs::path(out_dir_) / "input.json");
+    jl::write(f, j_);
+    f << "\n";
+  }
+
+  // monte_carlo.cpp:308-316
+  void kubo_create_particles() {
+    n_particles_ = j_["number of particles for kubo simulation"].as_int();
+    uint64_t seed = this->seed();
+    bool uniform = j_.has("injection") && j_["injection"].as_string() == "uniform";
+    int64_t ne = n_particles_;
+    kmc_inject inj{uniform ? KMC_INJECT_UNIFORM : KMC_INJECT_REGION, n_sections_, &ne, &seed};
+    check(kmc_init_excitons(ctx_, &inj), "kmc_init_excitons");
+    steps_ = 0;
+  }
+
+  // monte_carlo.cpp:319-342
+  void kubo_step(double dt) {
+    check(kmc_run(ctx_, 1, dt, velocity_, precision()), "kmc_run");
+    ++steps_;
+    time_ += dt;
+  }
+
+  // monte_carlo.cpp:382-409
+  void kubo_save_avg_dispalcement_squared() {
+    if (!msd_) {
+      msd_ = std::fopen((fs::path(out_dir_) / "particle_dispalcement.avg.squared.dat").c_str(), "w");
+      if (!msd_) throw std::runtime_error("cannot open the MSD file");
+      std::fprintf(msd_, "# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble over time\n");
+      std::fprintf(msd_, "# number of particles: %lld\n\ntime,x,y,z\n", (long long)n_particles_);
+    }
+    double s[3];
+    check(kmc_get_msd(ctx_, steps_ - 1, 1, s), "kmc_get_msd");
+    double n = double(n_particles_);
+    std::fprintf(msd_, "%+e,%+e,%+e,%+e\n", time_, s[0] / n, s[1] / n, s[2] / n);
+    std::fflush(msd_);
+  }
+
+  const kmc_nbr_stats& neighbor_stats() const { return nbr_; }
+  kmc_run_stats run_stats() const {
+    kmc_run_stats s{};
+    kmc_get_run_stats(ctx_, &s);
+    return s;
+  }
+
+ private:
+  uint64_t seed() const { return j_.has("philox seed") ? (uint64_t)j_["philox seed"].as_int() : 100u; }
+  int precision() const {
+    return (j_.has("precision") && j_["precision"].as_string() == "fp64") ? KMC_PREC_FP64 : KMC_PREC_MIXED;
+  }
+  // the film part of kubo_init / init: table, mesh, trim_scats, buckets and neighbour lists
+  void setup_film() {
     r_max_ = j_["max hopping radius [m]"].as_double();
     velocity_ = j_["exciton velocity [m/s]"].as_double();
     create_scattering_table();
@@ -117,59 +274,7 @@ class monte_carlo {
     t.rate = rates_.data();
     check(kmc_set_rate_table(ctx_, &t), "kmc_set_rate_table");
     check(kmc_build_neighbors(ctx_, r_max_, &nbr_), "kmc_build_neighbors");
-    n_sections_ = (int)j_["number of sections for injection region"].as_int();
-    max_time_ = j_["maximum time for kubo simulation [seconds]"].as_double();
   }
-
-  // monte_carlo.h:319-324
-  void save_json_properties() const {
-    std::ofstream f(fs::path(out_dir_) / "input.json");
-    jl::write(f, j_);
-    f << "\n";
-  }
-
-  // monte_carlo.cpp:308-316
-  void kubo_create_particles() {
-    n_particles_ = j_["number of particles for kubo simulation"].as_int();
-    uint64_t seed = j_.has("philox seed") ? (uint64_t)j_["philox seed"].as_int() : 100u;
-    bool uniform = j_.has("injection") && j_["injection"].as_string() == "uniform";
-    int64_t ne = n_particles_;
-    kmc_inject inj{uniform ? KMC_INJECT_UNIFORM : KMC_INJECT_REGION, n_sections_, &ne, &seed};
-    check(kmc_init_excitons(ctx_, &inj), "kmc_init_excitons");
-    steps_ = 0;
-  }
-
-  // monte_carlo.cpp:319-342
-  void kubo_step(double dt) {
-    int prec = (j_.has("precision") && j_["precision"].as_string() == "fp64") ? KMC_PREC_FP64 : KMC_PREC_MIXED;
-    check(kmc_run(ctx_, 1, dt, velocity_, prec), "kmc_run");
-    ++steps_;
-    time_ += dt;
-  }
-
-  // monte_carlo.cpp:382-409
-  void kubo_save_avg_dispalcement_squared() {
-    if (!msd_) {
-      msd_ = std::fopen((fs::path(out_dir_) / "particle_dispalcement.avg.squared.dat").c_str(), "w");
-      if (!msd_) throw std::runtime_error("cannot open the MSD file");
-      std::fprintf(msd_, "# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble over time\n");
-      std::fprintf(msd_, "# number of particles: %lld\n\ntime,x,y,z\n", (long long)n_particles_);
-    }
-    double s[3];
-    check(kmc_get_msd(ctx_, steps_ - 1, 1, s), "kmc_get_msd");
-    double n = double(n_particles_);
-    std::fprintf(msd_, "%+e,%+e,%+e,%+e\n", time_, s[0] / n, s[1] / n, s[2] / n);
-    std::fflush(msd_);
-  }
-
-  const kmc_nbr_stats& neighbor_stats() const { return nbr_; }
-  kmc_run_stats run_stats() const {
-    kmc_run_stats s{};
-    kmc_get_run_stats(ctx_, &s);
-    return s;
-  }
-
- private:
   void check(int rc, const char* what) const {
     if (rc != KMC_OK) throw std::runtime_error(std::string(what) + ": " + kmc_last_error(ctx_));
   }
@@ -264,6 +369,13 @@ class monte_carlo {
   std::vector<int32_t> left_, right_;
   kmc_nbr_stats nbr_{};
   std::FILE* msd_ = nullptr;
+  // contacts mode
+  int32_t n_seg_ = 0;
+  kmc_contacts_info cinfo_{};
+  std::vector<double> area_;
+  std::vector<int64_t> pop_, cur_;
+  int64_t live_ = 0;
+  std::FILE *pop_f_ = nullptr, *cur_f_ = nullptr;
 };
 
 }  // namespace cntkmc

@@ -132,6 +132,34 @@ class Engine:
         self.n_exc = ne
         return self
 
+    def contacts_init(self, n_segments: int, contact_pop=(1100, 0), seed: int = 100, capacity: int = 0) -> dict:
+        """Contacts (steady-state flux) mode set-up (replaces init_excitons).  Returns the slab
+        geometry: ymin, ymax, dy, n_initial, n_contact, capacity, area[n_segments] and the sites
+        per slab stat_pop[n_segments]."""
+        cfg = L.kmc_contacts(int(n_segments), (C.c_int64 * 2)(*[int(p) for p in contact_pop]), int(seed), int(capacity))
+        info = L.kmc_contacts_info()
+        area = np.zeros(int(n_segments))
+        stat = np.zeros(int(n_segments), np.int64)
+        self._check(self.lib.kmc_contacts_init(self.h, C.byref(cfg), C.byref(info), L.ptr(area, C.c_double),
+                                               L.ptr(stat, C.c_int64)))
+        self.n_segments = int(n_segments)
+        out = {k: getattr(info, k) for k, _ in L.kmc_contacts_info._fields_}
+        out["n_contact"] = tuple(info.n_contact)
+        out.update(area=area, stat_pop=stat)
+        self.n_exc = np.array([info.capacity], np.int64)
+        return out
+
+    def contacts_run(self, n_steps: int, dt: float, velocity: float, precision=L.KMC_PREC_MIXED):
+        """n_steps of step + save_metrics + repopulate_contacts.  Returns (population
+        [n_steps][n_segments], current [n_steps][n_segments - 1], n_live [n_steps]) as counts."""
+        n = self.n_segments
+        pop = np.zeros((max(n_steps, 1), n), np.int64)
+        cur = np.zeros((max(n_steps, 1), n - 1), np.int64)
+        live = np.zeros(max(n_steps, 1), np.int64)
+        self._check(self.lib.kmc_contacts_run(self.h, int(n_steps), float(dt), float(velocity), int(precision),
+                                              L.ptr(pop, C.c_int64), L.ptr(cur, C.c_int64), L.ptr(live, C.c_int64)))
+        return pop[:n_steps], cur[:n_steps], live[:n_steps]
+
     # ------------------------------------------------------------------ run and read
     def run(self, n_steps: int, dt: float, velocity: float, precision=L.KMC_PREC_MIXED):
         self._check(self.lib.kmc_run(self.h, int(n_steps), float(dt), float(velocity), int(precision)))

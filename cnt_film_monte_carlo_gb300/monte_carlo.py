@@ -1,7 +1,9 @@
-"""Host-side mirror of the reference's ``mc::monte_carlo`` Green-Kubo interface.
+"""Host-side mirror of the reference's ``mc::monte_carlo`` interface: the Green-Kubo driver
+(kubo_*) and the contacts / steady-state flux driver (init, step, save_metrics,
+repopulate_contacts).
 
-Same method names, argument meaning, JSON keys and output file as
-src/monte_carlo/monte_carlo.{h,cpp} and the driver loop of src/main.cpp:62-76, so a caller of
+Same method names, argument meaning, JSON keys and output files as
+src/monte_carlo/monte_carlo.{h,cpp} and the driver loops of src/main.cpp:62-105, so a caller of
 the reference switches by changing the import.  Every step runs on the GPU engine through the
 C ABI (include/cntkmc.h).
 
@@ -25,7 +27,7 @@ import shutil
 import numpy as np
 
 from . import _lib as L
-from . import tables
+from . import contacts, tables
 from .engine import Engine, read_mesh, trim_sites
 
 
@@ -110,6 +112,13 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
 
     def kubo_init(self):
         """monte_carlo.cpp:254-305."""
+        self._setup_film()
+        j = self._json_prop
+        self._n_sections = int(j["number of sections for injection region"])
+        self._max_time = float(j["maximum time for kubo simulation [seconds]"])
+
+    def _setup_film(self):
+        """The film part of kubo_init / init: table, mesh, trim_scats, buckets, neighbour lists."""
         j = self._json_prop
         self._max_hopping_radius = float(j["max hopping radius [m]"])
         self._particle_velocity = float(j["exciton velocity [m/s]"])
@@ -123,8 +132,59 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         e.load_arrays(np.array([0, len(lk)], np.int64), pos, ori, lk, rk)
         e.set_table(self._scat_table)
         self._nbr_stats = e.build(self._max_hopping_radius)
-        self._n_sections = int(j["number of sections for injection region"])
-        self._max_time = float(j["maximum time for kubo simulation [seconds]"])
+
+    # ------------------------------------------------------------------ contacts mode
+    def init(self):
+        """Contacts (steady-state flux) set-up, monte_carlo.h:157-195: the film, the y slabs
+        ("number of segments"), scatterer_statistics.dat, the contact sites and the initial
+        linear profile (create_particles :274-309).  Extensions: "contact populations" (default
+        [1100, 0], the reference's hard-coded values), "contacts capacity" (exciton slots),
+        "maximum time for contacts simulation [seconds]"."""
+        self._setup_film()
+        j = self._json_prop
+        self._n_seg = int(j["number of segments"])
+        pops = tuple(int(p) for p in j.get("contact populations", (1100, 0)))
+        g = self._engine.contacts_init(self._n_seg, pops, int(j.get("philox seed", 100)),
+                                       int(j.get("contacts capacity", 0)))
+        self._contacts = g
+        self._n_particles = int(g["n_initial"])
+        self._max_time = float(j.get("maximum time for contacts simulation [seconds]", 0.0))
+        with open(os.path.join(self._output_directory, "scatterer_statistics.dat"), "w") as f:
+            f.write(contacts.scatterer_statistics_text(g["ymin"], g["dy"], g["stat_pop"],
+                                                       int(self._nbr_stats["n_sites"]), g["area"]))
+        self._pop_file = self._cur_file = None
+        self._last = None
+
+    def contacts_max_time(self) -> float:
+        return self._max_time
+
+    def step(self, dt: float):
+        """step (monte_carlo.h:343-354).  The engine runs the step, the counts behind
+        save_metrics and repopulate_contacts as one unit, in the order of src/main.cpp:98-102."""
+        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
+        pop, cur, live = self._engine.contacts_run(1, dt, self._particle_velocity, prec)
+        self._last = (pop[0], cur[0], int(live[0]))
+        self._time += dt
+
+    def save_metrics(self, dt: float):
+        """save_metrics (monte_carlo.h:519-625): one row of population_profile.dat and of
+        region_current.dat for the last step."""
+        g = self._contacts
+        if self._pop_file is None:
+            self._pop_file = open(os.path.join(self._output_directory, "population_profile.dat"), "w")
+            self._cur_file = open(os.path.join(self._output_directory, "region_current.dat"), "w")
+            self._pop_file.write(contacts.population_header(g["area"], g["ymin"], g["dy"]))
+            self._cur_file.write(contacts.current_header(g["area"], g["ymin"], g["dy"]))
+        pop, cur, _ = self._last
+        self._pop_file.write(contacts.population_row(self._time, pop, g["area"], g["dy"]))
+        self._cur_file.write(contacts.current_row(self._time, cur, g["area"], dt))
+        self._pop_file.flush()
+        self._cur_file.flush()
+
+    def repopulate_contacts(self):
+        """repopulate_contacts (monte_carlo.h:443-455): done by the engine at the end of step();
+        the particle count changes here, as the reference's list does."""
+        self._n_particles = self._last[2]
 
     def save_json_properties(self):
         """monte_carlo.h:319-324."""
@@ -160,9 +220,11 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         self._msd_file.flush()
 
     def close(self):
-        if self._msd_file is not None:
-            self._msd_file.close()
-            self._msd_file = None
+        for name in ("_msd_file", "_pop_file", "_cur_file"):
+            f = getattr(self, name, None)
+            if f is not None:
+                f.close()
+                setattr(self, name, None)
         self._engine.close()
 
 
@@ -174,6 +236,19 @@ def run(input_json: str, device: int = 0) -> str:
         raise ValueError('json input file does not contain "exciton monte carlo"')
     jm = dict(j["exciton monte carlo"])
     dt = float(jm["monte carlo time step"])
+    if jm.get("mode") == "contacts":  # main.cpp:86-105, until the contacts time limit
+        if "maximum time for contacts simulation [seconds]" not in jm:
+            raise ValueError('contacts mode needs "maximum time for contacts simulation [seconds]"')
+        sim = monte_carlo(jm, device)
+        sim.init()
+        sim.save_json_properties()
+        while sim.time() < sim.contacts_max_time():
+            sim.step(dt)
+            sim.save_metrics(dt)
+            sim.repopulate_contacts()
+        out = sim.output_path()
+        sim.close()
+        return out
     sim = monte_carlo(jm, device)
     sim.kubo_init()
     sim.save_json_properties()

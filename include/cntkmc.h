@@ -27,6 +27,7 @@ extern "C" {
 #define KMC_ERR_HOP_CAP (-5)   /* an exciton exceeded the per-step hop cap (device error word) */
 #define KMC_ERR_NOMEM (-6)     /* device or host allocation failed */
 #define KMC_ERR_NO_DEVICE (-7) /* no CUDA device / wrong architecture */
+#define KMC_ERR_CAPACITY (-8)  /* contacts mode: more excitons than slots */
 
 #define KMC_TABLE_4D 4 /* rate(theta)(z_shift, axis_shift_1, axis_shift_2), nearest grid point */
 #define KMC_TABLE_2D 2 /* rate(centre distance, folded angle in [0, pi/2]), nearest grid point */
@@ -136,6 +137,46 @@ int kmc_get_msd_batches(kmc_ctx* ctx, int64_t first, int64_t count, double* out)
  * end times.  Host-only. */
 int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* times, int64_t n_steps,
                       int32_t batches, double fit_fraction, double D[3], double ci95[3]);
+
+/* ---- contacts (steady-state flux) mode: the reference's second driver, src/main.cpp:94-105 ----
+ * init (monte_carlo.h:157-195) up to the particles: y split into n_segments slabs; get_area
+ * (:628-688); get_scatterer_statistics (:691-710); contact_scats of slab 1 and slab n (:496-517);
+ * create_particles (:274-309), a linear profile from contact_pop[0] to contact_pop[1] excitons
+ * per slab at random sites of the slab.  Then each step is step (:343-354: particle::step of
+ * every exciton, nothing removed), save_metrics (:519-625: excitons per slab, net crossings of
+ * every slab interface) and repopulate_contacts (:443-493: the excitons inside slab 1 are removed
+ * and contact_pop[0] new ones placed at random contact-1 sites; then the same for slab n).
+ * Excitons live in slots: slot k draws from Philox stream k (key `seed`) and keeps its draw
+ * counter when its exciton is removed; the initial excitons take slots 0.. in create_particles
+ * order and the new excitons of a contact the lowest empty slots, in order.  One film only;
+ * kmc_get_excitons then reads every slot (site -1: empty). */
+typedef struct {
+  int32_t n_segments;     /* "number of segments" (2..4096) */
+  int64_t contact_pop[2]; /* excitons kept in contact 1 / contact n (the reference: 1100, 0) */
+  uint64_t seed;          /* Philox key */
+  int64_t capacity;       /* exciton slots (0: 2 (initial + contact_pop[0] + contact_pop[1]), >= 1024) */
+} kmc_contacts;
+
+typedef struct {
+  double ymin, ymax, dy;  /* domain in y and the slab width */
+  int64_t n_initial;      /* excitons placed by create_particles */
+  int64_t n_contact[2];   /* sites of contact 1 / contact n */
+  int64_t capacity;       /* slots (a multiple of 32) */
+} kmc_contacts_info;
+
+/* Set up contacts mode after kmc_build_neighbors (replaces kmc_init_excitons).  info, area
+ * [n_segments] (get_area) and stat_pop [n_segments] (sites per slab, get_scatterer_statistics)
+ * may be NULL.  KMC_ERR_ARG when a slab or contact that must receive excitons has no site (the
+ * reference divides by zero there). */
+int kmc_contacts_init(kmc_ctx* ctx, const kmc_contacts* cfg, kmc_contacts_info* info, double* area, int64_t* stat_pop);
+
+/* n_steps of step(dt) + save_metrics + repopulate_contacts, velocity in m/s.  population
+ * [n_steps][n_segments]: excitons per slab after the step (the population file holds
+ * count / (area dy)); current [n_steps][n_segments - 1]: net crossings of interface k
+ * (y = ymin + dy (k + 1)) in +y during the step (the current file holds count / (interface area
+ * dt)); n_live [n_steps]: excitons after repopulation.  Any output may be NULL. */
+int kmc_contacts_run(kmc_ctx* ctx, int64_t n_steps, double dt, double velocity, int32_t precision,
+                     int64_t* population, int64_t* current, int64_t* n_live);
 
 /* Exciton state (film-major, exciton order).  Any pointer may be NULL.  pos/delta are [n][3]. */
 int kmc_get_excitons(kmc_ctx* ctx, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,

@@ -276,6 +276,12 @@ struct orc_sim {
   int64_t n_exc;
   int64_t n_trace, trace_cap;
   int max_list; /* longest neighbour list (scratch size for per-hop recompute) */
+  /* contacts mode */
+  int n_seg;
+  int64_t c_pop[2];
+  int32_t* c_list[2];
+  int64_t c_n[2];
+  uint8_t* live; /* [n_exc] */
 };
 
 static void domain_of(const orc_sim* s, double mn[3], double mx[3]) {
@@ -772,11 +778,204 @@ void orc_sim_destroy(orc_sim* s) {
   free(s->col);
   free(s->cum);
   free(s->inject);
+  free(s->c_list[0]);
+  free(s->c_list[1]);
+  free(s->live);
   if (s->exc) {
     for (int64_t e = 0; e < s->n_exc; ++e) free(s->exc[e].trace);
     free(s->exc);
   }
   free(s);
+}
+
+/* ---------------------------------------------------------------- contacts mode
+ * The second driver of mc::monte_carlo: init (monte_carlo.h:157-195), step (:343-354),
+ * save_metrics (:519-625) and repopulate_contacts (:443-481), run as src/main.cpp:94-105 does.
+ * Exciton slots replace the reference's particle vector: slot k draws from Philox stream k, and
+ * its draw counter carries on when its exciton is removed and a new one takes the slot.  The
+ * initial excitons take slots 0.. in create_particles order; the n new excitons of a contact take
+ * the n lowest empty slots, in creation order. */
+
+static void contact_bounds(const orc_sim* s, double* ymin, double* ymax, double* dy) {
+  *ymin = s->mn[1];
+  *ymax = s->mx[1];
+  *dy = (*ymax - *ymin) / (double)s->n_seg;
+}
+
+/* particle(pos, s, v) at a drawn site of `list` (repopulate :476-486, create_particles :297-302,
+ * particle.h:48-52), into an empty slot whose stream carries on. */
+static void create_at(orc_sim* s, int64_t slot, const int32_t* list, int64_t n_list) {
+  orc_exc* p = s->exc + slot;
+  int dice = (int)((uint32_t)orc_rand(&p->rng) % (uint64_t)n_list);
+  int32_t site = list[dice];
+  p->site = site;
+  for (int c = 0; c < 3; ++c) {
+    p->pos[c] = p->old[c] = s->pos[3 * (int64_t)site + c];
+    p->delta[c] = 0.0;
+  }
+  p->ff = ff_time(s, site, &p->rng);
+  p->heading = orc_rand(&p->rng) % 2;
+  s->live[slot] = 1;
+}
+
+int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_t seed, int64_t capacity,
+                      double* area, int64_t* stat_pop, int64_t* n_contact) {
+  if (n_seg < 2 || pop1 < 0 || pop2 < 0 || capacity <= 0 || pop1 > INT32_MAX || pop2 > INT32_MAX) return -1;
+  if (!s->rowptr) orc_sim_build_csr(s);
+  s->use_csr = 1;
+  s->mode = 2; /* particle::step only: no Green-Kubo removal */
+  s->n_seg = n_seg;
+  s->c_pop[0] = pop1;
+  s->c_pop[1] = pop2;
+  double ymin, ymax, dy;
+  contact_bounds(s, &ymin, &ymax, &dy);
+  /* get_area, monte_carlo.h:628-681 (the else-if leaves a maximum unset while the minimum moves) */
+  double *xmn = malloc(sizeof(double) * n_seg), *xmx = malloc(sizeof(double) * n_seg);
+  double *zmn = malloc(sizeof(double) * n_seg), *zmx = malloc(sizeof(double) * n_seg);
+  for (int i = 0; i < n_seg; ++i) {
+    xmx[i] = s->mn[0];
+    xmn[i] = s->mx[0];
+    zmx[i] = s->mn[2];
+    zmn[i] = s->mx[2];
+  }
+  for (int64_t k = 0; k < s->n; ++k) {
+    const double* q = s->pos + 3 * k;
+    int i = (int)((q[1] - ymin) / dy);
+    i = i < 0 ? 0 : (i < n_seg ? i : n_seg - 1);
+    if (xmn[i] > q[0])
+      xmn[i] = q[0];
+    else if (xmx[i] < q[0])
+      xmx[i] = q[0];
+    if (zmn[i] > q[2])
+      zmn[i] = q[2];
+    else if (zmx[i] < q[2])
+      zmx[i] = q[2];
+  }
+  for (int i = 0; i < n_seg; ++i) {
+    if (area) area[i] = (zmx[i] - zmn[i]) * (xmx[i] - xmn[i]);
+    if (stat_pop) stat_pop[i] = 0;
+  }
+  free(xmn);
+  free(xmx);
+  free(zmn);
+  free(zmx);
+  /* get_scatterer_statistics, monte_carlo.h:691-710 */
+  if (stat_pop)
+    for (int64_t k = 0; k < s->n; ++k) stat_pop[(int)(fabs(s->pos[3 * k + 1] - ymin) / dy) % n_seg]++;
+  /* contact_scats(1) and contact_scats(n_seg), monte_carlo.h:496-517 */
+  for (int c = 0; c < 2; ++c) {
+    int i = c == 0 ? 1 : n_seg;
+    double y1 = ymin + (double)(i - 1) * dy, y2 = ymin + (double)i * dy;
+    free(s->c_list[c]);
+    s->c_list[c] = malloc(sizeof(int32_t) * (s->n ? s->n : 1));
+    s->c_n[c] = 0;
+    for (int64_t k = 0; k < s->n; ++k) {
+      double y = s->pos[3 * k + 1];
+      if (y >= y1 && y <= y2) s->c_list[c][s->c_n[c]++] = (int32_t)k;
+    }
+    if (n_contact) n_contact[c] = s->c_n[c];
+  }
+  /* slots */
+  if (s->exc) {
+    for (int64_t e = 0; e < s->n_exc; ++e) free(s->exc[e].trace);
+    free(s->exc);
+  }
+  free(s->live);
+  s->n_exc = capacity;
+  s->exc = (orc_exc*)calloc(capacity, sizeof(orc_exc));
+  s->live = (uint8_t*)calloc(capacity, 1);
+  for (int64_t e = 0; e < capacity; ++e) {
+    orc_rng_init(&s->exc[e].rng, seed, (uint64_t)e, 0);
+    s->exc[e].site = -1;
+  }
+  /* create_particles(domain, n_seg, scats, c1_pop, c2_pop), monte_carlo.h:274-309 */
+  int32_t* seg = malloc(sizeof(int32_t) * (s->n ? s->n : 1));
+  double dp = (double)(pop2 - pop1) / ((double)n_seg - 1);
+  int64_t slot = 0;
+  int rc = 0;
+  for (int i = 0; i < n_seg && rc == 0; ++i) {
+    int n_particle = (int)round((double)pop1 + (double)i * dp);
+    double y1 = ymin + (double)i * dy;
+    double y2 = y1 + dy;
+    int64_t ns = 0;
+    for (int64_t k = 0; k < s->n; ++k) {
+      double y = s->pos[3 * k + 1];
+      if (y1 <= y && y < y2) seg[ns++] = (int32_t)k;
+    }
+    if (n_particle > 0 && ns == 0) rc = -3; /* the reference takes rand() % 0 */
+    for (int n = 0; n < n_particle && rc == 0; ++n) {
+      if (slot >= capacity) {
+        rc = -4;
+        break;
+      }
+      create_at(s, slot++, seg, ns);
+    }
+  }
+  free(seg);
+  return rc;
+}
+
+/* repopulate(y1, y2, n, list), monte_carlo.h:458-493, on slots */
+static int repopulate(orc_sim* s, double y1, double y2, int64_t n_new, const int32_t* list, int64_t n_list) {
+  for (int64_t e = 0; e < s->n_exc; ++e) {
+    if (!s->live[e]) continue;
+    double y = s->exc[e].pos[1];
+    if (y >= y1 && y <= y2) {
+      s->live[e] = 0;
+      s->exc[e].site = -1;
+    }
+  }
+  if (n_new > 0 && n_list == 0) return -3;
+  int64_t made = 0;
+  for (int64_t e = 0; e < s->n_exc && made < n_new; ++e)
+    if (!s->live[e]) {
+      create_at(s, e, list, n_list);
+      ++made;
+    }
+  return made < n_new ? -4 : 0;
+}
+
+int orc_contacts_step(orc_sim* s, double dt, int64_t n_steps, int64_t* pop, int64_t* curr, int64_t* n_live) {
+  if (s->mode != 2) return -1;
+  const int n_seg = s->n_seg;
+  double ymin, ymax, dy;
+  contact_bounds(s, &ymin, &ymax, &dy);
+  double* yif = malloc(sizeof(double) * n_seg);
+  for (int i = 1; i < n_seg; ++i) yif[i - 1] = ymin + dy * (double)i; /* save_currents :585-589 */
+  int rc = 0;
+  for (int64_t st = 0; st < n_steps && rc == 0; ++st) {
+    /* step(dt), monte_carlo.h:343-354 */
+#pragma omp parallel for num_threads(s->n_threads) schedule(dynamic, 16)
+    for (int64_t e = 0; e < s->n_exc; ++e)
+      if (s->live[e]) step(s, s->exc + e, dt, NULL, NULL);
+    /* save_population_profile :528-575 and save_currents :578-625 (the counts; the files hold
+     * count / (area dy) and count / (interface area dt)) */
+    int64_t* P = pop + st * n_seg;
+    int64_t* J = curr + st * (n_seg - 1);
+    for (int i = 0; i < n_seg; ++i) P[i] = 0;
+    for (int i = 0; i < n_seg - 1; ++i) J[i] = 0;
+    for (int64_t e = 0; e < s->n_exc; ++e) {
+      if (!s->live[e]) continue;
+      const orc_exc* p = s->exc + e;
+      int i = (int)((p->pos[1] - ymin) / dy);
+      i = i < 0 ? 0 : (i < n_seg ? i : n_seg - 1);
+      P[i]++;
+      for (int k = 0; k < n_seg - 1; ++k) {
+        if (p->old[1] < yif[k] && p->pos[1] >= yif[k])
+          J[k]++;
+        else if (p->old[1] >= yif[k] && p->pos[1] < yif[k])
+          J[k]--;
+      }
+    }
+    /* repopulate_contacts, monte_carlo.h:443-455 */
+    rc = repopulate(s, ymin, ymin + dy, s->c_pop[0], s->c_list[0], s->c_n[0]);
+    if (rc == 0) rc = repopulate(s, ymin + (double)(n_seg - 1) * dy, ymax, s->c_pop[1], s->c_list[1], s->c_n[1]);
+    int64_t live = 0;
+    for (int64_t e = 0; e < s->n_exc; ++e) live += s->live[e];
+    if (n_live) n_live[st] = live;
+  }
+  free(yif);
+  return rc;
 }
 
 double orc_log_export(double x) { return orc_log(x); }

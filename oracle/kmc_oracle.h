@@ -100,6 +100,21 @@ void orc_sim_get_excitons(const orc_sim* s, int32_t* site, double* pos, double* 
 int64_t orc_sim_total_hops(const orc_sim* s);
 int64_t orc_sim_total_crossings(const orc_sim* s);
 
+/* Contacts (steady-state flux) mode: the reference's second driver, init (monte_carlo.h:157-195),
+ * step (:343-354), save_metrics (:519-625), repopulate_contacts (:443-493).  Slot k of `capacity`
+ * draws from Philox stream k (key seed) and keeps its draw counter when its exciton is removed;
+ * the initial excitons take slots 0.. in create_particles order and the n new excitons of a
+ * contact the n lowest empty slots.  area[n_seg] (get_area), stat_pop[n_seg]
+ * (get_scatterer_statistics), n_contact[2] (contact site counts) may be NULL.  Returns 0, -1 (bad
+ * argument), -3 (a segment or contact with excitons to place has no site) or -4 (capacity). */
+int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_t seed, int64_t capacity,
+                      double* area, int64_t* stat_pop, int64_t* n_contact);
+/* n_steps of step(dt), the counts behind save_metrics (pop[step][n_seg]: excitons per segment;
+ * curr[step][n_seg-1]: net crossings of each interface in +y) and repopulate_contacts;
+ * n_live[step] = excitons after repopulation.  orc_sim_get_excitons reads the slots (site -1:
+ * empty). */
+int orc_contacts_step(orc_sim* s, double dt, int64_t n_steps, int64_t* pop, int64_t* curr, int64_t* n_live);
+
 /* Exposed pieces for known-answer tests. */
 double orc_log_export(double x);
 void orc_log_array(const double* x, double* out, int64_t n);

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "ref_kubo")
 REF_TIMING_BIN = os.path.join(HERE, "_ref", "ref_kubo_timing")
+REF_CONTACTS_BIN = os.path.join(HERE, "_ref", "ref_contacts")
 REF_SRC = "/root/reference"
 
 _lib = None
@@ -78,6 +79,10 @@ def lib():
         L.orc_sim_total_hops.restype = I64
         L.orc_sim_total_crossings.argtypes = [C.c_void_p]
         L.orc_sim_total_crossings.restype = I64
+        L.orc_contacts_init.argtypes = [C.c_void_p, C.c_int, I64, I64, U64, I64, PD, PI64, PI64]
+        L.orc_contacts_init.restype = C.c_int
+        L.orc_contacts_step.argtypes = [C.c_void_p, D, I64, PI64, PI64, PI64]
+        L.orc_contacts_step.restype = C.c_int
         L.orc_log_export.argtypes = [D]
         L.orc_log_export.restype = D
         L.orc_log_array.argtypes = [PD, PD, I64]
@@ -258,6 +263,31 @@ class Sim:
                                    _p(out["draws"], C.c_uint64), _p(out["hops"], C.c_int64))
         return out
 
+    def contacts_init(self, n_seg, pop1, pop2, seed, capacity):
+        """Contacts mode set-up; returns dict(area, stat_pop, n_contact)."""
+        area = np.zeros(n_seg)
+        stat = np.zeros(n_seg, dtype=np.int64)
+        nc = np.zeros(2, dtype=np.int64)
+        rc = lib().orc_contacts_init(self.h, n_seg, pop1, pop2, seed, capacity, _p(area, D), _p(stat, C.c_int64),
+                                     _p(nc, C.c_int64))
+        if rc != 0:
+            raise RuntimeError(f"orc_contacts_init failed ({rc})")
+        self.n_exc = capacity
+        self.n_seg = n_seg
+        return {"area": area, "stat_pop": stat, "n_contact": nc}
+
+    def contacts_step(self, dt, n_steps):
+        """Returns (pop[n_steps][n_seg], curr[n_steps][n_seg-1], n_live[n_steps])."""
+        n = self.n_seg
+        pop = np.zeros((max(n_steps, 1), n), dtype=np.int64)
+        curr = np.zeros((max(n_steps, 1), n - 1), dtype=np.int64)
+        live = np.zeros(max(n_steps, 1), dtype=np.int64)
+        rc = lib().orc_contacts_step(self.h, dt, n_steps, _p(pop, C.c_int64), _p(curr, C.c_int64),
+                                     _p(live, C.c_int64))
+        if rc != 0:
+            raise RuntimeError(f"orc_contacts_step failed ({rc})")
+        return pop[:n_steps], curr[:n_steps], live[:n_steps]
+
     def trace(self, e, cap=1 << 20):
         buf = np.zeros(cap, dtype=np.int32)
         n = lib().orc_sim_get_trace(self.h, e, _p(buf, C.c_int32), cap)
@@ -296,4 +326,14 @@ def run_reference(input_json, out_path, n_steps, seed, n_trace=0, trace_cap=0, d
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     r = subprocess.run([exe, input_json, out_path, str(n_steps), str(seed), str(n_trace), str(trace_cap),
                         "1" if dump_csr else "0"], capture_output=True, text=True, env=env, check=True)
+    return json.loads(r.stdout.strip().splitlines()[-1]), read_ref_dump(out_path)
+
+
+def run_reference_contacts(input_json, out_path, n_steps, seed):
+    """Run oracle/_ref/ref_contacts (the reference's contacts mode) and return (json line, dump dict)."""
+    import json
+
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([REF_CONTACTS_BIN, input_json, out_path, str(n_steps), str(seed)], capture_output=True,
+                       text=True, env=env, check=True)
     return json.loads(r.stdout.strip().splitlines()[-1]), read_ref_dump(out_path)

@@ -6,10 +6,12 @@ against the project's Armadillo shim (oracle/_ref/ref_kubo, built by ``make -C o
 from the reference sources), with the per-exciton Philox rand() and the project log/acos
 interposed.  Each case stores the generated film, the config and everything the reference
 produced (trimmed sites, rate table, neighbour lists, per-step MSD sums, exciton states, hop
-traces).
+traces).  The contacts cases come from the reference's contacts (steady-state flux) mode
+(oracle/_ref/ref_contacts): per-step segment populations and interface currents, the exciton
+slots after the run, and the reference's own three output files.
 
 Needs the reference sources (REF_SRC, default /root/reference); the fixtures themselves are
-self-contained.  Run: python tests/golden/make_golden.py
+self-contained.  Run: python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -70,12 +72,61 @@ def make_case(name, c, tmp):
     print(name, info, {k: v.shape for k, v in out.items() if hasattr(v, "shape") and v.size > 1000})
 
 
-def main():
+# contacts (steady-state flux) mode: the reference's init / step / save_metrics / repopulate,
+# with its hard-coded contact populations (1100, 0)
+CONTACT_CASES = {
+    "ref_contacts_5seg": dict(tubes=12, length=40.0, box=(60, 60, 6), film_seed=3,
+                              trim=([5e-9, 55e-9], [-1e-6, 1e-6], [-1e-6, 1e-6]), r_max=10e-9, n_seg=5, dt=1e-14,
+                              steps=20, seed=1234),
+    "ref_contacts_8seg": dict(tubes=20, length=30.0, box=(80, 80, 8), film_seed=11,
+                              trim=([-1e-6, 1e-6], [2e-9, 78e-9], [-1e-6, 1e-6]), r_max=12e-9, n_seg=8, dt=3e-14,
+                              steps=12, seed=99),
+}
+CONTACT_FILES = ("population_profile.dat", "region_current.dat", "scatterer_statistics.dat")
+
+
+def make_contacts_case(name, c, tmp):
+    f = F.straight_tubes(c["tubes"], c["length"], box_nm=c["box"], seed=c["film_seed"])
+    mesh = os.path.join(tmp, name, "mesh")
+    F.write_mesh(f, mesh)
+    out_dir = os.path.join(tmp, name, "out")
+    mc = {
+        "mesh input directory": mesh, "output directory": out_dir, "keep old results": False,
+        "rate type": "forster", "zshift [m]": [1.5e-9, 10e-9, 11], "axis shift 1 [m]": [-10e-9, 10e-9, 11],
+        "axis shift 2 [m]": [-10e-9, 10e-9, 11], "theta [degrees]": [0, 180, 21], "temperature [kelvin]": 300,
+        "max hopping radius [m]": c["r_max"],
+        "trim limits": {"xlim": c["trim"][0], "ylim": c["trim"][1], "zlim": c["trim"][2]},
+        "exciton velocity [m/s]": 2e5, "monte carlo time step": c["dt"], "number of segments": c["n_seg"],
+    }
+    cfg_path = os.path.join(tmp, name, "input.json")
+    with open(cfg_path, "w") as fh:
+        json.dump({"exciton monte carlo": mc}, fh)
+    info, R = O.run_reference_contacts(cfg_path, os.path.join(tmp, name, "ref.bin"), c["steps"], c["seed"])
+    out = {
+        "film_pos_nm": f.pos_nm, "film_orient": f.orient, "film_left": f.left, "film_right": f.right,
+        "config": np.frombuffer(json.dumps({k: v for k, v in mc.items() if "directory" not in k}).encode(), np.uint8),
+        "seed": np.uint64(c["seed"]), "steps": np.int64(c["steps"]),
+    }
+    for k, v in R.items():
+        out["ref_" + k] = v
+    for fn in CONTACT_FILES:  # the reference's own output files, verbatim
+        with open(os.path.join(out_dir, fn), "rb") as fh:
+            out["file_" + fn.split(".")[0]] = np.frombuffer(fh.read(), np.uint8)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(name, info)
+
+
+def main(names=()):
+    """Regenerate the named cases (all when none is named)."""
     O.build(ref=True)
     with tempfile.TemporaryDirectory() as tmp:
         for name, c in CASES.items():
-            make_case(name, c, tmp)
+            if not names or name in names:
+                make_case(name, c, tmp)
+        for name, c in CONTACT_CASES.items():
+            if not names or name in names:
+                make_contacts_case(name, c, tmp)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -11,6 +11,7 @@ from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ("ref_forster_region", "ref_wong_region")
+CONTACT_CASES = ("ref_contacts_5seg", "ref_contacts_8seg")
 
 
 def load_case(name):
@@ -65,3 +66,24 @@ def synthetic_film(n_tubes=40, length=60.0, box=(120.0, 120.0, 8.0), seed=5):
 
 def oracle_sim(pos_m, orient, left, right, table, r_max, v, threads=1):
     return O.Sim(pos_m, orient, left, right, table, r_max, v, n_threads=threads)
+
+
+def contacts_inputs(d):
+    """Trimmed film (pos_m, orient, left, right), 4-D Förster table and run settings of a contacts
+    golden case (the reference's own trim_scats and create_forster_scatt_table, restated)."""
+    mc = d["config"]
+    tl = mc["trim limits"]
+    lim = [*tl["xlim"], *tl["ylim"], *tl["zlim"]]
+    pos, ori, lk, rk = O.trim(d["film_pos_nm"] * 1.0e-9, d["film_orient"], d["film_left"], d["film_right"], lim)
+    tab = O.forster_table(1e15, mc["theta [degrees]"], mc["zshift [m]"], mc["axis shift 1 [m]"],
+                          mc["axis shift 2 [m]"])
+    return dict(pos=pos, orient=ori, left=lk, right=rk, table=tab, r_max=mc["max hopping radius [m]"],
+                v=mc["exciton velocity [m/s]"], dt=mc["monte carlo time step"], n_seg=mc["number of segments"],
+                steps=int(d["steps"]), seed=int(d["seed"]), pops=tuple(int(x) for x in d["ref_contact_pop"]))
+
+
+def ref_slots(d):
+    """The reference's exciton slots after the run: live mask and per-slot state."""
+    site = d["ref_site"]
+    return {"live": site >= 0, "site": site, "heading": d["ref_heading"], "ff": d["ref_ff"],
+            "pos": d["ref_xpos"].reshape(-1, 3), "draws": d["ref_draws"], "hops": d["ref_hops"]}

@@ -1,0 +1,76 @@
+"""Contacts (steady-state flux) mode on the CPU: the oracle's restatement against the reference's
+own contacts mode (golden fixtures made by oracle/_ref/ref_contacts), and the host-side writers of
+the three output files against the reference's files, character for character."""
+import numpy as np
+import pytest
+
+from cnt_film_monte_carlo_gb300 import contacts as CF
+from helpers import CONTACT_CASES, contacts_inputs, load_case, ref_slots
+from oracle import oracle as O
+
+
+def oracle_contacts(d, threads=4, capacity=None):
+    c = contacts_inputs(d)
+    sim = O.Sim(c["pos"], c["orient"], c["left"], c["right"], c["table"], c["r_max"], c["v"], n_threads=threads)
+    cap = capacity or len(d["ref_site"]) + 64
+    geo = sim.contacts_init(c["n_seg"], c["pops"][0], c["pops"][1], c["seed"], cap)
+    pop, cur, live = sim.contacts_step(c["dt"], c["steps"])
+    return sim, geo, pop, cur, live, c
+
+
+@pytest.mark.parametrize("name", CONTACT_CASES)
+def test_oracle_contacts_equals_reference(name):
+    d = load_case(name)
+    sim, geo, pop, cur, live, c = oracle_contacts(d)
+    n = c["n_seg"]
+    assert np.array_equal(geo["area"], d["ref_area"])
+    assert tuple(geo["n_contact"]) == (len(d["ref_contact1"]), len(d["ref_contact2"]))
+    assert np.array_equal(pop.ravel(), d["ref_pop"])
+    assert np.array_equal(cur.ravel(), d["ref_curr"])
+    assert np.array_equal(live, d["ref_n_live"])
+    assert pop.shape == (c["steps"], n) and pop.sum(axis=1).min() > 1000
+    assert np.abs(cur).sum() > 0
+    R = ref_slots(d)
+    o = sim.excitons()
+    ns = len(R["site"])
+    assert (o["site"][ns:] == -1).all()
+    assert np.array_equal(o["site"][:ns], R["site"])
+    m = R["live"]
+    for k in ("heading", "ff", "pos"):
+        assert np.array_equal(o[k][:ns][m], R[k][m]), k
+    assert np.array_equal(o["draws"][:ns], R["draws"])
+    assert np.array_equal(o["hops"][:ns], R["hops"])
+
+
+@pytest.mark.parametrize("name", CONTACT_CASES)
+def test_file_writers_reproduce_reference_files(name):
+    d = load_case(name)
+    c = contacts_inputs(d)
+    ymin, ymax = c["pos"][:, 1].min(), c["pos"][:, 1].max()
+    n = c["n_seg"]
+    dy = (ymax - ymin) / float(n)
+    area = d["ref_area"]
+    sim = O.Sim(c["pos"], c["orient"], c["left"], c["right"], c["table"], c["r_max"], c["v"])
+    geo = sim.contacts_init(n, c["pops"][0], c["pops"][1], c["seed"], len(d["ref_site"]) + 64)
+    stats = CF.scatterer_statistics_text(ymin, dy, geo["stat_pop"], len(c["left"]), area)
+    assert stats == bytes(d["file_scatterer_statistics"]).decode()
+    pop = d["ref_pop"].reshape(-1, n)
+    cur = d["ref_curr"].reshape(-1, n - 1)
+    t = d["ref_time"]
+    ptxt = CF.population_header(area, ymin, dy) + "".join(CF.population_row(t[s], pop[s], area, dy) for s in range(len(t)))
+    assert ptxt == bytes(d["file_population_profile"]).decode()
+    ctxt = CF.current_header(area, ymin, dy) + "".join(CF.current_row(t[s], cur[s], area, c["dt"]) for s in range(len(t)))
+    assert ctxt == bytes(d["file_region_current"]).decode()
+
+
+def test_oracle_contacts_rejects_empty_contact_and_small_capacity():
+    d = load_case(CONTACT_CASES[0])
+    c = contacts_inputs(d)
+    sim = O.Sim(c["pos"], c["orient"], c["left"], c["right"], c["table"], c["r_max"], c["v"])
+    with pytest.raises(RuntimeError, match="-4"):  # fewer slots than initial excitons
+        sim.contacts_init(c["n_seg"], 1100, 0, 1, 100)
+    with pytest.raises(RuntimeError, match="-1"):
+        sim.contacts_init(1, 1100, 0, 1, 10000)
+    sim.contacts_init(c["n_seg"], 50, 20, 1, 1000)
+    pop, cur, live = sim.contacts_step(c["dt"], 3)
+    assert live.min() > 0 and pop.sum(axis=1).min() > 0
