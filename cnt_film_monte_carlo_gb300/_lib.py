@@ -93,6 +93,8 @@ SIGNATURES = {
     "kmc_fit_diffusion": (C.c_int, [PD, PI64, PD, C.c_int64, C.c_int32, C.c_double, PD, PD]),
     "kmc_contacts_init": (C.c_int, [C.c_void_p, C.POINTER(kmc_contacts), C.POINTER(kmc_contacts_info), PD, PI64]),
     "kmc_contacts_run": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_double, C.c_int32, PI64, PI64, PI64]),
+    "kmc_contacts_track": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_int64, PD, PI64,
+                                     PI32]),
     "kmc_get_excitons": (C.c_int, [C.c_void_p, PI32, PD, PD, PD, PI32, PU64, PI64]),
     "kmc_num_excitons": (C.c_int64, [C.c_void_p]),
     "kmc_get_run_stats": (C.c_int, [C.c_void_p, C.POINTER(kmc_run_stats)]),

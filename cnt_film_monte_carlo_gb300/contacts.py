@@ -6,9 +6,11 @@
   exciton density count / (area dy) of every y slab.
 * ``region_current.dat``: save_currents (:578-625), one row per step with the current
   count / (interface area dt) through every slab interface.
+* ``particle_path.<n>.dat``: track_particle (:786-818), the position after every step of one
+  exciton walked from contact 1 to the last slab.
 
-The reference writes them with iostreams in std::scientific (precision 6), the last two also with
-std::showpos, which prints a sign on every signed value -- also on the interface numbers of the
+The reference writes them with iostreams in std::scientific (precision 6), all but the first also
+with std::showpos, which prints a sign on every signed value -- also on the interface numbers of the
 current-file header ("interface+0"), but not on the unsigned section numbers ("section0").
 Densities and currents are formed from integer counts here exactly as there (one FP64 division
 by one FP64 product), so the files agree character for character.
@@ -84,3 +86,8 @@ def current_header(area, ymin: float, dy: float) -> str:
 def current_row(time: float, counts, area, dt: float) -> str:
     aif = interface_areas(area)
     return _e(time, True) + "".join("," + _e(_div(float(c), float(a) * dt), True) for c, a in zip(counts, aif)) + "\n"
+
+
+def track_text(path) -> str:
+    """particle_path.<n>.dat: "   x y z" per step (scientific, showpos), then an empty line."""
+    return "".join(f"   {_e(float(x), True)} {_e(float(y), True)} {_e(float(z), True)}\n" for x, y, z in path) + "\n"

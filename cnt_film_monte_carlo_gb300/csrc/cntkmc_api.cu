@@ -1115,6 +1115,37 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
   return KMC_OK;
 }
 
+int kmc_contacts_track(kmc_ctx* c, int64_t first, int32_t n_tracks, double dt, double v, int64_t max_steps,
+                       double* path, int64_t* len, int32_t* arrived) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_contacts_track: set up contacts mode first (kmc_contacts_init)");
+  if (first < 0 || n_tracks < 0 || max_steps < 0 || !(dt >= 0) || !(v > 0) || (n_tracks > 0 && (!path || !len || !arrived)))
+    FAIL(c, KMC_ERR_ARG, "kmc_contacts_track: bad arguments");
+  if (c->cargs.c_n[0] == 0) FAIL(c, KMC_ERR_ARG, "kmc_contacts_track: contact 1 has no site");
+  if ((double)n_tracks * (double)max_steps * 3.0 > (double)(1LL << 31))
+    FAIL(c, KMC_ERR_ARG, "kmc_contacts_track: n_tracks x max_steps too large");
+  if (n_tracks == 0) return KMC_OK;
+  CK(c, cudaSetDevice(c->device));
+  dt = dt + 0.0;
+  const size_t np = (size_t)n_tracks * (size_t)max_steps * 3;
+  DevBuf<double> d_path;
+  DevBuf<int64_t> d_len;
+  DevBuf<int32_t> d_arr;
+  CK(c, d_path.alloc(np));
+  CK(c, d_len.alloc(n_tracks));
+  CK(c, d_arr.alloc(n_tracks));
+  CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
+  kmc::HopArgs h = hop_args(c, dt, v);
+  CK(c, kmc::launch_contacts_track(h, c->cargs, first, n_tracks, max_steps, d_path.p, d_len.p, d_arr.p, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  int rc = check_device_error(c, "kmc_contacts_track");
+  if (rc) return rc;
+  if (np) CK(c, cudaMemcpy(path, d_path.p, np * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(len, d_len.p, n_tracks * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  CK(c, cudaMemcpy(arrived, d_arr.p, n_tracks * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return KMC_OK;
+}
+
 int kmc_set_work_order(kmc_ctx* c, int32_t mode) {
   if (!c) return KMC_ERR_ARG;
   if (mode != KMC_ORDER_AUTO && mode != KMC_ORDER_SLOTS && mode != KMC_ORDER_SPATIAL)

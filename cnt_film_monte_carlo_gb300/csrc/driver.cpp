@@ -29,14 +29,17 @@ int main(int argc, char** argv) {
     double time_step = jm["monte carlo time step"].as_double();
     auto t0 = std::chrono::steady_clock::now();
     if (jm.has("mode") && jm["mode"].as_string() == "contacts") {
-      // main.cpp:86-105: init, save_json_properties, then step / save_metrics /
-      // repopulate_contacts -- until "maximum time for contacts simulation [seconds]" (the
+      // main.cpp:86-105: init, save_json_properties, the tracked particles, then step /
+      // save_metrics / repopulate_contacts -- until "maximum time for contacts simulation [seconds]" (the
       // reference's loop has no end)
       if (!jm.has("maximum time for contacts simulation [seconds]"))
         throw std::invalid_argument("contacts mode needs \"maximum time for contacts simulation [seconds]\"");
       cntkmc::monte_carlo sim(jm);
       sim.init();
       sim.save_json_properties();
+      // main.cpp:88-90: 100 tracked particles ("number of tracked particles"), in one launch
+      sim.track_particles(time_step, jm.has("number of tracked particles") ? (int)jm["number of tracked particles"].as_int()
+                                                                           : 100);
       while (sim.time() < sim.contacts_max_time()) {
         sim.step(time_step);
         sim.save_metrics(time_step);

@@ -9,6 +9,8 @@
 //   repopulate  repopulate_contacts (:443-493): excitons in the contact-1 slab are removed and
 //               contact_pop[0] new ones placed at random contact-1 sites; then the same for the
 //               last segment
+//   track       track_particle (:786-818): single excitons walked from contact 1 to the last
+//               slab, one thread each
 //
 // The reference keeps a vector of particles; here excitons live in slots.  Slot k draws from
 // Philox stream k, and its draw counter carries on when its exciton is removed and a new one is
@@ -194,6 +196,49 @@ __global__ void __launch_bounds__(kCBlock) k_contacts_place(ContactArgs a, int c
 }
 
 __global__ void k_contacts_next(int64_t* step) { *step += 1; }
+
+// track_particle (monte_carlo.h:786-818): one exciton placed at a random contact-1 site
+// (repopulate into an empty list), stepped until its y reaches the last slab, its position
+// recorded after every step.  Track k draws from Philox stream kTrackStream0 + k.
+__global__ void k_contacts_track(HopArgs h, ContactArgs a, int64_t first, int32_t n_tracks, int64_t max_steps,
+                                 double* __restrict__ path, int64_t* __restrict__ len, int32_t* __restrict__ arrived) {
+  const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_tracks) return;
+  Exciton e{};
+  e.active = true;
+  e.trace_i = -1;
+  e.g.init(a.seed, kTrackStream0 + (uint64_t)(first + k), 0);
+  const uint32_t dice = e.g.next() % (uint32_t)a.c_n[0];
+  e.site = a.c_list[0][dice];
+  uint32_t r;
+  while ((r = e.g.next()) == 0) {
+  }
+  e.ff = dwell(a.inv_total[e.site], r, a.logtab);
+  e.heading = (e.g.next() % 2) != 0;
+  const double4_32a p = a.pos4[e.site];
+  e.px = p.x;
+  e.py = p.y;
+  e.pz = p.z;
+  const double y_end = a.rem_y1[1];  // ymin + (n_seg - 1) dy
+  int64_t n = 0;
+  double* out = path + (int64_t)k * max_steps * 3;
+  while (e.py < y_end && n < max_steps) {
+    if (!step_fp64(h, e, h.dt)) break;
+    out[3 * n] = e.px;
+    out[3 * n + 1] = e.py;
+    out[3 * n + 2] = e.pz;
+    ++n;
+  }
+  len[k] = n;
+  arrived[k] = e.py < y_end ? 0 : 1;
+}
+
+cudaError_t launch_contacts_track(const HopArgs& h, const ContactArgs& a, int64_t first, int32_t n_tracks,
+                                  int64_t max_steps, double* path, int64_t* len, int32_t* arrived, cudaStream_t s) {
+  if (n_tracks > 0)
+    k_contacts_track<<<(unsigned)((n_tracks + 63) / 64), 64, 0, s>>>(h, a, first, n_tracks, max_steps, path, len, arrived);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_contacts_init(const ContactArgs& a, const int32_t* seg_sites, const int64_t* seg_off,
                                  const int64_t* part_first, int64_t n_initial, cudaStream_t s) {

@@ -68,6 +68,56 @@ __device__ __forceinline__ void fly_full(const HopArgs& a, Exciton& e, double dt
   }
 }
 
+// particle::step (particle.cpp:57-80) in FP64 over the blocked rows: while the dwell time fits in
+// the rest of dt, fly, select the next site by the bisection of update_state
+// (scatterer.cpp:14-30) over the FP64 cumulative rates, move there, draw the next dwell time;
+// then fly the rest.  False when the exciton exceeded the hop cap (the error word is set).
+__device__ __forceinline__ bool step_fp64(const HopArgs& a, Exciton& e, double dt) {
+  double rem = dt;
+  int64_t hs = 0;
+  while (e.ff <= rem) {
+    rem -= e.ff;
+    fly_full(a, e, e.ff);
+    int32_t ns = e.site;
+    int64_t n = a.rec[e.site].len_flags & kLenMask;  // row length (rows are stored per slot)
+    if (n > 0) {
+      const int64_t bo = a.blkptr[e.site];
+      const double* cum = a.cump + bo * 8;
+      uint32_t r = e.g.next();
+      double dice = a.total[e.site] * (double)r / (double)kRandMax;
+      unsigned left = (unsigned)-1, right = (unsigned)(n - 1);
+      while (left + 1 < right) {
+        unsigned mid = (left + right) / 2;
+        if (cum[mid] <= dice)
+          left = mid;
+        else
+          right = mid;
+      }
+      ns = a.blocks[bo + (right >> 3)].col[right & 7];
+    }
+    e.hops++;
+    trace_push(a, e, ns);
+    if (ns != e.site) {
+      e.site = ns;
+      double4_32a p = a.pos4[ns];
+      e.px = p.x;
+      e.py = p.y;
+      e.pz = p.z;
+    }
+    uint32_t r;
+    while ((r = e.g.next()) == 0) {
+    }
+    e.ff = dwell(a.inv_total[e.site], r, a.logtab);
+    if (++hs > a.hop_cap) {
+      atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
+      return false;
+    }
+  }
+  fly_full(a, e, rem);
+  e.ff -= rem;
+  return true;
+}
+
 __device__ __forceinline__ void load_exciton(const HopArgs& a, int64_t slot, Exciton& e) {
   const int64_t ns = a.n_slots;
   uint32_t fl = a.e_flags[slot];

@@ -227,6 +227,11 @@ cudaError_t launch_contacts_init(const ContactArgs& a, const int32_t* seg_sites,
 // after a hop launch of one step: the metrics, both repopulations, the step counter
 cudaError_t enqueue_contacts_step(const ContactArgs& a, int64_t* scan_scratch, int64_t scratch_len, cudaStream_t s);
 int contacts_kernel_count(int64_t n_slots);
+// track_particle: track k (of first..) draws from Philox stream kTrackStream0 + k, apart from the
+// exciton slots' streams (< 2^31)
+constexpr uint64_t kTrackStream0 = 1ull << 32;
+cudaError_t launch_contacts_track(const HopArgs& h, const ContactArgs& a, int64_t first, int32_t n_tracks,
+                                  int64_t max_steps, double* path, int64_t* len, int32_t* arrived, cudaStream_t s);
 cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, const LogTab* tab,
                            cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,

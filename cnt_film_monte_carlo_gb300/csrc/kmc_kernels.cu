@@ -537,53 +537,7 @@ __global__ void __launch_bounds__(256) k_hop_fp64(HopArgs a, int64_t n_steps) {
   bool dead = false;
   for (int64_t s = 0; s < n_steps; ++s) {
     double ox = e.px, oy = e.py, oz = e.pz;
-    if (e.active && !dead) {
-      double rem = a.dt;
-      int64_t hs = 0;
-      while (e.ff <= rem) {  // particle::step, particle.cpp:71-84
-        rem -= e.ff;
-        fly_full(a, e, e.ff);
-        int32_t ns = e.site;
-        int64_t n = a.rec[e.site].len_flags & kLenMask;  // row length (rows are stored per slot)
-        if (n > 0) {  // update_state, scatterer.cpp:14-30
-          const int64_t bo = a.blkptr[e.site];
-          const double* cum = a.cump + bo * 8;
-          uint32_t r = e.g.next();
-          double dice = a.total[e.site] * (double)r / (double)kRandMax;
-          unsigned left = (unsigned)-1, right = (unsigned)(n - 1);
-          while (left + 1 < right) {
-            unsigned mid = (left + right) / 2;
-            if (cum[mid] <= dice)
-              left = mid;
-            else
-              right = mid;
-          }
-          ns = a.blocks[bo + (right >> 3)].col[right & 7];
-        }
-        e.hops++;
-        trace_push(a, e, ns);
-        if (ns != e.site) {
-          e.site = ns;
-          double4_32a p = a.pos4[ns];
-          e.px = p.x;
-          e.py = p.y;
-          e.pz = p.z;
-        }
-        uint32_t r;
-        while ((r = e.g.next()) == 0) {
-        }
-        e.ff = dwell(a.inv_total[e.site], r, a.logtab);
-        if (++hs > a.hop_cap) {
-          atomicOr(a.err, KMC_ERR_HOP_CAP_CODE);
-          dead = true;
-          break;
-        }
-      }
-      if (!dead) {
-        fly_full(a, e, rem);
-        e.ff -= rem;
-      }
-    }
+    if (e.active && !dead) dead = !step_fp64(a, e, a.dt);
     step_epilogue(a, f, film, e, ox, oy, oz, s);
   }
   e.at_site = false;

@@ -187,6 +187,13 @@ class monte_carlo {
   // particle count is updated here, where the reference's list changes size
   void repopulate_contacts() { n_particles_ = live_; }
 
+  // track_particle (monte_carlo.h:786-818): particle_path.<fileNo>.dat.  Track fileNo draws from
+  // its own stream, so track_particles(dt, n) (all n in one launch) writes the same files as n
+  // calls.  The reference loops until the exciton reaches the last slab; here at most
+  // "maximum steps per tracked particle" (default 2^20) steps, with a warning when it has not.
+  void track_particle(double dt, int fileNo) { tracks(dt, fileNo, 1); }
+  void track_particles(double dt, int count) { tracks(dt, 0, count); }
+
   double contacts_max_time() const { return max_time_; }
   const kmc_contacts_info& contacts_info() const { return cinfo_; }
 
@@ -238,6 +245,27 @@ class monte_carlo {
   }
 
  private:
+  void tracks(double dt, int first, int count) {
+    if (count <= 0) return;
+    const int64_t cap = j_.has("maximum steps per tracked particle") ? j_["maximum steps per tracked particle"].as_int()
+                                                                      : (int64_t)1 << 20;
+    std::vector<double> path((size_t)count * (size_t)cap * 3);
+    std::vector<int64_t> len((size_t)count);
+    std::vector<int32_t> arrived((size_t)count);
+    check(kmc_contacts_track(ctx_, first, count, dt, velocity_, cap, path.data(), len.data(), arrived.data()),
+          "kmc_contacts_track");
+    for (int t = 0; t < count; ++t) {
+      const std::string name = "particle_path." + std::to_string(first + t) + ".dat";
+      std::FILE* f = std::fopen((fs::path(out_dir_) / name).c_str(), "w");
+      if (!f) throw std::runtime_error("cannot open " + name);
+      const double* p = &path[(size_t)t * (size_t)cap * 3];
+      for (int64_t k = 0; k < len[t]; ++k) std::fprintf(f, "   %+e %+e %+e\n", p[3 * k], p[3 * k + 1], p[3 * k + 2]);
+      std::fprintf(f, "\n");
+      std::fclose(f);
+      if (!arrived[t])
+        std::fprintf(stderr, "track_particle %d: not at the last slab after %lld steps\n", first + t, (long long)cap);
+    }
+  }
   uint64_t seed() const { return j_.has("philox seed") ? (uint64_t)j_["philox seed"].as_int() : 100u; }
   int precision() const {
     return (j_.has("precision") && j_["precision"].as_string() == "fp64") ? KMC_PREC_FP64 : KMC_PREC_MIXED;

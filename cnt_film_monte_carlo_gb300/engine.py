@@ -160,6 +160,16 @@ class Engine:
                                               L.ptr(pop, C.c_int64), L.ptr(cur, C.c_int64), L.ptr(live, C.c_int64)))
         return pop[:n_steps], cur[:n_steps], live[:n_steps]
 
+    def contacts_track(self, first: int, n_tracks: int, dt: float, velocity: float, max_steps: int):
+        """track_particle for tracks first.. (contacts mode): a list of (path [steps][3], arrived)."""
+        path = np.zeros((max(n_tracks, 1), max(max_steps, 1), 3))
+        ln = np.zeros(max(n_tracks, 1), np.int64)
+        arr = np.zeros(max(n_tracks, 1), np.int32)
+        self._check(self.lib.kmc_contacts_track(self.h, int(first), int(n_tracks), float(dt), float(velocity),
+                                                int(max_steps), L.ptr(path, C.c_double), L.ptr(ln, C.c_int64),
+                                                L.ptr(arr, C.c_int32)))
+        return [(path[t, :ln[t]].copy(), bool(arr[t])) for t in range(n_tracks)]
+
     # ------------------------------------------------------------------ run and read
     def run(self, n_steps: int, dt: float, velocity: float, precision=L.KMC_PREC_MIXED):
         self._check(self.lib.kmc_run(self.h, int(n_steps), float(dt), float(velocity), int(precision)))

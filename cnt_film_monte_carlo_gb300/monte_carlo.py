@@ -155,6 +155,25 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         self._pop_file = self._cur_file = None
         self._last = None
 
+    def track_particle(self, dt: float, file_no: int):
+        """track_particle (monte_carlo.h:786-818): particle_path.<file_no>.dat."""
+        self.track_particles(dt, 1, first=file_no)
+
+    def track_particles(self, dt: float, count: int, first: int = 0):
+        """Tracks first .. first + count - 1 in one launch (each has its own stream, so this equals
+        count track_particle calls).  At most "maximum steps per tracked particle" (default 2^20)
+        steps each; the reference loops until the exciton reaches the last slab."""
+        if count <= 0:
+            return []
+        cap = int(self._json_prop.get("maximum steps per tracked particle", 1 << 20))
+        tr = self._engine.contacts_track(first, count, dt, self._particle_velocity, cap)
+        for t, (path, arrived) in enumerate(tr):
+            with open(os.path.join(self._output_directory, f"particle_path.{first + t}.dat"), "w") as f:
+                f.write(contacts.track_text(path))
+            if not arrived:
+                print(f"track_particle {first + t}: not at the last slab after {cap} steps")
+        return tr
+
     def contacts_max_time(self) -> float:
         return self._max_time
 
@@ -242,6 +261,7 @@ def run(input_json: str, device: int = 0) -> str:
         sim = monte_carlo(jm, device)
         sim.init()
         sim.save_json_properties()
+        sim.track_particles(dt, int(jm.get("number of tracked particles", 100)))  # main.cpp:88-90
         while sim.time() < sim.contacts_max_time():
             sim.step(dt)
             sim.save_metrics(dt)

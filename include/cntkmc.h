@@ -178,6 +178,15 @@ int kmc_contacts_init(kmc_ctx* ctx, const kmc_contacts* cfg, kmc_contacts_info* 
 int kmc_contacts_run(kmc_ctx* ctx, int64_t n_steps, double dt, double velocity, int32_t precision,
                      int64_t* population, int64_t* current, int64_t* n_live);
 
+/* track_particle (monte_carlo.h:786-818) for tracks first .. first + n_tracks - 1: one exciton
+ * placed at a random contact-1 site and stepped (particle::step, plain FP64) until its y reaches
+ * the last slab (y >= ymin + (n_segments - 1) dy), its position recorded after every step.  Track
+ * k draws from Philox stream 2^32 + k (key: the contacts seed); the exciton slots are untouched.
+ * The reference loops until the exciton arrives; here at most max_steps steps: len[t] = steps
+ * recorded, arrived[t] = 1 when it reached the slab.  path [n_tracks][max_steps][3]. */
+int kmc_contacts_track(kmc_ctx* ctx, int64_t first, int32_t n_tracks, double dt, double velocity, int64_t max_steps,
+                       double* path, int64_t* len, int32_t* arrived);
+
 /* Exciton state (film-major, exciton order).  Any pointer may be NULL.  pos/delta are [n][3]. */
 int kmc_get_excitons(kmc_ctx* ctx, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,
                      uint64_t* draws, int64_t* hops);

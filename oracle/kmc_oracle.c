@@ -281,6 +281,7 @@ struct orc_sim {
   int64_t c_pop[2];
   int32_t* c_list[2];
   int64_t c_n[2];
+  uint64_t c_seed;
   uint8_t* live; /* [n_exc] */
 };
 
@@ -803,9 +804,8 @@ static void contact_bounds(const orc_sim* s, double* ymin, double* ymax, double*
 }
 
 /* particle(pos, s, v) at a drawn site of `list` (repopulate :476-486, create_particles :297-302,
- * particle.h:48-52), into an empty slot whose stream carries on. */
-static void create_at(orc_sim* s, int64_t slot, const int32_t* list, int64_t n_list) {
-  orc_exc* p = s->exc + slot;
+ * particle.h:48-52), drawing from p's stream. */
+static void place(const orc_sim* s, orc_exc* p, const int32_t* list, int64_t n_list) {
   int dice = (int)((uint32_t)orc_rand(&p->rng) % (uint64_t)n_list);
   int32_t site = list[dice];
   p->site = site;
@@ -815,6 +815,11 @@ static void create_at(orc_sim* s, int64_t slot, const int32_t* list, int64_t n_l
   }
   p->ff = ff_time(s, site, &p->rng);
   p->heading = orc_rand(&p->rng) % 2;
+}
+
+/* into an empty slot, whose stream carries on */
+static void create_at(orc_sim* s, int64_t slot, const int32_t* list, int64_t n_list) {
+  place(s, s->exc + slot, list, n_list);
   s->live[slot] = 1;
 }
 
@@ -825,6 +830,7 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
   s->use_csr = 1;
   s->mode = 2; /* particle::step only: no Green-Kubo removal */
   s->n_seg = n_seg;
+  s->c_seed = seed;
   s->c_pop[0] = pop1;
   s->c_pop[1] = pop2;
   double ymin, ymax, dy;
@@ -976,6 +982,34 @@ int orc_contacts_step(orc_sim* s, double dt, int64_t n_steps, int64_t* pop, int6
   }
   free(yif);
   return rc;
+}
+
+/* track_particle, monte_carlo.h:786-818: one exciton placed at a random contact-1 site (repopulate
+ * into an empty list) and stepped until its y reaches the last slab, at most max_steps steps.
+ * Track k draws from Philox stream 2^32 + k. */
+int orc_contacts_track(orc_sim* s, int64_t first, int n_tracks, double dt, int64_t max_steps, double* path,
+                       int64_t* len, int32_t* arrived) {
+  if (s->mode != 2 || s->c_n[0] == 0) return -1;
+  double ymin, ymax, dy;
+  contact_bounds(s, &ymin, &ymax, &dy);
+  const double y_end = ymin + (double)(s->n_seg - 1) * dy;
+#pragma omp parallel for num_threads(s->n_threads) schedule(dynamic, 1)
+  for (int t = 0; t < n_tracks; ++t) {
+    orc_exc p;
+    memset(&p, 0, sizeof p);
+    orc_rng_init(&p.rng, s->c_seed, (1ull << 32) + (uint64_t)(first + t), 0);
+    place(s, &p, s->c_list[0], s->c_n[0]);
+    int64_t n = 0;
+    double* out = path + (int64_t)t * max_steps * 3;
+    while (p.pos[1] < y_end && n < max_steps) {
+      step(s, &p, dt, NULL, NULL);
+      for (int c = 0; c < 3; ++c) out[3 * n + c] = p.pos[c];
+      ++n;
+    }
+    len[t] = n;
+    arrived[t] = p.pos[1] < y_end ? 0 : 1;
+  }
+  return 0;
 }
 
 double orc_log_export(double x) { return orc_log(x); }

@@ -114,6 +114,10 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
  * n_live[step] = excitons after repopulation.  orc_sim_get_excitons reads the slots (site -1:
  * empty). */
 int orc_contacts_step(orc_sim* s, double dt, int64_t n_steps, int64_t* pop, int64_t* curr, int64_t* n_live);
+/* track_particle (monte_carlo.h:786-818) for tracks first..: path [n_tracks][max_steps][3],
+ * len[n_tracks] steps recorded, arrived[n_tracks].  Track k draws from Philox stream 2^32 + k. */
+int orc_contacts_track(orc_sim* s, int64_t first, int n_tracks, double dt, int64_t max_steps, double* path,
+                       int64_t* len, int32_t* arrived);
 
 /* Exposed pieces for known-answer tests. */
 double orc_log_export(double x);

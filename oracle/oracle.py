@@ -83,6 +83,8 @@ def lib():
         L.orc_contacts_init.restype = C.c_int
         L.orc_contacts_step.argtypes = [C.c_void_p, D, I64, PI64, PI64, PI64]
         L.orc_contacts_step.restype = C.c_int
+        L.orc_contacts_track.argtypes = [C.c_void_p, I64, C.c_int, D, I64, PD, PI64, PI32]
+        L.orc_contacts_track.restype = C.c_int
         L.orc_log_export.argtypes = [D]
         L.orc_log_export.restype = D
         L.orc_log_array.argtypes = [PD, PD, I64]
@@ -288,6 +290,17 @@ class Sim:
             raise RuntimeError(f"orc_contacts_step failed ({rc})")
         return pop[:n_steps], curr[:n_steps], live[:n_steps]
 
+    def contacts_track(self, first, n_tracks, dt, max_steps):
+        """track_particle for tracks first..: a list of (path [steps][3], arrived)."""
+        path = np.zeros((max(n_tracks, 1), max(max_steps, 1), 3))
+        ln = np.zeros(max(n_tracks, 1), dtype=np.int64)
+        arr = np.zeros(max(n_tracks, 1), dtype=np.int32)
+        rc = lib().orc_contacts_track(self.h, first, n_tracks, dt, max_steps, _p(path, D), _p(ln, C.c_int64),
+                                      _p(arr, C.c_int32))
+        if rc != 0:
+            raise RuntimeError(f"orc_contacts_track failed ({rc})")
+        return [(path[t, :ln[t]].copy(), bool(arr[t])) for t in range(n_tracks)]
+
     def trace(self, e, cap=1 << 20):
         buf = np.zeros(cap, dtype=np.int32)
         n = lib().orc_sim_get_trace(self.h, e, _p(buf, C.c_int32), cap)
@@ -329,11 +342,12 @@ def run_reference(input_json, out_path, n_steps, seed, n_trace=0, trace_cap=0, d
     return json.loads(r.stdout.strip().splitlines()[-1]), read_ref_dump(out_path)
 
 
-def run_reference_contacts(input_json, out_path, n_steps, seed):
-    """Run oracle/_ref/ref_contacts (the reference's contacts mode) and return (json line, dump dict)."""
+def run_reference_contacts(input_json, out_path, n_steps, seed, n_tracks=0, timeout=600):
+    """Run oracle/_ref/ref_contacts (the reference's contacts mode, with n_tracks track_particle
+    calls first) and return (json line, dump dict)."""
     import json
 
     env = dict(os.environ, OMP_NUM_THREADS="1")
-    r = subprocess.run([REF_CONTACTS_BIN, input_json, out_path, str(n_steps), str(seed)], capture_output=True,
-                       text=True, env=env, check=True)
+    r = subprocess.run([REF_CONTACTS_BIN, input_json, out_path, str(n_steps), str(seed), str(n_tracks)],
+                       capture_output=True, text=True, env=env, check=True, timeout=timeout)
     return json.loads(r.stdout.strip().splitlines()[-1]), read_ref_dump(out_path)

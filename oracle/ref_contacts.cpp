@@ -18,7 +18,11 @@
 // that the new particles of contact 1 are stamped before contact 2 moves them; the slab bounds
 // are computed with the same expressions.  Run single threaded (OMP_NUM_THREADS=1).
 //
-// usage: ref_contacts input.json out.bin n_steps seed
+// track_particle (monte_carlo.h:786-818), called n_tracks times before the loop as main.cpp:88-90
+// does, draws from stream 2^32 + k for track k; its positions are taken from the wrapped
+// particle::step.
+//
+// usage: ref_contacts input.json out.bin n_steps seed [n_tracks]
 #include <algorithm>
 #include <array>
 #include <cassert>
@@ -63,7 +67,10 @@
 
 namespace {
 unsigned long long g_seed = 0;
-int g_mode = 0;  // 1: creating particles, 2: stepping
+int g_mode = 0;  // 1: creating particles, 2: stepping, 3: track_particle
+orc_rng g_track;                  // stream of the current track_particle call
+std::vector<double> g_track_path; // its positions after every step
+const long long kTrackStepCap = 5000000;
 std::vector<orc_rng> g_streams;  // one per slot
 std::vector<long long> g_hops;   // per slot
 std::set<long long> g_free;      // emptied slots below the high-water mark
@@ -96,12 +103,18 @@ long long slot_of(const mc::particle& p) {
 extern "C" {
 const mc::scatterer* CAT(__real_, UPD_SYM)(const mc::scatterer* self, const double& r);
 const mc::scatterer* CAT(__wrap_, UPD_SYM)(const mc::scatterer* self, const double& r) {
-  if (g_cur >= 0) g_hops[g_cur]++;
+  if (g_mode == 2 && g_cur >= 0) g_hops[g_cur]++;  // hops of the slots' excitons (not of tracks)
   return CAT(__real_, UPD_SYM)(self, r);
 }
 
 void CAT(__real_, STEP_SYM)(mc::particle* self, double dt, const std::vector<mc::scatterer>& l, const double& r);
 void CAT(__wrap_, STEP_SYM)(mc::particle* self, double dt, const std::vector<mc::scatterer>& l, const double& r) {
+  if (g_mode == 3) {  // the particle of track_particle (not in the list, no slot)
+    CAT(__real_, STEP_SYM)(self, dt, l, r);
+    for (int c = 0; c < 3; ++c) g_track_path.push_back(self->_pos(c));
+    if ((long long)g_track_path.size() > 3 * kTrackStepCap) die("a tracked particle did not reach the last slab");
+    return;
+  }
   g_cur = slot_of(*self);
   CAT(__real_, STEP_SYM)(self, dt, l, r);
   g_cur = -1;
@@ -128,6 +141,7 @@ int rand(void) __THROW {
     }
     return v;
   }
+  if (g_mode == 3) return orc_rand(&g_track);
   if (g_mode == 2) {
     if (g_cur < 0) die("rand() outside a particle step");
     return orc_rand(&stream_of(g_cur));
@@ -172,7 +186,7 @@ void stamp_new(std::vector<mc::particle>& list) {
 
 int main(int argc, char** argv) {
   if (argc < 5) {
-    std::fprintf(stderr, "usage: %s input.json out.bin n_steps seed\n", argv[0]);
+    std::fprintf(stderr, "usage: %s input.json out.bin n_steps seed [n_tracks]\n", argv[0]);
     return 2;
   }
   std::ifstream in(argv[1]);
@@ -214,6 +228,24 @@ int main(int argc, char** argv) {
     d.put("contact_pop", "i8", pops, 2);
     long long n0 = (long long)sim._particle_list.size();
     d.put("n_initial", "i8", &n0, 1);
+  }
+
+  // main.cpp:88-90: track_particle(time_step, n) before the loop
+  const long long n_tracks = argc > 5 ? std::atoll(argv[5]) : 0;
+  {
+    std::vector<long long> tlen;
+    std::vector<double> tpath;
+    for (long long k = 0; k < n_tracks; ++k) {
+      orc_rng_init(&g_track, g_seed, (1ull << 32) + (uint64_t)k, 0);
+      g_track_path.clear();
+      g_mode = 3;
+      sim.track_particle(time_step, (int)k);
+      g_mode = 0;
+      tlen.push_back((long long)g_track_path.size() / 3);
+      tpath.insert(tpath.end(), g_track_path.begin(), g_track_path.end());
+    }
+    d.put("track_len", "i8", tlen.data(), (long long)tlen.size());
+    d.put("track_path", "f8", tpath.data(), (long long)tpath.size());
   }
 
   std::vector<long long> pop_all, curr_all, live_all;

@@ -15,6 +15,7 @@ self-contained.  Run: python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import sys
@@ -77,10 +78,10 @@ def make_case(name, c, tmp):
 CONTACT_CASES = {
     "ref_contacts_5seg": dict(tubes=12, length=40.0, box=(60, 60, 6), film_seed=3,
                               trim=([5e-9, 55e-9], [-1e-6, 1e-6], [-1e-6, 1e-6]), r_max=10e-9, n_seg=5, dt=1e-14,
-                              steps=20, seed=1234),
+                              steps=20, seed=1234, tracks=4),
     "ref_contacts_8seg": dict(tubes=20, length=30.0, box=(80, 80, 8), film_seed=11,
                               trim=([-1e-6, 1e-6], [2e-9, 78e-9], [-1e-6, 1e-6]), r_max=12e-9, n_seg=8, dt=3e-14,
-                              steps=12, seed=99),
+                              steps=12, seed=99, tracks=0),
 }
 CONTACT_FILES = ("population_profile.dat", "region_current.dat", "scatterer_statistics.dat")
 
@@ -101,7 +102,18 @@ def make_contacts_case(name, c, tmp):
     cfg_path = os.path.join(tmp, name, "input.json")
     with open(cfg_path, "w") as fh:
         json.dump({"exciton monte carlo": mc}, fh)
-    info, R = O.run_reference_contacts(cfg_path, os.path.join(tmp, name, "ref.bin"), c["steps"], c["seed"])
+    info, R = O.run_reference_contacts(cfg_path, os.path.join(tmp, name, "ref.bin"), c["steps"], c["seed"],
+                                       n_tracks=c["tracks"])
+    # track_particle paths: per track the SHA-256 of its FP64 positions, track 0 in full, and the
+    # reference's own particle_path.0.dat
+    tl, tp = R.pop("track_len"), R.pop("track_path").reshape(-1, 3)
+    off = np.concatenate([[0], np.cumsum(tl)])
+    digests = [hashlib.sha256(np.ascontiguousarray(tp[off[k]:off[k + 1]]).tobytes()).digest() for k in range(len(tl))]
+    out_tracks = {"ref_track_len": tl, "ref_track_sha256": np.frombuffer(b"".join(digests), np.uint8).reshape(-1, 32)}
+    if len(tl):
+        out_tracks["ref_track0_path"] = tp[:tl[0]]
+        with open(os.path.join(out_dir, "particle_path.0.dat"), "rb") as fh:
+            out_tracks["file_particle_path_0"] = np.frombuffer(fh.read(), np.uint8)
     out = {
         "film_pos_nm": f.pos_nm, "film_orient": f.orient, "film_left": f.left, "film_right": f.right,
         "config": np.frombuffer(json.dumps({k: v for k, v in mc.items() if "directory" not in k}).encode(), np.uint8),
@@ -109,6 +121,7 @@ def make_contacts_case(name, c, tmp):
     }
     for k, v in R.items():
         out["ref_" + k] = v
+    out.update(out_tracks)
     for fn in CONTACT_FILES:  # the reference's own output files, verbatim
         with open(os.path.join(out_dir, fn), "rb") as fh:
             out["file_" + fn.split(".")[0]] = np.frombuffer(fh.read(), np.uint8)

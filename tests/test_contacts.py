@@ -1,6 +1,8 @@
 """Contacts (steady-state flux) mode on the CPU: the oracle's restatement against the reference's
 own contacts mode (golden fixtures made by oracle/_ref/ref_contacts), and the host-side writers of
 the three output files against the reference's files, character for character."""
+import hashlib
+
 import numpy as np
 import pytest
 
@@ -74,3 +76,28 @@ def test_oracle_contacts_rejects_empty_contact_and_small_capacity():
     sim.contacts_init(c["n_seg"], 50, 20, 1, 1000)
     pop, cur, live = sim.contacts_step(c["dt"], 3)
     assert live.min() > 0 and pop.sum(axis=1).min() > 0
+
+
+def track_digest(path):
+    return hashlib.sha256(np.ascontiguousarray(path, dtype=np.float64).tobytes()).digest()
+
+
+def test_oracle_tracks_equal_reference():
+    d = load_case(CONTACT_CASES[0])
+    c = contacts_inputs(d)
+    sim = O.Sim(c["pos"], c["orient"], c["left"], c["right"], c["table"], c["r_max"], c["v"], n_threads=4)
+    sim.contacts_init(c["n_seg"], c["pops"][0], c["pops"][1], c["seed"], 8192)
+    n = len(d["ref_track_len"])
+    assert n == 4
+    tr = sim.contacts_track(0, n, c["dt"], 1 << 16)
+    for k, (path, arrived) in enumerate(tr):
+        assert arrived and len(path) == d["ref_track_len"][k]
+        assert track_digest(path) == bytes(d["ref_track_sha256"][k])
+    assert np.array_equal(tr[0][0], d["ref_track0_path"])
+    assert CF.track_text(tr[0][0]) == bytes(d["file_particle_path_0"]).decode()
+    # a track's draws do not depend on the others
+    tail = sim.contacts_track(2, 2, c["dt"], 1 << 16)
+    assert all(np.array_equal(a[0], b[0]) for a, b in zip(tail, tr[2:]))
+    # a step cap shorter than the walk: the path stops there and the track has not arrived
+    short = sim.contacts_track(1, 1, c["dt"], 100)[0]
+    assert not short[1] and np.array_equal(short[0], tr[1][0][:100])

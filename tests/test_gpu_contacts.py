@@ -6,8 +6,10 @@
 * a second contact that keeps excitons, and a 2.4 M-slot set-up (multi-level scans of the
   empty-slot counts) against the oracle;
 * too few slots is reported as KMC_ERR_CAPACITY (no fault), as the oracle reports it;
-* the drop-in driver and the Python class write the reference's three files verbatim.
+* track_particle paths equal the reference's (SHA-256 of the FP64 positions);
+* the drop-in driver and the Python class write the reference's files verbatim.
 """
+import hashlib
 import json
 import os
 import subprocess
@@ -142,6 +144,30 @@ def test_capacity_exhaustion_is_an_error():
     assert live[0] == 1024 and pop.sum() == 1024 and pop[0, 1] > 0  # counted before repopulation
 
 
+@pytest.mark.parametrize("precision", [L.KMC_PREC_MIXED, L.KMC_PREC_FP64])
+def test_golden_tracks(precision):
+    # track_particle runs the plain FP64 step whatever the precision of the slots' run
+    d = load_case(CONTACT_CASES[0])
+    c = contacts_inputs(d)
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, len(c["left"])], np.int64), c["pos"], c["orient"], c["left"], c["right"])
+    e.set_table(c["table"])
+    e.build(c["r_max"])
+    e.contacts_init(c["n_seg"], c["pops"], c["seed"], 8192)
+    e.contacts_run(3, c["dt"], c["v"], precision)  # the slots do not touch the tracks' streams
+    n = len(d["ref_track_len"])
+    tr = e.contacts_track(0, n, c["dt"], c["v"], 1 << 16)
+    tail = e.contacts_track(2, 2, c["dt"], c["v"], 1 << 16)
+    short = e.contacts_track(1, 1, c["dt"], c["v"], 100)[0]
+    e.close()
+    for k, (path, arrived) in enumerate(tr):
+        assert arrived and len(path) == d["ref_track_len"][k]
+        assert hashlib.sha256(np.ascontiguousarray(path).tobytes()).digest() == bytes(d["ref_track_sha256"][k])
+    assert np.array_equal(tr[0][0], d["ref_track0_path"])
+    assert all(np.array_equal(a[0], b[0]) for a, b in zip(tail, tr[2:]))
+    assert not short[1] and np.array_equal(short[0], tr[1][0][:100])
+
+
 def _contacts_json(d, tmp):
     mesh = os.path.join(tmp, "mesh")
     left = d["film_left"]
@@ -152,7 +178,8 @@ def _contacts_json(d, tmp):
     mc.update({"mesh input directory": mesh, "output directory": os.path.join(tmp, "out"), "keep old results": False,
                "philox seed": int(d["seed"]), "mode": "contacts",
                "maximum time for contacts simulation [seconds]": mc["monte carlo time step"] * int(d["steps"]),
-               "contacts capacity": len(d["ref_site"]) + 64})
+               "contacts capacity": len(d["ref_site"]) + 64,
+               "number of tracked particles": len(d["ref_track_len"]), "maximum steps per tracked particle": 1 << 16})
     path = os.path.join(tmp, "input.json")
     with open(path, "w") as f:
         json.dump({"exciton monte carlo": mc}, f)
@@ -160,6 +187,12 @@ def _contacts_json(d, tmp):
 
 
 def _check_files(out_dir, d):
+    n_tracks = len(d["ref_track_len"])
+    assert sorted(f for f in os.listdir(out_dir) if f.startswith("particle_path.")) == sorted(
+        f"particle_path.{k}.dat" for k in range(n_tracks))
+    if n_tracks:
+        with open(os.path.join(out_dir, "particle_path.0.dat")) as f:
+            assert f.read() == bytes(d["file_particle_path_0"]).decode()
     for key, fn in (("file_scatterer_statistics", "scatterer_statistics.dat"),
                     ("file_population_profile", "population_profile.dat"),
                     ("file_region_current", "region_current.dat")):
