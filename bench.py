@@ -170,6 +170,23 @@ class CpuSample:
 def reference_arm(args):
     films, tab, _, desc = workload(args.workload, args.films)
     f = films[0]
+    if args.workload == "contacts":
+        vals, secs = [], []
+        for i in range(args.warmup + args.steps):
+            v, sample, dt, threads = contacts_cpu_sample(f, tab, SEED)
+            if i >= args.warmup:
+                vals.append(v)
+                secs.append(dt)
+        value = float(np.mean(vals))
+        print(json.dumps({"impl": "reference", "metric": CONTACTS_METRIC, "value": value, "unit": UNIT,
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": f"{desc}; contacts mode, {CONTACTS_SEG} y slabs", "sample": sample},
+                          "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                                           "sample": sample},
+                          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
     # whole run within a few minutes: every step gets an equal share of ~150 s
     per_step = min(args.cpu_seconds, 150.0 / max(args.steps + args.warmup, 1))
     cs = CpuSample(f, tab, seconds=per_step)
@@ -189,6 +206,118 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+CONTACTS_SEG, CONTACTS_POP = 10, (200_000, 0)
+CONTACTS_METRIC = "exciton hops/s (contacts-mode step: hops, slab metrics, contact repopulation)"
+
+
+CONTACTS_CPU_POP = (1_000, 0)
+
+
+def contacts_cpu_sample(f, tab, seed):
+    """The reference's contacts loop on the host cores: the oracle's restatement with a fresh
+    neighbour search on every hop (scatterer.cpp:9-31), OpenMP over excitons, on the same film
+    with contact populations (1000, 0) (about 5,500 excitons): one 1 ps step."""
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, R_MAX, VEL, n_threads=threads)
+    p = CONTACTS_CPU_POP
+    sim.contacts_init(CONTACTS_SEG, p[0], p[1], seed, p[0] * (CONTACTS_SEG + 2) + 1024)
+    sim.use_csr(False)
+    t0 = time.perf_counter()
+    sim.contacts_step(BIN, 1)
+    dt = time.perf_counter() - t0
+    hops = sim.total_hops()
+    return hops / dt, (f"oracle contacts loop with the per-hop neighbour search, contact populations {p}, one 1 ps "
+                       f"step ({hops} hops, {dt:.2f} s)"), dt, threads
+
+
+def contacts_arm(args, local, rank, world):
+    """--workload contacts: the contacts (steady-state flux) loop on the cfg2 film, 10 y slabs,
+    contact populations (200000, 0) (about 1.1 M live excitons), 1 ps steps; one timed step =
+    one kmc_contacts_run step (hop launch + metrics + both repopulations, one CUDA graph)."""
+    import torch
+
+    from cnt_film_monte_carlo_gb300 import _lib as L
+    from cnt_film_monte_carlo_gb300 import engine as E
+    from cnt_film_monte_carlo_gb300 import replicas as R
+
+    films, tab, _, desc = workload("cfg2")
+    f = films[0]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    seed = R.replica_seed(SEED, rank)
+
+    def engine():
+        e = E.Engine(local)
+        e.load_films([f])
+        e.set_table(tab)
+        st = e.build(R_MAX)
+        g = e.contacts_init(CONTACTS_SEG, CONTACTS_POP, seed, 0)
+        return e, st, g
+
+    e, st, g = engine()
+    tune = e.autotune(BIN, VEL, trial_steps=2) if not args.no_tune else None
+    for _ in range(args.warmup):
+        e.contacts_run(1, BIN, VEL, L.KMC_PREC_MIXED)
+    h0 = e.stats()["hops"]
+    dev_ms, launches, live = 0.0, 0, []
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            _, _, n_live = e.contacts_run(1, BIN, VEL, L.KMC_PREC_MIXED)
+            s = e.stats()
+            dev_ms += s["last_run_ms"]
+            launches += s["last_launches"]
+            live.append(int(n_live[0]))
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    hops = e.stats()["hops"] - h0
+    e.close()
+    dev_s_max, wall_max, hops_all = R.job_timing(dev_ms / 1e3, wall, hops)
+    value = hops_all / dev_s_max
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        e3, _, _ = engine()
+        if tune:
+            e3.set_mixed_variant(tune["variant"])
+        for _ in range(args.steps):  # each step: run it, read its slab and interface counts back
+            e3.contacts_run(1, BIN, VEL, L.KMC_PREC_MIXED)
+        h3 = e3.stats()["hops"]
+        e3.close()
+        w3 = time.perf_counter() - t0
+        h2d = f.n_sites * (3 * 8 * 2 + 2 * 4) + 16 + tab["rate"].nbytes + sum(x.nbytes for x in tab["grids"])
+        e2e = {"value": h3 * world / w3, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": 8 * (2 * CONTACTS_SEG - 1 + 1), "seconds": w3,
+               "includes": "film+table upload and neighbour build (amortised over K), contacts set-up, K steps each "
+                           "followed by the read-back of its counts"}
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    bph = bytes_per_hop(st["k_mean"])
+    achieved = hops / (dev_ms / 1e3) * bph / 1e9
+    line = {
+        "metric": CONTACTS_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": f"{desc}; contacts mode: {CONTACTS_SEG} y slabs, contact populations {CONTACTS_POP}, "
+                               f"1 ps steps", "n_sites": st["n_sites"], "k_mean": st["k_mean"],
+                   "initial_excitons": g["n_initial"], "slots": g["capacity"], "live_excitons": live,
+                   "hops_timed": hops, "l2": "256 MB buffer written between timed steps"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "bytes_per_hop": bph,
+                     "note": "algorithmic bytes per hop x hops / device time of the whole contacts step"},
+        "gpu_launches": launches, "autotune": tune, "e2e": e2e, "clocks": clk.summary(),
+    }
+    if world == 1 and not args.no_cpu:
+        v, sample, _, threads = contacts_cpu_sample(f, tab, seed)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -196,7 +325,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-exc", type=int, default=None, help="excitons per film (default: the workload's)")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4"])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "contacts"])
     ap.add_argument("--films", type=int, default=256, help="films of the cfg3 batch")
     ap.add_argument("--bins-per-step", type=int, default=8,
                     help="1 ps MSD bins advanced per timed step (one kmc_run call)")
@@ -237,6 +366,12 @@ def main():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
+
+    if args.workload == "contacts":
+        contacts_arm(args, local, rank, world)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
 
     films, tab, n_exc, desc = workload(args.workload, args.films)
     if args.n_exc is not None:

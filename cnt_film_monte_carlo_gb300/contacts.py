@@ -1,10 +1,10 @@
 """Output files of the contacts (steady-state flux) mode in the reference's formats.
 
-* ``scatterer_statistics.dat``: get_scatterer_statistics (src/monte_carlo/monte_carlo.h:691-710),
+* ``scatterer_statistics.dat``: get_scatterer_statistics (src/monte_carlo/monte_carlo.h:691-719),
   written once by init.
-* ``population_profile.dat``: save_population_profile (:528-575), one row per step with the
+* ``population_profile.dat``: save_population_profile (:525-581), one row per step with the
   exciton density count / (area dy) of every y slab.
-* ``region_current.dat``: save_currents (:578-625), one row per step with the current
+* ``region_current.dat``: save_currents (:584-643), one row per step with the current
   count / (interface area dt) through every slab interface.
 * ``particle_path.<n>.dat``: track_particle (:786-818), the position after every step of one
   exciton walked from contact 1 to the last slab.
@@ -36,17 +36,17 @@ def _e(x: float, plus: bool) -> str:
 
 
 def slab_positions(ymin: float, dy: float, n: int) -> np.ndarray:
-    """Slab centres ymin + (i + 0.5) dy (monte_carlo.h:545-547, 704-706)."""
+    """Slab centres ymin + (i + 0.5) dy (monte_carlo.h:553, 708)."""
     return np.array([ymin + (float(i) + 0.5) * dy for i in range(n)])
 
 
 def interface_positions(ymin: float, dy: float, n: int) -> np.ndarray:
-    """Interfaces ymin + dy i, i = 1..n-1 (save_currents :585-589)."""
+    """Interfaces ymin + dy i, i = 1..n-1 (save_currents :595-597)."""
     return np.array([ymin + dy * float(i) for i in range(1, n)])
 
 
 def interface_areas(area) -> np.ndarray:
-    """(area[i-1] + area[i]) / 2 (save_currents :588)."""
+    """(area[i-1] + area[i]) / 2 (save_currents :597)."""
     a = np.asarray(area, dtype=np.float64)
     return np.array([(a[i - 1] + a[i]) / 2 for i in range(1, len(a))])
 

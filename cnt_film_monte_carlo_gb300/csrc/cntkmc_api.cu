@@ -877,7 +877,7 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
   std::vector<int32_t> rank(n);
   for (int64_t k = 0; k < n; ++k) rank[c->h_perm[k]] = (int32_t)k;
   auto y_of = [&](int64_t k) { return c->pos[3 * k + 1]; };
-  // get_area (monte_carlo.h:628-688): per slab the x and z extents, starting from the opposite
+  // get_area (monte_carlo.h:646-688): per slab the x and z extents, starting from the opposite
   // domain bounds; the else-if leaves a maximum unset while the minimum moves
   std::vector<double> xmn(n_seg, dom[3]), xmx(n_seg, dom[0]), zmn(n_seg, dom[5]), zmx(n_seg, dom[2]);
   for (int64_t k = 0; k < n; ++k) {
@@ -895,12 +895,12 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
   }
   if (area)
     for (int i = 0; i < n_seg; ++i) area[i] = (zmx[i] - zmn[i]) * (xmx[i] - xmn[i]);
-  // get_scatterer_statistics (:691-710)
+  // get_scatterer_statistics (:691-719)
   if (stat_pop) {
     std::fill(stat_pop, stat_pop + n_seg, 0);
     for (int64_t k = 0; k < n; ++k) stat_pop[(int)(std::fabs(y_of(k) - ymin) / dy) % n_seg]++;
   }
-  // contact_scats(1) and contact_scats(n_seg) (:496-517), in site order
+  // contact_scats(1) and contact_scats(n_seg) (:494-517), in site order
   std::vector<int32_t> clist;
   int64_t cn[2];
   for (int k = 0; k < 2; ++k) {
@@ -913,7 +913,7 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
     if (cfg->contact_pop[k] > 0 && cn[k] == 0)
       FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: contact %d has no site to place excitons at", k == 0 ? 1 : n_seg);
   }
-  // create_particles (:274-309): slab i gets round(pop1 + i dp) excitons at its sites
+  // create_particles (:274-316): slab i gets round(pop1 + i dp) excitons at its sites
   // [y1, y1 + dy), in site order
   std::vector<int32_t> seg_sites;
   std::vector<int64_t> seg_off(1, 0), part_first(1, 0);
@@ -961,7 +961,7 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
   CK(c, c->d_y_old.alloc(cap));
   CK(c, upload(c->d_c_list, clist.data(), clist.size(), c->stream));
   std::vector<double> yif(n_seg - 1);
-  for (int i = 1; i < n_seg; ++i) yif[i - 1] = ymin + dy * double(i);  // save_currents :585-589
+  for (int i = 1; i < n_seg; ++i) yif[i - 1] = ymin + dy * double(i);  // save_currents :595-597
   CK(c, upload(c->d_c_yif, yif.data(), yif.size(), c->stream));
   const int64_t nb = kmc::contacts_blocks(cap);
   CK(c, c->d_c_blk_a.alloc(nb + 1));

@@ -5,7 +5,7 @@
 // Reads the "exciton monte carlo" section of input.json (default file name as main.cpp:34-38),
 // then runs the same loop as main.cpp:64-76: kubo_init, save_json_properties,
 // kubo_create_particles, and while time < max time: kubo_step(dt), kubo_save_avg_dispalcement_squared.
-// With "mode": "contacts" it runs the reference's contacts loop instead (main.cpp:86-105).
+// With "mode": "contacts" it runs the reference's contacts loop instead (main.cpp:85-106).
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -29,7 +29,7 @@ int main(int argc, char** argv) {
     double time_step = jm["monte carlo time step"].as_double();
     auto t0 = std::chrono::steady_clock::now();
     if (jm.has("mode") && jm["mode"].as_string() == "contacts") {
-      // main.cpp:86-105: init, save_json_properties, the tracked particles, then step /
+      // main.cpp:85-106: init, save_json_properties, the tracked particles, then step /
       // save_metrics / repopulate_contacts -- until "maximum time for contacts simulation [seconds]" (the
       // reference's loop has no end)
       if (!jm.has("maximum time for contacts simulation [seconds]"))
@@ -37,7 +37,7 @@ int main(int argc, char** argv) {
       cntkmc::monte_carlo sim(jm);
       sim.init();
       sim.save_json_properties();
-      // main.cpp:88-90: 100 tracked particles ("number of tracked particles"), in one launch
+      // main.cpp:90-92: 100 tracked particles ("number of tracked particles"), in one launch
       sim.track_particles(time_step, jm.has("number of tracked particles") ? (int)jm["number of tracked particles"].as_int()
                                                                            : 100);
       while (sim.time() < sim.contacts_max_time()) {

@@ -1,12 +1,12 @@
 // kmc_contacts.cu -- contacts (steady-state flux) mode: the reference's second driver
-// (src/main.cpp:94-105 on mc::monte_carlo, src/monte_carlo/monte_carlo.h):
+// (src/main.cpp:85-106 on mc::monte_carlo, src/monte_carlo/monte_carlo.h):
 //
-//   init        create_particles (monte_carlo.h:274-309): a linear profile of excitons over the
+//   init        create_particles (monte_carlo.h:274-316): a linear profile of excitons over the
 //               y segments, each at a random site of its segment
 //   step        the hop kernels with nothing removed (step :343-354 = particle::step per exciton)
-//   metrics     save_population_profile (:528-575): excitons per y segment; save_currents
-//               (:578-625): net crossings of each segment interface during the step
-//   repopulate  repopulate_contacts (:443-493): excitons in the contact-1 slab are removed and
+//   metrics     save_population_profile (:525-581): excitons per y segment; save_currents
+//               (:584-643): net crossings of each segment interface during the step
+//   repopulate  repopulate_contacts (:443-491): excitons in the contact-1 slab are removed and
 //               contact_pop[0] new ones placed at random contact-1 sites; then the same for the
 //               last segment
 //   track       track_particle (:786-818): single excitons walked from contact 1 to the last
@@ -46,8 +46,8 @@ __device__ __forceinline__ int block_rank(bool flag, int* total) {
   return before + __popc(m & ((1u << lane) - 1u));
 }
 
-// particle(site pos, site, v) at a random site of `list` (the dice of create_particles :298 and
-// repopulate :479,486; the constructor's ff_time and heading, particle.h:48-52), drawing from the
+// particle(site pos, site, v) at a random site of `list` (the dice of create_particles :306 and
+// repopulate :480,486; the constructor's ff_time and heading, particle.h:48-52), drawing from the
 // slot's stream from draw n0 on.
 __device__ void create_exciton(const ContactArgs& a, int64_t s, uint64_t n0, const int32_t* list, int64_t n_list) {
   Rng g;
@@ -118,8 +118,8 @@ __device__ __forceinline__ int interfaces_below(const double* __restrict__ t, in
 
 // The step's metrics over the live excitons, then the contact-1 removal and the empty-slot
 // count of every block.
-//   segment: i = int((y - ymin) / dy) clamped to [0, n_seg)      (monte_carlo.h:561-564)
-//   interface k (y_k = ymin + dy (k + 1)): +1 if old < y_k <= y, -1 if y < y_k <= old (:609-616);
+//   segment: i = int((y - ymin) / dy) clamped to [0, n_seg)      (monte_carlo.h:569-570)
+//   interface k (y_k = ymin + dy (k + 1)): +1 if old < y_k <= y, -1 if y < y_k <= old (:628-636);
 //   the interfaces crossed form one index range, added to a difference array.
 __global__ void __launch_bounds__(kCBlock) k_contacts_metrics(ContactArgs a) {
   extern __shared__ int csh[];

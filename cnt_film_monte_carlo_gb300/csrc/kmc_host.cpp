@@ -234,6 +234,6 @@ int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* ti
   return KMC_OK;
 }
 
-const char* kmc_version(void) { return "cntkmc 0.2 (sm_103a)"; }
+const char* kmc_version(void) { return "cntkmc 0.3 (sm_103a)"; }
 
 }  // extern "C"

@@ -123,7 +123,7 @@ class monte_carlo {
     max_time_ = j_.has("maximum time for contacts simulation [seconds]")
                     ? j_["maximum time for contacts simulation [seconds]"].as_double()
                     : 0.0;
-    // get_scatterer_statistics, monte_carlo.h:691-710
+    // get_scatterer_statistics, monte_carlo.h:691-719
     std::FILE* f = std::fopen((fs::path(out_dir_) / "scatterer_statistics.dat").c_str(), "w");
     if (!f) throw std::runtime_error("cannot open scatterer_statistics.dat");
     std::fprintf(f, "position,distribution,population,density\n");
@@ -135,7 +135,7 @@ class monte_carlo {
   }
 
   // step (monte_carlo.h:343-354).  The engine runs the step, the counts behind save_metrics and
-  // repopulate_contacts as one unit, in the order of src/main.cpp:98-102.
+  // repopulate_contacts as one unit, in the order of src/main.cpp:99-102.
   void step(double dt) {
     if (!cinfo_.capacity) throw std::logic_error("step: call init() first");
     int64_t live = 0;
@@ -145,7 +145,7 @@ class monte_carlo {
     ++steps_;
   }
 
-  // save_metrics (monte_carlo.h:519-625): population_profile.dat and region_current.dat rows of
+  // save_metrics (monte_carlo.h:519-643): population_profile.dat and region_current.dat rows of
   // the last step
   void save_metrics(double dt) {
     const double dy = cinfo_.dy, ymin = cinfo_.ymin;

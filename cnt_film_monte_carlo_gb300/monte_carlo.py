@@ -137,7 +137,7 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
     def init(self):
         """Contacts (steady-state flux) set-up, monte_carlo.h:157-195: the film, the y slabs
         ("number of segments"), scatterer_statistics.dat, the contact sites and the initial
-        linear profile (create_particles :274-309).  Extensions: "contact populations" (default
+        linear profile (create_particles :274-316).  Extensions: "contact populations" (default
         [1100, 0], the reference's hard-coded values), "contacts capacity" (exciton slots),
         "maximum time for contacts simulation [seconds]"."""
         self._setup_film()
@@ -179,14 +179,14 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
 
     def step(self, dt: float):
         """step (monte_carlo.h:343-354).  The engine runs the step, the counts behind
-        save_metrics and repopulate_contacts as one unit, in the order of src/main.cpp:98-102."""
+        save_metrics and repopulate_contacts as one unit, in the order of src/main.cpp:99-102."""
         prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
         pop, cur, live = self._engine.contacts_run(1, dt, self._particle_velocity, prec)
         self._last = (pop[0], cur[0], int(live[0]))
         self._time += dt
 
     def save_metrics(self, dt: float):
-        """save_metrics (monte_carlo.h:519-625): one row of population_profile.dat and of
+        """save_metrics (monte_carlo.h:519-643): one row of population_profile.dat and of
         region_current.dat for the last step."""
         g = self._contacts
         if self._pop_file is None:
@@ -255,13 +255,13 @@ def run(input_json: str, device: int = 0) -> str:
         raise ValueError('json input file does not contain "exciton monte carlo"')
     jm = dict(j["exciton monte carlo"])
     dt = float(jm["monte carlo time step"])
-    if jm.get("mode") == "contacts":  # main.cpp:86-105, until the contacts time limit
+    if jm.get("mode") == "contacts":  # main.cpp:85-106, until the contacts time limit
         if "maximum time for contacts simulation [seconds]" not in jm:
             raise ValueError('contacts mode needs "maximum time for contacts simulation [seconds]"')
         sim = monte_carlo(jm, device)
         sim.init()
         sim.save_json_properties()
-        sim.track_particles(dt, int(jm.get("number of tracked particles", 100)))  # main.cpp:88-90
+        sim.track_particles(dt, int(jm.get("number of tracked particles", 100)))  # main.cpp:90-92
         while sim.time() < sim.contacts_max_time():
             sim.step(dt)
             sim.save_metrics(dt)

@@ -138,13 +138,13 @@ int kmc_get_msd_batches(kmc_ctx* ctx, int64_t first, int64_t count, double* out)
 int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* times, int64_t n_steps,
                       int32_t batches, double fit_fraction, double D[3], double ci95[3]);
 
-/* ---- contacts (steady-state flux) mode: the reference's second driver, src/main.cpp:94-105 ----
+/* ---- contacts (steady-state flux) mode: the reference's second driver, src/main.cpp:85-106 ----
  * init (monte_carlo.h:157-195) up to the particles: y split into n_segments slabs; get_area
- * (:628-688); get_scatterer_statistics (:691-710); contact_scats of slab 1 and slab n (:496-517);
- * create_particles (:274-309), a linear profile from contact_pop[0] to contact_pop[1] excitons
+ * (:646-688); get_scatterer_statistics (:691-719); contact_scats of slab 1 and slab n (:494-517);
+ * create_particles (:274-316), a linear profile from contact_pop[0] to contact_pop[1] excitons
  * per slab at random sites of the slab.  Then each step is step (:343-354: particle::step of
- * every exciton, nothing removed), save_metrics (:519-625: excitons per slab, net crossings of
- * every slab interface) and repopulate_contacts (:443-493: the excitons inside slab 1 are removed
+ * every exciton, nothing removed), save_metrics (:519-643: excitons per slab, net crossings of
+ * every slab interface) and repopulate_contacts (:443-491: the excitons inside slab 1 are removed
  * and contact_pop[0] new ones placed at random contact-1 sites; then the same for slab n).
  * Excitons live in slots: slot k draws from Philox stream k (key `seed`) and keeps its draw
  * counter when its exciton is removed; the initial excitons take slots 0.. in create_particles

@@ -791,7 +791,7 @@ void orc_sim_destroy(orc_sim* s) {
 
 /* ---------------------------------------------------------------- contacts mode
  * The second driver of mc::monte_carlo: init (monte_carlo.h:157-195), step (:343-354),
- * save_metrics (:519-625) and repopulate_contacts (:443-481), run as src/main.cpp:94-105 does.
+ * save_metrics (:519-643) and repopulate_contacts (:443-481), run as src/main.cpp:94-105 does.
  * Exciton slots replace the reference's particle vector: slot k draws from Philox stream k, and
  * its draw counter carries on when its exciton is removed and a new one takes the slot.  The
  * initial excitons take slots 0.. in create_particles order; the n new excitons of a contact take
@@ -803,7 +803,7 @@ static void contact_bounds(const orc_sim* s, double* ymin, double* ymax, double*
   *dy = (*ymax - *ymin) / (double)s->n_seg;
 }
 
-/* particle(pos, s, v) at a drawn site of `list` (repopulate :476-486, create_particles :297-302,
+/* particle(pos, s, v) at a drawn site of `list` (repopulate :478-488, create_particles :305-310,
  * particle.h:48-52), drawing from p's stream. */
 static void place(const orc_sim* s, orc_exc* p, const int32_t* list, int64_t n_list) {
   int dice = (int)((uint32_t)orc_rand(&p->rng) % (uint64_t)n_list);
@@ -835,7 +835,7 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
   s->c_pop[1] = pop2;
   double ymin, ymax, dy;
   contact_bounds(s, &ymin, &ymax, &dy);
-  /* get_area, monte_carlo.h:628-681 (the else-if leaves a maximum unset while the minimum moves) */
+  /* get_area, monte_carlo.h:646-688 (the else-if leaves a maximum unset while the minimum moves) */
   double *xmn = malloc(sizeof(double) * n_seg), *xmx = malloc(sizeof(double) * n_seg);
   double *zmn = malloc(sizeof(double) * n_seg), *zmx = malloc(sizeof(double) * n_seg);
   for (int i = 0; i < n_seg; ++i) {
@@ -865,10 +865,10 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
   free(xmx);
   free(zmn);
   free(zmx);
-  /* get_scatterer_statistics, monte_carlo.h:691-710 */
+  /* get_scatterer_statistics, monte_carlo.h:691-719 */
   if (stat_pop)
     for (int64_t k = 0; k < s->n; ++k) stat_pop[(int)(fabs(s->pos[3 * k + 1] - ymin) / dy) % n_seg]++;
-  /* contact_scats(1) and contact_scats(n_seg), monte_carlo.h:496-517 */
+  /* contact_scats(1) and contact_scats(n_seg), monte_carlo.h:494-517 */
   for (int c = 0; c < 2; ++c) {
     int i = c == 0 ? 1 : n_seg;
     double y1 = ymin + (double)(i - 1) * dy, y2 = ymin + (double)i * dy;
@@ -894,7 +894,7 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
     orc_rng_init(&s->exc[e].rng, seed, (uint64_t)e, 0);
     s->exc[e].site = -1;
   }
-  /* create_particles(domain, n_seg, scats, c1_pop, c2_pop), monte_carlo.h:274-309 */
+  /* create_particles(domain, n_seg, scats, c1_pop, c2_pop), monte_carlo.h:274-316 */
   int32_t* seg = malloc(sizeof(int32_t) * (s->n ? s->n : 1));
   double dp = (double)(pop2 - pop1) / ((double)n_seg - 1);
   int64_t slot = 0;
@@ -921,7 +921,7 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
   return rc;
 }
 
-/* repopulate(y1, y2, n, list), monte_carlo.h:458-493, on slots */
+/* repopulate(y1, y2, n, list), monte_carlo.h:458-491, on slots */
 static int repopulate(orc_sim* s, double y1, double y2, int64_t n_new, const int32_t* list, int64_t n_list) {
   for (int64_t e = 0; e < s->n_exc; ++e) {
     if (!s->live[e]) continue;
@@ -941,20 +941,36 @@ static int repopulate(orc_sim* s, double y1, double y2, int64_t n_new, const int
   return made < n_new ? -4 : 0;
 }
 
+void orc_sim_use_csr(orc_sim* s, int use_csr) {
+  if (use_csr && !s->rowptr) orc_sim_build_csr(s);
+  s->use_csr = use_csr;
+}
+
 int orc_contacts_step(orc_sim* s, double dt, int64_t n_steps, int64_t* pop, int64_t* curr, int64_t* n_live) {
   if (s->mode != 2) return -1;
   const int n_seg = s->n_seg;
   double ymin, ymax, dy;
   contact_bounds(s, &ymin, &ymax, &dy);
   double* yif = malloc(sizeof(double) * n_seg);
-  for (int i = 1; i < n_seg; ++i) yif[i - 1] = ymin + dy * (double)i; /* save_currents :585-589 */
+  for (int i = 1; i < n_seg; ++i) yif[i - 1] = ymin + dy * (double)i; /* save_currents :595-597 */
   int rc = 0;
   for (int64_t st = 0; st < n_steps && rc == 0; ++st) {
     /* step(dt), monte_carlo.h:343-354 */
-#pragma omp parallel for num_threads(s->n_threads) schedule(dynamic, 16)
-    for (int64_t e = 0; e < s->n_exc; ++e)
-      if (s->live[e]) step(s, s->exc + e, dt, NULL, NULL);
-    /* save_population_profile :528-575 and save_currents :578-625 (the counts; the files hold
+#pragma omp parallel num_threads(s->n_threads)
+    {
+      double* cum = NULL;
+      int32_t* col = NULL;
+      if (!s->use_csr) { /* the reference's neighbour search on every hop */
+        cum = (double*)malloc(sizeof(double) * (s->max_list + 1));
+        col = (int32_t*)malloc(sizeof(int32_t) * (s->max_list + 1));
+      }
+#pragma omp for schedule(dynamic, 16)
+      for (int64_t e = 0; e < s->n_exc; ++e)
+        if (s->live[e]) step(s, s->exc + e, dt, cum, col);
+      free(cum);
+      free(col);
+    }
+    /* save_population_profile :525-581 and save_currents :584-643 (the counts; the files hold
      * count / (area dy) and count / (interface area dt)) */
     int64_t* P = pop + st * n_seg;
     int64_t* J = curr + st * (n_seg - 1);

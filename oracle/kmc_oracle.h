@@ -101,7 +101,7 @@ int64_t orc_sim_total_hops(const orc_sim* s);
 int64_t orc_sim_total_crossings(const orc_sim* s);
 
 /* Contacts (steady-state flux) mode: the reference's second driver, init (monte_carlo.h:157-195),
- * step (:343-354), save_metrics (:519-625), repopulate_contacts (:443-493).  Slot k of `capacity`
+ * step (:343-354), save_metrics (:519-643), repopulate_contacts (:443-491).  Slot k of `capacity`
  * draws from Philox stream k (key seed) and keeps its draw counter when its exciton is removed;
  * the initial excitons take slots 0.. in create_particles order and the n new excitons of a
  * contact the n lowest empty slots.  area[n_seg] (get_area), stat_pop[n_seg]
@@ -114,6 +114,9 @@ int orc_contacts_init(orc_sim* s, int n_seg, int64_t pop1, int64_t pop2, uint64_
  * n_live[step] = excitons after repopulation.  orc_sim_get_excitons reads the slots (site -1:
  * empty). */
 int orc_contacts_step(orc_sim* s, double dt, int64_t n_steps, int64_t* pop, int64_t* curr, int64_t* n_live);
+/* Hops from the precomputed CSR (1, the default of contacts mode) or from a fresh neighbour search
+ * on every hop as the reference does (0); the results are the same. */
+void orc_sim_use_csr(orc_sim* s, int use_csr);
 /* track_particle (monte_carlo.h:786-818) for tracks first..: path [n_tracks][max_steps][3],
  * len[n_tracks] steps recorded, arrived[n_tracks].  Track k draws from Philox stream 2^32 + k. */
 int orc_contacts_track(orc_sim* s, int64_t first, int n_tracks, double dt, int64_t max_steps, double* path,

@@ -83,6 +83,7 @@ def lib():
         L.orc_contacts_init.restype = C.c_int
         L.orc_contacts_step.argtypes = [C.c_void_p, D, I64, PI64, PI64, PI64]
         L.orc_contacts_step.restype = C.c_int
+        L.orc_sim_use_csr.argtypes = [C.c_void_p, C.c_int]
         L.orc_contacts_track.argtypes = [C.c_void_p, I64, C.c_int, D, I64, PD, PI64, PI32]
         L.orc_contacts_track.restype = C.c_int
         L.orc_log_export.argtypes = [D]
@@ -289,6 +290,10 @@ class Sim:
         if rc != 0:
             raise RuntimeError(f"orc_contacts_step failed ({rc})")
         return pop[:n_steps], curr[:n_steps], live[:n_steps]
+
+    def use_csr(self, on):
+        """Hops from the CSR (True) or from the reference's per-hop neighbour search (False)."""
+        lib().orc_sim_use_csr(self.h, 1 if on else 0)
 
     def contacts_track(self, first, n_tracks, dt, max_steps):
         """track_particle for tracks first..: a list of (path [steps][3], arrived)."""

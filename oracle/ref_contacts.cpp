@@ -1,11 +1,11 @@
 // ref_contacts.cpp -- TEST INFRASTRUCTURE: drives the reference's contacts (steady-state flux)
 // mode -- mc::monte_carlo::init, step, save_metrics and repopulate (src/monte_carlo/monte_carlo.h,
-// compiled unchanged against oracle/shim) -- the way src/main.cpp:94-105 does, and dumps what the
+// compiled unchanged against oracle/shim) -- the way src/main.cpp:85-106 does, and dumps what the
 // oracle's contacts mode is checked against.
 //
 // Exciton slots (the engine's layout) are mapped onto the reference's particle vector:
 //   * rand() is defined here.  While excitons are created (create_particles inside init,
-//     monte_carlo.h:274-309, and repopulate :458-493) every creation takes a slot -- the lowest
+//     monte_carlo.h:274-316, and repopulate :458-491) every creation takes a slot -- the lowest
 //     slot emptied so far, else the next never-used one -- and its three kinds of draw (site dice,
 //     dwell time repeated while 0 (scatterer.h:76), heading (particle.h:51)) come from that slot's
 //     Philox stream, which keeps its counter across the slot's excitons.
@@ -18,7 +18,7 @@
 // that the new particles of contact 1 are stamped before contact 2 moves them; the slab bounds
 // are computed with the same expressions.  Run single threaded (OMP_NUM_THREADS=1).
 //
-// track_particle (monte_carlo.h:786-818), called n_tracks times before the loop as main.cpp:88-90
+// track_particle (monte_carlo.h:786-818), called n_tracks times before the loop as main.cpp:90-92
 // does, draws from stream 2^32 + k for track k; its positions are taken from the wrapped
 // particle::step.
 //
@@ -230,7 +230,7 @@ int main(int argc, char** argv) {
     d.put("n_initial", "i8", &n0, 1);
   }
 
-  // main.cpp:88-90: track_particle(time_step, n) before the loop
+  // main.cpp:90-92: track_particle(time_step, n) before the loop
   const long long n_tracks = argc > 5 ? std::atoll(argv[5]) : 0;
   {
     std::vector<long long> tlen;
@@ -255,7 +255,7 @@ int main(int argc, char** argv) {
     sim.step(time_step);
     g_mode = 0;
     sim.save_metrics(time_step);  // the reference's own files
-    // the integer counts behind those files (save_population_profile :560-566, save_currents :608-617)
+    // the integer counts behind those files (save_population_profile :568-573, save_currents :628-636)
     std::vector<long long> pop(n_seg, 0), curr(n_seg - 1, 0);
     for (const auto& p : sim._particle_list) {
       int i = (p.pos(1) - ymin) / dy;

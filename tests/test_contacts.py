@@ -101,3 +101,17 @@ def test_oracle_tracks_equal_reference():
     # a step cap shorter than the walk: the path stops there and the track has not arrived
     short = sim.contacts_track(1, 1, c["dt"], 100)[0]
     assert not short[1] and np.array_equal(short[0], tr[1][0][:100])
+
+
+def test_oracle_contacts_per_hop_search_equals_csr():
+    # the timed CPU baseline searches neighbours on every hop, as the reference does
+    d = load_case(CONTACT_CASES[1])
+    sim_a, _, pop_a, cur_a, live_a, c = oracle_contacts(d)
+    sim_b = O.Sim(c["pos"], c["orient"], c["left"], c["right"], c["table"], c["r_max"], c["v"], n_threads=4)
+    sim_b.contacts_init(c["n_seg"], c["pops"][0], c["pops"][1], c["seed"], len(d["ref_site"]) + 64)
+    sim_b.use_csr(False)
+    pop_b, cur_b, live_b = sim_b.contacts_step(c["dt"], c["steps"])
+    assert np.array_equal(pop_a, pop_b) and np.array_equal(cur_a, cur_b) and np.array_equal(live_a, live_b)
+    a, b = sim_a.excitons(), sim_b.excitons()
+    for k in ("site", "ff", "draws", "hops"):
+        assert np.array_equal(a[k], b[k]), k
