@@ -968,6 +968,9 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
   CK(c, c->d_c_blk_b.alloc(nb + 1));
   CK(c, c->d_c_scan.alloc(kmc::scan_scratch_len(nb + 1)));
   CK(c, c->d_c_step.alloc(1));
+  c->d_c_pop.release();  // sized by the number of slabs: reallocated by the next run
+  c->d_c_diff.release();
+  c->d_c_live.release();
   if (c->n_trace > 0) {
     CK(c, c->d_trace.alloc((size_t)(c->n_trace * c->trace_cap)));
     CK(c, c->d_trace_cnt.alloc(c->n_trace));
@@ -1049,9 +1052,13 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
   int rc = ensure_msd(c, 1);  // the hop kernels' MSD sums land in one scratch row
   if (rc) return rc;
   const int32_t n_seg = c->cargs.n_seg;
-  CK(c, c->d_c_pop.alloc((size_t)n_steps * n_seg));
-  CK(c, c->d_c_diff.alloc((size_t)n_steps * n_seg));
-  CK(c, c->d_c_live.alloc((size_t)n_steps));
+  // per-step outputs, kept between calls (a caller stepping one step at a time reuses them and
+  // the captured graph is updated in place)
+  if (c->d_c_live.n < (size_t)n_steps) {
+    CK(c, c->d_c_pop.alloc((size_t)n_steps * n_seg));
+    CK(c, c->d_c_diff.alloc((size_t)n_steps * n_seg));
+    CK(c, c->d_c_live.alloc((size_t)n_steps));
+  }
   CK(c, cudaMemsetAsync(c->d_c_pop.p, 0, (size_t)n_steps * n_seg * 8, c->stream));
   CK(c, cudaMemsetAsync(c->d_c_diff.p, 0, (size_t)n_steps * n_seg * 8, c->stream));
   CK(c, cudaMemsetAsync(c->d_c_live.p, 0, (size_t)n_steps * 8, c->stream));

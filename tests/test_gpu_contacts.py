@@ -226,3 +226,27 @@ def test_python_class_writes_reference_contacts_files(name, tmp_path):
     cfg = _contacts_json(d, str(tmp_path))
     out = MC.run(cfg)
     _check_files(out, d)
+
+
+def test_contacts_run_in_pieces_and_reinit():
+    # a run split over several calls equals one call; a second set-up with another slab count on
+    # the same engine starts afresh
+    d = load_case(CONTACT_CASES[0])
+    c = contacts_inputs(d)
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, len(c["left"])], np.int64), c["pos"], c["orient"], c["left"], c["right"])
+    e.set_table(c["table"])
+    e.build(c["r_max"])
+    e.contacts_init(3, (400, 100), 9, 0)
+    e.contacts_run(2, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    e.contacts_init(c["n_seg"], c["pops"], c["seed"], len(d["ref_site"]) + 64)
+    parts = [e.contacts_run(k, c["dt"], c["v"], L.KMC_PREC_MIXED) for k in (1, 1, 3, c["steps"] - 5)]
+    x = e.excitons()
+    e.close()
+    pop = np.concatenate([p[0] for p in parts])
+    cur = np.concatenate([p[1] for p in parts])
+    live = np.concatenate([p[2] for p in parts])
+    assert np.array_equal(pop.ravel(), d["ref_pop"])
+    assert np.array_equal(cur.ravel(), d["ref_curr"])
+    assert np.array_equal(live, d["ref_n_live"])
+    assert_slots(x, ref_slots(d))
