@@ -278,8 +278,16 @@ __device__ __forceinline__ double kmc_log(double x, const LogTab* __restrict__ t
 // and every other u lies in [2^-31, 1 - 2^-32], where |log u| >= 2^-32 and T >= 2^84 has a
 // non-zero high word.
 __device__ __forceinline__ double kmc_log_unit(double x, const LogTab* tab) {
-  if (x == 1.0) return 0.0;
-  return q116_to_double_big(log_fx_core((uint64_t)__double_as_longlong(x), 0, tab));
+  const uint64_t ix = (uint64_t)__double_as_longlong(x);
+  if (ix == 0x3FF0000000000000ull) return 0.0;  // x == 1 as an integer test (no FP64 compare)
+  return q116_to_double_big(log_fx_core(ix, 0, tab));
+}
+
+// log(RN(r / RAND_MAX)) of a dwell-time draw 1 <= r <= RAND_MAX: kmc_log_unit(u_from_rand(r)),
+// with u = 1 recognised from r
+__device__ __forceinline__ double kmc_dwell_log(uint32_t r, const LogTab* tab) {
+  if (r >= kRandMax) return 0.0;
+  return q116_to_double_big(log_fx_core((uint64_t)__double_as_longlong(u_from_rand(r)), 0, tab));
 }
 
 // ---------------------------------------------------------------- acos (asin Taylor series)

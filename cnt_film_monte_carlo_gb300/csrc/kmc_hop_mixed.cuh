@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       }
       // the dwell time's log does not depend on the row: computed here, it covers the latency of
       // the row loads
-      const double dlog = kmc_log_unit(u_from_rand(rf), s_log);
+      const double dlog = kmc_dwell_log(rf, s_log);
       if (n > 0) {
         const RowBlock* __restrict__ rb = a.blocks + f.blk0 + blk;
         bool resolved = false;

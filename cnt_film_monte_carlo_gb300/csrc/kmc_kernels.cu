@@ -569,7 +569,8 @@ int hop_mixed_blocks_per_sm(int variant, int64_t n_steps, int single_film) {
 
 // ============================================================================ self-checks
 // u_from_rand against IEEE division for r in [r0, r0 + count)
-// and the dwell-time log kmc_log_unit against the general kmc_log on the same uniform
+// and the dwell-time logs kmc_log_unit and kmc_dwell_log against the general kmc_log on the
+// same uniform
 __global__ void k_u_check(uint32_t r0, uint64_t count, unsigned long long* mism, const LogTab* tab) {
   uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
   unsigned long long bad = 0;
@@ -579,6 +580,7 @@ __global__ void k_u_check(uint32_t r0, uint64_t count, unsigned long long* mism,
     double a = u_from_rand(r), b = (double)r / (double)kRandMax;
     bad += (__double_as_longlong(a) != __double_as_longlong(b));
     bad += (__double_as_longlong(kmc_log_unit(a, tab)) != __double_as_longlong(kmc_log(b, tab)));
+    bad += (__double_as_longlong(kmc_dwell_log(r, tab)) != __double_as_longlong(kmc_log(b, tab)));
   }
   if (bad) atomicAdd(mism, bad);
 }
