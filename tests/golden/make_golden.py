@@ -82,12 +82,36 @@ CONTACT_CASES = {
     "ref_contacts_8seg": dict(tubes=20, length=30.0, box=(80, 80, 8), film_seed=11,
                               trim=([-1e-6, 1e-6], [2e-9, 78e-9], [-1e-6, 1e-6]), r_max=12e-9, n_seg=8, dt=3e-14,
                               steps=12, seed=99, tracks=0),
+    # sites on the slab boundaries: tubes along y with sites at whole nanometres and slabs of 2 nm
+    # put sites exactly on every boundary (k * 1e-9 rounds the same way as i * dy), where the
+    # reference's half-open segments, inclusive contacts and <, >= interface tests decide
+    "ref_contacts_grid": dict(film="grid", r_max=3e-9, n_seg=4, dt=1e-14, steps=15, seed=5,
+                              trim=([-1e-6, 1e-6], [-1e-6, 1e-6], [-1e-6, 1e-6]), tracks=2),
 }
 CONTACT_FILES = ("population_profile.dat", "region_current.dat", "scatterer_statistics.dat")
 
 
+def grid_film(nx=4, nz=3, n_pts=9):
+    """Tubes along y, sites at y = 0, 1, ..., n_pts - 1 nm; tube t at x = 1.5 (t mod nx) nm,
+    z = 1.25 (t div nx) nm."""
+    n_t = nx * nz
+    pos, ori, left, right = [], [], [], []
+    for t in range(n_t):
+        for k in range(n_pts):
+            i = t * n_pts + k
+            pos.append((1.5 * (t % nx), float(k), 1.25 * (t // nx)))
+            ori.append((0.0, 1.0, 0.0))
+            left.append(i - 1 if k > 0 else -1)
+            right.append(i + 1 if k < n_pts - 1 else -1)
+    return F.Film(np.array(pos), np.array(ori), np.array(left, np.int32), np.array(right, np.int32),
+                  np.arange(0, n_t * n_pts + 1, n_pts, dtype=np.int64))
+
+
 def make_contacts_case(name, c, tmp):
-    f = F.straight_tubes(c["tubes"], c["length"], box_nm=c["box"], seed=c["film_seed"])
+    if c.get("film") == "grid":
+        f = grid_film()
+    else:
+        f = F.straight_tubes(c["tubes"], c["length"], box_nm=c["box"], seed=c["film_seed"])
     mesh = os.path.join(tmp, name, "mesh")
     F.write_mesh(f, mesh)
     out_dir = os.path.join(tmp, name, "out")
