@@ -418,6 +418,7 @@ def main():
     # MSD of the last step over every replica's excitons (the path's only exchange)
     last = R.sum_msd(e.msd(0, e.stats()["steps_done"])[:, -1].sum(axis=0))
     d_eff = (last / (n_exc_total * world) / (2 * t_end)).tolist()
+    l2_gbs = e.probe_l2(32 << 20, 200)  # L2 read bandwidth, the L2 roofline's denominator
     e.close()
     dev_s = dev_ms / 1e3
     dev_s_max, wall_max, hops_all = R.job_timing(dev_s, wall, hops)
@@ -482,12 +483,21 @@ def main():
     spl = tune["steps_per_launch"] if tune else 32  # the engine's default steps per launch
     hop_launches = args.steps * math.ceil(bins / spl)
     traffic = None  # DRAM bytes per hop-kernel launch, from the ncu capture of this workload
+    l2 = None
     prof = os.path.join(ROOT, "profiles", "hop_mixed_traffic.json")
     if os.path.exists(prof):
         with open(prof) as fh:
             pj = json.load(fh).get(args.workload)
         if pj:
             traffic = pj["dram_bytes_per_hop"] * hops / max(hop_launches, 1)
+        if pj and "lts_bytes_per_hop" in pj:
+            # the film's rows stay in L2: L2->SM bytes per hop (ncu) x hops/s against the measured
+            # L2 read bandwidth
+            l2_ach = pj["lts_bytes_per_hop"] * hops / dev_s / 1e9
+            l2 = {"achieved": l2_ach, "peak": l2_gbs, "unit": "GB/s", "frac": l2_ach / l2_gbs,
+                  "bytes_per_hop": pj["lts_bytes_per_hop"],
+                  "peak_kind": "measured: kmc_probe_l2, 16-byte L2-only loads over a 32 MB buffer",
+                  "source": pj["source"]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -502,7 +512,8 @@ def main():
         "d_eff_m2_per_s": d_eff,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "bytes_per_hop": bph,
-                     "note": "algorithmic bytes per hop x hops / hop-kernel device time; CSR is L2-resident"},
+                     "note": "algorithmic bytes per hop x hops / hop-kernel device time; CSR is L2-resident",
+                     "l2": l2},
         "gpu_launches": launches,
         "autotune": tune,
         "e2e": e2e,

@@ -108,6 +108,7 @@ SIGNATURES = {
     "kmc_read_mesh": (C.c_int, [C.c_char_p, PI64, PI64, PD, PD, PI32, PI32]),
     "kmc_selftest_uniform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, PU64]),
     "kmc_math_probe": (C.c_int, [C.c_void_p, PD, C.c_int64, PD, PD]),
+    "kmc_probe_l2": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, PD]),
     "kmc_set_launch_config": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "kmc_set_mixed_variant": (C.c_int, [C.c_void_p, C.c_int32]),
     "kmc_set_work_order": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -1424,6 +1424,26 @@ int kmc_selftest_uniform(kmc_ctx* c, uint32_t r0, uint64_t count, uint64_t* mism
   return KMC_OK;
 }
 
+int kmc_probe_l2(kmc_ctx* c, int64_t bytes, int32_t reps, double* gbs) {
+  if (!c || !gbs) return KMC_ERR_ARG;
+  if (bytes < (1 << 20) || bytes % 16 || reps < 1) FAIL(c, KMC_ERR_ARG, "kmc_probe_l2: bytes >= 1 MiB, a multiple of 16; reps >= 1");
+  CK(c, cudaSetDevice(c->device));
+  DevBuf<unsigned char> buf;
+  DevBuf<unsigned long long> sink;
+  CK(c, buf.alloc((size_t)bytes));
+  CK(c, sink.alloc(1));
+  CK(c, cudaMemsetAsync(buf.p, 1, (size_t)bytes, c->stream));
+  CK(c, kmc::launch_l2_probe(buf.p, bytes, 2, c->n_sms, sink.p, c->stream));  // bring the buffer into L2
+  CK(c, cudaEventRecord(c->ev0, c->stream));
+  CK(c, kmc::launch_l2_probe(buf.p, bytes, reps, c->n_sms, sink.p, c->stream));
+  CK(c, cudaEventRecord(c->ev1, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  *gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
+  return KMC_OK;
+}
+
 int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, double* acos_out) {
   if (!c || !x || !log_out || !acos_out || n < 0) return KMC_ERR_ARG;
   if (n == 0) return KMC_OK;

@@ -234,6 +234,8 @@ cudaError_t launch_contacts_track(const HopArgs& h, const ContactArgs& a, int64_
                                   int64_t max_steps, double* path, int64_t* len, int32_t* arrived, cudaStream_t s);
 cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mismatches, const LogTab* tab,
                            cudaStream_t s);
+cudaError_t launch_l2_probe(const void* buf, int64_t bytes, int reps, int n_sms, unsigned long long* sink,
+                            cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,
                               cudaStream_t s);
 

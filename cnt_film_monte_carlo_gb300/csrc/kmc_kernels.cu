@@ -591,6 +591,26 @@ cudaError_t launch_u_check(uint32_t r0, uint64_t count, unsigned long long* mism
   return cudaGetLastError();
 }
 
+// L2 read bandwidth: every thread streams 16-byte L2-only loads (ld.global.cg) over an
+// L2-resident buffer; the XOR of what it read keeps the loads alive
+__global__ void __launch_bounds__(512) k_l2_probe(const int4* __restrict__ buf, int64_t n16, int reps,
+                                                  unsigned long long* sink) {
+  uint32_t acc = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < reps; ++r)
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += stride) {
+      const int4 v = __ldcg(buf + i);
+      acc ^= (uint32_t)(v.x ^ v.y ^ v.z ^ v.w);
+    }
+  if (acc == 0x9E3779B9u) atomicAdd(sink, 1ull);
+}
+
+cudaError_t launch_l2_probe(const void* buf, int64_t bytes, int reps, int n_sms, unsigned long long* sink,
+                            cudaStream_t s) {
+  k_l2_probe<<<(unsigned)(n_sms * 4), 512, 0, s>>>(reinterpret_cast<const int4*>(buf), bytes / 16, reps, sink);
+  return cudaGetLastError();
+}
+
 __global__ void k_math_probe(const double* x, double* lo, double* ao, int64_t n, const LogTab* tab) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;

@@ -170,6 +170,12 @@ class Engine:
                                                 L.ptr(arr, C.c_int32)))
         return [(path[t, :ln[t]].copy(), bool(arr[t])) for t in range(n_tracks)]
 
+    def probe_l2(self, nbytes: int = 32 << 20, reps: int = 20) -> float:
+        """L2 read bandwidth (GB/s) over an L2-resident buffer of nbytes."""
+        out = C.c_double(0.0)
+        self._check(self.lib.kmc_probe_l2(self.h, int(nbytes), int(reps), C.byref(out)))
+        return out.value
+
     # ------------------------------------------------------------------ run and read
     def run(self, n_steps: int, dt: float, velocity: float, precision=L.KMC_PREC_MIXED):
         self._check(self.lib.kmc_run(self.h, int(n_steps), float(dt), float(velocity), int(precision)))

@@ -236,6 +236,11 @@ int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* 
  * log, on the device for r in [r0, r0 + count); *mismatches gets the number of differences. */
 int kmc_selftest_uniform(kmc_ctx* ctx, uint32_t r0, uint64_t count, uint64_t* mismatches);
 
+/* L2 read bandwidth of this GPU (no counterpart in the reference; the denominator of the L2
+ * roofline of films whose rows stay in L2): 16-byte L2-only loads streamed over an L2-resident
+ * buffer of `bytes` (>= 1 MiB, a multiple of 16), reps passes timed with CUDA events; GB/s. */
+int kmc_probe_l2(kmc_ctx* ctx, int64_t bytes, int32_t reps, double* gbs);
+
 /* Evaluate the engine's device log and acos on x[n] (for accuracy tests). */
 int kmc_math_probe(kmc_ctx* ctx, const double* x, int64_t n, double* log_out, double* acos_out);
 

@@ -118,3 +118,14 @@ def test_free_flight_bounces_engine(precision):
         check_bounce(s0["site"], s0["heading"], s["pos"], s["heading"], k * dt)
     assert e.stats()["hops"] == 0
     e.close()
+
+
+@pytest.mark.gpu
+def test_l2_probe_separates_l2_from_hbm():
+    # the L2 roofline's denominator: an L2-resident buffer streams well above HBM speed, one far
+    # larger than the L2 at about the HBM copy rate
+    e = E.Engine(0)
+    l2 = e.probe_l2(32 << 20, 200)
+    hbm = e.probe_l2(512 << 20, 20)
+    e.close()
+    assert l2 > 1.5 * hbm > 3000.0
