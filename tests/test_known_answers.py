@@ -8,6 +8,7 @@
 * Free flight (particle::fly, particle.cpp:9-54): a three-site tube with a cutoff below its 1 nm
   spacing has no neighbours, so an exciton only flies and bounces between the tube ends; after a
   time t its position is the unfolded coordinate x0 + h v t reflected into [0, 2 nm].
+* The L2 probe behind the L2 roofline separates an L2-resident buffer from one far larger than L2.
 """
 import numpy as np
 import pytest
