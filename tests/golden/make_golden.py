@@ -87,6 +87,10 @@ CONTACT_CASES = {
     # reference's half-open segments, inclusive contacts and <, >= interface tests decide
     "ref_contacts_grid": dict(film="grid", r_max=3e-9, n_seg=4, dt=1e-14, steps=15, seed=5,
                               trim=([-1e-6, 1e-6], [-1e-6, 1e-6], [-1e-6, 1e-6]), tracks=2),
+    # two slabs: the contacts share the sites at y = ymin + dy, so contact 1's new excitons placed
+    # there are removed again by contact 2 in the same repopulation
+    "ref_contacts_grid2": dict(film="grid", r_max=3e-9, n_seg=2, dt=1e-14, steps=10, seed=8,
+                               trim=([-1e-6, 1e-6], [-1e-6, 1e-6], [-1e-6, 1e-6]), tracks=0),
 }
 CONTACT_FILES = ("population_profile.dat", "region_current.dat", "scatterer_statistics.dat")
 

@@ -11,7 +11,7 @@ from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ("ref_forster_region", "ref_wong_region")
-CONTACT_CASES = ("ref_contacts_5seg", "ref_contacts_8seg", "ref_contacts_grid")
+CONTACT_CASES = ("ref_contacts_5seg", "ref_contacts_8seg", "ref_contacts_grid", "ref_contacts_grid2")
 
 
 def load_case(name):

@@ -250,3 +250,25 @@ def test_contacts_run_in_pieces_and_reinit():
     assert np.array_equal(cur.ravel(), d["ref_curr"])
     assert np.array_equal(live, d["ref_n_live"])
     assert_slots(x, ref_slots(d))
+
+
+def test_contacts_at_scale_orders_and_precisions_agree():
+    # the cfg4 film (10.8 M sites), 20 slabs, 6 M initial excitons in 13 M slots: mixed precision
+    # in spatial and slot order equals the plain FP64 kernel, slot for slot
+    f = F.lognormal_tubes(20000, 500.0, 0.4, (5000.0, 5000.0, 50.0), seed=7)
+    c = dict(pos=f.pos_m(), orient=f.orient, left=f.left, right=f.right, table=tables.forster_2d(1e15),
+             r_max=10e-9, v=2e5, n_seg=20)
+    pops, seed, steps, dt = (500_000, 100_000), 4, 2, 2e-13
+    runs = []
+    for prec, order in ((L.KMC_PREC_MIXED, L.KMC_ORDER_SPATIAL), (L.KMC_PREC_MIXED, L.KMC_ORDER_SLOTS),
+                        (L.KMC_PREC_FP64, L.KMC_ORDER_AUTO)):
+        g, pop, cur, live, x, st = engine_contacts(c, pops, seed, 0, prec, steps, dt, order)
+        runs.append((g, pop, cur, live, x, st))
+    g0, pop0, cur0, live0, x0, st0 = runs[0]
+    assert g0["n_initial"] > 5_000_000 and g0["capacity"] > 10_000_000
+    assert (pop0.sum(axis=1) > 5_000_000).all() and np.abs(cur0).sum() > 0 and (live0 > 5_000_000).all()
+    for g, pop, cur, live, x, st in runs[1:]:
+        assert np.array_equal(pop, pop0) and np.array_equal(cur, cur0) and np.array_equal(live, live0)
+        for k in ("site", "pos", "ff", "heading", "draws", "hops"):
+            assert np.array_equal(x[k], x0[k]), k
+        assert st["hops"] == st0["hops"]
