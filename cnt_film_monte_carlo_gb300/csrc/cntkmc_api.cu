@@ -149,6 +149,15 @@ struct kmc_ctx {
   DevBuf<int64_t> d_c_blk_a, d_c_blk_b, d_c_scan, d_c_step;
   DevBuf<unsigned long long> d_c_pop, d_c_diff, d_c_live;
   cudaGraphExec_t cgexec = nullptr;  // one contacts step, replayed
+  // what the captured contacts step depends on; an unchanged key replays it without a new capture
+  struct ContactsGraphKey {
+    double dt, v;
+    int32_t precision, variant, ordered, grid_blocks, single_film;
+    int64_t hop_cap, n_trace, n_slots;
+    const void *pop, *diff, *live, *msd, *order, *cargs_step;
+  } cgkey{};
+  bool cgkey_valid = false;
+  int c_launches = 0;
 };
 
 #define FAIL(ctx, code, ...)                                          \
@@ -968,6 +977,7 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
   CK(c, c->d_c_blk_b.alloc(nb + 1));
   CK(c, c->d_c_scan.alloc(kmc::scan_scratch_len(nb + 1)));
   CK(c, c->d_c_step.alloc(1));
+  c->cgkey_valid = false;  // buffers and slots change: the next run captures its step afresh
   c->d_c_pop.release();  // sized by the number of slabs: reallocated by the next run
   c->d_c_diff.release();
   c->d_c_live.release();
@@ -1081,8 +1091,32 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
     return e;
   };
   if (c->use_graph) {
-    rc = capture_graph(c, &c->cgexec, enqueue);
-    if (rc) return rc;
+    kmc_ctx::ContactsGraphKey key{};
+    key.dt = dt;
+    key.v = v;
+    key.precision = precision;
+    key.variant = c->mixed_variant;
+    key.ordered = plan.ordered ? 1 : 0;
+    key.grid_blocks = plan.grid_blocks;
+    key.single_film = plan.single_film;
+    key.hop_cap = c->hop_cap;
+    key.n_trace = c->n_trace;
+    key.n_slots = c->n_slots;
+    key.pop = ca.pop;
+    key.diff = ca.diff;
+    key.live = ca.n_live;
+    key.msd = a.msd;
+    key.order = c->d_order.p;
+    key.cargs_step = ca.step;
+    if (!(c->cgexec && c->cgkey_valid && std::memcmp(&key, &c->cgkey, sizeof key) == 0)) {
+      c->cgkey_valid = false;
+      rc = capture_graph(c, &c->cgexec, enqueue);
+      if (rc) return rc;
+      c->cgkey = key;
+      c->cgkey_valid = true;
+      c->c_launches = nl;
+    }
+    nl = c->c_launches;
     CK(c, cudaEventRecord(c->ev0, c->stream));
     for (int64_t s = 0; s < n_steps; ++s) CK(c, cudaGraphLaunch(c->cgexec, c->stream));
   } else {
