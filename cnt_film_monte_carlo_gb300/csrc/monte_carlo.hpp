@@ -190,7 +190,7 @@ class monte_carlo {
   // track_particle (monte_carlo.h:786-818): particle_path.<fileNo>.dat.  Track fileNo draws from
   // its own stream, so track_particles(dt, n) (all n in one launch) writes the same files as n
   // calls.  The reference loops until the exciton reaches the last slab; here at most
-  // "maximum steps per tracked particle" (default 2^20) steps, with a warning when it has not.
+  // "maximum steps per tracked particle" (default 2^18) steps, with a warning when it has not.
   void track_particle(double dt, int fileNo) { tracks(dt, fileNo, 1); }
   void track_particles(double dt, int count) { tracks(dt, 0, count); }
 
@@ -248,7 +248,7 @@ class monte_carlo {
   void tracks(double dt, int first, int count) {
     if (count <= 0) return;
     const int64_t cap = j_.has("maximum steps per tracked particle") ? j_["maximum steps per tracked particle"].as_int()
-                                                                      : (int64_t)1 << 20;
+                                                                      : (int64_t)1 << 18;
     std::vector<double> path((size_t)count * (size_t)cap * 3);
     std::vector<int64_t> len((size_t)count);
     std::vector<int32_t> arrived((size_t)count);

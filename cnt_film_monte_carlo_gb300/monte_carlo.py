@@ -161,11 +161,11 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
 
     def track_particles(self, dt: float, count: int, first: int = 0):
         """Tracks first .. first + count - 1 in one launch (each has its own stream, so this equals
-        count track_particle calls).  At most "maximum steps per tracked particle" (default 2^20)
+        count track_particle calls).  At most "maximum steps per tracked particle" (default 2^18)
         steps each; the reference loops until the exciton reaches the last slab."""
         if count <= 0:
             return []
-        cap = int(self._json_prop.get("maximum steps per tracked particle", 1 << 20))
+        cap = int(self._json_prop.get("maximum steps per tracked particle", 1 << 18))
         tr = self._engine.contacts_track(first, count, dt, self._particle_velocity, cap)
         for t, (path, arrived) in enumerate(tr):
             with open(os.path.join(self._output_directory, f"particle_path.{first + t}.dat"), "w") as f:
