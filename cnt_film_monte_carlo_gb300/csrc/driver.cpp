@@ -6,6 +6,7 @@
 // then runs the same loop as main.cpp:64-76: kubo_init, save_json_properties,
 // kubo_create_particles, and while time < max time: kubo_step(dt), kubo_save_avg_dispalcement_squared.
 // With "mode": "contacts" it runs the reference's contacts loop instead (main.cpp:85-106).
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <fstream>
@@ -14,6 +15,8 @@
 #include <string>
 
 #include "monte_carlo.hpp"
+
+static const int64_t kChunk = 256;  // time steps per engine call
 
 int main(int argc, char** argv) {
   try {
@@ -40,11 +43,9 @@ int main(int argc, char** argv) {
       // main.cpp:90-92: 100 tracked particles ("number of tracked particles"), in one launch
       sim.track_particles(time_step, jm.has("number of tracked particles") ? (int)jm["number of tracked particles"].as_int()
                                                                            : 100);
-      while (sim.time() < sim.contacts_max_time()) {
-        sim.step(time_step);
-        sim.save_metrics(time_step);
-        sim.repopulate_contacts();
-      }
+      // the loop's steps in chunks of one engine call each (same rows as one call per step)
+      for (int64_t left = sim.steps_until(sim.contacts_max_time(), time_step); left > 0; left -= kChunk)
+        sim.contacts_steps_and_save(std::min<int64_t>(kChunk, left), time_step);
       kmc_run_stats rs = sim.run_stats();
       double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
       std::printf("contacts simulation finished: %lld steps, %lld hops, %u particles, wall %.3f s\n",
@@ -60,9 +61,9 @@ int main(int argc, char** argv) {
     std::printf("sites: %lld  neighbour entries: %lld (mean %.2f, max %d)  build: %.3f ms\n", (long long)nb.n_sites,
                 (long long)nb.nnz, nb.k_mean, nb.k_max, nb.build_ms);
     double dev_ms = 0;
-    while (sim.time() < sim.kubo_max_time()) {
-      sim.kubo_step(time_step);
-      sim.kubo_save_avg_dispalcement_squared();
+    // main.cpp:70-76's loop, its steps in chunks of one engine call each (same rows)
+    for (int64_t left = sim.steps_until(sim.kubo_max_time(), time_step); left > 0; left -= kChunk) {
+      sim.kubo_steps_and_save(std::min<int64_t>(kChunk, left), time_step);
       dev_ms += sim.run_stats().last_run_ms;
     }
     kmc_run_stats rs = sim.run_stats();

@@ -224,17 +224,55 @@ class monte_carlo {
 
   // monte_carlo.cpp:382-409
   void kubo_save_avg_dispalcement_squared() {
-    if (!msd_) {
-      msd_ = std::fopen((fs::path(out_dir_) / "particle_dispalcement.avg.squared.dat").c_str(), "w");
-      if (!msd_) throw std::runtime_error("cannot open the MSD file");
-      std::fprintf(msd_, "# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble over time\n");
-      std::fprintf(msd_, "# number of particles: %lld\n\ntime,x,y,z\n", (long long)n_particles_);
-    }
+    open_msd_file();
     double s[3];
     check(kmc_get_msd(ctx_, steps_ - 1, 1, s), "kmc_get_msd");
     double n = double(n_particles_);
     std::fprintf(msd_, "%+e,%+e,%+e,%+e\n", time_, s[0] / n, s[1] / n, s[2] / n);
     std::fflush(msd_);
+  }
+
+  // n calls of kubo_step(dt), each followed by kubo_save_avg_dispalcement_squared, run as one
+  // engine call (the rows and times are those of the n separate calls)
+  void kubo_steps_and_save(int64_t n, double dt) {
+    if (n <= 0) return;
+    check(kmc_run(ctx_, n, dt, velocity_, precision()), "kmc_run");
+    std::vector<double> s((size_t)(3 * n));
+    check(kmc_get_msd(ctx_, steps_, n, s.data()), "kmc_get_msd");
+    open_msd_file();
+    const double np = double(n_particles_);
+    for (int64_t k = 0; k < n; ++k) {
+      time_ += dt;
+      ++steps_;
+      std::fprintf(msd_, "%+e,%+e,%+e,%+e\n", time_, s[3 * k] / np, s[3 * k + 1] / np, s[3 * k + 2] / np);
+    }
+    std::fflush(msd_);
+  }
+
+  // n rounds of step(dt), save_metrics(dt), repopulate_contacts() as one engine call
+  void contacts_steps_and_save(int64_t n, double dt) {
+    if (n <= 0) return;
+    if (!cinfo_.capacity) throw std::logic_error("contacts_steps_and_save: call init() first");
+    std::vector<int64_t> pop((size_t)(n * n_seg_)), cur((size_t)(n * (n_seg_ - 1))), live((size_t)n);
+    check(kmc_contacts_run(ctx_, n, dt, velocity_, precision(), pop.data(), cur.data(), live.data()),
+          "kmc_contacts_run");
+    for (int64_t k = 0; k < n; ++k) {
+      std::copy(pop.begin() + k * n_seg_, pop.begin() + (k + 1) * n_seg_, pop_.begin());
+      std::copy(cur.begin() + k * (n_seg_ - 1), cur.begin() + (k + 1) * (n_seg_ - 1), cur_.begin());
+      live_ = live[(size_t)k];
+      time_ += dt;
+      ++steps_;
+      save_metrics(dt);
+      repopulate_contacts();
+    }
+  }
+
+  // the number of steps of main.cpp's `while (time < max time) step(dt)` from the current time,
+  // with the same floating-point accumulation of the time
+  int64_t steps_until(double t_max, double dt) const {
+    int64_t n = 0;
+    for (double t = time_; t < t_max; t += dt) ++n;
+    return n;
   }
 
   const kmc_nbr_stats& neighbor_stats() const { return nbr_; }
@@ -245,6 +283,13 @@ class monte_carlo {
   }
 
  private:
+  void open_msd_file() {
+    if (msd_) return;
+    msd_ = std::fopen((fs::path(out_dir_) / "particle_dispalcement.avg.squared.dat").c_str(), "w");
+    if (!msd_) throw std::runtime_error("cannot open the MSD file");
+    std::fprintf(msd_, "# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble over time\n");
+    std::fprintf(msd_, "# number of particles: %lld\n\ntime,x,y,z\n", (long long)n_particles_);
+  }
   void tracks(double dt, int first, int count) {
     if (count <= 0) return;
     const int64_t cap = j_.has("maximum steps per tracked particle") ? j_["maximum steps per tracked particle"].as_int()

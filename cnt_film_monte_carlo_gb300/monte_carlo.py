@@ -226,17 +226,58 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         self._step += 1
         self._time += dt
 
-    def kubo_save_avg_dispalcement_squared(self):
-        """monte_carlo.cpp:382-409: one row "time,<dx^2>,<dy^2>,<dz^2>" (showpos, scientific)."""
+    def _open_msd_file(self):
         if self._msd_file is None:
             self._msd_file = open(os.path.join(self._output_directory, "particle_dispalcement.avg.squared.dat"), "w")
             self._msd_file.write("# this file contains the average of dx^2, dy^2, and dz^2 of the particle ensemble "
                                  "over time\n")
             self._msd_file.write(f"# number of particles: {self._n_particles}\n\n")
             self._msd_file.write("time,x,y,z\n")
+
+    def kubo_save_avg_dispalcement_squared(self):
+        """monte_carlo.cpp:382-409: one row "time,<dx^2>,<dy^2>,<dz^2>" (showpos, scientific)."""
+        self._open_msd_file()
         s = self._engine.msd(self._step - 1, 1)[0, 0] / float(self._n_particles)
         self._msd_file.write(f"{self._time:+.6e},{s[0]:+.6e},{s[1]:+.6e},{s[2]:+.6e}\n")
         self._msd_file.flush()
+
+    def kubo_steps_and_save(self, n: int, dt: float):
+        """n calls of kubo_step(dt), each followed by kubo_save_avg_dispalcement_squared, as one
+        engine call (the rows and times are those of the n separate calls)."""
+        if n <= 0:
+            return
+        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
+        self._engine.run(n, dt, self._particle_velocity, prec)
+        sums = self._engine.msd(self._step, n)[0] / float(self._n_particles)
+        rows = []
+        for k in range(n):
+            self._time += dt
+            self._step += 1
+            rows.append(f"{self._time:+.6e},{sums[k, 0]:+.6e},{sums[k, 1]:+.6e},{sums[k, 2]:+.6e}\n")
+        self._open_msd_file()
+        self._msd_file.write("".join(rows))
+        self._msd_file.flush()
+
+    def contacts_steps_and_save(self, n: int, dt: float):
+        """n rounds of step(dt), save_metrics(dt), repopulate_contacts() as one engine call."""
+        if n <= 0:
+            return
+        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
+        pop, cur, live = self._engine.contacts_run(n, dt, self._particle_velocity, prec)
+        for k in range(n):
+            self._last = (pop[k], cur[k], int(live[k]))
+            self._time += dt
+            self.save_metrics(dt)
+            self.repopulate_contacts()
+
+    def steps_until(self, t_max: float, dt: float) -> int:
+        """The number of steps of main.cpp's `while (time < max time)` loop from the current time,
+        with the same floating-point accumulation of the time."""
+        n, t = 0, self._time
+        while t < t_max:
+            t += dt
+            n += 1
+        return n
 
     def close(self):
         for name in ("_msd_file", "_pop_file", "_cur_file"):
@@ -245,6 +286,9 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
                 f.close()
                 setattr(self, name, None)
         self._engine.close()
+
+
+CHUNK = 256  # time steps per engine call in run()
 
 
 def run(input_json: str, device: int = 0) -> str:
@@ -262,10 +306,10 @@ def run(input_json: str, device: int = 0) -> str:
         sim.init()
         sim.save_json_properties()
         sim.track_particles(dt, int(jm.get("number of tracked particles", 100)))  # main.cpp:90-92
-        while sim.time() < sim.contacts_max_time():
-            sim.step(dt)
-            sim.save_metrics(dt)
-            sim.repopulate_contacts()
+        left = sim.steps_until(sim.contacts_max_time(), dt)  # the loop's steps, in chunks of one call
+        while left > 0:
+            sim.contacts_steps_and_save(min(CHUNK, left), dt)
+            left -= CHUNK
         out = sim.output_path()
         sim.close()
         return out
@@ -273,9 +317,10 @@ def run(input_json: str, device: int = 0) -> str:
     sim.kubo_init()
     sim.save_json_properties()
     sim.kubo_create_particles()
-    while sim.time() < sim.kubo_max_time():
-        sim.kubo_step(dt)
-        sim.kubo_save_avg_dispalcement_squared()
+    left = sim.steps_until(sim.kubo_max_time(), dt)  # main.cpp:70-76's steps, in chunks of one call
+    while left > 0:
+        sim.kubo_steps_and_save(min(CHUNK, left), dt)
+        left -= CHUNK
     out = sim.output_path()
     sim.close()
     return out
