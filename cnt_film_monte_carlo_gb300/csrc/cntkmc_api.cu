@@ -101,6 +101,7 @@ struct kmc_ctx {
   int64_t nblk = 0;
   DevBuf<kmc::SiteRec> d_rec;
   DevBuf<double2> d_lt64;
+  DevBuf<double> d_ulink;
   // spatial storage order of the sites: perm[slot] = reference id, rank[id] = slot; the
   // hop kernels read positions and links per slot
   DevBuf<int32_t> d_perm, d_rank, d_left_i, d_right_i;
@@ -140,6 +141,9 @@ struct kmc_ctx {
   // the launch sequence of a run is captured into a CUDA graph and replayed
   bool use_graph = true;
   cudaGraphExec_t gexec = nullptr;
+  // steps of the last run averaged fewer than kShortStepHops hops per exciton: the mixed kernel
+  // batches step ends across each warp (see k_hop_mixed)
+  bool short_steps = true;
   // contacts (steady-state flux) mode
   bool contacts = false;
   kmc::ContactArgs cargs{};
@@ -482,6 +486,7 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, c->d_inv_total.alloc(n));
   CK(c, c->d_rec.alloc(n));
   CK(c, c->d_lt64.alloc(n));
+  CK(c, c->d_ulink.alloc(6 * (size_t)n));
   CK(c, c->d_pos4i.alloc(n));
   CK(c, c->d_left_i.alloc(n));
   CK(c, c->d_right_i.alloc(n));
@@ -667,6 +672,7 @@ static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   a.blast = c->d_blast.p;
   a.cump = c->d_cump.p;
   a.lt64 = c->d_lt64.p;
+  a.ulink = c->d_ulink.p;
   a.films = c->d_films.p;
   a.warp_film = c->d_warp_film.p;
   a.inject = c->d_inject.p;
@@ -691,7 +697,14 @@ static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   a.hop_cap = c->hop_cap;
   a.dt = dt;
   a.v = v;
+  a.hold_short = c->short_steps ? 1 : 0;
   return a;
+}
+
+// Hops per exciton-step of a run decide whether the next runs batch step ends (short steps).
+constexpr double kShortStepHops = 64.0;
+static void note_step_length(kmc_ctx* c, double hops, double exciton_steps) {
+  if (exciton_steps > 0) c->short_steps = hops < kShortStepHops * exciton_steps;
 }
 
 // Whether the mixed kernel takes the excitons in spatial order: on request, or (auto) when there
@@ -725,7 +738,8 @@ struct HopPlan {
 
 static int prepare_hops(kmc_ctx* c, double v, int32_t precision, int variant, int64_t steps_per_launch, HopPlan* p) {
   if (precision == KMC_PREC_MIXED && c->lt_v != v) {
-    CK(c, kmc::launch_link_times(c->d_pos4i.p, c->d_left_i.p, c->d_right_i.p, c->d_rec.p, c->d_lt64.p, c->n_sites, v,
+    CK(c, kmc::launch_link_times(c->d_pos4i.p, c->d_left_i.p, c->d_right_i.p, c->d_rec.p, c->d_lt64.p, c->d_ulink.p,
+                                 c->n_sites, v,
                                  c->stream));
     c->lt_v = v;
   }
@@ -857,6 +871,7 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   rc = run_steps(c, a, n_steps, c->steps_done, precision, c->mixed_variant, c->steps_per_launch, &ms, &launches);
   unsigned long long after[4];
   CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
+  note_step_length(c, (double)(after[0] - (unsigned long long)c->stats.hops), (double)c->n_exc_total * n_steps);
   c->steps_done += n_steps;
   c->stats.hops = (int64_t)after[0];
   c->stats.crossings = (int64_t)after[1];
@@ -1130,6 +1145,7 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
   rc = check_device_error(c, "kmc_contacts_run");
   unsigned long long after[4];
   CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
+  const unsigned long long hops_before = (unsigned long long)c->stats.hops;
   c->c_steps += n_steps;
   c->stats.hops = (int64_t)after[0];
   c->stats.crossings = (int64_t)after[1];
@@ -1153,6 +1169,9 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
     }
     if (n_live) n_live[s] = (int64_t)hl[s];
   }
+  double live_steps = 0;
+  for (int64_t s = 0; s < n_steps; ++s) live_steps += (double)hl[s];
+  note_step_length(c, (double)(after[0] - hops_before), live_steps);
   return KMC_OK;
 }
 

@@ -28,6 +28,9 @@ __device__ __forceinline__ bool link_time_less(uint32_t lt_hi, const double2* lt
   return lt < dtf;
 }
 
+// step-end batching: lanes at the end of a step of fewer than kHoldHops hops wait for the warp
+constexpr uint32_t kHoldHops = 64;
+
 // Exact ff <= rem for rem >= +0 and ff not a NaN with the sign bit set (device NaNs are
 // positive): non-negative doubles order like their bit patterns, and a negative ff (or -0.0)
 // is below every non-negative rem in both orders.
@@ -63,6 +66,66 @@ struct DrawRing {
   }
 };
 
+// fly(dtf) at the end of a step (particle.cpp:9-54), the position materialised in e.  From a
+// site (at_site: e's position is the site's) the link's flight time and unit vector are the
+// precomputed lt64 and ulink, which particle::fly's operations give from the site position; a
+// flight that starts between sites computes them as fly_full does.
+__device__ __forceinline__ void fly_end(const HopArgs& a, Exciton& e, bool at_site, double dtf) {
+  if (a.left[e.site] < 0 && a.right[e.site] < 0) return;
+  for (int guard = 0;; ++guard) {
+    if (guard >= kMaxCrossings) {
+      atomicOr(a.err, KMC_ERR_FLIGHT_CODE);
+      return;
+    }
+    const int32_t l = a.left[e.site], r = a.right[e.site];
+    const int32_t next = e.heading ? (r > -1 ? r : l) : (l > -1 ? l : r);
+    const bool to_right = (next == r);
+    e.heading = to_right;
+    const double4_32a t = a.pos4[next];
+    if (at_site) {
+      const double2 lt2 = a.lt64[e.site];
+      const double lt = to_right ? lt2.y : lt2.x;
+      if (lt < dtf) {
+        e.px = t.x;
+        e.py = t.y;
+        e.pz = t.z;
+        e.site = next;
+        dtf -= lt;
+        e.crossings++;
+        trace_push(a, e, -1 - next);
+        continue;
+      }
+      const double* u = a.ulink + (int64_t)e.site * 6 + (to_right ? 3 : 0);
+      const double k = a.v * dtf;
+      e.px = e.px + k * u[0];
+      e.py = e.py + k * u[1];
+      e.pz = e.pz + k * u[2];
+      return;
+    }
+    const double dist = norm3(e.px - t.x, e.py - t.y, e.pz - t.z);
+    if (dist / a.v < dtf) {
+      e.px = t.x;
+      e.py = t.y;
+      e.pz = t.z;
+      e.site = next;
+      dtf -= dist / a.v;
+      e.crossings++;
+      trace_push(a, e, -1 - next);
+      at_site = true;
+      continue;
+    }
+    const double e0 = t.x - e.px, e1 = t.y - e.py, e2 = t.z - e.pz;
+    const double nn = norm3(e0, e1, e2);
+    const double den = nn != 0 ? nn : 1.0;
+    const double u0 = e0 / den, u1 = e1 / den, u2 = e2 / den;
+    const double k = a.v * dtf;
+    e.px = e.px + k * u0;
+    e.py = e.py + k * u1;
+    e.pz = e.pz + k * u2;
+    return;
+  }
+}
+
 __device__ __forceinline__ void cold_trace(const HopArgs& a, int64_t t, int32_t v) {
   int64_t k = a.trace_cnt[t];
   if (k < a.trace_cap) a.trace[t * a.trace_cap + k] = v;
@@ -74,7 +137,7 @@ __device__ __forceinline__ void cold_trace(const HopArgs& a, int64_t t, int32_t 
 // through all n_steps steps of the launch on its own, stores it and takes the next one, so no
 // lane waits for another lane's exciton.  MSD sums of a single-film run without batches go to
 // block-shared bins (added to global memory once per block); otherwise to global memory.
-template <int BLOCK, int MINB>
+template <int BLOCK, int MINB, bool HOLD>
 __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_steps, unsigned long long* queue,
                                                          int single_film) {
   extern __shared__ double s_mem[];
@@ -189,7 +252,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       load_rec(site);
     }
     const FilmDev& f = *fp;
-    if (dwell_fits(ff, rem)) {
+    const bool step_end = !dwell_fits(ff, rem);
+    if (HOLD) {
+      // The end of a step is mostly FP64 work (flight, displacement, MSD), which the FP64 pipe
+      // runs at the same cost for one lane as for a warp.  When steps are short (few hops per
+      // step: the HOLD instantiation, launched when a.hold_short), a lane at the end of a short
+      // step waits until half of the warp's active lanes are at the end of theirs, so that they
+      // run it together.  The waiting lanes stay at their step ends and every other lane reaches
+      // its own, so the count only grows and the wait ends.  Only the order of work changes,
+      // never a result.
+      const unsigned act = __activemask();
+      const unsigned ends = __ballot_sync(act, step_end);
+      if (step_end && hs < kHoldHops && 2 * __popc(ends) < __popc(act)) continue;
+    }
+    if (!step_end) {
       // ------------------------------------------------ one event of particle::step (particle.cpp:71-84)
       rem -= ff;
       double dtf = ff;
@@ -425,7 +501,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       }
       e.trace_i = tracing ? cur - f.slot0 : -1;
       e.crossings = 0;
-      fly_full(a, e, rem);
+      fly_end(a, e, at_site, rem);
       ecross += (uint32_t)e.crossings;
       ff -= rem;
       // update_delta_pos: delta += pos - old_pos, with the step's start in the slot arrays
@@ -510,29 +586,34 @@ static size_t mixed_smem(int64_t n_steps, int single_film) {
          BLOCK * (sizeof(ColdState) + 8 * sizeof(uint32_t));
 }
 
+// a.hold_short picks the instantiation that batches the ends of short steps
 template <int BLOCK, int MINB>
 static cudaError_t launch_mixed_t(const HopArgs& a, int64_t n_steps, int grid_blocks, int single_film,
                                   unsigned long long* queue, cudaStream_t s) {
   const size_t smem = mixed_smem<BLOCK>(n_steps, single_film);
+  auto kern = a.hold_short ? k_hop_mixed<BLOCK, MINB, true> : k_hop_mixed<BLOCK, MINB, false>;
   if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_hop_mixed<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   int64_t need = (a.n_slots + BLOCK - 1) / BLOCK;
   int64_t nb = need < grid_blocks ? need : grid_blocks;
   cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
-  if (nb) k_hop_mixed<BLOCK, MINB><<<(unsigned)nb, BLOCK, smem, s>>>(a, n_steps, queue, single_film);
+  if (nb) kern<<<(unsigned)nb, BLOCK, smem, s>>>(a, n_steps, queue, single_film);
   return cudaGetLastError();
 }
 
+// resident blocks per SM (both instantiations are built for MINB blocks of BLOCK threads)
 template <int BLOCK, int MINB>
 static int blocks_per_sm_t(int64_t n_steps, int single_film) {
   int nb = 0;
   const size_t smem = mixed_smem<BLOCK>(n_steps, single_film);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(k_hop_mixed<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_hop_mixed<BLOCK, MINB>, BLOCK, smem) != cudaSuccess)
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_hop_mixed<BLOCK, MINB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_hop_mixed<BLOCK, MINB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_hop_mixed<BLOCK, MINB, false>, BLOCK, smem) != cudaSuccess)
     return 1;
   return nb > 0 ? nb : 1;
 }

@@ -79,6 +79,7 @@ struct HopArgs {
   const float* blast;     // last FP32 value of every block (second search level of long rows)
   const double* cump;     // FP64 cumulative rates in the blocked layout (8 per block)
   const double2* lt64;    // exact link times (left, right)
+  const double* ulink;    // [site][6]: unit vectors toward the left and the right neighbour
   // films and excitons
   const FilmDev* films;
   const int32_t* warp_film;
@@ -106,6 +107,7 @@ struct HopArgs {
   int32_t* err;
   int64_t hop_cap;
   double dt, v;
+  int32_t hold_short;     // mixed kernel: batch the ends of short steps across a warp (order only)
 };
 
 // FP32 screen of candidate pairs: squared-distance bounds (m^2) outside of which a pair is
@@ -162,7 +164,7 @@ cudaError_t launch_blk_counts(const BuildArgs& a, cudaStream_t s);
 cudaError_t exclusive_scan_i64(int64_t* data, int64_t n, int64_t* scratch, int64_t scratch_len, cudaStream_t s);
 int64_t scan_scratch_len(int64_t n);
 cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, const int32_t* right, SiteRec* rec,
-                              double2* lt64, int64_t n, double v, cudaStream_t s);
+                              double2* lt64, double* ulink, int64_t n, double v, cudaStream_t s);
 cudaError_t launch_init_excitons(const HopArgs& a, cudaStream_t s);
 // spatial storage order of the sites (see tile_bucket): tiles of kOrderTile x kOrderTile cell
 // columns; order_buckets(f) = tiled cell buckets of one film (with padding)

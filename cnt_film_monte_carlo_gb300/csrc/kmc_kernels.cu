@@ -329,30 +329,44 @@ cudaError_t launch_nbr_fill(const BuildArgs& a, cudaStream_t s) {
 
 // link times dist/v to the left and right tube neighbour, dist = norm(pos - next.pos) as in
 // fly (particle.cpp:40-42) evaluated at the site's own position
+// Per site and link: the flight time of the link (fly's dist / v) and the unit vector toward the
+// neighbour (fly's normalise(next - pos)), with the operations of particle::fly from the site
+// position, so that a flight starting at a site needs neither a root nor a division.
 __global__ void k_link_times(const double4_32a* __restrict__ pos4, const int32_t* __restrict__ left,
-                             const int32_t* __restrict__ right, SiteRec* rec, double2* lt64, int64_t n, double v) {
+                             const int32_t* __restrict__ right, SiteRec* rec, double2* lt64, double* ulink, int64_t n,
+                             double v) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (s >= n) return;
   double4_32a p = pos4[s];
   double tl = 0, tr = 0;
+  double u[6] = {0, 0, 0, 0, 0, 0};
   int32_t l = left[s], r = right[s];
-  if (l >= 0) {
-    double4_32a t = pos4[l];
-    tl = norm3(p.x - t.x, p.y - t.y, p.z - t.z) / v;
-  }
-  if (r >= 0) {
-    double4_32a t = pos4[r];
-    tr = norm3(p.x - t.x, p.y - t.y, p.z - t.z) / v;
+  for (int side = 0; side < 2; ++side) {
+    const int32_t nb = side ? r : l;
+    if (nb < 0) continue;
+    double4_32a t = pos4[nb];
+    const double lt = norm3(p.x - t.x, p.y - t.y, p.z - t.z) / v;
+    const double e0 = t.x - p.x, e1 = t.y - p.y, e2 = t.z - p.z;
+    const double nn = norm3(e0, e1, e2);
+    const double den = nn != 0 ? nn : 1.0;
+    u[3 * side] = e0 / den;
+    u[3 * side + 1] = e1 / den;
+    u[3 * side + 2] = e2 / den;
+    if (side)
+      tr = lt;
+    else
+      tl = lt;
   }
   lt64[s] = make_double2(tl, tr);
+  for (int k = 0; k < 6; ++k) ulink[6 * s + k] = u[k];
   rec[s].lt_hi_l = (uint32_t)((uint64_t)__double_as_longlong(tl) >> 32);
   rec[s].lt_hi_r = (uint32_t)((uint64_t)__double_as_longlong(tr) >> 32);
 }
 
 cudaError_t launch_link_times(const double4_32a* pos4, const int32_t* left, const int32_t* right, SiteRec* rec,
-                              double2* lt64, int64_t n, double v, cudaStream_t s) {
+                              double2* lt64, double* ulink, int64_t n, double v, cudaStream_t s) {
   int64_t nb = (n + 255) / 256;
-  if (nb) k_link_times<<<(unsigned)nb, 256, 0, s>>>(pos4, left, right, rec, lt64, n, v);
+  if (nb) k_link_times<<<(unsigned)nb, 256, 0, s>>>(pos4, left, right, rec, lt64, ulink, n, v);
   return cudaGetLastError();
 }
 

@@ -377,6 +377,29 @@ def test_work_order_and_graph_do_not_change_results():
         assert h == runs[0][2]
 
 
+def test_step_end_batching_does_not_change_results():
+    # the mixed kernel batches the ends of short steps across a warp when the previous run's steps
+    # averaged fewer than 64 hops: a long step (no batching next), short steps (batching off),
+    # short steps again (batching on), each against the plain FP64 kernel doing the same runs
+    films = [F.straight_tubes(60, 80.0, box_nm=(150, 150, 8), seed=12)]
+    tab = tables.forster_2d(1e15)
+    out = {}
+    for prec in (L.KMC_PREC_MIXED, L.KMC_PREC_FP64):
+        e = E.Engine(0)
+        e.load_films(films)
+        e.set_table(tab)
+        e.build(10e-9)
+        e.init_excitons([20000], [17], L.KMC_INJECT_REGION, n_sections=3)
+        for n, dt in ((1, 3e-13), (40, 1e-15), (40, 1e-15), (1, 3e-13)):
+            e.run(n, dt, 2e5, prec)
+        out[prec] = (e.excitons(), e.msd(0, 82), e.stats()["hops"])
+        e.close()
+    g, m, h = out[L.KMC_PREC_MIXED]
+    assert_states_equal(g, out[L.KMC_PREC_FP64][0])
+    assert_msd_close(m, out[L.KMC_PREC_FP64][1])
+    assert h == out[L.KMC_PREC_FP64][2] and h > 20000 * 100
+
+
 @pytest.mark.parametrize("table_kind", [2, 4])
 def test_random_geometry_csr_matches_oracle(table_kind):
     # sites at random points with random axes (each a one-site tube): pair distances and angles
