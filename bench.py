@@ -275,6 +275,7 @@ def contacts_arm(args, local, rank, world):
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     hops = e.stats()["hops"] - h0
+    l2_gbs = e.probe_l2(32 << 20, 200)
     e.close()
     dev_s_max, wall_max, hops_all = R.job_timing(dev_ms / 1e3, wall, hops)
     value = hops_all / dev_s_max
@@ -299,6 +300,17 @@ def contacts_arm(args, local, rank, world):
     peak, peak_kind = measured_peak()
     bph = bytes_per_hop(st["k_mean"])
     achieved = hops / (dev_ms / 1e3) * bph / 1e9
+    l2 = None
+    prof = os.path.join(ROOT, "profiles", "hop_mixed_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as fh:
+            pj = json.load(fh).get("cfg2")  # the same film
+        if pj and "lts_bytes_per_hop" in pj:
+            l2_ach = pj["lts_bytes_per_hop"] * hops / (dev_ms / 1e3) / 1e9
+            l2 = {"achieved": l2_ach, "peak": l2_gbs, "unit": "GB/s", "frac": l2_ach / l2_gbs,
+                  "bytes_per_hop": pj["lts_bytes_per_hop"],
+                  "peak_kind": "measured: kmc_probe_l2, 16-byte L2-only loads over a 32 MB buffer",
+                  "source": pj["source"] + " (the Green-Kubo launch on the same film)"}
     line = {
         "metric": CONTACTS_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": wall_max / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -309,7 +321,8 @@ def contacts_arm(args, local, rank, world):
                    "hops_timed": hops, "l2": "256 MB buffer written between timed steps"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind, "bytes_per_hop": bph,
-                     "note": "algorithmic bytes per hop x hops / device time of the whole contacts step"},
+                     "note": "algorithmic bytes per hop x hops / device time of the whole contacts step",
+                     "l2": l2},
         "gpu_launches": launches, "autotune": tune, "e2e": e2e, "clocks": clk.summary(),
     }
     if world == 1 and not args.no_cpu:
