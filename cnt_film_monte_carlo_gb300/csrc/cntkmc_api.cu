@@ -1282,10 +1282,32 @@ int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_
   a.msd = t_msd.p;
   a.msd_cap = trial_steps;
   a.n_trace = 0;
+  // one untimed trial measures the step length, so that the timed trials run the instantiation
+  // (short-step batching or not) that the runs will use
+  int rc = KMC_OK;
+  {
+    CK(c, copy_state(false));
+    CK(c, cudaMemcpyAsync(c->d_counters.p, counters, sizeof counters, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemsetAsync(t_msd.p, 0, t_msd.n * sizeof(double), c->stream));
+    float ms = 0;
+    int nl = 0;
+    rc = run_steps(c, a, trial_steps, 0, KMC_PREC_MIXED, c->mixed_variant, 1, &ms, &nl);
+    unsigned long long after[4];
+    CK(c, cudaMemcpy(after, c->d_counters.p, sizeof after, cudaMemcpyDeviceToHost));
+    int64_t live = 0;
+    for (int64_t ne : c->n_exc) live += ne;
+    if (c->contacts) {  // the slots' live count
+      std::vector<uint32_t> fl(ns);
+      CK(c, cudaMemcpy(fl.data(), c->d_e_flags.p, ns * 4, cudaMemcpyDeviceToHost));
+      live = 0;
+      for (uint32_t f : fl) live += (f & kmc::kExActive) ? 1 : 0;
+    }
+    if (rc == KMC_OK) note_step_length(c, (double)(after[0] - counters[0]), (double)live * trial_steps);
+    a.hold_short = c->short_steps ? 1 : 0;
+  }
   const int spl_options[3] = {1, 8, 32};
   double best = -1;
   int best_v = c->mixed_variant, best_spl = c->steps_per_launch;
-  int rc = KMC_OK;
   for (int variant = 0; variant < kmc::kMixedVariants && rc == KMC_OK; ++variant)
     for (int spl : spl_options) {
       if (spl > trial_steps && spl != 1) continue;
