@@ -939,15 +939,27 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
   }
   // create_particles (:274-316): slab i gets round(pop1 + i dp) excitons at its sites
   // [y1, y1 + dy), in site order
+  // the slab lists in one pass over the sites: a site can only be in the slab (y - ymin) / dy
+  // points at or in a neighbour of it (the rounded bounds can leave a site in two slabs or in
+  // none); each candidate is tested with the reference's bounds, in site order
+  std::vector<std::vector<int32_t>> seg_list((size_t)n_seg);
+  for (int64_t q = 0; q < n; ++q) {
+    const double y = y_of(q);
+    const double f = (y - ymin) / dy;
+    if (!(f > -2.0 && f < double(n_seg) + 2.0)) continue;
+    const int i0 = (int)std::floor(f);
+    for (int i = std::max(0, i0 - 1); i <= std::min(n_seg - 1, i0 + 1); ++i) {
+      const double y1 = ymin + double(i) * dy;
+      const double y2 = y1 + dy;
+      if (y1 <= y && y < y2) seg_list[(size_t)i].push_back(rank[q]);
+    }
+  }
   std::vector<int32_t> seg_sites;
   std::vector<int64_t> seg_off(1, 0), part_first(1, 0);
   const double dp = double(cfg->contact_pop[1] - cfg->contact_pop[0]) / (double(n_seg) - 1);
   for (int i = 0; i < n_seg; ++i) {
     const int n_particle = (int)std::round(double(cfg->contact_pop[0]) + double(i) * dp);
-    const double y1 = ymin + double(i) * dy;
-    const double y2 = y1 + dy;
-    for (int64_t q = 0; q < n; ++q)
-      if (y1 <= y_of(q) && y_of(q) < y2) seg_sites.push_back(rank[q]);
+    seg_sites.insert(seg_sites.end(), seg_list[(size_t)i].begin(), seg_list[(size_t)i].end());
     seg_off.push_back((int64_t)seg_sites.size());
     const int64_t np = std::max(n_particle, 0);
     if (np > 0 && seg_off[i + 1] == seg_off[i])
