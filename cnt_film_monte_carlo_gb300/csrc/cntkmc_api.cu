@@ -824,6 +824,8 @@ static int check_device_error(kmc_ctx* c, const char* who) {
   return KMC_OK;
 }
 
+constexpr int64_t kMaxGraphLaunches = 256;
+
 // Launch n_steps steps (step indices step0.. in a.msd) with the given shape; device time in *ms.
 // The launches (and the work-order rebuild before each mixed launch) are captured into a CUDA
 // graph; the graph of the previous run is updated in place when its topology matches.
@@ -838,7 +840,10 @@ static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0,
     if (e == cudaSuccess) e = enqueue_hops(c, a, n_steps, step0, precision, variant, spl, plan, &nl);
     return e;
   };
-  if (c->use_graph) {
+  // runs of many launches (a caller asking for 10^5 steps in one call) are launched directly:
+  // their graph would only add instantiation time
+  const bool graph = c->use_graph && (n_steps + spl - 1) / spl <= kMaxGraphLaunches;
+  if (graph) {
     rc = capture_graph(c, &c->gexec, enqueue);
     if (rc) return rc;
     CK(c, cudaEventRecord(c->ev0, c->stream));

@@ -400,6 +400,29 @@ def test_step_end_batching_does_not_change_results():
     assert h == out[L.KMC_PREC_FP64][2] and h > 20000 * 100
 
 
+def test_long_run_launched_directly_equals_graph_runs():
+    # a run of more than 256 launches is launched without a CUDA graph; the same steps as three
+    # graph-captured calls give the same state and MSD
+    films = [F.straight_tubes(30, 60.0, box_nm=(100, 100, 6), seed=21)]
+    tab = tables.forster_2d(1e15)
+    out = []
+    for chunks in ((300,), (100, 100, 100)):
+        e = E.Engine(0)
+        e.load_films(films)
+        e.set_table(tab)
+        e.build(10e-9)
+        e.set_launch_config(128, 1)
+        e.init_excitons([5000], [8], L.KMC_INJECT_UNIFORM)
+        for n in chunks:
+            e.run(n, 1e-15, 2e5, L.KMC_PREC_MIXED)
+        out.append((e.excitons(), e.msd(0, 300), e.stats()))
+        e.close()
+    assert out[0][2]["last_launches"] >= 300 and out[0][2]["steps_done"] == 300
+    assert_states_equal(out[0][0], out[1][0])
+    assert_msd_close(out[0][1], out[1][1])
+    assert out[0][2]["hops"] == out[1][2]["hops"]
+
+
 @pytest.mark.parametrize("table_kind", [2, 4])
 def test_random_geometry_csr_matches_oracle(table_kind):
     # sites at random points with random axes (each a one-site tube): pair distances and angles
