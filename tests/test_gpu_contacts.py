@@ -272,3 +272,44 @@ def test_contacts_at_scale_orders_and_precisions_agree():
         for k in ("site", "pos", "ff", "heading", "draws", "hops"):
             assert np.array_equal(x[k], x0[k]), k
         assert st["hops"] == st0["hops"]
+
+
+def test_contacts_argument_and_state_errors():
+    d = load_case(CONTACT_CASES[0])
+    c = contacts_inputs(d)
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, len(c["left"])], np.int64), c["pos"], c["orient"], c["left"], c["right"])
+    e.set_table(c["table"])
+    e.build(c["r_max"])
+    for args in ((1, (10, 0)), (5000, (10, 0)), (4, (-1, 0)), (4, (10, 1 << 40))):
+        with pytest.raises(L.KmcError) as ei:
+            e.contacts_init(args[0], args[1], 1, 0)
+        assert ei.value.code == L.KMC_ERR_ARG
+    with pytest.raises(L.KmcError) as ei:  # the contacts calls need the set-up first
+        e.contacts_run(1, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    assert ei.value.code == L.KMC_ERR_STATE
+    with pytest.raises(L.KmcError) as ei:
+        e.contacts_track(0, 1, c["dt"], c["v"], 10)
+    assert ei.value.code == L.KMC_ERR_STATE
+    e.contacts_init(4, (50, 10), 1, 0)
+    with pytest.raises(L.KmcError) as ei:  # Green-Kubo steps are refused on the contacts slots
+        e.run(1, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    assert ei.value.code == L.KMC_ERR_STATE
+    pop, _, live = e.contacts_run(2, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    assert live[-1] > 0
+    e.init_excitons(100, 3, L.KMC_INJECT_UNIFORM)  # back to Green-Kubo: contacts calls refused
+    e.run(1, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    with pytest.raises(L.KmcError) as ei:
+        e.contacts_run(1, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    assert ei.value.code == L.KMC_ERR_STATE
+    e.close()
+    # two films: contacts mode runs one
+    f2 = F.straight_tubes(10, 20.0, box_nm=(40, 40, 6), seed=2)
+    e = E.Engine(0)
+    e.load_films([f2, f2])
+    e.set_table(c["table"])
+    e.build(c["r_max"])
+    with pytest.raises(L.KmcError) as ei:
+        e.contacts_init(4, (10, 0), 1, 0)
+    assert ei.value.code == L.KMC_ERR_ARG
+    e.close()
