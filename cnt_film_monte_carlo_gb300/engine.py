@@ -26,6 +26,7 @@ class Engine:
         self._keep = []
         self.n_films = 0
         self.n_exc = None
+        self.n_segments = 2  # contacts mode: set by contacts_init
 
     def close(self):
         if getattr(self, "h", None):
