@@ -93,3 +93,33 @@ def test_python_class_writes_reference_msd(name, tmp_path):
     got = got[:len(t)]
     np.testing.assert_allclose(got[:, 0], t, rtol=1e-6)
     np.testing.assert_allclose(got[:, 1:], msd, rtol=1e-6, atol=1e-30)
+
+
+def test_driver_with_a_table_saved_by_the_reference(tmp_path):
+    # rate type "davoody" reads a table the reference saved (scattering_struct::save); the
+    # Förster table of the golden case, saved at full precision, gives the case's MSD file
+    from oracle import oracle as O
+    from test_tables import save_like_reference
+
+    name = "ref_forster_region"
+    d = load_case(name)
+    mc = d["config"]
+    tab = O.forster_table(1e15, mc["theta [degrees]"], mc["zshift [m]"], mc["axis shift 1 [m]"],
+                          mc["axis shift 2 [m]"])
+    tdir = os.path.join(str(tmp_path), "table")
+    os.makedirs(tdir)
+    save_like_reference(tab, tdir)
+    cfg = _input_json(d, str(tmp_path), "mixed")
+    with open(cfg) as f:
+        j = json.load(f)
+    j["exciton monte carlo"].update({"rate type": "davoody", "rate table directory": tdir})
+    with open(cfg, "w") as f:
+        json.dump(j, f)
+    B.build()
+    r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    got = _read_msd_file(os.path.join(str(tmp_path), "out"))
+    t, msd = _expected(d)
+    got = got[:len(t)]
+    np.testing.assert_allclose(got[:, 0], t, rtol=1e-6)
+    np.testing.assert_allclose(got[:, 1:], msd, rtol=1e-6, atol=1e-30)
