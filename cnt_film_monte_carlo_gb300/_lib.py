@@ -105,6 +105,7 @@ SIGNATURES = {
     "kmc_trim_sites": (C.c_int, [C.c_int64, PD, PD, PI32, PI32, PD, PI64]),
     "kmc_domain": (C.c_int, [C.c_int64, PD, PD, PD]),
     "kmc_forster_table": (C.c_int, [C.c_double, PD, PD, PD, PD, PD, PD, PD, PD, PD]),
+    "kmc_forster2d_table": (C.c_int, [C.c_double, PD, PD, PD, PD, PD]),
     "kmc_read_mesh": (C.c_int, [C.c_char_p, PI64, PI64, PD, PD, PI32, PI32]),
     "kmc_selftest_uniform": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, PU64]),
     "kmc_math_probe": (C.c_int, [C.c_void_p, PD, C.c_int64, PD, PD]),

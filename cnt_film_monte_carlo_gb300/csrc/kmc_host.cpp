@@ -117,6 +117,25 @@ int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]) {
   return KMC_OK;
 }
 
+int kmc_forster2d_table(double gamma_0, const double distance[3], const double theta_deg[3], double* dist,
+                        double* theta, double* rate) {
+  if (!distance || !theta_deg || !dist || !theta || !rate) return KMC_ERR_ARG;
+  const int64_t nd = (int64_t)distance[2], nt = (int64_t)theta_deg[2];
+  if (nd < 1 || nt < 1) return KMC_ERR_ARG;
+  linspace(distance[0], distance[1], nd, dist);
+  linspace(theta_deg[0], theta_deg[1], nt, theta);
+  const double scale = kRefPi / 180;
+  for (int64_t i = 0; i < nt; ++i) theta[i] = theta[i] * scale;
+  // the Förster formula of create_forster_scatt_table (monte_carlo.cpp:174-187) at zero axis
+  // shifts: gamma_0 cos^2(theta) (1 nm / d)^6
+  for (int64_t i = 0; i < nd; ++i)
+    for (int64_t k = 0; k < nt; ++k) {
+      const double c = std::cos(theta[k]);
+      rate[i * nt + k] = gamma_0 * (c * c) * std::pow(1.e-9 / dist[i], 6);
+    }
+  return KMC_OK;
+}
+
 int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
                       const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate) {
   if (!theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh || !a1 || !a2 || !rate) return KMC_ERR_ARG;

@@ -387,15 +387,27 @@ class monte_carlo {
       return;
     }
     if (rt == "forster2d") {
-      grids_ = {j_.has("distance [m]") ? lin(j_["distance [m]"]) : lin3(0.5e-9, 10e-9, 96),
-                j_.has("theta 2d [degrees]") ? lin(j_["theta 2d [degrees]"]) : lin3(0, 90, 91)};
-      for (auto& t : grids_[1]) t = t * (3.141592 / 180);
-      rates_.resize(grids_[0].size() * grids_[1].size());
-      for (size_t i = 0; i < grids_[0].size(); ++i)
-        for (size_t k = 0; k < grids_[1].size(); ++k) {
-          double c = std::cos(grids_[1][k]);
-          rates_[i * grids_[1].size() + k] = 1.e15 * (c * c) * std::pow(1.e-9 / grids_[0][i], 6);
+      auto g3 = [&](const char* key, double a, double b, double n, double* out) {
+        if (j_.has(key)) {
+          const jl::Value& g = j_[key];
+          a = g[0].as_double();
+          b = g[1].as_double();
+          n = g[2].as_double();
         }
+        out[0] = a;
+        out[1] = b;
+        out[2] = n;
+      };
+      double gd[3], gt[3];
+      g3("distance [m]", 0.5e-9, 10e-9, 96, gd);
+      g3("theta 2d [degrees]", 0, 90, 91, gt);
+      if (!(gd[2] >= 1 && gt[2] >= 1)) throw std::invalid_argument("bad rate-table grids");
+      grids_.assign(2, {});
+      grids_[0].resize((size_t)gd[2]);
+      grids_[1].resize((size_t)gt[2]);
+      rates_.resize(grids_[0].size() * grids_[1].size());
+      if (kmc_forster2d_table(1.e15, gd, gt, grids_[0].data(), grids_[1].data(), rates_.data()) != KMC_OK)
+        throw std::invalid_argument("bad rate-table grids");
       table_kind_ = KMC_TABLE_2D;
       return;
     }

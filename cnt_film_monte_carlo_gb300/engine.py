@@ -250,6 +250,20 @@ def trim_sites(pos_m, orient, left, right, lim):
     return pos[:n].copy(), ori[:n].copy(), lk[:n].copy(), rk[:n].copy()
 
 
+def forster2d_table(gamma_0, distance_m, theta_deg) -> dict:
+    """The 2-D (distance, folded angle) Förster-form table, built by the library."""
+    lib = L.load()
+    dd, th = _f64(distance_m), _f64(theta_deg)
+    nd, nt = int(dd[2]), int(th[2])
+    g = [np.zeros(nd), np.zeros(nt)]
+    rate = np.zeros((nd, nt))
+    rc = lib.kmc_forster2d_table(float(gamma_0), L.ptr(dd, C.c_double), L.ptr(th, C.c_double), L.ptr(g[0], C.c_double),
+                                 L.ptr(g[1], C.c_double), L.ptr(rate, C.c_double))
+    if rc != L.KMC_OK:
+        raise L.KmcError(rc, "kmc_forster2d_table failed")
+    return {"kind": 2, "grids": g, "rate": rate}
+
+
 def forster_table(gamma_0, theta_deg, zshift, ash1, ash2) -> dict:
     """The reference's Förster table on its 4-D grid (monte_carlo.cpp:156-200)."""
     lib = L.load()

@@ -41,10 +41,11 @@ def forster_4d(gamma_0, theta_deg, zshift, ash1, ash2) -> dict:
 
 
 def forster_2d(gamma_0: float = FORSTER_GAMMA, distance_m=(0.5e-9, 10e-9, 96), theta_deg=(0.0, 90.0, 91)) -> dict:
-    d = linspace(*distance_m)
-    th = linspace(*theta_deg) * (REF_PI / 180)
-    rate = gamma_0 * (np.cos(th)[None, :] ** 2) * (1.0e-9 / d[:, None]) ** 6
-    return {"kind": 2, "grids": [d, th], "rate": np.ascontiguousarray(rate)}
+    """Built by the library (kmc_forster2d_table), so that the C++ and Python drivers use the
+    same table bit for bit."""
+    from .engine import forster2d_table
+
+    return forster2d_table(gamma_0, distance_m, theta_deg)
 
 
 def read_reference_table(directory: str) -> dict:

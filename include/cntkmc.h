@@ -217,6 +217,14 @@ int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_
 /* Domain of a site set (find_simulation_domain, monte_carlo.h:328-340): mn[3], mx[3]. */
 int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]);
 
+/* The 2-D (centre distance, folded angle) Förster-form table of the benchmark films (no counterpart
+ * in the reference, which tabulates 4-D): the formula of create_forster_scatt_table
+ * (monte_carlo.cpp:174-187) at zero axis shifts, gamma_0 cos^2(theta) (1 nm / d)^6, on
+ * arma::linspace grids {start, end, n} (distance in m, theta in degrees scaled by 3.141592/180).
+ * Outputs: dist[nd], theta[nt], rate[nd][nt].  The C++ and Python drivers both use it. */
+int kmc_forster2d_table(double gamma_0, const double distance[3], const double theta_deg[3], double* dist,
+                        double* theta, double* rate);
+
 /* create_forster_scatt_table (monte_carlo.cpp:156-200) on arma::linspace grids {start, end, n};
  * the theta grid is in degrees and scaled by pi/180 with pi = 3.141592 (helper/constants.h:10).
  * Outputs: grids theta[nt], zsh[nz], ash1[n1], ash2[n2]; rate[nt][nz][n1][n2]. */

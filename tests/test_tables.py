@@ -42,3 +42,15 @@ def test_saved_table_at_stream_precision(tmp_path):
     t = tables.read_reference_table(str(tmp_path))
     np.testing.assert_allclose(t["rate"], tab["rate"], rtol=5e-6)
     np.testing.assert_allclose(t["grids"][0], tab["grids"][0], rtol=1e-4)
+
+
+def test_forster_2d_table_is_the_formula():
+    # gamma_0 cos^2(theta) (1 nm / d)^6 on the 2-D grids, built by the library for both drivers
+    t = tables.forster_2d(1e15, (0.5e-9, 10e-9, 96), (0.0, 90.0, 91))
+    d, th = t["grids"]
+    assert t["kind"] == 2 and t["rate"].shape == (96, 91)
+    assert np.array_equal(d, tables.linspace(0.5e-9, 10e-9, 96))
+    assert np.array_equal(th, tables.linspace(0.0, 90.0, 91) * (tables.REF_PI / 180))
+    want = 1e15 * np.cos(th)[None, :] ** 2 * (1e-9 / d[:, None]) ** 6
+    np.testing.assert_allclose(t["rate"], want, rtol=1e-14, atol=1e-300)
+    assert t["rate"][0, 0] == 1e15 * (1e-9 / 0.5e-9) ** 6
