@@ -1,7 +1,9 @@
 // json_lite.hpp -- a small JSON reader/writer for the drop-in driver's input.json.
-// Supports objects, arrays, numbers, strings (with \" \\ \/ \b \f \n \r \t \uXXXX escapes for
-// ASCII), true/false/null.  Object key order is kept for writing the file back.
+// Supports objects, arrays, numbers, strings (with \" \\ \/ \b \f \n \r \t \uXXXX escapes, the
+// last decoded to UTF-8), true/false/null.  Object key order is kept for writing the file back;
+// strings are written with quote, backslash and control characters escaped.
 #pragma once
+#include <cstdint>
 #include <cstdlib>
 #include <map>
 #include <memory>
@@ -123,6 +125,41 @@ class Parser {
     }
     return v;
   }
+  uint32_t hex4() {
+    if (i_ + 4 > s_.size()) fail("bad \\u escape");
+    uint32_t v = 0;
+    for (int k = 0; k < 4; ++k) {
+      const char h = s_[i_ + k];
+      v <<= 4;
+      if (h >= '0' && h <= '9')
+        v |= (uint32_t)(h - '0');
+      else if (h >= 'a' && h <= 'f')
+        v |= (uint32_t)(h - 'a' + 10);
+      else if (h >= 'A' && h <= 'F')
+        v |= (uint32_t)(h - 'A' + 10);
+      else
+        fail("bad \\u escape");
+    }
+    i_ += 4;
+    return v;
+  }
+  static void utf8(std::string& out, uint32_t cp) {
+    if (cp < 0x80) {
+      out += (char)cp;
+    } else if (cp < 0x800) {
+      out += (char)(0xC0 | (cp >> 6));
+      out += (char)(0x80 | (cp & 0x3F));
+    } else if (cp < 0x10000) {
+      out += (char)(0xE0 | (cp >> 12));
+      out += (char)(0x80 | ((cp >> 6) & 0x3F));
+      out += (char)(0x80 | (cp & 0x3F));
+    } else {
+      out += (char)(0xF0 | (cp >> 18));
+      out += (char)(0x80 | ((cp >> 12) & 0x3F));
+      out += (char)(0x80 | ((cp >> 6) & 0x3F));
+      out += (char)(0x80 | (cp & 0x3F));
+    }
+  }
   std::string string() {
     if (i_ >= s_.size() || s_[i_] != '"') fail("string expected");
     ++i_;
@@ -139,9 +176,14 @@ class Parser {
           case 'b': out += '\b'; break;
           case 'f': out += '\f'; break;
           case 'u': {
-            if (i_ + 4 > s_.size()) fail("bad \\u escape");
-            out += (char)std::strtol(s_.substr(i_, 4).c_str(), nullptr, 16);
-            i_ += 4;
+            uint32_t cp = hex4();
+            if (cp >= 0xD800 && cp < 0xDC00 && s_.compare(i_, 2, "\\u") == 0) {  // surrogate pair
+              i_ += 2;
+              const uint32_t lo = hex4();
+              if (lo < 0xDC00 || lo >= 0xE000) fail("bad surrogate pair");
+              cp = 0x10000 + ((cp - 0xD800) << 10) + (lo - 0xDC00);
+            }
+            utf8(out, cp);
             break;
           }
           default: out += e;
@@ -158,6 +200,30 @@ class Parser {
 
 inline Value parse(const std::string& text) { return Parser(text).parse(); }
 
+// a string as a JSON literal: quote, backslash and control characters escaped
+inline void write_string(std::ostream& o, const std::string& s) {
+  o << '"';
+  for (unsigned char c : s) {
+    switch (c) {
+      case '"': o << "\\\""; break;
+      case '\\': o << "\\\\"; break;
+      case '\n': o << "\\n"; break;
+      case '\t': o << "\\t"; break;
+      case '\r': o << "\\r"; break;
+      case '\b': o << "\\b"; break;
+      case '\f': o << "\\f"; break;
+      default:
+        if (c < 0x20) {
+          static const char hex[] = "0123456789abcdef";
+          o << "\\u00" << hex[c >> 4] << hex[c & 15];
+        } else {
+          o << (char)c;
+        }
+    }
+  }
+  o << '"';
+}
+
 inline void write(std::ostream& o, const Value& v, int indent = 0) {
   std::string pad(indent, ' '), pad2(indent + 4, ' ');
   switch (v.kind) {
@@ -170,7 +236,7 @@ inline void write(std::ostream& o, const Value& v, int indent = 0) {
       o << t.str();
       break;
     }
-    case Value::String: o << '"' << v.str << '"'; break;
+    case Value::String: write_string(o, v.str); break;
     case Value::Array:
       o << "[";
       for (size_t i = 0; i < v.arr.size(); ++i) {
@@ -182,7 +248,9 @@ inline void write(std::ostream& o, const Value& v, int indent = 0) {
     case Value::Object:
       o << "{\n";
       for (size_t i = 0; i < v.obj.size(); ++i) {
-        o << pad2 << '"' << v.obj[i].first << "\": ";
+        o << pad2;
+        write_string(o, v.obj[i].first);
+        o << ": ";
         write(o, v.obj[i].second, indent + 4);
         o << (i + 1 < v.obj.size() ? ",\n" : "\n");
       }

@@ -1,0 +1,83 @@
+"""The drop-in driver's JSON reader/writer (csrc/json_lite.hpp) against Python's json.
+
+The driver reads the reference's input.json (main.cpp:32-54 reads it with nlohmann::json) and
+writes the properties back beside its outputs (save_json_properties, monte_carlo.h:319-324).  A small
+helper compiled with g++ parses a file and writes it back; Python's json must read the same
+value out of the result, and malformed files must be refused.
+"""
+import json
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+REPO = Path(__file__).resolve().parents[1]
+
+GOOD = [
+    {"mode": "contacts", "number of segments": 5, "temperature [kelvin]": 300.0},
+    {"a": [1, -2, 3.5, 1e-9, 6.02214076e23, -0.0], "b": {"c": {"d": []}, "e": {}}},
+    {"flags": [True, False, None], "empty": "", "nested": [[[]], [{}]]},
+    {'quote " and backslash \\': 'path\\to\\"file"', "tab\tnew\nline": "\r\b\f\x01\x1f"},
+    {"unicode": "é中\U0001f600", "slash": "a/b"},
+    [0.1, 0.2, 0.30000000000000004, 2.2250738585072014e-308, 1.7976931348623157e308],
+    "just a string",
+    42,
+]
+
+BAD = [
+    "",
+    "{",
+    '{"a": }',
+    '{"a" 1}',
+    "[1, 2",
+    '"unterminated',
+    '{"a": 1} x',
+    '"\\u12"',
+    '"\\ud83d\\u0041"',
+    "nul",
+]
+
+
+@pytest.fixture(scope="module")
+def roundtrip(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path_factory.mktemp("jl") / "json_roundtrip"
+    subprocess.run(
+        ["g++", "-std=c++17", "-O1", "-I", str(REPO / "cnt_film_monte_carlo_gb300" / "csrc"),
+         str(REPO / "tests" / "json_roundtrip.cpp"), "-o", str(exe)],
+        check=True)
+    return exe
+
+
+def run(exe, tmp_path, text):
+    p = tmp_path / "in.json"
+    p.write_bytes(text.encode("utf-8"))
+    return subprocess.run([str(exe), str(p)], capture_output=True)
+
+
+@pytest.mark.parametrize("value", GOOD, ids=range(len(GOOD)))
+def test_round_trip(roundtrip, tmp_path, value):
+    for text in (json.dumps(value), json.dumps(value, indent=2, ensure_ascii=False)):
+        r = run(roundtrip, tmp_path, text)
+        assert r.returncode == 0, r.stderr
+        back = json.loads(r.stdout.decode("utf-8"))
+        assert back == value
+        # a second pass is a fixed point of the writer
+        r2 = run(roundtrip, tmp_path, r.stdout.decode("utf-8"))
+        assert r2.returncode == 0 and r2.stdout == r.stdout
+
+
+def test_numbers_exact(roundtrip, tmp_path):
+    vals = [1.0 / 3.0, 1e-300, 123456789.123456789, 5e-324, -2.5e-12]
+    r = run(roundtrip, tmp_path, json.dumps(vals))
+    assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout) == vals
+
+
+@pytest.mark.parametrize("text", BAD, ids=range(len(BAD)))
+def test_malformed_refused(roundtrip, tmp_path, text):
+    r = run(roundtrip, tmp_path, text)
+    assert r.returncode == 2, (text, r.stdout, r.stderr)
+    assert b"json:" in r.stderr
