@@ -24,6 +24,9 @@ KMC_ERR_NO_DEVICE = -7
 KMC_ERR_CAPACITY = -8
 KMC_TABLE_4D = 4
 KMC_TABLE_2D = 2
+KMC_TABLE_2D_SPECIES = 3
+KMC_MAX_SPECIES = 8
+KMC_MLP_HIDDEN = 64
 KMC_INJECT_REGION = 0
 KMC_INJECT_UNIFORM = 1
 KMC_PREC_FP64 = 0
@@ -38,6 +41,11 @@ PD = C.POINTER(C.c_double)
 PI32 = C.POINTER(C.c_int32)
 PI64 = C.POINTER(C.c_int64)
 PU64 = C.POINTER(C.c_uint64)
+PF32 = C.POINTER(C.c_float)
+
+
+def KMC_MLP_PARAMS(n_species: int) -> int:
+    return 4548 + 2 * n_species * n_species
 
 
 class kmc_film(C.Structure):
@@ -75,6 +83,26 @@ class kmc_contacts(C.Structure):
 class kmc_contacts_info(C.Structure):
     _fields_ = [("ymin", C.c_double), ("ymax", C.c_double), ("dy", C.c_double), ("n_initial", C.c_int64),
                 ("n_contact", C.c_int64 * 2), ("capacity", C.c_int64)]
+
+
+class kmc_mlp_shape(C.Structure):
+    _fields_ = [("n_species", C.c_int32), ("d_min", C.c_double), ("d_max", C.c_double), ("log_mean", C.c_double),
+                ("log_scale", C.c_double)]
+
+
+class kmc_species_model(C.Structure):
+    _fields_ = [("n_species", C.c_int32), ("gamma_0", C.c_double), ("energy", PD), ("diameter", PD),
+                ("diameter_ref", C.c_double), ("width", C.c_double), ("kT", C.c_double), ("floor", C.c_double),
+                ("near_field", C.c_double)]
+
+
+class kmc_mlp_train_cfg(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double), ("lr_final", C.c_double),
+                ("beta1", C.c_double), ("beta2", C.c_double), ("eps", C.c_double)]
+
+
+class kmc_mlp_train_stats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("first_loss", C.c_double), ("last_loss", C.c_double), ("seconds", C.c_double)]
 
 
 # every symbol include/cntkmc.h declares, with (restype, argtypes)
@@ -118,6 +146,16 @@ SIGNATURES = {
     "kmc_autotune": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int64, C.c_void_p]),
     "kmc_build_neighbors_noalloc": (C.c_int, [PD, PD, C.c_int64, C.POINTER(kmc_table), C.c_double, PI64, PI32, PD, PD,
                                               C.c_int64, PI64, C.c_void_p, C.c_char_p, C.c_int64]),
+    "kmc_set_site_species": (C.c_int, [C.c_void_p, PI32, C.c_int32]),
+    "kmc_species_rates": (C.c_int, [C.POINTER(kmc_species_model), C.c_int64, PD, PD, PI32, PI32, PD]),
+    "kmc_mlp_init": (C.c_int, [C.c_void_p, C.POINTER(kmc_mlp_shape), C.c_uint64]),
+    "kmc_mlp_set_params": (C.c_int, [C.c_void_p, PF32, C.c_int64]),
+    "kmc_mlp_get_params": (C.c_int, [C.c_void_p, PF32, C.c_int64]),
+    "kmc_mlp_set_samples": (C.c_int, [C.c_void_p, C.c_int64, PD, PD, PI32, PD]),
+    "kmc_mlp_gradient": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, PF32, PD]),
+    "kmc_mlp_train": (C.c_int, [C.c_void_p, C.POINTER(kmc_mlp_train_cfg), C.POINTER(kmc_mlp_train_stats)]),
+    "kmc_mlp_predict": (C.c_int, [C.c_void_p, C.c_int64, PD, PD, PI32, PD]),
+    "kmc_mlp_rate_table": (C.c_int, [C.c_void_p, C.c_int32, PD, C.c_int32, PD, PD]),
     "kmc_version": (C.c_char_p, []),
 }
 

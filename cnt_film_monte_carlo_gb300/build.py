@@ -24,7 +24,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-
 CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-Wall", f"-I{INCLUDE}",
              f"-I{CSRC}"]
 
-CU_SOURCES = ["kmc_kernels.cu", "kmc_mixed_small.cu", "kmc_mixed_large.cu", "cntkmc_api.cu", "kmc_noalloc.cu", "kmc_contacts.cu"]
+CU_SOURCES = ["kmc_kernels.cu", "kmc_mixed_small.cu", "kmc_mixed_large.cu", "cntkmc_api.cu", "kmc_noalloc.cu", "kmc_contacts.cu",
+              "kmc_mlp.cu"]
 CXX_SOURCES = ["kmc_host.cpp"]
 DRIVER_SOURCES = ["driver.cpp"]
 

@@ -87,6 +87,18 @@ struct kmc_ctx {
   bool has_table = false;
   kmc::TableDev table{};
   DevBuf<double> d_grid[4], d_rate;
+  // chirality of each site (read by KMC_TABLE_2D_SPECIES tables); 0 = not set
+  int32_t n_species = 0;
+  DevBuf<int32_t> d_species;
+  // learned pair-rate surrogate
+  bool mlp_ready = false;
+  kmc_mlp_shape mlp_shape{};
+  int32_t mlp_np = 0;
+  int64_t mlp_adam_t = 0, mlp_n_samples = 0;
+  DevBuf<float> d_mlp_master, d_mlp_m1, d_mlp_m2, d_mlp_part, d_mlp_grad;
+  DevBuf<uint16_t> d_mlp_wbf;
+  DevBuf<double> d_mlp_ploss, d_mlp_loss;
+  DevBuf<float4> d_mlp_samples;
   // neighbours
   bool built = false;
   double r_max = 0;
@@ -312,6 +324,24 @@ int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
   CK(c, upload(c->d_site_film, sf.data(), n, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   c->film_loaded = true;
+  c->n_species = 0;
+  c->built = false;
+  c->inited = false;
+  return KMC_OK;
+}
+
+int kmc_set_site_species(kmc_ctx* c, const int32_t* species, int32_t n_species) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->film_loaded) FAIL(c, KMC_ERR_STATE, "kmc_set_site_species: load a film first");
+  if (!species || n_species < 1 || n_species > KMC_MAX_SPECIES)
+    FAIL(c, KMC_ERR_ARG, "kmc_set_site_species: need species[n_sites] and 1 <= n_species <= %d", KMC_MAX_SPECIES);
+  for (int64_t i = 0; i < c->n_sites; ++i)
+    if (species[i] < 0 || species[i] >= n_species)
+      FAIL(c, KMC_ERR_ARG, "kmc_set_site_species: site %lld has species %d", (long long)i, species[i]);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, upload(c->d_species, species, (size_t)c->n_sites, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->n_species = n_species;
   c->built = false;
   c->inited = false;
   return KMC_OK;
@@ -319,11 +349,13 @@ int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
 
 int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   if (!c) return KMC_ERR_ARG;
-  if (!t || (t->kind != KMC_TABLE_4D && t->kind != KMC_TABLE_2D) || !t->rate)
-    FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: kind must be 4 or 2");
+  if (!t || (t->kind != KMC_TABLE_4D && t->kind != KMC_TABLE_2D && t->kind != KMC_TABLE_2D_SPECIES) || !t->rate)
+    FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: kind must be 4, 2 or 3");
+  if (t->kind == KMC_TABLE_2D_SPECIES && (t->n[2] < 1 || t->n[2] > KMC_MAX_SPECIES))
+    FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: species table needs 1 <= n[2] <= %d", KMC_MAX_SPECIES);
   CK(c, cudaSetDevice(c->device));
   int dims = t->kind == KMC_TABLE_4D ? 4 : 2;
-  int64_t nr = 1;
+  int64_t nr = t->kind == KMC_TABLE_2D_SPECIES ? (int64_t)t->n[2] * t->n[2] : 1;
   c->table = kmc::TableDev{};
   c->table.kind = t->kind;
   for (int d = 0; d < dims; ++d) {
@@ -338,6 +370,7 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
     double span = t->grid[d][t->n[d] - 1] - t->grid[d][0];
     c->table.inv_h[d] = (asc && span > 0) ? (double)(t->n[d] - 1) / span : 0.0;
   }
+  if (t->kind == KMC_TABLE_2D_SPECIES) c->table.n[2] = t->n[2];
   CK(c, upload(c->d_rate, t->rate, nr, c->stream));
   c->table.rate = c->d_rate.p;
   CK(c, cudaStreamSynchronize(c->stream));
@@ -376,6 +409,9 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   if (!c) return KMC_ERR_ARG;
   if (!c->film_loaded || !c->has_table) FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: load a film and a rate table first");
   if (!(r_max > 0)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: radius must be positive");
+  if (c->table.kind == KMC_TABLE_2D_SPECIES && c->n_species != c->table.n[2])
+    FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: the species table has %d chiralities, the sites %d", c->table.n[2],
+         c->n_species);
   CK(c, cudaSetDevice(c->device));
   const int64_t n = c->n_sites;
   // cell grids, monte_carlo.h:375-387: n_d = ceil((max - min) / r) + 1
@@ -442,6 +478,7 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   a.cell_members = c->d_cell_members.p;
   a.n_cells = ncell;
   a.table = c->table;
+  a.table.species = c->table.kind == KMC_TABLE_2D_SPECIES ? c->d_species.p : nullptr;
   a.r_max = r_max;
   a.counts = c->d_rowptr.p;
   a.rowptr = c->d_rowptr.p;
@@ -1551,6 +1588,243 @@ int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, doub
   dx.release();
   dl.release();
   da.release();
+  return KMC_OK;
+}
+
+// ---- learned pair-rate surrogate ----
+
+static kmc::MlpDev mlp_dev(const kmc_ctx* c) {
+  kmc::MlpDev m{};
+  m.n_species = c->mlp_shape.n_species;
+  m.n_params = c->mlp_np;
+  m.d_min = c->mlp_shape.d_min;
+  m.inv_span = 2.0 / std::log(c->mlp_shape.d_max / c->mlp_shape.d_min);
+  m.log_mean = c->mlp_shape.log_mean;
+  m.log_scale = c->mlp_shape.log_scale;
+  m.master = c->d_mlp_master.p;
+  m.wbf = c->d_mlp_wbf.p;
+  return m;
+}
+
+// SplitMix64 (Steele, Lea & Flood, "Fast splittable pseudorandom number generators", 2014)
+static uint64_t splitmix64(uint64_t& x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// master parameters from the host, BF16 copies, Adam moments cleared
+static int mlp_upload_params(kmc_ctx* c, const float* params) {
+  const size_t np = (size_t)c->mlp_np;
+  CK(c, cudaMemcpyAsync(c->d_mlp_master.p, params, np * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemsetAsync(c->d_mlp_m1.p, 0, np * sizeof(float), c->stream));
+  CK(c, cudaMemsetAsync(c->d_mlp_m2.p, 0, np * sizeof(float), c->stream));
+  CK(c, kmc::launch_mlp_bf16(c->d_mlp_master.p, c->d_mlp_wbf.p, c->mlp_np, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->mlp_adam_t = 0;
+  c->mlp_ready = true;
+  return KMC_OK;
+}
+
+// gradient-kernel grid: one block per SM at most, no more blocks than 128-sample chunks
+static int mlp_grid(const kmc_ctx* c, int64_t count) {
+  const int64_t chunks = (count + kmc::kMlpChunk - 1) / kmc::kMlpChunk;
+  return (int)std::min<int64_t>(chunks, c->n_sms);
+}
+
+int kmc_mlp_init(kmc_ctx* c, const kmc_mlp_shape* sh, uint64_t seed) {
+  if (!c) return KMC_ERR_ARG;
+  if (!sh || sh->n_species < 1 || sh->n_species > KMC_MAX_SPECIES || !(sh->d_min > 0) || !(sh->d_max > sh->d_min) ||
+      !(sh->log_scale > 0) || !std::isfinite(sh->log_mean) || !std::isfinite(sh->d_max) || !std::isfinite(sh->log_scale))
+    FAIL(c, KMC_ERR_ARG, "kmc_mlp_init: need 1 <= n_species <= %d, 0 < d_min < d_max, log_scale > 0", KMC_MAX_SPECIES);
+  CK(c, cudaSetDevice(c->device));
+  const int32_t np = KMC_MLP_PARAMS(sh->n_species);
+  c->mlp_ready = false;
+  c->mlp_n_samples = 0;
+  CK(c, c->d_mlp_master.alloc(np));
+  CK(c, c->d_mlp_m1.alloc(np));
+  CK(c, c->d_mlp_m2.alloc(np));
+  CK(c, c->d_mlp_grad.alloc(np));
+  CK(c, c->d_mlp_wbf.alloc(np));
+  CK(c, c->d_mlp_part.alloc((size_t)c->n_sms * np));
+  // partial entries no thread owns (the padding after b3) stay zero
+  CK(c, cudaMemsetAsync(c->d_mlp_part.p, 0, (size_t)c->n_sms * np * sizeof(float), c->stream));
+  CK(c, c->d_mlp_ploss.alloc(c->n_sms));
+  CK(c, c->d_mlp_loss.alloc(2));
+  c->mlp_shape = *sh;
+  c->mlp_np = np;
+  std::vector<float> p(np, 0.f);
+  uint64_t x = seed;
+  auto uni = [&](double bound) { return (float)(bound * (2.0 * std::ldexp((double)(splitmix64(x) >> 11), -53) - 1.0)); };
+  for (int i = kmc::kMlpOffW1; i < kmc::kMlpOffW2; ++i) p[i] = uni(0.5);    // W1, b1: fan-in 4
+  for (int i = kmc::kMlpOffW2; i < kmc::kMlpOffB3; ++i) p[i] = uni(0.125);  // W2, b2, W3: fan-in 64
+  for (int i = kmc::kMlpOffE; i < np; ++i) p[i] = uni(1.0);                 // embedding
+  return mlp_upload_params(c, p.data());
+}
+
+int kmc_mlp_set_params(kmc_ctx* c, const float* params, int64_t n) {
+  if (!c) return KMC_ERR_ARG;
+  if (c->mlp_np == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_set_params: call kmc_mlp_init first");
+  if (!params || n != c->mlp_np) FAIL(c, KMC_ERR_ARG, "kmc_mlp_set_params: need %d parameters", c->mlp_np);
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(params[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_set_params: parameter %lld is not finite", (long long)i);
+  CK(c, cudaSetDevice(c->device));
+  return mlp_upload_params(c, params);
+}
+
+int kmc_mlp_get_params(kmc_ctx* c, float* params, int64_t n) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_get_params: call kmc_mlp_init first");
+  if (!params || n != c->mlp_np) FAIL(c, KMC_ERR_ARG, "kmc_mlp_get_params: need room for %d parameters", c->mlp_np);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpyAsync(params, c->d_mlp_master.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return KMC_OK;
+}
+
+// checks the pair inputs shared by set_samples and predict
+static int mlp_check_pairs(kmc_ctx* c, const char* who, int64_t n, const double* dist, const double* theta,
+                           const int32_t* pair) {
+  const int32_t np2 = c->mlp_shape.n_species * c->mlp_shape.n_species;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!(dist[i] > 0) || !std::isfinite(dist[i]) || !std::isfinite(theta[i]))
+      FAIL(c, KMC_ERR_ARG, "%s: sample %lld has distance %g, angle %g", who, (long long)i, dist[i], theta[i]);
+    if (pair[i] < 0 || pair[i] >= np2) FAIL(c, KMC_ERR_ARG, "%s: sample %lld has pair %d", who, (long long)i, pair[i]);
+  }
+  return KMC_OK;
+}
+
+int kmc_mlp_set_samples(kmc_ctx* c, int64_t n, const double* dist, const double* theta, const int32_t* pair,
+                        const double* log_rate) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_set_samples: call kmc_mlp_init first");
+  if (n < 1 || n > (1LL << 31) || !dist || !theta || !pair || !log_rate)
+    FAIL(c, KMC_ERR_ARG, "kmc_mlp_set_samples: need 1 <= n <= 2^31 and four arrays");
+  if (int rc = mlp_check_pairs(c, "kmc_mlp_set_samples", n, dist, theta, pair)) return rc;
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(log_rate[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_set_samples: label %lld is not finite", (long long)i);
+  CK(c, cudaSetDevice(c->device));
+  DevBuf<double> dd, dt, dl;
+  DevBuf<int32_t> dp;
+  CK(c, upload(dd, dist, n, c->stream));
+  CK(c, upload(dt, theta, n, c->stream));
+  CK(c, upload(dp, pair, n, c->stream));
+  CK(c, upload(dl, log_rate, n, c->stream));
+  CK(c, c->d_mlp_samples.alloc(n));
+  CK(c, kmc::launch_mlp_samples(mlp_dev(c), dd.p, dt.p, dp.p, dl.p, n, c->d_mlp_samples.p, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->mlp_n_samples = n;
+  return KMC_OK;
+}
+
+int kmc_mlp_gradient(kmc_ctx* c, int64_t first, int64_t count, float* grad, double* loss) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->mlp_ready || c->mlp_n_samples == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_gradient: set parameters and samples first");
+  if (first < 0 || count < 1 || first + count > c->mlp_n_samples || !grad)
+    FAIL(c, KMC_ERR_ARG, "kmc_mlp_gradient: samples [%lld, +%lld) outside [0, %lld)", (long long)first, (long long)count,
+         (long long)c->mlp_n_samples);
+  CK(c, cudaSetDevice(c->device));
+  const kmc::MlpDev m = mlp_dev(c);
+  const int grid = mlp_grid(c, count);
+  kmc::MlpStep st{};
+  st.inv_count = 1.0 / (double)count;
+  CK(c, kmc::launch_mlp_grad(m, c->d_mlp_samples.p, first, count, c->d_mlp_part.p, c->d_mlp_ploss.p, grid, c->stream));
+  CK(c, kmc::launch_mlp_update(m, c->d_mlp_master.p, c->d_mlp_wbf.p, c->d_mlp_m1.p, c->d_mlp_m2.p, c->d_mlp_part.p,
+                               c->d_mlp_ploss.p, grid, st, c->d_mlp_grad.p, c->d_mlp_loss.p, c->stream));
+  CK(c, cudaMemcpyAsync(grad, c->d_mlp_grad.p, c->mlp_np * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  double l = 0;
+  CK(c, cudaMemcpyAsync(&l, c->d_mlp_loss.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (loss) *loss = l;
+  return KMC_OK;
+}
+
+int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats* stats) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->mlp_ready || c->mlp_n_samples == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_train: set parameters and samples first");
+  if (!cfg || cfg->epochs < 1 || cfg->batch < kmc::kMlpChunk || cfg->batch % kmc::kMlpChunk || cfg->batch > c->mlp_n_samples ||
+      !(cfg->lr > 0) || !(cfg->lr_final >= 0) || !(cfg->beta1 >= 0 && cfg->beta1 < 1) || !(cfg->beta2 >= 0 && cfg->beta2 < 1) ||
+      !(cfg->eps > 0))
+    FAIL(c, KMC_ERR_ARG, "kmc_mlp_train: need epochs >= 1, batch a multiple of 128 within the samples, lr > 0, "
+                         "lr_final >= 0, betas in [0, 1), eps > 0");
+  CK(c, cudaSetDevice(c->device));
+  const kmc::MlpDev m = mlp_dev(c);
+  const int64_t per_epoch = c->mlp_n_samples / cfg->batch;
+  const int64_t total = per_epoch * cfg->epochs;
+  const int grid = mlp_grid(c, cfg->batch);
+  CK(c, cudaEventRecord(c->ev0, c->stream));
+  for (int64_t k = 0; k < total; ++k) {
+    const int64_t t = ++c->mlp_adam_t;
+    kmc::MlpStep st{};
+    const double cosine = 0.5 * (1.0 + std::cos(3.141592653589793 * (double)k / (double)total));
+    st.lr = (float)(cfg->lr_final + (cfg->lr - cfg->lr_final) * cosine);
+    st.beta1 = (float)cfg->beta1;
+    st.beta2 = (float)cfg->beta2;
+    st.eps = (float)cfg->eps;
+    st.c1 = (float)(1.0 / (1.0 - std::pow(cfg->beta1, (double)t)));
+    st.c2 = (float)(1.0 / (1.0 - std::pow(cfg->beta2, (double)t)));
+    st.inv_count = 1.0 / (double)cfg->batch;
+    st.update = 1;
+    double* loss_out = k == 0 ? c->d_mlp_loss.p : (k == total - 1 ? c->d_mlp_loss.p + 1 : nullptr);
+    CK(c, kmc::launch_mlp_grad(m, c->d_mlp_samples.p, (k % per_epoch) * cfg->batch, cfg->batch, c->d_mlp_part.p,
+                               c->d_mlp_ploss.p, grid, c->stream));
+    CK(c, kmc::launch_mlp_update(m, c->d_mlp_master.p, c->d_mlp_wbf.p, c->d_mlp_m1.p, c->d_mlp_m2.p, c->d_mlp_part.p,
+                                 c->d_mlp_ploss.p, grid, st, nullptr, loss_out, c->stream));
+  }
+  CK(c, cudaEventRecord(c->ev1, c->stream));
+  double l[2] = {0, 0};
+  CK(c, cudaMemcpyAsync(l, c->d_mlp_loss.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  float ms = 0;
+  CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (stats) {
+    stats->steps = total;
+    stats->first_loss = l[0];
+    stats->last_loss = total > 1 ? l[1] : l[0];
+    stats->seconds = ms * 1e-3;
+  }
+  return KMC_OK;
+}
+
+int kmc_mlp_predict(kmc_ctx* c, int64_t n, const double* dist, const double* theta, const int32_t* pair,
+                    double* log_rate) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_predict: call kmc_mlp_init first");
+  if (n < 0 || (n > 0 && (!dist || !theta || !pair || !log_rate))) FAIL(c, KMC_ERR_ARG, "kmc_mlp_predict: bad arrays");
+  if (n == 0) return KMC_OK;
+  if (int rc = mlp_check_pairs(c, "kmc_mlp_predict", n, dist, theta, pair)) return rc;
+  CK(c, cudaSetDevice(c->device));
+  DevBuf<double> dd, dt, out;
+  DevBuf<int32_t> dp;
+  CK(c, upload(dd, dist, n, c->stream));
+  CK(c, upload(dt, theta, n, c->stream));
+  CK(c, upload(dp, pair, n, c->stream));
+  CK(c, out.alloc(n));
+  CK(c, kmc::launch_mlp_predict(mlp_dev(c), dd.p, dt.p, dp.p, n, out.p, c->stream));
+  CK(c, cudaMemcpyAsync(log_rate, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return KMC_OK;
+}
+
+int kmc_mlp_rate_table(kmc_ctx* c, int32_t nd, const double* dist, int32_t nt, const double* theta, double* rate) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_rate_table: call kmc_mlp_init first");
+  if (nd < 1 || nt < 1 || !dist || !theta || !rate) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: empty grid");
+  for (int32_t i = 0; i < nd; ++i)
+    if (!(dist[i] > 0) || !std::isfinite(dist[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: distance %d is %g", i, dist[i]);
+  for (int32_t i = 0; i < nt; ++i)
+    if (!std::isfinite(theta[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: angle %d is not finite", i);
+  CK(c, cudaSetDevice(c->device));
+  const int64_t S = c->mlp_shape.n_species;
+  const int64_t n = S * S * nd * nt;
+  DevBuf<double> dd, dt, out;
+  CK(c, upload(dd, dist, nd, c->stream));
+  CK(c, upload(dt, theta, nt, c->stream));
+  CK(c, out.alloc(n));
+  CK(c, kmc::launch_mlp_table(mlp_dev(c), dd.p, nd, dt.p, nt, out.p, c->stream));
+  CK(c, cudaMemcpyAsync(rate, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
   return KMC_OK;
 }
 

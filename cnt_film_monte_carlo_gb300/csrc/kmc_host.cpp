@@ -136,6 +136,32 @@ int kmc_forster2d_table(double gamma_0, const double distance[3], const double t
   return KMC_OK;
 }
 
+int kmc_species_rates(const kmc_species_model* m, int64_t n, const double* dist, const double* theta,
+                      const int32_t* donor, const int32_t* acceptor, double* rate) {
+  if (!m || n < 0 || (n > 0 && (!dist || !theta || !donor || !acceptor || !rate))) return KMC_ERR_ARG;
+  if (m->n_species < 1 || m->n_species > KMC_MAX_SPECIES || !m->energy || !m->diameter || !(m->diameter_ref > 0) ||
+      !(m->width > 0) || !(m->kT > 0))
+    return KMC_ERR_ARG;
+  const double ell2 = m->near_field * m->near_field;
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t a = donor[i], b = acceptor[i];
+    if (a < 0 || a >= m->n_species || b < 0 || b >= m->n_species) return KMC_ERR_ARG;
+    // donor/acceptor factor: size of the two transition dipoles, spectral overlap of the two
+    // exciton lines, and the Boltzmann factor of an uphill transfer
+    const double de = m->energy[b] - m->energy[a];
+    double s = (m->diameter[a] * m->diameter[b]) / (m->diameter_ref * m->diameter_ref);
+    s = s * std::exp(-(de * de) / (2 * m->width * m->width));
+    s = s * (de > 0 ? std::exp(-de / m->kT) : 1.0);
+    // the Förster form of create_forster_scatt_table (monte_carlo.cpp:174-187) at zero axis
+    // shifts, with an angle floor and a near-field length; sqrt(d^2) == d keeps the neutral
+    // case equal to kmc_forster2d_table
+    const double c = std::cos(theta[i]);
+    const double r = std::sqrt(dist[i] * dist[i] + ell2);
+    rate[i] = m->gamma_0 * s * (c * c + m->floor) * std::pow(1.e-9 / r, 6);
+  }
+  return KMC_OK;
+}
+
 int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
                       const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate) {
   if (!theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh || !a1 || !a2 || !rate) return KMC_ERR_ARG;

@@ -58,6 +58,8 @@ struct TableDev {
   const double* grid[4];
   const double* rate;
   double inv_h[4];  // (n - 1) / (grid[n-1] - grid[0]) for ascending grids, 0: always scan in full
+  const int32_t* species;  // kind 3: chirality of each site (reference id); pair table
+                           // (species[donor], species[acceptor]) of n[2] x n[2]
 };
 
 // Exciton flags
@@ -240,5 +242,42 @@ cudaError_t launch_l2_probe(const void* buf, int64_t bytes, int reps, int n_sms,
                             cudaStream_t s);
 cudaError_t launch_math_probe(const double* x, double* log_out, double* acos_out, int64_t n, const LogTab* tab,
                               cudaStream_t s);
+
+// ---- learned pair-rate surrogate (kmc_mlp.cu): 4 -> 64 -> 64 -> 1, GELU, BF16 weight matrices
+constexpr int kMlpH = 64;
+constexpr int kMlpOffW1 = 0, kMlpOffB1 = 256, kMlpOffW2 = 320, kMlpOffB2 = 4416, kMlpOffW3 = 4480,
+              kMlpOffB3 = 4544, kMlpOffE = 4548;
+constexpr int kMlpChunk = 128;  // samples per block pass of the gradient kernel (one per thread)
+struct MlpDev {
+  int32_t n_species, n_params;
+  double d_min, inv_span;     // log-distance input: ln(d / d_min) inv_span - 1
+  double log_mean, log_scale; // ln rate = y log_scale + log_mean
+  const float* master;        // [n_params] FP32 master parameters (biases, embedding read here)
+  const uint16_t* wbf;        // [n_params] BF16 copies (weight-matrix entries used)
+};
+struct MlpStep {
+  float lr, beta1, beta2, eps;
+  float c1, c2;               // Adam bias corrections 1 / (1 - beta^t)
+  double inv_count;           // 1 / samples of the step (loss = sum r^2 inv_count)
+  int32_t update;             // 0: only reduce the gradient
+};
+size_t mlp_grad_smem_bytes();
+// labelled samples -> {log-distance input, angle input, pair bits, normalised label}
+cudaError_t launch_mlp_samples(const MlpDev& m, const double* dist, const double* theta, const int32_t* pair,
+                               const double* log_rate, int64_t n, float4* out, cudaStream_t s);
+// per-block gradient partials part[grid][n_params] and squared-error sums part_loss[grid] of
+// samples [first, first + count)
+cudaError_t launch_mlp_grad(const MlpDev& m, const float4* samples, int64_t first, int64_t count, float* part,
+                            double* part_loss, int grid, cudaStream_t s);
+// sum of the partials in block order (grad_out, loss_out optional) and, if st.update, one Adam
+// step of master (and its BF16 copy)
+cudaError_t launch_mlp_update(const MlpDev& m, float* master, uint16_t* wbf, float* mom1, float* mom2,
+                              const float* part, const double* part_loss, int grid, const MlpStep& st,
+                              float* grad_out, double* loss_out, cudaStream_t s);
+cudaError_t launch_mlp_bf16(const float* master, uint16_t* wbf, int32_t n, cudaStream_t s);
+cudaError_t launch_mlp_predict(const MlpDev& m, const double* dist, const double* theta, const int32_t* pair,
+                               int64_t n, double* log_rate, cudaStream_t s);
+cudaError_t launch_mlp_table(const MlpDev& m, const double* dist, int32_t nd, const double* theta, int32_t nt,
+                             double* rate, cudaStream_t s);
 
 }  // namespace kmc

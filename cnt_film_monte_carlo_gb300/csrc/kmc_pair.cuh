@@ -9,7 +9,7 @@ namespace kmc {
 // not inlined: six inlined grid lookups made this translation unit take minutes to compile,
 // and the neighbour build is not on the hop path
 static __device__ __noinline__ double table_rate(const TableDev& t, double th, double zsh, double a1, double a2,
-                                             double dist) {
+                                             double dist, int64_t pair_off) {
   auto idx = [&](int d, double x) {
     return t.inv_h[d] > 0 ? index_min_abs_fast(t.grid[d], t.n[d], x, t.inv_h[d]) : index_min_abs(t.grid[d], t.n[d], x);
   };
@@ -22,15 +22,23 @@ static __device__ __noinline__ double table_rate(const TableDev& t, double th, d
   }
   int i0 = idx(0, dist);
   int i1 = idx(1, th);
-  return t.rate[(int64_t)i0 * t.n[1] + i1];
+  return t.rate[pair_off + (int64_t)i0 * t.n[1] + i1];
 }
 
-// Pair rate of find_neighbors (scatterer.cpp:40-68) for a pair already inside the window.
+// Offset of the (donor, acceptor) table of a KMC_TABLE_2D_SPECIES table (0 for the others).
+__device__ __forceinline__ int64_t pair_table(const TableDev& t, int64_t donor, int64_t acceptor) {
+  if (t.kind != 3) return 0;
+  return ((int64_t)t.species[donor] * t.n[2] + t.species[acceptor]) * ((int64_t)t.n[0] * t.n[1]);
+}
+
+// Pair rate of find_neighbors (scatterer.cpp:40-68) for a pair already inside the window;
+// pair_off selects the chirality pair's table (pair_table).
 __device__ __forceinline__ double pair_rate(const TableDev& t, const double4_32a& p1, const double* a1v, const double4_32a& p2,
-                                            const double* a2v, double dR0, double dR1, double dR2, double distance) {
+                                            const double* a2v, double dR0, double dR1, double dR2, double distance,
+                                            int64_t pair_off = 0) {
   double cosT = dot3(a1v[0], a1v[1], a1v[2], a2v[0], a2v[1], a2v[2]);
   double theta, ash1 = 0, ash2 = 0, zsh = 0;
-  if (t.kind == 2) {
+  if (t.kind != 4) {  // 2-D tables: folded angle
     double ac = fabs(cosT);
     theta = ac >= 1.0 ? 0.0 : kmc_acos(ac);
   } else if (cosT == 1) {
@@ -49,7 +57,7 @@ __device__ __forceinline__ double pair_rate(const TableDev& t, const double4_32a
     zsh = norm3((ash1 * a1v[0] + p1.x) - (ash2 * a2v[0] + p2.x), (ash1 * a1v[1] + p1.y) - (ash2 * a2v[1] + p2.y),
                 (ash1 * a1v[2] + p1.z) - (ash2 * a2v[2] + p2.z));
   }
-  return table_rate(t, theta, zsh, ash1, ash2, distance);
+  return table_rate(t, theta, zsh, ash1, ash2, distance, pair_off);
 }
 
 }  // namespace kmc

@@ -69,16 +69,26 @@ class Engine:
         return self
 
     def set_table(self, table: dict):
-        """``table = {"kind": 4|2, "grids": [...], "rate": ndarray}``."""
+        """``table = {"kind": 4|2|3, "grids": [...], "rate": ndarray}``; kind 3 (one 2-D table per
+        chirality pair) has rate [S][S][n_dist][n_theta]."""
         grids = [_f64(g) for g in table["grids"]]
-        rate = _f64(table["rate"]).ravel()
+        rate_nd = _f64(table["rate"])
+        rate = rate_nd.ravel()
         t = L.kmc_table()
         t.kind = int(table["kind"])
         for d, g in enumerate(grids):
             t.n[d] = len(g)
             t.grid[d] = L.ptr(g, C.c_double)
+        if t.kind == L.KMC_TABLE_2D_SPECIES:
+            t.n[2] = rate_nd.shape[0]
         t.rate = L.ptr(rate, C.c_double)
         self._check(self.lib.kmc_set_rate_table(self.h, C.byref(t)))
+        return self
+
+    def set_species(self, species, n_species: int):
+        """Chirality index of every loaded site (read by kind-3 tables)."""
+        sp = np.ascontiguousarray(species, dtype=np.int32)
+        self._check(self.lib.kmc_set_site_species(self.h, L.ptr(sp, C.c_int32), int(n_species)))
         return self
 
     def build(self, r_max: float) -> dict:
@@ -233,6 +243,78 @@ class Engine:
 
 
 # ---------------------------------------------------------------------- host-side algorithms
+    # ------------------------------------------------------------ rate surrogate
+    def mlp_init(self, n_species: int, d_min: float, d_max: float, log_mean: float, log_scale: float, seed: int = 0):
+        sh = L.kmc_mlp_shape(int(n_species), float(d_min), float(d_max), float(log_mean), float(log_scale))
+        self._check(self.lib.kmc_mlp_init(self.h, C.byref(sh), int(seed)))
+        self.mlp_species = int(n_species)
+        return self
+
+    def mlp_params(self) -> np.ndarray:
+        p = np.zeros(L.KMC_MLP_PARAMS(self.mlp_species), np.float32)
+        self._check(self.lib.kmc_mlp_get_params(self.h, L.ptr(p, C.c_float), len(p)))
+        return p
+
+    def mlp_set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.lib.kmc_mlp_set_params(self.h, L.ptr(p, C.c_float), len(p)))
+        return self
+
+    def mlp_set_samples(self, dist, theta, pair, log_rate):
+        d, t, lr = _f64(dist), _f64(theta), _f64(log_rate)
+        pr = np.ascontiguousarray(pair, dtype=np.int32)
+        self._check(self.lib.kmc_mlp_set_samples(self.h, len(d), L.ptr(d, C.c_double), L.ptr(t, C.c_double),
+                                                 L.ptr(pr, C.c_int32), L.ptr(lr, C.c_double)))
+        return self
+
+    def mlp_gradient(self, first: int, count: int):
+        g = np.zeros(L.KMC_MLP_PARAMS(self.mlp_species), np.float32)
+        loss = C.c_double(0)
+        self._check(self.lib.kmc_mlp_gradient(self.h, int(first), int(count), L.ptr(g, C.c_float), C.byref(loss)))
+        return g, loss.value
+
+    def mlp_train(self, epochs: int, batch: int, lr: float, lr_final: float, beta1=0.9, beta2=0.999, eps=1e-8) -> dict:
+        cfg = L.kmc_mlp_train_cfg(int(epochs), int(batch), float(lr), float(lr_final), float(beta1), float(beta2),
+                                  float(eps))
+        st = L.kmc_mlp_train_stats()
+        self._check(self.lib.kmc_mlp_train(self.h, C.byref(cfg), C.byref(st)))
+        return {k: getattr(st, k) for k, _ in L.kmc_mlp_train_stats._fields_}
+
+    def mlp_predict(self, dist, theta, pair) -> np.ndarray:
+        d, t = _f64(dist), _f64(theta)
+        pr = np.ascontiguousarray(pair, dtype=np.int32)
+        out = np.zeros(len(d))
+        self._check(self.lib.kmc_mlp_predict(self.h, len(d), L.ptr(d, C.c_double), L.ptr(t, C.c_double),
+                                             L.ptr(pr, C.c_int32), L.ptr(out, C.c_double)))
+        return out
+
+    def mlp_rate_table(self, dist, theta) -> np.ndarray:
+        d, t = _f64(dist), _f64(theta)
+        S = self.mlp_species
+        out = np.zeros((S, S, len(d), len(t)))
+        self._check(self.lib.kmc_mlp_rate_table(self.h, len(d), L.ptr(d, C.c_double), len(t), L.ptr(t, C.c_double),
+                                                L.ptr(out, C.c_double)))
+        return out
+
+
+def species_rates(model: dict, dist, theta, donor, acceptor) -> np.ndarray:
+    """The chirality-resolved labeller (kmc_species_rates) for pairs donor[i] -> acceptor[i]."""
+    lib = L.load()
+    e, dia = _f64(model["energy"]), _f64(model["diameter"])
+    m = L.kmc_species_model(len(e), float(model["gamma_0"]), L.ptr(e, C.c_double), L.ptr(dia, C.c_double),
+                            float(model["diameter_ref"]), float(model["width"]), float(model["kT"]),
+                            float(model["floor"]), float(model["near_field"]))
+    d, t = _f64(dist), _f64(theta)
+    a = np.ascontiguousarray(donor, dtype=np.int32)
+    b = np.ascontiguousarray(acceptor, dtype=np.int32)
+    out = np.zeros(len(d))
+    rc = lib.kmc_species_rates(C.byref(m), len(d), L.ptr(d, C.c_double), L.ptr(t, C.c_double), L.ptr(a, C.c_int32),
+                               L.ptr(b, C.c_int32), L.ptr(out, C.c_double))
+    if rc != L.KMC_OK:
+        raise L.KmcError(rc, "kmc_species_rates failed")
+    return out
+
+
 def trim_sites(pos_m, orient, left, right, lim):
     """trim_scats on copies; returns the kept (pos, orient, left, right)."""
     lib = L.load()

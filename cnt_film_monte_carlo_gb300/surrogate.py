@@ -1,0 +1,153 @@
+"""Learned pair-rate surrogate for mixed-chirality films.
+
+The reference fills one rate table per film from exciton_transfer
+(src/exciton_transfer/exciton_transfer.cpp:380-441), for one chirality pair.  A film of several
+chiralities needs a table per (donor, acceptor) pair.  This module trains the engine's
+4 -> 64 -> 64 -> 1 network (the kmc_mlp_* calls: forward, backward and Adam kernels on the GPU)
+on labelled (distance, angle, pair) samples and turns it into a KMC_TABLE_2D_SPECIES table that
+the neighbour build reads per site pair.
+
+Labels come from the chirality-resolved Förster-form labeller (kmc_species_rates), which stands
+in for exciton_transfer in this package; the labeller's own tables stay the fallback and the
+yardstick of the network's error (``rate_errors``, and the diffusion coefficient of a film run
+with each table).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import engine as E
+
+A_LATTICE = 0.246e-9  # graphene lattice constant, m
+CHIRALITIES = ((6, 5), (7, 5), (8, 3), (8, 4))
+E11_EV = (1.27, 1.21, 1.30, 1.12)  # approximate E11 exciton energies of those tubes, eV
+D_RANGE = (0.5e-9, 10e-9)          # centre distances of the tables, m
+BATCH = 152 * 128                  # one 128-sample chunk per SM per step
+
+
+def tube_diameter(n: int, m: int) -> float:
+    """Diameter of an (n, m) tube: a sqrt(n^2 + n m + m^2) / pi."""
+    return A_LATTICE * math.sqrt(n * n + n * m + m * m) / math.pi
+
+
+def species_model(chiralities=CHIRALITIES, energies_ev=E11_EV, gamma_0=1e15, width_ev=0.1, kT_ev=0.02585,
+                  floor=0.05, near_field=0.3e-9, reference=(7, 5)) -> dict:
+    """Parameters of the labeller for a set of chiralities (diameters relative to ``reference``)."""
+    return {
+        "chiralities": tuple(chiralities),
+        "gamma_0": float(gamma_0),
+        "energy": np.asarray(energies_ev, np.float64),
+        "diameter": np.asarray([tube_diameter(*c) for c in chiralities]),
+        "diameter_ref": tube_diameter(*reference),
+        "width": float(width_ev),
+        "kT": float(kT_ev),
+        "floor": float(floor),
+        "near_field": float(near_field),
+    }
+
+
+def neutral_model(n_species: int = 1, gamma_0: float = 1e15) -> dict:
+    """Equal chiralities, no angle floor, no near-field length: the plain Förster form."""
+    return {"chiralities": ((7, 5),) * n_species, "gamma_0": float(gamma_0), "energy": np.zeros(n_species),
+            "diameter": np.ones(n_species), "diameter_ref": 1.0, "width": 1.0, "kT": 1.0, "floor": 0.0,
+            "near_field": 0.0}
+
+
+def n_species(model: dict) -> int:
+    return len(model["energy"])
+
+
+def draw_samples(model: dict, n: int, seed: int = 0, d_range=D_RANGE) -> dict:
+    """n labelled samples: distance and folded angle uniform, donor and acceptor uniform."""
+    rng = np.random.default_rng(seed)
+    S = n_species(model)
+    dist = rng.uniform(d_range[0], d_range[1], n)
+    theta = rng.uniform(0.0, math.pi / 2, n)
+    donor = rng.integers(0, S, n).astype(np.int32)
+    acceptor = rng.integers(0, S, n).astype(np.int32)
+    rate = E.species_rates(model, dist, theta, donor, acceptor)
+    return {"dist": dist, "theta": theta, "donor": donor, "acceptor": acceptor,
+            "pair": (donor * S + acceptor).astype(np.int32), "log_rate": np.log(rate)}
+
+
+def grids(n_dist: int = 96, n_theta: int = 91, d_range=D_RANGE):
+    """Distance grid (m) and folded-angle grid (rad) of the tables."""
+    return np.linspace(d_range[0], d_range[1], n_dist), np.linspace(0.0, math.pi / 2, n_theta)
+
+
+def labeller_table(model: dict, dist, theta) -> dict:
+    """The labeller's own KMC_TABLE_2D_SPECIES table (the fallback the network replaces)."""
+    S = n_species(model)
+    dist = np.asarray(dist, np.float64)
+    theta = np.asarray(theta, np.float64)
+    a, b, i, k = np.meshgrid(np.arange(S), np.arange(S), np.arange(len(dist)), np.arange(len(theta)), indexing="ij")
+    rate = E.species_rates(model, dist[i.ravel()], theta[k.ravel()], a.ravel(), b.ravel())
+    return {"kind": 3, "grids": [dist, theta], "rate": rate.reshape(S, S, len(dist), len(theta))}
+
+
+def single_table(model: dict, dist, theta, species: int = 1) -> dict:
+    """One chirality's table used for every pair: a film modelled without the surrogate."""
+    t = labeller_table(model, dist, theta)
+    return {"kind": 2, "grids": t["grids"], "rate": t["rate"][species, species].copy()}
+
+
+class RateSurrogate:
+    """The network of one engine context, trained on labelled samples."""
+
+    def __init__(self, engine: E.Engine, model: dict, d_range=D_RANGE):
+        self.e = engine
+        self.model = model
+        self.S = n_species(model)
+        self.d_range = d_range
+
+    def fit(self, samples: dict, epochs: int = 60, batch: int = BATCH, lr: float = 3e-3, lr_final: float = 3e-5,
+            seed: int = 0) -> dict:
+        """Initialise (output scaled to the labels' mean and spread) and train with Adam."""
+        lr_ = samples["log_rate"]
+        self.e.mlp_init(self.S, self.d_range[0], self.d_range[1], float(lr_.mean()), float(lr_.std()), seed)
+        self.e.mlp_set_samples(samples["dist"], samples["theta"], samples["pair"], lr_)
+        return self.e.mlp_train(epochs, batch, lr, lr_final)
+
+    def predict(self, dist, theta, pair) -> np.ndarray:
+        return self.e.mlp_predict(dist, theta, pair)
+
+    def table(self, dist, theta) -> dict:
+        return {"kind": 3, "grids": [np.asarray(dist, np.float64), np.asarray(theta, np.float64)],
+                "rate": self.e.mlp_rate_table(dist, theta)}
+
+    def rate_errors(self, samples: dict) -> dict:
+        """Relative rate error |rate_net / rate_label - 1| over held-out samples."""
+        pred = self.predict(samples["dist"], samples["theta"], samples["pair"])
+        rel = np.abs(np.expm1(pred - samples["log_rate"]))
+        return {"median": float(np.median(rel)), "p99": float(np.quantile(rel, 0.99)), "max": float(rel.max())}
+
+
+def film_diffusion(film, species, n_species_: int, table: dict, n_excitons: int, n_steps: int, dt: float,
+                   velocity: float, seed: int, r_max: float = 10e-9, batches: int = 32, device: int = 0):
+    """Diffusion coefficient (D[3], 95% CI[3], m^2/s) of a mixed film run with a rate table:
+    uniform injection, mixed-precision hops, MSD in ``batches`` exciton batches."""
+    from . import _lib as L
+    from . import diffusion
+
+    e = E.Engine(device)
+    try:
+        e.load_films(film)
+        e.set_species(species, n_species_)
+        e.set_table(table)
+        e.build(r_max)
+        e.set_msd_batches(batches)
+        e.init_excitons(n_excitons, seed, L.KMC_INJECT_UNIFORM)
+        e.run(n_steps, dt, velocity, L.KMC_PREC_MIXED)
+        msd = e.msd_batches(0, n_steps)[0]
+    finally:
+        e.close()
+    t = np.arange(1, n_steps + 1) * dt
+    return diffusion.fit(msd, n_excitons, t)
+
+
+def site_species(film, tube_species) -> np.ndarray:
+    """Per-site chirality index from one index per tube of a Film."""
+    lens = np.diff(film.tube_offsets)
+    return np.repeat(np.asarray(tube_species, np.int32), lens)

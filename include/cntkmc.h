@@ -31,6 +31,8 @@ extern "C" {
 
 #define KMC_TABLE_4D 4 /* rate(theta)(z_shift, axis_shift_1, axis_shift_2), nearest grid point */
 #define KMC_TABLE_2D 2 /* rate(centre distance, folded angle in [0, pi/2]), nearest grid point */
+#define KMC_TABLE_2D_SPECIES 3 /* one 2-D table per (donor, acceptor) chirality pair of the sites */
+#define KMC_MAX_SPECIES 8      /* chiralities of a mixed film */
 
 #define KMC_INJECT_REGION 0  /* reference Green-Kubo set-up: central cell of an n^3 split, removal slab */
 #define KMC_INJECT_UNIFORM 1 /* every site is an injection site, nothing is removed */
@@ -56,7 +58,9 @@ typedef struct {
 } kmc_film;
 
 /* Rate table (scattering_struct, src/monte_carlo/scattering_struct.h:21-52).  grid[d] has n[d]
- * points; rate is row-major [n0][n1][n2][n3] (4-D) or [n0][n1] (2-D). */
+ * points; rate is row-major [n0][n1][n2][n3] (4-D) or [n0][n1] (2-D).  KMC_TABLE_2D_SPECIES:
+ * grids 0 and 1 as 2-D, n[2] = number of chiralities S, rate [S][S][n0][n1] (donor, acceptor,
+ * distance, angle); the sites' chiralities come from kmc_set_site_species. */
 typedef struct {
   int32_t kind;
   int32_t n[4];
@@ -103,6 +107,11 @@ int kmc_load_film(kmc_ctx* ctx, const kmc_film* film);
 
 /* Copy a rate table to the device (replaces set_scat_table, monte_carlo.h:419-423). */
 int kmc_set_rate_table(kmc_ctx* ctx, const kmc_table* table);
+
+/* Chirality index of every loaded site, species[n_sites] in [0, n_species) (no counterpart in
+ * the reference, whose films hold one chirality).  A KMC_TABLE_2D_SPECIES table reads the pair
+ * (species[donor], species[acceptor]).  Cleared by kmc_load_film. */
+int kmc_set_site_species(kmc_ctx* ctx, const int32_t* species, int32_t n_species);
 
 /* Cell binning and the per-site neighbour/rate CSR, built once on the device (replaces
  * create_scatterer_buckets monte_carlo.h:368-416, set_max_rate :426-440, and the per-hop
@@ -311,6 +320,92 @@ int kmc_autotune(kmc_ctx* ctx, double dt, double velocity, int64_t trial_steps, 
 int kmc_build_neighbors_noalloc(const double* pos, const double* orient, int64_t n_sites, const kmc_table* table,
                                 double max_hopping_radius, int64_t* rowptr, int32_t* col, double* cum, double* total,
                                 int64_t capacity, int64_t* nnz, void* stream, char* err, int64_t err_len);
+
+/* ---- learned pair-rate surrogate (no counterpart in the reference) ----
+ *
+ * Rates of mixed-chirality films come from a small network instead of one exciton_transfer table
+ * per chirality pair (exciton_transfer.cpp:380-441 computes one pair's table).  The network maps
+ * (centre distance d, folded angle theta, chirality pair) to the normalised log-rate
+ * y = (ln rate - log_mean) / log_scale: 4 inputs (2 ln(d / d_min) / ln(d_max / d_min) - 1,
+ * 2 theta / (pi/2) - 1, and a learned 2-wide embedding of the ordered pair donor * S + acceptor),
+ * two hidden layers of 64 with GELU (tanh form), one output.  The three weight matrices are held
+ * in BF16 (with FP32 master copies for training); biases and the embedding are FP32; every sum is
+ * FP32.  Parameters form one FP32 vector of KMC_MLP_PARAMS(S) values: W1[64][4] at 0, b1[64] at
+ * 256, W2[64][64] (row = output unit) at 320, b2[64] at 4416, W3[64] at 4480, b3 at 4544, three
+ * unused, E[S*S][2] at 4548.  Training is deterministic: same samples, parameters and
+ * configuration give the same weights on the same GPU model. */
+#define KMC_MLP_HIDDEN 64
+#define KMC_MLP_PARAMS(S) (4548 + 2 * (S) * (S))
+
+typedef struct {
+  int32_t n_species;           /* S, 1..KMC_MAX_SPECIES */
+  double d_min, d_max;         /* m: distance range of the log-distance input */
+  double log_mean, log_scale;  /* output scaling of ln(rate) */
+} kmc_mlp_shape;
+
+/* The labeller that stands in for exciton_transfer (not built here): the Förster formula of
+ * create_forster_scatt_table (monte_carlo.cpp:174-187) at zero axis shifts, extended by chirality:
+ *   rate = gamma_0 s_ab (cos^2 theta + floor) (1 nm / sqrt(d^2 + near_field^2))^6,
+ *   s_ab = (D_a D_b / D_ref^2) exp(-dE^2 / (2 width^2)) min(1, exp(-dE / kT)), dE = E_b - E_a,
+ * for donor a and acceptor b.  Equal energies and diameters with floor = near_field = 0 give
+ * kmc_forster2d_table's values bit for bit. */
+typedef struct {
+  int32_t n_species;       /* S */
+  double gamma_0;          /* 1/s */
+  const double* energy;    /* [S] exciton energies, eV */
+  const double* diameter;  /* [S] tube diameters, m */
+  double diameter_ref;     /* m */
+  double width;            /* eV */
+  double kT;               /* eV */
+  double floor;            /* added to cos^2(theta) */
+  double near_field;       /* m */
+} kmc_species_model;
+
+/* Host labeller: rate[i] for donor[i] -> acceptor[i] at dist[i] (m) and theta[i] (rad). */
+int kmc_species_rates(const kmc_species_model* model, int64_t n, const double* dist, const double* theta,
+                      const int32_t* donor, const int32_t* acceptor, double* rate);
+
+/* The network of a context: shape and parameters drawn uniformly in +-1/sqrt(fan-in) (the
+ * embedding in +-1, b3 = 0) from a SplitMix64 stream of `seed`; training state reset. */
+int kmc_mlp_init(kmc_ctx* ctx, const kmc_mlp_shape* shape, uint64_t seed);
+/* Replace / read the FP32 master parameters (n = KMC_MLP_PARAMS(S)); set also resets Adam. */
+int kmc_mlp_set_params(kmc_ctx* ctx, const float* params, int64_t n);
+int kmc_mlp_get_params(kmc_ctx* ctx, float* params, int64_t n);
+
+/* Labelled samples kept on the device: dist (m), folded theta (rad), pair = donor * S + acceptor,
+ * log_rate = ln(rate). */
+int kmc_mlp_set_samples(kmc_ctx* ctx, int64_t n, const double* dist, const double* theta, const int32_t* pair,
+                        const double* log_rate);
+
+/* Mean squared error of y against the normalised labels of samples [first, first + count) and its
+ * gradient grad[KMC_MLP_PARAMS(S)] with respect to the parameters (BF16 weights' gradient);
+ * parameters are not changed. */
+int kmc_mlp_gradient(kmc_ctx* ctx, int64_t first, int64_t count, float* grad, double* loss);
+
+typedef struct {
+  int32_t epochs;
+  int32_t batch;            /* samples per step, a multiple of 128, <= number of samples */
+  double lr, lr_final;      /* Adam step size, cosine schedule from lr to lr_final */
+  double beta1, beta2, eps; /* Adam moments */
+} kmc_mlp_train_cfg;
+
+typedef struct {
+  int64_t steps;
+  double first_loss, last_loss; /* mean squared error of the first and the last step's batch */
+  double seconds;               /* device time of the whole training (CUDA events) */
+} kmc_mlp_train_stats;
+
+/* Adam training over the samples: epochs x floor(n / batch) steps, batch k of an epoch being
+ * samples [k batch, (k + 1) batch).  Continues from the current parameters and Adam moments. */
+int kmc_mlp_train(kmc_ctx* ctx, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats* stats);
+
+/* Predicted ln(rate) for n pairs. */
+int kmc_mlp_predict(kmc_ctx* ctx, int64_t n, const double* dist, const double* theta, const int32_t* pair,
+                    double* log_rate);
+
+/* A KMC_TABLE_2D_SPECIES rate table from the network: rate[S][S][nd][nt] = exp(predicted ln rate)
+ * on the grids dist[nd] (m) and theta[nt] (rad). */
+int kmc_mlp_rate_table(kmc_ctx* ctx, int32_t nd, const double* dist, int32_t nt, const double* theta, double* rate);
 
 /* Library version string. */
 const char* kmc_version(void);

@@ -1,0 +1,245 @@
+"""The learned pair-rate surrogate on the GPU, through the C ABI: forward, gradient and Adam step
+against the CPU oracle (oracle/mlp.py), deterministic training, the network's tables, the
+chirality-pair neighbour build against exact sums, and what the trained network gains for a
+mixed-chirality film over a single-chirality table."""
+import math
+
+import numpy as np
+import pytest
+
+from cnt_film_monte_carlo_gb300 import _lib as L
+from cnt_film_monte_carlo_gb300 import engine as E
+from cnt_film_monte_carlo_gb300 import film as F
+from cnt_film_monte_carlo_gb300 import surrogate as SG
+from oracle import mlp as M
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+D_MIN, D_MAX = SG.D_RANGE
+
+
+def engine_with_net(S=4, seed=11, log_mean=20.0, log_scale=5.0):
+    e = E.Engine(0)
+    e.mlp_init(S, D_MIN, D_MAX, log_mean, log_scale, seed)
+    return e
+
+
+def oracle_inputs(s, S, log_mean, log_scale):
+    feat = M.features(s["dist"], s["theta"], D_MIN, D_MAX)
+    return feat, s["pair"], M.targets(s["log_rate"], log_mean, log_scale)
+
+
+def test_forward_matches_oracle():
+    model = SG.species_model()
+    s = SG.draw_samples(model, 5000, seed=1)
+    e = engine_with_net()
+    p = e.mlp_params()
+    got = e.mlp_predict(s["dist"], s["theta"], s["pair"])
+    e.close()
+    y, _ = M.forward(p, 4, M.features(s["dist"], s["theta"], D_MIN, D_MAX), s["pair"])
+    # FP32 sums of 64 products against float64 on the same BF16 weights
+    np.testing.assert_allclose((got - 20.0) / 5.0, y, atol=2e-5)
+
+
+@pytest.mark.parametrize("first,count", [(0, 1000), (123, 40000), (0, 128)])
+def test_gradient_matches_oracle(first, count):
+    model = SG.species_model()
+    s = SG.draw_samples(model, 50000, seed=2)
+    mean, scale = float(s["log_rate"].mean()), float(s["log_rate"].std())
+    e = engine_with_net(log_mean=mean, log_scale=scale)
+    e.mlp_set_samples(s["dist"], s["theta"], s["pair"], s["log_rate"])
+    g, loss = e.mlp_gradient(first, count)
+    p = e.mlp_params()
+    e.close()
+    feat, pair, tgt = oracle_inputs(s, 4, mean, scale)
+    sl = slice(first, first + count)
+    lo, go = M.loss_and_grad(p, 4, feat[sl], pair[sl], tgt[sl])
+    assert loss == pytest.approx(lo, rel=1e-5)
+    err = np.abs(g - go)
+    assert np.all(err <= 1e-3 * np.abs(go) + 1e-4 * np.abs(go).max()), int(np.argmax(err / (np.abs(go) + 1e-30)))
+    assert np.all(g[M.OFF_B3 + 1:M.OFF_E] == 0)
+
+
+def test_adam_step_matches_oracle():
+    model = SG.species_model()
+    n = 2560
+    s = SG.draw_samples(model, n, seed=4)
+    mean, scale = float(s["log_rate"].mean()), float(s["log_rate"].std())
+    e = engine_with_net(log_mean=mean, log_scale=scale)
+    e.mlp_set_samples(s["dist"], s["theta"], s["pair"], s["log_rate"])
+    p0 = e.mlp_params()
+    g, _ = e.mlp_gradient(0, n)
+    lr = 1e-2
+    st = e.mlp_train(1, n, lr, lr)
+    p1 = e.mlp_params()
+    e.close()
+    assert st["steps"] == 1
+    want, _, _ = M.adam(p0, np.zeros_like(g, np.float64), np.zeros_like(g, np.float64), g.astype(np.float64), 1, lr)
+    np.testing.assert_allclose(p1, want, atol=2e-3 * lr + 1e-7, rtol=0)
+    moved = np.abs(p1 - p0)
+    assert np.median(moved[g != 0]) == pytest.approx(lr, rel=1e-3)
+
+
+def test_training_is_deterministic_and_lowers_the_loss():
+    model = SG.species_model()
+    s = SG.draw_samples(model, 60000, seed=5)
+    out = []
+    for _ in range(2):
+        e = E.Engine(0)
+        net = SG.RateSurrogate(e, model)
+        st = net.fit(s, epochs=40, batch=SG.BATCH, lr=3e-3, lr_final=1e-3, seed=9)
+        out.append((e.mlp_params(), st))
+        e.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    st = out[0][1]
+    assert st["steps"] == 40 * (60000 // SG.BATCH)
+    assert st["last_loss"] < 0.2 * st["first_loss"]
+
+
+def test_rate_table_is_the_network_on_the_grid():
+    e = engine_with_net(S=3, seed=3)
+    dist, theta = SG.grids(9, 7)
+    tab = e.mlp_rate_table(dist, theta)
+    a, b, i, k = np.meshgrid(np.arange(3), np.arange(3), np.arange(9), np.arange(7), indexing="ij")
+    pred = e.mlp_predict(dist[i.ravel()], theta[k.ravel()], (a * 3 + b).ravel())
+    e.close()
+    assert tab.shape == (3, 3, 9, 7)
+    np.testing.assert_allclose(np.log(tab.ravel()), pred, rtol=0, atol=1e-12)
+
+
+def mixed_film(seed=3, n_tubes=40, length=30.0, box=(60.0, 60.0, 8.0), S=4):
+    f = F.straight_tubes(n_tubes, length, box, 5.0, 1.0, seed)
+    tube_sp = np.random.default_rng(seed).integers(0, S, n_tubes)
+    return f, SG.site_species(f, tube_sp)
+
+
+def gpu_neighbors(f, sp, S, table, r_max=10e-9):
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_species(sp, S)
+    e.set_table(table)
+    st = e.build(r_max)
+    g = e.neighbors(f.n_sites, st["nnz"])
+    e.close()
+    return g
+
+
+def test_species_table_build_is_exact():
+    # The oracle finds each neighbour's grid cell: with an index-valued 2-D table, every entry's
+    # rate is an exact integer (prefix sums of integers below 2^53 are exact), so the row's
+    # differences give the cells.  The expected row is then the FP64 running sum of the pair
+    # tables' values in list order, as find_neighbors sums (scatterer.cpp:78-80).
+    f, sp = mixed_film()
+    model = SG.species_model()
+    dist, theta = SG.grids(40, 31)
+    nd, nt = len(dist), len(theta)
+    idx_tab = {"kind": 2, "grids": [dist, theta], "rate": np.arange(1, nd * nt + 1, dtype=np.float64).reshape(nd, nt)}
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, idx_tab, 10e-9, 2e5)
+    csr = sim.build_csr()
+    lab = SG.labeller_table(model, dist, theta)
+    flat = lab["rate"].reshape(4, 4, nd * nt)
+    g = gpu_neighbors(f, sp, 4, lab)
+    assert np.array_equal(g["rowptr"], csr["rowptr"]) and np.array_equal(g["col"], csr["col"])
+    want = np.zeros(len(csr["cum"]))
+    total = np.zeros(f.n_sites)
+    for s in range(f.n_sites):
+        r0, r1 = csr["rowptr"][s], csr["rowptr"][s + 1]
+        cells = np.diff(np.concatenate([[0.0], csr["cum"][r0:r1]])).astype(np.int64) - 1
+        run = 0.0
+        for j in range(r1 - r0):
+            v = float(flat[sp[s], sp[csr["col"][r0 + j]], cells[j]])
+            run = v if j == 0 else run + v
+            want[r0 + j] = run
+        total[s] = run if r1 > r0 else 0.0
+    assert np.array_equal(g["cum"], want)
+    assert np.array_equal(g["total"], total)
+
+
+def test_identical_pair_tables_give_the_2d_build():
+    f, sp = mixed_film(seed=4)
+    t2 = SG.single_table(SG.species_model(), *SG.grids(50, 41), species=2)
+    t3 = {"kind": 3, "grids": t2["grids"], "rate": np.broadcast_to(t2["rate"], (4, 4) + t2["rate"].shape).copy()}
+    a = gpu_neighbors(f, sp, 4, t3)
+    b = gpu_neighbors(f, sp, 4, t2)
+    for k in ("rowptr", "col", "cum", "total"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_errors_are_reported():
+    e = E.Engine(0)
+    with pytest.raises(L.KmcError) as ex:
+        e.mlp_train(1, 128, 1e-3, 1e-3)
+    assert ex.value.code == L.KMC_ERR_STATE
+    e.mlp_init(4, D_MIN, D_MAX, 0.0, 1.0, 0)
+    s = SG.draw_samples(SG.species_model(), 1000, seed=6)
+    with pytest.raises(L.KmcError) as ex:
+        e.mlp_set_samples(s["dist"], s["theta"], s["pair"] + 16, s["log_rate"])
+    assert ex.value.code == L.KMC_ERR_ARG
+    e.mlp_set_samples(s["dist"], s["theta"], s["pair"], s["log_rate"])
+    with pytest.raises(L.KmcError) as ex:
+        e.mlp_train(1, 100, 1e-3, 1e-3)  # not a multiple of 128
+    assert ex.value.code == L.KMC_ERR_ARG
+    with pytest.raises(L.KmcError) as ex:
+        e.mlp_gradient(900, 200)  # past the samples
+    assert ex.value.code == L.KMC_ERR_ARG
+    f, sp = mixed_film()
+    e.load_films(f)
+    with pytest.raises(L.KmcError) as ex:
+        e.set_species(sp + 4, 4)
+    assert ex.value.code == L.KMC_ERR_ARG
+    e.set_table(SG.labeller_table(SG.species_model(), *SG.grids(10, 10)))
+    with pytest.raises(L.KmcError) as ex:
+        e.build(10e-9)  # a species table without site species
+    assert ex.value.code == L.KMC_ERR_STATE
+    e.set_species(sp, 4)
+    e.build(10e-9)
+    e.close()
+
+
+@pytest.fixture(scope="module")
+def trained():
+    model = SG.species_model()
+    train = SG.draw_samples(model, 2_000_000, seed=100)
+    held = SG.draw_samples(model, 200_000, seed=101)
+    e = E.Engine(0)
+    net = SG.RateSurrogate(e, model)
+    st = net.fit(train, epochs=200, lr=3e-3, lr_final=3e-5, seed=1)
+    yield model, net, st, held
+    e.close()
+
+
+def test_trained_network_rate_error(trained):
+    # 200 epochs over 2M samples (20,400 Adam steps): median 0.21 %, p99 1.4 %, max 7.6 % on a
+    # GB300; the bounds leave room for labels that differ in the last bits between host libms
+    model, net, st, held = trained
+    err = net.rate_errors(held)
+    print("rate errors", err, "training", st)
+    assert err["median"] < 0.005 and err["p99"] < 0.03 and err["max"] < 0.15
+    dist, theta = SG.grids()
+    rel = np.abs(net.table(dist, theta)["rate"] / SG.labeller_table(model, dist, theta)["rate"] - 1)
+    assert np.median(rel) < 0.005
+
+
+def test_network_tables_reproduce_the_labeller_film_diffusion(trained):
+    # Mixed (6,5)/(7,5)/(8,3)/(8,4) film: D from the labeller's pair tables (the yardstick), from
+    # the network's tables, and from one (7,5) table for every pair (the film without the
+    # surrogate: a single exciton_transfer table).  Same excitons and Philox streams for all.
+    model, net, st, held = trained
+    f = F.straight_tubes(300, 80.0, (250.0, 250.0, 10.0), 5.0, 1.0, 21)
+    sp = SG.site_species(f, np.random.default_rng(21).integers(0, 4, 300))
+    dist, theta = SG.grids()
+    # A rate that differs in the last digits moves a selection near a bin edge, after which the
+    # trajectories decorrelate, so the comparison is statistical: the in-plane D from the network's
+    # tables lies within twice the combined 95 % interval of the labeller's, the single table's
+    # more than three times outside it (on a GB300: -2.2 % and +28 %, intervals ~3 %).
+    args = (20000, 100, 1e-12, 2e5, 77)
+    runs = {}
+    for name, tab in (("labeller", SG.labeller_table(model, dist, theta)), ("network", net.table(dist, theta)),
+                      ("single", SG.single_table(model, dist, theta, species=1))):
+        d, ci = SG.film_diffusion(f, sp, 4, tab, *args)
+        runs[name] = (float(np.mean(d[:2])), float(np.hypot(ci[0], ci[1]) / 2))
+    print("in-plane D and 95 % interval", runs)
+    (lab, cl), (nn, cn), (one, co) = runs["labeller"], runs["network"], runs["single"]
+    assert abs(nn - lab) < 2 * np.hypot(cl, cn)
+    assert abs(one - lab) > 3 * np.hypot(cl, co)

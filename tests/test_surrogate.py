@@ -1,0 +1,118 @@
+"""The learned pair-rate surrogate on the CPU: the labeller that stands in for exciton_transfer,
+pinned to the reference's Förster form, the oracle network's gradient against finite
+differences, and the host-side argument checks of the C ABI (no device calls)."""
+import math
+
+import numpy as np
+import pytest
+
+from cnt_film_monte_carlo_gb300 import _lib as L
+from cnt_film_monte_carlo_gb300 import engine as E
+from cnt_film_monte_carlo_gb300 import surrogate as SG
+from cnt_film_monte_carlo_gb300 import tables
+from oracle import mlp as M
+
+
+def test_neutral_labeller_is_the_forster_table_bit_for_bit():
+    # equal chiralities, no floor, no near field: gamma_0 cos^2(theta) (1 nm / d)^6 of
+    # create_forster_scatt_table (monte_carlo.cpp:174-187) as kmc_forster2d_table builds it
+    t = tables.forster_2d(1e15, (0.5e-9, 10e-9, 96), (0.0, 90.0, 91))
+    dist, theta = t["grids"]
+    i, k = np.meshgrid(np.arange(len(dist)), np.arange(len(theta)), indexing="ij")
+    z = np.zeros(i.size, np.int32)
+    got = E.species_rates(SG.neutral_model(1), dist[i.ravel()], theta[k.ravel()], z, z)
+    assert np.array_equal(got, t["rate"].ravel())
+
+
+def test_labeller_matches_oracle():
+    model = SG.species_model()
+    s = SG.draw_samples(model, 20000, seed=3)
+    want = M.species_rates(model, s["dist"], s["theta"], s["donor"], s["acceptor"])
+    np.testing.assert_allclose(np.exp(s["log_rate"]), want, rtol=1e-13)
+    # the chirality factor: downhill and same-chirality transfers are not damped, uphill ones are
+    S = SG.n_species(model)
+    d = np.full(S * S, 2e-9)
+    th = np.zeros(S * S)
+    a, b = np.divmod(np.arange(S * S), S)
+    r = E.species_rates(model, d, th, a, b).reshape(S, S)
+    e = model["energy"]
+    lo, hi = int(np.argmin(e)), int(np.argmax(e))
+    assert r[hi, lo] > 10 * r[lo, hi]
+
+
+def test_labeller_table_layout():
+    model = SG.species_model()
+    dist, theta = SG.grids(7, 5)
+    t = SG.labeller_table(model, dist, theta)
+    assert t["kind"] == L.KMC_TABLE_2D_SPECIES and t["rate"].shape == (4, 4, 7, 5)
+    a, b, i, k = 2, 3, 4, 1
+    want = M.species_rates(model, [dist[i]], [theta[k]], [a], [b])[0]
+    assert t["rate"][a, b, i, k] == pytest.approx(want, rel=1e-13)
+    single = SG.single_table(model, dist, theta, species=1)
+    assert single["kind"] == L.KMC_TABLE_2D and np.array_equal(single["rate"], t["rate"][1, 1])
+
+
+def test_labeller_rejects_bad_arguments():
+    model = SG.species_model()
+    with pytest.raises(L.KmcError):
+        E.species_rates(model, [1e-9], [0.0], [0], [4])  # species out of range
+    bad = dict(model, width=0.0)
+    with pytest.raises(L.KmcError):
+        E.species_rates(bad, [1e-9], [0.0], [0], [1])
+
+
+def test_bf16_rounding_known_answers():
+    x = np.array([1.0, 1 + 2 ** -8, 1 + 3 * 2 ** -8, 1 + 2 ** -9, -2.5, 3.140625, 1e-20], np.float32)
+    got = M.bf16(x)
+    want = np.array([1.0, 1.0, 1 + 2 ** -6, 1.0, -2.5, 3.140625], np.float32)
+    assert got[:6].tolist() == want[:6].tolist()
+    assert got[6].view(np.uint32) & 0xFFFF == 0 and abs(got[6] / np.float32(1e-20) - 1) < 2 ** -8
+
+
+def oracle_problem(n=300, S=3, seed=1):
+    rng = np.random.default_rng(seed)
+    params = (rng.standard_normal(M.n_params(S)) * 0.3).astype(np.float32)
+    dist = rng.uniform(0.5e-9, 10e-9, n)
+    theta = rng.uniform(0, math.pi / 2, n)
+    pair = rng.integers(0, S * S, n)
+    feat = M.features(dist, theta, 0.5e-9, 10e-9)
+    target = rng.standard_normal(n).astype(np.float32)
+    return params, S, feat, pair, target
+
+
+def test_oracle_gradient_matches_finite_differences():
+    params, S, feat, pair, target = oracle_problem()
+    p64 = params.astype(np.float64)
+    _, g = M.loss_and_grad(p64, S, feat, pair, target, quantize=False)
+    rng = np.random.default_rng(5)
+    idx = np.concatenate([rng.choice(np.arange(M.OFF_W1, M.OFF_B1), 6), rng.choice(np.arange(M.OFF_B1, M.OFF_W2), 3),
+                          rng.choice(np.arange(M.OFF_W2, M.OFF_B2), 10), rng.choice(np.arange(M.OFF_B2, M.OFF_W3), 3),
+                          rng.choice(np.arange(M.OFF_W3, M.OFF_B3), 4), [M.OFF_B3],
+                          np.arange(M.OFF_E, M.n_params(S))])
+
+    def loss_at(p):
+        y, _ = M.forward(p, S, feat, pair, quantize=False)
+        return float(np.mean((y - target.astype(np.float64)) ** 2))
+
+    h = 1e-6
+    for i in idx:
+        pp, pm = p64.copy(), p64.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (loss_at(pp) - loss_at(pm)) / (2 * h)
+        assert fd == pytest.approx(g[i], rel=2e-5, abs=1e-9), i
+    assert np.all(g[M.OFF_B3 + 1:M.OFF_E] == 0)  # padding
+
+
+def test_oracle_adam_first_step_moves_by_lr():
+    rng = np.random.default_rng(2)
+    p = rng.standard_normal(50).astype(np.float32)
+    g = rng.standard_normal(50)
+    q, m, v = M.adam(p, np.zeros(50), np.zeros(50), g, 1, 1e-3)
+    # bias-corrected first step: m_hat / sqrt(v_hat) = sign(g)
+    np.testing.assert_allclose(p.astype(np.float64) - q, 1e-3 * np.sign(g), rtol=1e-4, atol=1e-7)
+
+
+def test_parameter_layout():
+    assert L.KMC_MLP_PARAMS(4) == M.n_params(4) == 4548 + 32
+    assert M.OFF_B3 == 4544 and M.OFF_W2 == 320
