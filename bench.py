@@ -13,6 +13,11 @@ Multi-GPU (torchrun): independent replicas (seed + rank), weak scaling, no colle
 data path.  --impl reference times the reference's algorithm (the oracle's restatement, which
 recomputes every neighbour list on every hop like src/monte_carlo/scatterer.cpp:9-31) on the host
 cores.
+Other workloads (--workload): cfg3 (256-film batch), cfg4 (10.8 M-site film), contacts (the
+contacts-mode loop on the cfg2 film) and cfg5: 64 mixed-chirality films whose pair rate tables
+come from the surrogate network trained on the GPU in the set-up (untimed); its line adds a
+"surrogate" object (training throughput, held-out rate error, D error against the labeller's
+tables on a mixed film).
 """
 from __future__ import annotations
 
@@ -56,10 +61,66 @@ def workload(name="cfg2", films=256):
         return out, tab, ne, (f"cfg3 batch: {films} films, tubes U{{50..2000}}, lognormal length (median 300 nm, "
                                "sigma 0.5), 1000x1000x20 nm boxes, 1 nm segments, 10 nm cutoff, 100 excitons per tube, "
                                "one persistent launch")
+    if name == "cfg5":
+        from cnt_film_monte_carlo_gb300 import surrogate as SG
+
+        n_f = CFG5_FILMS if films == 256 else films
+        out = [F.lognormal_tubes(1000, 300.0, 0.5, (1000.0, 1000.0, 20.0), seed=5000 + i) for i in range(n_f)]
+        # the reference reads one table: its arm (and the CPU sample) use the (7,5) table for every
+        # pair; the GPU arm replaces it with the network's pair tables (cfg5_surrogate)
+        single = SG.single_table(SG.species_model(), *SG.grids(), species=1)
+        return out, single, [CFG5_EXC] * n_f, (
+            f"cfg5 batch: {n_f} mixed-chirality films of 1000 tubes ((6,5), (7,5), (8,3), (8,4) uniform per tube), "
+            "lognormal length (median 300 nm, sigma 0.5), 1000x1000x20 nm boxes, 1 nm segments, 10 nm cutoff, "
+            "16 (donor, acceptor) rate tables of 96 x 91 built by the trained surrogate")
     f = F.straight_tubes(FILM["n_tubes"], FILM["length_nm"], box_nm=FILM["box_nm"], max_tilt_deg=FILM["tilt_deg"],
                          seed=FILM["film_seed"])
     return [f], tab, [N_EXC], ("cfg2 film: 100 tubes x 200 nm, 500x500x10 nm, 1 nm segments, 10 nm cutoff, "
                                "2-D rate table")
+
+
+CFG5_FILMS, CFG5_EXC = 64, 100_000
+
+
+def cfg5_surrogate(films, device):
+    """Per-site chiralities of the cfg5 films, the rate tables of the network trained on the GPU
+    (2M labelled samples, 200 epochs) and its report: training throughput, held-out rate error,
+    and the D error it brings to a mixed film against the labeller's own tables."""
+    from cnt_film_monte_carlo_gb300 import engine as E
+    from cnt_film_monte_carlo_gb300 import film as F
+    from cnt_film_monte_carlo_gb300 import surrogate as SG
+
+    model = SG.species_model()
+    species = [SG.site_species(f, np.random.default_rng(500 + i).integers(0, 4, f.n_tubes)) for i, f in enumerate(films)]
+    train = SG.draw_samples(model, 2_000_000, seed=100)
+    held = SG.draw_samples(model, 200_000, seed=101)
+    dist_g, theta_g = SG.grids()
+    e = E.Engine(device)
+    net = SG.RateSurrogate(e, model)
+    st = net.fit(train, epochs=200)
+    err = net.rate_errors(held)
+    tab = net.table(dist_g, theta_g)
+    e.close()
+    lab_tab = SG.labeller_table(model, dist_g, theta_g)
+    f = F.straight_tubes(300, 80.0, (250.0, 250.0, 10.0), 5.0, 1.0, 21)
+    sp = SG.site_species(f, np.random.default_rng(21).integers(0, 4, 300))
+    run = (20000, 100, BIN, VEL, 77)
+    d_lab, c_lab = SG.film_diffusion(f, sp, 4, lab_tab, *run, device=device)
+    d_net, c_net = SG.film_diffusion(f, sp, 4, tab, *run, device=device)
+    lab, net_d = float(np.mean(d_lab[:2])), float(np.mean(d_net[:2]))
+    report = {
+        "network": "4 -> 64 -> 64 -> 1 GELU, BF16 weight matrices, FP32 sums; labels from the chirality-resolved "
+                   "Förster-form labeller (stand-in for exciton_transfer)",
+        "training": {"samples": len(train["dist"]), "epochs": 200, "steps": st["steps"], "seconds": st["seconds"],
+                     "samples_per_s": st["steps"] * SG.BATCH / st["seconds"], "first_loss": st["first_loss"],
+                     "last_loss": st["last_loss"]},
+        "rate_error_held_out": err,
+        "d_error": {"film": "300 tubes x 80 nm, 250x250x10 nm, 20,000 excitons, 100 x 1 ps",
+                    "labeller_in_plane": lab, "network_in_plane": net_d, "rel_error": net_d / lab - 1,
+                    "ci95_labeller": float(np.hypot(c_lab[0], c_lab[1]) / 2),
+                    "ci95_network": float(np.hypot(c_net[0], c_net[1]) / 2)},
+    }
+    return species, tab, report
 
 
 def config(desc, n_sites, n_exc, bins_per_step, extra=None):
@@ -168,7 +229,7 @@ class CpuSample:
 
 
 def reference_arm(args):
-    films, tab, _, desc = workload(args.workload, args.films)
+    films, tab, ne, desc = workload(args.workload, args.films)
     f = films[0]
     if args.workload == "contacts":
         vals, secs = [], []
@@ -193,6 +254,8 @@ def reference_arm(args):
     vals, secs, sample = [], [], ""
     for i in range(args.warmup + args.steps):
         v, sample, dt = cs.run()
+        if args.workload == "cfg5":
+            sample += "; (7,5) table for every pair (the reference reads one table; same per-hop work)"
         if i >= args.warmup:
             vals.append(v)
             secs.append(dt)
@@ -200,7 +263,7 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config(desc, films[0].n_sites, N_EXC, 1, {"sample": sample}),
+            "config": config(desc, sum(x.n_sites for x in films), int(sum(ne)), 1, {"sample": sample}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cs.threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -338,11 +401,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-exc", type=int, default=None, help="excitons per film (default: the workload's)")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "contacts"])
-    ap.add_argument("--films", type=int, default=256, help="films of the cfg3 batch")
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5", "contacts"])
+    ap.add_argument("--films", type=int, default=256, help="films of the cfg3 batch (cfg5: default 64)")
     ap.add_argument("--bins-per-step", type=int, default=8,
                     help="1 ps MSD bins advanced per timed step (one kmc_run call)")
-    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=None, help="plain FP64 comparison steps (default 3, cfg5 1)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall seconds of one CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -352,6 +415,8 @@ def main():
                     help="order in which the mixed kernel takes excitons")
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     args = ap.parse_args()
+    if args.fp64_steps is None:
+        args.fp64_steps = 1 if args.workload == "cfg5" else 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -387,14 +452,24 @@ def main():
         return
 
     films, tab, n_exc, desc = workload(args.workload, args.films)
+    cpu_tab, species, surrogate = tab, None, None
+    if args.workload == "cfg5":
+        species, tab, surrogate = cfg5_surrogate(films, local)
+        species = np.concatenate(species)
     if args.n_exc is not None:
         n_exc = [args.n_exc] * len(films)
     n_exc_total = int(sum(n_exc))
     f = films[0]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def load(eng):
+        eng.load_films(films)
+        if species is not None:
+            eng.set_species(species, 4)
+        eng.set_table(tab)
+
     e = E.Engine(local)
-    e.load_films(films)
-    e.set_table(tab)
+    load(e)
     st = e.build(R_MAX)
     e.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
     bins = args.bins_per_step
@@ -441,8 +516,7 @@ def main():
     fp64 = None
     if args.fp64_steps > 0:
         e2 = E.Engine(local)
-        e2.load_films(films)
-        e2.set_table(tab)
+        load(e2)
         e2.build(R_MAX)
         e2.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
         e2.run(bins, BIN, VEL, L.KMC_PREC_FP64)  # one warm-up step
@@ -462,8 +536,7 @@ def main():
         barrier()
         t0 = time.perf_counter()
         e3 = E.Engine(local)
-        e3.load_films(films)
-        e3.set_table(tab)
+        load(e3)
         e3.build(R_MAX)
         e3.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
         e3.set_work_order(order)
@@ -483,6 +556,8 @@ def main():
         w3 = time.perf_counter() - t0
         n_all = sum(x.n_sites for x in films)
         h2d = n_all * (3 * 8 * 2 + 2 * 4) + 8 * (len(films) + 1) + tab["rate"].nbytes + sum(g.nbytes for g in tab["grids"])
+        if species is not None:
+            h2d += species.nbytes
         e2e = {"value": h3 * world / w3, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                "d2h_bytes_per_step": int(d2h / args.steps), "seconds": w3,
                "includes": "film+table upload and neighbour build (per step: amortised over K), exciton creation, "
@@ -532,9 +607,13 @@ def main():
         "e2e": e2e,
         "clocks": clk.summary(),
     }
+    if surrogate is not None:
+        line["surrogate"] = surrogate
     if world == 1 and not args.no_cpu:
-        cs = CpuSample(f, tab, seconds=args.cpu_seconds)
+        cs = CpuSample(f, cpu_tab, seconds=args.cpu_seconds)
         v, sample, _ = cs.run()
+        if species is not None:
+            sample += "; (7,5) table for every pair (the reference reads one table; same per-hop work)"
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cs.threads, "kind": "port", "sample": sample}
     print(json.dumps(line))
     if dist is not None:
