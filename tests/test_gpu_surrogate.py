@@ -61,6 +61,27 @@ def test_gradient_matches_oracle(first, count):
     assert np.all(g[M.OFF_B3 + 1:M.OFF_E] == 0)
 
 
+@pytest.mark.parametrize("S", [1, 8])
+def test_gradient_matches_oracle_at_the_species_limits(S):
+    # S = 8: every one of the block's 128 threads owns an embedding entry; S = 1: a single pair
+    rng = np.random.default_rng(S)
+    n = 3000
+    dist = rng.uniform(D_MIN, D_MAX, n)
+    theta = rng.uniform(0, math.pi / 2, n)
+    pair = rng.integers(0, S * S, n).astype(np.int32)
+    log_rate = rng.normal(20.0, 4.0, n)
+    e = engine_with_net(S=S, seed=S + 20, log_mean=20.0, log_scale=4.0)
+    e.mlp_set_samples(dist, theta, pair, log_rate)
+    g, loss = e.mlp_gradient(0, n)
+    p = e.mlp_params()
+    e.close()
+    assert len(g) == M.n_params(S)
+    lo, go = M.loss_and_grad(p, S, M.features(dist, theta, D_MIN, D_MAX), pair, M.targets(log_rate, 20.0, 4.0))
+    assert loss == pytest.approx(lo, rel=1e-5)
+    assert np.all(np.abs(g - go) <= 1e-3 * np.abs(go) + 1e-4 * np.abs(go).max())
+    assert np.all(g[M.OFF_E:] != 0)  # every pair occurs, so every embedding entry has a gradient
+
+
 def test_adam_step_matches_oracle():
     model = SG.species_model()
     n = 2560
