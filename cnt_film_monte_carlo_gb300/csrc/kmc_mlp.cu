@@ -339,8 +339,15 @@ cudaError_t launch_mlp_bf16(const float* master, uint16_t* wbf, int32_t n, cudaS
 cudaError_t launch_mlp_grad(const MlpDev& m, const float4* samples, int64_t first, int64_t count, float* part,
                             double* part_loss, int grid, cudaStream_t s) {
   const size_t bytes = mlp_grad_smem_bytes();
-  cudaError_t e = cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  static thread_local int opted = -1;  // the shared-memory opt-in, once per thread and device
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  if (opted != dev) {
+    e = cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    opted = dev;
+  }
   k_mlp_grad<<<grid, kMlpChunk, bytes, s>>>(m, samples, first, count, part, part_loss);
   return cudaGetLastError();
 }
