@@ -27,6 +27,7 @@ class Engine:
         self.n_films = 0
         self.n_exc = None
         self.n_segments = 2  # contacts mode: set by contacts_init
+        self.mlp_species = 1  # rate surrogate: set by mlp_init
 
     def close(self):
         if getattr(self, "h", None):

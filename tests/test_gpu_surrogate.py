@@ -192,6 +192,9 @@ def test_errors_are_reported():
     with pytest.raises(L.KmcError) as ex:
         e.mlp_train(1, 128, 1e-3, 1e-3)
     assert ex.value.code == L.KMC_ERR_STATE
+    with pytest.raises(L.KmcError) as ex:
+        e.mlp_params()
+    assert ex.value.code == L.KMC_ERR_STATE
     e.mlp_init(4, D_MIN, D_MAX, 0.0, 1.0, 0)
     s = SG.draw_samples(SG.species_model(), 1000, seed=6)
     with pytest.raises(L.KmcError) as ex:

@@ -137,3 +137,19 @@ def test_samples_are_reproducible_and_cover_the_pairs():
     assert np.all(a["pair"] == a["donor"] * 4 + a["acceptor"])
     assert a["dist"].min() >= SG.D_RANGE[0] and a["dist"].max() <= SG.D_RANGE[1]
     assert a["theta"].min() >= 0 and a["theta"].max() <= math.pi / 2
+
+
+def test_surrogate_calls_fail_loudly_without_a_device_or_network():
+    # without a GPU the context cannot be created; with one, reading parameters before
+    # kmc_mlp_init is a state error (checked on the GPU in test_gpu_surrogate)
+    import ctypes as C
+
+    lib = L.load()
+    st = C.c_int(0)
+    h = lib.kmc_create(0, C.byref(st))
+    if h:
+        lib.kmc_destroy(h)
+        pytest.skip("a CUDA device is present")
+    assert st.value == L.KMC_ERR_NO_DEVICE
+    with pytest.raises(L.KmcError):
+        E.Engine(0)
