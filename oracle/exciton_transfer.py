@@ -1,0 +1,134 @@
+"""CPU oracle for exciton_transfer's Coulomb sum -- TEST INFRASTRUCTURE ONLY.
+
+Only the tests use this module, to check future device kernels; the product never calls it.
+
+What it restates (reference project paths):
+
+* ``cnt_geometry``: ``cnt::get_parameters`` (src/exciton_transfer/cnt.cpp:16-60, 81-86) and
+  ``cnt::get_atom_coordinates`` (cnt.cpp:120-210).  The graphene lattice constant is
+  a_l = sqrt(float(3)) a_cc (cnt.h:25-26: the square root is taken in single precision), pi is
+  3.141592 (src/exciton_transfer/constants.h:10), the lattice is rotated so that the chiral
+  vector lies along x, and the unit-cell (A-atom) positions are wrapped into the chiral period.
+* ``unit_cells_3d`` / ``unit_cells_2d``: the lambdas make_Ru_3d / make_Ru_2d of
+  ``exciton_transfer::calculate_J`` (exciton_transfer.cpp:310-355): every graphene unit cell of
+  the whole tube, centred on its axis, shifted along it and in z, rotated about z.
+* ``coulomb_j``: calculate_J (exciton_transfer.cpp:357-377),
+  J = sum_i sum_j exp(-i k_i . r_i) exp(+i k_f . r_j) / |R_i - R_j|.
+
+Parity: unpinned against the reference.  cnt.cpp and exciton_transfer.cpp need Armadillo's
+complex matrices, cubes, fields and eig_sym, which the shim behind the oracle's other parts does
+not provide.  The tests check tube-geometry invariants, a brute-force double loop, far-field
+and conjugation identities instead.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+A_CC = 1.42e-10                               # carbon-carbon distance, m (cnt.h:25)
+A_L = float(np.sqrt(np.float32(3.0))) * A_CC  # cnt.h:26: std::sqrt(float(3.0)) * a_cc
+PI = 3.141592                                 # constants.h:10
+
+
+def cnt_geometry(n: int, m: int, n_cells: int) -> dict:
+    """Lattice vectors (rotated frame), radius, translation vector, the Nu unit-cell positions in
+    the unrolled sheet and on the cylinder, and the axial k step dk_l = K2 / n_cells."""
+    s3 = math.sqrt(3.0)
+    a1 = np.array([A_L * s3 / 2.0, +A_L / 2.0])
+    a2 = np.array([A_L * s3 / 2.0, -A_L / 2.0])
+    b1 = np.array([1.0 / math.sqrt(3.0) * 2.0 * PI / A_L, +2.0 * PI / A_L])
+    b2 = np.array([1.0 / math.sqrt(3.0) * 2.0 * PI / A_L, -2.0 * PI / A_L])
+    acc = 1.0 / 3.0 * (a1 + a2)
+    ch = float(n) * a1 + float(m) * a2
+    ch_len = float(np.linalg.norm(ch))
+    radius = ch_len / 2.0 / PI
+    dR = math.gcd(2 * n + m, n + 2 * m)
+    t1 = (2 * m + n) // dR
+    t2 = -(2 * n + m) // dR
+    tv = float(t1) * a1 + float(t2) * a2
+    Nu = int(2 * (n * n + m * m + n * m) / dR)
+    c = ch[0] / np.linalg.norm(ch)
+    s = ch[1] / np.linalg.norm(ch)
+
+    def rot(v):  # [[c, s], [-s, c]] v
+        return np.array([c * v[0] + s * v[1], -s * v[0] + c * v[1]])
+
+    ch, tv, a1, a2, b1, b2, acc = (rot(v) for v in (ch, tv, a1, a2, b1, b2, acc))
+    t3 = np.array([0.0, tv[1], 0.0])
+    K2 = (float(m) * b1 - float(n) * b2) / float(Nu)
+    dk_l = K2 / float(n_cells)
+    # unit-cell (A-atom) positions inside the chiral period
+    pos_a = []
+    for i in range(0, t1 + n + 1):
+        for j in range(t2, m + 1):
+            f1 = (t2 * i) / t1 <= j
+            f2 = (m * i) / n >= j
+            f3 = (t2 * (i - n)) / t1 > (j - m)
+            f4 = (m * (i - t1)) / n < (j - t2)
+            if f1 and f2 and f3 and f4:
+                p = float(i) * a1 + float(j) * a2
+                for d in range(2):
+                    if p[d] > ch[d]:
+                        p[d] -= ch[d]
+                    if p[d] < 0.0:
+                        p[d] += ch[d]
+                pos_a.append(p)
+    pos_a = np.array(pos_a)
+    if len(pos_a) != Nu:
+        raise ValueError(f"({n},{m}): found {len(pos_a)} unit cells, expected {Nu}")
+    pos3 = np.stack([radius * np.cos(pos_a[:, 0] / radius), pos_a[:, 1], radius * np.sin(pos_a[:, 0] / radius)], 1)
+    return {"n": n, "m": m, "a1": a1, "a2": a2, "acc": acc, "ch": ch, "ch_len": ch_len, "radius": radius, "t_vec": tv,
+            "t_vec_3d": t3, "Nu": Nu, "t1": t1, "t2": t2, "dR": dR, "pos_u_2d": pos_a, "pos_u_3d": pos3,
+            "dk_l": dk_l, "n_cells": n_cells}
+
+
+def unit_cells_3d(g: dict, shift_along_axis: float, z_shift: float, angle: float) -> np.ndarray:
+    """make_Ru_3d: all unit cells of the tube, centred in y, shifted, rotated about z."""
+    cells = np.concatenate([g["pos_u_3d"] + i * g["t_vec_3d"] for i in range(g["n_cells"])])
+    y_max, y_min = cells[:, 1].max(), cells[:, 1].min()
+    cells[:, 1] -= (y_max + y_min) / 2.0
+    cells[:, 1] += shift_along_axis
+    cells[:, 2] += z_shift
+    x = cells[:, 0] * math.cos(angle) - cells[:, 1] * math.sin(angle)
+    y = cells[:, 0] * math.sin(angle) + cells[:, 1] * math.cos(angle)
+    cells[:, 0], cells[:, 1] = x, y
+    return cells
+
+
+def unit_cells_2d(g: dict) -> np.ndarray:
+    """make_Ru_2d: all unit cells of the tube in the unrolled sheet."""
+    return np.concatenate([g["pos_u_2d"] + i * g["t_vec"] for i in range(g["n_cells"])])
+
+
+def coulomb_j(gi: dict, gf: dict, ik_i: int, ik_f: int, shifts=(0.0, 0.0), z_shift: float = 0.0,
+              angle: float = 0.0, block: int = 4096) -> complex:
+    """calculate_J for the centre-of-mass momenta ik_i dk_l(i) and ik_f dk_l(f)."""
+    Ri = unit_cells_3d(gi, shifts[0], 0.0, 0.0)
+    Rf = unit_cells_3d(gf, shifts[1], z_shift, angle)
+    ki = ik_i * gi["dk_l"]
+    kf = ik_f * gf["dk_l"]
+    ei = np.exp(-1j * (unit_cells_2d(gi) @ ki))
+    ef = np.exp(+1j * (unit_cells_2d(gf) @ kf))
+    J = 0j
+    for a in range(0, len(Ri), block):
+        d = np.linalg.norm(Ri[a:a + block, None, :] - Rf[None, :, :], axis=2)
+        J += complex(ei[a:a + block] @ (ef[None, :] / d).sum(axis=1))
+    return J
+
+
+def coulomb_j_loops(gi: dict, gf: dict, ik_i: int, ik_f: int, shifts=(0.0, 0.0), z_shift: float = 0.0,
+                    angle: float = 0.0) -> complex:
+    """The double loop of calculate_J as written (small tubes only)."""
+    Ri = unit_cells_3d(gi, shifts[0], 0.0, 0.0)
+    Rf = unit_cells_3d(gf, shifts[1], z_shift, angle)
+    ri, rf = unit_cells_2d(gi), unit_cells_2d(gf)
+    ki = ik_i * gi["dk_l"]
+    kf = ik_f * gf["dk_l"]
+    f_exp = [complex(np.exp(+1j * float(kf @ rf[j]))) for j in range(len(rf))]
+    J = 0j
+    for i in range(len(ri)):
+        i_exp = complex(np.exp(-1j * float(ki @ ri[i])))
+        for j in range(len(rf)):
+            J += i_exp * f_exp[j] / float(np.linalg.norm(Ri[i] - Rf[j]))
+    return J

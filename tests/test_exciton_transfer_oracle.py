@@ -1,0 +1,86 @@
+"""The CPU restatement of exciton_transfer's tube geometry and Coulomb sum (oracle/
+exciton_transfer.py), which future device kernels for the labeller are checked against.  The
+reference's own code cannot be compiled here (it needs Armadillo's complex types and eig_sym), so
+the restatement is checked against the tube-geometry closed forms (Saito, Dresselhaus &
+Dresselhaus), the calculate_J double loop as written, and identities of the sum."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import exciton_transfer as X
+
+CHIRALITIES = [(6, 5), (7, 5), (8, 3), (8, 4), (10, 0), (5, 5)]
+
+
+@pytest.mark.parametrize("n,m", CHIRALITIES)
+def test_tube_geometry_closed_forms(n, m):
+    g = X.cnt_geometry(n, m, 2)
+    dR = math.gcd(2 * n + m, 2 * m + n)
+    assert g["Nu"] == 2 * (n * n + n * m + m * m) // dR
+    ch_len = X.A_L * math.sqrt(n * n + n * m + m * m)
+    assert g["ch_len"] == pytest.approx(ch_len, rel=1e-12)
+    assert np.linalg.norm(g["t_vec"]) == pytest.approx(math.sqrt(3) * ch_len / dR, rel=1e-12)
+    assert g["radius"] == pytest.approx(ch_len / (2 * 3.141592), rel=1e-15)
+    # the rotated frame: chiral vector along x, translation vector along y
+    assert abs(g["ch"][1]) < 1e-15 * ch_len and abs(g["t_vec"][0]) < 1e-15 * ch_len
+    # unit cells inside one period, on the cylinder
+    p = g["pos_u_2d"]
+    assert p[:, 0].min() >= 0 and p[:, 0].max() <= g["ch"][0]
+    assert p[:, 1].min() >= 0 and p[:, 1].max() <= g["t_vec"][1]
+    q = g["pos_u_3d"]
+    np.testing.assert_allclose(np.hypot(q[:, 0], q[:, 2]), g["radius"], rtol=1e-14)
+
+
+@pytest.mark.parametrize("n,m", CHIRALITIES)
+def test_unit_cells_form_the_graphene_lattice(n, m):
+    # every A atom's nearest A neighbours (periodic images across the chiral and translation
+    # periods included) sit one lattice constant away, and no two unit cells coincide
+    g = X.cnt_geometry(n, m, 1)
+    p = g["pos_u_2d"]
+    ch, tv = g["ch"], g["t_vec"]
+    images = np.concatenate([p + a * ch + b * tv for a in (-1, 0, 1) for b in (-1, 0, 1)])
+    d = np.linalg.norm(p[:, None, :] - images[None, :, :], axis=2)
+    d[d < 1e-3 * X.A_L] = np.inf  # the atom itself
+    np.testing.assert_allclose(d.min(axis=1), X.A_L, rtol=1e-9)
+    assert np.all((d < 0.999 * X.A_L).sum(axis=1) == 0)
+    # and the A-B bond is a_cc
+    assert np.linalg.norm(g["acc"]) == pytest.approx(X.A_L / math.sqrt(3), rel=1e-12)
+
+
+def test_lattice_constant_keeps_the_single_precision_square_root():
+    # cnt.h:26 takes sqrt(float(3.0)): the lattice constant differs from sqrt(3) a_cc in the 8th digit
+    assert X.A_L == float(np.float32(math.sqrt(3.0))) * 1.42e-10
+    assert abs(X.A_L / (math.sqrt(3) * 1.42e-10) - 1) > 1e-9
+
+
+def small_pair():
+    return X.cnt_geometry(5, 0, 3), X.cnt_geometry(5, 5, 4)
+
+
+def test_coulomb_sum_equals_the_double_loop():
+    gi, gf = small_pair()
+    for ik_i, ik_f, shifts, z, ang in [(0, 0, (0.0, 0.0), 2e-9, 0.0), (1, -2, (1e-10, -3e-10), 1.5e-9, 0.7),
+                                       (3, 2, (0.0, 5e-10), 3e-9, 1.9)]:
+        a = X.coulomb_j(gi, gf, ik_i, ik_f, shifts, z, ang, block=7)
+        b = X.coulomb_j_loops(gi, gf, ik_i, ik_f, shifts, z, ang)
+        assert abs(a - b) <= 1e-12 * abs(b)
+
+
+def test_coulomb_sum_identities():
+    gi, gf = small_pair()
+    # real kernel 1/|R|: flipping both momenta conjugates J
+    a = X.coulomb_j(gi, gf, 2, -1, (0.0, 0.0), 2e-9, 0.4)
+    b = X.coulomb_j(gi, gf, -2, 1, (0.0, 0.0), 2e-9, 0.4)
+    assert abs(a - b.conjugate()) <= 1e-12 * abs(a)
+    # zero momenta: a sum of positive terms
+    c = X.coulomb_j(gi, gf, 0, 0, (0.0, 0.0), 2e-9, 0.4)
+    assert abs(c.imag) < 1e-12 * c.real and c.real > 0
+    # far field at zero momenta: N_i N_f / separation (the tubes are ~2 nm long, 1 um apart)
+    z = 1e-6
+    far = X.coulomb_j(gi, gf, 0, 0, (0.0, 0.0), z, 0.3)
+    n_i, n_f = len(X.unit_cells_2d(gi)), len(X.unit_cells_2d(gf))
+    assert far.real == pytest.approx(n_i * n_f / z, rel=1e-5) and abs(far.imag) < 1e-12 * far.real
+    # at nonzero momenta a whole tube's phases cancel, so the monopole term vanishes
+    ei = np.exp(-1j * (X.unit_cells_2d(gi) @ (1 * gi["dk_l"]))).sum()
+    assert abs(ei) < 1e-6 * n_i
