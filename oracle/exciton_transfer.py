@@ -1,4 +1,4 @@
-"""CPU oracle for exciton_transfer's Coulomb sum -- TEST INFRASTRUCTURE ONLY.
+"""CPU oracle for exciton_transfer's tube geometry, bands and Coulomb sum -- TEST INFRASTRUCTURE ONLY.
 
 Only the tests use this module, to check future device kernels; the product never calls it.
 
@@ -14,11 +14,15 @@ What it restates (reference project paths):
   the whole tube, centred on its axis, shifted along it and in z, rotated about z.
 * ``coulomb_j``: calculate_J (exciton_transfer.cpp:357-377),
   J = sum_i sum_j exp(-i k_i . r_i) exp(+i k_f . r_j) / |R_i - R_j|.
+* ``electron_bands``: cnt::electron_full_unit_cell (cnt.cpp:212-292), the nearest-neighbour
+  tight-binding bands of the full tube unit cell; ``zone_folded_bands`` is the closed form it
+  must equal (graphene bands on the tube's cutting lines).
 
 Parity: unpinned against the reference.  cnt.cpp and exciton_transfer.cpp need Armadillo's
 complex matrices, cubes, fields and eig_sym, which the shim behind the oracle's other parts does
 not provide.  The tests check tube-geometry invariants, a brute-force double loop, far-field
-and conjugation identities instead.
+and conjugation identities, and the bands against zone-folded graphene (to rounding with an
+exact pi; the reference's pi = 3.141592 moves them by ~1e-5 t0) instead.
 """
 from __future__ import annotations
 
@@ -58,8 +62,18 @@ def cnt_geometry(n: int, m: int, n_cells: int) -> dict:
     t3 = np.array([0.0, tv[1], 0.0])
     K2 = (float(m) * b1 - float(n) * b2) / float(Nu)
     dk_l = K2 / float(n_cells)
-    # unit-cell (A-atom) positions inside the chiral period
-    pos_a = []
+    K1 = (-float(t2) * b1 + float(t1) * b2) / float(Nu)
+    # unit-cell (A-atom) and B-atom positions inside the chiral period
+    pos_a, pos_b = [], []
+
+    def wrap(p):
+        for d in range(2):
+            if p[d] > ch[d]:
+                p[d] -= ch[d]
+            if p[d] < 0.0:
+                p[d] += ch[d]
+        return p
+
     for i in range(0, t1 + n + 1):
         for j in range(t2, m + 1):
             f1 = (t2 * i) / t1 <= j
@@ -68,19 +82,79 @@ def cnt_geometry(n: int, m: int, n_cells: int) -> dict:
             f4 = (m * (i - t1)) / n < (j - t2)
             if f1 and f2 and f3 and f4:
                 p = float(i) * a1 + float(j) * a2
-                for d in range(2):
-                    if p[d] > ch[d]:
-                        p[d] -= ch[d]
-                    if p[d] < 0.0:
-                        p[d] += ch[d]
-                pos_a.append(p)
-    pos_a = np.array(pos_a)
+                q = p + acc
+                pos_a.append(wrap(p))
+                pos_b.append(wrap(q))
+    pos_a, pos_b = np.array(pos_a), np.array(pos_b)
     if len(pos_a) != Nu:
         raise ValueError(f"({n},{m}): found {len(pos_a)} unit cells, expected {Nu}")
-    pos3 = np.stack([radius * np.cos(pos_a[:, 0] / radius), pos_a[:, 1], radius * np.sin(pos_a[:, 0] / radius)], 1)
-    return {"n": n, "m": m, "a1": a1, "a2": a2, "acc": acc, "ch": ch, "ch_len": ch_len, "radius": radius, "t_vec": tv,
-            "t_vec_3d": t3, "Nu": Nu, "t1": t1, "t2": t2, "dR": dR, "pos_u_2d": pos_a, "pos_u_3d": pos3,
-            "dk_l": dk_l, "n_cells": n_cells}
+
+    def roll(p2):
+        return np.stack([radius * np.cos(p2[:, 0] / radius), p2[:, 1], radius * np.sin(p2[:, 0] / radius)], 1)
+
+    pos_2d = np.concatenate([pos_a, pos_b])
+    return {"n": n, "m": m, "a1": a1, "a2": a2, "b1": b1, "b2": b2, "acc": acc, "ch": ch, "ch_len": ch_len,
+            "radius": radius, "t_vec": tv, "t_vec_3d": t3, "Nu": Nu, "t1": t1, "t2": t2, "dR": dR, "K1": K1, "K2": K2,
+            "pos_u_2d": pos_a, "pos_u_3d": roll(pos_a), "pos_2d": pos_2d, "pos_3d": roll(pos_2d), "dk_l": dk_l,
+            "n_cells": n_cells}
+
+
+EV = 1.6e-19       # constants.h:12
+T0 = 2.7 * EV      # nearest-neighbour hopping, cnt.h:29 (on-site e2p = 0, overlap s0 = 0)
+
+
+def electron_bands(g: dict, vectors: bool = False):
+    """cnt::electron_full_unit_cell (cnt.cpp:212-292): the 2Nu x 2Nu nearest-neighbour
+    tight-binding Hamiltonian of one tube unit cell with Bloch phases exp(i k l T) across the
+    translation period, at k = (n - nk/2) |dk_l| for n < nk = number of unit cells; energies
+    ascending [2Nu][nk] (J) and, with vectors, eigenvectors [nk][2Nu][2Nu] with the reference's
+    phase fix (first component real and non-negative)."""
+    p = g["pos_3d"]
+    t3 = g["t_vec_3d"]
+    N2 = len(p)
+    nn = []
+    for i in range(N2):
+        row = []
+        for j in range(N2):
+            for l in (-1, 0, 1):
+                dR = np.linalg.norm(p[i] - p[j] + float(l) * t3)
+                if i != j and dR < 1.4 * A_CC:
+                    row.append((j, l))
+        if len(row) != 3:
+            raise ValueError(f"atom {i}: {len(row)} nearest neighbours")
+        nn.append(row)
+    nk = g["n_cells"]
+    t_len = float(np.linalg.norm(t3))
+    dk = float(np.linalg.norm(g["dk_l"]))
+    E = np.zeros((N2, nk))
+    C = np.zeros((nk, N2, N2), complex) if vectors else None
+    for n in range(nk):
+        wave_vec = float(n - nk // 2) * dk
+        H = np.zeros((N2, N2), complex)
+        for i in range(N2):
+            for j, l in nn[i]:
+                H[i, j] += T0 * np.exp(1j * wave_vec * float(l) * t_len)
+        e, c = np.linalg.eigh(H)
+        E[:, n] = e
+        if vectors:
+            phi = np.conj(c[0, :]) / np.abs(c[0, :])
+            C[n] = c * phi[None, :]
+    return (E, C) if vectors else E
+
+
+def zone_folded_bands(g: dict) -> np.ndarray:
+    """Nearest-neighbour graphene bands +-t0 |1 + exp(i k.a1) + exp(i k.a2)| on the tube's
+    cutting lines k = mu K1 + kappa K2/|K2| (mu < Nu), at the axial momenta of electron_bands."""
+    nk = g["n_cells"]
+    dk = float(np.linalg.norm(g["dk_l"]))
+    K2h = g["K2"] / np.linalg.norm(g["K2"])
+    out = np.zeros((2 * g["Nu"], nk))
+    for n in range(nk):
+        kappa = float(n - nk // 2) * dk
+        ks = np.arange(g["Nu"])[:, None] * g["K1"][None, :] + kappa * K2h[None, :]
+        f = np.abs(1 + np.exp(1j * (ks @ g["a1"])) + np.exp(1j * (ks @ g["a2"])))
+        out[:, n] = np.sort(np.concatenate([-T0 * f, T0 * f]))
+    return out
 
 
 def unit_cells_3d(g: dict, shift_along_axis: float, z_shift: float, angle: float) -> np.ndarray:

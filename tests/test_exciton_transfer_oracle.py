@@ -84,3 +84,35 @@ def test_coulomb_sum_identities():
     # at nonzero momenta a whole tube's phases cancel, so the monopole term vanishes
     ei = np.exp(-1j * (X.unit_cells_2d(gi) @ (1 * gi["dk_l"]))).sum()
     assert abs(ei) < 1e-6 * n_i
+
+
+@pytest.mark.parametrize("n,m,nk", [(5, 5, 6), (10, 0, 9), (7, 5, 12), (8, 4, 30)])
+def test_tight_binding_bands_are_zone_folded_graphene(n, m, nk, monkeypatch):
+    # with pi exact, the tube Hamiltonian's eigenvalues are graphene's nearest-neighbour bands on
+    # the tube's cutting lines to rounding
+    monkeypatch.setattr(X, "PI", math.pi)
+    g = X.cnt_geometry(n, m, nk)
+    np.testing.assert_allclose(X.electron_bands(g), X.zone_folded_bands(g), rtol=0, atol=1e-12 * X.T0)
+
+
+def test_reference_pi_shifts_the_bands_slightly():
+    # exciton_transfer's pi = 3.141592 enters the reciprocal vectors, so b.a != 2 pi and the
+    # axial momenta sit 2e-7 off the Brillouin-zone grid: bands move by ~1e-5 t0
+    g = X.cnt_geometry(7, 5, 12)
+    d = np.abs(X.electron_bands(g) - X.zone_folded_bands(g)).max() / X.T0
+    assert 1e-8 < d < 1e-4
+
+
+def test_band_gaps_and_eigenvector_phases():
+    # armchair (5,5) is metallic (a k point of a 6-cell grid hits the Dirac point), (7,5) has
+    # E11 ~ 2 t0 a_cc / d = 0.94 eV
+    g = X.cnt_geometry(5, 5, 6)
+    assert np.abs(X.electron_bands(g)).min() < 1e-5 * X.EV
+    g = X.cnt_geometry(7, 5, 60)
+    gap = 2 * np.abs(X.electron_bands(g)).min() / X.EV
+    assert 0.9 < gap < 1.0
+    E, C = X.electron_bands(X.cnt_geometry(5, 0, 4), vectors=True)
+    first = C[:, 0, :]
+    assert np.all(np.abs(first.imag) < 1e-12) and np.all(first.real >= 0)
+    for k in range(C.shape[0]):
+        np.testing.assert_allclose(C[k].conj().T @ C[k], np.eye(C.shape[1]), atol=1e-12)
