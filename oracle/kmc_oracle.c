@@ -90,7 +90,8 @@ void orc_forster_table(double gamma_0, const double th_deg[3], const double zsh[
 }
 
 /* get_rate, scattering_struct.h:38-52 (and the 2-D (distance, theta) extension) */
-static inline double table_rate(const orc_table* t, double th, double zsh, double a1, double a2, double dist) {
+static inline double table_rate(const orc_table* t, double th, double zsh, double a1, double a2, double dist,
+                                int64_t pair_off) {
   if (t->kind == 4) {
     int i0 = orc_index_min_export(t->grid[0], t->n[0], th);
     int i1 = orc_index_min_export(t->grid[1], t->n[1], zsh);
@@ -100,7 +101,7 @@ static inline double table_rate(const orc_table* t, double th, double zsh, doubl
   }
   int i0 = orc_index_min_export(t->grid[0], t->n[0], dist);
   int i1 = orc_index_min_export(t->grid[1], t->n[1], th);
-  return t->rate[(int64_t)i0 * t->n[1] + i1];
+  return t->rate[pair_off + (int64_t)i0 * t->n[1] + i1];
 }
 
 /* ---------------------------------------------------------------- trim */
@@ -255,6 +256,7 @@ struct orc_sim {
   int32_t *left, *right;
   orc_table tab;
   double* tab_store;
+  int32_t* species_store; /* kind-3 tables: chirality of each site */
   double r_max, v;
   int n_threads;
   double mn[3], mx[3];
@@ -354,7 +356,7 @@ int orc_find_neighbors(const orc_sim* s, int64_t site, double* cum, int32_t* col
         const double* a2 = s->orient + 3 * (int64_t)j;
         double cosT = v3_dot(a1, a2);
         double theta, ash1, ash2, zsh;
-        if (s->tab.kind == 2) {
+        if (s->tab.kind != 4) { /* 2-D tables: folded angle */
           double ac = fabs(cosT);
           theta = ac >= 1.0 ? 0.0 : orc_acos(ac);
           ash1 = ash2 = zsh = 0;
@@ -376,7 +378,11 @@ int orc_find_neighbors(const orc_sim* s, int64_t site, double* cum, int32_t* col
           for (int c3 = 0; c3 < 3; ++c3) w[c3] = (ash1 * a1[c3] + p1[c3]) - (ash2 * a2[c3] + p2[c3]);
           zsh = v3_norm(w);
         }
-        double rate = table_rate(&s->tab, theta, zsh, ash1, ash2, distance);
+        const int64_t pair_off =
+            s->tab.kind == 3
+                ? ((int64_t)s->tab.species[site] * s->tab.n[2] + s->tab.species[j]) * ((int64_t)s->tab.n[0] * s->tab.n[1])
+                : 0;
+        double rate = table_rate(&s->tab, theta, zsh, ash1, ash2, distance, pair_off);
         if (k < cap) {
           cum[k] = rate;
           col[k] = j;
@@ -412,6 +418,11 @@ orc_sim* orc_sim_create(int64_t n_sites, const double* pos, const double* orient
                         const int32_t* right, const orc_table* table, double r_max, double velocity,
                         int n_threads) {
   if (n_sites <= 0) return NULL;
+  if (table->kind == 3) {
+    if (!table->species || table->n[2] < 1) return NULL;
+    for (int64_t i = 0; i < n_sites; ++i)
+      if (table->species[i] < 0 || table->species[i] >= table->n[2]) return NULL;
+  }
   orc_sim* s = (orc_sim*)calloc(1, sizeof(orc_sim));
   s->n = n_sites;
   s->pos = (double*)malloc(sizeof(double) * 3 * n_sites);
@@ -427,7 +438,7 @@ orc_sim* orc_sim_create(int64_t n_sites, const double* pos, const double* orient
   s->n_threads = n_threads > 0 ? n_threads : 1;
   /* copy the table */
   s->tab = *table;
-  int64_t nr = 1, ng = 0;
+  int64_t nr = table->kind == 3 ? (int64_t)table->n[2] * table->n[2] : 1, ng = 0;
   int dims = table->kind == 4 ? 4 : 2;
   for (int d = 0; d < dims; ++d) {
     nr *= table->n[d];
@@ -442,6 +453,13 @@ orc_sim* orc_sim_create(int64_t n_sites, const double* pos, const double* orient
   }
   memcpy(w, table->rate, sizeof(double) * nr);
   s->tab.rate = w;
+  s->species_store = NULL;
+  s->tab.species = NULL;
+  if (table->kind == 3) {
+    s->species_store = (int32_t*)malloc(sizeof(int32_t) * n_sites);
+    memcpy(s->species_store, table->species, sizeof(int32_t) * n_sites);
+    s->tab.species = s->species_store;
+  }
   domain_of(s, s->mn, s->mx);
   build_buckets(s);
   /* set_max_rate, monte_carlo.h:426-440 / scatterer.h:89-93.  An empty list is undefined
@@ -770,6 +788,7 @@ void orc_sim_destroy(orc_sim* s) {
   free(s->left);
   free(s->right);
   free(s->tab_store);
+  free(s->species_store);
   free(s->cell_start);
   free(s->cell_members);
   free(s->close_cells);

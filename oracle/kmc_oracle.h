@@ -22,12 +22,16 @@ extern "C" {
 
 /* Rate table.  kind 4: rate(theta)(z_shift, axis_shift_1, axis_shift_2) of
  * src/monte_carlo/scattering_struct.h:38-52, stored [n0][n1][n2][n3] row-major.
- * kind 2: rate(distance, theta_folded), stored [n0][n1] row-major. */
+ * kind 2: rate(distance, theta_folded), stored [n0][n1] row-major.
+ * kind 3 (mixed-chirality films, no counterpart in the reference): one kind-2 table per
+ * (donor, acceptor) chirality pair, n[2] = chiralities S, stored [S][S][n0][n1]; species[site]
+ * gives each site's chirality (NULL for the other kinds). */
 typedef struct {
   int kind;
   int n[4];
   const double* grid[4];
   const double* rate;
+  const int32_t* species;
 } orc_table;
 
 typedef struct orc_sim orc_sim;

@@ -33,7 +33,8 @@ PU32 = C.POINTER(C.c_uint32)
 
 
 class orc_table(C.Structure):
-    _fields_ = [("kind", C.c_int), ("n", C.c_int * 4), ("grid", PD * 4), ("rate", PD)]
+    _fields_ = [("kind", C.c_int), ("n", C.c_int * 4), ("grid", PD * 4), ("rate", PD),
+                ("species", C.POINTER(C.c_int32))]
 
 
 def build(ref: bool = False) -> None:
@@ -177,7 +178,9 @@ def trim(pos, orient, left, right, lim):
 class Sim:
     """The oracle engine over one film (positions in metres, [n][3])."""
 
-    def __init__(self, pos_m, orient, left, right, table, r_max, velocity, n_threads=1):
+    def __init__(self, pos_m, orient, left, right, table, r_max, velocity, n_threads=1, species=None):
+        """``table`` as the engine takes it; kind 3 (one 2-D table per chirality pair, rate
+        [S][S][n_dist][n_theta]) also needs ``species`` (each site's chirality)."""
         self.pos = np.ascontiguousarray(pos_m, dtype=np.float64)
         self.orient = np.ascontiguousarray(orient, dtype=np.float64)
         self.left = np.ascontiguousarray(left, dtype=np.int32)
@@ -191,6 +194,10 @@ class Sim:
             t.n[d] = len(g)
             t.grid[d] = _p(g, D)
         t.rate = _p(self._rate, D)
+        if table["kind"] == 3:
+            self._species = np.ascontiguousarray(species, dtype=np.int32)
+            t.n[2] = self._rate.shape[0]
+            t.species = _p(self._species, C.c_int32)
         self._t = t
         self.h = lib().orc_sim_create(self.n, _p(self.pos, D), _p(self.orient, D), _p(self.left, C.c_int32),
                                       _p(self.right, C.c_int32), C.byref(t), r_max, velocity, n_threads)

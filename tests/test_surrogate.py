@@ -153,3 +153,55 @@ def test_surrogate_calls_fail_loudly_without_a_device_or_network():
     assert st.value == L.KMC_ERR_NO_DEVICE
     with pytest.raises(L.KmcError):
         E.Engine(0)
+
+
+def mixed_film(seed=3, n_tubes=30, length=25.0, box=(50.0, 50.0, 8.0), S=4):
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    f = F.straight_tubes(n_tubes, length, box, 5.0, 1.0, seed)
+    return f, SG.site_species(f, np.random.default_rng(seed).integers(0, S, n_tubes))
+
+
+def test_oracle_species_tables_are_exact_sums():
+    # the oracle's chirality-pair rows: with an index-valued 2-D table the row differences give
+    # each entry's grid cell exactly; the pair-table row is then the FP64 running sum of the
+    # pair tables' values in list order (find_neighbors, scatterer.cpp:78-80)
+    from oracle import oracle as O
+
+    f, sp = mixed_film()
+    dist, theta = SG.grids(30, 21)
+    nd, nt = len(dist), len(theta)
+    idx = {"kind": 2, "grids": [dist, theta], "rate": np.arange(1, nd * nt + 1, dtype=np.float64).reshape(nd, nt)}
+    ci = O.Sim(f.pos_m(), f.orient, f.left, f.right, idx, 10e-9, 2e5).build_csr()
+    lab = SG.labeller_table(SG.species_model(), dist, theta)
+    cs = O.Sim(f.pos_m(), f.orient, f.left, f.right, lab, 10e-9, 2e5, species=sp).build_csr()
+    assert np.array_equal(cs["rowptr"], ci["rowptr"]) and np.array_equal(cs["col"], ci["col"])
+    flat = lab["rate"].reshape(4, 4, nd * nt)
+    for s in range(f.n_sites):
+        r0, r1 = ci["rowptr"][s], ci["rowptr"][s + 1]
+        cells = np.diff(np.concatenate([[0.0], ci["cum"][r0:r1]])).astype(np.int64) - 1
+        run = 0.0
+        for j in range(r1 - r0):
+            v = float(flat[sp[s], sp[ci["col"][r0 + j]], cells[j]])
+            run = v if j == 0 else run + v
+            assert cs["cum"][r0 + j] == run
+        assert cs["total"][s] == (run if r1 > r0 else 0.0)
+
+
+def test_oracle_identical_pair_tables_equal_the_2d_table():
+    from oracle import oracle as O
+
+    f, sp = mixed_film(seed=5)
+    t2 = SG.single_table(SG.species_model(), *SG.grids(40, 31), species=3)
+    t3 = {"kind": 3, "grids": t2["grids"], "rate": np.broadcast_to(t2["rate"], (4, 4) + t2["rate"].shape).copy()}
+    a = O.Sim(f.pos_m(), f.orient, f.left, f.right, t3, 10e-9, 2e5, species=sp)
+    b = O.Sim(f.pos_m(), f.orient, f.left, f.right, t2, 10e-9, 2e5)
+    ca, cb = a.build_csr(), b.build_csr()
+    for k in ("rowptr", "col", "cum", "total"):
+        assert np.array_equal(ca[k], cb[k]), k
+    # same hops on both: the Green-Kubo step reads only the rows
+    for sim in (a, b):
+        sim.create_excitons(1, 0, 200, 9)
+        sim.step(1e-13, 2)
+    ea, eb = a.excitons(), b.excitons()
+    assert np.array_equal(ea["site"], eb["site"]) and a.total_hops() == b.total_hops() > 0
