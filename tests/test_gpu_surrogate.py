@@ -267,3 +267,38 @@ def test_network_tables_reproduce_the_labeller_film_diffusion(trained):
     (lab, cl), (nn, cn), (one, co) = runs["labeller"], runs["network"], runs["single"]
     assert abs(nn - lab) < 2 * np.hypot(cl, cn)
     assert abs(one - lab) > 3 * np.hypot(cl, co)
+
+
+@pytest.mark.parametrize("precision", [L.KMC_PREC_FP64, L.KMC_PREC_MIXED])
+def test_mixed_film_hops_match_oracle(precision):
+    # a mixed-chirality film on the labeller's pair tables: neighbour rows, hop sequences and
+    # exciton states bit for bit against the oracle's pair-table lookup
+    f, sp = mixed_film(seed=6)
+    tab = SG.labeller_table(SG.species_model(), *SG.grids(48, 37))
+    n_exc, seed, dt, v, steps = 400, 31, 2e-13, 2e5, 6
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, 10e-9, v, species=sp)
+    sim.set_trace(8, 1 << 18)
+    sim.create_excitons(1, 0, n_exc, seed)
+    om = sim.step(dt, steps)
+    o = sim.excitons()
+    csr = sim.build_csr()
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_species(sp, 4)
+    e.set_table(tab)
+    st = e.build(10e-9)
+    nb = e.neighbors(f.n_sites, st["nnz"])
+    assert np.array_equal(nb["col"], csr["col"]) and np.array_equal(nb["cum"], csr["cum"])
+    e.set_trace(8, 1 << 18)
+    e.init_excitons(n_exc, seed, L.KMC_INJECT_UNIFORM)
+    e.run(steps, dt, v, precision)
+    g = e.excitons()
+    for k in ("site", "pos", "delta", "ff", "heading", "draws"):
+        assert np.array_equal(g[k], o[k]), k
+    np.testing.assert_allclose(e.msd(0, steps).ravel(), np.asarray(om).ravel(), rtol=1e-12, atol=0)
+    for i in range(8):
+        a, na = e.trace(i)
+        b, nb_ = sim.trace(i)
+        assert na == nb_ and np.array_equal(a, b)
+    assert e.stats()["hops"] == sim.total_hops() > 0
+    e.close()
