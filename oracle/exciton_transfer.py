@@ -17,6 +17,8 @@ What it restates (reference project paths):
 * ``electron_bands``: cnt::electron_full_unit_cell (cnt.cpp:212-292), the nearest-neighbour
   tight-binding bands of the full tube unit cell; ``zone_folded_bands`` is the closed form it
   must equal (graphene bands on the tube's cutting lines).
+* ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-593), the Fourier sums of the Ohno
+  potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
 Parity: unpinned against the reference.  cnt.cpp and exciton_transfer.cpp need Armadillo's
 complex matrices, cubes, fields and eig_sym, which the shim behind the oracle's other parts does
@@ -155,6 +157,59 @@ def zone_folded_bands(g: dict) -> np.ndarray:
         f = np.abs(1 + np.exp(1j * (ks @ g["a1"])) + np.exp(1j * (ks @ g["a2"])))
         out[:, n] = np.sort(np.concatenate([-T0 * f, T0 * f]))
     return out
+
+
+EPS0 = 8.85e-12    # constants.h:17
+Q0 = 1.6e-19       # constants.h:18
+UPP = 11.3 * EV    # Ohno potential constant, cnt.h:32
+
+
+def vq_positions(g: dict, n_cells: int) -> np.ndarray:
+    """The relative positions of calculate_vq (cnt.cpp:532-567): atoms of each sublattice pair
+    (aa, ab, ba, bb) relative to the first A / B atom, folded once into +-ch/2 along the
+    circumference, repeated over an odd number of unit cells centred on 0: [4][Nu n][2]."""
+    if n_cells % 2 == 0:
+        n_cells += 1
+    a, b = g["pos_u_2d"], g["pos_2d"][g["Nu"]:]
+    half = g["ch"][0] / 2
+    rel = [a - a[0], a - b[0], b - a[0], b - b[0]]
+    for r in rel:
+        r[r[:, 0] > half, 0] -= g["ch"][0]
+    h = n_cells // 2
+    return np.stack([np.concatenate([r + i * g["t_vec"] for i in range(-h, h + 1)]) for r in rel])
+
+
+def calculate_vq(g: dict, iq_range, mu_range, n_cells: int) -> np.ndarray:
+    """cnt::calculate_vq (cnt.cpp:520-593): the Ohno potential U / sqrt(c |R|^2 + 1),
+    c = (4 pi eps0 U / q0^2)^2, Fourier-summed as sum_R exp(i q.R) over vq_positions for
+    q = iq dk_l + mu K1, divided by 2 Nu n: [nq][n_mu][4] complex."""
+    rel = vq_positions(g, n_cells)
+    n_eff = rel.shape[1] // g["Nu"]
+    coeff = (4. * PI * EPS0 * UPP / Q0 / Q0) ** 2
+    pot = UPP / np.sqrt(coeff * (rel[..., 0] ** 2 + rel[..., 1] ** 2) + 1)
+    out = np.zeros((iq_range[1] - iq_range[0], mu_range[1] - mu_range[0], 4), complex)
+    for a, iq in enumerate(range(*iq_range)):
+        for b, mu in enumerate(range(*mu_range)):
+            q = iq * g["dk_l"] + mu * g["K1"]
+            out[a, b] = (np.exp(1j * (rel @ q)) * pot).sum(axis=1)
+    return out / (2 * g["Nu"] * n_eff)
+
+
+def calculate_vq_loops(g: dict, iq_range, mu_range, n_cells: int) -> np.ndarray:
+    """calculate_vq's loops as written, term by term (small tubes only)."""
+    rel = vq_positions(g, n_cells)
+    n_eff = rel.shape[1] // g["Nu"]
+    coeff = (4. * PI * EPS0 * UPP / Q0 / Q0) ** 2
+    out = np.zeros((iq_range[1] - iq_range[0], mu_range[1] - mu_range[0], 4), complex)
+    for a, iq in enumerate(range(*iq_range)):
+        for b, mu in enumerate(range(*mu_range)):
+            q = iq * g["dk_l"] + mu * g["K1"]
+            for i in range(4):
+                acc = 0j
+                for R in rel[i]:
+                    acc += complex(np.exp(1j * float(q @ R))) * UPP / math.sqrt(coeff * (R[0] ** 2 + R[1] ** 2) + 1)
+                out[a, b, i] = acc
+    return out / (2 * g["Nu"] * n_eff)
 
 
 def unit_cells_3d(g: dict, shift_along_axis: float, z_shift: float, angle: float) -> np.ndarray:

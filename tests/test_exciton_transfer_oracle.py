@@ -116,3 +116,28 @@ def test_band_gaps_and_eigenvector_phases():
     assert np.all(np.abs(first.imag) < 1e-12) and np.all(first.real >= 0)
     for k in range(C.shape[0]):
         np.testing.assert_allclose(C[k].conj().T @ C[k], np.eye(C.shape[1]), atol=1e-12)
+
+
+def test_vq_equals_the_loops_as_written():
+    g = X.cnt_geometry(5, 0, 5)
+    a = X.calculate_vq(g, (-2, 3), (0, 4), 5)
+    b = X.calculate_vq_loops(g, (-2, 3), (0, 4), 5)
+    np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
+
+
+def test_vq_identities():
+    g = X.cnt_geometry(7, 5, 11)
+    v = X.calculate_vq(g, (-2, 3), (0, 3), 11)
+    # q = 0: the plain sum of the potential over each sublattice pair's positions
+    rel = X.vq_positions(g, 11)
+    coeff = (4. * X.PI * X.EPS0 * X.UPP / X.Q0 / X.Q0) ** 2
+    pot = X.UPP / np.sqrt(coeff * (rel[..., 0] ** 2 + rel[..., 1] ** 2) + 1)
+    q0 = v[2, 0]  # iq = 0, mu = 0
+    np.testing.assert_allclose(q0.real, pot.sum(axis=1) / (2 * g["Nu"] * 11), rtol=1e-12)
+    assert np.all(q0.imag == 0)
+    # same-sublattice sums agree (A-A and B-B see the same lattice); A-B and B-A are mirror
+    # images, conjugate up to the one-sided fold at +-ch/2
+    np.testing.assert_allclose(v[..., 0], v[..., 3], rtol=1e-9, atol=1e-12 * np.abs(v).max())
+    assert np.abs(v[..., 1] - np.conj(v[..., 2])).max() < 1e-2 * np.abs(v).max()
+    # an even cell count is made odd, as the reference does
+    assert X.vq_positions(g, 10).shape == X.vq_positions(g, 11).shape
