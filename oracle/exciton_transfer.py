@@ -14,10 +14,10 @@ What it restates (reference project paths):
   the whole tube, centred on its axis, shifted along it and in z, rotated about z.
 * ``coulomb_j``: calculate_J (exciton_transfer.cpp:357-377),
   J = sum_i sum_j exp(-i k_i . r_i) exp(+i k_f . r_j) / |R_i - R_j|.
-* ``electron_bands``: cnt::electron_full_unit_cell (cnt.cpp:212-292), the nearest-neighbour
+* ``electron_bands``: cnt::electron_full_unit_cell (cnt.cpp:212-300), the nearest-neighbour
   tight-binding bands of the full tube unit cell; ``zone_folded_bands`` is the closed form it
   must equal (graphene bands on the tube's cutting lines).
-* ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-593), the Fourier sums of the Ohno
+* ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
   potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
 Parity: unpinned against the reference.  cnt.cpp and exciton_transfer.cpp need Armadillo's
@@ -106,7 +106,7 @@ T0 = 2.7 * EV      # nearest-neighbour hopping, cnt.h:29 (on-site e2p = 0, overl
 
 
 def electron_bands(g: dict, vectors: bool = False):
-    """cnt::electron_full_unit_cell (cnt.cpp:212-292): the 2Nu x 2Nu nearest-neighbour
+    """cnt::electron_full_unit_cell (cnt.cpp:212-300): the 2Nu x 2Nu nearest-neighbour
     tight-binding Hamiltonian of one tube unit cell with Bloch phases exp(i k l T) across the
     translation period, at k = (n - nk/2) |dk_l| for n < nk = number of unit cells; energies
     ascending [2Nu][nk] (J) and, with vectors, eigenvectors [nk][2Nu][2Nu] with the reference's
@@ -180,7 +180,7 @@ def vq_positions(g: dict, n_cells: int) -> np.ndarray:
 
 
 def calculate_vq(g: dict, iq_range, mu_range, n_cells: int) -> np.ndarray:
-    """cnt::calculate_vq (cnt.cpp:520-593): the Ohno potential U / sqrt(c |R|^2 + 1),
+    """cnt::calculate_vq (cnt.cpp:520-631): the Ohno potential U / sqrt(c |R|^2 + 1),
     c = (4 pi eps0 U / q0^2)^2, Fourier-summed as sum_R exp(i q.R) over vq_positions for
     q = iq dk_l + mu K1, divided by 2 Nu n: [nq][n_mu][4] complex."""
     rel = vq_positions(g, n_cells)
