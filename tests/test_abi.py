@@ -101,3 +101,23 @@ def test_create_without_device_fails_cleanly():
     st = C.c_int(0)
     h = L.load().kmc_create(0, C.byref(st))
     assert not h and st.value == L.KMC_ERR_NO_DEVICE
+
+
+def test_header_compiles_as_c_and_host_calls_work_from_c(tmp_path):
+    # include/cntkmc.h is a C ABI: a C99 program includes it, links libcntkmc.so and calls the
+    # host entry points
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        import pytest
+
+        pytest.skip("gcc not available")
+    pkg = os.path.join(ROOT, "cnt_film_monte_carlo_gb300")
+    exe = str(tmp_path / "abi_from_c")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_from_c.c"), "-L", pkg, "-lcntkmc", "-Wl,-rpath," + pkg, "-lm",
+                    "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    assert r.stdout.startswith("ok cntkmc")
