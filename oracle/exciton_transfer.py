@@ -17,6 +17,8 @@ What it restates (reference project paths):
 * ``electron_bands``: cnt::electron_full_unit_cell (cnt.cpp:212-300), the nearest-neighbour
   tight-binding bands of the full tube unit cell; ``zone_folded_bands`` is the closed form it
   must equal (graphene bands on the tube's cutting lines).
+* ``electron_energy`` / ``k2_extended`` / ``find_valleys``: the two-band bands of the
+  K2-extended representation and their valleys (cnt.cpp:302-410, 1061-1066).
 * ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
   potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
@@ -65,6 +67,16 @@ def cnt_geometry(n: int, m: int, n_cells: int) -> dict:
     K2 = (float(m) * b1 - float(n) * b2) / float(Nu)
     dk_l = K2 / float(n_cells)
     K1 = (-float(t2) * b1 + float(t1) * b2) / float(Nu)
+    # K2-extended representation (cnt.cpp:88-114): the first p with (1 + t2 p) divisible by t1
+    p_min = (1. / float(t1) + 1. / float(n)) / (float(m) / float(n) - float(t2) / float(t1))
+    p_max = (1. / float(t1) + float(Nu) / float(n)) / (float(m) / float(n) - float(t2) / float(t1))
+    M = Q = None
+    for pp in range(math.ceil(p_min), math.ceil(p_max)):
+        if (1 + t2 * pp) % t1 == 0:
+            qq = (1 + t2 * pp) // t1
+            M = m * pp - n * qq
+            Q = math.gcd(Nu, M)
+            break
     # unit-cell (A-atom) and B-atom positions inside the chiral period
     pos_a, pos_b = [], []
 
@@ -97,6 +109,7 @@ def cnt_geometry(n: int, m: int, n_cells: int) -> dict:
     pos_2d = np.concatenate([pos_a, pos_b])
     return {"n": n, "m": m, "a1": a1, "a2": a2, "b1": b1, "b2": b2, "acc": acc, "ch": ch, "ch_len": ch_len,
             "radius": radius, "t_vec": tv, "t_vec_3d": t3, "Nu": Nu, "t1": t1, "t2": t2, "dR": dR, "K1": K1, "K2": K2,
+            "M": M, "Q": Q,
             "pos_u_2d": pos_a, "pos_u_3d": roll(pos_a), "pos_2d": pos_2d, "pos_3d": roll(pos_2d), "dk_l": dk_l,
             "n_cells": n_cells}
 
@@ -157,6 +170,44 @@ def zone_folded_bands(g: dict) -> np.ndarray:
         f = np.abs(1 + np.exp(1j * (ks @ g["a1"])) + np.exp(1j * (ks @ g["a2"])))
         out[:, n] = np.sort(np.concatenate([-T0 * f, T0 * f]))
     return out
+
+
+def electron_energy(g: dict, ik_range, mu_range):
+    """cnt::electron_energy (cnt.cpp:302-345): two-band graphene tight binding at
+    k = mu K1 + ik dk_l, f(k) summed over the three bond vectors; energies [2][nk][n_mu]
+    (valence -t0|f|, conduction +t0|f|) and wavefunctions [n_mu][2 atoms][2 bands][nk]."""
+    a1, a2 = g["a1"], g["a2"]
+    d = [(a1 + a2) / 3., (a1 - 2. * a2) / 3., (a2 - 2. * a1) / 3.]
+    nk, n_mu = ik_range[1] - ik_range[0], mu_range[1] - mu_range[0]
+    energy = np.zeros((2, nk, n_mu))
+    wf = np.zeros((n_mu, 2, 2, nk), complex)
+    for b, mu in enumerate(range(*mu_range)):
+        for a, ik in enumerate(range(*ik_range)):
+            k = float(mu) * g["K1"] + float(ik) * g["dk_l"]
+            fk = sum(np.exp(1j * float(k @ v)) for v in d)
+            energy[1, a, b] = +T0 * abs(fk)
+            energy[0, a, b] = -T0 * abs(fk)
+            wf[b, 0, 1, a] = wf[b, 0, 0, a] = 1. / math.sqrt(2.)
+            wf[b, 1, 1, a] = -1. / math.sqrt(2.) * np.conj(fk) / abs(fk)
+            wf[b, 1, 0, a] = +1. / math.sqrt(2.) * np.conj(fk) / abs(fk)
+    return energy, wf
+
+
+def k2_extended(g: dict):
+    """The K2-extended grid of calculate_exciton_dispersion (cnt.cpp:1061-1064)."""
+    return electron_energy(g, (0, g["Nu"] // g["Q"] * g["n_cells"]), (0, g["Q"]))
+
+
+def find_valleys(energy) -> list:
+    """cnt::find_valleys (cnt.cpp:362-410): conduction-band minima along ik (periodic) on each
+    cutting line, sorted by energy and paired.  The reference sorts with std::sort, which orders
+    equal energies arbitrarily; this restatement keeps their grid order."""
+    e = energy[1]
+    nk, n_mu = e.shape
+    idx = [(ik, mu) for ik in range(nk) for mu in range(n_mu)
+           if e[ik, mu] < e[(ik - 1) % nk, mu] and e[ik, mu] < e[(ik + 1) % nk, mu]]
+    idx.sort(key=lambda v: e[v[0], v[1]])
+    return [(idx[2 * i], idx[2 * i + 1]) for i in range(len(idx) // 2)]
 
 
 EPS0 = 8.85e-12    # constants.h:17

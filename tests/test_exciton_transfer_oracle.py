@@ -141,3 +141,35 @@ def test_vq_identities():
     assert np.abs(v[..., 1] - np.conj(v[..., 2])).max() < 1e-2 * np.abs(v).max()
     # an even cell count is made odd, as the reference does
     assert X.vq_positions(g, 10).shape == X.vq_positions(g, 11).shape
+
+
+@pytest.mark.parametrize("n,m,nk", [(7, 5, 6), (8, 4, 10), (5, 5, 6), (10, 0, 5)])
+def test_k2_extended_bands_relabel_the_full_unit_cell_bands(n, m, nk, monkeypatch):
+    # the K2-extended grid (Q cutting lines x Nu/Q nk points) holds the same k points as the
+    # full-unit-cell grid (Nu lines x nk points): with pi exact, the same energies
+    monkeypatch.setattr(X, "PI", math.pi)
+    g = X.cnt_geometry(n, m, nk)
+    assert g["M"] is not None and g["Nu"] % g["Q"] == 0
+    E, _ = X.k2_extended(g)
+    np.testing.assert_allclose(np.sort(E.ravel()), np.sort(X.electron_bands(g).ravel()), rtol=0, atol=1e-11 * X.T0)
+
+
+def test_two_band_eigenpairs_and_valleys():
+    g = X.cnt_geometry(7, 5, 8)
+    E, W = X.k2_extended(g)
+    d = [(g["a1"] + g["a2"]) / 3., (g["a1"] - 2. * g["a2"]) / 3., (g["a2"] - 2. * g["a1"]) / 3.]
+    for ik in (0, 17, 555, 1743):
+        k = 0 * g["K1"] + ik * g["dk_l"]
+        f = sum(np.exp(1j * float(k @ v)) for v in d)
+        H = np.array([[0, -X.T0 * f], [-X.T0 * np.conj(f), 0]])
+        psi = W[0][:, :, ik]  # [atom][band]
+        for band in (0, 1):
+            np.testing.assert_allclose(H @ psi[:, band], E[band, ik, 0] * psi[:, band], atol=1e-12 * X.T0)
+        np.testing.assert_allclose(psi.conj().T @ psi, np.eye(2), atol=1e-14)
+    valleys = X.find_valleys(E)
+    assert valleys, "no valley"
+    (a, b) = valleys[0]
+    assert E[1][a] == pytest.approx(E[1][b], rel=1e-6)  # K and K' valleys
+    assert E[1][a] == E[1].min()
+    # E11 of (7,5) in this tight binding: 2 x the valley energy, ~0.94 eV
+    assert 0.9 < 2 * E[1].min() / X.EV < 1.0
