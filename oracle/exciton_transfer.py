@@ -19,6 +19,8 @@ What it restates (reference project paths):
   must equal (graphene bands on the tube's cutting lines).
 * ``electron_energy`` / ``k2_extended`` / ``find_valleys``: the two-band bands of the
   K2-extended representation and their valleys (cnt.cpp:302-410, 1061-1066).
+* ``calculate_polarization`` / ``calculate_dielectric``: the static polarisation of the
+  K2-extended bands and the dielectric function (cnt.cpp:634-757).
 * ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
   potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
@@ -208,6 +210,73 @@ def find_valleys(energy) -> list:
            if e[ik, mu] < e[(ik - 1) % nk, mu] and e[ik, mu] < e[(ik + 1) % nk, mu]]
     idx.sort(key=lambda v: e[v[0], v[1]])
     return [(idx[2 * i], idx[2 * i + 1]) for i in range(len(idx) // 2)]
+
+
+def _kq(g, ik, mu_k, iq, mu_q, ik_range, mu_range):
+    """get_kq of calculate_polarization (cnt.cpp:650-668): k + q wrapped into the K2-extended zone
+    (a wrap across the cutting lines moves ik by nk_K1 M)."""
+    n_mu, nk = mu_range[1] - mu_range[0], ik_range[1] - ik_range[0]
+    mu_kq = mu_k + mu_q
+    w = np.floor_divide(mu_kq - mu_range[0], n_mu)
+    mu_kq = mu_kq - w * n_mu
+    ikq = ik + iq + w * g["n_cells"] * g["M"]
+    ikq = ik_range[0] + np.mod(ikq - ik_range[0], nk)
+    return ikq, mu_kq
+
+
+def calculate_polarization(g: dict, iq_range, mu_q_range, energy, wf, ik_range, mu_range) -> np.ndarray:
+    """cnt::calculate_polarization (cnt.cpp:634-720): PI(q, mu_q) = 2 sum_{k, mu_k}
+    |<v(k)|c(k+q)>|^2 / (E_c(k+q) - E_v(k)) + |<c(k)|v(k+q)>|^2 / (E_c(k) - E_v(k+q)) over the
+    K2-extended bands (energy [2][nk][n_mu], wavefunctions [n_mu][atom][band][nk])."""
+    nk, n_mu = ik_range[1] - ik_range[0], mu_range[1] - mu_range[0]
+    ik, mu_k = np.meshgrid(np.arange(*ik_range), np.arange(*mu_range), indexing="ij")
+    ik_i, mu_i = ik - ik_range[0], mu_k - mu_range[0]
+    psi = np.transpose(wf, (0, 3, 2, 1))  # [mu][k][band][atom]
+    out = np.zeros((iq_range[1] - iq_range[0], mu_q_range[1] - mu_q_range[0]))
+    for a, iq in enumerate(range(*iq_range)):
+        for b, mu_q in enumerate(range(*mu_q_range)):
+            ikq, mu_kq = _kq(g, ik, mu_k, iq, mu_q, ik_range, mu_range)
+            kq_i, mkq_i = ikq - ik_range[0], mu_kq - mu_range[0]
+            vk, ck = psi[mu_i, ik_i, 0], psi[mu_i, ik_i, 1]
+            vkq, ckq = psi[mkq_i, kq_i, 0], psi[mkq_i, kq_i, 1]
+            t1 = np.abs((np.conj(vk) * ckq).sum(-1)) ** 2 / (energy[1, kq_i, mkq_i] - energy[0, ik_i, mu_i])
+            t2 = np.abs((np.conj(ck) * vkq).sum(-1)) ** 2 / (energy[1, ik_i, mu_i] - energy[0, kq_i, mkq_i])
+            out[a, b] = (t1 + t2).sum()
+    return 2 * out
+
+
+def calculate_polarization_loops(g: dict, iq_range, mu_q_range, energy, wf, ik_range, mu_range) -> np.ndarray:
+    """calculate_polarization's loops as written, with get_kq's while loops (small grids only)."""
+    nk, n_mu = ik_range[1] - ik_range[0], mu_range[1] - mu_range[0]
+    out = np.zeros((iq_range[1] - iq_range[0], mu_q_range[1] - mu_q_range[0]))
+    for iq in range(*iq_range):
+        for mu_q in range(*mu_q_range):
+            acc = 0.0
+            for ik in range(*ik_range):
+                for mu_k in range(*mu_range):
+                    mu_kq, ikq = mu_k + mu_q, ik + iq
+                    while mu_kq >= mu_range[1]:
+                        mu_kq -= n_mu
+                        ikq += g["n_cells"] * g["M"]
+                    while mu_kq < mu_range[0]:
+                        mu_kq += n_mu
+                        ikq -= g["n_cells"] * g["M"]
+                    while ikq >= ik_range[1]:
+                        ikq -= nk
+                    while ikq < ik_range[0]:
+                        ikq += nk
+                    a, m_ = ik - ik_range[0], mu_k - mu_range[0]
+                    c, mq = ikq - ik_range[0], mu_kq - mu_range[0]
+                    acc += abs(np.vdot(wf[m_][:, 0, a], wf[mq][:, 1, c])) ** 2 / (energy[1, c, mq] - energy[0, a, m_])
+                    acc += abs(np.vdot(wf[m_][:, 1, a], wf[mq][:, 0, c])) ** 2 / (energy[1, a, m_] - energy[0, c, mq])
+            out[iq - iq_range[0], mu_q - mu_q_range[0]] = acc
+    return 2 * out
+
+
+def calculate_dielectric(vq: np.ndarray, pi: np.ndarray) -> np.ndarray:
+    """cnt::calculate_dielectric (cnt.cpp:735-757) on matching (q, mu) grids:
+    eps = 1 + Re(mean of vq over the four sublattice pairs) PI."""
+    return 1. + np.real(vq.mean(axis=2)) * pi
 
 
 EPS0 = 8.85e-12    # constants.h:17

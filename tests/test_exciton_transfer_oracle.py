@@ -173,3 +173,39 @@ def test_two_band_eigenpairs_and_valleys():
     assert E[1][a] == E[1].min()
     # E11 of (7,5) in this tight binding: 2 x the valley energy, ~0.94 eV
     assert 0.9 < 2 * E[1].min() / X.EV < 1.0
+
+
+@pytest.mark.parametrize("n,m,cells", [(5, 5, 4), (8, 4, 2)])
+def test_polarization_equals_the_loops_and_is_symmetric(n, m, cells):
+    g = X.cnt_geometry(n, m, cells)
+    E, W = X.k2_extended(g)
+    ikr, mur = (0, g["Nu"] // g["Q"] * cells), (0, g["Q"])
+    # the q range of calculate_exciton_dispersion (cnt.cpp:1069-1070)
+    iqr, muqr = (-(ikr[1] - 1), ikr[1]), (-(mur[1] - 1), mur[1])
+    a = X.calculate_polarization(g, iqr, muqr, E, W, ikr, mur)
+    b = X.calculate_polarization_loops(g, iqr, muqr, E, W, ikr, mur)
+    # at q = 0 (same k) valence and conduction states are orthogonal and PI is rounding noise
+    # (~1e-12 against ~1e20), hence the absolute floor
+    np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
+    assert np.all(a >= 0)  # every term is a squared overlap over a positive gap
+    assert a[ikr[1] - 1, mur[1] - 1] < 1e-20 * a.max()
+    # time reversal: |f(-k)| = |f(k)|
+    np.testing.assert_allclose(a, a[::-1, ::-1], rtol=1e-10, atol=1e-12 * a.max())
+
+
+def test_dielectric_function():
+    g = X.cnt_geometry(5, 5, 3)
+    E, W = X.k2_extended(g)
+    ikr, mur = (0, g["Nu"] // g["Q"] * 3), (0, g["Q"])
+    iqr, muqr = (-(ikr[1] - 1), ikr[1]), (-(mur[1] - 1), mur[1])
+    pi = X.calculate_polarization(g, iqr, muqr, E, W, ikr, mur)
+    vq = X.calculate_vq(g, iqr, muqr, 3)
+    eps = X.calculate_dielectric(vq, pi)
+    np.testing.assert_allclose(eps, 1 + vq.real.mean(axis=2) * pi, rtol=1e-15)
+    # no interband polarisation at q = 0: eps = 1 there; the positive Ohno potential screens
+    # every other q
+    q0 = (ikr[1] - 1, mur[1] - 1)
+    assert eps[q0] == pytest.approx(1.0, abs=1e-12)
+    mask = np.ones_like(eps, bool)
+    mask[q0] = False
+    assert np.all(eps[mask] > 1.0)
