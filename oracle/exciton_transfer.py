@@ -17,8 +17,9 @@ What it restates (reference project paths):
 * ``electron_bands``: cnt::electron_full_unit_cell (cnt.cpp:212-300), the nearest-neighbour
   tight-binding bands of the full tube unit cell; ``zone_folded_bands`` is the closed form it
   must equal (graphene bands on the tube's cutting lines).
-* ``electron_energy`` / ``k2_extended`` / ``find_valleys``: the two-band bands of the
-  K2-extended representation and their valleys (cnt.cpp:302-410, 1061-1066).
+* ``electron_energy`` / ``k2_extended`` / ``find_valleys`` / ``find_relev_ik_range``: the
+  two-band bands of the K2-extended representation, their valleys and the states within an
+  energy window of each valley bottom (cnt.cpp:302-505, 1061-1066).
 * ``calculate_polarization`` / ``calculate_dielectric``: the static polarisation of the
   K2-extended bands and the dielectric function (cnt.cpp:634-757).
 * ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
@@ -210,6 +211,39 @@ def find_valleys(energy) -> list:
            if e[ik, mu] < e[(ik - 1) % nk, mu] and e[ik, mu] < e[(ik + 1) % nk, mu]]
     idx.sort(key=lambda v: e[v[0], v[1]])
     return [(idx[2 * i], idx[2 * i + 1]) for i in range(len(idx) // 2)]
+
+
+def find_relev_ik_range(energy, valley_pair, delta_energy: float, ik_range=None, mu_range=(0, 0)) -> list:
+    """cnt::find_relev_ik_range (cnt.cpp:419-505) for one valley pair: starting at each valley
+    bottom, walk outwards along its cutting line (periodic in ik) one step at a time on both
+    sides, keeping states below bottom + delta_energy, until a step keeps none; returns, per
+    valley, the (ik, mu) list in ik order around the bottom."""
+    e = energy[1]
+    nk = e.shape[0]
+    ik0 = 0 if ik_range is None else ik_range[0]
+    out = []
+    for (ikb_idx, mub_idx) in valley_pair:
+        ik_bottom, mu_bottom = ikb_idx + ik0, mub_idx + mu_range[0]
+        max_e = e[ikb_idx, mub_idx] + delta_energy
+        states = [(ik_bottom, mu_bottom)]
+        count, in_range = 0, True
+        while in_range:
+            in_range = False
+            count += 1
+            ik = ik_bottom + count
+            while ik >= ik0 + nk:
+                ik -= nk
+            if e[ik - ik0, mub_idx] < max_e:
+                states.append((ik, mu_bottom))
+                in_range = True
+            ik = ik_bottom - count
+            while ik < ik0:
+                ik += nk
+            if e[ik - ik0, mub_idx] < max_e:
+                states.insert(0, (ik, mu_bottom))
+                in_range = True
+        out.append(states)
+    return out
 
 
 def _kq(g, ik, mu_k, iq, mu_q, ik_range, mu_range):

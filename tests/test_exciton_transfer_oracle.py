@@ -209,3 +209,22 @@ def test_dielectric_function():
     mask = np.ones_like(eps, bool)
     mask[q0] = False
     assert np.all(eps[mask] > 1.0)
+
+
+def test_relevant_states_around_the_valleys():
+    # the states within 1 eV of each valley bottom (calculate_exciton_dispersion's window,
+    # cnt.cpp:1066): contiguous in ik around the bottom, all below the window, and the two
+    # equivalent valleys keep the same number of states
+    g = X.cnt_geometry(7, 5, 10)
+    E, _ = X.k2_extended(g)
+    valleys = X.find_valleys(E)
+    rel = X.find_relev_ik_range(E, valleys[0], 1.0 * X.EV)
+    nk = E.shape[1]
+    assert len(rel) == 2 and len(rel[0]) == len(rel[1]) > 1
+    for states, (ikb, mub) in zip(rel, valleys[0]):
+        iks = [ik for ik, mu in states]
+        assert all(mu == mub for _, mu in states)
+        steps = [(b - a) % nk for a, b in zip(iks, iks[1:])]
+        assert steps == [1] * len(steps)  # contiguous, wrapping across the zone edge
+        assert ikb in iks
+        assert max(E[1, ik, mub] for ik in iks) < E[1, ikb, mub] + 1.0 * X.EV
