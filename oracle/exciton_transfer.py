@@ -22,6 +22,8 @@ What it restates (reference project paths):
   energy window of each valley bottom (cnt.cpp:302-505, 1061-1066).
 * ``calculate_polarization`` / ``calculate_dielectric``: the static polarisation of the
   K2-extended bands and the dielectric function (cnt.cpp:634-757).
+* ``calculate_a_excitons``: the Bethe-Salpeter kernels and A-exciton energies
+  (cnt.cpp:783-1000).
 * ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
   potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
@@ -311,6 +313,97 @@ def calculate_dielectric(vq: np.ndarray, pi: np.ndarray) -> np.ndarray:
     """cnt::calculate_dielectric (cnt.cpp:735-757) on matching (q, mu) grids:
     eps = 1 + Re(mean of vq over the four sublattice pairs) PI."""
     return 1. + np.real(vq.mean(axis=2)) * pi
+
+
+def calculate_a_excitons(energy, wf, relev, vq, vq_ranges, eps, ik_cm_range, ik_range, mu_range) -> dict:
+    """cnt::calculate_A_excitons (cnt.cpp:783-1000): for each centre-of-mass momentum ik_cm the
+    Bethe-Salpeter kernels between the relevant states of the two valleys (relev, from
+    find_relev_ik_range): kernel_11 (band energies minus the screened direct term within valley
+    1), kernel_12 (direct term across the valleys) and the exchange kernel; each is filled on one
+    triangle, completed with its conjugate transpose (Armadillo's .t()) and its diagonal halved.
+    Eigen-decompositions give the A1 (K11 - K12), A2 triplet (K11 + K12) and A2 singlet
+    (K11 + K12 + 2 Kx) excitons.  vq [iq][mu][4] and eps [iq][mu] on vq_ranges = (iq0, mu0)."""
+    nk = ik_range[1] - ik_range[0]
+    iq0, mu0 = vq_ranges
+    v1, v2 = relev
+    n = len(v1)
+
+    def ikv(ik_c, ik_cm):
+        return ik_range[0] + (ik_c - ik_cm - ik_range[0]) % nk
+
+    def ikc(ik_v, ik_cm):
+        return ik_range[0] + (ik_v + ik_cm - ik_range[0]) % nk
+
+    def psi(mu, atom, band, ik):
+        return wf[mu - mu_range[0]][atom, band, ik - ik_range[0]]
+
+    def direct(ik_c, mu_c, ik_v, mu_v, ik_cp, mu_cp, ik_vp, mu_vp):
+        dk = ik_range[0] + (ik_c - ik_cp - ik_range[0]) % nk
+        dmu = mu_c - mu_cp
+        acc = 0j
+        for i in range(2):
+            for j in range(2):
+                acc += (np.conj(psi(mu_c, i, 1, ik_c)) * psi(mu_v, j, 0, ik_v) * psi(mu_cp, i, 1, ik_cp)
+                        * np.conj(psi(mu_vp, j, 0, ik_vp)) * vq[dk - iq0, dmu - mu0, 2 * i + j] / eps[dk - iq0, dmu - mu0])
+        return acc
+
+    def exchange(ik_cm, ik_c, mu_c, ik_v, mu_v, ik_cp, mu_cp, ik_vp, mu_vp):
+        acc = 0j
+        for i in range(2):
+            for j in range(2):
+                acc += (np.conj(psi(mu_c, i, 1, ik_c)) * psi(mu_v, i, 0, ik_v) * psi(mu_cp, j, 1, ik_cp)
+                        * np.conj(psi(mu_vp, j, 0, ik_vp)) * vq[ik_cm - iq0, 0 - mu0, 2 * i + j])
+        return acc
+
+    out = {"A1": [], "A2_triplet": [], "A2_singlet": [], "kernels": []}
+    for ik_cm in range(*ik_cm_range):
+        k11 = np.zeros((n, n), complex)
+        k12 = np.zeros((n, n), complex)
+        kx = np.zeros((n, n), complex)
+        for c in range(n):
+            ik_c, mu_c = v1[c]
+            ik_v, mu_v = ikv(ik_c, ik_cm), mu_c
+            k11[c, c] += energy[1, ik_c - ik_range[0], mu_c - mu_range[0]] - energy[0, ik_v - ik_range[0], mu_c - mu_range[0]]
+            for cp in range(c + 1):
+                ik_cp, mu_cp = v1[cp]
+                ik_vp, mu_vp = ikv(ik_cp, ik_cm), mu_cp
+                k11[c, cp] -= direct(ik_c, mu_c, ik_v, mu_v, ik_cp, mu_cp, ik_vp, mu_vp)
+                kx[c, cp] += 2 * exchange(ik_cm, ik_c, mu_c, ik_v, mu_v, ik_cp, mu_cp, ik_vp, mu_vp)
+            for vp in range(c, n):
+                ik_vp, mu_vp = v2[vp]
+                ik_cp, mu_cp = ikc(ik_vp, ik_cm), mu_vp
+                k12[c, n - 1 - vp] -= direct(ik_c, mu_c, ik_v, mu_v, ik_cp, mu_cp, ik_vp, mu_vp)
+        for k in (k11, k12, kx):
+            k += k.conj().T
+            k[np.diag_indices(n)] /= 2
+        out["A1"].append(np.linalg.eigvalsh(k11 - k12))
+        out["A2_triplet"].append(np.linalg.eigvalsh(k11 + k12))
+        out["A2_singlet"].append(np.linalg.eigvalsh(k11 + k12 + 2 * kx))
+        out["kernels"].append((k11, k12, kx))
+    for key in ("A1", "A2_triplet", "A2_singlet"):
+        out[key] = np.array(out[key])
+    return out
+
+
+def exciton_dispersion(g: dict, window_ev: float = 1.0, interaction: bool = True) -> dict:
+    """calculate_exciton_dispersion (cnt.cpp:1056-1080) on the tube of g: K2-extended bands, the
+    lowest valley pair (_i_sub = 0, cnt.h:117), the states within window_ev of its bottom, vq,
+    PI and eps over the full q range, and the A excitons for k_cm within +-(states per valley).
+    interaction=False zeroes vq (eps = 1): the kernels hold the bare pair energies."""
+    E, W = k2_extended(g)
+    ik_range, mu_range = (0, E.shape[1]), (0, E.shape[2])
+    relev = find_relev_ik_range(E, find_valleys(E)[0], window_ev * EV)
+    iq_range = (-(ik_range[1] - 1), ik_range[1])
+    mq_range = (-(mu_range[1] - 1), mu_range[1])
+    vq = calculate_vq(g, iq_range, mq_range, g["n_cells"])
+    if not interaction:
+        vq = np.zeros_like(vq)
+    pi = calculate_polarization(g, iq_range, mq_range, E, W, ik_range, mu_range)
+    eps = calculate_dielectric(vq, pi)
+    n = len(relev[0])
+    ex = calculate_a_excitons(E, W, relev, vq, (iq_range[0], mq_range[0]), eps, (-n, n), ik_range, mu_range)
+    ex.update({"relev": relev, "energy": E, "ik_cm_range": (-n, n), "vq": vq, "eps": eps})
+    return ex
 
 
 EPS0 = 8.85e-12    # constants.h:17

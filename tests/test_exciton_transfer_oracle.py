@@ -228,3 +228,36 @@ def test_relevant_states_around_the_valleys():
         assert steps == [1] * len(steps)  # contiguous, wrapping across the zone edge
         assert ikb in iks
         assert max(E[1, ik, mub] for ik in iks) < E[1, ikb, mub] + 1.0 * X.EV
+
+
+@pytest.fixture(scope="module")
+def excitons_84():
+    g = X.cnt_geometry(8, 4, 12)
+    return X.exciton_dispersion(g), X.exciton_dispersion(g, interaction=False)
+
+
+def test_bse_without_interaction_gives_the_free_pairs(excitons_84):
+    # vq = 0, eps = 1: the kernels are diagonal with the pair energies E_c(k) - E_v(k - k_cm)
+    _, free = excitons_84
+    E = free["energy"]
+    nk = E.shape[1]
+    v1 = free["relev"][0]
+    for a, ik_cm in enumerate(range(*free["ik_cm_range"])):
+        pairs = sorted(E[1, ik, mu] - E[0, (ik - ik_cm) % nk, mu] for ik, mu in v1)
+        for key in ("A1", "A2_triplet", "A2_singlet"):
+            np.testing.assert_allclose(free[key][a], pairs, rtol=0, atol=1e-12 * X.T0)
+
+
+def test_bse_binds_the_a_excitons(excitons_84):
+    ex, free = excitons_84
+    k0 = -ex["ik_cm_range"][0]
+    gap = 2 * ex["energy"][1].min()
+    assert free["A1"][k0].min() == pytest.approx(gap, rel=1e-12)
+    for k11, k12, kx in ex["kernels"]:
+        for k in (k11, k12, kx):
+            assert np.abs(k - k.conj().T).max() == 0.0
+    # screened attraction binds the lowest exciton well below the band gap; exchange pushes the
+    # singlet above the triplet; screening never anti-screens
+    assert 0.2 * gap < ex["A1"][k0].min() < 0.8 * gap
+    assert ex["A2_singlet"][k0].min() > ex["A2_triplet"][k0].min()
+    assert ex["eps"].min() >= 1.0
