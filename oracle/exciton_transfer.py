@@ -24,6 +24,9 @@ What it restates (reference project paths):
   K2-extended bands and the dielectric function (cnt.cpp:634-757).
 * ``calculate_a_excitons``: the Bethe-Salpeter kernels and A-exciton energies
   (cnt.cpp:783-1000).
+* ``relevant_states``, ``q_partial``, ``first_order``: the thermal A2-singlet states, the
+  Q matrix element and the first-order transfer rate (exciton_transfer.cpp:226-304, 380-424;
+  exciton_transfer.h:30-33, 167-196).
 * ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
   potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
@@ -378,7 +381,20 @@ def calculate_a_excitons(energy, wf, relev, vq, vq_ranges, eps, ik_cm_range, ik_
             k[np.diag_indices(n)] /= 2
         out["A1"].append(np.linalg.eigvalsh(k11 - k12))
         out["A2_triplet"].append(np.linalg.eigvalsh(k11 + k12))
-        out["A2_singlet"].append(np.linalg.eigvalsh(k11 + k12 + 2 * kx))
+        e_s, v_s = np.linalg.eigh(k11 + k12 + 2 * kx)
+        out["A2_singlet"].append(e_s)
+        # A2 singlet states over both valleys (cnt.cpp:962-965): +v/sqrt2 on each
+        out.setdefault("A2_singlet_psi", []).append(np.vstack([v_s, v_s]) / math.sqrt(2.))
+        # indices of the (conduction, valence) states of each row (cnt.cpp:969-997)
+        idx = np.zeros((4, 2 * n), int)
+        for c in range(n):
+            ik_c, mu_c = v1[c]
+            idx[:, c] = (ik_c - ik_range[0], mu_c - mu_range[0], ikv(ik_c, ik_cm) - ik_range[0], mu_c - mu_range[0])
+        for v in range(n):
+            ik_v, mu_v = v2[v]
+            idx[:, 2 * n - 1 - v] = (ikc(ik_v, ik_cm) - ik_range[0], mu_v - mu_range[0], ik_v - ik_range[0],
+                                     mu_v - mu_range[0])
+        out.setdefault("ik_idx", []).append(idx)
         out["kernels"].append((k11, k12, kx))
     for key in ("A1", "A2_triplet", "A2_singlet"):
         out[key] = np.array(out[key])
@@ -402,8 +418,74 @@ def exciton_dispersion(g: dict, window_ev: float = 1.0, interaction: bool = True
     eps = calculate_dielectric(vq, pi)
     n = len(relev[0])
     ex = calculate_a_excitons(E, W, relev, vq, (iq_range[0], mq_range[0]), eps, (-n, n), ik_range, mu_range)
-    ex.update({"relev": relev, "energy": E, "ik_cm_range": (-n, n), "vq": vq, "eps": eps})
+    ex.update({"relev": relev, "energy": E, "wavefunc": W, "ik_cm_range": (-n, n), "vq": vq, "eps": eps})
     return ex
+
+
+KB = 1.3865e-23        # constants.h:14
+HB = 6.5e-16 * EV      # constants.h:13
+BROADENING = 4e-3 * EV  # exciton_transfer.h:42
+
+
+def lorentzian(e, broadening=BROADENING):
+    """exciton_transfer.h:30-33"""
+    return (1. / PI) * broadening / (e * e + broadening * broadening)
+
+
+def relevant_states(ex: dict, min_energy: float, temperature: float = 300.) -> list:
+    """get_relevant_states (exciton_transfer.cpp:226-250) of the A2 singlet: (energy, ik_cm,
+    ik_cm_idx, i_principal) with energy within |ln 1e-3| kT of min_energy, by energy."""
+    thr = min_energy + abs(math.log(1.e-3) * KB * temperature)
+    e = ex["A2_singlet"]
+    st = [(e[a, i], a + ex["ik_cm_range"][0], a, i) for i in range(e.shape[1]) for a in range(e.shape[0])
+          if e[a, i] <= thr]
+    return sorted(st, key=lambda t: t[0])
+
+
+def q_partial(g: dict, ex: dict, state) -> complex:
+    """The per-state factor of calculate_Q (exciton_transfer.cpp:276-297)."""
+    _, ik_cm, a, i_n = state
+    W = ex["wavefunc"]
+    idx = ex["ik_idx"][a]
+    k = ik_cm * g["dk_l"]
+    ef = np.array([1.0 + 0j, np.exp(1j * float(k @ g["acc"]))])
+    acc = 0j
+    for r in range(idx.shape[1]):
+        cc = W[idx[1, r]][:, 1, idx[0, r]]
+        cv = W[idx[3, r]][:, 0, idx[2, r]]
+        acc += ex["A2_singlet_psi"][a][r, i_n] * np.sum(cc * np.conj(cv) * ef)
+    return acc
+
+
+def length_m(g: dict) -> float:
+    return float(g["n_cells"]) * float(np.linalg.norm(g["t_vec"]))
+
+
+def area_u(g: dict) -> float:
+    """cnt::Au (cnt.h:346-349): the graphene unit-cell area."""
+    return abs(g["a1"][0] * g["a2"][1] - g["a1"][1] * g["a2"][0])
+
+
+def first_order(gd: dict, exd: dict, ga: dict, exa: dict, z_shift: float, axis_shifts=(0., 0.), theta: float = 0.,
+                temperature: float = 300.) -> float:
+    """exciton_transfer::first_order (exciton_transfer.cpp:380-424): the thermal, Lorentzian-matched
+    sum of (2 pi / hbar) |Q J|^2 / (L_d L_a) over donor/acceptor A2-singlet states."""
+    min_energy = exd["A2_singlet"].min()
+    ds = relevant_states(exd, min_energy, temperature)
+    as_ = relevant_states(exa, min_energy, temperature)
+    Z = sum(math.exp(-d[0] / (KB * temperature)) for d in ds)
+    coeff = (Q0 ** 2 * area_u(gd) * area_u(ga)) / (16 * PI ** 3 * EPS0 * gd["radius"] * ga["radius"]
+                                                    * math.sqrt(length_m(gd) * length_m(ga)))
+    rate = 0.0
+    for d in ds:
+        for a in as_:
+            if not lorentzian(d[0] - a[0]) > 1.e-2 * lorentzian(0.0):
+                continue
+            Q = coeff * np.conj(q_partial(gd, exd, d)) * q_partial(ga, exa, a)
+            J = coulomb_j(gd, ga, d[1], a[1], axis_shifts, z_shift, theta)
+            M = abs(Q * J) / math.sqrt(length_m(gd) * length_m(ga))
+            rate += (2 * PI / HB) * (math.exp(-d[0] / (KB * temperature)) / Z) * M ** 2 * lorentzian(d[0] - a[0])
+    return rate
 
 
 EPS0 = 8.85e-12    # constants.h:17

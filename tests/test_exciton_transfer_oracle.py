@@ -261,3 +261,19 @@ def test_bse_binds_the_a_excitons(excitons_84):
     assert 0.2 * gap < ex["A1"][k0].min() < 0.8 * gap
     assert ex["A2_singlet"][k0].min() > ex["A2_triplet"][k0].min()
     assert ex["eps"].min() >= 1.0
+
+
+def test_first_order_rate_of_the_restated_model(excitons_84):
+    # the reference's first-order transfer rate between two parallel (8,4) tubes of 12 unit cells
+    # (13.5 nm): positive, falling with the centre distance, of the Förster form's order at a few
+    # nanometres (gamma_0 (1 nm / d)^6 = 1.4e12 /s at 3 nm)
+    ex, _ = excitons_84
+    g = X.cnt_geometry(8, 4, 12)
+    rates = [X.first_order(g, ex, g, ex, z) for z in (1.5e-9, 3e-9, 6e-9)]
+    assert rates[0] > rates[1] > rates[2] > 0
+    assert 1e11 < rates[1] < 1e14
+    # the matrix element does not depend on the phase of the exciton eigenvectors
+    st = X.relevant_states(ex, ex["A2_singlet"].min())[0]
+    q = X.q_partial(g, ex, st)
+    ex2 = dict(ex, A2_singlet_psi=[p * np.exp(0.7j) for p in ex["A2_singlet_psi"]])
+    assert abs(X.q_partial(g, ex2, st)) == pytest.approx(abs(q), rel=1e-12)
