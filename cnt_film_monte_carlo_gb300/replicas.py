@@ -1,7 +1,8 @@
 """Replicas on several GPUs, one process per GPU: the only exchange of the path.
 
 Excitons are independent given the read-only neighbour rows, so N GPUs run N replicas of the
-film(s) with different Philox keys (replica r uses seed + r) and nothing crosses GPUs while they
+film(s) with different Philox keys (replica r of a film whose seed is s uses the 64-bit key
+r * 2^32 + s, so every (film, replica) pair has its own key) and nothing crosses GPUs while they
 run.  The exchange comes once, at the end: the MSD sums of every (step, batch) and the exciton
 counts are combined over replicas (the final reduction of kubo_save_avg_dispalcement_squared,
 src/monte_carlo/monte_carlo.cpp:382-409, over the union of the replicas' excitons; batches are
@@ -14,8 +15,16 @@ import numpy as np
 
 
 def replica_seed(seed: int, rank: int) -> int:
-    """Philox key of replica ``rank`` (streams of different replicas never overlap)."""
-    return int(seed) + int(rank)
+    """Philox key of replica ``rank`` of a film seeded ``seed``: the rank in the upper 32 bits of
+    the 64-bit key, the film's seed (below 2^32) in the lower 32.  Films with distinct seeds on
+    any replicas never share a key, so their streams never overlap; replica 0 keeps the film's
+    own seed, so a one-GPU run is unchanged."""
+    seed, rank = int(seed), int(rank)
+    if not 0 <= seed < (1 << 32):
+        raise ValueError(f"replica_seed: film seed {seed} outside [0, 2^32)")
+    if not 0 <= rank < (1 << 32):
+        raise ValueError(f"replica_seed: rank {rank} outside [0, 2^32)")
+    return (rank << 32) | seed
 
 
 def _dist():

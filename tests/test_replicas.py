@@ -32,8 +32,13 @@ def _replica_data(rank, n_steps=40, batches=8):
     return msd, counts, t
 
 
+FILMS = 256
+
+
 def _worker(rank, world, port, out_dir):
     import sys
+
+    import torch
 
     sys.path.insert(0, ROOT)
     import torch.distributed as dist
@@ -47,9 +52,13 @@ def _worker(rank, world, port, out_dir):
     gm, gc = replicas.gather_batches(msd, counts)
     D, ci = diffusion.fit_counts(gm, gc, t)
     dev, wall, hops = replicas.job_timing(1.0 + rank, 2.0 - rank, 1000 * (rank + 1))
-    assert replicas.replica_seed(7, rank) == 7 + rank
+    # the Philox keys of this replica's films (bench.py seeds film i with 1 + i), gathered: no two
+    # (film, replica) pairs may share a key
+    keys = torch.tensor([replicas.replica_seed(1 + i, rank) for i in range(FILMS)], dtype=torch.int64)
+    all_keys = [torch.empty_like(keys) for _ in range(world)]
+    dist.all_gather(all_keys, keys)
     np.savez(os.path.join(out_dir, f"r{rank}.npz"), total=total, gm=gm, gc=gc, D=D, ci=ci,
-             timing=np.array([dev, wall, hops]))
+             timing=np.array([dev, wall, hops]), keys=torch.cat(all_keys).numpy())
     dist.barrier()
     dist.destroy_process_group()
 
@@ -78,6 +87,8 @@ def test_two_replicas_over_gloo(tmp_path):
         np.testing.assert_allclose(r["D"], D, rtol=1e-14)
         np.testing.assert_allclose(r["ci"], ci, rtol=1e-14)
         np.testing.assert_array_equal(r["timing"], [2.0, 2.0, 3000.0])
+        assert len(r["keys"]) == world * FILMS and len(np.unique(r["keys"])) == world * FILMS
+        np.testing.assert_array_equal(r["keys"][:FILMS], 1 + np.arange(FILMS))  # replica 0: the films' seeds
 
 
 def test_single_process_is_identity():
@@ -88,3 +99,15 @@ def test_single_process_is_identity():
     assert np.array_equal(m, msd) and np.array_equal(c, counts)
     assert np.array_equal(replicas.sum_msd(msd), msd)
     assert replicas.job_timing(1.5, 2.5, 10) == (1.5, 2.5, 10.0)
+
+
+def test_replica_keys_distinct_and_bounded():
+    from cnt_film_monte_carlo_gb300 import replicas
+
+    keys = {replicas.replica_seed(s, r) for s in range(300) for r in range(8)}
+    assert len(keys) == 300 * 8
+    assert replicas.replica_seed(5, 0) == 5 and replicas.replica_seed(5, 1) == (1 << 32) + 5
+    assert all(k < (1 << 64) for k in keys)
+    for bad in ((-1, 0), (1 << 32, 0), (0, -1), (0, 1 << 32)):
+        with pytest.raises(ValueError):
+            replicas.replica_seed(*bad)
