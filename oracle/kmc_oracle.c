@@ -89,6 +89,23 @@ void orc_forster_table(double gamma_0, const double th_deg[3], const double zsh[
   }
 }
 
+/* The 2-D (centre distance, folded angle) table of the benchmark films: create_forster_scatt_table's
+ * formula (monte_carlo.cpp:174-187) at zero axis shifts, gamma_0 cos^2(theta) (1 nm / d)^6, on
+ * linspace grids of distance (m) and angle (degrees, scaled by the reference's pi, :167). */
+void orc_forster2d_table(double gamma_0, const double distance[3], const double th_deg[3], double* dist,
+                         double* theta, double* rate) {
+  int64_t nd = (int64_t)distance[2], nt = (int64_t)th_deg[2];
+  orc_linspace(distance[0], distance[1], nd, dist);
+  orc_linspace(th_deg[0], th_deg[1], nt, theta);
+  double scale = ORC_REF_PI / 180;
+  for (int64_t i = 0; i < nt; ++i) theta[i] = theta[i] * scale;
+  for (int64_t i = 0; i < nd; ++i)
+    for (int64_t k = 0; k < nt; ++k) {
+      double c = cos(theta[k]);
+      rate[i * nt + k] = gamma_0 * (c * c) * pow(1.e-9 / dist[i], 6);
+    }
+}
+
 /* get_rate, scattering_struct.h:38-52 (and the 2-D (distance, theta) extension) */
 static inline double table_rate(const orc_table* t, double th, double zsh, double a1, double a2, double dist,
                                 int64_t pair_off) {

@@ -39,6 +39,10 @@ typedef struct orc_sim orc_sim;
 /* arma::linspace as the shim defines it (used by monte_carlo.cpp:66-75). */
 void orc_linspace(double start, double end, int64_t num, double* out);
 
+/* The benchmark films' 2-D table: the Förster formula of monte_carlo.cpp:174-187 at zero axis
+ * shifts on a (distance [m], angle [deg]) grid; rate is [nd][nt], theta in radians. */
+void orc_forster2d_table(double gamma_0, const double distance[3], const double th_deg[3], double* dist,
+                         double* theta, double* rate);
 /* create_forster_scatt_table, src/monte_carlo/monte_carlo.cpp:156-200.  rate is
  * [n_th][n_zsh][n_a1][n_a2]; theta grid in degrees is scaled by pi/180 with the reference's
  * pi = 3.141592 (src/helper/constants.h:10). */

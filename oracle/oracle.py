@@ -17,7 +17,14 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "ref_kubo")
 REF_TIMING_BIN = os.path.join(HERE, "_ref", "ref_kubo_timing")
 REF_CONTACTS_BIN = os.path.join(HERE, "_ref", "ref_contacts")
-REF_SRC = "/root/reference"
+# the reference checkout (its sources are compiled into oracle/_ref); unset: no oracle/_ref
+REF_ENV = "CNT_REFERENCE_DIR"
+
+
+def reference_dir():
+    """The reference checkout named by $CNT_REFERENCE_DIR, or None when it is unset."""
+    d = os.environ.get(REF_ENV, "")
+    return d or None
 
 _lib = None
 
@@ -37,12 +44,17 @@ class orc_table(C.Structure):
                 ("species", C.POINTER(C.c_int32))]
 
 
-def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and, if the reference sources are present, oracle/_ref)."""
+def build(ref_dir: str | None = None) -> None:
+    """Compile liboracle.so and, when ``ref_dir`` names a reference checkout, oracle/_ref from its
+    sources."""
     targets = ["lib"]
-    if ref and os.path.isdir(REF_SRC):
+    env = dict(os.environ)
+    if ref_dir:
+        if not os.path.isfile(os.path.join(ref_dir, "src", "monte_carlo", "particle.cpp")):
+            raise RuntimeError(f"oracle.build: no reference sources under {ref_dir!r}")
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+        env["CNT_REFERENCE_DIR"] = ref_dir
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True, env=env)
 
 
 def lib():
@@ -53,6 +65,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.orc_linspace.argtypes = [D, D, I64, PD]
         L.orc_forster_table.argtypes = [D, PD, PD, PD, PD, PD, PD, PD, PD, PD]
+        L.orc_forster2d_table.argtypes = [D, PD, PD, PD, PD, PD]
         L.orc_trim.argtypes = [I64, PD, PD, PI32, PI32, PD]
         L.orc_trim.restype = I64
         L.orc_sim_create.argtypes = [I64, PD, PD, PI32, PI32, C.POINTER(orc_table), D, D, C.c_int]
@@ -148,6 +161,18 @@ def linspace(a, b, n):
     out = np.zeros(max(int(n), 1), dtype=np.float64)
     lib().orc_linspace(a, b, int(n), _p(out, C.c_double))
     return out[: int(n)]
+
+
+def forster2d_table(gamma_0=1e15, distance_m=(0.5e-9, 10e-9, 96), theta_deg=(0.0, 90.0, 91)):
+    """The benchmark films' 2-D (distance, folded angle) Förster-form table: dict(kind=2,
+    grids=[distance m, theta rad], rate=ndarray[nd, nt])."""
+    dd = np.ascontiguousarray(distance_m, dtype=np.float64)
+    th = np.ascontiguousarray(theta_deg, dtype=np.float64)
+    nd, nt = int(dd[2]), int(th[2])
+    g = [np.zeros(nd), np.zeros(nt)]
+    rate = np.zeros((nd, nt))
+    lib().orc_forster2d_table(float(gamma_0), _p(dd, D), _p(th, D), _p(g[0], D), _p(g[1], D), _p(rate, D))
+    return {"kind": 2, "grids": g, "rate": rate}
 
 
 def forster_table(gamma_0, theta_deg, zsh, ash1, ash2):

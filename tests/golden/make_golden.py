@@ -10,8 +10,9 @@ traces).  The contacts cases come from the reference's contacts (steady-state fl
 (oracle/_ref/ref_contacts): per-step segment populations and interface currents, the exciton
 slots after the run, and the reference's own three output files.
 
-Needs the reference sources (REF_SRC, default /root/reference); the fixtures themselves are
-self-contained.  Run: python tests/golden/make_golden.py [case ...]
+Needs the reference sources: set CNT_REFERENCE_DIR to the reference checkout (the script stops
+with a message when it is unset); the fixtures themselves are self-contained.
+Run: CNT_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -159,7 +160,10 @@ def make_contacts_case(name, c, tmp):
 
 def main(names=()):
     """Regenerate the named cases (all when none is named)."""
-    O.build(ref=True)
+    ref_dir = O.reference_dir()
+    if ref_dir is None:
+        sys.exit("make_golden.py: set CNT_REFERENCE_DIR to the reference checkout")
+    O.build(ref_dir)
     with tempfile.TemporaryDirectory() as tmp:
         for name, c in CASES.items():
             if not names or name in names:

@@ -54,3 +54,15 @@ def test_forster_2d_table_is_the_formula():
     want = 1e15 * np.cos(th)[None, :] ** 2 * (1e-9 / d[:, None]) ** 6
     np.testing.assert_allclose(t["rate"], want, rtol=1e-14, atol=1e-300)
     assert t["rate"][0, 0] == 1e15 * (1e-9 / 0.5e-9) ** 6
+
+
+def test_oracle_2d_table_equals_library_table():
+    # the oracle builds the benchmark films' table on its own (the CPU reference arm of bench.py
+    # never loads the library); it must be the library's table bit for bit
+    for args in (((0.5e-9, 10e-9, 96), (0.0, 90.0, 91)), ((0.3e-9, 12e-9, 17), (0.0, 90.0, 7))):
+        t = tables.forster_2d(1e15, *args)
+        o = O.forster2d_table(1e15, *args)
+        assert o["kind"] == t["kind"] == 2
+        for a, b in zip(o["grids"], t["grids"]):
+            assert np.array_equal(a, b)
+        assert np.array_equal(o["rate"], t["rate"])
