@@ -1,23 +1,26 @@
 """Benchmark: exciton hops/s of the Green-Kubo hot path on GB300.
 
-Workload (one "step" = all excitons advanced by 8 MSD bins of 1 ps, one kmc_run call):
-  film: 100 straight tubes x 200 nm, uniform centres in a 500 x 500 x 10 nm box, azimuth U[0, pi),
-        z-tilt U[-5, 5] deg, 1 nm segments (20,000 sites), 10 nm hopping cutoff, 2-D
-        (distance 0.5-10 nm x angle 0-90 deg) Förster-form rate table;
-  1,000,000 excitons injected uniformly at random sites, Philox seed 1, MSD sampled every 1 ps,
-  exciton velocity 2e5 m/s.  Synthetic film (the reference's meshes are not available).
+Default workload (--workload cfg3), the batched mixed-precision form: 256 independent films of
+uneven size in one persistent launch.  Film i (seed i, i = 0..255): tube count uniform in
+50..2000, tube lengths lognormal (median 300 nm, sigma 0.5), uniform centres in a 1000 x 1000 x
+20 nm box, azimuth U[0, pi), z-tilt U[-5, 5] deg, 1 nm segments, 10 nm hopping cutoff, 2-D
+(distance 0.5-10 nm x angle 0-90 deg) Förster-form rate table; 100 excitons per tube injected
+uniformly at random sites, Philox key i for film i, exciton velocity 2e5 m/s.  One "step" = all
+excitons advanced by one 1 ps MSD bin (one kmc_run call, one persistent launch over all films).
+Synthetic films (the reference's meshes are not available).
 value: hops/s of the mixed-precision kernel, device time from CUDA events on the launching
-stream, max over ranks; e2e: the same metric through the public API from host buffers (film and
-table uploaded, neighbour lists built, excitons created, K steps run, MSD read back).
-Multi-GPU (torchrun): independent replicas (seed + rank), weak scaling, no collective on the
-data path.  --impl reference times the reference's algorithm (the oracle's restatement, which
-recomputes every neighbour list on every hop like src/monte_carlo/scatterer.cpp:9-31) on the host
-cores.
-Other workloads (--workload): cfg3 (256-film batch), cfg4 (10.8 M-site film), contacts (the
-contacts-mode loop on the cfg2 film) and cfg5: 64 mixed-chirality films whose pair rate tables
-come from the surrogate network trained on the GPU in the set-up (untimed); its line adds a
-"surrogate" object (training throughput, held-out rate error, D error against the labeller's
-tables on a mixed film).
+stream, max over ranks; e2e: the same metric through the public API from host buffers (films
+and table uploaded, neighbour lists built, excitons created, K steps run, MSD read back).
+Multi-GPU (torchrun): independent replicas (Philox key rank * 2^32 + film seed), weak scaling, no
+collective on the data path.  --impl reference times the reference's algorithm (the oracle's
+restatement, which recomputes every neighbour list on every hop like
+src/monte_carlo/scatterer.cpp:9-31) on the host cores, with its inputs built by the oracle: the
+reference arm never loads the engine's library.
+Other workloads (--workload): cfg2 (the 100-tube film with 10^6 excitons, 8 bins per step), cfg4
+(10.8 M-site film), contacts (the contacts-mode loop on the cfg2 film) and cfg5: 64
+mixed-chirality films whose pair rate tables come from the surrogate network trained on the GPU
+in the set-up (untimed); its line adds a "surrogate" object (training throughput, held-out rate
+error, D error against the labeller's tables on a mixed film).
 """
 from __future__ import annotations
 
@@ -41,16 +44,23 @@ METRIC = "exciton hops/s (Green-Kubo hop kernel)"
 UNIT = "hops/s"
 
 
-def workload(name="cfg2", films=256):
-    """(list of films, rate table, excitons per film, description)."""
-    from cnt_film_monte_carlo_gb300 import film as F
-    from cnt_film_monte_carlo_gb300 import tables
+def workload(name="cfg3", films=256, table=None):
+    """(list of films, rate table, excitons per film, Philox key per film, description).
 
-    tab = tables.forster_2d(1e15)
+    ``table`` builds the 2-D Förster-form table from gamma_0 (default: the engine's
+    tables.forster_2d; the reference arm passes the oracle's own, equal bit for bit)."""
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    if table is None:
+        from cnt_film_monte_carlo_gb300 import tables
+
+        table = tables.forster_2d
+    if name != "cfg5":
+        tab = table(1e15)
     if name == "cfg4":
         f = F.lognormal_tubes(20000, 500.0, 0.4, (5000.0, 5000.0, 50.0), seed=7)
-        return [f], tab, [10_000_000], ("cfg4 film: 20,000 tubes, lognormal length (median 500 nm, sigma 0.4), "
-                                          "5x5 um x 50 nm box, 1 nm segments, 10 nm cutoff, 2-D rate table")
+        return [f], tab, [10_000_000], [7], ("cfg4 film: 20,000 tubes, lognormal length (median 500 nm, sigma 0.4), "
+                                             "5x5 um x 50 nm box, 1 nm segments, 10 nm cutoff, 2-D rate table, seed 7")
     if name == "cfg3":
         out, ne = [], []
         for i in range(films):
@@ -58,9 +68,10 @@ def workload(name="cfg2", films=256):
             n_t = int(rng.integers(50, 2001))
             out.append(F.lognormal_tubes(n_t, 300.0, 0.5, (1000.0, 1000.0, 20.0), seed=i))
             ne.append(100 * n_t)
-        return out, tab, ne, (f"cfg3 batch: {films} films, tubes U{{50..2000}}, lognormal length (median 300 nm, "
-                               "sigma 0.5), 1000x1000x20 nm boxes, 1 nm segments, 10 nm cutoff, 100 excitons per tube, "
-                               "one persistent launch")
+        return out, tab, ne, list(range(films)), (
+            f"cfg3 batch: {films} films (seeds 0-{films - 1}), tubes U{{50..2000}}, lognormal length (median 300 nm, "
+            "sigma 0.5), 1000x1000x20 nm boxes, 1 nm segments, 10 nm cutoff, 2-D rate table, 100 excitons per tube, "
+            "one persistent launch")
     if name == "cfg5":
         from cnt_film_monte_carlo_gb300 import surrogate as SG
 
@@ -69,14 +80,14 @@ def workload(name="cfg2", films=256):
         # the CPU legs read the labeller's pair tables; the GPU arm replaces them with the
         # network's (cfg5_surrogate)
         pairs = SG.labeller_table(SG.species_model(), *SG.grids())
-        return out, pairs, [CFG5_EXC] * n_f, (
+        return out, pairs, [CFG5_EXC] * n_f, [SEED + i for i in range(n_f)], (
             f"cfg5 batch: {n_f} mixed-chirality films of 1000 tubes ((6,5), (7,5), (8,3), (8,4) uniform per tube), "
             "lognormal length (median 300 nm, sigma 0.5), 1000x1000x20 nm boxes, 1 nm segments, 10 nm cutoff, "
             "16 (donor, acceptor) rate tables of 96 x 91 built by the trained surrogate")
     f = F.straight_tubes(FILM["n_tubes"], FILM["length_nm"], box_nm=FILM["box_nm"], max_tilt_deg=FILM["tilt_deg"],
                          seed=FILM["film_seed"])
-    return [f], tab, [N_EXC], ("cfg2 film: 100 tubes x 200 nm, 500x500x10 nm, 1 nm segments, 10 nm cutoff, "
-                               "2-D rate table")
+    return [f], tab, [N_EXC], [SEED], ("cfg2 film: 100 tubes x 200 nm, 500x500x10 nm, 1 nm segments, 10 nm cutoff, "
+                                       "2-D rate table")
 
 
 CFG5_FILMS, CFG5_EXC = 64, 100_000
@@ -197,11 +208,20 @@ def measured_peak():
 
 
 def bytes_per_hop(k_mean):
-    """Algorithmic bytes of one hop of the mixed kernel: the destination site's 64-byte record
-    (1/total, links, link times, first search level) and the one 64-byte row block holding the
-    chosen entry (8 FP32 cumulative values + 8 neighbour ids); rows of 65-512 entries add the
-    32-byte second level."""
+    """Bytes one hop of the mixed kernel must move in its own layout: the destination site's
+    64-byte record (1/total, links, link times, first search level) and the one 64-byte row block
+    holding the chosen entry (8 FP32 cumulative values + 8 neighbour ids); rows of 65-512 entries
+    add the 32-byte second level."""
     return 128 if k_mean <= 64 else 160
+
+
+def algorithmic_bytes_per_hop(k_mean):
+    """Algorithmic bytes of one hop of a plain CSR walk with an FP32 cumulative table, each
+    dependent random access one 32-byte sector: the destination site record (64 B: position,
+    row offset, 1/total, links), one column-index sector and the bisection's sectors,
+    max(1, ceil(log2 k) - 2) of them (8 FP32 values per sector, the last three probes share one),
+    at the measured mean row length k."""
+    return 64 + 32 + 32 * max(1, math.ceil(math.log2(max(k_mean, 2.0))) - 2)
 
 
 class CpuSample:
@@ -210,10 +230,10 @@ class CpuSample:
     of excitons so that one sample (all of them advanced by one 1 ps bin from their injection) takes
     about `seconds` of wall time."""
 
-    def __init__(self, f, tab, seconds=10.0, threads=None, species=None):
+    def __init__(self, f, tab, seconds=10.0, threads=None, species=None, seed=SEED):
         from oracle import oracle as O
 
-        self.O, self.f, self.tab, self.species = O, f, tab, species
+        self.O, self.f, self.tab, self.species, self.seed = O, f, tab, species, seed
         self.threads = threads or os.cpu_count() or 1
         n = max(self.threads * 16, 128)
         sim = self._sim(n)
@@ -228,7 +248,7 @@ class CpuSample:
         f = self.f
         sim = self.O.Sim(f.pos_m(), f.orient, f.left, f.right, self.tab, R_MAX, VEL, n_threads=self.threads,
                          species=self.species)
-        sim.create_excitons(1, 0, n, SEED, use_csr=False)
+        sim.create_excitons(1, 0, n, self.seed, use_csr=False)
         return sim
 
     def run(self):
@@ -241,7 +261,12 @@ class CpuSample:
 
 
 def reference_arm(args):
-    films, tab, ne, desc = workload(args.workload, args.films)
+    """The reference's algorithm on the host cores.  Films come from the numpy generator and the
+    rate table from the oracle (oracle.forster2d_table, equal bit for bit to the engine's), so this
+    process never loads the engine's library."""
+    from oracle import oracle as O
+
+    films, tab, ne, seeds, desc = workload(args.workload, args.films, table=O.forster2d_table)
     f = films[0]
     if args.workload == "contacts":
         vals, secs = [], []
@@ -263,10 +288,12 @@ def reference_arm(args):
     # whole run within a few minutes: every step gets an equal share of ~150 s
     per_step = min(args.cpu_seconds, 150.0 / max(args.steps + args.warmup, 1))
     sp0 = cfg5_species(films[:1])[0] if args.workload == "cfg5" else None
-    cs = CpuSample(f, tab, seconds=per_step, species=sp0)
+    cs = CpuSample(f, tab, seconds=per_step, species=sp0, seed=seeds[0])
     vals, secs, sample = [], [], ""
     for i in range(args.warmup + args.steps):
         v, sample, dt = cs.run()
+        if len(films) > 1:
+            sample += f"; film 0 of the {len(films)}-film batch ({f.n_sites} sites)"
         if args.workload == "cfg5":
             sample += "; the labeller's 16 pair tables (per-pair lookup added to the reference's algorithm)"
         if i >= args.warmup:
@@ -276,7 +303,10 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config(desc, sum(x.n_sites for x in films), int(sum(ne)), 1, {"sample": sample}),
+            "config": config(desc, sum(x.n_sites for x in films), int(sum(ne)), 1,
+                             {"sample": sample, "cpu_arm": "a bounded sample of the workload (the excitons of one "
+                                                           "film of the batch for one 1 ps bin), timed on the host "
+                                                           "cores; hops/s is the comparable figure"}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cs.threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -318,7 +348,7 @@ def contacts_arm(args, local, rank, world):
     from cnt_film_monte_carlo_gb300 import engine as E
     from cnt_film_monte_carlo_gb300 import replicas as R
 
-    films, tab, _, desc = workload("cfg2")
+    films, tab, _, _, desc = workload("cfg2")
     f = films[0]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     seed = R.replica_seed(SEED, rank)
@@ -414,11 +444,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n-exc", type=int, default=None, help="excitons per film (default: the workload's)")
-    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cfg3", "cfg4", "cfg5", "contacts"])
+    ap.add_argument("--workload", default="cfg3", choices=["cfg2", "cfg3", "cfg4", "cfg5", "contacts"])
     ap.add_argument("--films", type=int, default=256, help="films of the cfg3 batch (cfg5: default 64)")
-    ap.add_argument("--bins-per-step", type=int, default=8,
-                    help="1 ps MSD bins advanced per timed step (one kmc_run call)")
-    ap.add_argument("--fp64-steps", type=int, default=None, help="plain FP64 comparison steps (default 3, cfg5 1)")
+    ap.add_argument("--bins-per-step", type=int, default=None,
+                    help="1 ps MSD bins advanced per timed step (one kmc_run call; default 1 for cfg3, 8 otherwise)")
+    ap.add_argument("--fp64-steps", type=int, default=None,
+                    help="plain FP64 comparison steps (default 3; cfg3 and cfg5 1)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="wall seconds of one CPU sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -429,7 +460,9 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     args = ap.parse_args()
     if args.fp64_steps is None:
-        args.fp64_steps = 1 if args.workload == "cfg5" else 3
+        args.fp64_steps = 1 if args.workload in ("cfg3", "cfg5") else 3
+    if args.bins_per_step is None:
+        args.bins_per_step = 1 if args.workload == "cfg3" else 8
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -464,7 +497,8 @@ def main():
             dist.destroy_process_group()
         return
 
-    films, tab, n_exc, desc = workload(args.workload, args.films)
+    films, tab, n_exc, film_seeds, desc = workload(args.workload, args.films)
+    keys = [R.replica_seed(sd, rank) for sd in film_seeds]
     cpu_tab, species, surrogate = tab, None, None
     if args.workload == "cfg5":
         species, tab, surrogate = cfg5_surrogate(films, local)
@@ -484,7 +518,7 @@ def main():
     e = E.Engine(local)
     load(e)
     st = e.build(R_MAX)
-    e.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+    e.init_excitons(n_exc, keys, L.KMC_INJECT_UNIFORM)
     bins = args.bins_per_step
     order = {"auto": L.KMC_ORDER_AUTO, "slots": L.KMC_ORDER_SLOTS, "spatial": L.KMC_ORDER_SPATIAL}[args.order]
     e.set_work_order(order)
@@ -492,7 +526,8 @@ def main():
     if args.variant is not None:
         e.set_mixed_variant(args.variant)
     # trials of one step's length, so launches of up to `bins` steps are among the candidates
-    tune = e.autotune(BIN, VEL, trial_steps=max(2, bins)) if not (args.no_tune or args.variant is not None) else None
+    tune = e.autotune(BIN, VEL, trial_steps=max(1 if args.workload == "cfg3" else 2, bins)) \
+        if not (args.no_tune or args.variant is not None) else None
     for _ in range(args.warmup):
         e.run(bins, BIN, VEL, L.KMC_PREC_MIXED)
     s0 = e.stats()
@@ -531,7 +566,7 @@ def main():
         e2 = E.Engine(local)
         load(e2)
         e2.build(R_MAX)
-        e2.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+        e2.init_excitons(n_exc, keys, L.KMC_INJECT_UNIFORM)
         e2.run(bins, BIN, VEL, L.KMC_PREC_FP64)  # one warm-up step
         h1 = e2.stats()["hops"]
         ms = 0.0
@@ -551,7 +586,7 @@ def main():
         e3 = E.Engine(local)
         load(e3)
         e3.build(R_MAX)
-        e3.init_excitons(n_exc, [R.replica_seed(SEED + i, rank) for i in range(len(films))], L.KMC_INJECT_UNIFORM)
+        e3.init_excitons(n_exc, keys, L.KMC_INJECT_UNIFORM)
         e3.set_work_order(order)
         e3.set_graph(not args.no_graph)
         if tune:
@@ -580,7 +615,9 @@ def main():
         return
     peak, peak_kind = measured_peak()
     bph = bytes_per_hop(st["k_mean"])
-    achieved = hops / dev_s * bph / 1e9
+    abph = algorithmic_bytes_per_hop(st["k_mean"])
+    achieved = hops / dev_s * abph / 1e9
+    kernel_achieved = hops / dev_s * bph / 1e9
     spl = tune["steps_per_launch"] if tune else 32  # the engine's default steps per launch
     hop_launches = args.steps * math.ceil(bins / spl)
     traffic = None  # DRAM bytes per hop-kernel launch, from the ncu capture of this workload
@@ -612,8 +649,16 @@ def main():
         "fp64_plain_value": fp64, "speedup_vs_fp64": (value / world / fp64) if fp64 else None,
         "d_eff_m2_per_s": d_eff,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind, "bytes_per_hop": bph,
-                     "note": "algorithmic bytes per hop x hops / hop-kernel device time; CSR is L2-resident",
+                     "traffic": traffic, "peak_kind": peak_kind, "bytes_per_hop": abph,
+                     "note": ("algorithmic bytes per hop (plain CSR walk with FP32 cumulative rows at the measured "
+                              "mean row length) x hops / hop-kernel device time; rows the excitons in flight hop "
+                              "over are served mostly from L2, so DRAM traffic (traffic, per launch) stays below "
+                              "the algorithmic bytes"),
+                     "kernel_layout": {"bytes_per_hop": bph, "achieved": kernel_achieved,
+                                       "frac": kernel_achieved / peak,
+                                       "note": "the two dependent 64-byte lines (site record, row block) this "
+                                               "kernel reads per hop, +32 B second level for rows over 64 entries"},
+                     "dram_bytes_per_hop": (traffic * max(hop_launches, 1) / hops) if traffic else None,
                      "l2": l2},
         "gpu_launches": launches,
         "autotune": tune,
