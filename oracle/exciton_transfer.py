@@ -30,11 +30,16 @@ What it restates (reference project paths):
 * ``calculate_vq``: cnt::calculate_vq (cnt.cpp:520-631), the Fourier sums of the Ohno
   potential per sublattice pair that the dielectric function and the Bethe-Salpeter kernel use.
 
-Parity: unpinned against the reference.  cnt.cpp and exciton_transfer.cpp need Armadillo's
-complex matrices, cubes, fields and eig_sym, which the shim behind the oracle's other parts does
-not provide.  The tests check tube-geometry invariants, a brute-force double loop, far-field
-and conjugation identities, and the bands against zone-folded graphene (to rounding with an
-exact pi; the reference's pi = 3.141592 moves them by ~1e-5 t0) instead.
+Parity: pinned against the reference's own code.  oracle/_ref/ref_exciton is cnt.cpp and
+exciton_transfer.cpp compiled unchanged against a second Armadillo shim (oracle/shim_et), and
+tests/golden/ref_et_*.npz hold what it computes for four tube pairs (the two pairs of the
+reference's input.json and two of the surrogate's chiralities).  This restatement reproduces
+them: lattice vectors, K2-extended parameters, valleys and relevant-state windows exactly; bands,
+vq, PI, eps and the A-exciton energies to ~1e-15 relative; J to ~1e-14; |Q|, M and the
+first-order rate to ~1e-12 (tests/test_exciton_transfer_golden.py).  Eigenvector phases are not
+compared (neither LAPACK's nor the shim's Jacobi fixes them); everything compared is phase-free.
+The older tests also check tube-geometry invariants, a brute-force double loop, far-field and
+conjugation identities, and the bands against zone-folded graphene.
 """
 from __future__ import annotations
 
@@ -466,6 +471,17 @@ def area_u(g: dict) -> float:
     return abs(g["a1"][0] * g["a2"][1] - g["a1"][1] * g["a2"][0])
 
 
+def q_coeff(gd: dict, ga: dict) -> float:
+    """The prefactor of calculate_Q (exciton_transfer.cpp:299-301)."""
+    return (Q0 ** 2 * area_u(gd) * area_u(ga)) / (16 * PI ** 3 * EPS0 * gd["radius"] * ga["radius"]
+                                                   * math.sqrt(length_m(gd) * length_m(ga)))
+
+
+def calculate_q(gd: dict, exd: dict, ga: dict, exa: dict, d_state, a_state) -> complex:
+    """calculate_Q (exciton_transfer.cpp:273-304) of one donor/acceptor state pair."""
+    return q_coeff(gd, ga) * np.conj(q_partial(gd, exd, d_state)) * q_partial(ga, exa, a_state)
+
+
 def first_order(gd: dict, exd: dict, ga: dict, exa: dict, z_shift: float, axis_shifts=(0., 0.), theta: float = 0.,
                 temperature: float = 300.) -> float:
     """exciton_transfer::first_order (exciton_transfer.cpp:380-424): the thermal, Lorentzian-matched
@@ -474,14 +490,12 @@ def first_order(gd: dict, exd: dict, ga: dict, exa: dict, z_shift: float, axis_s
     ds = relevant_states(exd, min_energy, temperature)
     as_ = relevant_states(exa, min_energy, temperature)
     Z = sum(math.exp(-d[0] / (KB * temperature)) for d in ds)
-    coeff = (Q0 ** 2 * area_u(gd) * area_u(ga)) / (16 * PI ** 3 * EPS0 * gd["radius"] * ga["radius"]
-                                                    * math.sqrt(length_m(gd) * length_m(ga)))
     rate = 0.0
     for d in ds:
         for a in as_:
             if not lorentzian(d[0] - a[0]) > 1.e-2 * lorentzian(0.0):
                 continue
-            Q = coeff * np.conj(q_partial(gd, exd, d)) * q_partial(ga, exa, a)
+            Q = calculate_q(gd, exd, ga, exa, d, a)
             J = coulomb_j(gd, ga, d[1], a[1], axis_shifts, z_shift, theta)
             M = abs(Q * J) / math.sqrt(length_m(gd) * length_m(ga))
             rate += (2 * PI / HB) * (math.exp(-d[0] / (KB * temperature)) / Z) * M ** 2 * lorentzian(d[0] - a[0])
