@@ -13,9 +13,11 @@
 // max_hopping_radius over the film's bounding box); larger inputs are rejected with
 // KMC_ERR_ARG and a message.  The first call on a device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call before any stream
-// capture.  All calls share the one array, and each call clears what must start at zero; calls
-// whose GPU work overlaps (different streams or host threads on the same device) race on it
-// and must be serialised by the caller.
+// capture.  The address is kept for the life of the process, so the entry point must not be
+// called again on a device after cudaDeviceReset (the library's module, and the array with it,
+// is reloaded at a new address).  All calls share the one array, and each call clears what must
+// start at zero; calls whose GPU work overlaps (different streams or host threads on the same
+// device) race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -34,6 +36,7 @@ using namespace kmc;
 struct NoAllocScratch {
   int32_t cell_of[KMC_NOALLOC_MAX_SITES];
   int32_t members[KMC_NOALLOC_MAX_SITES];
+  int32_t sorted[KMC_NOALLOC_MAX_SITES];  // members of a cell in site order, before the copy back
   int32_t cell_start[KMC_NOALLOC_MAX_CELLS + 1];
   int32_t cursor[KMC_NOALLOC_MAX_CELLS];
   unsigned long long dom[6];  // order-preserving keys of min x,y,z and max x,y,z
@@ -138,20 +141,35 @@ __global__ void k_na_scatter(int64_t n, NoAllocScratch* sc) {
   sc->members[sc->cell_start[c] + k] = (int32_t)s;
 }
 
-// members back into site order (push_back order of monte_carlo.h:389-395)
-__global__ void k_na_sort(int32_t n_cells, NoAllocScratch* sc) {
-  int32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n_cells) return;
-  int32_t b = sc->cell_start[c], e = sc->cell_start[c + 1];
-  for (int32_t i = b + 1; i < e; ++i) {
-    int32_t v = sc->members[i];
-    int32_t j = i - 1;
-    while (j >= b && sc->members[j] > v) {
-      sc->members[j + 1] = sc->members[j];
-      --j;
+// Members back into site order (push_back order of monte_carlo.h:389-395): one block per cell.
+// Site ids are distinct, so a member's place is the number of members with a smaller id; each
+// thread counts that for its members against the cell's members staged through shared memory,
+// tile by tile, and writes them to `sorted`, which the block then copies back.  m members cost
+// m^2 / blockDim comparisons per thread from shared memory (a whole 65,536-site film in one cell:
+// ~17 M per thread), against m^2 dependent global accesses for a per-cell insertion sort.
+constexpr int kNaSortThreads = 256;
+constexpr int kNaSortTile = 2048;
+__global__ void __launch_bounds__(kNaSortThreads) k_na_sort(NoAllocScratch* sc) {
+  __shared__ int32_t tile[kNaSortTile];
+  const int32_t c = blockIdx.x;
+  const int32_t b = sc->cell_start[c], m = sc->cell_start[c + 1] - b;
+  if (m < 2) return;  // uniform over the block
+  for (int32_t i0 = 0; i0 < m; i0 += kNaSortThreads) {
+    const int32_t i = i0 + (int32_t)threadIdx.x;
+    const int32_t v = i < m ? sc->members[b + i] : 0;
+    int32_t rank = 0;
+    for (int32_t t0 = 0; t0 < m; t0 += kNaSortTile) {
+      const int32_t nt = min(kNaSortTile, m - t0);
+      __syncthreads();
+      for (int32_t j = threadIdx.x; j < nt; j += kNaSortThreads) tile[j] = sc->members[b + t0 + j];
+      __syncthreads();
+      if (i < m)
+        for (int32_t j = 0; j < nt; ++j) rank += tile[j] < v ? 1 : 0;
     }
-    sc->members[j + 1] = v;
+    if (i < m) sc->sorted[b + rank] = v;
   }
+  __syncthreads();  // the block's writes to `sorted` are visible to the whole block
+  for (int32_t i = threadIdx.x; i < m; i += kNaSortThreads) sc->members[b + i] = sc->sorted[b + i];
 }
 
 // neighbours of site s in find_neighbors order (scatterer.cpp:34-83; cells x-outer, y, z-inner)
@@ -309,7 +327,7 @@ extern "C" int kmc_build_neighbors_noalloc(const double* pos, const double* orie
   k_na_cells<<<nb, 256, 0, st>>>(pos, n_sites, g, sc);
   k_na_scan<int32_t><<<1, 1024, 0, st>>>(sc->cell_start, (int64_t)g.n_cells + 1);
   k_na_scatter<<<nb, 256, 0, st>>>(n_sites, sc);
-  k_na_sort<<<(unsigned)((g.n_cells + 127) / 128), 128, 0, st>>>(g.n_cells, sc);
+  k_na_sort<<<(unsigned)g.n_cells, kNaSortThreads, 0, st>>>(sc);
   // row lengths -> row pointers (caller's buffer)
   k_na_count<<<(unsigned)((n_sites + 1 + 127) / 128), 128, 0, st>>>(pos, n_sites, g, max_hopping_radius, sc, rowptr);
   k_na_scan<int64_t><<<1, 1024, 0, st>>>(rowptr, n_sites + 1);

@@ -5,7 +5,9 @@ cudaMalloc while they run.  This entry point builds one film's neighbour/rate CS
 the caller passes, using a fixed device array for its intermediate storage.  The test allocates
 the buffers itself (with torch) and checks the result against kmc_build_neighbors +
 kmc_get_neighbors bit for bit, on two different films in a row (the second smaller, so stale
-contents of the shared array would show), plus the sizing call and the size limits.
+contents of the shared array would show), plus the sizing call and the size limits; that a
+call after the first leaves the device's free memory unchanged; and that a film crowded into a
+few cells (hundreds of sites per cell) keeps every cell's members in site order.
 """
 import ctypes as C
 
@@ -112,3 +114,63 @@ def test_noalloc_rejects_sizes_beyond_its_limits():
     rc = lib.kmc_build_neighbors_noalloc(_ptr(pos, C.c_double), _ptr(pos, C.c_double), 2, C.byref(t), 1e-9,
                                          _ptr(rowptr, C.c_int64), None, None, p, 0, C.byref(nnz), None, err, 256)
     assert rc == L.KMC_ERR_ARG and b"cells" in err.value
+
+
+def _buffers(torch, f, tab):
+    """Device inputs and a kmc_table of device pointers for one film (kept alive by the caller)."""
+    keep = {"pos": _dev(torch, f.pos_m(), torch.float64), "ori": _dev(torch, f.orient, torch.float64),
+            "grids": [_dev(torch, g, torch.float64) for g in tab["grids"]],
+            "rate": _dev(torch, np.ravel(tab["rate"]), torch.float64)}
+    t = L.kmc_table()
+    t.kind = tab["kind"]
+    for d, g in enumerate(keep["grids"]):
+        t.n[d] = g.numel()
+        t.grid[d] = _ptr(g, C.c_double)
+    t.rate = _ptr(keep["rate"], C.c_double)
+    return keep, t
+
+
+def test_noalloc_leaves_device_free_memory_unchanged():
+    # everything the call needs is allocated here first; a second call (the first may load the
+    # library's kernels) must not change the device's free memory
+    torch = pytest.importorskip("torch")
+    lib = L.load()
+    f = F.straight_tubes(40, 60.0, box_nm=(120.0, 120.0, 8.0), seed=5)
+    ref = _existing(f, tables.forster_2d(1e15), 10e-9)
+    keep, t = _buffers(torch, f, tables.forster_2d(1e15))
+    n, cap = f.n_sites, int(ref["rowptr"][-1])
+    rowptr = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    total = torch.zeros(n, dtype=torch.float64, device="cuda")
+    col = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    cum = torch.zeros(cap, dtype=torch.float64, device="cuda")
+    nnz = C.c_int64(-1)
+    err = C.create_string_buffer(256)
+
+    def call():
+        rc = lib.kmc_build_neighbors_noalloc(_ptr(keep["pos"], C.c_double), _ptr(keep["ori"], C.c_double), n,
+                                             C.byref(t), 10e-9, _ptr(rowptr, C.c_int64), _ptr(col, C.c_int32),
+                                             _ptr(cum, C.c_double), _ptr(total, C.c_double), cap, C.byref(nnz), None,
+                                             err, 256)
+        assert rc == L.KMC_OK, err.value
+
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert np.array_equal(col.cpu().numpy(), ref["col"]) and np.array_equal(cum.cpu().numpy(), ref["cum"])
+
+
+def test_noalloc_crowded_cells_match_build_neighbors():
+    # 2,000 sites in about 20 x 20 x 5 nm with a 10 nm radius: 18 cells of ~110 sites each (the
+    # per-cell ranking runs over many members, more than one pass of the block's threads in the
+    # fullest cells)
+    torch = pytest.importorskip("torch")
+    f = F.straight_tubes(400, 5.0, box_nm=(15.0, 15.0, 4.0), seed=11)
+    tab = tables.forster_2d(1e15)
+    got = _noalloc(torch, f, tab, 10e-9)
+    ref = _existing(f, tab, 10e-9)
+    for k in ("rowptr", "col", "cum", "total"):
+        assert np.array_equal(got[k], ref[k]), k
