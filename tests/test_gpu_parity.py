@@ -509,3 +509,63 @@ def test_zero_rate_entries_match_oracle(precision):
     assert_msd_close(e.msd(0, steps), om)
     assert e.stats()["hops"] == sim.total_hops()
     e.close()
+
+
+def bad_table(kind):
+    """The 2-D Förster-form table with bad values planted at a few grid points: NaN (rows with a
+    NaN total: excitons landing there get a NaN dwell clock and never hop again), +inf (rows with
+    an infinite total: zero dwell times, the selection clamps to the last neighbour) or negative
+    rates (rows whose cumulative values fall; a few rows with a negative total)."""
+    base = tables.forster_2d(1e15)
+    r = base["rate"].copy()
+    if kind == "nan":
+        r[50, 10:20] = np.nan
+    elif kind == "inf":
+        r[80, 45] = np.inf
+    else:
+        r[:, 60:70] *= -1.0
+        r[5:9, 60:62] *= 1e3
+    return {"kind": 2, "grids": base["grids"], "rate": r}
+
+
+def same_bits_or_both_nan(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    if a.dtype.kind != "f":
+        return np.array_equal(a, b)
+    return a.shape == b.shape and bool(np.all((a == b) | (np.isnan(a) & np.isnan(b))))
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("kind", ["nan", "inf", "neg"])
+def test_bad_table_values_follow_the_oracle(kind, precision):
+    # the reference has no check on its table; NaN, infinite and negative rates flow through
+    # its prefix sum, dwell time and bisection (scatterer.cpp:9-31, scatterer.h:74-93).  The
+    # engine routes such rows to the FP64 bisection and must land where the oracle lands
+    f = F.straight_tubes(40, 60.0, box_nm=(120.0, 120.0, 8.0), seed=5)
+    tab = bad_table(kind)
+    n_exc, seed, dt, v, steps = 800, 77, 2e-13, 2e5, 8
+    sim = O.Sim(f.pos_m(), f.orient, f.left, f.right, tab, 10e-9, v)
+    csr = sim.build_csr()
+    bad_rows = {"nan": np.isnan(csr["total"]), "inf": np.isinf(csr["total"]),
+                "neg": csr["total"] < 0}[kind]
+    assert np.any(bad_rows)
+    sim.create_excitons(1, 0, n_exc, seed)
+    om = sim.step(dt, steps)
+    o = sim.excitons()
+    e = E.Engine(0)
+    e.load_films(f)
+    e.set_table(tab)
+    st = e.build(10e-9)
+    nb = e.neighbors(f.n_sites, st["nnz"])
+    for k in ("rowptr", "col", "cum", "total"):
+        assert same_bits_or_both_nan(nb[k], csr[k]), k
+    e.init_excitons(n_exc, seed, L.KMC_INJECT_UNIFORM)
+    e.run(steps, dt, v, precision)
+    g = e.excitons()
+    for k in ("site", "pos", "delta", "ff", "heading", "draws"):
+        assert same_bits_or_both_nan(g[k], o[k]), k
+    if kind == "nan":
+        assert np.isnan(g["ff"]).sum() > 100  # excitons frozen on NaN rows
+    assert e.stats()["hops"] == sim.total_hops()
+    np.testing.assert_allclose(e.msd(0, steps).ravel(), om.ravel(), rtol=MSD_RTOL, atol=0)
+    e.close()
