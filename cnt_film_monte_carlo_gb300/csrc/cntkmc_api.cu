@@ -168,7 +168,7 @@ struct kmc_ctx {
   // what the captured contacts step depends on; an unchanged key replays it without a new capture
   struct ContactsGraphKey {
     double dt, v;
-    int32_t precision, variant, ordered, grid_blocks, single_film;
+    int32_t precision, variant, ordered, grid_blocks, single_film, hold_short;
     int64_t hop_cap, n_trace, n_slots;
     const void *pop, *diff, *live, *msd, *order, *cargs_step;
   } cgkey{};
@@ -190,6 +190,14 @@ struct kmc_ctx {
                                 "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
   } while (0)
 
+// Film, table, species, neighbour lists, trace or batch settings changed: the excitons (and a
+// contacts set-up, whose slot lists and captured step hold the old buffers' addresses) are gone.
+static void drop_excitons(kmc_ctx* c) {
+  c->inited = false;
+  c->contacts = false;
+  c->cgkey_valid = false;
+}
+
 template <typename T>
 static cudaError_t upload(DevBuf<T>& b, const T* h, size_t n, cudaStream_t s) {
   cudaError_t e = b.alloc(n);
@@ -197,6 +205,12 @@ static cudaError_t upload(DevBuf<T>& b, const T* h, size_t n, cudaStream_t s) {
   if (n) e = cudaMemcpyAsync(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s);
   return e;
 }
+
+namespace kmc {
+int ctx_device(const kmc_ctx* c) { return c->device; }
+cudaStream_t ctx_stream(const kmc_ctx* c) { return c->stream; }
+void ctx_set_error(kmc_ctx* c, const char* msg) { c->err = msg; }
+}  // namespace kmc
 
 extern "C" {
 
@@ -326,7 +340,7 @@ int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
   c->film_loaded = true;
   c->n_species = 0;
   c->built = false;
-  c->inited = false;
+  drop_excitons(c);
   return KMC_OK;
 }
 
@@ -343,7 +357,7 @@ int kmc_set_site_species(kmc_ctx* c, const int32_t* species, int32_t n_species) 
   CK(c, cudaStreamSynchronize(c->stream));
   c->n_species = n_species;
   c->built = false;
-  c->inited = false;
+  drop_excitons(c);
   return KMC_OK;
 }
 
@@ -376,7 +390,7 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   CK(c, cudaStreamSynchronize(c->stream));
   c->has_table = true;
   c->built = false;
-  c->inited = false;
+  drop_excitons(c);
   return KMC_OK;
 }
 
@@ -548,7 +562,7 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   c->r_max = r_max;
   c->lt_v = -1;
   c->built = true;
-  c->inited = false;
+  drop_excitons(c);
   if (st) {
     st->n_sites = n;
     st->nnz = c->nnz;
@@ -567,7 +581,7 @@ int kmc_set_trace(kmc_ctx* c, int64_t n_trace, int64_t cap) {
   if (n_trace < 0 || cap < 0 || (n_trace > 0 && cap == 0)) FAIL(c, KMC_ERR_ARG, "kmc_set_trace: bad sizes");
   c->n_trace = n_trace;
   c->trace_cap = cap;
-  c->inited = false;
+  drop_excitons(c);
   return KMC_OK;
 }
 
@@ -1122,7 +1136,8 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
 int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision, int64_t* population,
                      int64_t* current, int64_t* n_live) {
   if (!c) return KMC_ERR_ARG;
-  if (!c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_contacts_run: set up contacts mode first (kmc_contacts_init)");
+  if (!c->contacts || !c->built || !c->inited)
+    FAIL(c, KMC_ERR_STATE, "kmc_contacts_run: set up contacts mode first (kmc_contacts_init)");
   if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_contacts_run: bad step count, time step or velocity");
   if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_contacts_run: bad precision");
   CK(c, cudaSetDevice(c->device));
@@ -1168,6 +1183,7 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
     key.ordered = plan.ordered ? 1 : 0;
     key.grid_blocks = plan.grid_blocks;
     key.single_film = plan.single_film;
+    key.hold_short = a.hold_short;
     key.hop_cap = c->hop_cap;
     key.n_trace = c->n_trace;
     key.n_slots = c->n_slots;
@@ -1232,7 +1248,8 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
 int kmc_contacts_track(kmc_ctx* c, int64_t first, int32_t n_tracks, double dt, double v, int64_t max_steps,
                        double* path, int64_t* len, int32_t* arrived) {
   if (!c) return KMC_ERR_ARG;
-  if (!c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_contacts_track: set up contacts mode first (kmc_contacts_init)");
+  if (!c->contacts || !c->built || !c->inited)
+    FAIL(c, KMC_ERR_STATE, "kmc_contacts_track: set up contacts mode first (kmc_contacts_init)");
   if (first < 0 || n_tracks < 0 || max_steps < 0 || !(dt >= 0) || !(v > 0) || (n_tracks > 0 && (!path || !len || !arrived)))
     FAIL(c, KMC_ERR_ARG, "kmc_contacts_track: bad arguments");
   if (c->cargs.c_n[0] == 0) FAIL(c, KMC_ERR_ARG, "kmc_contacts_track: contact 1 has no site");
@@ -1438,7 +1455,7 @@ int kmc_set_msd_batches(kmc_ctx* c, int32_t batches) {
   if (!c) return KMC_ERR_ARG;
   if (batches < 1 || batches > 4096) FAIL(c, KMC_ERR_ARG, "kmc_set_msd_batches: 1..4096 batches");
   c->msd_batches = batches;
-  c->inited = false;
+  drop_excitons(c);
   return KMC_OK;
 }
 

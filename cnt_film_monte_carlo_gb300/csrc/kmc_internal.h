@@ -12,6 +12,8 @@
 #define KMC_ERR_FLIGHT_CODE 4    // a free flight crossed more than kMaxCrossings links
 #define KMC_ERR_CAPACITY_CODE 8  // contacts mode: fewer empty slots than new excitons
 
+struct kmc_ctx;  // the engine context (include/cntkmc.h; defined in cntkmc_api.cu)
+
 namespace kmc {
 
 // Per-film constants (device copy).
@@ -279,5 +281,10 @@ cudaError_t launch_mlp_predict(const MlpDev& m, const double* dist, const double
                                int64_t n, double* log_rate, cudaStream_t s);
 cudaError_t launch_mlp_table(const MlpDev& m, const double* dist, int32_t nd, const double* theta, int32_t nt,
                              double* rate, cudaStream_t s);
+
+// a context's device and stream, and its error message, for the modules outside cntkmc_api.cu
+int ctx_device(const kmc_ctx* c);
+cudaStream_t ctx_stream(const kmc_ctx* c);
+void ctx_set_error(kmc_ctx* c, const char* msg);
 
 }  // namespace kmc

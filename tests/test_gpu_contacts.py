@@ -313,3 +313,41 @@ def test_contacts_argument_and_state_errors():
         e.contacts_init(4, (10, 0), 1, 0)
     assert ei.value.code == L.KMC_ERR_ARG
     e.close()
+
+
+@pytest.mark.parametrize("change", ["build", "table", "film", "trace", "batches"])
+def test_contacts_refused_after_buffers_change(change):
+    # every call that reallocates the sites, rows, trace or exciton buffers ends the contacts
+    # set-up: the captured contacts step holds the old buffers' addresses, so running it would
+    # read freed memory; the library refuses instead, and a fresh set-up runs again
+    d = load_case(CONTACT_CASES[0])
+    c = contacts_inputs(d)
+    off = np.array([0, len(c["left"])], np.int64)
+    e = E.Engine(0)
+    e.load_arrays(off, c["pos"], c["orient"], c["left"], c["right"])
+    e.set_table(c["table"])
+    e.build(c["r_max"])
+    e.contacts_init(4, (50, 10), 1, 0)
+    e.contacts_run(2, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    if change == "build":
+        e.build(c["r_max"])
+    elif change == "table":
+        e.set_table(c["table"])
+    elif change == "film":
+        e.load_arrays(off, c["pos"], c["orient"], c["left"], c["right"])
+    elif change == "trace":
+        e.set_trace(4, 64)
+    else:
+        e.set_msd_batches(2)
+    for call in (lambda: e.contacts_run(1, c["dt"], c["v"], L.KMC_PREC_MIXED),
+                 lambda: e.contacts_track(0, 1, c["dt"], c["v"], 10)):
+        with pytest.raises(L.KmcError) as ei:
+            call()
+        assert ei.value.code == L.KMC_ERR_STATE
+    if change in ("table", "film"):
+        e.set_table(c["table"])
+        e.build(c["r_max"])
+    e.contacts_init(4, (50, 10), 1, 0)
+    _, _, live = e.contacts_run(2, c["dt"], c["v"], L.KMC_PREC_MIXED)
+    assert live[-1] > 0
+    e.close()
