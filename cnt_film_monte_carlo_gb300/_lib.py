@@ -36,6 +36,9 @@ KMC_ORDER_SLOTS = 0
 KMC_ORDER_SPATIAL = 1
 KMC_NOALLOC_MAX_SITES = 65536
 KMC_NOALLOC_MAX_CELLS = 65536
+KMC_CNT_MAX_RELEVANT = 64
+(KMC_CNT_GEOMETRY, KMC_CNT_POS_U_3D, KMC_CNT_BANDS, KMC_CNT_VALLEYS, KMC_CNT_RELEVANT, KMC_CNT_VQ, KMC_CNT_PI,
+ KMC_CNT_EPS, KMC_CNT_A1, KMC_CNT_A2_TRIPLET, KMC_CNT_A2_SINGLET, KMC_CNT_IK_IDX, KMC_CNT_Q_PARTIAL) = range(13)
 
 PD = C.POINTER(C.c_double)
 PI32 = C.POINTER(C.c_int32)
@@ -105,6 +108,16 @@ class kmc_mlp_train_stats(C.Structure):
     _fields_ = [("steps", C.c_int64), ("first_loss", C.c_double), ("last_loss", C.c_double), ("seconds", C.c_double)]
 
 
+class kmc_cnt_info(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("n", "m", "cells", "Nu", "M", "Q", "t1", "t2", "nk", "n_mu", "n_valley_pairs",
+                                         "n_relevant", "iq0", "nq", "mq0", "nmq", "ik_cm0", "nk_cm")] + \
+               [("radius", C.c_double), ("length", C.c_double), ("area_u", C.c_double)]
+
+
+class kmc_transfer_cfg(C.Structure):
+    _fields_ = [("temperature", C.c_double), ("broadening", C.c_double), ("precision", C.c_int32)]
+
+
 # every symbol include/cntkmc.h declares, with (restype, argtypes)
 SIGNATURES = {
     "kmc_create": (C.c_void_p, [C.c_int, C.POINTER(C.c_int)]),
@@ -157,6 +170,15 @@ SIGNATURES = {
     "kmc_mlp_predict": (C.c_int, [C.c_void_p, C.c_int64, PD, PD, PI32, PD]),
     "kmc_mlp_rate_table": (C.c_int, [C.c_void_p, C.c_int32, PD, C.c_int32, PD, PD]),
     "kmc_version": (C.c_char_p, []),
+    "kmc_cnt_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "kmc_cnt_destroy": (None, [C.c_void_p]),
+    "kmc_cnt_get_info": (C.c_int, [C.c_void_p, C.POINTER(kmc_cnt_info)]),
+    "kmc_cnt_get_array": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "kmc_exciton_j": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, PI32, PD, C.c_int32, PD]),
+    "kmc_exciton_rates": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(kmc_transfer_cfg), C.c_int64, PD,
+                                    PD]),
+    "kmc_davoody_table": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(kmc_transfer_cfg), PD, PD, PD, PD,
+                                    PD, PD, PD, PD, PD]),
 }
 
 _lib = None

@@ -25,7 +25,7 @@ CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math"
              f"-I{CSRC}"]
 
 CU_SOURCES = ["kmc_kernels.cu", "kmc_mixed_small.cu", "kmc_mixed_large.cu", "cntkmc_api.cu", "kmc_noalloc.cu", "kmc_contacts.cu",
-              "kmc_mlp.cu"]
+              "kmc_mlp.cu", "kmc_exciton.cu"]
 CXX_SOURCES = ["kmc_host.cpp"]
 DRIVER_SOURCES = ["driver.cpp"]
 

@@ -311,10 +311,11 @@ int kmc_autotune(kmc_ctx* ctx, double dt, double velocity, int64_t trial_steps, 
  *   finished its work.  err/err_len: optional buffer for a message.
  * Limits: n_sites <= KMC_NOALLOC_MAX_SITES and the film's cell grid (cells of side
  * max_hopping_radius) <= KMC_NOALLOC_MAX_CELLS; larger inputs are rejected with KMC_ERR_ARG.
- * Intermediate storage is one fixed device array (about 1 MB) that every GPU loading this
+ * Intermediate storage is one fixed device array (about 1.3 MB) that every GPU loading this
  * library keeps until exit.  The first call on a device looks up that array's address with the
- * device current; make it before any stream capture.  All calls share the array (each clears
- * what must start at zero); calls that overlap on the GPU race and must be serialised. */
+ * device current; make it before any stream capture, and do not call again on a device after
+ * cudaDeviceReset (the address is kept for the process).  All calls share the array (each
+ * clears what must start at zero); calls that overlap on the GPU race and must be serialised. */
 #define KMC_NOALLOC_MAX_SITES 65536
 #define KMC_NOALLOC_MAX_CELLS 65536
 int kmc_build_neighbors_noalloc(const double* pos, const double* orient, int64_t n_sites, const kmc_table* table,
@@ -409,6 +410,80 @@ int kmc_mlp_rate_table(kmc_ctx* ctx, int32_t nd, const double* dist, int32_t nt,
 
 /* Library version string. */
 const char* kmc_version(void);
+
+/* ---- exciton-transfer physics: the labeller of pair transfer rates ----
+ *
+ * The reference computes pair rates from a tight-binding / Bethe-Salpeter exciton model of each
+ * tube (src/exciton_transfer/cnt.cpp) and the first-order (Foerster-like) transfer rate between
+ * two tubes (src/exciton_transfer/exciton_transfer.cpp); its "davoody" rate table fills the 4-D
+ * scattering table with that rate (src/monte_carlo/monte_carlo.cpp:64-153).  Here the sums run on
+ * the GPU: vq, the polarisation, the Bethe-Salpeter kernels and their eigen-decompositions when a
+ * tube is created, and the Coulomb sum J of every matched state pair at every geometry.
+ * A geometry is (z_shift [m], axis shift 1 [m], axis shift 2 [m], theta [rad]) as in
+ * exciton_transfer::first_order: the donor along y shifted by axis shift 1, the acceptor shifted
+ * by axis shift 2 along its own axis and by z_shift in z, then rotated by theta about z. */
+typedef struct kmc_cnt kmc_cnt;
+
+#define KMC_CNT_MAX_RELEVANT 64 /* relevant states per valley (1 eV window): tubes up to ~80 nm */
+
+typedef struct {
+  int32_t n, m, cells, Nu, M, Q, t1, t2; /* chirality, length in unit cells, cnt parameters */
+  int32_t nk, n_mu;                      /* K2-extended grid */
+  int32_t n_valley_pairs, n_relevant;    /* valley pairs; relevant states per valley */
+  int32_t iq0, nq, mq0, nmq;             /* vq / PI / eps grid: iq in [iq0, iq0 + nq), mu likewise */
+  int32_t ik_cm0, nk_cm;                 /* exciton centre-of-mass momenta */
+  double radius, length, area_u;         /* m, m (cells x |T|), m^2 (graphene unit cell) */
+} kmc_cnt_info;
+
+/* What kmc_cnt_get_array copies out (doubles unless noted; complex as (re, im) pairs):
+ * GEOMETRY [26]: a1, a2, b1, b2, aCC, ch, t_vec, K1, K2, dk_l (2 each), t_vec_3d (3), radius,
+ *   |ch|, length; POS_U_3D [Nu][3]; BANDS [2][nk][n_mu] (valence, conduction); VALLEYS int32
+ *   [n_valley_pairs][2][2] (ik, mu); RELEVANT int32 [2][n_relevant][2]; VQ complex
+ *   [nq][nmq][4]; PI, EPS [nq][nmq]; A1, A2_TRIPLET, A2_SINGLET [nk_cm][n_relevant] (J);
+ *   IK_IDX int32 [nk_cm][4][2 n_relevant]; Q_PARTIAL complex [nk_cm][n_relevant]. */
+#define KMC_CNT_GEOMETRY 0
+#define KMC_CNT_POS_U_3D 1
+#define KMC_CNT_BANDS 2
+#define KMC_CNT_VALLEYS 3
+#define KMC_CNT_RELEVANT 4
+#define KMC_CNT_VQ 5
+#define KMC_CNT_PI 6
+#define KMC_CNT_EPS 7
+#define KMC_CNT_A1 8
+#define KMC_CNT_A2_TRIPLET 9
+#define KMC_CNT_A2_SINGLET 10
+#define KMC_CNT_IK_IDX 11
+#define KMC_CNT_Q_PARTIAL 12
+
+typedef struct {
+  double temperature;  /* K ("temperature", exciton_transfer.h:85-90; the table uses 300) */
+  double broadening;   /* J, Lorentzian half width (exciton_transfer.h:93-97; the table uses 4 meV) */
+  int32_t precision;   /* KMC_PREC_FP64: J in FP64; KMC_PREC_MIXED: FP32 positions and tile sums */
+} kmc_transfer_cfg;
+
+/* cnt(json) + cnt::calculate_exciton_dispersion (cnt.h:146-187, cnt.cpp:1056-1080): the exciton
+ * model of an (n, m) tube of length_cells unit cells, computed on the context's GPU.  The model
+ * lives in host memory; destroy it with kmc_cnt_destroy. */
+int kmc_cnt_create(kmc_ctx* ctx, int32_t n, int32_t m, int32_t length_cells, kmc_cnt** out);
+void kmc_cnt_destroy(kmc_cnt* tube);
+int kmc_cnt_get_info(const kmc_cnt* tube, kmc_cnt_info* info);
+/* Copy one of the model's arrays (KMC_CNT_*); count must equal its number of values. */
+int kmc_cnt_get_array(const kmc_cnt* tube, int32_t which, void* out, int64_t count);
+/* exciton_transfer::calculate_J (exciton_transfer.cpp:307-377) for n_pairs (donor ik_cm,
+ * acceptor ik_cm) pairs at one geometry; j_out complex [n_pairs][2]. */
+int kmc_exciton_j(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, int64_t n_pairs,
+                  const int32_t* ik_cm_pairs, const double geometry[4], int32_t precision, double* j_out);
+/* exciton_transfer::first_order (exciton_transfer.cpp:380-424) at n_geometries geometries
+ * [n][4]; rate [n] in 1/s. */
+int kmc_exciton_rates(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, const kmc_transfer_cfg* cfg,
+                      int64_t n_geometries, const double* geometries, double* rate);
+/* monte_carlo::create_davoody_scatt_table (monte_carlo.cpp:64-153): the first-order rate on the
+ * 4-D grid theta (degrees, scaled by the reference's pi / 180) x z_shift x axis shift 1 x axis
+ * shift 2 ({start, end, count} linspace each); outputs the grids and rate [nt][nz][n1][n2],
+ * the layout of a KMC_TABLE_4D table. */
+int kmc_davoody_table(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, const kmc_transfer_cfg* cfg,
+                      const double theta_deg[3], const double zshift[3], const double ash1[3], const double ash2[3],
+                      double* theta, double* zsh, double* a1, double* a2, double* rate);
 
 #ifdef __cplusplus
 }
