@@ -7,10 +7,12 @@ chiralities needs a table per (donor, acceptor) pair.  This module trains the en
 on labelled (distance, angle, pair) samples and turns it into a KMC_TABLE_2D_SPECIES table that
 the neighbour build reads per site pair.
 
-Labels come from the chirality-resolved Förster-form labeller (kmc_species_rates), which stands
-in for exciton_transfer in this package; the labeller's own tables stay the fallback and the
-yardstick of the network's error (``rate_errors``, and the diffusion coefficient of a film run
-with each table).
+Labels come from the reference's exciton-transfer model on the GPU
+(``exciton.PairLabeller``: exciton_transfer::first_order between tubes of the film's
+chiralities); its own tables stay the fallback and the yardstick of the network's error
+(``rate_errors``, and the diffusion coefficient of a film run with each table).  A closed-form
+chirality-resolved Förster labeller (kmc_species_rates, a model dict from ``species_model``)
+serves the unit tests of the network's kernels, which need cheap labels of a known form.
 """
 from __future__ import annotations
 
@@ -55,19 +57,27 @@ def neutral_model(n_species: int = 1, gamma_0: float = 1e15) -> dict:
             "near_field": 0.0}
 
 
-def n_species(model: dict) -> int:
-    return len(model["energy"])
+def n_species(labeller) -> int:
+    """Chiralities of a labeller: an exciton.PairLabeller or a closed-form model dict."""
+    return labeller.n_species if hasattr(labeller, "n_species") else len(labeller["energy"])
 
 
-def draw_samples(model: dict, n: int, seed: int = 0, d_range=D_RANGE) -> dict:
+def label(labeller, dist, theta, donor, acceptor) -> np.ndarray:
+    """Pair rates (1/s) from an exciton.PairLabeller or a closed-form model dict."""
+    if hasattr(labeller, "rates"):
+        return labeller.rates(dist, theta, donor, acceptor)
+    return E.species_rates(labeller, dist, theta, donor, acceptor)
+
+
+def draw_samples(labeller, n: int, seed: int = 0, d_range=D_RANGE) -> dict:
     """n labelled samples: distance and folded angle uniform, donor and acceptor uniform."""
     rng = np.random.default_rng(seed)
-    S = n_species(model)
+    S = n_species(labeller)
     dist = rng.uniform(d_range[0], d_range[1], n)
     theta = rng.uniform(0.0, math.pi / 2, n)
     donor = rng.integers(0, S, n).astype(np.int32)
     acceptor = rng.integers(0, S, n).astype(np.int32)
-    rate = E.species_rates(model, dist, theta, donor, acceptor)
+    rate = label(labeller, dist, theta, donor, acceptor)
     return {"dist": dist, "theta": theta, "donor": donor, "acceptor": acceptor,
             "pair": (donor * S + acceptor).astype(np.int32), "log_rate": np.log(rate)}
 
@@ -77,29 +87,33 @@ def grids(n_dist: int = 96, n_theta: int = 91, d_range=D_RANGE):
     return np.linspace(d_range[0], d_range[1], n_dist), np.linspace(0.0, math.pi / 2, n_theta)
 
 
-def labeller_table(model: dict, dist, theta) -> dict:
+def labeller_table(labeller, dist, theta) -> dict:
     """The labeller's own KMC_TABLE_2D_SPECIES table (the fallback the network replaces)."""
-    S = n_species(model)
+    S = n_species(labeller)
     dist = np.asarray(dist, np.float64)
     theta = np.asarray(theta, np.float64)
     a, b, i, k = np.meshgrid(np.arange(S), np.arange(S), np.arange(len(dist)), np.arange(len(theta)), indexing="ij")
-    rate = E.species_rates(model, dist[i.ravel()], theta[k.ravel()], a.ravel(), b.ravel())
+    rate = label(labeller, dist[i.ravel()], theta[k.ravel()], a.ravel(), b.ravel())
     return {"kind": 3, "grids": [dist, theta], "rate": rate.reshape(S, S, len(dist), len(theta))}
 
 
-def single_table(model: dict, dist, theta, species: int = 1) -> dict:
+def single_table(labeller, dist, theta, species: int = 1) -> dict:
     """One chirality's table used for every pair: a film modelled without the surrogate."""
-    t = labeller_table(model, dist, theta)
-    return {"kind": 2, "grids": t["grids"], "rate": t["rate"][species, species].copy()}
+    dist = np.asarray(dist, np.float64)
+    theta = np.asarray(theta, np.float64)
+    i, k = np.meshgrid(np.arange(len(dist)), np.arange(len(theta)), indexing="ij")
+    s = np.full(i.size, species)
+    rate = label(labeller, dist[i.ravel()], theta[k.ravel()], s, s)
+    return {"kind": 2, "grids": [dist, theta], "rate": rate.reshape(len(dist), len(theta))}
 
 
 class RateSurrogate:
     """The network of one engine context, trained on labelled samples."""
 
-    def __init__(self, engine: E.Engine, model: dict, d_range=D_RANGE):
+    def __init__(self, engine: E.Engine, labeller, d_range=D_RANGE):
         self.e = engine
-        self.model = model
-        self.S = n_species(model)
+        self.labeller = labeller
+        self.S = n_species(labeller)
         self.d_range = d_range
 
     def fit(self, samples: dict, epochs: int = 200, batch: int = BATCH, lr: float = 3e-3, lr_final: float = 3e-5,

@@ -36,9 +36,8 @@ def test_reference_arm_prints_one_contract_line(workload):
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
     assert d["config"]["workload"].startswith(workload)
-    if workload != "cfg5":  # cfg5's labeller tables come from the engine's library
-        # the reference arm's inputs come from the oracle and numpy: the engine is never loaded
-        assert "ENGINE_LIBRARY_NOT_MAPPED" in r.stderr
+    # the reference arm's inputs come from the oracle and numpy: the engine is never loaded
+    assert "ENGINE_LIBRARY_NOT_MAPPED" in r.stderr
 
 
 def test_gpu_arm_fails_loudly_without_a_device():

@@ -1,7 +1,8 @@
 """The learned pair-rate surrogate on the GPU, through the C ABI: forward, gradient and Adam step
 against the CPU oracle (oracle/mlp.py), deterministic training, the network's tables, the
-chirality-pair neighbour build against exact sums, and what the trained network gains for a
-mixed-chirality film over a single-chirality table."""
+chirality-pair neighbour build against exact sums, and, trained on labels of the reference's
+exciton-transfer model (exciton.PairLabeller), what the network gains over that labeller: the
+time to build a film's pair tables and the diffusion coefficient the tables give."""
 import math
 
 import numpy as np
@@ -245,10 +246,10 @@ def test_trained_network_rate_error(trained):
     assert np.median(rel) < 0.01
 
 
-def test_network_tables_reproduce_the_labeller_film_diffusion(trained):
-    # Mixed (6,5)/(7,5)/(8,3)/(8,4) film: D from the labeller's pair tables (the yardstick), from
-    # the network's tables, and from one (7,5) table for every pair (the film without the
-    # surrogate: a single exciton_transfer table).  Same excitons and Philox streams for all.
+def test_network_tables_reproduce_the_closed_form_labeller_film_diffusion(trained):
+    # Mixed (6,5)/(7,5)/(8,3)/(8,4) film with the closed-form labeller: D from its pair tables
+    # (the yardstick), from the network's tables, and from one (7,5) table for every pair.  Same
+    # excitons and Philox streams for all.
     model, net, st, held = trained
     f = F.straight_tubes(300, 80.0, (250.0, 250.0, 10.0), 5.0, 1.0, 21)
     sp = SG.site_species(f, np.random.default_rng(21).integers(0, 4, 300))
@@ -267,6 +268,61 @@ def test_network_tables_reproduce_the_labeller_film_diffusion(trained):
     (lab, cl), (nn, cn), (one, co) = runs["labeller"], runs["network"], runs["single"]
     assert abs(nn - lab) < 2 * np.hypot(cl, cn)
     assert abs(one - lab) > 3 * np.hypot(cl, co)
+
+
+@pytest.fixture(scope="module")
+def exciton_trained():
+    from cnt_film_monte_carlo_gb300 import exciton as X
+
+    e = E.Engine(0)
+    lab = X.PairLabeller(e)
+    train = SG.draw_samples(lab, 1_000_000, seed=200)
+    held = SG.draw_samples(lab, 100_000, seed=201)
+    net = SG.RateSurrogate(e, lab)
+    st = net.fit(train, epochs=200, lr=3e-3, lr_final=3e-5, seed=1)
+    yield lab, net, st, held
+    lab.close()
+    e.close()
+
+
+def test_network_trained_on_exciton_transfer_labels(exciton_trained):
+    # labels: exciton_transfer::first_order between ~40 nm tubes of (6,5), (7,5), (8,3), (8,4),
+    # computed on the GPU by the library's labeller
+    lab, net, st, held = exciton_trained
+    err = net.rate_errors(held)
+    print("rate errors on exciton-transfer labels", err, "training", st)
+    assert st["last_loss"] < st["first_loss"] / 100
+    assert err["median"] < 0.03 and err["p99"] < 0.3
+
+
+def test_network_replaces_the_exciton_labeller(exciton_trained):
+    # What the network gains over the labeller it replaces, on a mixed film of the four
+    # chiralities: its 16 pair tables (96 x 91) come orders of magnitude faster than the
+    # labeller's, and give the same in-plane diffusion coefficient within the statistical
+    # interval (same excitons and Philox streams); one (7,5) table for every pair (the film
+    # without per-pair rates) is reported beside them.
+    import time
+
+    lab, net, st, held = exciton_trained
+    dist, theta = SG.grids()
+    t0 = time.perf_counter()
+    lab_tab = SG.labeller_table(lab, dist, theta)
+    t_lab = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    net_tab = net.table(dist, theta)
+    t_net = time.perf_counter() - t0
+    f = F.straight_tubes(300, 80.0, (250.0, 250.0, 10.0), 5.0, 1.0, 21)
+    sp = SG.site_species(f, np.random.default_rng(21).integers(0, 4, 300))
+    args = (20000, 100, 1e-12, 2e5, 77)
+    runs = {}
+    for name, tab in (("labeller", lab_tab), ("network", net_tab),
+                      ("single", SG.single_table(lab, dist, theta, species=1))):
+        d, ci = SG.film_diffusion(f, sp, 4, tab, *args)
+        runs[name] = (float(np.mean(d[:2])), float(np.hypot(ci[0], ci[1]) / 2))
+    print("table seconds: labeller", t_lab, "network", t_net, "; in-plane D and 95 % interval", runs)
+    (dl, cl), (dn, cn) = runs["labeller"], runs["network"]
+    assert t_net * 50 < t_lab
+    assert abs(dn - dl) < 2 * np.hypot(cl, cn)
 
 
 @pytest.mark.parametrize("precision", [L.KMC_PREC_FP64, L.KMC_PREC_MIXED])
