@@ -89,6 +89,8 @@ def workload(name="cfg3", films=256, table=None):
 
 
 CFG5_FILMS, CFG5_EXC = 64, 100_000
+CFG5_EPOCHS = 600            # Adam epochs over the 2M labels (4.4 s on a GB300)
+CFG5_D_EXCITONS = 2_000_000  # excitons of each D comparison run (95 % interval ~ +-3.5 %)
 
 
 def cfg5_species(films):
@@ -113,12 +115,12 @@ def cfg5_surrogate(films, device):
     e = E.Engine(device)
     lab = X.PairLabeller(e)
     t0 = time.perf_counter()
-    train = SG.draw_samples(lab, 2_000_000, seed=100)
+    train = SG.draw_samples(lab, 2_000_000, seed=100, log_distance=True)
     t_label = time.perf_counter() - t0
     held = SG.draw_samples(lab, 200_000, seed=101)
     dist_g, theta_g = SG.grids()
     net = SG.RateSurrogate(e, lab)
-    st = net.fit(train, epochs=200, seed=1)
+    st = net.fit(train, epochs=CFG5_EPOCHS, seed=1)
     err = net.rate_errors(held)
     t0 = time.perf_counter()
     tab = net.table(dist_g, theta_g)
@@ -131,7 +133,7 @@ def cfg5_surrogate(films, device):
     e.close()
     f = F.straight_tubes(300, 80.0, (250.0, 250.0, 10.0), 5.0, 1.0, 21)
     sp = SG.site_species(f, np.random.default_rng(21).integers(0, 4, 300))
-    run = (200_000, 100, BIN, VEL, 77)
+    run = (CFG5_D_EXCITONS, 100, BIN, VEL, 77)
     d_lab, c_lab = SG.film_diffusion(f, sp, 4, lab_tab, *run, device=device)
     d_net, c_net = SG.film_diffusion(f, sp, 4, tab, *run, device=device)
     d_one, c_one = SG.film_diffusion(f, sp, 4, one_tab, *run, device=device)
@@ -140,12 +142,14 @@ def cfg5_surrogate(films, device):
         "network": "4 -> 64 -> 64 -> 1 GELU, BF16 weight matrices, FP32 sums; labels from exciton_transfer::first_order "
                    "between ~40 nm tubes of (6,5), (7,5), (8,3), (8,4), computed on the GPU (kmc_exciton_rates)",
         "labelling": {"samples": len(train["dist"]), "seconds": t_label, "samples_per_s": len(train["dist"]) / t_label},
-        "training": {"samples": len(train["dist"]), "epochs": 200, "steps": st["steps"], "seconds": st["seconds"],
+        "training": {"samples": len(train["dist"]), "epochs": CFG5_EPOCHS, "distance_sampling": "uniform in ln d",
+                     "steps": st["steps"], "seconds": st["seconds"],
                      "samples_per_s": st["steps"] * SG.BATCH / st["seconds"], "first_loss": st["first_loss"],
                      "last_loss": st["last_loss"]},
         "rate_error_held_out": err,
         "pair_tables_seconds": {"labeller": t_lab_table, "network": t_net_table, "tables": "16 x 96 x 91"},
-        "d_error": {"film": "300 tubes x 80 nm, 250x250x10 nm, 200,000 excitons, 100 x 1 ps, same Philox streams",
+        "d_error": {"film": f"300 tubes x 80 nm, 250x250x10 nm, {CFG5_D_EXCITONS} excitons, 100 x 1 ps, same Philox "
+                            "streams",
                     "labeller_in_plane": lab_d, "network_in_plane": net_d, "rel_error": net_d / lab_d - 1,
                     "ci95_labeller": float(np.hypot(c_lab[0], c_lab[1]) / 2),
                     "ci95_network": float(np.hypot(c_net[0], c_net[1]) / 2),

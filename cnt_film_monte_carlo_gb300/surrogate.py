@@ -69,11 +69,16 @@ def label(labeller, dist, theta, donor, acceptor) -> np.ndarray:
     return E.species_rates(labeller, dist, theta, donor, acceptor)
 
 
-def draw_samples(labeller, n: int, seed: int = 0, d_range=D_RANGE) -> dict:
-    """n labelled samples: distance and folded angle uniform, donor and acceptor uniform."""
+def draw_samples(labeller, n: int, seed: int = 0, d_range=D_RANGE, log_distance: bool = False) -> dict:
+    """n labelled samples: distance uniform (or, with log_distance, uniform in ln d, which puts
+    more samples where rates are large and change fastest), folded angle uniform, donor and
+    acceptor uniform."""
     rng = np.random.default_rng(seed)
     S = n_species(labeller)
-    dist = rng.uniform(d_range[0], d_range[1], n)
+    if log_distance:
+        dist = np.exp(rng.uniform(math.log(d_range[0]), math.log(d_range[1]), n))
+    else:
+        dist = rng.uniform(d_range[0], d_range[1], n)
     theta = rng.uniform(0.0, math.pi / 2, n)
     donor = rng.integers(0, S, n).astype(np.int32)
     acceptor = rng.integers(0, S, n).astype(np.int32)
