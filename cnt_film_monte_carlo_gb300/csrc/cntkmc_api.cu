@@ -86,7 +86,7 @@ struct kmc_ctx {
   // table
   bool has_table = false;
   kmc::TableDev table{};
-  DevBuf<double> d_grid[4], d_rate;
+  DevBuf<double> d_grid[4], d_rate, d_cut_d2, d_cut_cos;
   // chirality of each site (read by KMC_TABLE_2D_SPECIES tables); 0 = not set
   int32_t n_species = 0;
   DevBuf<int32_t> d_species;
@@ -387,6 +387,22 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   if (t->kind == KMC_TABLE_2D_SPECIES) c->table.n[2] = t->n[2];
   CK(c, upload(c->d_rate, t->rate, nr, c->stream));
   c->table.rate = c->d_rate.p;
+  // 2-D tables: grid midpoints for the neighbour build's lookup without sqrt and arccosine
+  // (pair_rate_2d); the distance grid must be non-negative and the angle grid inside [0, pi],
+  // where the square and the cosine are monotonic
+  if (dims == 2 && c->table.inv_h[0] > 0 && c->table.inv_h[1] > 0 && t->grid[0][0] >= 0 && t->grid[1][0] >= 0 &&
+      t->grid[1][t->n[1] - 1] <= 3.141592653589793) {
+    std::vector<double> cd(t->n[0] - 1), cc(t->n[1] - 1);
+    for (int32_t k = 0; k + 1 < t->n[0]; ++k) {
+      const double m = (t->grid[0][k] + t->grid[0][k + 1]) / 2;
+      cd[k] = m * m;
+    }
+    for (int32_t k = 0; k + 1 < t->n[1]; ++k) cc[k] = std::cos((t->grid[1][k] + t->grid[1][k + 1]) / 2);
+    CK(c, upload(c->d_cut_d2, cd.data(), cd.size(), c->stream));
+    CK(c, upload(c->d_cut_cos, cc.data(), cc.size(), c->stream));
+    c->table.cut_d2 = c->d_cut_d2.p;
+    c->table.cut_cos = c->d_cut_cos.p;
+  }
   CK(c, cudaStreamSynchronize(c->stream));
   c->has_table = true;
   c->built = false;

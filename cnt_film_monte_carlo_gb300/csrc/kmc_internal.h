@@ -62,6 +62,12 @@ struct TableDev {
   double inv_h[4];  // (n - 1) / (grid[n-1] - grid[0]) for ascending grids, 0: always scan in full
   const int32_t* species;  // kind 3: chirality of each site (reference id); pair table
                            // (species[donor], species[acceptor]) of n[2] x n[2]
+  // 2-D tables (kinds 2, 3) with ascending grids: the squared distances between neighbouring
+  // distance-grid points (cut_d2[k] = ((g_k + g_k+1) / 2)^2, ascending) and the cosines of the
+  // midpoints of the angle grid (cut_cos[k] = cos((g_k + g_k+1) / 2), descending); nullptr when
+  // the grids do not allow it (the lookup then always takes the exact path)
+  const double* cut_d2;
+  const double* cut_cos;
 };
 
 // Exciton flags

@@ -242,9 +242,14 @@ __global__ void k_nbr_fill(BuildArgs a) {
     const int32_t q = a.blocks[bo + (j >> 3)].col[j & 7];
     const double4_32a p2 = a.pos4[q];
     const double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
-    const double distance = norm3(dR0, dR1, dR2);
     double a2v[3] = {a.orient[3 * (int64_t)q], a.orient[3 * (int64_t)q + 1], a.orient[3 * (int64_t)q + 2]};
-    double rate = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance, pair_table(a.table, s, q));
+    double rate;
+    if (a.table.kind != 4) {
+      rate = pair_rate_2d(a.table, a1v, a2v, dR0, dR1, dR2, pair_table(a.table, s, q), p1, p2);
+    } else {
+      const double distance = norm3(dR0, dR1, dR2);
+      rate = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance, pair_table(a.table, s, q));
+    }
     negative |= rate < 0;
     run = (j == 0) ? rate : run + rate;  // in-place inclusive prefix sum, scatterer.cpp:78-80
     cump[j] = run;

@@ -60,4 +60,34 @@ __device__ __forceinline__ double pair_rate(const TableDev& t, const double4_32a
   return table_rate(t, theta, zsh, ash1, ash2, distance, pair_off);
 }
 
+// Rate of a 2-D table (kinds 2, 3) for a pair in the window, from dR and the two axes: the same
+// table entry as pair_rate, found without its FP64 square root and arccosine.  The nearest
+// distance index follows from d^2 against the squared midpoints of the distance grid, the
+// nearest angle index from |cos theta| against the cosines of the midpoints of the angle grid;
+// both are seeded by an FP32 estimate and confirmed in FP64 with a margin (1e-12 relative in d^2,
+// 1e-13 in |cos theta|) far wider than the rounding of the reference's own path (FP64 sqrt,
+// kmc_acos within 2 ulp, index_min's FP64 differences).  A value inside a margin, or an estimate
+// the check rejects, takes pair_rate's exact path, so the entry is always the one the reference
+// picks.
+__device__ __forceinline__ double pair_rate_2d(const TableDev& t, const double* a1v, const double* a2v, double dR0,
+                                               double dR1, double dR2, int64_t pair_off, const double4_32a& p1,
+                                               const double4_32a& p2) {
+  const double d2 = dot3(dR0, dR1, dR2, dR0, dR1, dR2);
+  const double cosT = dot3(a1v[0], a1v[1], a1v[2], a2v[0], a2v[1], a2v[2]);
+  const double ac = fabs(cosT);
+  if (t.cut_d2 && t.cut_cos && ac <= 1.0) {
+    const int n0 = t.n[0], n1 = t.n[1];
+    int c0 = (int)floorf(((float)sqrt((float)d2) - (float)t.grid[0][0]) * (float)t.inv_h[0] + 0.5f);
+    c0 = c0 < 0 ? 0 : (c0 > n0 - 1 ? n0 - 1 : c0);
+    int c1 = (int)floorf((acosf((float)ac) - (float)t.grid[1][0]) * (float)t.inv_h[1] + 0.5f);
+    c1 = c1 < 0 ? 0 : (c1 > n1 - 1 ? n1 - 1 : c1);
+    const bool ok0 = (c0 == 0 || d2 > t.cut_d2[c0 - 1] * (1.0 + 1e-12)) &&
+                     (c0 == n0 - 1 || d2 < t.cut_d2[c0] * (1.0 - 1e-12));
+    const bool ok1 = (c1 == 0 || ac < t.cut_cos[c1 - 1] - 1e-13) && (c1 == n1 - 1 || ac > t.cut_cos[c1] + 1e-13);
+    if (ok0 && ok1) return t.rate[pair_off + (int64_t)c0 * n1 + c1];
+  }
+  const double a1c[3] = {a1v[0], a1v[1], a1v[2]}, a2c[3] = {a2v[0], a2v[1], a2v[2]};
+  return pair_rate(t, p1, a1c, p2, a2c, dR0, dR1, dR2, sqrt(d2), pair_off);
+}
+
 }  // namespace kmc
