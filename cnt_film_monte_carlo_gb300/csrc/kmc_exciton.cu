@@ -604,7 +604,6 @@ struct Cx<double> {
   typedef double2 type;
 };
 
-__device__ __forceinline__ float inv_len(float r2) { return rsqrtf(r2); }
 __device__ __forceinline__ double inv_len(double r2) { return 1.0 / sqrt(r2); }
 
 constexpr int kJThreads = 128;
@@ -696,6 +695,92 @@ __global__ void __launch_bounds__(kJThreads) k_coulomb_j(const double3* __restri
     }
     __syncthreads();
     if (threadIdx.x < nq) {  // this block's partial, summed over blocks in order by k_j_reduce
+      double2 s = make_double2(0, 0);
+      for (int k = 0; k < kJThreads / 32; ++k) s = cadd(s, red[k][threadIdx.x]);
+      part[(((size_t)blockIdx.y * gridDim.x + blockIdx.x) * np + p) * nq + threadIdx.x] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// The FP32 form of k_coulomb_j for KMC_PREC_MIXED: base positions (float4) and acceptor phases
+// (float2) converted once on the host, the geometry applied in FP32, products accumulated with
+// fused multiply-adds and the tile sums added into a Kahan-compensated FP32 total per acceptor
+// momentum, so the FP64 pipe (1/64 of the FP32 rate on this GPU) is left out of the inner loops.
+template <int NQ>
+__global__ void __launch_bounds__(kJThreads) k_coulomb_j32(const float4* __restrict__ rd, int nd,
+                                                           const float4* __restrict__ ra, int na,
+                                                           const double2* __restrict__ ap, int np,
+                                                           const float2* __restrict__ bq, int nq,
+                                                           const JGeom* __restrict__ geo, double2* __restrict__ part) {
+  __shared__ float4 sr[kJTile];
+  __shared__ float2 sb[kJTile * NQ];
+  __shared__ double2 red[kJThreads / 32][NQ];
+  const JGeom g = geo[blockIdx.y];
+  const float ct = (float)g.ct, st = (float)g.st, a1 = (float)g.ash1, a2 = (float)g.ash2, zs = (float)g.zsh;
+  const int i = blockIdx.x * kJThreads + threadIdx.x;
+  const bool live = i < nd;
+  float xi = 0, yi = 0, zi = 0;
+  if (live) {
+    const float4 r = rd[i];
+    xi = r.x;
+    yi = r.y + a1;
+    zi = r.z;
+  }
+  float hx[NQ], hy[NQ], cx_[NQ], cy_[NQ];  // Kahan sums over the tiles
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) hx[q] = hy[q] = cx_[q] = cy_[q] = 0.f;
+  for (int j0 = 0; j0 < na; j0 += kJTile) {
+    const int nt = min(kJTile, na - j0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < nt; j += kJThreads) {
+      const float4 r = ra[j0 + j];
+      const float y = r.y + a2;
+      sr[j] = make_float4(r.x * ct - y * st, r.x * st + y * ct, r.z + zs, 0.f);
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) sb[j * NQ + q] = q < nq ? bq[(size_t)q * na + j0 + j] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float ax[NQ], ay[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) ax[q] = ay[q] = 0.f;
+    if (live)
+      for (int j = 0; j < nt; ++j) {
+        const float4 r = sr[j];
+        const float dx = xi - r.x, dy = yi - r.y, dz = zi - r.z;
+        const float inv = rsqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx)));
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+          const float2 b = sb[j * NQ + q];
+          ax[q] = __fmaf_rn(b.x, inv, ax[q]);
+          ay[q] = __fmaf_rn(b.y, inv, ay[q]);
+        }
+      }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {  // Kahan: sum += tile, carrying the rounding error
+      float y = ax[q] - cx_[q], t = hx[q] + y;
+      cx_[q] = (t - hx[q]) - y;
+      hx[q] = t;
+      y = ay[q] - cy_[q];
+      t = hy[q] + y;
+      cy_[q] = (t - hy[q]) - y;
+      hy[q] = t;
+    }
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int p = 0; p < np; ++p) {
+    const double2 a = live ? ap[(size_t)p * nd + i] : make_double2(0, 0);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      double2 v = cmul(a, make_double2((double)hx[q] - (double)cx_[q], (double)hy[q] - (double)cy_[q]));
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (l == 0) red[w][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nq) {
       double2 s = make_double2(0, 0);
       for (int k = 0; k < kJThreads / 32; ++k) s = cadd(s, red[k][threadIdx.x]);
       part[(((size_t)blockIdx.y * gridDim.x + blockIdx.x) * np + p) * nq + threadIdx.x] = s;
@@ -1014,13 +1099,16 @@ void launch_nq(int nq, dim3 grid, cudaStream_t st, const double3* rd, int nd, co
   else
     k_coulomb_j<T, 16><<<grid, kJThreads, 0, st>>>(rd, nd, ra, na, ap, np, bq, nq, geo, part);
 }
-void launch_coulomb_j(int32_t precision, int nq, dim3 grid, cudaStream_t st, const double3* rd, int nd,
-                      const double3* ra, int na, const double2* ap, int np, const double2* bq, const JGeom* geo,
-                      double2* part) {
-  if (precision == KMC_PREC_FP64)
-    launch_nq<double>(nq, grid, st, rd, nd, ra, na, ap, np, bq, geo, part);
+void launch_coulomb_j32(int nq, dim3 grid, cudaStream_t st, const float4* rd, int nd, const float4* ra, int na,
+                        const double2* ap, int np, const float2* bq, const JGeom* geo, double2* part) {
+  if (nq <= 2)
+    k_coulomb_j32<2><<<grid, kJThreads, 0, st>>>(rd, nd, ra, na, ap, np, bq, nq, geo, part);
+  else if (nq <= 4)
+    k_coulomb_j32<4><<<grid, kJThreads, 0, st>>>(rd, nd, ra, na, ap, np, bq, nq, geo, part);
+  else if (nq <= 8)
+    k_coulomb_j32<8><<<grid, kJThreads, 0, st>>>(rd, nd, ra, na, ap, np, bq, nq, geo, part);
   else
-    launch_nq<float>(nq, grid, st, rd, nd, ra, na, ap, np, bq, geo, part);
+    k_coulomb_j32<16><<<grid, kJThreads, 0, st>>>(rd, nd, ra, na, ap, np, bq, nq, geo, part);
 }
 
 // J[g][p][q] for the geometries geo[g] = (z_shift, ash1, ash2, theta)
@@ -1038,6 +1126,21 @@ int coulomb_j(const kmc_cnt& d, const kmc_cnt& a, const std::vector<int>& kd, co
   XCK(h2d(d_rd, rd.data(), rd.size(), st));
   XCK(h2d(d_ra, ra.data(), ra.size(), st));
   XCK(h2d(d_pd, pd.data(), pd.size(), st));
+  // the FP32 form's inputs, converted once
+  DBuf<float4> d_rd32, d_ra32;
+  DBuf<float2> d_pa32;
+  std::vector<float2> pa32;
+  if (precision != KMC_PREC_FP64) {
+    std::vector<float4> r32(rd.size());
+    for (size_t k = 0; k < rd.size(); ++k) r32[k] = make_float4((float)rd[k].x, (float)rd[k].y, (float)rd[k].z, 0.f);
+    XCK(h2d(d_rd32, r32.data(), r32.size(), st));
+    r32.resize(ra.size());
+    for (size_t k = 0; k < ra.size(); ++k) r32[k] = make_float4((float)ra[k].x, (float)ra[k].y, (float)ra[k].z, 0.f);
+    XCK(h2d(d_ra32, r32.data(), r32.size(), st));
+    XCK(cudaStreamSynchronize(st));  // r32 is reused below only after its copies are done
+    pa32.resize(pa.size());
+    for (size_t k = 0; k < pa.size(); ++k) pa32[k] = make_float2((float)pa[k].x, (float)pa[k].y);
+  }
   std::vector<JGeom> g(ng);
   for (int64_t i = 0; i < ng; ++i)
     g[i] = JGeom{geo[4 * i], geo[4 * i + 1], geo[4 * i + 2], std::cos(geo[4 * i + 3]), std::sin(geo[4 * i + 3])};
@@ -1049,7 +1152,10 @@ int coulomb_j(const kmc_cnt& d, const kmc_cnt& a, const std::vector<int>& kd, co
   std::vector<double2> Jc;
   for (int q0 = 0; q0 < nq_all; q0 += kJMaxQ) {
     const int nq = std::min(kJMaxQ, nq_all - q0);
-    XCK(h2d(d_pa, pa.data() + (size_t)q0 * ra.size(), (size_t)nq * ra.size(), st));
+    if (precision == KMC_PREC_FP64)
+      XCK(h2d(d_pa, pa.data() + (size_t)q0 * ra.size(), (size_t)nq * ra.size(), st));
+    else
+      XCK(h2d(d_pa32, pa32.data() + (size_t)q0 * ra.size(), (size_t)nq * ra.size(), st));
     DBuf<double2> d_Jc, d_part;
     const int ntile = (int)((rd.size() + kJThreads - 1) / kJThreads);
     XCK(d_Jc.alloc((size_t)ng * np * nq));
@@ -1058,8 +1164,12 @@ int coulomb_j(const kmc_cnt& d, const kmc_cnt& a, const std::vector<int>& kd, co
       const int gn = (int)std::min<int64_t>(65535, ng - g0);
       const dim3 grid((unsigned)ntile, (unsigned)gn);
       double2* pp = d_part.p + (size_t)g0 * ntile * np * nq;
-      launch_coulomb_j(precision, nq, grid, st, d_rd.p, (int)rd.size(), d_ra.p, (int)ra.size(), d_pd.p, np, d_pa.p,
-                       d_g.p + g0, pp);
+      if (precision == KMC_PREC_FP64)
+        launch_nq<double>(nq, grid, st, d_rd.p, (int)rd.size(), d_ra.p, (int)ra.size(), d_pd.p, np, d_pa.p,
+                          d_g.p + g0, pp);
+      else
+        launch_coulomb_j32(nq, grid, st, d_rd32.p, (int)rd.size(), d_ra32.p, (int)ra.size(), d_pd.p, np, d_pa32.p,
+                           d_g.p + g0, pp);
       XCK(cudaGetLastError());
     }
     const int64_t nj = (int64_t)ng * np * nq;
