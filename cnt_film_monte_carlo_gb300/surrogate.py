@@ -69,19 +69,33 @@ def label(labeller, dist, theta, donor, acceptor) -> np.ndarray:
     return E.species_rates(labeller, dist, theta, donor, acceptor)
 
 
+def contact_distance(labeller, donor, acceptor) -> np.ndarray:
+    """Closest centre distance of two tubes (m) per pair, below which the labeller's rate is flat;
+    0 for a labeller without one (the closed-form model)."""
+    donor, acceptor = np.asarray(donor), np.asarray(acceptor)
+    if not hasattr(labeller, "contact"):
+        return np.zeros(np.broadcast(donor, acceptor).shape)
+    S = n_species(labeller)
+    c = np.array([[labeller.contact(a, b) for b in range(S)] for a in range(S)])
+    return c[donor, acceptor]
+
+
 def draw_samples(labeller, n: int, seed: int = 0, d_range=D_RANGE, log_distance: bool = False) -> dict:
     """n labelled samples: distance uniform (or, with log_distance, uniform in ln d, which puts
     more samples where rates are large and change fastest), folded angle uniform, donor and
     acceptor uniform."""
     rng = np.random.default_rng(seed)
     S = n_species(labeller)
-    if log_distance:
-        dist = np.exp(rng.uniform(math.log(d_range[0]), math.log(d_range[1]), n))
-    else:
-        dist = rng.uniform(d_range[0], d_range[1], n)
+    u = rng.uniform(0.0, 1.0, n)
     theta = rng.uniform(0.0, math.pi / 2, n)
     donor = rng.integers(0, S, n).astype(np.int32)
     acceptor = rng.integers(0, S, n).astype(np.int32)
+    # a labeller with a contact distance (exciton.PairLabeller) is flat below it: samples start there
+    lo = np.maximum(d_range[0], contact_distance(labeller, donor, acceptor))
+    if log_distance:
+        dist = np.exp(np.log(lo) + u * (math.log(d_range[1]) - np.log(lo)))
+    else:
+        dist = lo + u * (d_range[1] - lo)
     rate = label(labeller, dist, theta, donor, acceptor)
     return {"dist": dist, "theta": theta, "donor": donor, "acceptor": acceptor,
             "pair": (donor * S + acceptor).astype(np.int32), "log_rate": np.log(rate)}
@@ -130,12 +144,28 @@ class RateSurrogate:
         self.e.mlp_set_samples(samples["dist"], samples["theta"], samples["pair"], lr_)
         return self.e.mlp_train(epochs, batch, lr, lr_final)
 
+    def _clamp(self, dist, pair):
+        pair = np.asarray(pair)
+        return np.maximum(np.asarray(dist, np.float64), contact_distance(self.labeller, pair // self.S, pair % self.S))
+
     def predict(self, dist, theta, pair) -> np.ndarray:
-        return self.e.mlp_predict(dist, theta, pair)
+        """ln(rate) of the network; below a pair's contact distance, its value at contact (the
+        labeller's rates are flat there and the network is trained from contact outwards)."""
+        return self.e.mlp_predict(self._clamp(dist, pair), theta, pair)
 
     def table(self, dist, theta) -> dict:
-        return {"kind": 3, "grids": [np.asarray(dist, np.float64), np.asarray(theta, np.float64)],
-                "rate": self.e.mlp_rate_table(dist, theta)}
+        dist, theta = np.asarray(dist, np.float64), np.asarray(theta, np.float64)
+        rate = self.e.mlp_rate_table(dist, theta)
+        if hasattr(self.labeller, "contact"):  # rows below contact take the contact-distance rate
+            for a in range(self.S):
+                for b in range(self.S):
+                    dc = self.labeller.contact(a, b)
+                    rows = np.nonzero(dist < dc)[0]
+                    if len(rows):
+                        at = np.exp(self.e.mlp_predict(np.full(len(theta), dc), theta,
+                                                       np.full(len(theta), a * self.S + b, np.int32)))
+                        rate[a, b, rows, :] = at[None, :]
+        return {"kind": 3, "grids": [dist, theta], "rate": rate}
 
     def rate_errors(self, samples: dict) -> dict:
         """Relative rate error |rate_net / rate_label - 1| over held-out samples."""
