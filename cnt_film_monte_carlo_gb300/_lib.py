@@ -12,6 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcntkmc.so")
+LIB_CHECK_PATH = os.path.join(HERE, "libcntkmc_check.so")  # the KMC_CHECK build (device bounds checks)
 
 KMC_OK = 0
 KMC_ERR_ARG = -1
@@ -22,6 +23,7 @@ KMC_ERR_HOP_CAP = -5
 KMC_ERR_NOMEM = -6
 KMC_ERR_NO_DEVICE = -7
 KMC_ERR_CAPACITY = -8
+KMC_ERR_CHECK = -9
 KMC_TABLE_4D = 4
 KMC_TABLE_2D = 2
 KMC_TABLE_2D_SPECIES = 3
@@ -137,6 +139,7 @@ SIGNATURES = {
     "kmc_contacts_track": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_double, C.c_int64, PD, PI64,
                                      PI32]),
     "kmc_get_excitons": (C.c_int, [C.c_void_p, PI32, PD, PD, PD, PI32, PU64, PI64]),
+    "kmc_set_excitons": (C.c_int, [C.c_void_p, PI32, PD, PD, PD, PI32, PU64, PI64]),
     "kmc_num_excitons": (C.c_int64, [C.c_void_p]),
     "kmc_get_run_stats": (C.c_int, [C.c_void_p, C.POINTER(kmc_run_stats)]),
     "kmc_get_neighbors": (C.c_int, [C.c_void_p, PI64, PI32, PD, PD]),
@@ -181,22 +184,24 @@ SIGNATURES = {
                                     PD, PD, PD, PD, PD]),
 }
 
-_lib = None
+_libs = {}
 
 
-def load():
-    """Load libcntkmc.so (fails loudly if it has not been built)."""
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise RuntimeError(f"{LIB_PATH} is missing: run cnt_film_monte_carlo_gb300.build.build() first")
-        lib = C.CDLL(LIB_PATH)
+def load(checked: bool = False):
+    """Load libcntkmc.so, or with checked=True libcntkmc_check.so (the same ABI with device bounds
+    checks); fails loudly if it has not been built.  Both may be loaded in one process: each is
+    opened locally and binds its own symbols."""
+    path = LIB_CHECK_PATH if checked else LIB_PATH
+    if path not in _libs:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run cnt_film_monte_carlo_gb300.build.build() first")
+        lib = C.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        _lib = lib
-    return _lib
+        _libs[path] = lib
+    return _libs[path]
 
 
 def ptr(a: np.ndarray, t):

@@ -1,7 +1,11 @@
-"""Build the engine's native code in-tree: libcntkmc.so (CUDA, sm_103a) and the drop-in driver.
+"""Build the engine's native code in-tree: libcntkmc.so (CUDA, sm_103a), its bounds-checked
+twin libcntkmc_check.so and the drop-in driver.
 
 nvcc cross-compiles sm_103a on a machine without a GPU.  Objects go to ``_build/`` next to
-this file; the shared library and the ``cntkmc_run`` driver land in this package directory.
+this file; the shared libraries and the ``cntkmc_run`` driver land in this package directory.
+libcntkmc_check.so is the same library with the hop, neighbour-build and contacts kernels
+compiled with -DKMC_CHECK: device bounds checks on site, row-block and link indices, MSD and
+slab bins and Philox counters, reported as KMC_ERR_CHECK (engine.Engine(checked=True)).
 """
 from __future__ import annotations
 
@@ -16,6 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libcntkmc.so")
+LIB_CHECK = os.path.join(HERE, "libcntkmc_check.so")
 DRIVER = os.path.join(HERE, "cntkmc_run")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -27,6 +32,7 @@ CXX_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math"
 CU_SOURCES = ["kmc_kernels.cu", "kmc_mixed_small.cu", "kmc_mixed_large.cu", "cntkmc_api.cu", "kmc_noalloc.cu", "kmc_contacts.cu",
               "kmc_mlp.cu", "kmc_exciton.cu"]
 CXX_SOURCES = ["kmc_host.cpp"]
+CHECK_SOURCES = ["kmc_kernels.cu", "kmc_mixed_small.cu", "kmc_mixed_large.cu", "kmc_contacts.cu"]  # -DKMC_CHECK twins
 DRIVER_SOURCES = ["driver.cpp"]
 
 
@@ -54,7 +60,7 @@ def _stale(target, deps):
 def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) -> str:
     """Compile (when sources changed) and return the path of libcntkmc.so."""
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".hpp"))]
     headers.append(os.path.join(INCLUDE, "cntkmc.h"))
     jobs, objs = [], []
     for src in CU_SOURCES:
@@ -70,12 +76,25 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(["g++"] + CXX_FLAGS + ["-c", s, "-o", o])
+    check_objs = []
+    for src in CU_SOURCES:
+        if src not in CHECK_SOURCES:
+            check_objs.append(os.path.join(BUILD, src + ".o"))
+            continue
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, "check_" + src + ".o")
+        check_objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append([nvcc()] + ARCH + NVCC_FLAGS + ["-DKMC_CHECK", "-c", s, "-o", o])
+    check_objs += [os.path.join(BUILD, src + ".o") for src in CXX_SOURCES]
     out = []
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         for text in ex.map(_run, jobs):
             out.append(text)
     if force or jobs or _stale(LIB, objs):
-        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]))
+        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"]))
+    if force or jobs or _stale(LIB_CHECK, check_objs):
+        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB_CHECK] + check_objs + ["-lcudart", "-ldl"]))
     drv_src = [os.path.join(CSRC, s) for s in DRIVER_SOURCES]
     if all(os.path.exists(s) for s in drv_src) and (force or _stale(DRIVER, drv_src + headers + [LIB])):
         out.append(_run(["g++"] + CXX_FLAGS + ["-o", DRIVER] + drv_src + ["-L" + HERE, "-lcntkmc",

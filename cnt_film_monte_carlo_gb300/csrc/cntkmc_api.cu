@@ -298,6 +298,7 @@ int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
   if (!f || f->n_films < 1 || !f->film_site_offsets || !f->pos || !f->orient || !f->left || !f->right)
     FAIL(c, KMC_ERR_ARG, "kmc_load_film: missing arrays");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_load_film");
   const int32_t nf = f->n_films;
   const int64_t n = f->film_site_offsets[nf];
   if (f->film_site_offsets[0] != 0 || n <= 0 || n >= (1LL << 31)) FAIL(c, KMC_ERR_ARG, "kmc_load_film: bad offsets");
@@ -368,6 +369,7 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   if (t->kind == KMC_TABLE_2D_SPECIES && (t->n[2] < 1 || t->n[2] > KMC_MAX_SPECIES))
     FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: species table needs 1 <= n[2] <= %d", KMC_MAX_SPECIES);
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_set_rate_table");
   int dims = t->kind == KMC_TABLE_4D ? 4 : 2;
   int64_t nr = t->kind == KMC_TABLE_2D_SPECIES ? (int64_t)t->n[2] * t->n[2] : 1;
   c->table = kmc::TableDev{};
@@ -443,6 +445,8 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
     FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: the species table has %d chiralities, the sites %d", c->table.n[2],
          c->n_species);
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_build_neighbors");
+  kmc::NvtxRange phase("build: cell grids");
   const int64_t n = c->n_sites;
   // cell grids, monte_carlo.h:375-387: n_d = ceil((max - min) / r) + 1
   int64_t ncell = 0;
@@ -516,11 +520,13 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   a.right = c->d_right.p;
   a.err = c->d_err.p;
   a.stats = c->d_stats.p;
+  phase.next("build: cells and site order");
   CK(c, cudaEventRecord(c->ev0, c->stream));
   CK(c, kmc::launch_cell_ids(a, c->stream));
   CK(c, kmc::exclusive_scan_i64(c->d_cell_start.p, ncell + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
   CK(c, kmc::launch_cell_fill(a, c->stream));
   CK(c, kmc::build_site_order(a, d_ord0.p, n_tb, d_tsizes.p, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
+  phase.next("build: row lengths");
   CK(c, kmc::launch_nbr_count(a, c->stream));
   CK(c, kmc::exclusive_scan_i64(c->d_rowptr.p, n + 1, c->d_scan.p, (int64_t)c->d_scan.n, c->stream));
   CK(c, c->d_blkptr.alloc(n + 1));
@@ -566,6 +572,7 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   a.total = c->d_total.p;
   a.inv_total = c->d_inv_total.p;
   a.rec = c->d_rec.p;
+  phase.next("build: rows");
   CK(c, kmc::launch_nbr_fill(a, c->stream));
   CK(c, cudaEventRecord(c->ev1, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
@@ -614,6 +621,7 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
   if (!inj || !inj->n_excitons || !inj->seeds) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: missing arrays");
   if (inj->mode != KMC_INJECT_REGION && inj->mode != KMC_INJECT_UNIFORM) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: bad mode");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_init_excitons");
   const int nsec = inj->n_sections;
   if (inj->mode == KMC_INJECT_REGION && !(nsec > 1 && nsec % 2 == 1 && nsec < 1000))
     FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: number of sections must be odd and > 1");
@@ -740,6 +748,8 @@ static kmc::HopArgs hop_args(kmc_ctx* c, double dt, double v) {
   a.cump = c->d_cump.p;
   a.lt64 = c->d_lt64.p;
   a.ulink = c->d_ulink.p;
+  a.n_sites = c->n_sites;
+  a.n_blocks = c->nblk;
   a.films = c->d_films.p;
   a.warp_film = c->d_warp_film.p;
   a.inject = c->d_inject.p;
@@ -883,6 +893,8 @@ static int capture_graph(kmc_ctx* c, cudaGraphExec_t* exec, const std::function<
 static int check_device_error(kmc_ctx* c, const char* who) {
   int32_t herr = 0;
   CK(c, cudaMemcpy(&herr, c->d_err.p, sizeof herr, cudaMemcpyDeviceToHost));
+  if (herr & KMC_ERR_CHECK_CODE)
+    FAIL(c, KMC_ERR_CHECK, "%s: a device bounds check failed (site, row block, MSD bin or Philox counter)", who);
   if (herr & KMC_ERR_HOP_CAP_CODE)
     FAIL(c, KMC_ERR_HOP_CAP, "%s: an exciton exceeded %lld hops in one step", who, (long long)c->hop_cap);
   if (herr & KMC_ERR_CAPACITY_CODE)
@@ -898,6 +910,7 @@ constexpr int64_t kMaxGraphLaunches = 256;
 // graph; the graph of the previous run is updated in place when its topology matches.
 static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0, int32_t precision, int variant,
                      int spl, float* ms, int* launches) {
+  kmc::NvtxRange phase("run: plan");
   HopPlan plan;
   int rc = prepare_hops(c, a.v, precision, variant, std::min<int64_t>(spl, n_steps), &plan);
   if (rc) return rc;
@@ -911,15 +924,19 @@ static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0,
   // their graph would only add instantiation time
   const bool graph = c->use_graph && (n_steps + spl - 1) / spl <= kMaxGraphLaunches;
   if (graph) {
+    phase.next("run: graph capture");
     rc = capture_graph(c, &c->gexec, enqueue);
     if (rc) return rc;
+    phase.next("run: launch");
     CK(c, cudaEventRecord(c->ev0, c->stream));
     CK(c, cudaGraphLaunch(c->gexec, c->stream));
   } else {
+    phase.next("run: launch");
     CK(c, cudaEventRecord(c->ev0, c->stream));
     CK(c, enqueue());
   }
   CK(c, cudaEventRecord(c->ev1, c->stream));
+  phase.next("run: hop kernels (wait)");
   CK(c, cudaStreamSynchronize(c->stream));
   CK(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
   *launches = nl;
@@ -934,6 +951,7 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_run: bad precision");
   CK(c, cudaSetDevice(c->device));
   if (n_steps == 0) return KMC_OK;
+  kmc::NvtxRange nv("kmc_run");
   dt = dt + 0.0;  // a zero time step is +0 (the kernels compare non-negative doubles bitwise)
   int rc = ensure_msd(c, c->steps_done + n_steps);
   if (rc) return rc;
@@ -966,6 +984,7 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
     if (cfg->contact_pop[k] < 0 || cfg->contact_pop[k] > INT32_MAX)
       FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: contact population out of range");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_contacts_init");
   const int64_t n = c->n_sites;
   const auto& dom = c->domains[0];
   const double ymin = dom[1], ymax = dom[4];
@@ -1157,6 +1176,7 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
   if (n_steps < 0 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_contacts_run: bad step count, time step or velocity");
   if (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED) FAIL(c, KMC_ERR_ARG, "kmc_contacts_run: bad precision");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_contacts_run");
   if (n_steps == 0) return KMC_OK;
   dt = dt + 0.0;
   int rc = ensure_msd(c, 1);  // the hop kernels' MSD sums land in one scratch row
@@ -1177,6 +1197,7 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
   kmc::ContactArgs ca = c->cargs;
   ca.pop = c->d_c_pop.p;
   ca.diff = c->d_c_diff.p;
+  ca.steps_cap = (int64_t)c->d_c_live.n;
   ca.n_live = c->d_c_live.p;
   kmc::HopArgs a = hop_args(c, dt, v);
   HopPlan plan;
@@ -1273,6 +1294,7 @@ int kmc_contacts_track(kmc_ctx* c, int64_t first, int32_t n_tracks, double dt, d
     FAIL(c, KMC_ERR_ARG, "kmc_contacts_track: n_tracks x max_steps too large");
   if (n_tracks == 0) return KMC_OK;
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_contacts_track");
   dt = dt + 0.0;
   const size_t np = (size_t)n_tracks * (size_t)max_steps * 3;
   DevBuf<double> d_path;
@@ -1325,6 +1347,7 @@ int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_autotune: create the excitons first");
   if (trial_steps < 1 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_autotune: bad arguments");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_autotune");
   dt = dt + 0.0;
   const int64_t ns = c->n_slots;
   // save the exciton state and counters; trials run into a scratch MSD buffer
@@ -1442,6 +1465,7 @@ int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) {
   if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
   if (count == 0) return KMC_OK;
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_get_msd_batches");
   const size_t row = (size_t)c->msd_batches * 3;
   CK(c, cudaMemcpy2DAsync(out, count * row * sizeof(double), c->d_msd.p + first * row, c->msd_cap * row * sizeof(double),
                           count * row * sizeof(double), c->n_films, cudaMemcpyDeviceToHost, c->stream));
@@ -1453,6 +1477,7 @@ int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) {
   if (!c) return KMC_ERR_ARG;
   if (c->msd_batches == 1) return kmc_get_msd_batches(c, first, count, out);
   if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
+  kmc::NvtxRange nv("kmc_get_msd: batch reduce");
   const int64_t B = c->msd_batches;
   std::vector<double> tmp((size_t)c->n_films * count * B * 3);
   int rc = kmc_get_msd_batches(c, first, count, tmp.data());
@@ -1482,6 +1507,7 @@ int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, doub
   if (!c) return KMC_ERR_ARG;
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_get_excitons: no excitons");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_get_excitons");
   const int64_t ns = c->n_slots;
   std::vector<int32_t> hs(ns);
   std::vector<uint32_t> hf(ns);
@@ -1511,6 +1537,67 @@ int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, doub
       if (hops) hops[o] = (int64_t)hh[s];
     }
   }
+  return KMC_OK;
+}
+
+// The inverse of kmc_get_excitons on the set kmc_init_excitons laid out (same films, counts,
+// seeds and injection mode): every field is checked on the host first, then written to the
+// slots.  The Philox stream of exciton i of a film is (film seed, i) at counter draws[i], so a
+// run resumed from a saved state draws the numbers the uninterrupted run would have drawn.
+// kExAtSite (the mixed kernel's "position is the site's" shortcut) is set where the position
+// equals the site's bit for bit; the shortcut and the general path give the same doubles there.
+int kmc_set_excitons(kmc_ctx* c, const int32_t* site, const double* pos, const double* delta, const double* ff,
+                     const int32_t* heading, const uint64_t* draws, const int64_t* hops) {
+  if (!c) return KMC_ERR_ARG;
+  if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_set_excitons: lay the excitons out with kmc_init_excitons first");
+  if (c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_set_excitons: contacts mode keeps its own particle state");
+  if (!site || !pos || !delta || !ff || !heading || !draws || !hops) FAIL(c, KMC_ERR_ARG, "kmc_set_excitons: missing arrays");
+  CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_set_excitons");
+  const int64_t ns = c->n_slots, n = c->n_sites;
+  std::vector<int32_t> rank(n);
+  for (int64_t k = 0; k < n; ++k) rank[c->h_perm[k]] = (int32_t)k;
+  std::vector<int32_t> hs(ns, -1);
+  std::vector<uint32_t> hf(ns, 0);
+  std::vector<double> hp(3 * ns, 0.0), hd(3 * ns, 0.0), hff(ns, 0.0);
+  std::vector<uint64_t> hdr(ns, 0), hh(ns, 0);
+  int64_t o = 0;
+  for (int32_t f = 0; f < c->n_films; ++f) {
+    const FilmDev& fd = c->films[f];
+    for (int64_t i = 0; i < fd.n_exc; ++i, ++o) {
+      const int64_t s = fd.slot0 + i;
+      if (site[o] < 0 || site[o] >= fd.n_sites) FAIL(c, KMC_ERR_ARG, "kmc_set_excitons: exciton %lld: site out of range", (long long)o);
+      if (heading[o] != 0 && heading[o] != 1) FAIL(c, KMC_ERR_ARG, "kmc_set_excitons: exciton %lld: heading is 0 or 1", (long long)o);
+      if (hops[o] < 0) FAIL(c, KMC_ERR_ARG, "kmc_set_excitons: exciton %lld: negative hop count", (long long)o);
+      bool finite = std::isfinite(ff[o]) && ff[o] >= 0;
+      for (int k = 0; k < 3; ++k) finite = finite && std::isfinite(pos[3 * o + k]) && std::isfinite(delta[3 * o + k]);
+      if (!finite) FAIL(c, KMC_ERR_ARG, "kmc_set_excitons: exciton %lld: non-finite state", (long long)o);
+      const int64_t gid = fd.site0 + site[o];
+      const double* q = &c->pos[3 * gid];
+      bool at = true;
+      for (int k = 0; k < 3; ++k) {
+        hp[k * ns + s] = pos[3 * o + k];
+        hd[k * ns + s] = delta[3 * o + k];
+        at = at && std::memcmp(&q[k], &pos[3 * o + k], sizeof(double)) == 0;
+      }
+      hs[s] = rank[gid];
+      hf[s] = kmc::kExActive | (heading[o] ? kmc::kExHeading : 0u) | (at ? kmc::kExAtSite : 0u);
+      hff[s] = ff[o];
+      hdr[s] = draws[o];
+      hh[s] = (uint64_t)hops[o];
+    }
+  }
+  CK(c, cudaMemcpyAsync(c->d_e_site.p, hs.data(), ns * 4, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_e_flags.p, hf.data(), ns * 4, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_e_pos.p, hp.data(), 3 * ns * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_e_delta.p, hd.data(), 3 * ns * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_e_ff.p, hff.data(), ns * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_e_draws.p, hdr.data(), ns * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_e_hops.p, hh.data(), ns * 8, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemsetAsync(c->d_counters.p, 0, 4 * sizeof(unsigned long long), c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->steps_done = 0;  // the resumed run's MSD bins and statistics start at its first step
+  c->stats = kmc_run_stats{};
   return KMC_OK;
 }
 
@@ -1782,6 +1869,7 @@ int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats*
     FAIL(c, KMC_ERR_ARG, "kmc_mlp_train: need epochs >= 1, batch a multiple of 128 within the samples, lr > 0, "
                          "lr_final >= 0, betas in [0, 1), eps > 0");
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_mlp_train");
   const kmc::MlpDev m = mlp_dev(c);
   const int64_t per_epoch = c->mlp_n_samples / cfg->batch;
   const int64_t total = per_epoch * cfg->epochs;
@@ -1849,6 +1937,7 @@ int kmc_mlp_rate_table(kmc_ctx* c, int32_t nd, const double* dist, int32_t nt, c
   for (int32_t i = 0; i < nt; ++i)
     if (!std::isfinite(theta[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: angle %d is not finite", i);
   CK(c, cudaSetDevice(c->device));
+  kmc::NvtxRange nv("kmc_mlp_rate_table");
   const int64_t S = c->mlp_shape.n_species;
   const int64_t n = S * S * nd * nt;
   DevBuf<double> dd, dt, out;

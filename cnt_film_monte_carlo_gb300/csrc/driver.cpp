@@ -6,6 +6,8 @@
 // then runs the same loop as main.cpp:64-76: kubo_init, save_json_properties,
 // kubo_create_particles, and while time < max time: kubo_step(dt), kubo_save_avg_dispalcement_squared.
 // With "mode": "contacts" it runs the reference's contacts loop instead (main.cpp:85-106).
+// Either way it ends by writing run_report.json (what ran, hop counters, hops/s, and in
+// Green-Kubo mode D with its 95 % interval) beside the reference's output files.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -48,8 +50,9 @@ int main(int argc, char** argv) {
         sim.contacts_steps_and_save(std::min<int64_t>(kChunk, left), time_step);
       kmc_run_stats rs = sim.run_stats();
       double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-      std::printf("contacts simulation finished: %lld steps, %lld hops, %u particles, wall %.3f s\n",
-                  (long long)rs.steps_done, (long long)rs.hops, sim.number_of_particles(), wall);
+      sim.write_run_report(wall);
+      std::printf("contacts simulation finished: %lld steps, %lld hops, %u particles, device %.3f s, wall %.3f s\n",
+                  (long long)rs.steps_done, (long long)rs.hops, sim.number_of_particles(), sim.device_seconds(), wall);
       std::printf("output: %s\n", sim.output_path().c_str());
       return 0;
     }
@@ -60,16 +63,14 @@ int main(int argc, char** argv) {
     const kmc_nbr_stats& nb = sim.neighbor_stats();
     std::printf("sites: %lld  neighbour entries: %lld (mean %.2f, max %d)  build: %.3f ms\n", (long long)nb.n_sites,
                 (long long)nb.nnz, nb.k_mean, nb.k_max, nb.build_ms);
-    double dev_ms = 0;
     // main.cpp:70-76's loop, its steps in chunks of one engine call each (same rows)
-    for (int64_t left = sim.steps_until(sim.kubo_max_time(), time_step); left > 0; left -= kChunk) {
+    for (int64_t left = sim.steps_until(sim.kubo_max_time(), time_step); left > 0; left -= kChunk)
       sim.kubo_steps_and_save(std::min<int64_t>(kChunk, left), time_step);
-      dev_ms += sim.run_stats().last_run_ms;
-    }
     kmc_run_stats rs = sim.run_stats();
     double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    sim.write_run_report(wall);
     std::printf("Green-Kubo simulation finished: %lld steps, %lld hops, %lld crossings, device %.3f s, wall %.3f s\n",
-                (long long)rs.steps_done, (long long)rs.hops, (long long)rs.crossings, dev_ms / 1e3, wall);
+                (long long)rs.steps_done, (long long)rs.hops, (long long)rs.crossings, sim.device_seconds(), wall);
     std::printf("output: %s\n", sim.output_path().c_str());
     return 0;
   } catch (const std::exception& e) {

@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(kCBlock) k_contacts_metrics(ContactArgs a) {
     if (blockIdx.x == 0) a.blk_a[gridDim.x] = 0;
   }
   __syncthreads();
+  if (!KMC_DCHECK(a.err, step < a.steps_cap)) return;  // after the block's last barrier
   for (int i = threadIdx.x; i < a.n_seg; i += kCBlock) {
     if (spop[i]) atomicAdd(&a.pop[step * a.n_seg + i], (unsigned long long)spop[i]);
     if (sdiff[i]) atomicAdd(&a.diff[step * a.n_seg + i], (unsigned long long)(long long)sdiff[i]);
@@ -191,7 +192,8 @@ __global__ void __launch_bounds__(kCBlock) k_contacts_place(ContactArgs a, int c
   } else {
     if (live) a.y_old[s] = a.e_pos[ns + s];
     block_rank(live, &total);
-    if (threadIdx.x == 0 && total) atomicAdd(&a.n_live[*a.step], (unsigned long long)total);
+    if (threadIdx.x == 0 && total && KMC_DCHECK(a.err, *a.step < a.steps_cap))
+      atomicAdd(&a.n_live[*a.step], (unsigned long long)total);
   }
 }
 

@@ -830,6 +830,7 @@ cudaError_t h2d(DBuf<T>& b, const T* h, size_t n, cudaStream_t s) {
 
 // vq, PI, eps, Bethe-Salpeter kernels and their eigenpairs on the device
 int screening_and_excitons(kmc_cnt& t, cudaStream_t st, std::string& err) {
+  kmc::NvtxRange phase("cnt: vq");
   const Consts& k = K();
   // vq (cnt.cpp:526-600)
   int ncell = t.cells;
@@ -874,6 +875,7 @@ int screening_and_excitons(kmc_cnt& t, cudaStream_t st, std::string& err) {
                                   1.0 / double(2 * Nu * ncell), d_vq.p);
   XCK(cudaGetLastError());
   // PI (cnt.cpp:634-720)
+  phase.next("cnt: polarisation");
   XCK(h2d(d_en, t.energy.data(), t.energy.size(), st));
   XCK(h2d(d_wf, reinterpret_cast<const double2*>(t.wf.data()), t.wf.size(), st));
   XCK(d_pi.alloc(nb));
@@ -893,6 +895,7 @@ int screening_and_excitons(kmc_cnt& t, cudaStream_t st, std::string& err) {
   }
   XCK(h2d(d_eps, t.eps.data(), t.eps.size(), st));
   // Bethe-Salpeter kernels (cnt.cpp:818-947)
+  phase.next("cnt: Bethe-Salpeter kernels and eigen-solve");
   const int nr = (int)t.relev[0].size();
   if ((int)t.relev[1].size() != nr) {
     err = "valleys with different numbers of relevant states";
@@ -1236,6 +1239,7 @@ int kmc_cnt_create(kmc_ctx* ctx, int32_t n, int32_t m, int32_t length_cells, kmc
   if (n < 1 || m < 1 || m > n || length_cells < 1 || length_cells > 4096)
     return fail(ctx, KMC_ERR_ARG, "kmc_cnt_create: need chirality n >= m >= 1 and 1..4096 unit cells");
   if (cudaSetDevice(ctx_device(ctx)) != cudaSuccess) return fail(ctx, KMC_ERR_CUDA, "kmc_cnt_create: cudaSetDevice");
+  kmc::NvtxRange nv("kmc_cnt_create");
   kmc_cnt* t = new kmc_cnt();
   t->n = n;
   t->m = m;
@@ -1320,6 +1324,7 @@ int kmc_exciton_j(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, i
     return fail(ctx, KMC_ERR_ARG, "kmc_exciton_j: bad arguments");
   if (n_pairs == 0) return KMC_OK;
   if (cudaSetDevice(ctx_device(ctx)) != cudaSuccess) return fail(ctx, KMC_ERR_CUDA, "kmc_exciton_j: cudaSetDevice");
+  kmc::NvtxRange nv("kmc_exciton_j");
   std::vector<int> kd, ka;
   std::vector<int2> pq(n_pairs);
   auto slot = [](std::vector<int>& v, int x) {
@@ -1346,6 +1351,7 @@ int kmc_exciton_rates(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* accepto
   if (!ctx || !donor || !acceptor || !cfg_ok(cfg) || n_geometries < 0 || (n_geometries > 0 && (!geometries || !rate)))
     return fail(ctx, KMC_ERR_ARG, "kmc_exciton_rates: bad arguments");
   if (cudaSetDevice(ctx_device(ctx)) != cudaSuccess) return fail(ctx, KMC_ERR_CUDA, "kmc_exciton_rates: cudaSetDevice");
+  kmc::NvtxRange nv("kmc_exciton_rates");
   std::string err;
   int rc = rates(*donor, *acceptor, *cfg, n_geometries, geometries, rate, ctx_stream(ctx), err);
   return rc ? fail(ctx, rc, "kmc_exciton_rates: " + err) : KMC_OK;

@@ -43,6 +43,7 @@ __device__ __forceinline__ void fly_full(const HopArgs& a, Exciton& e, double dt
     }
     int32_t l = a.left[e.site], r = a.right[e.site];
     int32_t next = e.heading ? (r > -1 ? r : l) : (l > -1 ? l : r);
+    if (!KMC_DCHECK(a.err, next >= 0 && next < a.n_sites)) return;
     e.heading = (next == r);
     double4_32a t = a.pos4[next];
     double dist = norm3(e.px - t.x, e.py - t.y, e.pz - t.z);
@@ -82,6 +83,7 @@ __device__ __forceinline__ bool step_fp64(const HopArgs& a, Exciton& e, double d
     int64_t n = a.rec[e.site].len_flags & kLenMask;  // row length (rows are stored per slot)
     if (n > 0) {
       const int64_t bo = a.blkptr[e.site];
+      if (!KMC_DCHECK(a.err, bo >= 0 && bo + ((n + 7) >> 3) <= a.n_blocks)) return false;  // the exciton stops
       const double* cum = a.cump + bo * 8;
       uint32_t r = e.g.next();
       double dice = a.total[e.site] * (double)r / (double)kRandMax;
@@ -94,6 +96,7 @@ __device__ __forceinline__ bool step_fp64(const HopArgs& a, Exciton& e, double d
           right = mid;
       }
       ns = a.blocks[bo + (right >> 3)].col[right & 7];
+      if (!KMC_DCHECK(a.err, ns >= 0 && ns < a.n_sites)) return false;
     }
     e.hops++;
     trace_push(a, e, ns);
@@ -125,6 +128,7 @@ __device__ __forceinline__ void load_exciton(const HopArgs& a, int64_t slot, Exc
   e.heading = (fl & kExHeading) != 0;
   e.at_site = (fl & kExAtSite) != 0;
   e.site = a.e_site[slot];
+  if (e.active && !KMC_DCHECK(a.err, e.site >= 0 && e.site < a.n_sites)) e.active = false;  // slot left as it is
   e.px = a.e_pos[slot];
   e.py = a.e_pos[ns + slot];
   e.pz = a.e_pos[2 * ns + slot];
@@ -139,6 +143,7 @@ __device__ __forceinline__ void load_exciton(const HopArgs& a, int64_t slot, Exc
 __device__ __forceinline__ void store_exciton(const HopArgs& a, int64_t slot, const Exciton& e) {
   const int64_t ns = a.n_slots;
   if (!e.active) return;
+  (void)KMC_DCHECK(a.err, e.g.n >= a.e_draws[slot]);  // a Philox counter only moves forward (no wrap)
   a.e_flags[slot] = kExActive | (e.heading ? kExHeading : 0u) | (e.at_site ? kExAtSite : 0u);
   a.e_site[slot] = e.site;
   a.e_pos[slot] = e.px;
@@ -166,6 +171,7 @@ __device__ __forceinline__ void maybe_reinject(const HopArgs& a, const FilmDev& 
   if (!out) return;
   uint32_t dice = e.g.next() % (uint32_t)f.n_inj;
   int32_t site = a.inject[f.inj0 + dice];
+  if (!KMC_DCHECK(a.err, site >= 0 && site < a.n_sites)) return;
   double4_32a p = a.pos4[site];
   e.px = p.x;
   e.py = p.y;
@@ -190,7 +196,7 @@ __device__ __forceinline__ void step_epilogue(const HopArgs& a, const FilmDev& f
   sx = warp_sum(sx);
   sy = warp_sum(sy);
   sz = warp_sum(sz);
-  if ((threadIdx.x & 31) == 0) {
+  if ((threadIdx.x & 31) == 0 && KMC_DCHECK(a.err, a.step0 + s < a.msd_cap)) {
     const int64_t batch = ((int64_t)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x - f.slot0) >> 5) % a.msd_batches;
     double* m = a.msd + (((int64_t)film * a.msd_cap + a.step0 + s) * a.msd_batches + batch) * 3;
     atomicAdd(m, sx);

@@ -79,6 +79,7 @@ __device__ __forceinline__ void fly_end(const HopArgs& a, Exciton& e, bool at_si
     }
     const int32_t l = a.left[e.site], r = a.right[e.site];
     const int32_t next = e.heading ? (r > -1 ? r : l) : (l > -1 ? l : r);
+    if (!KMC_DCHECK(a.err, next >= 0 && next < a.n_sites)) return;
     const bool to_right = (next == r);
     e.heading = to_right;
     const double4_32a t = a.pos4[next];
@@ -182,6 +183,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
     lnk_r = q1.y;
     lth_l = (uint32_t)q1.z;
     lth_r = (uint32_t)q1.w;
+#ifdef KMC_CHECK
+    // the record's row must lie inside the block arrays and its links inside the sites; a bad
+    // row is treated as empty and a bad link as none
+    if (!KMC_DCHECK(a.err, fp->blk0 + (int64_t)blk + (int64_t)(((lenf & kLenMask) + 7) >> 3) <= a.n_blocks))
+      lenf &= ~kLenMask;
+    if (!KMC_DCHECK(a.err, lnk_l < a.n_sites)) lnk_l = -1;
+    if (!KMC_DCHECK(a.err, lnk_r < a.n_sites)) lnk_r = -1;
+#endif
   };
   for (;;) {
     // all 32 lanes meet here once per event, so every event starts with the warp converged
@@ -220,6 +229,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       heading = (fl & kExHeading) != 0;
       at_site = (fl & kExAtSite) != 0;
       site = a.e_site[cur];
+      if (!KMC_DCHECK(a.err, site >= 0 && site < a.n_sites)) {  // slot left as it is
+        cur = -1;
+        continue;
+      }
       ff = a.e_ff[cur];
       int64_t local = cur - fp->slot0;
       tracing = film == 0 && local < a.n_trace;
@@ -456,6 +469,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
           nsite = rb[right >> 3].col[right & 7];
         }
       }
+      if (!KMC_DCHECK(a.err, nsite >= 0 && nsite < a.n_sites)) nsite = site;
       ehops++;
       if (tracing) cold_trace(a, cur - a.films[film].slot0, nsite);
       if (nsite != site) {
@@ -537,7 +551,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
         atomicAdd(&s_bins[s * 3 + 0], dx * dx);
         atomicAdd(&s_bins[s * 3 + 1], dy * dy);
         atomicAdd(&s_bins[s * 3 + 2], dz * dz);
-      } else {
+      } else if (KMC_DCHECK(a.err, a.step0 + s < a.msd_cap)) {
         const int64_t batch = ((cur - f.slot0) >> 5) % a.msd_batches;
         double* m = a.msd + (((int64_t)film * a.msd_cap + a.step0 + s) * a.msd_batches + batch) * 3;
         atomicAdd(m, dx * dx);
@@ -568,7 +582,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_hop_mixed(HopArgs a, int64_t n_
       load_rec(site);
     }
   }
-  if (single_film) {
+  if (single_film && KMC_DCHECK(a.err, a.step0 + n_steps <= a.msd_cap)) {
     __syncthreads();
     double* m = a.msd + a.step0 * 3;
     for (int64_t i = threadIdx.x; i < n_steps * 3; i += blockDim.x) atomicAdd(m + i, s_bins[i]);

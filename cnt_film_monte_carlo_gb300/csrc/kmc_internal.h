@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <cstdint>
 
 #include "kmc_device.cuh"
@@ -11,10 +13,35 @@
 #define KMC_ERR_CELL_CODE 2      // a site fell outside the cell grid
 #define KMC_ERR_FLIGHT_CODE 4    // a free flight crossed more than kMaxCrossings links
 #define KMC_ERR_CAPACITY_CODE 8  // contacts mode: fewer empty slots than new excitons
+#define KMC_ERR_CHECK_CODE 16    // KMC_CHECK builds: an index or counter failed its bounds check
+
+// Device bounds checks of the KMC_CHECK build (libcntkmc_check.so): KMC_DCHECK(err, cond) is
+// false, and sets KMC_ERR_CHECK_CODE in the error word, when cond fails; the caller then skips
+// or replaces the access it guards, so that the kernel stays in bounds and the host reports the
+// failure after the launch.  In the normal build it is the constant true and compiles away.
+#ifdef KMC_CHECK
+#define KMC_DCHECK(err, cond) ((cond) ? true : (atomicOr((err), KMC_ERR_CHECK_CODE), false))
+#else
+#define KMC_DCHECK(err, cond) true
+#endif
 
 struct kmc_ctx;  // the engine context (include/cntkmc.h; defined in cntkmc_api.cu)
 
 namespace kmc {
+
+// NVTX range over the host span of an entry point or one of its phases (build, launch, reduce),
+// for Nsight Systems timelines; without a tool attached a push/pop is a branch on a null hook.
+// next() closes the current phase and opens the following one; early returns close it.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  void next(const char* name) {
+    nvtxRangePop();
+    nvtxRangePushA(name);
+  }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Per-film constants (device copy).
 struct FilmDev {
@@ -90,6 +117,7 @@ struct HopArgs {
   const double* cump;     // FP64 cumulative rates in the blocked layout (8 per block)
   const double2* lt64;    // exact link times (left, right)
   const double* ulink;    // [site][6]: unit vectors toward the left and the right neighbour
+  int64_t n_sites, n_blocks;  // extents of the site and row-block arrays (KMC_CHECK bounds)
   // films and excitons
   const FilmDev* films;
   const int32_t* warp_film;
@@ -229,6 +257,7 @@ struct ContactArgs {
   unsigned long long* pop;  // [steps][n_seg] excitons per segment
   unsigned long long* diff; // [steps][n_seg] interface crossings as a difference array
   unsigned long long* n_live;  // [steps] excitons after repopulation
+  int64_t steps_cap;        // rows of pop, diff and n_live (KMC_CHECK bounds)
   int32_t* err;
 };
 int64_t contacts_blocks(int64_t n_slots);

@@ -268,6 +268,7 @@ extern "C" int kmc_build_neighbors_noalloc(const double* pos, const double* orie
   if (!table->rate) return fail(err, err_len, KMC_ERR_ARG, "kmc_build_neighbors_noalloc: missing rates");
   td.rate = table->rate;
   cudaStream_t st = (cudaStream_t)stream;
+  kmc::NvtxRange nv("kmc_build_neighbors_noalloc");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(err, err_len, KMC_ERR_NO_DEVICE, "kmc_build_neighbors_noalloc: no current CUDA device");

@@ -140,6 +140,8 @@ class monte_carlo {
     if (!cinfo_.capacity) throw std::logic_error("step: call init() first");
     int64_t live = 0;
     check(kmc_contacts_run(ctx_, 1, dt, velocity_, precision(), pop_.data(), cur_.data(), &live), "kmc_contacts_run");
+    device_ms_ += run_stats().last_run_ms;
+    dt_ = dt;
     live_ = live;
     time_ += dt;
     ++steps_;
@@ -204,22 +206,30 @@ class monte_carlo {
     f << "\n";
   }
 
-  // monte_carlo.cpp:308-316
+  // monte_carlo.cpp:308-316.  The MSD sums are also kept per exciton batch (exciton i in batch
+  // (i / 32) mod B, B = min(32, n / 32)), for the diffusion coefficient's interval in the run
+  // report; the file's rows are the batch sums added in batch order.
   void kubo_create_particles() {
     n_particles_ = j_["number of particles for kubo simulation"].as_int();
     uint64_t seed = this->seed();
     bool uniform = j_.has("injection") && j_["injection"].as_string() == "uniform";
     int64_t ne = n_particles_;
+    batches_ = (int32_t)std::max<int64_t>(1, std::min<int64_t>(32, ne / 32));
+    batch_counts_.assign((size_t)batches_, 0);
+    for (int64_t w = 0; w * 32 < ne; ++w) batch_counts_[(size_t)(w % batches_)] += std::min<int64_t>(32, ne - w * 32);
+    check(kmc_set_msd_batches(ctx_, batches_), "kmc_set_msd_batches");
     kmc_inject inj{uniform ? KMC_INJECT_UNIFORM : KMC_INJECT_REGION, n_sections_, &ne, &seed};
     check(kmc_init_excitons(ctx_, &inj), "kmc_init_excitons");
     steps_ = 0;
+    times_.clear();
   }
 
   // monte_carlo.cpp:319-342
   void kubo_step(double dt) {
-    check(kmc_run(ctx_, 1, dt, velocity_, precision()), "kmc_run");
+    run(1, dt);
     ++steps_;
     time_ += dt;
+    times_.push_back(time_);
   }
 
   // monte_carlo.cpp:382-409
@@ -236,7 +246,7 @@ class monte_carlo {
   // engine call (the rows and times are those of the n separate calls)
   void kubo_steps_and_save(int64_t n, double dt) {
     if (n <= 0) return;
-    check(kmc_run(ctx_, n, dt, velocity_, precision()), "kmc_run");
+    run(n, dt);
     std::vector<double> s((size_t)(3 * n));
     check(kmc_get_msd(ctx_, steps_, n, s.data()), "kmc_get_msd");
     open_msd_file();
@@ -244,6 +254,7 @@ class monte_carlo {
     for (int64_t k = 0; k < n; ++k) {
       time_ += dt;
       ++steps_;
+      times_.push_back(time_);
       std::fprintf(msd_, "%+e,%+e,%+e,%+e\n", time_, s[3 * k] / np, s[3 * k + 1] / np, s[3 * k + 2] / np);
     }
     std::fflush(msd_);
@@ -256,6 +267,8 @@ class monte_carlo {
     std::vector<int64_t> pop((size_t)(n * n_seg_)), cur((size_t)(n * (n_seg_ - 1))), live((size_t)n);
     check(kmc_contacts_run(ctx_, n, dt, velocity_, precision(), pop.data(), cur.data(), live.data()),
           "kmc_contacts_run");
+    device_ms_ += run_stats().last_run_ms;
+    dt_ = dt;
     for (int64_t k = 0; k < n; ++k) {
       std::copy(pop.begin() + k * n_seg_, pop.begin() + (k + 1) * n_seg_, pop_.begin());
       std::copy(cur.begin() + k * (n_seg_ - 1), cur.begin() + (k + 1) * (n_seg_ - 1), cur_.begin());
@@ -276,6 +289,77 @@ class monte_carlo {
   }
 
   const kmc_nbr_stats& neighbor_stats() const { return nbr_; }
+  double device_seconds() const { return device_ms_ / 1e3; }
+
+  // run_report.json in the output directory (no counterpart in the reference, which prints only
+  // wall-clock start and end, main.cpp:26-27,109-111): what ran (mode, precision, seed,
+  // injection, particles, steps, time step), the film's neighbour lists, the hop counters, device
+  // and wall seconds with hops/s, and in Green-Kubo mode the diffusion coefficient per axis with
+  // its 95 % interval from the exciton batches (kmc_fit_diffusion over the last 80 % of the steps).
+  void write_run_report(double wall_seconds) const {
+    const kmc_run_stats rs = run_stats();
+    const bool kubo = !cinfo_.capacity;
+    std::FILE* f = std::fopen((fs::path(out_dir_) / "run_report.json").c_str(), "w");
+    if (!f) throw std::runtime_error("cannot open run_report.json");
+    auto num = [&](double v) {
+      if (std::isfinite(v))
+        std::fprintf(f, "%.17g", v);
+      else
+        std::fprintf(f, "null");
+    };
+    std::fprintf(f, "{\n  \"engine\": \"%s\",\n  \"mode\": \"%s\",\n", kmc_version(), kubo ? "kubo" : "contacts");
+    std::fprintf(f, "  \"precision\": \"%s\",\n  \"philox seed\": %llu,\n", precision() == KMC_PREC_FP64 ? "fp64" : "mixed",
+                 (unsigned long long)seed());
+    if (kubo)
+      std::fprintf(f, "  \"injection\": \"%s\",\n",
+                   j_.has("injection") && j_["injection"].as_string() == "uniform" ? "uniform" : "region");
+    std::fprintf(f, "  \"particles\": %lld,\n  \"steps\": %lld,\n  \"time step [s]\": ", (long long)n_particles_,
+                 (long long)steps_);
+    num(dt_);
+    std::fprintf(f, ",\n  \"simulated time [s]\": ");
+    num(time_);
+    std::fprintf(f, ",\n  \"sites\": %lld,\n  \"neighbour entries\": %lld,\n  \"mean neighbours per site\": ",
+                 (long long)nbr_.n_sites, (long long)nbr_.nnz);
+    num(nbr_.k_mean);
+    std::fprintf(f, ",\n  \"max neighbours per site\": %d,\n  \"neighbour build [s]\": ", nbr_.k_max);
+    num(nbr_.build_ms / 1e3);
+    std::fprintf(f, ",\n  \"hops\": %lld,\n  \"crossings\": %lld,\n  \"exact re-resolves\": %lld,\n", (long long)rs.hops,
+                 (long long)rs.crossings, (long long)rs.exact_resolves);
+    const double dev_s = device_ms_ / 1e3;
+    std::fprintf(f, "  \"device seconds\": ");
+    num(dev_s);
+    std::fprintf(f, ",\n  \"hops per second (device)\": ");
+    num(dev_s > 0 ? (double)rs.hops / dev_s : NAN);
+    std::fprintf(f, ",\n  \"wall seconds\": ");
+    num(wall_seconds);
+    std::fprintf(f, ",\n  \"hops per second (wall)\": ");
+    num(wall_seconds > 0 ? (double)rs.hops / wall_seconds : NAN);
+    if (kubo) {
+      double D[3] = {NAN, NAN, NAN}, ci[3] = {NAN, NAN, NAN};
+      if (steps_ >= 2 && (int64_t)times_.size() == steps_) {
+        std::vector<double> m((size_t)steps_ * (size_t)batches_ * 3);
+        check(kmc_get_msd_batches(ctx_, 0, steps_, m.data()), "kmc_get_msd_batches");
+        check(kmc_fit_diffusion(m.data(), batch_counts_.data(), times_.data(), steps_, batches_, 0.8, D, ci),
+              "kmc_fit_diffusion");
+      }
+      std::fprintf(f, ",\n  \"msd batches\": %d,\n  \"fit fraction\": 0.8,\n  \"diffusion coefficient [m^2/s]\": [",
+                   batches_);
+      for (int k = 0; k < 3; ++k) {
+        if (k) std::fprintf(f, ", ");
+        num(D[k]);
+      }
+      std::fprintf(f, "],\n  \"diffusion 95%% interval [m^2/s]\": [");
+      for (int k = 0; k < 3; ++k) {
+        if (k) std::fprintf(f, ", ");
+        num(ci[k]);
+      }
+      std::fprintf(f, "]");
+    } else {
+      std::fprintf(f, ",\n  \"live excitons\": %lld", (long long)live_);
+    }
+    std::fprintf(f, "\n}\n");
+    std::fclose(f);
+  }
   kmc_run_stats run_stats() const {
     kmc_run_stats s{};
     kmc_get_run_stats(ctx_, &s);
@@ -312,6 +396,11 @@ class monte_carlo {
     }
   }
   uint64_t seed() const { return j_.has("philox seed") ? (uint64_t)j_["philox seed"].as_int() : 100u; }
+  void run(int64_t n, double dt) {
+    check(kmc_run(ctx_, n, dt, velocity_, precision()), "kmc_run");
+    device_ms_ += run_stats().last_run_ms;
+    dt_ = dt;
+  }
   int precision() const {
     return (j_.has("precision") && j_["precision"].as_string() == "fp64") ? KMC_PREC_FP64 : KMC_PREC_MIXED;
   }
@@ -448,6 +537,10 @@ class monte_carlo {
   double time_ = 0, max_time_ = 0, r_max_ = 0, velocity_ = 0;
   int n_sections_ = 5;
   int64_t n_particles_ = 0, steps_ = 0;
+  double dt_ = 0, device_ms_ = 0;
+  int32_t batches_ = 1;
+  std::vector<int64_t> batch_counts_;
+  std::vector<double> times_;  // end time of every Green-Kubo step, accumulated as time_
   int table_kind_ = KMC_TABLE_4D;
   std::vector<std::vector<double>> grids_;
   std::vector<double> rates_, pos_, orient_;

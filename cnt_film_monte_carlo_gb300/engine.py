@@ -17,8 +17,9 @@ class Engine:
     """Owns a kmc_ctx on one CUDA device.  Every method maps to one C-ABI call and raises
     ``KmcError`` with the library's message when the call fails."""
 
-    def __init__(self, device: int = 0):
-        self.lib = L.load()
+    def __init__(self, device: int = 0, checked: bool = False):
+        # checked: the KMC_CHECK build, whose kernels bounds-check their indices and counters
+        self.lib = L.load(checked)
         st = C.c_int(0)
         self.h = self.lib.kmc_create(device, C.byref(st))
         if not self.h:
@@ -212,6 +213,23 @@ class Engine:
                                               L.ptr(out["heading"], C.c_int32), L.ptr(out["draws"], C.c_uint64),
                                               L.ptr(out["hops"], C.c_int64)))
         return out
+
+    def set_excitons(self, state: dict) -> None:
+        """Restore a state excitons() returned (checkpoint/resume) into the set init_excitons laid
+        out with the same films, counts, seeds and injection mode; MSD bins and stats restart."""
+        n = int(self.lib.kmc_num_excitons(self.h))
+        conv = {"site": np.int32, "pos": np.float64, "delta": np.float64, "ff": np.float64, "heading": np.int32,
+                "draws": np.uint64, "hops": np.int64}
+        a = {}
+        for k, t in conv.items():
+            v = np.ascontiguousarray(state[k], dtype=t)
+            if v.shape != ((n, 3) if k in ("pos", "delta") else (n,)):
+                raise ValueError(f"set_excitons: {k} has shape {v.shape} for {n} excitons")
+            a[k] = v
+        self._check(self.lib.kmc_set_excitons(self.h, L.ptr(a["site"], C.c_int32), L.ptr(a["pos"], C.c_double),
+                                              L.ptr(a["delta"], C.c_double), L.ptr(a["ff"], C.c_double),
+                                              L.ptr(a["heading"], C.c_int32), L.ptr(a["draws"], C.c_uint64),
+                                              L.ptr(a["hops"], C.c_int64)))
 
     def neighbors(self, n_sites: int, nnz: int) -> dict:
         rowptr = np.zeros(n_sites + 1, np.int64)

@@ -21,13 +21,15 @@ Extensions: "philox seed" (default 100, the reference's srand(100) of main.cpp:3
 from __future__ import annotations
 
 import json
+import math
 import os
 import shutil
+import time
 
 import numpy as np
 
 from . import _lib as L
-from . import contacts, tables
+from . import contacts, diffusion, tables
 from .engine import Engine, read_mesh, trim_sites
 
 
@@ -79,6 +81,12 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         self._max_time = 0.0
         self._msd_file = None
         self._n_particles = 0
+        self._device_ms = 0.0
+        self._dt = 0.0
+        self._step = 0
+        self._times = []
+        self._batches = 1
+        self._contacts = None
 
     # -- monte_carlo.h:139
     def time(self) -> float:
@@ -180,8 +188,10 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
     def step(self, dt: float):
         """step (monte_carlo.h:343-354).  The engine runs the step, the counts behind
         save_metrics and repopulate_contacts as one unit, in the order of src/main.cpp:99-102."""
-        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
-        pop, cur, live = self._engine.contacts_run(1, dt, self._particle_velocity, prec)
+        pop, cur, live = self._engine.contacts_run(1, dt, self._particle_velocity, self._precision())
+        self._device_ms += self._engine.stats()["last_run_ms"]
+        self._dt = dt
+        self._step += 1
         self._last = (pop[0], cur[0], int(live[0]))
         self._time += dt
 
@@ -211,20 +221,33 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
             json.dump(self._json_prop, f, indent=4)
 
     def kubo_create_particles(self):
-        """monte_carlo.cpp:308-316 (exciton i draws from Philox stream i of "philox seed")."""
+        """monte_carlo.cpp:308-316 (exciton i draws from Philox stream i of "philox seed").  The
+        MSD sums are also kept per exciton batch (exciton i in batch (i // 32) % B, B = min(32,
+        n // 32)) for the interval of D in the run report."""
         j = self._json_prop
         n = int(j["number of particles for kubo simulation"])
         mode = L.KMC_INJECT_UNIFORM if j.get("injection", "region") == "uniform" else L.KMC_INJECT_REGION
+        self._batches = max(1, min(32, n // 32))
+        self._engine.set_msd_batches(self._batches)
         self._engine.init_excitons(n, int(j.get("philox seed", 100)), mode, self._n_sections)
         self._n_particles = n
         self._step = 0
+        self._times = []
+
+    def _precision(self) -> int:
+        return L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
+
+    def _run(self, n: int, dt: float):
+        self._engine.run(n, dt, self._particle_velocity, self._precision())
+        self._device_ms += self._engine.stats()["last_run_ms"]
+        self._dt = dt
 
     def kubo_step(self, dt: float):
         """monte_carlo.cpp:319-342."""
-        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
-        self._engine.run(1, dt, self._particle_velocity, prec)
+        self._run(1, dt)
         self._step += 1
         self._time += dt
+        self._times.append(self._time)
 
     def _open_msd_file(self):
         if self._msd_file is None:
@@ -246,13 +269,13 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         engine call (the rows and times are those of the n separate calls)."""
         if n <= 0:
             return
-        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
-        self._engine.run(n, dt, self._particle_velocity, prec)
+        self._run(n, dt)
         sums = self._engine.msd(self._step, n)[0] / float(self._n_particles)
         rows = []
         for k in range(n):
             self._time += dt
             self._step += 1
+            self._times.append(self._time)
             rows.append(f"{self._time:+.6e},{sums[k, 0]:+.6e},{sums[k, 1]:+.6e},{sums[k, 2]:+.6e}\n")
         self._open_msd_file()
         self._msd_file.write("".join(rows))
@@ -262,8 +285,10 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
         """n rounds of step(dt), save_metrics(dt), repopulate_contacts() as one engine call."""
         if n <= 0:
             return
-        prec = L.KMC_PREC_FP64 if self._json_prop.get("precision", "mixed") == "fp64" else L.KMC_PREC_MIXED
-        pop, cur, live = self._engine.contacts_run(n, dt, self._particle_velocity, prec)
+        pop, cur, live = self._engine.contacts_run(n, dt, self._particle_velocity, self._precision())
+        self._device_ms += self._engine.stats()["last_run_ms"]
+        self._dt = dt
+        self._step += n
         for k in range(n):
             self._last = (pop[k], cur[k], int(live[k]))
             self._time += dt
@@ -278,6 +303,50 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
             t += dt
             n += 1
         return n
+
+    def run_report(self, wall_seconds: float) -> dict:
+        """The run report (no counterpart in the reference, which prints only wall-clock start and
+        end, main.cpp:26-27,109-111), with the keys cntkmc_run writes to run_report.json: what ran,
+        the neighbour lists, hop counters, device and wall seconds with hops/s, and in Green-Kubo
+        mode D per axis with its 95 % interval from the exciton batches (last 80 % of the steps)."""
+        st = self._engine.stats()
+        nb = self._nbr_stats
+        j = self._json_prop
+        kubo = self._contacts is None
+        fin = (lambda v: float(v) if math.isfinite(v) else None)
+        dev_s = self._device_ms / 1e3
+        r = {"engine": L.load().kmc_version().decode(), "mode": "kubo" if kubo else "contacts",
+             "precision": "fp64" if self._precision() == L.KMC_PREC_FP64 else "mixed",
+             "philox seed": int(j.get("philox seed", 100))}
+        if kubo:
+            r["injection"] = "uniform" if j.get("injection", "region") == "uniform" else "region"
+        r.update({"particles": int(self._n_particles), "steps": int(self._step), "time step [s]": fin(self._dt),
+                  "simulated time [s]": fin(self._time), "sites": int(nb["n_sites"]), "neighbour entries": int(nb["nnz"]),
+                  "mean neighbours per site": fin(nb["k_mean"]), "max neighbours per site": int(nb["k_max"]),
+                  "neighbour build [s]": fin(nb["build_ms"] / 1e3), "hops": int(st["hops"]),
+                  "crossings": int(st["crossings"]), "exact re-resolves": int(st["exact_resolves"]),
+                  "device seconds": fin(dev_s), "hops per second (device)": fin(st["hops"] / dev_s) if dev_s > 0 else None,
+                  "wall seconds": fin(wall_seconds),
+                  "hops per second (wall)": fin(st["hops"] / wall_seconds) if wall_seconds > 0 else None})
+        if kubo:
+            D, ci = [None] * 3, [None] * 3
+            if self._step >= 2 and len(self._times) == self._step:
+                m = self._engine.msd_batches(0, self._step)[0]
+                d, c = diffusion.fit_counts(m, diffusion.batch_counts(self._n_particles, self._batches),
+                                            np.array(self._times), 0.8)
+                D, ci = [fin(v) for v in d], [fin(v) for v in c]
+            r.update({"msd batches": self._batches, "fit fraction": 0.8, "diffusion coefficient [m^2/s]": D,
+                      "diffusion 95% interval [m^2/s]": ci})
+        else:
+            r["live excitons"] = int(self._last[2]) if self._last is not None else int(self._n_particles)
+        return r
+
+    def write_run_report(self, wall_seconds: float) -> dict:
+        r = self.run_report(wall_seconds)
+        with open(os.path.join(self._output_directory, "run_report.json"), "w") as f:
+            json.dump(r, f, indent=2)
+            f.write("\n")
+        return r
 
     def close(self):
         for name in ("_msd_file", "_pop_file", "_cur_file"):
@@ -299,6 +368,7 @@ def run(input_json: str, device: int = 0) -> str:
         raise ValueError('json input file does not contain "exciton monte carlo"')
     jm = dict(j["exciton monte carlo"])
     dt = float(jm["monte carlo time step"])
+    t0 = time.perf_counter()
     if jm.get("mode") == "contacts":  # main.cpp:85-106, until the contacts time limit
         if "maximum time for contacts simulation [seconds]" not in jm:
             raise ValueError('contacts mode needs "maximum time for contacts simulation [seconds]"')
@@ -310,6 +380,7 @@ def run(input_json: str, device: int = 0) -> str:
         while left > 0:
             sim.contacts_steps_and_save(min(CHUNK, left), dt)
             left -= CHUNK
+        sim.write_run_report(time.perf_counter() - t0)
         out = sim.output_path()
         sim.close()
         return out
@@ -321,6 +392,7 @@ def run(input_json: str, device: int = 0) -> str:
     while left > 0:
         sim.kubo_steps_and_save(min(CHUNK, left), dt)
         left -= CHUNK
+    sim.write_run_report(time.perf_counter() - t0)
     out = sim.output_path()
     sim.close()
     return out

@@ -28,6 +28,7 @@ extern "C" {
 #define KMC_ERR_NOMEM (-6)     /* device or host allocation failed */
 #define KMC_ERR_NO_DEVICE (-7) /* no CUDA device / wrong architecture */
 #define KMC_ERR_CAPACITY (-8)  /* contacts mode: more excitons than slots */
+#define KMC_ERR_CHECK (-9)     /* libcntkmc_check.so only: a device bounds check failed (index or counter) */
 
 #define KMC_TABLE_4D 4 /* rate(theta)(z_shift, axis_shift_1, axis_shift_2), nearest grid point */
 #define KMC_TABLE_2D 2 /* rate(centre distance, folded angle in [0, pi/2]), nearest grid point */
@@ -199,6 +200,16 @@ int kmc_contacts_track(kmc_ctx* ctx, int64_t first, int32_t n_tracks, double dt,
 /* Exciton state (film-major, exciton order).  Any pointer may be NULL.  pos/delta are [n][3]. */
 int kmc_get_excitons(kmc_ctx* ctx, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,
                      uint64_t* draws, int64_t* hops);
+/* Checkpoint/resume (no counterpart in the reference, whose runs are not resumable): writes the
+ * state kmc_get_excitons returned back into the set kmc_init_excitons laid out with the same films,
+ * exciton counts, seeds and injection mode.  site is film-local; heading 0/1; pos, delta finite;
+ * ff finite and >= 0; hops >= 0; every array required.  draws is each exciton's Philox counter, so
+ * the resumed run continues every random stream where the saved one stopped: k steps, save,
+ * restore into a fresh context, n - k steps gives the state of n steps bit for bit.  The MSD bins
+ * and run statistics start again at zero.  KMC_ERR_STATE before kmc_init_excitons or in contacts
+ * mode; KMC_ERR_ARG on a bad field (nothing written). */
+int kmc_set_excitons(kmc_ctx* ctx, const int32_t* site, const double* pos, const double* delta, const double* ff,
+                     const int32_t* heading, const uint64_t* draws, const int64_t* hops);
 int64_t kmc_num_excitons(const kmc_ctx* ctx);
 int kmc_get_run_stats(kmc_ctx* ctx, kmc_run_stats* stats);
 

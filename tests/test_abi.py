@@ -29,6 +29,10 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, s), s
     assert set(syms) == set(L.SIGNATURES)
     assert lib.kmc_version().decode().startswith("cntkmc")
+    chk = L.load(checked=True)  # the KMC_CHECK build: same ABI, loaded beside the normal library
+    assert chk is not lib
+    for s in syms:
+        assert hasattr(chk, s), s
 
 
 def test_trim_and_forster_table_match_oracle():

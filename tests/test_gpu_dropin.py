@@ -123,3 +123,47 @@ def test_driver_with_a_table_saved_by_the_reference(tmp_path):
     got = got[:len(t)]
     np.testing.assert_allclose(got[:, 0], t, rtol=1e-6)
     np.testing.assert_allclose(got[:, 1:], msd, rtol=1e-6, atol=1e-30)
+
+
+REPORT_KEYS = ("engine", "mode", "precision", "philox seed", "injection", "particles", "steps", "time step [s]",
+               "simulated time [s]", "sites", "neighbour entries", "mean neighbours per site", "max neighbours per site",
+               "neighbour build [s]", "hops", "crossings", "exact re-resolves", "device seconds",
+               "hops per second (device)", "wall seconds", "hops per second (wall)", "msd batches", "fit fraction",
+               "diffusion coefficient [m^2/s]", "diffusion 95% interval [m^2/s]")
+
+
+@pytest.mark.parametrize("name", CASES[:1])
+def test_run_reports_of_driver_and_class_agree(name, tmp_path):
+    # run_report.json from cntkmc_run and from the Python class: the same counters, and the same
+    # D per axis (MSD batch sums of device atomics: equal to rounding)
+    d = load_case(name)
+    reports = []
+    for which in ("driver", "class"):
+        tmp = os.path.join(str(tmp_path), which)
+        os.makedirs(tmp)
+        cfg = _input_json(d, tmp, "mixed")
+        if which == "driver":
+            B.build()
+            r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
+            assert r.returncode == 0, r.stderr
+            out = os.path.join(tmp, "out")
+        else:
+            out = MC.run(cfg)
+        with open(os.path.join(out, "run_report.json")) as f:
+            rep = json.load(f)
+        assert set(REPORT_KEYS) <= set(rep), set(REPORT_KEYS) - set(rep)
+        rows = _read_msd_file(out)
+        assert rep["mode"] == "kubo" and rep["precision"] == "mixed" and rep["philox seed"] == int(d["seed"])
+        assert rep["steps"] == rows.shape[0] and rep["simulated time [s]"] == pytest.approx(rows[-1, 0], rel=1e-6)
+        assert rep["particles"] == d["config"]["number of particles for kubo simulation"]
+        assert rep["hops"] > 0 and rep["device seconds"] > 0 and rep["hops per second (device)"] > 0
+        reports.append(rep)
+    a, b = reports
+    for k in ("particles", "steps", "sites", "neighbour entries", "max neighbours per site", "hops", "crossings",
+              "exact re-resolves", "msd batches"):
+        assert a[k] == b[k], k
+    if a["steps"] >= 2:
+        np.testing.assert_allclose(a["diffusion coefficient [m^2/s]"], b["diffusion coefficient [m^2/s]"], rtol=1e-9)
+        assert all(v is not None for v in a["diffusion coefficient [m^2/s]"])
+        if a["msd batches"] >= 2:
+            assert all(v is not None and v > 0 for v in a["diffusion 95% interval [m^2/s]"])
