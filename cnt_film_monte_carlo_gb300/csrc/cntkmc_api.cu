@@ -95,7 +95,7 @@ struct kmc_ctx {
   kmc_mlp_shape mlp_shape{};
   int32_t mlp_np = 0;
   int64_t mlp_adam_t = 0, mlp_n_samples = 0;
-  DevBuf<float> d_mlp_master, d_mlp_m1, d_mlp_m2, d_mlp_part, d_mlp_grad;
+  DevBuf<float> d_mlp_master, d_mlp_m1, d_mlp_m2, d_mlp_part, d_mlp_grad, d_mlp_image;
   DevBuf<uint16_t> d_mlp_wbf;
   DevBuf<double> d_mlp_ploss, d_mlp_loss;
   DevBuf<float4> d_mlp_samples;
@@ -1723,6 +1723,7 @@ static kmc::MlpDev mlp_dev(const kmc_ctx* c) {
   m.log_scale = c->mlp_shape.log_scale;
   m.master = c->d_mlp_master.p;
   m.wbf = c->d_mlp_wbf.p;
+  m.image = c->d_mlp_image.p;
   return m;
 }
 
@@ -1768,6 +1769,8 @@ int kmc_mlp_init(kmc_ctx* c, const kmc_mlp_shape* sh, uint64_t seed) {
   CK(c, c->d_mlp_grad.alloc(np));
   CK(c, c->d_mlp_wbf.alloc(np));
   CK(c, c->d_mlp_part.alloc((size_t)c->n_sms * np));
+  CK(c, c->d_mlp_image.alloc(kmc::kMlpImageFloats));
+  CK(c, cudaMemsetAsync(c->d_mlp_image.p, 0, kmc::kMlpImageFloats * sizeof(float), c->stream));
   // partial entries no thread owns (the padding after b3) stay zero
   CK(c, cudaMemsetAsync(c->d_mlp_part.p, 0, (size_t)c->n_sms * np * sizeof(float), c->stream));
   CK(c, c->d_mlp_ploss.alloc(c->n_sms));
@@ -1847,6 +1850,7 @@ int kmc_mlp_gradient(kmc_ctx* c, int64_t first, int64_t count, float* grad, doub
   CK(c, cudaSetDevice(c->device));
   const kmc::MlpDev m = mlp_dev(c);
   const int grid = mlp_grid(c, count);
+  CK(c, kmc::launch_mlp_image(m, c->stream));
   kmc::MlpStep st{};
   st.inv_count = 1.0 / (double)count;
   CK(c, kmc::launch_mlp_grad(m, c->d_mlp_samples.p, first, count, c->d_mlp_part.p, c->d_mlp_ploss.p, grid, c->stream));
@@ -1871,13 +1875,17 @@ int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats*
   CK(c, cudaSetDevice(c->device));
   kmc::NvtxRange nv("kmc_mlp_train");
   const kmc::MlpDev m = mlp_dev(c);
+  CK(c, kmc::launch_mlp_image(m, c->stream));
   const int64_t per_epoch = c->mlp_n_samples / cfg->batch;
   const int64_t total = per_epoch * cfg->epochs;
   const int grid = mlp_grid(c, cfg->batch);
-  CK(c, cudaEventRecord(c->ev0, c->stream));
+  // the whole schedule (cosine learning rate, Adam bias corrections, where the loss is kept) on
+  // the device; each gradient launch advances a device counter that its update launch reads, so
+  // one epoch of launches with fixed arguments is captured once and replayed every epoch
+  std::vector<kmc::MlpStep> sched((size_t)total);
   for (int64_t k = 0; k < total; ++k) {
-    const int64_t t = ++c->mlp_adam_t;
-    kmc::MlpStep st{};
+    const int64_t t = c->mlp_adam_t + k + 1;
+    kmc::MlpStep& st = sched[(size_t)k];
     const double cosine = 0.5 * (1.0 + std::cos(3.141592653589793 * (double)k / (double)total));
     st.lr = (float)(cfg->lr_final + (cfg->lr - cfg->lr_final) * cosine);
     st.beta1 = (float)cfg->beta1;
@@ -1887,11 +1895,39 @@ int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats*
     st.c2 = (float)(1.0 / (1.0 - std::pow(cfg->beta2, (double)t)));
     st.inv_count = 1.0 / (double)cfg->batch;
     st.update = 1;
-    double* loss_out = k == 0 ? c->d_mlp_loss.p : (k == total - 1 ? c->d_mlp_loss.p + 1 : nullptr);
-    CK(c, kmc::launch_mlp_grad(m, c->d_mlp_samples.p, (k % per_epoch) * cfg->batch, cfg->batch, c->d_mlp_part.p,
-                               c->d_mlp_ploss.p, grid, c->stream));
-    CK(c, kmc::launch_mlp_update(m, c->d_mlp_master.p, c->d_mlp_wbf.p, c->d_mlp_m1.p, c->d_mlp_m2.p, c->d_mlp_part.p,
-                                 c->d_mlp_ploss.p, grid, st, nullptr, loss_out, c->stream));
+    st.loss_slot = k == 0 ? 0 : (k == total - 1 ? 1 : -1);
+  }
+  c->mlp_adam_t += total;
+  DevBuf<kmc::MlpStep> d_sched;
+  DevBuf<unsigned long long> d_ctr;
+  CK(c, upload(d_sched, sched.data(), sched.size(), c->stream));
+  CK(c, d_ctr.alloc(1));
+  CK(c, cudaMemsetAsync(d_ctr.p, 0, sizeof(unsigned long long), c->stream));
+  auto epoch = [&]() -> cudaError_t {
+    for (int64_t k = 0; k < per_epoch; ++k) {
+      cudaError_t e = kmc::launch_mlp_grad(m, c->d_mlp_samples.p, k * cfg->batch, cfg->batch, c->d_mlp_part.p,
+                                           c->d_mlp_ploss.p, grid, c->stream, d_ctr.p);
+      if (e == cudaSuccess)
+        e = kmc::launch_mlp_update(m, c->d_mlp_master.p, c->d_mlp_wbf.p, c->d_mlp_m1.p, c->d_mlp_m2.p,
+                                   c->d_mlp_part.p, c->d_mlp_ploss.p, grid, kmc::MlpStep{}, nullptr, c->d_mlp_loss.p,
+                                   c->stream, d_sched.p, d_ctr.p);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
+  cudaGraphExec_t exec = nullptr;
+  const bool graph = c->use_graph && per_epoch <= 1024 && cfg->epochs > 1;
+  if (graph) {
+    int rc = capture_graph(c, &exec, epoch);
+    if (rc) return rc;
+  }
+  CK(c, cudaEventRecord(c->ev0, c->stream));
+  for (int64_t e = 0; e < cfg->epochs; ++e) {
+    cudaError_t err = graph ? cudaGraphLaunch(exec, c->stream) : epoch();
+    if (err != cudaSuccess) {
+      if (exec) cudaGraphExecDestroy(exec);
+      CK(c, err);
+    }
   }
   CK(c, cudaEventRecord(c->ev1, c->stream));
   double l[2] = {0, 0};
@@ -1899,6 +1935,7 @@ int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats*
   CK(c, cudaStreamSynchronize(c->stream));
   float ms = 0;
   CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  if (exec) cudaGraphExecDestroy(exec);
   if (stats) {
     stats->steps = total;
     stats->first_loss = l[0];

@@ -291,26 +291,37 @@ struct MlpDev {
   double log_mean, log_scale; // ln rate = y log_scale + log_mean
   const float* master;        // [n_params] FP32 master parameters (biases, embedding read here)
   const uint16_t* wbf;        // [n_params] BF16 copies (weight-matrix entries used)
+  float* image;               // [kMlpImageFloats] the gradient kernel's shared-memory weights
 };
+// The network as the gradient kernel holds it in shared memory: W2 and W2^T with 68-word rows,
+// W1, b1, b2, w3, the embedding, b3 (FP32; matrices widened from BF16).  Kept in global memory
+// by the update kernel so that each gradient launch copies it with 16-byte loads.
+constexpr int kMlpImageFloats = 2 * kMlpH * 68 + kMlpH * 4 + 3 * kMlpH + 2 * 8 * 8 + 4;
 struct MlpStep {
   float lr, beta1, beta2, eps;
   float c1, c2;               // Adam bias corrections 1 / (1 - beta^t)
   double inv_count;           // 1 / samples of the step (loss = sum r^2 inv_count)
   int32_t update;             // 0: only reduce the gradient
+  int32_t loss_slot;          // scheduled steps: the loss goes to loss_out[loss_slot] (-1: not kept)
 };
 size_t mlp_grad_smem_bytes();
+cudaError_t launch_mlp_image(const MlpDev& m, cudaStream_t s);  // the image from master / wbf
 // labelled samples -> {log-distance input, angle input, pair bits, normalised label}
 cudaError_t launch_mlp_samples(const MlpDev& m, const double* dist, const double* theta, const int32_t* pair,
                                const double* log_rate, int64_t n, float4* out, cudaStream_t s);
 // per-block gradient partials part[grid][n_params] and squared-error sums part_loss[grid] of
 // samples [first, first + count)
+// step_ctr (optional): block 0 adds 1 when the launch starts (the scheduled training loop)
 cudaError_t launch_mlp_grad(const MlpDev& m, const float4* samples, int64_t first, int64_t count, float* part,
-                            double* part_loss, int grid, cudaStream_t s);
+                            double* part_loss, int grid, cudaStream_t s, unsigned long long* step_ctr = nullptr);
 // sum of the partials in block order (grad_out, loss_out optional) and, if st.update, one Adam
-// step of master (and its BF16 copy)
+// step of master (and its BF16 copy).  With sched, the step is sched[*step_ctr - 1] (the counter
+// the gradient launch advanced) and its loss goes to loss_out[loss_slot]: a CUDA graph of launches
+// with fixed arguments then runs every step of a schedule.
 cudaError_t launch_mlp_update(const MlpDev& m, float* master, uint16_t* wbf, float* mom1, float* mom2,
                               const float* part, const double* part_loss, int grid, const MlpStep& st,
-                              float* grad_out, double* loss_out, cudaStream_t s);
+                              float* grad_out, double* loss_out, cudaStream_t s, const MlpStep* sched = nullptr,
+                              const unsigned long long* step_ctr = nullptr);
 cudaError_t launch_mlp_bf16(const float* master, uint16_t* wbf, int32_t n, cudaStream_t s);
 cudaError_t launch_mlp_predict(const MlpDev& m, const double* dist, const double* theta, const int32_t* pair,
                                int64_t n, double* log_rate, cudaStream_t s);
