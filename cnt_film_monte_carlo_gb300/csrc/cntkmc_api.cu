@@ -437,6 +437,20 @@ static kmc::PairScreen pair_screen(double r, double M) {
   return sc;
 }
 
+// The largest double x with sqrt(x) <= v (le) or the smallest with sqrt(x) >= v (ge), sqrt
+// correctly rounded (IEEE 754, as on the device): the window test on squared distances.
+static double sqrt_bound(double v, bool ge) {
+  double x = v * v;
+  if (ge) {
+    while (x > 0 && std::sqrt(std::nextafter(x, 0.0)) >= v) x = std::nextafter(x, 0.0);
+    while (std::sqrt(x) < v) x = std::nextafter(x, INFINITY);
+  } else {
+    while (std::sqrt(std::nextafter(x, INFINITY)) <= v) x = std::nextafter(x, INFINITY);
+    while (x > 0 && std::sqrt(x) > v) x = std::nextafter(x, 0.0);
+  }
+  return x;
+}
+
 int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   if (!c) return KMC_ERR_ARG;
   if (!c->film_loaded || !c->has_table) FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: load a film and a rate table first");
@@ -455,7 +469,8 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
     const auto& d = c->domains[i];
     double nd[3];
     for (int k = 0; k < 3; ++k) nd[k] = std::ceil((d[3 + k] - d[k]) / r_max) + 1;
-    if (!(nd[0] * nd[1] * nd[2] < 4e9)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: cell grid too large");
+    if (!(nd[0] * nd[1] * nd[2] < 2147483648.0))  // cell indices within a film are 32-bit
+      FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: cell grid too large (2^31 cells per film)");
     fd.nx = (int32_t)nd[0];
     fd.ny = (int32_t)nd[1];
     fd.nz = (int32_t)nd[2];
@@ -499,6 +514,8 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   a.n_films = c->n_films;
   a.pos4f = c->d_pos4f.p;
   a.scr = pair_screen(r_max, max_coord);
+  a.win_lo2 = sqrt_bound(kmc::kMinHopDist, false);  // d2 > win_lo2  <=>  sqrt(d2) > kMinHopDist
+  a.win_hi2 = sqrt_bound(r_max, true);              // d2 < win_hi2  <=>  sqrt(d2) < r_max
   a.perm = c->d_perm.p;
   a.rank = c->d_rank.p;
   a.pos4 = c->d_pos4.p;

@@ -160,6 +160,10 @@ struct BuildArgs {
   const double4_32a* pos4;
   const float4* pos4f;     // FP32 copy of pos4
   PairScreen scr;
+  // find_neighbors' window kMinHopDist < sqrt(d2) < r_max (FP64 root, scatterer.cpp:43) as
+  // d2 > win_lo2 && d2 < win_hi2: the root is correctly rounded and monotone, so these squared
+  // bounds (found on the host) give the same answer for every double d2 without a root
+  double win_lo2, win_hi2;
   const double* orient;    // [n][3]
   const int32_t* site_film;
   const FilmDev* films;

@@ -161,20 +161,31 @@ cudaError_t ids_to_slots(int32_t* ids, int64_t n, const int32_t* rank, cudaStrea
 }
 
 // ============================================================================ K2: neighbour + rate CSR
-// Visit the neighbours of site s in find_neighbors order; fn(j, p2, dR, distance) per neighbour.
+// Visit the neighbours of site s in find_neighbors order; fn(j) per neighbour (reference id).
 // Candidates are screened with FP32 squared distances: a candidate clear of both window edges
 // (0.4 nm, r) by the screen's error bound is in or out without FP64 work; only those within
-// the bound of an edge take the reference's FP64 test, so the neighbour set is exact.  With
-// kGeom false (counting) accepted candidates get no FP64 geometry either.
-template <bool kGeom, typename F>
+// the bound of an edge take the reference's FP64 test, on the squared distance against the
+// window's squared bounds (no root), so the neighbour set is exact.
+// The FP64 window test of a pair the FP32 screen left undecided, out of line: it runs for a
+// few candidates in 10^4, and the screen loop runs several times faster without FP64 code in it.
+static __device__ __noinline__ bool in_window_fp64(const BuildArgs& a, int64_t s, int32_t q) {
+  const double4_32a p1 = a.pos4[s], p2 = a.pos4[q];
+  const double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
+  const double e2 = dot3(dR0, dR1, dR2, dR0, dR1, dR2);  // norm3's sum, before its root
+  return e2 < a.win_hi2 && e2 > a.win_lo2;
+}
+
+// kOutline: the FP64 test as a call (the counting pass, whose loop is otherwise FP64-free and
+// runs ~2.8x faster so); inline in the filling pass, whose FP64 rate code makes a call in the
+// loop cost more than it saves.
+template <bool kOutline, typename F>
 __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s, F fn) {
   const FilmDev& f = a.films[a.site_film[s]];
-  double4_32a p1 = a.pos4[s];
   const float4 p1f = a.pos4f[s];
-  int64_t local = a.cell_of[s] - f.cell0;
-  int ix = (int)(local % f.nx);
-  int iy = (int)((local / f.nx) % f.ny);
-  int iz = (int)(local / ((int64_t)f.nx * f.ny));
+  const int local = (int)(a.cell_of[s] - f.cell0);  // a film's cell grid has fewer than 2^31 cells
+  const int ix = local % f.nx;
+  const int iy = (local / f.nx) % f.ny;
+  const int iz = local / (f.nx * f.ny);
   for (int i = ix - 1; i <= ix + 1; ++i) {
     if (i < 0 || i >= f.nx) continue;
     for (int j = iy - 1; j <= iy + 1; ++j) {
@@ -188,15 +199,17 @@ __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s,
           const float fx = p1f.x - p2f.x, fy = p1f.y - p2f.y, fz = p1f.z - p2f.z;
           const float d2 = fx * fx + fy * fy + fz * fz;
           if (d2 >= a.scr.out_hi2 || d2 <= a.scr.out_lo2) continue;  // surely outside the window
-          const bool inside = d2 < a.scr.in_hi2 && d2 > a.scr.in_lo2;  // surely inside
-          if (!kGeom && inside) {
-            fn(q, p1, 0.0, 0.0, 0.0, 0.0);
-            continue;
+          if (!(d2 < a.scr.in_hi2 && d2 > a.scr.in_lo2)) {  // not surely inside
+            if (kOutline) {
+              if (!in_window_fp64(a, s, q)) continue;
+            } else {
+              const double4_32a p1 = a.pos4[s], p2 = a.pos4[q];
+              const double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
+              const double e2 = dot3(dR0, dR1, dR2, dR0, dR1, dR2);
+              if (!(e2 < a.win_hi2 && e2 > a.win_lo2)) continue;
+            }
           }
-          double4_32a p2 = a.pos4[q];
-          double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
-          double distance = norm3(dR0, dR1, dR2);
-          if (inside || ((distance < a.r_max) && (distance > kMinHopDist))) fn(q, p2, dR0, dR1, dR2, distance);
+          fn(q);
         }
       }
     }
@@ -205,15 +218,24 @@ __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s,
 
 // Both passes take the sites in storage order (thread i: site perm[i]), so the threads of a warp
 // scan the same cells and write neighbouring rows.
+// The longest row and the empty rows are reduced over the warp first: one atomic per warp, not
+// one per site on the same two words.
 __global__ void k_nbr_count(BuildArgs a) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= a.n_sites) return;
-  const int64_t s = a.perm[i];
-  int64_t n = 0;
-  for_each_neighbor<false>(a, s, [&](int32_t, const double4_32a&, double, double, double, double) { ++n; });
-  a.counts[s] = n;
-  atomicMax(&a.stats[0], (unsigned long long)n);
-  if (n == 0) atomicAdd(&a.stats[1], 1ull);
+  const bool live = i < a.n_sites;
+  unsigned n = 0;
+  if (live) {
+    const int64_t s = a.perm[i];
+    for_each_neighbor<true>(a, s, [&](int32_t) { ++n; });
+    a.counts[s] = n;
+  }
+  const unsigned m = __activemask();
+  const unsigned kmax = __reduce_max_sync(m, n);
+  const unsigned empty = __popc(__ballot_sync(m, live && n == 0));
+  if ((threadIdx.x & 31) == __ffs(m) - 1) {
+    atomicMax(&a.stats[0], (unsigned long long)kmax);
+    if (empty) atomicAdd(&a.stats[1], (unsigned long long)empty);
+  }
 }
 
 // Row of site s (reference id) into storage slot rank[s]; neighbour ids and links are stored as
@@ -232,7 +254,7 @@ __global__ void k_nbr_fill(BuildArgs a) {
   const int64_t bo = a.blkptr[si];
   double* cump = a.cump + bo * 8;  // this row's FP64 cumulative rates (8 per block)
   int64_t k = 0;
-  for_each_neighbor<false>(a, s, [&](int32_t q, const double4_32a&, double, double, double, double) {
+  for_each_neighbor<false>(a, s, [&](int32_t q) {
     a.blocks[bo + (k >> 3)].col[k & 7] = q;
     ++k;
   });

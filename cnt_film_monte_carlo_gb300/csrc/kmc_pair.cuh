@@ -60,6 +60,15 @@ __device__ __forceinline__ double pair_rate(const TableDev& t, const double4_32a
   return table_rate(t, theta, zsh, ash1, ash2, distance, pair_off);
 }
 
+// pair_rate_2d's exact path (the reference's root and arccosine), out of line: it runs for a
+// few pairs in 10^4, and inlined it would sit in the row loop of every pair.
+static __device__ __noinline__ double pair_rate_2d_exact(const TableDev& t, const double* a1v, const double* a2v,
+                                                         double dR0, double dR1, double dR2, double d2, int64_t pair_off,
+                                                         const double4_32a& p1, const double4_32a& p2) {
+  const double a1c[3] = {a1v[0], a1v[1], a1v[2]}, a2c[3] = {a2v[0], a2v[1], a2v[2]};
+  return pair_rate(t, p1, a1c, p2, a2c, dR0, dR1, dR2, sqrt(d2), pair_off);
+}
+
 // Rate of a 2-D table (kinds 2, 3) for a pair in the window, from dR and the two axes: the same
 // table entry as pair_rate, found without its FP64 square root and arccosine.  The nearest
 // distance index follows from d^2 against the squared midpoints of the distance grid, the
@@ -86,8 +95,7 @@ __device__ __forceinline__ double pair_rate_2d(const TableDev& t, const double* 
     const bool ok1 = (c1 == 0 || ac < t.cut_cos[c1 - 1] - 1e-13) && (c1 == n1 - 1 || ac > t.cut_cos[c1] + 1e-13);
     if (ok0 && ok1) return t.rate[pair_off + (int64_t)c0 * n1 + c1];
   }
-  const double a1c[3] = {a1v[0], a1v[1], a1v[2]}, a2c[3] = {a2v[0], a2v[1], a2v[2]};
-  return pair_rate(t, p1, a1c, p2, a2c, dR0, dR1, dR2, sqrt(d2), pair_off);
+  return pair_rate_2d_exact(t, a1v, a2v, dR0, dR1, dR2, d2, pair_off, p1, p2);
 }
 
 }  // namespace kmc
