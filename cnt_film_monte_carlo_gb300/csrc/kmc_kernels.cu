@@ -182,19 +182,25 @@ template <bool kOutline, typename F>
 __device__ __forceinline__ void for_each_neighbor(const BuildArgs& a, int64_t s, F fn) {
   const FilmDev& f = a.films[a.site_film[s]];
   const float4 p1f = a.pos4f[s];
-  const int local = (int)(a.cell_of[s] - f.cell0);  // a film's cell grid has fewer than 2^31 cells
-  const int ix = local % f.nx;
-  const int iy = (local / f.nx) % f.ny;
-  const int iz = local / (f.nx * f.ny);
+  // the film's cell grid in 32-bit indices (fewer than 2^31 cells per film)
+  const int nx = f.nx, ny = f.ny, nz = f.nz;
+  const int64_t* __restrict__ cstart = a.cell_start + f.cell0;
+  const int local = (int)(a.cell_of[s] - f.cell0);
+  const int ix = local % nx;
+  const int iy = (local / nx) % ny;
+  const int iz = local / (nx * ny);
   for (int i = ix - 1; i <= ix + 1; ++i) {
-    if (i < 0 || i >= f.nx) continue;
+    if (i < 0 || i >= nx) continue;
     for (int j = iy - 1; j <= iy + 1; ++j) {
-      if (j < 0 || j >= f.ny) continue;
+      if (j < 0 || j >= ny) continue;
       for (int k = iz - 1; k <= iz + 1; ++k) {
-        if (k < 0 || k >= f.nz) continue;
-        int64_t c = f.cell0 + i + (int64_t)j * f.nx + (int64_t)k * f.nx * f.ny;
-        for (int64_t m = a.cell_start[c], e = a.cell_start[c + 1]; m < e; ++m) {
-          int32_t q = a.cell_members[m];
+        if (k < 0 || k >= nz) continue;
+        const int lc = i + j * nx + k * nx * ny;
+        const int64_t m0 = cstart[lc];
+        const int nm = (int)(cstart[lc + 1] - m0);
+        const int32_t* __restrict__ cm = a.cell_members + m0;
+        for (int t = 0; t < nm; ++t) {
+          const int32_t q = cm[t];
           const float4 p2f = a.pos4f[q];
           const float fx = p1f.x - p2f.x, fy = p1f.y - p2f.y, fz = p1f.z - p2f.z;
           const float d2 = fx * fx + fy * fy + fz * fz;
