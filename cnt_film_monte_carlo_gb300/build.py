@@ -92,9 +92,9 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
         for text in ex.map(_run, jobs):
             out.append(text)
     if force or jobs or _stale(LIB, objs):
-        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"]))
+        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl", "-lpthread"]))
     if force or jobs or _stale(LIB_CHECK, check_objs):
-        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB_CHECK] + check_objs + ["-lcudart", "-ldl"]))
+        out.append(_run([nvcc()] + ARCH + ["-shared", "-o", LIB_CHECK] + check_objs + ["-lcudart", "-ldl", "-lpthread"]))
     drv_src = [os.path.join(CSRC, s) for s in DRIVER_SOURCES]
     if all(os.path.exists(s) for s in drv_src) and (force or _stale(DRIVER, drv_src + headers + [LIB])):
         out.append(_run(["g++"] + CXX_FLAGS + ["-o", DRIVER] + drv_src + ["-L" + HERE, "-lcntkmc",

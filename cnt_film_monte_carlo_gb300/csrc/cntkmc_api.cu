@@ -9,6 +9,7 @@
 #include <cstring>
 #include <functional>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -293,51 +294,91 @@ void kmc_destroy(kmc_ctx* c) {
 
 const char* kmc_last_error(const kmc_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+// The positions of every site on the host ([n][3], reference order), fetched from the device
+// the first time a host-side step needs them (region injection, contacts set-up, restored
+// exciton states); kmc_load_film does not keep a host copy.
+static int host_positions(kmc_ctx* c) {
+  const int64_t n = c->n_sites;
+  if ((int64_t)c->pos.size() == 3 * n) return KMC_OK;
+  std::vector<double4_32a> p4((size_t)n);
+  CK(c, cudaMemcpyAsync(p4.data(), c->d_pos4.p, (size_t)n * sizeof(double4_32a), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->pos.resize(3 * (size_t)n);
+  for (int64_t s = 0; s < n; ++s) {
+    c->pos[3 * s] = p4[s].x;
+    c->pos[3 * s + 1] = p4[s].y;
+    c->pos[3 * s + 2] = p4[s].z;
+  }
+  return KMC_OK;
+}
+
 int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
   if (!c) return KMC_ERR_ARG;
   if (!f || f->n_films < 1 || !f->film_site_offsets || !f->pos || !f->orient || !f->left || !f->right)
     FAIL(c, KMC_ERR_ARG, "kmc_load_film: missing arrays");
   CK(c, cudaSetDevice(c->device));
   kmc::NvtxRange nv("kmc_load_film");
+  c->film_loaded = false;  // until every check below has passed
+  c->built = false;
+  drop_excitons(c);
   const int32_t nf = f->n_films;
   const int64_t n = f->film_site_offsets[nf];
   if (f->film_site_offsets[0] != 0 || n <= 0 || n >= (1LL << 31)) FAIL(c, KMC_ERR_ARG, "kmc_load_film: bad offsets");
-  std::vector<int32_t> L(n), R(n), sf(n);
-  std::vector<double4_32a> p4(n);
   c->films.assign(nf, FilmDev{});
   c->domains.assign(nf, {});
   for (int32_t i = 0; i < nf; ++i) {
-    int64_t s0 = f->film_site_offsets[i], s1 = f->film_site_offsets[i + 1];
+    const int64_t s0 = f->film_site_offsets[i], s1 = f->film_site_offsets[i + 1];
     if (s1 <= s0) FAIL(c, KMC_ERR_ARG, "kmc_load_film: film %d has no sites", i);
-    FilmDev& fd = c->films[i];
-    fd.site0 = s0;
-    fd.n_sites = s1 - s0;
-    double mn[3], mx[3];
-    kmc_domain(s1 - s0, f->pos + 3 * s0, mn, mx);
-    for (int k = 0; k < 3; ++k) {
-      c->domains[i][k] = mn[k];
-      c->domains[i][3 + k] = mx[k];
-      fd.mn[k] = mn[k];
-    }
-    for (int64_t s = s0; s < s1; ++s) {
-      int32_t l = f->left[s], r = f->right[s];
-      if (l >= fd.n_sites || r >= fd.n_sites || l < -1 || r < -1) FAIL(c, KMC_ERR_ARG, "kmc_load_film: bad link at %lld", (long long)s);
-      L[s] = l < 0 ? -1 : (int32_t)(s0 + l);
-      R[s] = r < 0 ? -1 : (int32_t)(s0 + r);
-      sf[s] = i;
-      p4[s] = make_double4_32a(f->pos[3 * s], f->pos[3 * s + 1], f->pos[3 * s + 2], 0.0);
-    }
+    c->films[i].site0 = s0;
+    c->films[i].n_sites = s1 - s0;
   }
+  // the raw arrays go to the device as they are (the copies overlap the domains below); a kernel
+  // forms the padded positions, the global links and each site's film
+  DevBuf<double> d_pos_raw;
+  DevBuf<int32_t> d_l_raw, d_r_raw;
+  DevBuf<int64_t> d_off;
+  DevBuf<unsigned long long> d_bad;
+  CK(c, upload(d_off, f->film_site_offsets, (size_t)nf + 1, c->stream));
+  CK(c, upload(d_pos_raw, f->pos, 3 * (size_t)n, c->stream));
+  CK(c, upload(d_l_raw, f->left, (size_t)n, c->stream));
+  CK(c, upload(d_r_raw, f->right, (size_t)n, c->stream));
+  CK(c, upload(c->d_orient, f->orient, 3 * (size_t)n, c->stream));
+  CK(c, d_bad.alloc(1));
+  CK(c, cudaMemsetAsync(d_bad.p, 0xFF, sizeof(unsigned long long), c->stream));
+  CK(c, c->d_pos4.alloc(n));
+  CK(c, c->d_left.alloc(n));
+  CK(c, c->d_right.alloc(n));
+  CK(c, c->d_site_film.alloc(n));
+  CK(c, kmc::launch_load_sites(n, nf, d_off.p, d_pos_raw.p, d_l_raw.p, d_r_raw.p, c->d_pos4.p, c->d_left.p,
+                               c->d_right.p, c->d_site_film.p, d_bad.p, c->stream));
+  // find_simulation_domain of every film (monte_carlo.h:328-340), on the host threads
+  {
+    const unsigned nt = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)nf));
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t)
+      pool.emplace_back([&, t]() {
+        for (int32_t i = (int32_t)t; i < nf; i += (int32_t)nt) {
+          const FilmDev& fd = c->films[i];
+          double mn[3], mx[3];
+          kmc_domain(fd.n_sites, f->pos + 3 * fd.site0, mn, mx);
+          for (int k = 0; k < 3; ++k) {
+            c->domains[i][k] = mn[k];
+            c->domains[i][3 + k] = mx[k];
+          }
+        }
+      });
+    for (auto& th : pool) th.join();
+  }
+  for (int32_t i = 0; i < nf; ++i)
+    for (int k = 0; k < 3; ++k) c->films[i].mn[k] = c->domains[i][k];
+  unsigned long long bad = 0;
+  CK(c, cudaMemcpyAsync(&bad, d_bad.p, sizeof bad, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (bad != ~0ull) FAIL(c, KMC_ERR_ARG, "kmc_load_film: bad link at %lld", (long long)bad);
   c->n_films = nf;
   c->n_sites = n;
   c->film_off.assign(f->film_site_offsets, f->film_site_offsets + nf + 1);
-  c->pos.assign(f->pos, f->pos + 3 * n);
-  CK(c, upload(c->d_pos4, p4.data(), n, c->stream));
-  CK(c, upload(c->d_orient, f->orient, 3 * n, c->stream));
-  CK(c, upload(c->d_left, L.data(), n, c->stream));
-  CK(c, upload(c->d_right, R.data(), n, c->stream));
-  CK(c, upload(c->d_site_film, sf.data(), n, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));
+  c->pos.clear();  // the host copy of the positions is fetched from the device when first needed
   c->film_loaded = true;
   c->n_species = 0;
   c->built = false;
@@ -507,7 +548,8 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   CK(c, cudaMemsetAsync(c->d_stats.p, 0, 4 * sizeof(unsigned long long), c->stream));
   CK(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int32_t), c->stream));
   double max_coord = 0;
-  for (double v : c->pos) max_coord = std::max(max_coord, std::fabs(v));
+  for (const auto& d : c->domains)  // the largest coordinate magnitude: the films' domain bounds
+    for (double v : d) max_coord = std::max(max_coord, std::fabs(v));
   CK(c, c->d_pos4f.alloc(n));
   CK(c, kmc::launch_pos_f32(c->d_pos4.p, c->d_pos4f.p, n, c->stream));
   kmc::BuildArgs a{};
@@ -642,6 +684,8 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
   const int nsec = inj->n_sections;
   if (inj->mode == KMC_INJECT_REGION && !(nsec > 1 && nsec % 2 == 1 && nsec < 1000))
     FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: number of sections must be odd and > 1");
+  if (inj->mode == KMC_INJECT_REGION)
+    if (int rc = host_positions(c)) return rc;
   std::vector<int32_t> inject;
   std::vector<int32_t> warp_film;
   int64_t slot = 0, total = 0;
@@ -1002,6 +1046,7 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
       FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: contact population out of range");
   CK(c, cudaSetDevice(c->device));
   kmc::NvtxRange nv("kmc_contacts_init");
+  if (int rc = host_positions(c)) return rc;
   const int64_t n = c->n_sites;
   const auto& dom = c->domains[0];
   const double ymin = dom[1], ymax = dom[4];
@@ -1571,6 +1616,7 @@ int kmc_set_excitons(kmc_ctx* c, const int32_t* site, const double* pos, const d
   if (!site || !pos || !delta || !ff || !heading || !draws || !hops) FAIL(c, KMC_ERR_ARG, "kmc_set_excitons: missing arrays");
   CK(c, cudaSetDevice(c->device));
   kmc::NvtxRange nv("kmc_set_excitons");
+  if (int rc = host_positions(c)) return rc;
   const int64_t ns = c->n_slots, n = c->n_sites;
   std::vector<int32_t> rank(n);
   for (int64_t k = 0; k < n; ++k) rank[c->h_perm[k]] = (int32_t)k;

@@ -198,6 +198,13 @@ struct BuildArgs {
 
 // launchers (kmc_kernels.cu); all return cudaError_t of the launch
 cudaError_t launch_pos_f32(const double4_32a* p, float4* out, int64_t n, cudaStream_t s);
+// The loaded films' sites on the device: positions [n][3] -> pos4, film-local links -> global
+// links, the film of every site (offsets[n_films + 1]).  A link outside its film sets *bad_site
+// to the smallest such site index (initialised to INT64_MAX by the caller).
+cudaError_t launch_load_sites(int64_t n, int32_t n_films, const int64_t* offsets, const double* pos,
+                              const int32_t* left_local, const int32_t* right_local, double4_32a* pos4,
+                              int32_t* left, int32_t* right, int32_t* site_film, unsigned long long* bad_site,
+                              cudaStream_t s);
 cudaError_t launch_cell_ids(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_cell_fill(const BuildArgs& a, cudaStream_t s);
 cudaError_t launch_nbr_count(const BuildArgs& a, cudaStream_t s);

@@ -72,6 +72,38 @@ __global__ void k_pos_f32(const double4_32a* __restrict__ p, float4* __restrict_
   out[s] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
 }
 
+__global__ void k_load_sites(int64_t n, int32_t n_films, const int64_t* __restrict__ off, const double* __restrict__ pos,
+                             const int32_t* __restrict__ lloc, const int32_t* __restrict__ rloc, double4_32a* pos4,
+                             int32_t* left, int32_t* right, int32_t* site_film, unsigned long long* bad) {
+  const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int lo = 0, hi = n_films;  // the film f with off[f] <= s < off[f + 1]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) / 2;
+    if (off[mid] <= s)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const int64_t s0 = off[lo], ns = off[lo + 1] - s0;
+  const int32_t l = lloc[s], r = rloc[s];
+  if (l < -1 || r < -1 || l >= ns || r >= ns) atomicMin(bad, (unsigned long long)s);
+  left[s] = l < 0 ? -1 : (int32_t)(s0 + l);
+  right[s] = r < 0 ? -1 : (int32_t)(s0 + r);
+  site_film[s] = lo;
+  pos4[s] = make_double4_32a(pos[3 * s], pos[3 * s + 1], pos[3 * s + 2], 0.0);
+}
+
+cudaError_t launch_load_sites(int64_t n, int32_t n_films, const int64_t* offsets, const double* pos,
+                              const int32_t* left_local, const int32_t* right_local, double4_32a* pos4,
+                              int32_t* left, int32_t* right, int32_t* site_film, unsigned long long* bad_site,
+                              cudaStream_t s) {
+  const int64_t nb = (n + 255) / 256;
+  if (nb) k_load_sites<<<(unsigned)nb, 256, 0, s>>>(n, n_films, offsets, pos, left_local, right_local, pos4, left,
+                                                       right, site_film, bad_site);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pos_f32(const double4_32a* p, float4* out, int64_t n, cudaStream_t s) {
   int64_t nb = (n + 255) / 256;
   if (nb) k_pos_f32<<<(unsigned)nb, 256, 0, s>>>(p, out, n);

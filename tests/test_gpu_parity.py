@@ -241,6 +241,17 @@ def test_argument_errors():
         e.run(1, 1e-13, 2e5)
     assert ex.value.code == L.KMC_ERR_STATE
     f, tab, r_max = synthetic_case(2, n_tubes=4, length=10.0, box=(20, 20, 2))
+    bad = f.right.copy()
+    bad[3] = f.n_sites + 5  # a link outside the film: reported, the film stays unloaded
+    with pytest.raises(L.KmcError) as ex:
+        e.load_arrays(np.array([0, f.n_sites], np.int64), f.pos_m(), f.orient, f.left, bad)
+    assert ex.value.code == L.KMC_ERR_ARG and "bad link at 3" in str(ex.value)
+    e.set_table(tab)
+    with pytest.raises(L.KmcError) as ex:
+        e.build(r_max)
+    assert ex.value.code == L.KMC_ERR_STATE
+    e.close()
+    e = E.Engine(0)
     e.load_films(f)
     with pytest.raises(L.KmcError):
         e.build(r_max)  # no table yet
