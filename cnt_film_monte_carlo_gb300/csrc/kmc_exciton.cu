@@ -715,7 +715,8 @@ __global__ void __launch_bounds__(kJThreads) k_coulomb_j32(const float4* __restr
                                                            const JGeom* __restrict__ geo, double2* __restrict__ part) {
   __shared__ float4 sr[kJTile];
   __shared__ float2 sb[kJTile * NQ];
-  __shared__ double2 red[kJThreads / 32][NQ];
+  __shared__ double2 prod[kJThreads * ((NQ < 8 ? NQ : 8) + 1)];  // [donor cell][q] products of one pass (padded rows)
+  __shared__ double2 runs[kJThreads];                       // [run][q] sums of NQC rows
   const JGeom g = geo[blockIdx.y];
   const float ct = (float)g.ct, st = (float)g.st, a1 = (float)g.ash1, a2 = (float)g.ash2, zs = (float)g.zsh;
   const int i = blockIdx.x * kJThreads + threadIdx.x;
@@ -767,25 +768,36 @@ __global__ void __launch_bounds__(kJThreads) k_coulomb_j32(const float4* __restr
       hy[q] = t;
     }
   }
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  // The block's sum over its donor cells of a_p(i) S_q(i), in FP64: S_q(i) formed once per q;
+  // per donor momentum p, the products go to shared memory and are added column by column
+  // (runs of NQC rows by 128 / NQC threads, then the runs in order by NQC threads), so each
+  // thread adds a few values where a warp butterfly would add five levels on every lane (the
+  // FP64 pipe runs at 1/64 of the FP32 rate on this GPU).
+  double2 S[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) S[q] = make_double2((double)hx[q] - (double)cx_[q], (double)hy[q] - (double)cy_[q]);
+  constexpr int NQC = NQ < 8 ? NQ : 8;   // q columns per pass
+  constexpr int RUN = kJThreads / NQC;   // runs per column; each run adds NQC rows
+  const int qc = threadIdx.x % NQC, run = threadIdx.x / NQC;
   for (int p = 0; p < np; ++p) {
     const double2 a = live ? ap[(size_t)p * nd + i] : make_double2(0, 0);
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      double2 v = cmul(a, make_double2((double)hx[q] - (double)cx_[q], (double)hy[q] - (double)cy_[q]));
-      for (int o = 16; o > 0; o >>= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    for (int q0 = 0; q0 < NQ; q0 += NQC) {
+#pragma unroll
+      for (int q = 0; q < NQC; ++q) prod[threadIdx.x * (NQC + 1) + q] = cmul(a, S[q0 + q]);
+      __syncthreads();
+      double2 r = prod[(run * NQC) * (NQC + 1) + qc];
+#pragma unroll
+      for (int k = 1; k < NQC; ++k) r = cadd(r, prod[(run * NQC + k) * (NQC + 1) + qc]);
+      runs[run * NQC + qc] = r;
+      __syncthreads();
+      if (threadIdx.x < NQC && q0 + threadIdx.x < nq) {  // this block's partial, summed over blocks in order by k_j_reduce
+        double2 t = runs[threadIdx.x];
+        for (int k = 1; k < RUN; ++k) t = cadd(t, runs[k * NQC + threadIdx.x]);
+        part[(((size_t)blockIdx.y * gridDim.x + blockIdx.x) * np + p) * nq + q0 + threadIdx.x] = t;
       }
-      if (l == 0) red[w][q] = v;
+      __syncthreads();
     }
-    __syncthreads();
-    if (threadIdx.x < nq) {
-      double2 s = make_double2(0, 0);
-      for (int k = 0; k < kJThreads / 32; ++k) s = cadd(s, red[k][threadIdx.x]);
-      part[(((size_t)blockIdx.y * gridDim.x + blockIdx.x) * np + p) * nq + threadIdx.x] = s;
-    }
-    __syncthreads();
   }
 }
 
