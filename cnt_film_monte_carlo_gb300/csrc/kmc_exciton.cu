@@ -738,8 +738,11 @@ __global__ void __launch_bounds__(kJThreads) k_coulomb_j32(const float4* __restr
       const float4 r = ra[j0 + j];
       const float y = r.y + a2;
       sr[j] = make_float4(r.x * ct - y * st, r.x * st + y * ct, r.z + zs, 0.f);
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) sb[j * NQ + q] = q < nq ? bq[(size_t)q * na + j0 + j] : make_float2(0.f, 0.f);
+    }
+    // the phases [j][q], stored by consecutive threads to consecutive words (no bank conflicts)
+    for (int e = threadIdx.x; e < nt * NQ; e += kJThreads) {
+      const int j = e / NQ, q = e % NQ;
+      sb[e] = q < nq ? bq[(size_t)q * na + j0 + j] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     float ax[NQ], ay[NQ];
