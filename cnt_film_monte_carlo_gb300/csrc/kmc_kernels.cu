@@ -321,7 +321,9 @@ __global__ void k_nbr_fill(BuildArgs a) {
   a.inv_total[si] = inv;
   bool exact = negative || !(tot > 0.0) || !(tot < __longlong_as_double(0x7FF0000000000000ll));
   if (exact && k > 0) atomicAdd(&a.stats[2], 1ull);
-  // FP32 normalised values, padding, second and first search levels
+  // FP32 normalised values, padding, second and first search levels.  cum * (1/total) instead of
+  // cum / total: within 2^-52 of the quotient before the FP32 rounding (the mixed kernel's
+  // margins are 2^-20), monotone along the row, and one FP64 multiply instead of a division
   const float kInf = __int_as_float(0x7f800000);
   const int64_t nb = (k + 7) / 8;
   for (int64_t j = 0; j < nb; ++j) {
@@ -329,7 +331,7 @@ __global__ void k_nbr_fill(BuildArgs a) {
     for (int i = 0; i < 8; ++i) {
       int64_t q = 8 * j + i;
       if (q < k) {
-        blk.c[i] = exact ? 0.0f : (float)(cump[q] / tot);
+        blk.c[i] = exact ? 0.0f : (float)(cump[q] * inv);
       } else {
         blk.c[i] = kInf;
         blk.col[i] = -1;
@@ -337,7 +339,7 @@ __global__ void k_nbr_fill(BuildArgs a) {
       }
     }
     int64_t last = min(8 * j + 7, k - 1);
-    a.blast[bo + j] = exact ? 0.0f : (float)(cump[last] / tot);
+    a.blast[bo + j] = exact ? 0.0f : (float)(cump[last] * inv);
   }
   SiteRec r;
   r.inv_total = inv;
@@ -351,7 +353,7 @@ __global__ void k_nbr_fill(BuildArgs a) {
   for (int i = 0; i < 8; ++i) {
     if (i * G < nb && !exact) {
       int64_t last = min(8 * G * (i + 1) - 1, k - 1);
-      r.coarse[i] = (float)(cump[last] / tot);
+      r.coarse[i] = (float)(cump[last] * inv);
     } else {
       r.coarse[i] = kInf;
     }
