@@ -87,7 +87,7 @@ struct kmc_ctx {
   // table
   bool has_table = false;
   kmc::TableDev table{};
-  DevBuf<double> d_grid[4], d_rate, d_cut_d2, d_cut_cos;
+  DevBuf<double> d_grid[4], d_rate, d_cut[4];  // d2_above, d2_below, cos_below, cos_above
   // chirality of each site (read by KMC_TABLE_2D_SPECIES tables); 0 = not set
   int32_t n_species = 0;
   DevBuf<int32_t> d_species;
@@ -435,16 +435,27 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   // where the square and the cosine are monotonic
   if (dims == 2 && c->table.inv_h[0] > 0 && c->table.inv_h[1] > 0 && t->grid[0][0] >= 0 && t->grid[1][0] >= 0 &&
       t->grid[1][t->n[1] - 1] <= 3.141592653589793) {
-    std::vector<double> cd(t->n[0] - 1), cc(t->n[1] - 1);
+    std::vector<double> cut[4] = {std::vector<double>(t->n[0] - 1), std::vector<double>(t->n[0] - 1),
+                                  std::vector<double>(t->n[1] - 1), std::vector<double>(t->n[1] - 1)};
     for (int32_t k = 0; k + 1 < t->n[0]; ++k) {
       const double m = (t->grid[0][k] + t->grid[0][k + 1]) / 2;
-      cd[k] = m * m;
+      cut[0][k] = (m * m) * (1.0 + 1e-12);
+      cut[1][k] = (m * m) * (1.0 - 1e-12);
     }
-    for (int32_t k = 0; k + 1 < t->n[1]; ++k) cc[k] = std::cos((t->grid[1][k] + t->grid[1][k + 1]) / 2);
-    CK(c, upload(c->d_cut_d2, cd.data(), cd.size(), c->stream));
-    CK(c, upload(c->d_cut_cos, cc.data(), cc.size(), c->stream));
-    c->table.cut_d2 = c->d_cut_d2.p;
-    c->table.cut_cos = c->d_cut_cos.p;
+    for (int32_t k = 0; k + 1 < t->n[1]; ++k) {
+      const double cm = std::cos((t->grid[1][k] + t->grid[1][k + 1]) / 2);
+      cut[2][k] = cm - 1e-13;
+      cut[3][k] = cm + 1e-13;
+    }
+    for (int q = 0; q < 4; ++q) CK(c, upload(c->d_cut[q], cut[q].data(), cut[q].size(), c->stream));
+    c->table.d2_above = c->d_cut[0].p;
+    c->table.d2_below = c->d_cut[1].p;
+    c->table.cos_below = c->d_cut[2].p;
+    c->table.cos_above = c->d_cut[3].p;
+    for (int d = 0; d < 2; ++d) {
+      c->table.g0f[d] = (float)t->grid[d][0];
+      c->table.ihf[d] = (float)c->table.inv_h[d];
+    }
   }
   CK(c, cudaStreamSynchronize(c->stream));
   c->has_table = true;

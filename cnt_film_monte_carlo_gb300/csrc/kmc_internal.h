@@ -90,11 +90,17 @@ struct TableDev {
   const int32_t* species;  // kind 3: chirality of each site (reference id); pair table
                            // (species[donor], species[acceptor]) of n[2] x n[2]
   // 2-D tables (kinds 2, 3) with ascending grids: the squared distances between neighbouring
-  // distance-grid points (cut_d2[k] = ((g_k + g_k+1) / 2)^2, ascending) and the cosines of the
-  // midpoints of the angle grid (cut_cos[k] = cos((g_k + g_k+1) / 2), descending); nullptr when
-  // the grids do not allow it (the lookup then always takes the exact path)
-  const double* cut_d2;
-  const double* cut_cos;
+  // distance-grid points (m_k^2, m_k = (g_k + g_k+1) / 2, ascending) and the cosines of the
+  // midpoints of the angle grid (cos m_k, descending), each with the lookup's safety margin
+  // applied on the host: d2_above[k] = m_k^2 (1 + 1e-12), d2_below[k] = m_k^2 (1 - 1e-12),
+  // cos_below[k] = cos m_k - 1e-13, cos_above[k] = cos m_k + 1e-13; nullptr when the grids do
+  // not allow it (the lookup then always takes the exact path).  g0f, ihf: the first grid points
+  // and inverse spacings of both grids in FP32 (the index estimate).
+  const double* d2_above;
+  const double* d2_below;
+  const double* cos_below;
+  const double* cos_above;
+  float g0f[2], ihf[2];
 };
 
 // Exciton flags

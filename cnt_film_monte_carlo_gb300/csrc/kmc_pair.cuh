@@ -84,15 +84,14 @@ __device__ __forceinline__ double pair_rate_2d(const TableDev& t, const double* 
   const double d2 = dot3(dR0, dR1, dR2, dR0, dR1, dR2);
   const double cosT = dot3(a1v[0], a1v[1], a1v[2], a2v[0], a2v[1], a2v[2]);
   const double ac = fabs(cosT);
-  if (t.cut_d2 && t.cut_cos && ac <= 1.0) {
+  if (t.d2_above && ac <= 1.0) {
     const int n0 = t.n[0], n1 = t.n[1];
-    int c0 = (int)floorf(((float)sqrt((float)d2) - (float)t.grid[0][0]) * (float)t.inv_h[0] + 0.5f);
+    int c0 = (int)floorf(((float)sqrt((float)d2) - t.g0f[0]) * t.ihf[0] + 0.5f);
     c0 = c0 < 0 ? 0 : (c0 > n0 - 1 ? n0 - 1 : c0);
-    int c1 = (int)floorf((acosf((float)ac) - (float)t.grid[1][0]) * (float)t.inv_h[1] + 0.5f);
+    int c1 = (int)floorf((acosf((float)ac) - t.g0f[1]) * t.ihf[1] + 0.5f);
     c1 = c1 < 0 ? 0 : (c1 > n1 - 1 ? n1 - 1 : c1);
-    const bool ok0 = (c0 == 0 || d2 > t.cut_d2[c0 - 1] * (1.0 + 1e-12)) &&
-                     (c0 == n0 - 1 || d2 < t.cut_d2[c0] * (1.0 - 1e-12));
-    const bool ok1 = (c1 == 0 || ac < t.cut_cos[c1 - 1] - 1e-13) && (c1 == n1 - 1 || ac > t.cut_cos[c1] + 1e-13);
+    const bool ok0 = (c0 == 0 || d2 > t.d2_above[c0 - 1]) && (c0 == n0 - 1 || d2 < t.d2_below[c0]);
+    const bool ok1 = (c1 == 0 || ac < t.cos_below[c1 - 1]) && (c1 == n1 - 1 || ac > t.cos_above[c1]);
     if (ok0 && ok1) return t.rate[pair_off + (int64_t)c0 * n1 + c1];
   }
   return pair_rate_2d_exact(t, a1v, a2v, dR0, dR1, dR2, d2, pair_off, p1, p2);
