@@ -88,6 +88,7 @@ struct kmc_ctx {
   bool has_table = false;
   kmc::TableDev table{};
   DevBuf<double> d_grid[4], d_rate, d_cut[4];  // d2_above, d2_below, cos_below, cos_above
+  std::vector<double> h_cut[4];                 // host copies of d_cut (the FP32 lookup's bounds)
   // chirality of each site (read by KMC_TABLE_2D_SPECIES tables); 0 = not set
   int32_t n_species = 0;
   DevBuf<int32_t> d_species;
@@ -430,6 +431,7 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   if (t->kind == KMC_TABLE_2D_SPECIES) c->table.n[2] = t->n[2];
   CK(c, upload(c->d_rate, t->rate, nr, c->stream));
   c->table.rate = c->d_rate.p;
+  for (auto& v : c->h_cut) v.clear();
   // 2-D tables: grid midpoints for the neighbour build's lookup without sqrt and arccosine
   // (pair_rate_2d); the distance grid must be non-negative and the angle grid inside [0, pi],
   // where the square and the cosine are monotonic
@@ -447,7 +449,10 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
       cut[2][k] = cm - 1e-13;
       cut[3][k] = cm + 1e-13;
     }
-    for (int q = 0; q < 4; ++q) CK(c, upload(c->d_cut[q], cut[q].data(), cut[q].size(), c->stream));
+    for (int q = 0; q < 4; ++q) {
+      CK(c, upload(c->d_cut[q], cut[q].data(), cut[q].size(), c->stream));
+      c->h_cut[q] = cut[q];
+    }
     c->table.d2_above = c->d_cut[0].p;
     c->table.d2_below = c->d_cut[1].p;
     c->table.cos_below = c->d_cut[2].p;
@@ -567,6 +572,42 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
   a.n_films = c->n_films;
   a.pos4f = c->d_pos4f.p;
   a.scr = pair_screen(r_max, max_coord);
+  // The FP32 table lookup of the fill pass: the 2-D lookup's bounds widened by the largest FP32
+  // error of a pair's squared distance and of its |cos theta|, then rounded outward to FP32.
+  // With u = 2^-24 and M the largest coordinate magnitude, a component of dR formed from FP32
+  // positions is off by at most d = 2uM + u r + 2u^2 M, so the sum of squares by at most
+  // d (2 sqrt(3) r + 3 d), and its three FP32 roundings add 3.01u (r + d)^2; taken 1.5 times.
+  // |cos theta| from FP32 unit vectors: at most 5.1u (two roundings of the components, three
+  // of the products and sums), taken as 1e-6.
+  DevBuf<float4> d_orient4f;
+  DevBuf<float> d_cutf[4];
+  if (c->table.d2_above && !c->h_cut[0].empty()) {
+    const double u = std::ldexp(1.0, -24);
+    const double d = 2 * u * max_coord + u * r_max + 2 * u * u * max_coord;
+    const double eps_d2 = 1.5 * (d * (2 * std::sqrt(3.0) * r_max + 3 * d) + 3.01 * u * (r_max + d) * (r_max + d));
+    const double eps_c = 1e-6;
+    auto up = [](double v) {
+      float f = (float)v;
+      return (double)f < v ? std::nextafterf(f, INFINITY) : f;
+    };
+    auto dn = [](double v) {
+      float f = (float)v;
+      return (double)f > v ? std::nextafterf(f, -INFINITY) : f;
+    };
+    std::vector<float> cf[4];
+    for (double v : c->h_cut[0]) cf[0].push_back(up(v + eps_d2));
+    for (double v : c->h_cut[1]) cf[1].push_back(dn(v - eps_d2));
+    for (double v : c->h_cut[2]) cf[2].push_back(dn(v - eps_c));
+    for (double v : c->h_cut[3]) cf[3].push_back(up(v + eps_c));
+    for (int q = 0; q < 4; ++q) CK(c, upload(d_cutf[q], cf[q].data(), cf[q].size(), c->stream));
+    CK(c, d_orient4f.alloc(n));
+    CK(c, kmc::launch_orient_f32(c->d_orient.p, d_orient4f.p, n, c->stream));
+    a.orient4f = d_orient4f.p;
+    a.d2_above_f = d_cutf[0].p;
+    a.d2_below_f = d_cutf[1].p;
+    a.cos_below_f = d_cutf[2].p;
+    a.cos_above_f = d_cutf[3].p;
+  }
   a.win_lo2 = sqrt_bound(kmc::kMinHopDist, false);  // d2 > win_lo2  <=>  sqrt(d2) > kMinHopDist
   a.win_hi2 = sqrt_bound(r_max, true);              // d2 < win_hi2  <=>  sqrt(d2) < r_max
   a.perm = c->d_perm.p;

@@ -166,6 +166,15 @@ struct BuildArgs {
   const double4_32a* pos4;
   const float4* pos4f;     // FP32 copy of pos4
   PairScreen scr;
+  // 2-D tables: the lookup's bounds widened by the worst FP32 error of a pair's squared distance
+  // (from pos4f) and of its |cos theta| (from orient4f), rounded outward to FP32, so that an FP32
+  // pair inside its cell's bounds is surely where the FP64 lookup puts it.  nullptr: no FP32
+  // lookup.
+  const float4* orient4f;  // FP32 copy of orient (x, y, z, 0)
+  const float* d2_above_f;
+  const float* d2_below_f;
+  const float* cos_below_f;
+  const float* cos_above_f;
   // find_neighbors' window kMinHopDist < sqrt(d2) < r_max (FP64 root, scatterer.cpp:43) as
   // d2 > win_lo2 && d2 < win_hi2: the root is correctly rounded and monotone, so these squared
   // bounds (found on the host) give the same answer for every double d2 without a root
@@ -204,6 +213,7 @@ struct BuildArgs {
 
 // launchers (kmc_kernels.cu); all return cudaError_t of the launch
 cudaError_t launch_pos_f32(const double4_32a* p, float4* out, int64_t n, cudaStream_t s);
+cudaError_t launch_orient_f32(const double* orient, float4* out, int64_t n, cudaStream_t s);  // [n][3] -> float4
 // The loaded films' sites on the device: positions [n][3] -> pos4, film-local links -> global
 // links, the film of every site (offsets[n_films + 1]).  A link outside its film sets *bad_site
 // to the smallest such site index (initialised to INT64_MAX by the caller).

@@ -72,6 +72,18 @@ __global__ void k_pos_f32(const double4_32a* __restrict__ p, float4* __restrict_
   out[s] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
 }
 
+__global__ void k_orient_f32(const double* __restrict__ o, float4* __restrict__ out, int64_t n) {
+  int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  out[s] = make_float4((float)o[3 * s], (float)o[3 * s + 1], (float)o[3 * s + 2], 0.f);
+}
+
+cudaError_t launch_orient_f32(const double* orient, float4* out, int64_t n, cudaStream_t s) {
+  const int64_t nb = (n + 255) / 256;
+  if (nb) k_orient_f32<<<(unsigned)nb, 256, 0, s>>>(orient, out, n);
+  return cudaGetLastError();
+}
+
 __global__ void k_load_sites(int64_t n, int32_t n_films, const int64_t* __restrict__ off, const double* __restrict__ pos,
                              const int32_t* __restrict__ lloc, const int32_t* __restrict__ rloc, double4_32a* pos4,
                              int32_t* left, int32_t* right, int32_t* site_film, unsigned long long* bad) {
@@ -296,24 +308,65 @@ __global__ void k_nbr_fill(BuildArgs a) {
     a.blocks[bo + (k >> 3)].col[k & 7] = q;
     ++k;
   });
-  double run = 0.0;
-  bool negative = false;
-  for (int64_t j = 0; j < k; ++j) {
+  // Pass 1: every entry's rate into its cump slot.  With the FP32 lookup (2-D tables), a pair
+  // clear of its cell's widened bounds takes the entry the FP64 lookup would take, without FP64
+  // work; the few others are listed for pass 2, so that a warp runs the FP64 lookup a few times
+  // per row instead of on every entry some lane could not decide.
+  const bool f32 = a.d2_above_f != nullptr;
+  constexpr int kUndecided = 8;
+  int32_t undecided[kUndecided];
+  int n_und = 0;
+  bool all = !f32;  // FP64 for every entry (no FP32 lookup, or the list overflowed)
+  if (f32) {
+    const float4 p1f = a.pos4f[s], o1f = a.orient4f[s];
+    const int n0 = a.table.n[0], n1 = a.table.n[1];
+    for (int64_t j = 0; j < k; ++j) {
+      const int32_t q = a.blocks[bo + (j >> 3)].col[j & 7];
+      const float4 p2f = a.pos4f[q], o2f = a.orient4f[q];
+      const float fx = p1f.x - p2f.x, fy = p1f.y - p2f.y, fz = p1f.z - p2f.z;
+      const float d2f = fx * fx + fy * fy + fz * fz;
+      const float acf = fabsf(o1f.x * o2f.x + o1f.y * o2f.y + o1f.z * o2f.z);
+      int c0 = (int)floorf((sqrtf(d2f) - a.table.g0f[0]) * a.table.ihf[0] + 0.5f);
+      c0 = c0 < 0 ? 0 : (c0 > n0 - 1 ? n0 - 1 : c0);
+      int c1 = (int)floorf((acosf(fminf(acf, 1.f)) - a.table.g0f[1]) * a.table.ihf[1] + 0.5f);
+      c1 = c1 < 0 ? 0 : (c1 > n1 - 1 ? n1 - 1 : c1);
+      // |cos theta| above the first angle bound: angle index 0 on both FP64 paths (the fast one,
+      // and the exact one that parallel pairs with |cos| > 1 by rounding take)
+      if ((c0 == 0 || d2f > a.d2_above_f[c0 - 1]) && (c0 == n0 - 1 || d2f < a.d2_below_f[c0]) &&
+          (c1 == 0 || acf < a.cos_below_f[c1 - 1]) && (c1 == n1 - 1 || acf > a.cos_above_f[c1])) {
+        cump[j] = a.table.rate[pair_table(a.table, s, q) + (int64_t)c0 * n1 + c1];
+      } else if (n_und < kUndecided) {
+        undecided[n_und++] = (int32_t)j;
+      } else {
+        all = true;
+      }
+    }
+  }
+  // Pass 2: the FP64 lookup (pair geometry in the reference's operations) for the listed
+  // entries, or for every entry
+  const int64_t n2 = all ? k : n_und;
+  for (int64_t t = 0; t < n2; ++t) {
+    const int64_t j = all ? t : undecided[t];
     const int32_t q = a.blocks[bo + (j >> 3)].col[j & 7];
     const double4_32a p2 = a.pos4[q];
     const double dR0 = p1.x - p2.x, dR1 = p1.y - p2.y, dR2 = p1.z - p2.z;
     double a2v[3] = {a.orient[3 * (int64_t)q], a.orient[3 * (int64_t)q + 1], a.orient[3 * (int64_t)q + 2]};
-    double rate;
     if (a.table.kind != 4) {
-      rate = pair_rate_2d(a.table, a1v, a2v, dR0, dR1, dR2, pair_table(a.table, s, q), p1, p2);
+      cump[j] = pair_rate_2d(a.table, a1v, a2v, dR0, dR1, dR2, pair_table(a.table, s, q), p1, p2);
     } else {
       const double distance = norm3(dR0, dR1, dR2);
-      rate = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance, pair_table(a.table, s, q));
+      cump[j] = pair_rate(a.table, p1, a1v, p2, a2v, dR0, dR1, dR2, distance, pair_table(a.table, s, q));
     }
+  }
+  // Pass 3: the running sum in list order (scatterer.cpp:78-80) and the neighbours as storage slots
+  double run = 0.0;
+  bool negative = false;
+  for (int64_t j = 0; j < k; ++j) {
+    const double rate = cump[j];
     negative |= rate < 0;
-    run = (j == 0) ? rate : run + rate;  // in-place inclusive prefix sum, scatterer.cpp:78-80
+    run = (j == 0) ? rate : run + rate;
     cump[j] = run;
-    a.blocks[bo + (j >> 3)].col[j & 7] = a.rank[q];
+    a.blocks[bo + (j >> 3)].col[j & 7] = a.rank[a.blocks[bo + (j >> 3)].col[j & 7]];
   }
   double tot = k > 0 ? run : 0.0;
   double inv = 1. / tot;
