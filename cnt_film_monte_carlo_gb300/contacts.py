@@ -91,3 +91,56 @@ def current_row(time: float, counts, area, dt: float) -> str:
 def track_text(path) -> str:
     """particle_path.<n>.dat: "   x y z" per step (scientific, showpos), then an empty line."""
     return "".join(f"   {_e(float(x), True)} {_e(float(y), True)} {_e(float(z), True)}\n" for x, y, z in path) + "\n"
+
+
+# ---------------------------------------------------------------- flux-gradient diffusion coefficient
+def _csv_rows(text: str):
+    return [line.split(",") for line in text.splitlines()]
+
+
+def read_population(text: str) -> dict:
+    """population_profile.dat as the reference's get_population reads it
+    (visualization/monte_carlo_results.py:70-109, without its low-pass filter, which only the
+    plots use): area, dy and section positions from the header rows, the densities per step,
+    and their average over the steps."""
+    rows = _csv_rows(text)
+    area = np.array([float(v) for v in rows[0][1:]])
+    dy = np.array([float(v) for v in rows[2][1:]])
+    pos = np.array([float(v) for v in rows[4][1:]])
+    data = np.array([[float(v) for v in r] for r in rows[7:] if r and r[0]])
+    pop = data[:, 1:]
+    return {"time": data[:, 0], "pop": pop, "area": area, "dy": dy, "pos": pos, "avg_pop": pop.mean(axis=0)}
+
+
+def read_current(text: str) -> dict:
+    """region_current.dat as the reference's get_current reads it (monte_carlo_results.py:31-68,
+    without the filter): interface areas and positions, the current per step and its average over
+    the steps (the steady current)."""
+    rows = _csv_rows(text)
+    area = np.array([float(v) for v in rows[0][1:]])
+    pos = np.array([float(v) for v in rows[2][1:]])
+    data = np.array([[float(v) for v in r] for r in rows[5:] if r and r[0]])
+    cur = data[:, 1:]
+    return {"time": data[:, 0], "current": cur, "area": area, "pos": pos, "steady": cur.mean(axis=0)}
+
+
+def flux_gradient_diffusion(population: dict, current: dict) -> np.ndarray:
+    """The contacts mode's diffusion coefficient at every slab interface, as the reference's
+    post-processing forms it (monte_carlo_results.py:428-442): the steady current over the
+    gradient of the average density, D_k = steady_k / ((avg_pop[k+1] - avg_pop[k]) / dy[k]).
+    A current down the gradient gives a negative value, as there."""
+    dp_dy = np.diff(population["avg_pop"]) / population["dy"][:-1]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return current["steady"] / dp_dy
+
+
+def flux_gradient_diffusion_from_counts(population_counts, current_counts, area, dy: float, dt: float) -> np.ndarray:
+    """The same coefficient from the engine's counts ([steps][n_segments] excitons per slab,
+    [steps][n_segments - 1] net crossings per interface) instead of the files' rounded values."""
+    pc = np.asarray(population_counts, dtype=np.float64)
+    cc = np.asarray(current_counts, dtype=np.float64)
+    area = np.asarray(area, dtype=np.float64)
+    avg_pop = (pc / (area * dy)).mean(axis=0)
+    steady = (cc / (interface_areas(area) * dt)).mean(axis=0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return steady / (np.diff(avg_pop) / dy)

@@ -174,6 +174,13 @@ class monte_carlo {
       for (int32_t i = 1; i < n; ++i) std::fprintf(cur_f_, ",interface%+d", i - 1);
       std::fprintf(cur_f_, "\n");
     }
+    if (pop_sum_.size() != (size_t)n) {
+      pop_sum_.assign((size_t)n, 0);
+      cur_sum_.assign((size_t)n - 1, 0);
+    }
+    for (int32_t i = 0; i < n; ++i) pop_sum_[i] += pop_[i];
+    for (int32_t i = 0; i + 1 < n; ++i) cur_sum_[i] += cur_[i];
+    ++metric_rows_;
     std::fprintf(pop_f_, "%+e", time_);
     for (int32_t i = 0; i < n; ++i) std::fprintf(pop_f_, ",%+e", double(pop_[i]) / (area_[i] * dy));
     std::fprintf(pop_f_, "\n");
@@ -355,7 +362,19 @@ class monte_carlo {
       }
       std::fprintf(f, "]");
     } else {
-      std::fprintf(f, ",\n  \"live excitons\": %lld", (long long)live_);
+      // the flux-gradient D of every slab interface (visualization/monte_carlo_results.py:428-442):
+      // steady current over the gradient of the average density, both averaged over the rows of
+      // the output files, here from their exact counts
+      std::fprintf(f, ",\n  \"live excitons\": %lld,\n  \"flux-gradient D [m^2/s]\": [", (long long)live_);
+      const double dy = cinfo_.dy;
+      for (int32_t k = 0; k + 1 < n_seg_ && metric_rows_ > 0; ++k) {
+        const double rows = double(metric_rows_);
+        const double p0 = double(pop_sum_[k]) / rows / (area_[k] * dy), p1 = double(pop_sum_[k + 1]) / rows / (area_[k + 1] * dy);
+        const double steady = double(cur_sum_[k]) / rows / (((area_[k] + area_[k + 1]) / 2) * dt_);
+        if (k) std::fprintf(f, ", ");
+        num(steady / ((p1 - p0) / dy));
+      }
+      std::fprintf(f, "]");
     }
     std::fprintf(f, "\n}\n");
     std::fclose(f);
@@ -552,6 +571,8 @@ class monte_carlo {
   kmc_contacts_info cinfo_{};
   std::vector<double> area_;
   std::vector<int64_t> pop_, cur_;
+  std::vector<long long> pop_sum_, cur_sum_;  // the counts summed over the metric rows written
+  int64_t metric_rows_ = 0;
   int64_t live_ = 0;
   std::FILE *pop_f_ = nullptr, *cur_f_ = nullptr;
 };

@@ -162,6 +162,8 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
                                                        int(self._nbr_stats["n_sites"]), g["area"]))
         self._pop_file = self._cur_file = None
         self._last = None
+        self._pop_sum = self._cur_sum = None
+        self._metric_rows = 0
 
     def track_particle(self, dt: float, file_no: int):
         """track_particle (monte_carlo.h:786-818): particle_path.<file_no>.dat."""
@@ -205,6 +207,9 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
             self._pop_file.write(contacts.population_header(g["area"], g["ymin"], g["dy"]))
             self._cur_file.write(contacts.current_header(g["area"], g["ymin"], g["dy"]))
         pop, cur, _ = self._last
+        self._pop_sum = self._pop_sum + np.asarray(pop, np.int64) if self._pop_sum is not None else np.asarray(pop, np.int64)
+        self._cur_sum = self._cur_sum + np.asarray(cur, np.int64) if self._cur_sum is not None else np.asarray(cur, np.int64)
+        self._metric_rows += 1
         self._pop_file.write(contacts.population_row(self._time, pop, g["area"], g["dy"]))
         self._cur_file.write(contacts.current_row(self._time, cur, g["area"], dt))
         self._pop_file.flush()
@@ -339,6 +344,14 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
                       "diffusion 95% interval [m^2/s]": ci})
         else:
             r["live excitons"] = int(self._last[2]) if self._last is not None else int(self._n_particles)
+            D = []
+            if self._metric_rows:  # the flux-gradient D per interface (monte_carlo_results.py:428-442)
+                g = self._contacts
+                D = contacts.flux_gradient_diffusion_from_counts(
+                    (self._pop_sum / self._metric_rows)[None, :], (self._cur_sum / self._metric_rows)[None, :],
+                    g["area"], g["dy"], self._dt)
+                D = [fin(float(v)) for v in D]
+            r["flux-gradient D [m^2/s]"] = D
         return r
 
     def write_run_report(self, wall_seconds: float) -> dict:

@@ -115,3 +115,29 @@ def test_oracle_contacts_per_hop_search_equals_csr():
     a, b = sim_a.excitons(), sim_b.excitons()
     for k in ("site", "ff", "draws", "hops"):
         assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("name", CONTACT_CASES)
+def test_flux_gradient_diffusion_from_reference_files(name):
+    # the contacts mode's D per interface as the reference's post-processing forms it
+    # (visualization/monte_carlo_results.py:428-442) from the reference's own output files, against
+    # the same formula on the exact counts (the files hold 7 significant digits)
+    d = load_case(name)
+    c = contacts_inputs(d)
+    n = c["n_seg"]
+    ymin, ymax = c["pos"][:, 1].min(), c["pos"][:, 1].max()
+    dy = (ymax - ymin) / float(n)
+    p = CF.read_population(bytes(d["file_population_profile"]).decode())
+    cur = CF.read_current(bytes(d["file_region_current"]).decode())
+    assert p["pop"].shape == (len(d["ref_time"]), n) and cur["current"].shape == (len(d["ref_time"]), n - 1)
+    np.testing.assert_allclose(p["area"], d["ref_area"], rtol=1e-6)
+    np.testing.assert_allclose(p["dy"], dy, rtol=1e-6)
+    # the reference's own steps restated: averages over the steps, then steady / (diff(avg) / dy)
+    want = cur["current"].mean(axis=0) / (np.diff(p["pop"].mean(axis=0)) / p["dy"][:-1])
+    got = CF.flux_gradient_diffusion(p, cur)
+    np.testing.assert_array_equal(got, want)
+    exact = CF.flux_gradient_diffusion_from_counts(d["ref_pop"].reshape(-1, n), d["ref_curr"].reshape(-1, n - 1),
+                                                   d["ref_area"], dy, c["dt"])
+    fin = np.isfinite(exact) & np.isfinite(got)
+    assert fin.any()
+    np.testing.assert_allclose(got[fin], exact[fin], rtol=1e-5)

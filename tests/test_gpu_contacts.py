@@ -18,6 +18,7 @@ import numpy as np
 import pytest
 
 from cnt_film_monte_carlo_gb300 import _lib as L
+from cnt_film_monte_carlo_gb300 import contacts as CF
 from cnt_film_monte_carlo_gb300 import build as B
 from cnt_film_monte_carlo_gb300 import engine as E
 from cnt_film_monte_carlo_gb300 import film as F
@@ -210,6 +211,24 @@ def _check_files(out_dir, d):
         assert got[k:len(want)] == want[k:], fn
 
 
+def _check_report(out_dir):
+    # run_report.json: the flux-gradient D of every interface from the counts equals the reference's
+    # post-processing of the written files (7 significant digits)
+    with open(os.path.join(out_dir, "run_report.json")) as f:
+        rep = json.load(f)
+    assert rep["mode"] == "contacts" and rep["hops"] > 0
+    with open(os.path.join(out_dir, "population_profile.dat")) as f:
+        p = CF.read_population(f.read())
+    with open(os.path.join(out_dir, "region_current.dat")) as f:
+        c = CF.read_current(f.read())
+    want = CF.flux_gradient_diffusion(p, c)
+    got = np.array([np.nan if v is None else v for v in rep["flux-gradient D [m^2/s]"]], dtype=float)
+    assert got.shape == want.shape
+    fin = np.isfinite(want)
+    assert np.array_equal(np.isfinite(got), fin)
+    np.testing.assert_allclose(got[fin], want[fin], rtol=1e-5)
+
+
 @pytest.mark.parametrize("name", CONTACT_CASES)
 def test_driver_writes_reference_contacts_files(name, tmp_path):
     d = load_case(name)
@@ -218,6 +237,7 @@ def test_driver_writes_reference_contacts_files(name, tmp_path):
     r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     _check_files(os.path.join(str(tmp_path), "out"), d)
+    _check_report(os.path.join(str(tmp_path), "out"))
 
 
 @pytest.mark.parametrize("name", CONTACT_CASES)
@@ -226,6 +246,7 @@ def test_python_class_writes_reference_contacts_files(name, tmp_path):
     cfg = _contacts_json(d, str(tmp_path))
     out = MC.run(cfg)
     _check_files(out, d)
+    _check_report(out)
 
 
 def test_contacts_run_in_pieces_and_reinit():
