@@ -52,7 +52,7 @@ __device__ __forceinline__ float gelu(float z, float& t) {
 }
 // The training kernel's GELU: tanh(u) = 1 - 2 / (1 + e^(2u)) with the hardware exponential and
 // division (u clamped to [-9, 9], where tanh is +-1 in FP32), ~5e-7 absolute against tanhf; the
-// outputs the network is judged by (k_mlp_predict, k_mlp_table) use tanhf.
+// network's outputs (k_mlp_predict, k_mlp_table) use tanhf.
 __device__ __forceinline__ float gelu_train(float z, float& t) {
   const float u = fminf(fmaxf(kGeluK0 * (z + kGeluK1 * z * z * z), -9.f), 9.f);
   t = 1.f - __fdividef(2.f, 1.f + __expf(2.f * u));
