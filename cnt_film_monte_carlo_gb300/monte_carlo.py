@@ -34,7 +34,9 @@ from .engine import Engine, read_mesh, trim_sites
 
 
 def _expand(path: str) -> str:
-    return os.path.expanduser(path) if path.startswith("~") else path
+    """A leading '~' is replaced by $HOME, nothing more (prepare_directory.hpp:12-16, 75-79):
+    "~/out" is $HOME/out and "~out" is $HOMEout, not another user's home."""
+    return os.environ.get("HOME", "") + path[1:] if path.startswith("~") else path
 
 
 def prepare_directory(path: str, keep_old_files: bool = True) -> str:
