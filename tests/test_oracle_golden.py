@@ -69,7 +69,7 @@ def test_green_kubo_run(case, use_csr):
 def test_live_reference_matches_oracle(tmp_path):
     """A fresh seed against the reference run right now (needs the reference sources)."""
     if not os.path.exists(O.REF_BIN):
-        pytest.skip("oracle/_ref not built (reference sources absent)")
+        pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
     import json
 
     from cnt_film_monte_carlo_gb300 import film as F
