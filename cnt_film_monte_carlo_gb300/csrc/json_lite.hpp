@@ -1,8 +1,14 @@
 // json_lite.hpp -- a small JSON reader/writer for the drop-in driver's input.json.
 // Supports objects, arrays, numbers, strings (with \" \\ \/ \b \f \n \r \t \uXXXX escapes, the
-// last decoded to UTF-8), true/false/null.  Object key order is kept for writing the file back;
-// strings are written with quote, backslash and control characters escaped.
+// last decoded to UTF-8), true/false/null, and refuses what RFC 8259 does not allow (as the
+// reference's nlohmann::json reader does): numbers outside the JSON grammar (nan, inf, hex, a
+// leading '+' or zero, a bare '.'), other escapes, raw control characters and unpaired
+// surrogates in strings.  Object key order is kept for writing the file back; a number read from
+// text is written back as that text (so integers stay integers and 0.1 stays 0.1); strings are
+// written with quote, backslash and control characters escaped.
 #pragma once
+#include <charconv>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <map>
@@ -19,6 +25,7 @@ struct Value {
   enum Kind { Null, Bool, Number, String, Array, Object } kind = Null;
   bool b = false;
   double num = 0;
+  std::string lit;  // a number's text as read (empty for numbers made in code)
   std::string str;
   std::vector<Value> arr;
   std::vector<std::pair<std::string, Value>> obj;
@@ -116,14 +123,36 @@ class Parser {
     } else if (s_.compare(i_, 4, "null") == 0) {
       i_ += 4;
     } else {
-      const char* p = s_.c_str() + i_;
-      char* e;
-      v.num = std::strtod(p, &e);
-      if (e == p) fail("value expected");
-      v.kind = Value::Number;
-      i_ += (size_t)(e - p);
+      number(v);
     }
     return v;
+  }
+  bool digit_at(size_t j) const { return j < s_.size() && s_[j] >= '0' && s_[j] <= '9'; }
+  // -?(0|[1-9][0-9]*)(.[0-9]+)?([eE][+-]?[0-9]+)?, converted by strtod (C locale)
+  void number(Value& v) {
+    size_t j = i_;
+    if (j < s_.size() && s_[j] == '-') ++j;
+    if (!digit_at(j)) fail("value expected");
+    if (s_[j] == '0') {
+      ++j;
+    } else {
+      while (digit_at(j)) ++j;
+    }
+    if (j < s_.size() && s_[j] == '.') {
+      ++j;
+      if (!digit_at(j)) fail("digit expected after '.'");
+      while (digit_at(j)) ++j;
+    }
+    if (j < s_.size() && (s_[j] == 'e' || s_[j] == 'E')) {
+      ++j;
+      if (j < s_.size() && (s_[j] == '+' || s_[j] == '-')) ++j;
+      if (!digit_at(j)) fail("digit expected in exponent");
+      while (digit_at(j)) ++j;
+    }
+    v.lit = s_.substr(i_, j - i_);
+    v.num = std::strtod(v.lit.c_str(), nullptr);
+    v.kind = Value::Number;
+    i_ = j;
   }
   uint32_t hex4() {
     if (i_ + 4 > s_.size()) fail("bad \\u escape");
@@ -166,6 +195,7 @@ class Parser {
     std::string out;
     while (i_ < s_.size() && s_[i_] != '"') {
       char c = s_[i_++];
+      if ((unsigned char)c < 0x20) fail("control character in string");
       if (c == '\\') {
         if (i_ >= s_.size()) fail("bad escape");
         char e = s_[i_++];
@@ -175,9 +205,14 @@ class Parser {
           case 'r': out += '\r'; break;
           case 'b': out += '\b'; break;
           case 'f': out += '\f'; break;
+          case '"':
+          case '\\':
+          case '/': out += e; break;
           case 'u': {
             uint32_t cp = hex4();
-            if (cp >= 0xD800 && cp < 0xDC00 && s_.compare(i_, 2, "\\u") == 0) {  // surrogate pair
+            if (cp >= 0xDC00 && cp < 0xE000) fail("unpaired surrogate");
+            if (cp >= 0xD800 && cp < 0xDC00) {  // must be the first half of a surrogate pair
+              if (s_.compare(i_, 2, "\\u") != 0) fail("unpaired surrogate");
               i_ += 2;
               const uint32_t lo = hex4();
               if (lo < 0xDC00 || lo >= 0xE000) fail("bad surrogate pair");
@@ -186,7 +221,7 @@ class Parser {
             utf8(out, cp);
             break;
           }
-          default: out += e;
+          default: fail("bad escape");
         }
       } else {
         out += c;
@@ -230,10 +265,21 @@ inline void write(std::ostream& o, const Value& v, int indent = 0) {
     case Value::Null: o << "null"; break;
     case Value::Bool: o << (v.b ? "true" : "false"); break;
     case Value::Number: {
-      std::ostringstream t;
-      t.precision(17);
-      t << v.num;
-      o << t.str();
+      if (!v.lit.empty()) {
+        o << v.lit;
+        break;
+      }
+      // made in code: the shortest text that reads back as the same double, kept a float
+      // literal ("2.0", not "2"); JSON has no infinities or NaNs
+      if (!std::isfinite(v.num)) {
+        o << "null";
+        break;
+      }
+      char buf[64];
+      const auto r = std::to_chars(buf, buf + sizeof buf, v.num);
+      std::string t(buf, r.ptr);
+      if (t.find_first_of(".e") == std::string::npos) t += ".0";
+      o << t;
       break;
     }
     case Value::String: write_string(o, v.str); break;

@@ -36,6 +36,10 @@ BAD = [
     '"\\u12"',
     '"\\ud83d\\u0041"',
     "nul",
+    # numbers outside the JSON grammar
+    "nan", "NaN", "inf", "-Infinity", "-", "01", "-01", "+1", ".5", "1.", "1e", "1e+", "0x10", "1.5.2",
+    # escapes and characters JSON strings do not allow
+    '"\\q"', '"\\x41"', '"\\ud83d"', '"\\ud83d x"', '"\\udc00"', '"a\x01b"', '"tab\there"',
 ]
 
 
@@ -76,8 +80,47 @@ def test_numbers_exact(roundtrip, tmp_path):
     assert json.loads(r.stdout) == vals
 
 
+def test_numbers_keep_their_text(roundtrip, tmp_path):
+    """A number is written back as it was read: integers stay integers, floats stay floats (0.0,
+    2.0, 1e-15 and -0.0 are not turned into 0, 2 or 1.0000000000000001e-15), and integers past
+    2^53 keep every digit."""
+    text = "[0, 0.0, -0.0, 2.0, 1e-15, 1E+3, 0.1, 12345678901234567890, -7]"
+    r = run(roundtrip, tmp_path, text)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.decode().strip() == text
+    back = json.loads(r.stdout)
+    assert [type(x) for x in back] == [int, float, float, float, float, float, float, int, int]
+    assert back[7] == 12345678901234567890
+
+
 @pytest.mark.parametrize("text", BAD, ids=range(len(BAD)))
 def test_malformed_refused(roundtrip, tmp_path, text):
     r = run(roundtrip, tmp_path, text)
     assert r.returncode == 2, (text, r.stdout, r.stderr)
     assert b"json:" in r.stderr
+
+
+def test_random_documents_round_trip(roundtrip, tmp_path_factory):
+    """Random JSON documents (nested objects and arrays, unicode strings with escapes, finite
+    doubles including subnormals and -0.0, integers up to 2^53) read back equal after one pass
+    through the C++ reader and writer."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    d = tmp_path_factory.mktemp("jl_random")
+    text_st = st.text(st.characters(exclude_categories=("Cs",)), max_size=12)
+    scalars = (st.none() | st.booleans() | st.integers(-(2**53), 2**53)
+               | st.floats(allow_nan=False, allow_infinity=False) | text_st)
+    docs = st.recursive(scalars, lambda c: st.lists(c, max_size=5) | st.dictionaries(text_st, c, max_size=5),
+                        max_leaves=25)
+
+    @hyp.settings(max_examples=150, deadline=None, database=None)
+    @hyp.given(docs)
+    def check(value):
+        text = json.dumps(value, ensure_ascii=False)
+        r = run(roundtrip, d, text)
+        assert r.returncode == 0, (text, r.stderr)
+        back = json.loads(r.stdout.decode("utf-8"))
+        assert back == value
+        assert json.dumps(back, sort_keys=True) == json.dumps(value, sort_keys=True)  # -0.0 and key sets
+
+    check()
