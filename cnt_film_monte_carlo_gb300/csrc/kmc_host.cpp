@@ -1,6 +1,7 @@
 // kmc_host.cpp -- host-side reference algorithms of the C ABI (no device code).
 // Compiled with -ffp-contract=off so every expression rounds as written.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -36,6 +37,17 @@ void linspace(double start, double end, int64_t num, double* out) {
   out[num - 1] = end;
 }
 
+// A grid's point count {start, end, n}[2]: a whole number of points, 1 .. 2^31 - 1 (a NaN, a
+// fraction below 1 or a huge value is refused before it is converted).
+bool grid_count(double x, int64_t& n) {
+  if (!(x >= 1.0 && x <= 2147483647.0)) return false;
+  n = (int64_t)x;
+  return true;
+}
+
+// One mesh matrix as the reference's arma::mat::load reads it: numbers separated by blanks
+// (commas read as blanks), one matrix row per non-blank line, every row as long as the first.
+// A token that is not a number fails the load, as it fails Armadillo's.
 bool read_matrix(const std::string& path, std::vector<double>& v, int64_t& rows, int64_t& cols) {
   std::ifstream f(path);
   if (!f) return false;
@@ -56,6 +68,8 @@ bool read_matrix(const std::string& path, std::vector<double>& v, int64_t& rows,
       ++c;
       s = e;
     }
+    while (*s == ' ' || *s == '\t' || *s == '\r' || *s == '\v' || *s == '\f') ++s;
+    if (*s != '\0') return false;  // text that is not a number
     if (c == 0) continue;
     if (cols < 0) cols = c;
     if (c != cols) return false;
@@ -71,7 +85,11 @@ extern "C" {
 
 int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_t* right, const double lim[6],
                    int64_t* n_out) {
-  if (n < 0 || (n > 0 && (!pos || !orient || !left || !right)) || !lim || !n_out) return KMC_ERR_ARG;
+  if (n < 0 || n > INT32_MAX || (n > 0 && (!pos || !orient || !left || !right)) || !lim || !n_out)
+    return KMC_ERR_ARG;
+  // links are followed and written below: each must be -1 or a site of the film
+  for (int64_t i = 0; i < n; ++i)
+    if (left[i] < -1 || left[i] >= n || right[i] < -1 || right[i] >= n) return KMC_ERR_ARG;
   // monte_carlo.h:730-750: exchange sites i and j, first pointing their tube neighbours at the new slots
   auto swap_sites = [&](int64_t i, int64_t j) {
     int32_t iL = left[i], iR = right[i], jL = left[j], jR = right[j];
@@ -120,8 +138,8 @@ int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]) {
 int kmc_forster2d_table(double gamma_0, const double distance[3], const double theta_deg[3], double* dist,
                         double* theta, double* rate) {
   if (!distance || !theta_deg || !dist || !theta || !rate) return KMC_ERR_ARG;
-  const int64_t nd = (int64_t)distance[2], nt = (int64_t)theta_deg[2];
-  if (nd < 1 || nt < 1) return KMC_ERR_ARG;
+  int64_t nd = 0, nt = 0;
+  if (!grid_count(distance[2], nd) || !grid_count(theta_deg[2], nt)) return KMC_ERR_ARG;
   linspace(distance[0], distance[1], nd, dist);
   linspace(theta_deg[0], theta_deg[1], nt, theta);
   const double scale = kRefPi / 180;
@@ -165,8 +183,10 @@ int kmc_species_rates(const kmc_species_model* m, int64_t n, const double* dist,
 int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
                       const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate) {
   if (!theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh || !a1 || !a2 || !rate) return KMC_ERR_ARG;
-  int64_t nt = (int64_t)theta_deg[2], nz = (int64_t)zshift[2], n1 = (int64_t)ash1[2], n2 = (int64_t)ash2[2];
-  if (nt < 1 || nz < 1 || n1 < 1 || n2 < 1) return KMC_ERR_ARG;
+  int64_t nt = 0, nz = 0, n1 = 0, n2 = 0;
+  if (!grid_count(theta_deg[2], nt) || !grid_count(zshift[2], nz) || !grid_count(ash1[2], n1) ||
+      !grid_count(ash2[2], n2))
+    return KMC_ERR_ARG;
   linspace(zshift[0], zshift[1], nz, zsh);
   linspace(ash1[0], ash1[1], n1, a1);
   linspace(ash2[0], ash2[1], n2, a2);
@@ -208,6 +228,7 @@ int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* 
     rows = r;
     cols = c;
   }
+  if (cols > 0 && rows > INT32_MAX / cols) return KMC_ERR_IO;  // site ids are 32-bit
   *n_tubes = rows;
   *n_points = cols;
   if (!pos && !orient && !left && !right) return KMC_OK;

@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <filesystem>
 #include <fstream>
+#include <initializer_list>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -459,17 +460,22 @@ class monte_carlo {
   void check(int rc, const char* what) const {
     if (rc != KMC_OK) throw std::runtime_error(std::string(what) + ": " + kmc_last_error(ctx_));
   }
-  static std::vector<double> lin(const jl::Value& g) { return lin3(g[0].as_double(), g[1].as_double(), g[2].as_int()); }
-  // arma::linspace as the engine defines it: a + i (b - a)/(n - 1), last element b
-  static std::vector<double> lin3(double a, double b, int64_t n) {
-    std::vector<double> x((size_t)std::max<int64_t>(n, 0));
-    if (n == 1) x[0] = b;
-    if (n >= 2) {
-      const double delta = (b - a) / double(n - 1);
-      for (int64_t i = 0; i < n - 1; ++i) x[i] = a + double(i) * delta;
-      x[n - 1] = b;
+  // A table grid's point count {start, end, n}[2]: a number in [1, 2^31 - 1], as the library
+  // checks it, taken before any array is sized from it.
+  static size_t grid_n(double x) {
+    if (!(x >= 1.0 && x <= 2147483647.0)) throw std::invalid_argument("bad rate-table grids");
+    return (size_t)x;
+  }
+  // entries of a table with these grid sizes, refused past 2^34 (128 GiB of rates) so that the
+  // product cannot wrap and leave the library a buffer smaller than the table it writes
+  static size_t table_size(std::initializer_list<size_t> n) {
+    const size_t cap = size_t(1) << 34;
+    size_t p = 1;
+    for (size_t k : n) {
+      if (k > cap / p) throw std::invalid_argument("rate table too large");
+      p *= k;
     }
-    return x;
+    return p;
   }
   // monte_carlo.cpp:24-61
   void create_scattering_table() {
@@ -482,12 +488,14 @@ class monte_carlo {
       double gz[3] = {(*z)[0].as_double(), (*z)[1].as_double(), (*z)[2].as_double()};
       double g1[3] = {(*a1)[0].as_double(), (*a1)[1].as_double(), (*a1)[2].as_double()};
       double g2[3] = {(*a2)[0].as_double(), (*a2)[1].as_double(), (*a2)[2].as_double()};
+      const size_t nt = grid_n(gt[2]), nz = grid_n(gz[2]), n1 = grid_n(g1[2]), n2 = grid_n(g2[2]);
+      const size_t n_rates = table_size({nt, nz, n1, n2});
       grids_.assign(4, {});
-      grids_[0].resize((size_t)gt[2]);
-      grids_[1].resize((size_t)gz[2]);
-      grids_[2].resize((size_t)g1[2]);
-      grids_[3].resize((size_t)g2[2]);
-      rates_.resize(grids_[0].size() * grids_[1].size() * grids_[2].size() * grids_[3].size());
+      grids_[0].resize(nt);
+      grids_[1].resize(nz);
+      grids_[2].resize(n1);
+      grids_[3].resize(n2);
+      rates_.resize(n_rates);
       if (kmc_forster_table(g0, gt, gz, g1, g2, grids_[0].data(), grids_[1].data(), grids_[2].data(), grids_[3].data(),
                             rates_.data()) != KMC_OK)
         throw std::invalid_argument("bad rate-table grids");
@@ -509,11 +517,12 @@ class monte_carlo {
       double gd[3], gt[3];
       g3("distance [m]", 0.5e-9, 10e-9, 96, gd);
       g3("theta 2d [degrees]", 0, 90, 91, gt);
-      if (!(gd[2] >= 1 && gt[2] >= 1)) throw std::invalid_argument("bad rate-table grids");
+      const size_t nd = grid_n(gd[2]), nt = grid_n(gt[2]);
+      const size_t n_rates = table_size({nd, nt});
       grids_.assign(2, {});
-      grids_[0].resize((size_t)gd[2]);
-      grids_[1].resize((size_t)gt[2]);
-      rates_.resize(grids_[0].size() * grids_[1].size());
+      grids_[0].resize(nd);
+      grids_[1].resize(nt);
+      rates_.resize(n_rates);
       if (kmc_forster2d_table(1.e15, gd, gt, grids_[0].data(), grids_[1].data(), rates_.data()) != KMC_OK)
         throw std::invalid_argument("bad rate-table grids");
       table_kind_ = KMC_TABLE_2D;
@@ -545,7 +554,9 @@ class monte_carlo {
     rates_.clear();
     double x;
     while (f >> x) rates_.push_back(x);
-    if (rates_.size() != grids_[0].size() * grids_[1].size() * grids_[2].size() * grids_[3].size())
+    for (const auto& g : grids_)
+      if (g.empty()) throw std::runtime_error("scat_table: an empty grid file");
+    if (rates_.size() != table_size({grids_[0].size(), grids_[1].size(), grids_[2].size(), grids_[3].size()}))
       throw std::runtime_error("scat_table.rates.dat does not match its grids");
     table_kind_ = KMC_TABLE_4D;
   }

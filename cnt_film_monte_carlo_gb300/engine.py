@@ -334,6 +334,26 @@ def species_rates(model: dict, dist, theta, donor, acceptor) -> np.ndarray:
     return out
 
 
+def _grid_n(spec, what: str) -> int:
+    """A grid's point count {start, end, n}[2], checked as the library checks it (a number in
+    [1, 2^31 - 1]) before the output arrays are sized from it."""
+    x = float(spec[2])
+    if not (1.0 <= x <= 2147483647.0):
+        raise L.KmcError(L.KMC_ERR_ARG, f"{what}: point count {spec[2]!r} is not in [1, 2^31 - 1]")
+    return int(x)
+
+
+def _table_size(ns, what: str) -> int:
+    """Entries of a table with grid sizes ns, refused past 2^34 (128 GiB of rates) before anything
+    is allocated, as the C++ driver refuses it."""
+    p = 1
+    for k in ns:
+        p *= int(k)
+    if p > 1 << 34:
+        raise L.KmcError(L.KMC_ERR_ARG, f"{what}: rate table too large ({p} entries)")
+    return p
+
+
 def trim_sites(pos_m, orient, left, right, lim):
     """trim_scats on copies; returns the kept (pos, orient, left, right)."""
     lib = L.load()
@@ -355,7 +375,8 @@ def forster2d_table(gamma_0, distance_m, theta_deg) -> dict:
     """The 2-D (distance, folded angle) Förster-form table, built by the library."""
     lib = L.load()
     dd, th = _f64(distance_m), _f64(theta_deg)
-    nd, nt = int(dd[2]), int(th[2])
+    nd, nt = _grid_n(dd, "forster2d_table"), _grid_n(th, "forster2d_table")
+    _table_size((nd, nt), "forster2d_table")
     g = [np.zeros(nd), np.zeros(nt)]
     rate = np.zeros((nd, nt))
     rc = lib.kmc_forster2d_table(float(gamma_0), L.ptr(dd, C.c_double), L.ptr(th, C.c_double), L.ptr(g[0], C.c_double),
@@ -369,7 +390,8 @@ def forster_table(gamma_0, theta_deg, zshift, ash1, ash2) -> dict:
     """The reference's Förster table on its 4-D grid (monte_carlo.cpp:156-200)."""
     lib = L.load()
     th, z, a1, a2 = (_f64(v) for v in (theta_deg, zshift, ash1, ash2))
-    n = [int(th[2]), int(z[2]), int(a1[2]), int(a2[2])]
+    n = [_grid_n(v, "forster_table") for v in (th, z, a1, a2)]
+    _table_size(n, "forster_table")
     g = [np.zeros(k) for k in n]
     rate = np.zeros(n)
     rc = lib.kmc_forster_table(float(gamma_0), L.ptr(th, C.c_double), L.ptr(z, C.c_double), L.ptr(a1, C.c_double),

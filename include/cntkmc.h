@@ -230,7 +230,8 @@ int kmc_set_hop_cap(kmc_ctx* ctx, int64_t cap);
 
 /* trim_scats (monte_carlo.h:722-782): remove sites outside lim = {xmin,xmax,ymin,ymax,zmin,zmax}
  * by swapping them to the end and repairing tube links; arrays are permuted in place and
- * *n_out gets the number kept. */
+ * *n_out gets the number kept.  KMC_ERR_ARG (nothing changed) when n > 2^31 - 1 or a link is
+ * neither -1 nor a site index below n. */
 int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_t* right, const double lim[6],
                    int64_t* n_out);
 
@@ -241,19 +242,22 @@ int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]);
  * in the reference, which tabulates 4-D): the formula of create_forster_scatt_table
  * (monte_carlo.cpp:174-187) at zero axis shifts, gamma_0 cos^2(theta) (1 nm / d)^6, on
  * arma::linspace grids {start, end, n} (distance in m, theta in degrees scaled by 3.141592/180).
- * Outputs: dist[nd], theta[nt], rate[nd][nt].  The C++ and Python drivers both use it. */
+ * Outputs: dist[nd], theta[nt], rate[nd][nt].  The C++ and Python drivers both use it.
+ * KMC_ERR_ARG unless each n is a number in [1, 2^31 - 1]. */
 int kmc_forster2d_table(double gamma_0, const double distance[3], const double theta_deg[3], double* dist,
                         double* theta, double* rate);
 
 /* create_forster_scatt_table (monte_carlo.cpp:156-200) on arma::linspace grids {start, end, n};
  * the theta grid is in degrees and scaled by pi/180 with pi = 3.141592 (helper/constants.h:10).
- * Outputs: grids theta[nt], zsh[nz], ash1[n1], ash2[n2]; rate[nt][nz][n1][n2]. */
+ * Outputs: grids theta[nt], zsh[nz], ash1[n1], ash2[n2]; rate[nt][nz][n1][n2].
+ * KMC_ERR_ARG unless each n is a number in [1, 2^31 - 1]. */
 int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
                       const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate);
 
 /* Mesh directory (single_cnt.{pos,orient}.{x,y,z}.dat, monte_carlo.h:199-271): first call with
  * NULL arrays returns *n_tubes and *n_points; second call fills pos/orient [n][3] (pos in m)
- * and left/right. */
+ * and left/right.  KMC_ERR_IO when a file is missing, holds a token that is not a number, has
+ * rows of different lengths or a shape unlike the others, or holds more than 2^31 - 1 points. */
 int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* pos, double* orient,
                   int32_t* left, int32_t* right);
 
@@ -355,7 +359,8 @@ typedef struct {
   double log_mean, log_scale;  /* output scaling of ln(rate) */
 } kmc_mlp_shape;
 
-/* The labeller that stands in for exciton_transfer (not built here): the Förster formula of
+/* A closed-form chirality labeller, much cheaper than exciton_transfer's first-order rate
+ * (kmc_exciton_rates, which labels the surrogate for mixed films): the Förster formula of
  * create_forster_scatt_table (monte_carlo.cpp:174-187) at zero axis shifts, extended by chirality:
  *   rate = gamma_0 s_ab (cos^2 theta + floor) (1 nm / sqrt(d^2 + near_field^2))^6,
  *   s_ab = (D_a D_b / D_ref^2) exp(-dE^2 / (2 width^2)) min(1, exp(-dE / kT)), dE = E_b - E_a,

@@ -167,3 +167,33 @@ def test_run_reports_of_driver_and_class_agree(name, tmp_path):
         assert all(v is not None for v in a["diffusion coefficient [m^2/s]"])
         if a["msd batches"] >= 2:
             assert all(v is not None and v > 0 for v in a["diffusion 95% interval [m^2/s]"])
+
+
+BIG = 2147483647
+BAD_GRIDS = [
+    ({"zshift [m]": [1.5e-9, 10e-9, 0.5]}, "bad rate-table grids"),
+    ({"zshift [m]": [1.5e-9, 10e-9, -3]}, "bad rate-table grids"),
+    ({"axis shift 1 [m]": [-1e-9, 1e-9, 1e300]}, "bad rate-table grids"),
+    ({k: [0.0, 1.0, BIG] for k in ("theta [degrees]", "zshift [m]", "axis shift 1 [m]", "axis shift 2 [m]")},
+     "rate table too large"),
+    ({"rate type": "forster2d", "distance [m]": [0.5e-9, 10e-9, 0]}, "bad rate-table grids"),
+]
+
+
+@pytest.mark.parametrize("change,message", BAD_GRIDS, ids=range(len(BAD_GRIDS)))
+def test_bad_table_grids_are_refused(change, message, tmp_path):
+    # a grid's point count outside [1, 2^31 - 1], or a table past 2^34 entries, is refused
+    # before anything is sized from it, by the driver and by the Python class
+    d = load_case(CASES[0])
+    cfg = _input_json(d, str(tmp_path), "mixed")
+    with open(cfg) as f:
+        j = json.load(f)
+    j["exciton monte carlo"].update(change)
+    with open(cfg, "w") as f:
+        json.dump(j, f)
+    B.build()
+    r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
+    assert r.returncode != 0 and message in r.stdout + r.stderr, (r.returncode, r.stdout, r.stderr)
+    with pytest.raises(Exception) as ei:
+        MC.run(cfg)
+    assert "point count" in str(ei.value) or "too large" in str(ei.value) or "grid" in str(ei.value)

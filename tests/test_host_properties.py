@@ -140,3 +140,79 @@ def test_t_quantiles_of_small_fits_are_exact():
         D, ci = diffusion.fit_counts(msd, np.ones(batches, np.int64), times, 1.0)
         se = np.std(np.arange(batches, dtype=np.float64), ddof=1) / np.sqrt(batches)
         assert ci[0] == pytest.approx(stats.t.ppf(0.975, batches - 1) * se, rel=2e-15)
+
+
+def test_trim_refuses_links_outside_the_film():
+    f = F.straight_tubes(3, 5.0, box_nm=(20, 20, 2), seed=1)
+    lim = [-1, 1, -1, 1, -1, 1]
+    for field, bad in (("left", f.n_sites), ("right", -2), ("left", 2**31 - 1)):
+        lk, rk = f.left.copy(), f.right.copy()
+        (lk if field == "left" else rk)[2] = bad
+        with pytest.raises(E.L.KmcError) as ei:
+            E.trim_sites(f.pos_m(), f.orient, lk, rk, lim)
+        assert ei.value.code == E.L.KMC_ERR_ARG
+
+
+@pytest.mark.parametrize("n", [float("nan"), 0.0, 0.5, -3.0, 1e300, float("inf")])
+def test_tables_refuse_bad_point_counts(n):
+    with pytest.raises(E.L.KmcError) as ei:
+        E.forster2d_table(1e15, (0.5e-9, 10e-9, n), (0.0, 90.0, 5))
+    assert ei.value.code == E.L.KMC_ERR_ARG
+    with pytest.raises(E.L.KmcError) as ei:
+        E.forster_table(1e15, (0.0, 90.0, 3), (1e-9, 2e-9, 2), (0.0, 1e-9, n), (0.0, 1e-9, 2))
+    assert ei.value.code == E.L.KMC_ERR_ARG
+
+
+def _write_mesh_files(d, texts):
+    names = ["single_cnt.pos.x.dat", "single_cnt.pos.y.dat", "single_cnt.pos.z.dat",
+             "single_cnt.orient.x.dat", "single_cnt.orient.y.dat", "single_cnt.orient.z.dat"]
+    for name, t in zip(names, texts):
+        (d / name).write_bytes(t if isinstance(t, bytes) else t.encode())
+
+
+def test_mesh_reader_refuses_malformed_files(tmp_path_factory):
+    good = "1 2 3\n4 5 6\n"
+    cases = {
+        "token": ["1 2 3\n4 x 6\n"] + [good] * 5,
+        "trailing text": ["1 2 3 # three\n4 5 6\n"] + [good] * 5,
+        "ragged": ["1 2 3\n4 5\n"] + [good] * 5,
+        "shape": [good] * 5 + ["1 2\n3 4\n5 6\n"],
+        "missing": [good] * 5,
+    }
+    for name, texts in cases.items():
+        d = tmp_path_factory.mktemp("bad_mesh")
+        _write_mesh_files(d, texts)
+        with pytest.raises(E.L.KmcError) as ei:
+            E.read_mesh(str(d))
+        assert ei.value.code == E.L.KMC_ERR_IO, name
+    # blank lines, CRLF endings, commas and exponents are read
+    d = tmp_path_factory.mktemp("ok_mesh")
+    _write_mesh_files(d, ["1,2,3\r\n\r\n4e0 5 6\r\n"] * 6)
+    pos, ori, lk, rk = E.read_mesh(str(d))
+    assert np.array_equal(ori[:, 0], [1, 2, 3, 4, 5, 6]) and np.array_equal(lk, [-1, 0, 1, -1, 3, 4])
+
+
+@SETTINGS
+@hyp.given(st.lists(st.binary(max_size=64) | st.text(alphabet="0123456789 .,-+eE\n\r\tnaif", max_size=64),
+                    min_size=6, max_size=6))
+def test_mesh_reader_never_crashes(tmp_path_factory, texts):
+    """Any six files give either a mesh or KMC_ERR_IO."""
+    d = tmp_path_factory.mktemp("fuzz_mesh")
+    _write_mesh_files(d, texts)
+    try:
+        pos, ori, lk, rk = E.read_mesh(str(d))
+    except E.L.KmcError as e:
+        assert e.code == E.L.KMC_ERR_IO
+        return
+    n = len(lk)
+    assert pos.shape == (n, 3) and ori.shape == (n, 3)
+    assert np.all((lk >= -1) & (lk < n)) and np.all((rk >= -1) & (rk < n))
+
+
+def test_tables_past_2_to_34_entries_are_refused_before_allocation():
+    big = (0.0, 1.0, 2**31 - 1)
+    with pytest.raises(E.L.KmcError, match="too large") as ei:
+        E.forster_table(1e15, big, big, big, big)
+    assert ei.value.code == E.L.KMC_ERR_ARG
+    with pytest.raises(E.L.KmcError, match="too large"):
+        E.forster2d_table(1e15, (0.5e-9, 10e-9, 2**31 - 1), (0.0, 90.0, 2**20))
