@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/cntkmc.h"
+#include "kmc_abi_guard.h"
 #include "kmc_internal.h"
 
 using kmc::FilmDev;
@@ -212,11 +213,22 @@ namespace kmc {
 int ctx_device(const kmc_ctx* c) { return c->device; }
 cudaStream_t ctx_stream(const kmc_ctx* c) { return c->stream; }
 void ctx_set_error(kmc_ctx* c, const char* msg) { c->err = msg; }
+int abi_fail(kmc_ctx* c, const char* fn) noexcept {
+  const char* what = nullptr;
+  const int code = abi_status(&what);
+  if (c) {
+    try {
+      c->err = std::string(fn) + ": " + what;
+    } catch (...) {  // no room for the message: the status alone
+    }
+  }
+  return code;
+}
 }  // namespace kmc
 
 extern "C" {
 
-kmc_ctx* kmc_create(int device, int* status) {
+kmc_ctx* kmc_create(int device, int* status) try {
   auto set = [&](int v) {
     if (status) *status = v;
   };
@@ -251,9 +263,14 @@ kmc_ctx* kmc_create(int device, int* status) {
   }
   set(KMC_OK);
   return c;
+} catch (...) {
+  const char* what = nullptr;
+  const int code = kmc::abi_status(&what);
+  if (status) *status = code;
+  return nullptr;
 }
 
-void kmc_destroy(kmc_ctx* c) {
+void kmc_destroy(kmc_ctx* c) try {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
@@ -291,6 +308,7 @@ void kmc_destroy(kmc_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+} catch (...) {
 }
 
 const char* kmc_last_error(const kmc_ctx* c) { return c ? c->err.c_str() : "null context"; }
@@ -313,7 +331,7 @@ static int host_positions(kmc_ctx* c) {
   return KMC_OK;
 }
 
-int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
+int kmc_load_film(kmc_ctx* c, const kmc_film* f) try {
   if (!c) return KMC_ERR_ARG;
   if (!f || f->n_films < 1 || !f->film_site_offsets || !f->pos || !f->orient || !f->left || !f->right)
     FAIL(c, KMC_ERR_ARG, "kmc_load_film: missing arrays");
@@ -385,9 +403,11 @@ int kmc_load_film(kmc_ctx* c, const kmc_film* f) {
   c->built = false;
   drop_excitons(c);
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_load_film");
 }
 
-int kmc_set_site_species(kmc_ctx* c, const int32_t* species, int32_t n_species) {
+int kmc_set_site_species(kmc_ctx* c, const int32_t* species, int32_t n_species) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->film_loaded) FAIL(c, KMC_ERR_STATE, "kmc_set_site_species: load a film first");
   if (!species || n_species < 1 || n_species > KMC_MAX_SPECIES)
@@ -402,9 +422,11 @@ int kmc_set_site_species(kmc_ctx* c, const int32_t* species, int32_t n_species) 
   c->built = false;
   drop_excitons(c);
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_site_species");
 }
 
-int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
+int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) try {
   if (!c) return KMC_ERR_ARG;
   if (!t || (t->kind != KMC_TABLE_4D && t->kind != KMC_TABLE_2D && t->kind != KMC_TABLE_2D_SPECIES) || !t->rate)
     FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: kind must be 4, 2 or 3");
@@ -467,6 +489,8 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) {
   c->built = false;
   drop_excitons(c);
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_rate_table");
 }
 
 // Bounds of the FP32 pair screen.  With M the largest coordinate magnitude, the FP32 distance of
@@ -508,7 +532,7 @@ static double sqrt_bound(double v, bool ge) {
   return x;
 }
 
-int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
+int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->film_loaded || !c->has_table) FAIL(c, KMC_ERR_STATE, "kmc_build_neighbors: load a film and a rate table first");
   if (!(r_max > 0)) FAIL(c, KMC_ERR_ARG, "kmc_build_neighbors: radius must be positive");
@@ -708,25 +732,31 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) {
     st->build_ms = ms;
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_build_neighbors");
 }
 
-int kmc_set_trace(kmc_ctx* c, int64_t n_trace, int64_t cap) {
+int kmc_set_trace(kmc_ctx* c, int64_t n_trace, int64_t cap) try {
   if (!c) return KMC_ERR_ARG;
   if (n_trace < 0 || cap < 0 || (n_trace > 0 && cap == 0)) FAIL(c, KMC_ERR_ARG, "kmc_set_trace: bad sizes");
   c->n_trace = n_trace;
   c->trace_cap = cap;
   drop_excitons(c);
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_trace");
 }
 
-int kmc_set_hop_cap(kmc_ctx* c, int64_t cap) {
+int kmc_set_hop_cap(kmc_ctx* c, int64_t cap) try {
   if (!c) return KMC_ERR_ARG;
   if (cap < 1) FAIL(c, KMC_ERR_ARG, "kmc_set_hop_cap: cap must be >= 1");
   c->hop_cap = cap;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_hop_cap");
 }
 
-int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
+int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_init_excitons: build the neighbour lists first");
   if (!inj || !inj->n_excitons || !inj->seeds) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: missing arrays");
@@ -826,6 +856,8 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) {
   c->contacts = false;
   c->inited = true;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_init_excitons");
 }
 
 static int ensure_msd(kmc_ctx* c, int64_t need) {
@@ -1056,7 +1088,7 @@ static int run_steps(kmc_ctx* c, kmc::HopArgs a, int64_t n_steps, int64_t step0,
   return check_device_error(c, "kmc_run");
 }
 
-int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision) {
+int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_run: create the excitons first");
   if (c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_run: the excitons are in contacts mode (kmc_contacts_run)");
@@ -1083,10 +1115,12 @@ int kmc_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision)
   c->stats.last_run_ms = ms;
   c->stats.last_launches = launches;
   return rc;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_run");
 }
 
 // ---------------------------------------------------------------- contacts mode
-int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* info, double* area, int64_t* stat_pop) {
+int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* info, double* area, int64_t* stat_pop) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_contacts_init: build the neighbour lists first");
   if (!cfg) FAIL(c, KMC_ERR_ARG, "kmc_contacts_init: missing configuration");
@@ -1280,10 +1314,12 @@ int kmc_contacts_init(kmc_ctx* c, const kmc_contacts* cfg, kmc_contacts_info* in
     info->capacity = cap;
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_contacts_init");
 }
 
 int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t precision, int64_t* population,
-                     int64_t* current, int64_t* n_live) {
+                     int64_t* current, int64_t* n_live) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->contacts || !c->built || !c->inited)
     FAIL(c, KMC_ERR_STATE, "kmc_contacts_run: set up contacts mode first (kmc_contacts_init)");
@@ -1394,10 +1430,12 @@ int kmc_contacts_run(kmc_ctx* c, int64_t n_steps, double dt, double v, int32_t p
   for (int64_t s = 0; s < n_steps; ++s) live_steps += (double)hl[s];
   note_step_length(c, (double)(after[0] - hops_before), live_steps);
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_contacts_run");
 }
 
 int kmc_contacts_track(kmc_ctx* c, int64_t first, int32_t n_tracks, double dt, double v, int64_t max_steps,
-                       double* path, int64_t* len, int32_t* arrived) {
+                       double* path, int64_t* len, int32_t* arrived) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->contacts || !c->built || !c->inited)
     FAIL(c, KMC_ERR_STATE, "kmc_contacts_track: set up contacts mode first (kmc_contacts_init)");
@@ -1427,36 +1465,46 @@ int kmc_contacts_track(kmc_ctx* c, int64_t first, int32_t n_tracks, double dt, d
   CK(c, cudaMemcpy(len, d_len.p, n_tracks * sizeof(int64_t), cudaMemcpyDeviceToHost));
   CK(c, cudaMemcpy(arrived, d_arr.p, n_tracks * sizeof(int32_t), cudaMemcpyDeviceToHost));
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_contacts_track");
 }
 
-int kmc_set_work_order(kmc_ctx* c, int32_t mode) {
+int kmc_set_work_order(kmc_ctx* c, int32_t mode) try {
   if (!c) return KMC_ERR_ARG;
   if (mode != KMC_ORDER_AUTO && mode != KMC_ORDER_SLOTS && mode != KMC_ORDER_SPATIAL)
     FAIL(c, KMC_ERR_ARG, "kmc_set_work_order: mode must be KMC_ORDER_AUTO, _SLOTS or _SPATIAL");
   c->work_order = mode;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_work_order");
 }
 
-int kmc_get_work_order(kmc_ctx* c, int32_t* in_effect) {
+int kmc_get_work_order(kmc_ctx* c, int32_t* in_effect) try {
   if (!c || !in_effect) return KMC_ERR_ARG;
   *in_effect = order_in_effect(c) ? KMC_ORDER_SPATIAL : KMC_ORDER_SLOTS;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_get_work_order");
 }
 
-int kmc_set_graph(kmc_ctx* c, int32_t on) {
+int kmc_set_graph(kmc_ctx* c, int32_t on) try {
   if (!c) return KMC_ERR_ARG;
   c->use_graph = on != 0;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_graph");
 }
 
-int kmc_set_mixed_variant(kmc_ctx* c, int32_t variant) {
+int kmc_set_mixed_variant(kmc_ctx* c, int32_t variant) try {
   if (!c) return KMC_ERR_ARG;
   if (variant < 0 || variant >= kmc::kMixedVariants) FAIL(c, KMC_ERR_ARG, "kmc_set_mixed_variant: 0..%d", kmc::kMixedVariants - 1);
   c->mixed_variant = variant;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_mixed_variant");
 }
 
-int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_result* out) {
+int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_result* out) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_autotune: create the excitons first");
   if (trial_steps < 1 || !(dt >= 0) || !(v > 0)) FAIL(c, KMC_ERR_ARG, "kmc_autotune: bad arguments");
@@ -1572,9 +1620,11 @@ int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_
     out->hops_per_s = best;
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_autotune");
 }
 
-int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) {
+int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) try {
   if (!c) return KMC_ERR_ARG;
   if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
   if (count == 0) return KMC_OK;
@@ -1585,9 +1635,11 @@ int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) {
                           count * row * sizeof(double), c->n_films, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_get_msd_batches");
 }
 
-int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) {
+int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) try {
   if (!c) return KMC_ERR_ARG;
   if (c->msd_batches == 1) return kmc_get_msd_batches(c, first, count, out);
   if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
@@ -1604,20 +1656,24 @@ int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) {
         out[(f * count + s) * 3 + k] = acc;
       }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_get_msd");
 }
 
-int kmc_set_msd_batches(kmc_ctx* c, int32_t batches) {
+int kmc_set_msd_batches(kmc_ctx* c, int32_t batches) try {
   if (!c) return KMC_ERR_ARG;
   if (batches < 1 || batches > 4096) FAIL(c, KMC_ERR_ARG, "kmc_set_msd_batches: 1..4096 batches");
   c->msd_batches = batches;
   drop_excitons(c);
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_msd_batches");
 }
 
 int64_t kmc_num_excitons(const kmc_ctx* c) { return c && c->inited ? c->n_exc_total : 0; }
 
 int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, double* ff, int32_t* heading,
-                     uint64_t* draws, int64_t* hops) {
+                     uint64_t* draws, int64_t* hops) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_get_excitons: no excitons");
   CK(c, cudaSetDevice(c->device));
@@ -1652,6 +1708,8 @@ int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, doub
     }
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_get_excitons");
 }
 
 // The inverse of kmc_get_excitons on the set kmc_init_excitons laid out (same films, counts,
@@ -1661,7 +1719,7 @@ int kmc_get_excitons(kmc_ctx* c, int32_t* site, double* pos, double* delta, doub
 // kExAtSite (the mixed kernel's "position is the site's" shortcut) is set where the position
 // equals the site's bit for bit; the shortcut and the general path give the same doubles there.
 int kmc_set_excitons(kmc_ctx* c, const int32_t* site, const double* pos, const double* delta, const double* ff,
-                     const int32_t* heading, const uint64_t* draws, const int64_t* hops) {
+                     const int32_t* heading, const uint64_t* draws, const int64_t* hops) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->inited) FAIL(c, KMC_ERR_STATE, "kmc_set_excitons: lay the excitons out with kmc_init_excitons first");
   if (c->contacts) FAIL(c, KMC_ERR_STATE, "kmc_set_excitons: contacts mode keeps its own particle state");
@@ -1714,15 +1772,19 @@ int kmc_set_excitons(kmc_ctx* c, const int32_t* site, const double* pos, const d
   c->steps_done = 0;  // the resumed run's MSD bins and statistics start at its first step
   c->stats = kmc_run_stats{};
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_excitons");
 }
 
-int kmc_get_run_stats(kmc_ctx* c, kmc_run_stats* st) {
+int kmc_get_run_stats(kmc_ctx* c, kmc_run_stats* st) try {
   if (!c || !st) return KMC_ERR_ARG;
   *st = c->stats;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_get_run_stats");
 }
 
-int kmc_get_neighbors(kmc_ctx* c, int64_t* rowptr, int32_t* col, double* cum, double* total) {
+int kmc_get_neighbors(kmc_ctx* c, int64_t* rowptr, int32_t* col, double* cum, double* total) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->built) FAIL(c, KMC_ERR_STATE, "kmc_get_neighbors: not built");
   CK(c, cudaSetDevice(c->device));
@@ -1754,9 +1816,11 @@ int kmc_get_neighbors(kmc_ctx* c, int64_t* rowptr, int32_t* col, double* cum, do
     }
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_get_neighbors");
 }
 
-int64_t kmc_get_trace(kmc_ctx* c, int64_t e, int32_t* out, int64_t cap) {
+int64_t kmc_get_trace(kmc_ctx* c, int64_t e, int32_t* out, int64_t cap) try {
   if (!c || !c->inited || e < 0 || e >= c->n_trace || !out) return KMC_ERR_ARG;
   if (cudaSetDevice(c->device) != cudaSuccess) return KMC_ERR_CUDA;
   int64_t cnt = 0;
@@ -1771,9 +1835,11 @@ int64_t kmc_get_trace(kmc_ctx* c, int64_t e, int32_t* out, int64_t cap) {
     else if (v != INT32_MIN) out[j] = -1 - c->h_perm[-1 - v];
   }
   return cnt;
+} catch (...) {
+  return (int64_t)kmc::abi_fail(c, "kmc_get_trace");
 }
 
-int kmc_selftest_uniform(kmc_ctx* c, uint32_t r0, uint64_t count, uint64_t* mismatches) {
+int kmc_selftest_uniform(kmc_ctx* c, uint32_t r0, uint64_t count, uint64_t* mismatches) try {
   if (!c || !mismatches) return KMC_ERR_ARG;
   CK(c, cudaSetDevice(c->device));
   DevBuf<unsigned long long> m;
@@ -1786,9 +1852,11 @@ int kmc_selftest_uniform(kmc_ctx* c, uint32_t r0, uint64_t count, uint64_t* mism
   m.release();
   *mismatches = h;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_selftest_uniform");
 }
 
-int kmc_probe_l2(kmc_ctx* c, int64_t bytes, int32_t reps, double* gbs) {
+int kmc_probe_l2(kmc_ctx* c, int64_t bytes, int32_t reps, double* gbs) try {
   if (!c || !gbs) return KMC_ERR_ARG;
   if (bytes < (1 << 20) || bytes % 16 || reps < 1) FAIL(c, KMC_ERR_ARG, "kmc_probe_l2: bytes >= 1 MiB, a multiple of 16; reps >= 1");
   CK(c, cudaSetDevice(c->device));
@@ -1806,9 +1874,11 @@ int kmc_probe_l2(kmc_ctx* c, int64_t bytes, int32_t reps, double* gbs) {
   CK(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
   *gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_probe_l2");
 }
 
-int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, double* acos_out) {
+int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, double* acos_out) try {
   if (!c || !x || !log_out || !acos_out || n < 0) return KMC_ERR_ARG;
   if (n == 0) return KMC_OK;
   CK(c, cudaSetDevice(c->device));
@@ -1824,6 +1894,8 @@ int kmc_math_probe(kmc_ctx* c, const double* x, int64_t n, double* log_out, doub
   dl.release();
   da.release();
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_math_probe");
 }
 
 // ---- learned pair-rate surrogate ----
@@ -1869,7 +1941,7 @@ static int mlp_grid(const kmc_ctx* c, int64_t count) {
   return (int)std::min<int64_t>(chunks, c->n_sms);
 }
 
-int kmc_mlp_init(kmc_ctx* c, const kmc_mlp_shape* sh, uint64_t seed) {
+int kmc_mlp_init(kmc_ctx* c, const kmc_mlp_shape* sh, uint64_t seed) try {
   if (!c) return KMC_ERR_ARG;
   if (!sh || sh->n_species < 1 || sh->n_species > KMC_MAX_SPECIES || !(sh->d_min > 0) || !(sh->d_max > sh->d_min) ||
       !(sh->log_scale > 0) || !std::isfinite(sh->log_mean) || !std::isfinite(sh->d_max) || !std::isfinite(sh->log_scale))
@@ -1899,9 +1971,11 @@ int kmc_mlp_init(kmc_ctx* c, const kmc_mlp_shape* sh, uint64_t seed) {
   for (int i = kmc::kMlpOffW2; i < kmc::kMlpOffB3; ++i) p[i] = uni(0.125);  // W2, b2, W3: fan-in 64
   for (int i = kmc::kMlpOffE; i < np; ++i) p[i] = uni(1.0);                 // embedding
   return mlp_upload_params(c, p.data());
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_init");
 }
 
-int kmc_mlp_set_params(kmc_ctx* c, const float* params, int64_t n) {
+int kmc_mlp_set_params(kmc_ctx* c, const float* params, int64_t n) try {
   if (!c) return KMC_ERR_ARG;
   if (c->mlp_np == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_set_params: call kmc_mlp_init first");
   if (!params || n != c->mlp_np) FAIL(c, KMC_ERR_ARG, "kmc_mlp_set_params: need %d parameters", c->mlp_np);
@@ -1909,9 +1983,11 @@ int kmc_mlp_set_params(kmc_ctx* c, const float* params, int64_t n) {
     if (!std::isfinite(params[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_set_params: parameter %lld is not finite", (long long)i);
   CK(c, cudaSetDevice(c->device));
   return mlp_upload_params(c, params);
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_set_params");
 }
 
-int kmc_mlp_get_params(kmc_ctx* c, float* params, int64_t n) {
+int kmc_mlp_get_params(kmc_ctx* c, float* params, int64_t n) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_get_params: call kmc_mlp_init first");
   if (!params || n != c->mlp_np) FAIL(c, KMC_ERR_ARG, "kmc_mlp_get_params: need room for %d parameters", c->mlp_np);
@@ -1919,6 +1995,8 @@ int kmc_mlp_get_params(kmc_ctx* c, float* params, int64_t n) {
   CK(c, cudaMemcpyAsync(params, c->d_mlp_master.p, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_get_params");
 }
 
 // checks the pair inputs shared by set_samples and predict
@@ -1934,7 +2012,7 @@ static int mlp_check_pairs(kmc_ctx* c, const char* who, int64_t n, const double*
 }
 
 int kmc_mlp_set_samples(kmc_ctx* c, int64_t n, const double* dist, const double* theta, const int32_t* pair,
-                        const double* log_rate) {
+                        const double* log_rate) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_set_samples: call kmc_mlp_init first");
   if (n < 1 || n > (1LL << 31) || !dist || !theta || !pair || !log_rate)
@@ -1954,9 +2032,11 @@ int kmc_mlp_set_samples(kmc_ctx* c, int64_t n, const double* dist, const double*
   CK(c, cudaStreamSynchronize(c->stream));
   c->mlp_n_samples = n;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_set_samples");
 }
 
-int kmc_mlp_gradient(kmc_ctx* c, int64_t first, int64_t count, float* grad, double* loss) {
+int kmc_mlp_gradient(kmc_ctx* c, int64_t first, int64_t count, float* grad, double* loss) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready || c->mlp_n_samples == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_gradient: set parameters and samples first");
   if (first < 0 || count < 1 || first + count > c->mlp_n_samples || !grad)
@@ -1977,9 +2057,11 @@ int kmc_mlp_gradient(kmc_ctx* c, int64_t first, int64_t count, float* grad, doub
   CK(c, cudaStreamSynchronize(c->stream));
   if (loss) *loss = l;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_gradient");
 }
 
-int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats* stats) {
+int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats* stats) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready || c->mlp_n_samples == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_train: set parameters and samples first");
   if (!cfg || cfg->epochs < 1 || cfg->batch < kmc::kMlpChunk || cfg->batch % kmc::kMlpChunk || cfg->batch > c->mlp_n_samples ||
@@ -2058,10 +2140,12 @@ int kmc_mlp_train(kmc_ctx* c, const kmc_mlp_train_cfg* cfg, kmc_mlp_train_stats*
     stats->seconds = ms * 1e-3;
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_train");
 }
 
 int kmc_mlp_predict(kmc_ctx* c, int64_t n, const double* dist, const double* theta, const int32_t* pair,
-                    double* log_rate) {
+                    double* log_rate) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_predict: call kmc_mlp_init first");
   if (n < 0 || (n > 0 && (!dist || !theta || !pair || !log_rate))) FAIL(c, KMC_ERR_ARG, "kmc_mlp_predict: bad arrays");
@@ -2078,9 +2162,11 @@ int kmc_mlp_predict(kmc_ctx* c, int64_t n, const double* dist, const double* the
   CK(c, cudaMemcpyAsync(log_rate, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_predict");
 }
 
-int kmc_mlp_rate_table(kmc_ctx* c, int32_t nd, const double* dist, int32_t nt, const double* theta, double* rate) {
+int kmc_mlp_rate_table(kmc_ctx* c, int32_t nd, const double* dist, int32_t nt, const double* theta, double* rate) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_rate_table: call kmc_mlp_init first");
   if (nd < 1 || nt < 1 || !dist || !theta || !rate) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: empty grid");
@@ -2100,14 +2186,18 @@ int kmc_mlp_rate_table(kmc_ctx* c, int32_t nd, const double* dist, int32_t nt, c
   CK(c, cudaMemcpyAsync(rate, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_mlp_rate_table");
 }
 
-int kmc_set_launch_config(kmc_ctx* c, int32_t block, int32_t steps_per_launch) {
+int kmc_set_launch_config(kmc_ctx* c, int32_t block, int32_t steps_per_launch) try {
   if (!c) return KMC_ERR_ARG;
   if (block < 32 || block > 256 || block % 32 || steps_per_launch < 1 || steps_per_launch > 1024) FAIL(c, KMC_ERR_ARG, "kmc_set_launch_config: bad values");
   c->block = block;
   c->steps_per_launch = steps_per_launch;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(c, "kmc_set_launch_config");
 }
 
 }  // extern "C"

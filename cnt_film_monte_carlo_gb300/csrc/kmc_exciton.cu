@@ -39,6 +39,7 @@
 #include <vector>
 
 #include "../../include/cntkmc.h"
+#include "kmc_abi_guard.h"
 #include "kmc_internal.h"
 
 using cx = std::complex<double>;
@@ -1248,7 +1249,7 @@ bool cfg_ok(const kmc_transfer_cfg* cfg) {
 
 extern "C" {
 
-int kmc_cnt_create(kmc_ctx* ctx, int32_t n, int32_t m, int32_t length_cells, kmc_cnt** out) {
+int kmc_cnt_create(kmc_ctx* ctx, int32_t n, int32_t m, int32_t length_cells, kmc_cnt** out) try {
   if (!ctx || !out) return KMC_ERR_ARG;
   *out = nullptr;
   if (n < 1 || m < 1 || m > n || length_cells < 1 || length_cells > 4096)
@@ -1278,11 +1279,13 @@ int kmc_cnt_create(kmc_ctx* ctx, int32_t n, int32_t m, int32_t length_cells, kmc
   }
   *out = t;
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(ctx, "kmc_cnt_create");
 }
 
 void kmc_cnt_destroy(kmc_cnt* t) { delete t; }
 
-int kmc_cnt_get_info(const kmc_cnt* t, kmc_cnt_info* info) {
+int kmc_cnt_get_info(const kmc_cnt* t, kmc_cnt_info* info) try {
   if (!t || !info) return KMC_ERR_ARG;
   kmc_cnt_info& o = *info;
   o.n = t->n, o.m = t->m, o.cells = t->cells, o.Nu = t->Nu, o.M = t->M, o.Q = t->Q, o.t1 = t->t1, o.t2 = t->t2;
@@ -1290,9 +1293,12 @@ int kmc_cnt_get_info(const kmc_cnt* t, kmc_cnt_info* info) {
   o.iq0 = t->iq0, o.nq = t->nq, o.mq0 = t->mq0, o.nmq = t->nmq, o.ik_cm0 = t->ik_cm0, o.nk_cm = t->nk_cm;
   o.radius = t->radius, o.length = t->length, o.area_u = t->au;
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
-int kmc_cnt_get_array(const kmc_cnt* t, int32_t which, void* out, int64_t count) {
+int kmc_cnt_get_array(const kmc_cnt* t, int32_t which, void* out, int64_t count) try {
   if (!t || !out || count < 0) return KMC_ERR_ARG;
   std::vector<double> dv;
   std::vector<int32_t> iv;
@@ -1330,10 +1336,13 @@ int kmc_cnt_get_array(const kmc_cnt* t, int32_t which, void* out, int64_t count)
   if (!dv.empty()) std::memcpy(out, dv.data(), dv.size() * sizeof(double));
   else if (!iv.empty()) std::memcpy(out, iv.data(), iv.size() * sizeof(int32_t));
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 int kmc_exciton_j(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, int64_t n_pairs,
-                  const int32_t* ik_cm_pairs, const double geometry[4], int32_t precision, double* j_out) {
+                  const int32_t* ik_cm_pairs, const double geometry[4], int32_t precision, double* j_out) try {
   if (!ctx || !donor || !acceptor || n_pairs < 0 || (n_pairs > 0 && (!ik_cm_pairs || !geometry || !j_out)) ||
       (precision != KMC_PREC_FP64 && precision != KMC_PREC_MIXED))
     return fail(ctx, KMC_ERR_ARG, "kmc_exciton_j: bad arguments");
@@ -1359,10 +1368,12 @@ int kmc_exciton_j(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, i
     j_out[2 * i + 1] = v.y;
   }
   return KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(ctx, "kmc_exciton_j");
 }
 
 int kmc_exciton_rates(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, const kmc_transfer_cfg* cfg,
-                      int64_t n_geometries, const double* geometries, double* rate) {
+                      int64_t n_geometries, const double* geometries, double* rate) try {
   if (!ctx || !donor || !acceptor || !cfg_ok(cfg) || n_geometries < 0 || (n_geometries > 0 && (!geometries || !rate)))
     return fail(ctx, KMC_ERR_ARG, "kmc_exciton_rates: bad arguments");
   if (cudaSetDevice(ctx_device(ctx)) != cudaSuccess) return fail(ctx, KMC_ERR_CUDA, "kmc_exciton_rates: cudaSetDevice");
@@ -1370,11 +1381,13 @@ int kmc_exciton_rates(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* accepto
   std::string err;
   int rc = rates(*donor, *acceptor, *cfg, n_geometries, geometries, rate, ctx_stream(ctx), err);
   return rc ? fail(ctx, rc, "kmc_exciton_rates: " + err) : KMC_OK;
+} catch (...) {
+  return kmc::abi_fail(ctx, "kmc_exciton_rates");
 }
 
 int kmc_davoody_table(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, const kmc_transfer_cfg* cfg,
                       const double theta_deg[3], const double zshift[3], const double ash1[3], const double ash2[3],
-                      double* theta, double* zsh, double* a1, double* a2, double* rate) {
+                      double* theta, double* zsh, double* a1, double* a2, double* rate) try {
   if (!ctx || !donor || !acceptor || !cfg_ok(cfg) || !theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh ||
       !a1 || !a2 || !rate)
     return fail(ctx, KMC_ERR_ARG, "kmc_davoody_table: bad arguments");
@@ -1399,6 +1412,8 @@ int kmc_davoody_table(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* accepto
           geo[4 * g + 3] = theta[it];
         }
   return kmc_exciton_rates(ctx, donor, acceptor, cfg, (int64_t)g, geo.data(), rate);
+} catch (...) {
+  return kmc::abi_fail(ctx, "kmc_davoody_table");
 }
 
 }  // extern "C"

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/cntkmc.h"
+#include "kmc_abi_guard.h"
 
 namespace {
 
@@ -75,6 +76,9 @@ bool read_matrix(const std::string& path, std::vector<double>& v, int64_t& rows,
     if (c != cols) return false;
     ++rows;
   }
+  // the stream stops at the end of the file, or on a read error (an allocation that failed inside
+  // getline sets badbit rather than throwing): only the first is a matrix
+  if (f.bad() || !f.eof()) return false;
   if (cols < 0) cols = 0;
   return true;
 }
@@ -84,7 +88,7 @@ bool read_matrix(const std::string& path, std::vector<double>& v, int64_t& rows,
 extern "C" {
 
 int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_t* right, const double lim[6],
-                   int64_t* n_out) {
+                   int64_t* n_out) try {
   if (n < 0 || n > INT32_MAX || (n > 0 && (!pos || !orient || !left || !right)) || !lim || !n_out)
     return KMC_ERR_ARG;
   // links are followed and written below: each must be -1 or a site of the film
@@ -120,9 +124,12 @@ int kmc_trim_sites(int64_t n, double* pos, double* orient, int32_t* left, int32_
   }
   *n_out = j;
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
-int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]) {
+int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]) try {
   if (n <= 0 || !pos || !mn || !mx) return KMC_ERR_ARG;
   // find_simulation_domain, monte_carlo.h:328-340
   for (int c = 0; c < 3; ++c) mn[c] = mx[c] = pos[c];
@@ -133,10 +140,13 @@ int kmc_domain(int64_t n, const double* pos, double mn[3], double mx[3]) {
       mx[c] = mx[c] < p ? p : mx[c];
     }
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 int kmc_forster2d_table(double gamma_0, const double distance[3], const double theta_deg[3], double* dist,
-                        double* theta, double* rate) {
+                        double* theta, double* rate) try {
   if (!distance || !theta_deg || !dist || !theta || !rate) return KMC_ERR_ARG;
   int64_t nd = 0, nt = 0;
   if (!grid_count(distance[2], nd) || !grid_count(theta_deg[2], nt)) return KMC_ERR_ARG;
@@ -152,10 +162,13 @@ int kmc_forster2d_table(double gamma_0, const double distance[3], const double t
       rate[i * nt + k] = gamma_0 * (c * c) * std::pow(1.e-9 / dist[i], 6);
     }
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 int kmc_species_rates(const kmc_species_model* m, int64_t n, const double* dist, const double* theta,
-                      const int32_t* donor, const int32_t* acceptor, double* rate) {
+                      const int32_t* donor, const int32_t* acceptor, double* rate) try {
   if (!m || n < 0 || (n > 0 && (!dist || !theta || !donor || !acceptor || !rate))) return KMC_ERR_ARG;
   if (m->n_species < 1 || m->n_species > KMC_MAX_SPECIES || !m->energy || !m->diameter || !(m->diameter_ref > 0) ||
       !(m->width > 0) || !(m->kT > 0))
@@ -178,10 +191,13 @@ int kmc_species_rates(const kmc_species_model* m, int64_t n, const double* dist,
     rate[i] = m->gamma_0 * s * (c * c + m->floor) * std::pow(1.e-9 / r, 6);
   }
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zshift[3], const double ash1[3],
-                      const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate) {
+                      const double ash2[3], double* theta, double* zsh, double* a1, double* a2, double* rate) try {
   if (!theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh || !a1 || !a2 || !rate) return KMC_ERR_ARG;
   int64_t nt = 0, nz = 0, n1 = 0, n2 = 0;
   if (!grid_count(theta_deg[2], nt) || !grid_count(zshift[2], nz) || !grid_count(ash1[2], n1) ||
@@ -212,10 +228,13 @@ int kmc_forster_table(double gamma_0, const double theta_deg[3], const double zs
         }
   }
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* pos, double* orient, int32_t* left,
-                  int32_t* right) {
+                  int32_t* right) try {
   if (!dir || !n_tubes || !n_points) return KMC_ERR_ARG;
   static const char* names[6] = {"single_cnt.pos.x.dat",    "single_cnt.pos.y.dat",    "single_cnt.pos.z.dat",
                                  "single_cnt.orient.x.dat", "single_cnt.orient.y.dat", "single_cnt.orient.z.dat"};
@@ -245,6 +264,9 @@ int kmc_read_mesh(const char* dir, int64_t* n_tubes, int64_t* n_points, double* 
       right[s] = j + 1 < cols ? (int32_t)(s + 1) : -1;
     }
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 // Two-sided 95% quantile of Student's t with nu degrees of freedom.  nu <= 31 (every fit of up
@@ -273,7 +295,7 @@ static double t975(int nu) {
 }
 
 int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* times, int64_t n_steps, int32_t batches,
-                      double fit_fraction, double D[3], double ci95[3]) {
+                      double fit_fraction, double D[3], double ci95[3]) try {
   if (!msd || !counts || !times || !D || !ci95 || n_steps < 2 || batches < 1 || !(fit_fraction > 0) ||
       fit_fraction > 1)
     return KMC_ERR_ARG;
@@ -310,6 +332,9 @@ int kmc_fit_diffusion(const double* msd, const int64_t* counts, const double* ti
                             : NAN;
   }
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  return kmc::abi_status(&what);
 }
 
 const char* kmc_version(void) { return "cntkmc 0.3 (sm_103a)"; }

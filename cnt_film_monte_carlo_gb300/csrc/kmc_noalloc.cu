@@ -26,6 +26,7 @@
 #include <mutex>
 
 #include "../../include/cntkmc.h"
+#include "kmc_abi_guard.h"
 #include "kmc_internal.h"
 #include "kmc_pair.cuh"
 
@@ -246,7 +247,7 @@ int fail(char* err, int64_t err_len, int code, const char* msg) {
 extern "C" int kmc_build_neighbors_noalloc(const double* pos, const double* orient, int64_t n_sites,
                                            const kmc_table* table, double max_hopping_radius, int64_t* rowptr,
                                            int32_t* col, double* cum, double* total, int64_t capacity,
-                                           int64_t* nnz, void* stream, char* err, int64_t err_len) {
+                                           int64_t* nnz, void* stream, char* err, int64_t err_len) try {
   char msg[256];
   if (!pos || !orient || !table || !rowptr || !total || !nnz || capacity < 0)
     return fail(err, err_len, KMC_ERR_ARG, "kmc_build_neighbors_noalloc: missing argument");
@@ -352,4 +353,8 @@ extern "C" int kmc_build_neighbors_noalloc(const double* pos, const double* orie
   NA_CK(cudaStreamSynchronize(st));
 #undef NA_CK
   return KMC_OK;
+} catch (...) {
+  const char* what = nullptr;
+  const int code = kmc::abi_status(&what);
+  return fail(err, err_len, code, what);
 }

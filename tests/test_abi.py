@@ -125,3 +125,38 @@ def test_header_compiles_as_c_and_host_calls_work_from_c(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
     assert r.stdout.startswith("ok cntkmc")
+
+
+GUARD_CHILD = r"""
+import ctypes as C, os, resource, sys
+sys.path.insert(0, sys.argv[2])
+from cnt_film_monte_carlo_gb300 import _lib as L
+lib = L.load()
+nt, npnt = C.c_int64(0), C.c_int64(0)
+vm = next(int(l.split()[1]) for l in open("/proc/self/status") if l.startswith("VmSize:")) * 1024
+resource.setrlimit(resource.RLIMIT_AS, (vm + (int(sys.argv[3]) << 20), resource.RLIM_INFINITY))
+rc = lib.kmc_read_mesh(sys.argv[1].encode(), C.byref(nt), C.byref(npnt), None, None, None, None)
+os.write(1, b"%d" % rc)
+"""
+
+
+def test_host_allocation_failure_is_a_status_not_an_abort(tmp_path):
+    # A C++ exception must not cross the C ABI.  With the child's address space capped a little
+    # above what it uses, reading a 16 MB one-line matrix (8 M numbers: a 64 MB vector) cannot
+    # allocate: inside getline the stream reports a read error (KMC_ERR_IO), in the vector's
+    # growth the exception is caught at the ABI (KMC_ERR_NOMEM).  Either way the call returns
+    # a status instead of ending the process in std::terminate, and never reports a mesh.
+    import subprocess
+    import sys
+
+    row = b"0 " * (8 << 20) + b"\n"
+    for name in ("pos.x", "pos.y", "pos.z", "orient.x", "orient.y", "orient.z"):
+        (tmp_path / f"single_cnt.{name}.dat").write_bytes(row)
+    codes = []
+    for headroom_mb in (24, 40, 56, 72, 88):
+        r = subprocess.run([sys.executable, "-c", GUARD_CHILD, str(tmp_path), ROOT, str(headroom_mb)],
+                           capture_output=True, timeout=120)
+        assert r.returncode == 0, (headroom_mb, r.returncode, r.stdout, r.stderr[-2000:])
+        codes.append(int(r.stdout))
+    assert set(codes) <= {L.KMC_ERR_IO, L.KMC_ERR_NOMEM}, codes
+    assert L.KMC_ERR_NOMEM in codes, codes
