@@ -4,7 +4,9 @@
  * boundary is the C++ class mc::monte_carlo driven by src/main.cpp:62-76.  Each entry point
  * below names the reference code it replaces.  Conventions:
  *   - every call returns int: KMC_OK (0) or a negative KMC_ERR_* code; kmc_last_error()
- *     gives the message of the last failure on that context; nothing throws across the ABI;
+ *     gives the message of the last failure on that context; nothing throws across the ABI
+ *     (a host allocation that fails inside a call is KMC_ERR_NOMEM, any other C++ exception
+ *     KMC_ERR_ARG with its message);
  *   - plain pointers and sizes only; host buffers are copied in (the caller keeps them),
  *     device memory belongs to the context;
  *   - SI units (m, s, 1/s); positions [n][3] row-major;
