@@ -544,6 +544,7 @@ class monte_carlo {
       std::vector<double> v;
       double x;
       while (f >> x) v.push_back(x);
+      if (!f.eof()) throw std::runtime_error(std::string("scat_table.") + name + ".dat: a token that is not a number");
       return v;
     };
     grids_ = {col("theta"), col("z_shift"), col("axis_shift_1"), col("axis_shift_2")};
@@ -554,6 +555,7 @@ class monte_carlo {
     rates_.clear();
     double x;
     while (f >> x) rates_.push_back(x);
+    if (!f.eof()) throw std::runtime_error("scat_table.rates.dat: missing, or a token that is not a number");
     for (const auto& g : grids_)
       if (g.empty()) throw std::runtime_error("scat_table: an empty grid file");
     if (rates_.size() != table_size({grids_[0].size(), grids_[1].size(), grids_[2].size(), grids_[3].size()}))

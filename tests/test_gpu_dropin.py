@@ -197,3 +197,33 @@ def test_bad_table_grids_are_refused(change, message, tmp_path):
     with pytest.raises(Exception) as ei:
         MC.run(cfg)
     assert "point count" in str(ei.value) or "too large" in str(ei.value) or "grid" in str(ei.value)
+
+
+def test_corrupt_saved_table_is_refused(tmp_path):
+    # a saved table (rate type "davoody") whose grid or rates file holds a token that is not a
+    # number is refused by the driver and by the Python class, not read short
+    from oracle import oracle as O
+    from test_tables import save_like_reference
+
+    d = load_case(CASES[0])
+    mc = d["config"]
+    tab = O.forster_table(1e15, mc["theta [degrees]"], mc["zshift [m]"], mc["axis shift 1 [m]"],
+                          mc["axis shift 2 [m]"])
+    for target in ("scat_table.z_shift.dat", "scat_table.rates.dat"):
+        run_dir = tmp_path / target
+        tdir = run_dir / "table"
+        os.makedirs(tdir)
+        save_like_reference(tab, str(tdir))
+        with open(tdir / target, "a") as f:
+            f.write("\nnot-a-number\n")
+        cfg = _input_json(d, str(run_dir), "mixed")
+        with open(cfg) as f:
+            j = json.load(f)
+        j["exciton monte carlo"].update({"rate type": "davoody", "rate table directory": str(tdir)})
+        with open(cfg, "w") as f:
+            json.dump(j, f)
+        B.build()
+        r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
+        assert r.returncode != 0 and "not a number" in r.stdout + r.stderr, (target, r.stdout, r.stderr)
+        with pytest.raises(ValueError):
+            MC.run(cfg)
