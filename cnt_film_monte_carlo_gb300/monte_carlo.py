@@ -375,10 +375,16 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
 CHUNK = 256  # time steps per engine call in run()
 
 
+def _no_constant(name: str):
+    raise ValueError(f"json: {name} is not a JSON number")
+
+
 def run(input_json: str, device: int = 0) -> str:
-    """src/main.cpp:32-80: read input.json, run the Green-Kubo loop, return the output directory."""
+    """src/main.cpp:32-80: read input.json, run the Green-Kubo loop, return the output directory.
+    The file is read as strictly as the reference's nlohmann::json reads it (and as cntkmc_run
+    does): NaN, Infinity and -Infinity are refused."""
     with open(input_json) as f:
-        j = json.load(f)
+        j = json.load(f, parse_constant=_no_constant)
     if "exciton monte carlo" not in j:
         raise ValueError('json input file does not contain "exciton monte carlo"')
     jm = dict(j["exciton monte carlo"])

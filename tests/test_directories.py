@@ -152,3 +152,13 @@ def test_leading_tilde_is_home(mirror, tmp_path, monkeypatch):
     assert Path(f"{home}x").is_dir()
     (home / "out" / "f").write_text("f")
     assert mirror.check("~/out") == f"{home}/out"
+
+
+@pytest.mark.parametrize("literal", ["NaN", "Infinity", "-Infinity"])
+def test_python_driver_refuses_non_json_numbers(tmp_path, literal):
+    # input.json is refused before anything else happens (no device needed), as cntkmc_run's
+    # reader refuses it
+    p = tmp_path / "input.json"
+    p.write_text('{"exciton monte carlo": {"monte carlo time step": %s}}' % literal)
+    with pytest.raises(ValueError, match="not a JSON number"):
+        M.run(str(p))
