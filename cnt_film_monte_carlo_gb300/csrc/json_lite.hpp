@@ -2,8 +2,8 @@
 // Supports objects, arrays, numbers, strings (with \" \\ \/ \b \f \n \r \t \uXXXX escapes, the
 // last decoded to UTF-8), true/false/null, and refuses what RFC 8259 does not allow (as the
 // reference's nlohmann::json reader does): numbers outside the JSON grammar (nan, inf, hex, a
-// leading '+' or zero, a bare '.'), other escapes, raw control characters and unpaired
-// surrogates in strings.  Object key order is kept for writing the file back; a number read from
+// leading '+' or zero, a bare '.'), other escapes, raw control characters, unpaired
+// surrogates and invalid UTF-8 in strings.  Object key order is kept for writing the file back; a number read from
 // text is written back as that text (so integers stay integers and 0.1 stays 0.1); strings are
 // written with quote, backslash and control characters escaped.
 #pragma once
@@ -72,6 +72,10 @@ class Parser {
  private:
   const std::string& s_;
   size_t i_ = 0;
+  // objects and arrays nest at most this deep: the reader and the writer recurse once per level,
+  // and a file of a few hundred kilobytes of brackets would otherwise overflow the stack
+  static constexpr int kMaxDepth = 512;
+  int depth_ = 0;
   [[noreturn]] void fail(const char* what) {
     throw std::invalid_argument(std::string("json: ") + what + " at offset " + std::to_string(i_));
   }
@@ -91,10 +95,14 @@ class Parser {
     if (i_ >= s_.size()) fail("unexpected end");
     char c = s_[i_];
     Value v;
+    if ((c == '{' || c == '[') && ++depth_ > kMaxDepth) fail("objects and arrays nested too deep");
     if (c == '{') {
       ++i_;
       v.kind = Value::Object;
-      if (eat('}')) return v;
+      if (eat('}')) {
+        --depth_;
+        return v;
+      }
       do {
         ws();
         std::string k = string();
@@ -102,14 +110,19 @@ class Parser {
         v.obj.emplace_back(k, value());
       } while (eat(','));
       if (!eat('}')) fail("'}' expected");
+      --depth_;
     } else if (c == '[') {
       ++i_;
       v.kind = Value::Array;
-      if (eat(']')) return v;
+      if (eat(']')) {
+        --depth_;
+        return v;
+      }
       do {
         v.arr.push_back(value());
       } while (eat(','));
       if (!eat(']')) fail("']' expected");
+      --depth_;
     } else if (c == '"') {
       v.kind = Value::String;
       v.str = string();
@@ -189,6 +202,33 @@ class Parser {
       out += (char)(0x80 | (cp & 0x3F));
     }
   }
+  // One multi-byte UTF-8 character whose lead byte b was just read (RFC 3629: no overlong forms,
+  // no surrogates, nothing above U+10FFFF), appended to out as it is.
+  void utf8_sequence(unsigned char b, std::string& out) {
+    int n;
+    unsigned char lo = 0x80, hi = 0xBF;  // range of the first continuation byte
+    if (b >= 0xC2 && b <= 0xDF) {
+      n = 1;
+    } else if (b >= 0xE0 && b <= 0xEF) {
+      n = 2;
+      if (b == 0xE0) lo = 0xA0;
+      if (b == 0xED) hi = 0x9F;
+    } else if (b >= 0xF0 && b <= 0xF4) {
+      n = 3;
+      if (b == 0xF0) lo = 0x90;
+      if (b == 0xF4) hi = 0x8F;
+    } else {
+      fail("invalid UTF-8 in string");
+    }
+    out += (char)b;
+    for (int k = 0; k < n; ++k) {
+      if (i_ >= s_.size()) fail("invalid UTF-8 in string");
+      const unsigned char t = (unsigned char)s_[i_];
+      if (t < (k == 0 ? lo : 0x80) || t > (k == 0 ? hi : 0xBF)) fail("invalid UTF-8 in string");
+      out += (char)t;
+      ++i_;
+    }
+  }
   std::string string() {
     if (i_ >= s_.size() || s_[i_] != '"') fail("string expected");
     ++i_;
@@ -196,6 +236,10 @@ class Parser {
     while (i_ < s_.size() && s_[i_] != '"') {
       char c = s_[i_++];
       if ((unsigned char)c < 0x20) fail("control character in string");
+      if ((unsigned char)c >= 0x80) {
+        utf8_sequence((unsigned char)c, out);
+        continue;
+      }
       if (c == '\\') {
         if (i_ >= s_.size()) fail("bad escape");
         char e = s_[i_++];

@@ -124,3 +124,59 @@ def test_random_documents_round_trip(roundtrip, tmp_path_factory):
         assert json.dumps(back, sort_keys=True) == json.dumps(value, sort_keys=True)  # -0.0 and key sets
 
     check()
+
+
+@pytest.mark.parametrize("raw", [b"\x80", b"\xc0\xaf", b"\xc3", b"\xe0\x80\xaf", b"\xed\xa0\x80",
+                                 b"\xf4\x90\x80\x80", b"\xf5\x80\x80\x80", b"\xff", b"\xe2\x82"])
+def test_invalid_utf8_in_strings_is_refused(roundtrip, tmp_path, raw):
+    # stray continuation, overlong, truncated, surrogate (U+D800), above U+10FFFF, never-valid bytes
+    p = tmp_path / "in.json"
+    p.write_bytes(b'{"a": "x' + raw + b'y"}')
+    r = subprocess.run([str(roundtrip), str(p)], capture_output=True)
+    assert r.returncode == 2 and b"UTF-8" in r.stderr, (raw, r.returncode, r.stderr)
+
+
+def test_valid_utf8_edges_are_read(roundtrip, tmp_path):
+    s = "\u0080\u07ff\u0800\ud7ff\ue000\uffff\U00010000\U0010ffff"
+    p = tmp_path / "in.json"
+    p.write_bytes(json.dumps({"a": s}, ensure_ascii=False).encode("utf-8"))
+    r = subprocess.run([str(roundtrip), str(p)], capture_output=True)
+    assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout.decode("utf-8")) == {"a": s}
+
+
+def test_nesting_depth_is_bounded(roundtrip, tmp_path):
+    """512 levels of objects or arrays are read; deeper files are refused with a message instead
+    of overflowing the stack of the recursive reader."""
+    r = run(roundtrip, tmp_path, "[" * 512 + "]" * 512)
+    assert r.returncode == 0 and json.loads(r.stdout) is not None
+    r = run(roundtrip, tmp_path, '{"a":' * 512 + "1" + "}" * 512)
+    assert r.returncode == 0
+    for text in ("[" * 513 + "]" * 513, "[" * 200000 + "]" * 200000, '{"a":' * 100000):
+        r = run(roundtrip, tmp_path, text)
+        assert r.returncode == 2 and b"nested too deep" in r.stderr, (len(text), r.returncode)
+
+
+def test_arbitrary_bytes_are_read_or_refused(roundtrip, tmp_path_factory):
+    """Any file is either a JSON document (exit 0, and Python's json reads the same value out of
+    the writer's output) or refused with a message (exit 2): never a crash."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    d = tmp_path_factory.mktemp("jl_bytes")
+    pieces = st.sampled_from(['{', '}', '[', ']', ',', ':', '"', '\\', 'u', 'd83d', 'e', '-', '+', '.', '0', '1',
+                              '9', 'true', 'false', 'null', ' ', '\n', 'NaN', '\x00', '\x1f', 'é', '\udc00'])
+    texts = st.lists(pieces, max_size=40).map("".join) | st.binary(max_size=60).map(
+        lambda b: b.decode("latin-1"))
+
+    @hyp.settings(max_examples=300, deadline=None, database=None)
+    @hyp.given(texts)
+    def check(text):
+        p = d / "in.json"
+        p.write_bytes(text.encode("utf-8", "surrogatepass"))
+        r = subprocess.run([str(roundtrip), str(p)], capture_output=True)
+        assert r.returncode in (0, 2), (text, r.returncode, r.stderr)
+        if r.returncode == 0:
+            back = json.loads(r.stdout.decode("utf-8"))
+            assert back == json.loads(text.encode("utf-8", "surrogatepass").decode("utf-8"))
+
+    check()
