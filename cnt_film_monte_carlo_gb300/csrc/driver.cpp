@@ -43,7 +43,7 @@ int main(int argc, char** argv) {
       sim.init();
       sim.save_json_properties();
       // main.cpp:90-92: 100 tracked particles ("number of tracked particles"), in one launch
-      sim.track_particles(time_step, jm.has("number of tracked particles") ? (int)jm["number of tracked particles"].as_int()
+      sim.track_particles(time_step, jm.has("number of tracked particles") ? jm["number of tracked particles"].as_int32()
                                                                            : 100);
       // the loop's steps in chunks of one engine call each (same rows as one call per step)
       for (int64_t left = sim.steps_until(sim.contacts_max_time(), time_step); left > 0; left -= kChunk)

@@ -48,7 +48,19 @@ struct Value {
     if (kind != Number) throw std::invalid_argument("json: number expected");
     return num;
   }
-  long long as_int() const { return (long long)as_double(); }
+  // the number truncated toward zero, as nlohmann's get<int>() converts a float; a value outside
+  // the range of long long (1e999 reads as infinity) is refused instead of converted
+  long long as_int() const {
+    const double x = as_double();
+    if (!(x > -9223372036854775808.0 && x < 9223372036854775808.0))
+      throw std::invalid_argument("json: integer out of range");
+    return (long long)x;
+  }
+  int as_int32() const {
+    const long long v = as_int();
+    if (v < -2147483648LL || v > 2147483647LL) throw std::invalid_argument("json: integer out of range");
+    return (int)v;
+  }
   bool as_bool() const {
     if (kind != Bool) throw std::invalid_argument("json: bool expected");
     return b;

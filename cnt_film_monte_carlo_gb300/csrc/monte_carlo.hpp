@@ -94,7 +94,7 @@ class monte_carlo {
   // monte_carlo.cpp:254-305
   void kubo_init() {
     setup_film();
-    n_sections_ = (int)j_["number of sections for injection region"].as_int();
+    n_sections_ = j_["number of sections for injection region"].as_int32();
     max_time_ = j_["maximum time for kubo simulation [seconds]"].as_double();
   }
 
@@ -105,7 +105,7 @@ class monte_carlo {
   // "maximum time for contacts simulation [seconds]" (the reference's loop never ends).
   void init() {
     setup_film();
-    n_seg_ = (int32_t)j_["number of segments"].as_int();
+    n_seg_ = j_["number of segments"].as_int32();
     int64_t pops[2] = {1100, 0};
     if (j_.has("contact populations"))
       for (int k = 0; k < 2; ++k) pops[k] = j_["contact populations"][k].as_int();

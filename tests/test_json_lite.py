@@ -180,3 +180,21 @@ def test_arbitrary_bytes_are_read_or_refused(roundtrip, tmp_path_factory):
             assert back == json.loads(text.encode("utf-8", "surrogatepass").decode("utf-8"))
 
     check()
+
+
+@pytest.mark.parametrize("text,mode,expect", [
+    ("3.9", "int", b"3"), ("-3.9", "int", b"-3"), ("1e18", "int", b"1000000000000000000"),
+    ("1e999", "int", None), ("-1e999", "int", None), ("9.3e18", "int", None), ('"7"', "int", None),
+    ("2147483647", "int32", b"2147483647"), ("-2147483648", "int32", b"-2147483648"),
+    ("2147483648", "int32", None), ("-2147483649", "int32", None), ("1e10", "int32", None),
+])
+def test_integer_conversions_are_range_checked(roundtrip, tmp_path, text, mode, expect):
+    # the driver reads counts (particles, sections, segments, tracked particles) through these:
+    # a value outside the integer's range is refused, not converted with undefined behaviour
+    p = tmp_path / "in.json"
+    p.write_text(text)
+    r = subprocess.run([str(roundtrip), str(p), mode], capture_output=True)
+    if expect is None:
+        assert r.returncode == 2 and b"json:" in r.stderr, (text, mode, r.returncode, r.stdout)
+    else:
+        assert r.returncode == 0 and r.stdout.strip() == expect, (text, mode, r.stdout, r.stderr)
