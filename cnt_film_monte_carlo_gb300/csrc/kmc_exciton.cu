@@ -1391,8 +1391,18 @@ int kmc_davoody_table(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* accepto
   if (!ctx || !donor || !acceptor || !cfg_ok(cfg) || !theta_deg || !zshift || !ash1 || !ash2 || !theta || !zsh ||
       !a1 || !a2 || !rate)
     return fail(ctx, KMC_ERR_ARG, "kmc_davoody_table: bad arguments");
-  const int64_t nt = (int64_t)theta_deg[2], nz = (int64_t)zshift[2], n1 = (int64_t)ash1[2], n2 = (int64_t)ash2[2];
-  if (nt < 1 || nz < 1 || n1 < 1 || n2 < 1) return fail(ctx, KMC_ERR_ARG, "kmc_davoody_table: empty grid");
+  // point counts: numbers in [1, 2^31 - 1], checked before they are converted; the table at most
+  // 2^34 entries (its geometries are a host array of four doubles each)
+  auto count = [](double x, int64_t& n) {
+    if (!(x >= 1.0 && x <= 2147483647.0)) return false;
+    n = (int64_t)x;
+    return true;
+  };
+  int64_t nt = 0, nz = 0, n1 = 0, n2 = 0;
+  if (!count(theta_deg[2], nt) || !count(zshift[2], nz) || !count(ash1[2], n1) || !count(ash2[2], n2))
+    return fail(ctx, KMC_ERR_ARG, "kmc_davoody_table: a grid's point count is not in [1, 2^31 - 1]");
+  const double entries = (double)nt * (double)nz * (double)n1 * (double)n2;
+  if (entries > 17179869184.0) return fail(ctx, KMC_ERR_ARG, "kmc_davoody_table: table too large");
   // monte_carlo.cpp:65-75: linspace grids, theta scaled by the reference's pi / 180
   linspace(zshift[0], zshift[1], nz, zsh);
   linspace(ash1[0], ash1[1], n1, a1);

@@ -9,6 +9,13 @@ from . import _lib as L
 from .film import Film
 
 
+def _need(ok: bool, msg: str) -> None:
+    """The C ABI reads as many elements as its counts say; a numpy buffer shorter than that is
+    refused here, before its pointer is passed."""
+    if not ok:
+        raise L.KmcError(L.KMC_ERR_ARG, msg)
+
+
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
@@ -63,6 +70,10 @@ class Engine:
         orient = _f64(orient)
         left = np.ascontiguousarray(left, dtype=np.int32)
         right = np.ascontiguousarray(right, dtype=np.int32)
+        _need(offsets.ndim == 1 and len(offsets) >= 2, "load_arrays: offsets needs n_films + 1 entries")
+        n = int(offsets[-1])
+        _need(n >= 0 and pos_m.size == 3 * n and orient.size == 3 * n and left.size == n and right.size == n,
+              f"load_arrays: {n} sites need pos and orient [n][3] and left, right [n]")
         f = L.kmc_film(len(offsets) - 1, L.ptr(offsets, C.c_int64), L.ptr(pos_m, C.c_double),
                        L.ptr(orient, C.c_double), L.ptr(left, C.c_int32), L.ptr(right, C.c_int32))
         self._check(self.lib.kmc_load_film(self.h, C.byref(f)))
@@ -78,6 +89,12 @@ class Engine:
         rate = rate_nd.ravel()
         t = L.kmc_table()
         t.kind = int(table["kind"])
+        _need(len(grids) == (4 if t.kind == L.KMC_TABLE_4D else 2), "set_table: 4 grids for kind 4, 2 otherwise")
+        n_rates = int(np.prod([len(g) for g in grids]))
+        if t.kind == L.KMC_TABLE_2D_SPECIES:
+            _need(rate_nd.ndim == 4 and rate_nd.shape[0] == rate_nd.shape[1], "set_table: kind 3 rate is [S][S][nd][nt]")
+            n_rates *= rate_nd.shape[0] * rate_nd.shape[1]
+        _need(rate.size == n_rates, f"set_table: {rate.size} rates for grids of {n_rates} points")
         for d, g in enumerate(grids):
             t.n[d] = len(g)
             t.grid[d] = L.ptr(g, C.c_double)
@@ -90,13 +107,16 @@ class Engine:
     def set_species(self, species, n_species: int):
         """Chirality index of every loaded site (read by kind-3 tables)."""
         sp = np.ascontiguousarray(species, dtype=np.int32)
+        _need(hasattr(self, "offsets") and sp.size == int(self.offsets[-1]),
+              "set_species: one species per loaded site")
         self._check(self.lib.kmc_set_site_species(self.h, L.ptr(sp, C.c_int32), int(n_species)))
         return self
 
     def build(self, r_max: float) -> dict:
         st = L.kmc_nbr_stats()
         self._check(self.lib.kmc_build_neighbors(self.h, float(r_max), C.byref(st)))
-        return {k: getattr(st, k) for k, _ in L.kmc_nbr_stats._fields_}
+        self._nbr = {k: getattr(st, k) for k, _ in L.kmc_nbr_stats._fields_}
+        return dict(self._nbr)
 
     def set_trace(self, n_trace: int, cap: int):
         self._check(self.lib.kmc_set_trace(self.h, n_trace, cap))
@@ -232,6 +252,9 @@ class Engine:
                                               L.ptr(a["hops"], C.c_int64)))
 
     def neighbors(self, n_sites: int, nnz: int) -> dict:
+        nb = getattr(self, "_nbr", None)
+        _need(nb is not None and int(n_sites) == int(nb["n_sites"]) and int(nnz) == int(nb["nnz"]),
+              "neighbors: n_sites and nnz must be the last build's")
         rowptr = np.zeros(n_sites + 1, np.int64)
         col = np.zeros(max(nnz, 1), np.int32)
         cum = np.zeros(max(nnz, 1))
@@ -282,6 +305,7 @@ class Engine:
     def mlp_set_samples(self, dist, theta, pair, log_rate):
         d, t, lr = _f64(dist), _f64(theta), _f64(log_rate)
         pr = np.ascontiguousarray(pair, dtype=np.int32)
+        _need(t.size == d.size and lr.size == d.size and pr.size == d.size, "mlp_set_samples: arrays of one length")
         self._check(self.lib.kmc_mlp_set_samples(self.h, len(d), L.ptr(d, C.c_double), L.ptr(t, C.c_double),
                                                  L.ptr(pr, C.c_int32), L.ptr(lr, C.c_double)))
         return self
@@ -302,6 +326,7 @@ class Engine:
     def mlp_predict(self, dist, theta, pair) -> np.ndarray:
         d, t = _f64(dist), _f64(theta)
         pr = np.ascontiguousarray(pair, dtype=np.int32)
+        _need(t.size == d.size and pr.size == d.size, "mlp_predict: arrays of one length")
         out = np.zeros(len(d))
         self._check(self.lib.kmc_mlp_predict(self.h, len(d), L.ptr(d, C.c_double), L.ptr(t, C.c_double),
                                              L.ptr(pr, C.c_int32), L.ptr(out, C.c_double)))
@@ -326,6 +351,8 @@ def species_rates(model: dict, dist, theta, donor, acceptor) -> np.ndarray:
     d, t = _f64(dist), _f64(theta)
     a = np.ascontiguousarray(donor, dtype=np.int32)
     b = np.ascontiguousarray(acceptor, dtype=np.int32)
+    _need(t.size == d.size and a.size == d.size and b.size == d.size, "species_rates: arrays of one length")
+    _need(e.size == int(model.get("n_species", e.size)) == dia.size, "species_rates: energy and diameter per species")
     out = np.zeros(len(d))
     rc = lib.kmc_species_rates(C.byref(m), len(d), L.ptr(d, C.c_double), L.ptr(t, C.c_double), L.ptr(a, C.c_int32),
                                L.ptr(b, C.c_int32), L.ptr(out, C.c_double))
@@ -362,6 +389,9 @@ def trim_sites(pos_m, orient, left, right, lim):
     lk = np.ascontiguousarray(left, dtype=np.int32).copy()
     rk = np.ascontiguousarray(right, dtype=np.int32).copy()
     lim = _f64(lim)
+    n = lk.size
+    _need(pos.size == 3 * n and ori.size == 3 * n and rk.size == n and lim.size == 6,
+          "trim_sites: pos and orient [n][3], left and right [n], lim [6]")
     n_out = C.c_int64(0)
     rc = lib.kmc_trim_sites(len(lk), L.ptr(pos, C.c_double), L.ptr(ori, C.c_double), L.ptr(lk, C.c_int32),
                             L.ptr(rk, C.c_int32), L.ptr(lim, C.c_double), C.byref(n_out))

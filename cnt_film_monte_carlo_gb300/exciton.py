@@ -21,6 +21,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib as L
+from . import engine as E
 
 TEMPERATURE = 300.0            # K, exciton_transfer.h:40
 BROADENING = 4e-3 * 1.6e-19     # J (4 meV), exciton_transfer.h:41
@@ -86,6 +87,8 @@ def coulomb_j(engine, donor: Tube, acceptor: Tube, ik_cm_pairs, geometry, precis
     """calculate_J for (donor ik_cm, acceptor ik_cm) pairs at one geometry (complex)."""
     pairs = np.ascontiguousarray(ik_cm_pairs, dtype=np.int32).reshape(-1, 2)
     g = _f64(geometry)
+    if g.size != 4:
+        raise L.KmcError(L.KMC_ERR_ARG, "coulomb_j: geometry is (z_shift, ash1, ash2, theta)")
     out = np.zeros((len(pairs), 2))
     engine._check(engine.lib.kmc_exciton_j(engine.h, donor.h, acceptor.h, len(pairs), L.ptr(pairs, C.c_int32),
                                            L.ptr(g, C.c_double), int(precision), L.ptr(out, C.c_double)))
@@ -109,7 +112,8 @@ def davoody_table(engine, donor: Tube, acceptor: Tube, theta_deg=(0, 180, 21), z
     """create_davoody_scatt_table on the reference's default grids (input.json:47-50): a KMC_TABLE_4D
     table dict for Engine.set_table."""
     specs = [_f64(x) for x in (theta_deg, zshift, ash1, ash2)]
-    n = [int(x[2]) for x in specs]
+    n = [E._grid_n(x, "davoody_table") for x in specs]
+    E._table_size(n, "davoody_table")
     g = [np.zeros(k) for k in n]
     rate = np.zeros(n)
     cfg = _cfg(temperature, broadening, precision)

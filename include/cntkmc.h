@@ -498,7 +498,8 @@ int kmc_exciton_rates(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* accepto
 /* monte_carlo::create_davoody_scatt_table (monte_carlo.cpp:64-153): the first-order rate on the
  * 4-D grid theta (degrees, scaled by the reference's pi / 180) x z_shift x axis shift 1 x axis
  * shift 2 ({start, end, count} linspace each); outputs the grids and rate [nt][nz][n1][n2],
- * the layout of a KMC_TABLE_4D table. */
+ * the layout of a KMC_TABLE_4D table.  KMC_ERR_ARG unless each count is a number in
+ * [1, 2^31 - 1] and the table has at most 2^34 entries. */
 int kmc_davoody_table(kmc_ctx* ctx, const kmc_cnt* donor, const kmc_cnt* acceptor, const kmc_transfer_cfg* cfg,
                       const double theta_deg[3], const double zshift[3], const double ash1[3], const double ash2[3],
                       double* theta, double* zsh, double* a1, double* a2, double* rate);
