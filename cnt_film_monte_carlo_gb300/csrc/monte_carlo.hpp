@@ -290,9 +290,19 @@ class monte_carlo {
 
   // the number of steps of main.cpp's `while (time < max time) step(dt)` from the current time,
   // with the same floating-point accumulation of the time
+  // The number of steps of main.cpp's `while (time < max time)` loop from the current time, with
+  // the loop's own accumulation of the time.  A time step that cannot advance the clock (not
+  // positive, or too small to change it) would make that loop run forever, and one that needs
+  // more than 1e10 steps practically so: both are refused.
   int64_t steps_until(double t_max, double dt) const {
+    if (time_ < t_max && (t_max - time_) / dt > 1e10)
+      throw std::invalid_argument("monte carlo time step: more than 1e10 steps to the maximum time");
     int64_t n = 0;
-    for (double t = time_; t < t_max; t += dt) ++n;
+    for (double t = time_; t < t_max; t += dt) {
+      if (!(dt > 0) || !std::isfinite(dt) || t + dt == t)
+        throw std::invalid_argument("monte carlo time step does not advance the time");
+      ++n;
+    }
     return n;
   }
 

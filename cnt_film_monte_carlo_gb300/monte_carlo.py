@@ -304,9 +304,14 @@ class monte_carlo:  # noqa: N801  (the reference's class name)
 
     def steps_until(self, t_max: float, dt: float) -> int:
         """The number of steps of main.cpp's `while (time < max time)` loop from the current time,
-        with the same floating-point accumulation of the time."""
+        with the same floating-point accumulation of the time.  A time step that cannot advance
+        the time, or needs more than 1e10 steps, is refused (the loop would not end)."""
         n, t = 0, self._time
+        if t < t_max and dt > 0 and (t_max - t) / dt > 1e10:
+            raise ValueError("monte carlo time step: more than 1e10 steps to the maximum time")
         while t < t_max:
+            if not (0 < dt < math.inf) or t + dt == t:  # the loop would never end
+                raise ValueError("monte carlo time step does not advance the time")
             t += dt
             n += 1
         return n

@@ -162,3 +162,32 @@ def test_python_driver_refuses_non_json_numbers(tmp_path, literal):
     p.write_text('{"exciton monte carlo": {"monte carlo time step": %s}}' % literal)
     with pytest.raises(ValueError, match="not a JSON number"):
         M.run(str(p))
+
+
+@pytest.mark.parametrize("dt", [0.0, -1e-15, float("nan"), float("inf"), 1e-40])
+def test_time_steps_that_never_reach_the_end_are_refused(dt):
+    # main.cpp's `while (time < max time) { time += dt; ... }` never ends for these steps; the
+    # driver refuses them instead of looping (a NaN step would compare false and run 0 steps in
+    # the reference's loop, but it is refused here too)
+    sim = object.__new__(M.monte_carlo)
+    sim._time = 0.0
+    with pytest.raises(ValueError, match="time step"):
+        sim.steps_until(1e-12, dt)
+
+
+def test_time_step_stuck_on_a_large_clock_is_refused():
+    sim = object.__new__(M.monte_carlo)
+    sim._time = 1.0  # 1e-20 s is below half an ulp of 1 s: the sum stays at 1.0
+    with pytest.raises(ValueError, match="time step"):
+        sim.steps_until(1.0 + 1e-9, 1e-20)
+
+
+def test_step_count_follows_the_reference_accumulation():
+    sim = object.__new__(M.monte_carlo)
+    sim._time = 0.0
+    n, t = 0, 0.0
+    while t < 1e-12:
+        t += 1e-15
+        n += 1
+    assert sim.steps_until(1e-12, 1e-15) == n
+    assert sim.steps_until(0.0, 1e-15) == 0

@@ -227,3 +227,18 @@ def test_corrupt_saved_table_is_refused(tmp_path):
         assert r.returncode != 0 and "not a number" in r.stdout + r.stderr, (target, r.stdout, r.stderr)
         with pytest.raises(ValueError):
             MC.run(cfg)
+
+
+@pytest.mark.parametrize("dt", [0.0, -1e-15, 1e-40])
+def test_time_steps_that_never_reach_the_end_are_refused_by_the_driver(dt, tmp_path):
+    # main.cpp's loop `while (time < max time)` would never end with these steps
+    d = load_case(CASES[0])
+    cfg = _input_json(d, str(tmp_path), "mixed")
+    with open(cfg) as f:
+        j = json.load(f)
+    j["exciton monte carlo"]["monte carlo time step"] = dt
+    with open(cfg, "w") as f:
+        json.dump(j, f)
+    B.build()
+    r = subprocess.run([B.DRIVER, cfg], capture_output=True, text=True, timeout=300)
+    assert r.returncode != 0 and "time step" in r.stdout + r.stderr, (r.returncode, r.stdout, r.stderr)
