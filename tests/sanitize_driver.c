@@ -175,6 +175,37 @@ int main(int argc, char** argv) {
     int32_t *l = malloc(sizeof(int32_t) * nt * np), *r = malloc(sizeof(int32_t) * nt * np);
     CHECK(kmc_read_mesh(argv[1], &nt, &np, p, o, l, r) == KMC_OK);
     free(p), free(o), free(l), free(r);
+    /* a token that is not a number, appended to one file: refused, not read short */
+    char path[4096];
+    snprintf(path, sizeof path, "%s/single_cnt.pos.y.dat", argv[1]);
+    FILE* f = fopen(path, "a");
+    CHECK(f != NULL);
+    fprintf(f, " 1 x\n");
+    fclose(f);
+    CHECK(kmc_read_mesh(argv[1], &nt, &np, NULL, NULL, NULL, NULL) == KMC_ERR_IO);
+  }
+  { /* refusals: nothing is read or written past the inputs */
+    int32_t *l = malloc(sizeof(int32_t) * n), *l0 = malloc(sizeof(int32_t) * n);
+    double *p = malloc(sizeof(double) * 3 * n), *o = malloc(sizeof(double) * 3 * n);
+    int32_t* r = malloc(sizeof(int32_t) * n);
+    memcpy(l, left, sizeof(int32_t) * n);
+    memcpy(r, right, sizeof(int32_t) * n);
+    memcpy(p, pos, sizeof(double) * 3 * n);
+    memcpy(o, orient, sizeof(double) * 3 * n);
+    l[3] = (int32_t)n + 5; /* a link past the film */
+    memcpy(l0, l, sizeof(int32_t) * n);
+    const double lim[6] = {-1e-6, 1e-6, 2e-9, 1e-6, -1e-6, 1e-6};
+    int64_t kept = -1;
+    CHECK(kmc_trim_sites(n, p, o, l, r, lim, &kept) == KMC_ERR_ARG && kept == -1);
+    CHECK(memcmp(l, l0, sizeof(int32_t) * n) == 0 && memcmp(p, pos, sizeof(double) * 3 * n) == 0);
+    free(l), free(l0), free(p), free(o), free(r);
+    const double bad_counts[4] = {NAN, 0.5, -3.0, 1e300};
+    for (int k = 0; k < 4; ++k) {
+      const double dd[3] = {0.5e-9, 10e-9, bad_counts[k]};
+      CHECK(kmc_forster2d_table(1e15, dd, th2, g0, g1, r2) == KMC_ERR_ARG);
+      const double zz[3] = {1e-9, 2e-9, bad_counts[k]};
+      CHECK(kmc_forster_table(1e15, th4, zz, a1, a2, h0, h1, h2, h3, r4) == KMC_ERR_ARG);
+    }
   }
   free(g0), free(g1), free(r2), free(h0), free(h1), free(h2), free(h3), free(r4);
   free(pos), free(orient), free(left), free(right);

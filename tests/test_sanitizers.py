@@ -3,7 +3,8 @@
 tests/sanitize_driver.c exercises oracle/kmc_oracle.c (every entry point the tests use: tables,
 neighbour lists, both hop paths, batched MSD, contacts mode, tracks, trim) and
 cnt_film_monte_carlo_gb300/csrc/kmc_host.cpp (trim, domain, tables, the closed-form labeller,
-the diffusion fit, the mesh reader).  Compiled with -fsanitize=address,undefined and run with
+the diffusion fit, the mesh reader), including their refusals (a link past the film, a grid
+count that is NaN, fractional, negative or huge, a mesh file with a token that is not a number).  Compiled with -fsanitize=address,undefined and run with
 halt_on_error: any out-of-bounds access, leak or undefined operation fails the test.  CPU only.
 """
 import os
