@@ -440,6 +440,7 @@ int kmc_set_rate_table(kmc_ctx* c, const kmc_table* t) try {
   c->table.kind = t->kind;
   for (int d = 0; d < dims; ++d) {
     if (t->n[d] < 1 || !t->grid[d]) FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: grid %d empty", d);
+    if (t->n[d] > (int64_t(1) << 34) / nr) FAIL(c, KMC_ERR_ARG, "kmc_set_rate_table: more than 2^34 rates");
     nr *= t->n[d];
     CK(c, upload(c->d_grid[d], t->grid[d], t->n[d], c->stream));
     c->table.n[d] = t->n[d];

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -90,7 +91,7 @@ class Engine:
         t = L.kmc_table()
         t.kind = int(table["kind"])
         _need(len(grids) == (4 if t.kind == L.KMC_TABLE_4D else 2), "set_table: 4 grids for kind 4, 2 otherwise")
-        n_rates = int(np.prod([len(g) for g in grids]))
+        n_rates = math.prod(len(g) for g in grids)  # Python integers: no wrap-around
         if t.kind == L.KMC_TABLE_2D_SPECIES:
             _need(rate_nd.ndim == 4 and rate_nd.shape[0] == rate_nd.shape[1], "set_table: kind 3 rate is [S][S][nd][nt]")
             n_rates *= rate_nd.shape[0] * rate_nd.shape[1]

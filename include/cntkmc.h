@@ -108,7 +108,9 @@ const char* kmc_last_error(const kmc_ctx* ctx);
  * trim_scats :722-782, which the host applies with kmc_trim_sites). */
 int kmc_load_film(kmc_ctx* ctx, const kmc_film* film);
 
-/* Copy a rate table to the device (replaces set_scat_table, monte_carlo.h:419-423). */
+/* Copy a rate table to the device (replaces set_scat_table, monte_carlo.h:419-423).  Reads
+ * n[0] x n[1] (x n[2] x n[3] for kind 4; x S^2 for kind 3) rates; KMC_ERR_ARG for an empty grid
+ * or more than 2^34 rates. */
 int kmc_set_rate_table(kmc_ctx* ctx, const kmc_table* table);
 
 /* Chirality index of every loaded site, species[n_sites] in [0, n_species) (no counterpart in

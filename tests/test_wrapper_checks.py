@@ -105,3 +105,11 @@ def test_exciton_wrappers_check_geometry_and_grids():
     refused(X.davoody_table, e, None, None, zshift=(1e-9, 2e-9, float("nan")))
     big = (0.0, 1.0, 2**31 - 1)
     refused(X.davoody_table, e, None, None, theta_deg=big, zshift=big, ash1=big, ash2=big)
+
+
+def test_rate_counts_are_exact_for_huge_grids():
+    # the rate count of a table is the exact product of its grid lengths (np.prod would wrap in
+    # int64 for grids whose product passes 2^63): 2^16 points per grid is 2^64 rates, refused
+    e = bare_engine()
+    g = np.zeros(1 << 16)
+    refused(e.set_table, {"kind": 4, "grids": [g, g, g, g], "rate": np.zeros(1)})
