@@ -740,6 +740,10 @@ int kmc_build_neighbors(kmc_ctx* c, double r_max, kmc_nbr_stats* st) try {
 int kmc_set_trace(kmc_ctx* c, int64_t n_trace, int64_t cap) try {
   if (!c) return KMC_ERR_ARG;
   if (n_trace < 0 || cap < 0 || (n_trace > 0 && cap == 0)) FAIL(c, KMC_ERR_ARG, "kmc_set_trace: bad sizes");
+  // the trace buffer holds n_trace x cap entries, which the hop kernels index as t * cap + k:
+  // the product is bounded (2^36 entries, 256 GiB) so that it can neither wrap nor be sized short
+  if (n_trace > 0 && cap > (int64_t(1) << 36) / n_trace)
+    FAIL(c, KMC_ERR_ARG, "kmc_set_trace: n_trace x cap above 2^36 entries");
   c->n_trace = n_trace;
   c->trace_cap = cap;
   drop_excitons(c);

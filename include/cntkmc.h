@@ -223,7 +223,8 @@ int kmc_get_neighbors(kmc_ctx* ctx, int64_t* rowptr, int32_t* col, double* cum, 
 
 /* Hop trace of excitons [0, n_trace) of film 0, cap entries each (must be set before
  * kmc_init_excitons): update_state result -> site; free-flight crossing -> -1 - site;
- * reinjection -> INT32_MIN then the new site.  get returns the number of events recorded. */
+ * reinjection -> INT32_MIN then the new site.  get returns the number of events recorded.
+ * KMC_ERR_ARG for negative sizes or n_trace x cap above 2^36 entries. */
 int kmc_set_trace(kmc_ctx* ctx, int64_t n_trace, int64_t cap);
 int64_t kmc_get_trace(kmc_ctx* ctx, int64_t exciton, int32_t* out, int64_t cap);
 

@@ -261,6 +261,11 @@ def test_argument_errors():
     e.build(r_max)
     with pytest.raises(L.KmcError):
         e.init_excitons(10, 1, L.KMC_INJECT_REGION, 4)  # even number of sections
+    for n_trace, cap in ((1 << 20, 1 << 17), (2**62, 2**2), (-1, 8), (4, 0)):  # too large to index, or bad
+        with pytest.raises(L.KmcError) as ex:
+            e.set_trace(n_trace, cap)
+        assert ex.value.code == L.KMC_ERR_ARG
+    e.set_trace(4, 1 << 10)
     e.close()
 
 
