@@ -808,6 +808,9 @@ int kmc_init_excitons(kmc_ctx* c, const kmc_inject* inj) try {
     }
     if (ne > 0 && fd.n_inj == 0) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: film %d has no injection site", i);
     if (fd.n_inj >= (1LL << 31)) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: too many injection sites");
+    // every exciton holds ~80 bytes of state on the device: 2^31 slots (~170 GB) is past what
+    // one GPU holds, and the bound keeps the slot arithmetic below far from overflow
+    if (ne > (1LL << 31) - slot) FAIL(c, KMC_ERR_ARG, "kmc_init_excitons: more than 2^31 excitons");
     fd.slot0 = slot;
     fd.n_exc = ne;
     int64_t padded = (ne + 31) / 32 * 32;
@@ -1631,7 +1634,7 @@ int kmc_autotune(kmc_ctx* c, double dt, double v, int64_t trial_steps, kmc_tune_
 
 int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) try {
   if (!c) return KMC_ERR_ARG;
-  if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
+  if (!out || first < 0 || count < 0 || count > c->steps_done - first) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
   if (count == 0) return KMC_OK;
   CK(c, cudaSetDevice(c->device));
   kmc::NvtxRange nv("kmc_get_msd_batches");
@@ -1647,7 +1650,7 @@ int kmc_get_msd_batches(kmc_ctx* c, int64_t first, int64_t count, double* out) t
 int kmc_get_msd(kmc_ctx* c, int64_t first, int64_t count, double* out) try {
   if (!c) return KMC_ERR_ARG;
   if (c->msd_batches == 1) return kmc_get_msd_batches(c, first, count, out);
-  if (!out || first < 0 || count < 0 || first + count > c->steps_done) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
+  if (!out || first < 0 || count < 0 || count > c->steps_done - first) FAIL(c, KMC_ERR_ARG, "kmc_get_msd: range outside the steps run");
   kmc::NvtxRange nv("kmc_get_msd: batch reduce");
   const int64_t B = c->msd_batches;
   std::vector<double> tmp((size_t)c->n_films * count * B * 3);
@@ -2044,7 +2047,7 @@ int kmc_mlp_set_samples(kmc_ctx* c, int64_t n, const double* dist, const double*
 int kmc_mlp_gradient(kmc_ctx* c, int64_t first, int64_t count, float* grad, double* loss) try {
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready || c->mlp_n_samples == 0) FAIL(c, KMC_ERR_STATE, "kmc_mlp_gradient: set parameters and samples first");
-  if (first < 0 || count < 1 || first + count > c->mlp_n_samples || !grad)
+  if (first < 0 || count < 1 || count > c->mlp_n_samples - first || !grad)
     FAIL(c, KMC_ERR_ARG, "kmc_mlp_gradient: samples [%lld, +%lld) outside [0, %lld)", (long long)first, (long long)count,
          (long long)c->mlp_n_samples);
   CK(c, cudaSetDevice(c->device));
@@ -2175,6 +2178,8 @@ int kmc_mlp_rate_table(kmc_ctx* c, int32_t nd, const double* dist, int32_t nt, c
   if (!c) return KMC_ERR_ARG;
   if (!c->mlp_ready) FAIL(c, KMC_ERR_STATE, "kmc_mlp_rate_table: call kmc_mlp_init first");
   if (nd < 1 || nt < 1 || !dist || !theta || !rate) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: empty grid");
+  if ((int64_t)nd * nt > (int64_t(1) << 34) / ((int64_t)c->mlp_shape.n_species * c->mlp_shape.n_species))
+    FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: more than 2^34 rates");
   for (int32_t i = 0; i < nd; ++i)
     if (!(dist[i] > 0) || !std::isfinite(dist[i])) FAIL(c, KMC_ERR_ARG, "kmc_mlp_rate_table: distance %d is %g", i, dist[i]);
   for (int32_t i = 0; i < nt; ++i)

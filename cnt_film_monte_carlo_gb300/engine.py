@@ -336,6 +336,7 @@ class Engine:
     def mlp_rate_table(self, dist, theta) -> np.ndarray:
         d, t = _f64(dist), _f64(theta)
         S = self.mlp_species
+        _table_size((S, S, len(d), len(t)), "mlp_rate_table")
         out = np.zeros((S, S, len(d), len(t)))
         self._check(self.lib.kmc_mlp_rate_table(self.h, len(d), L.ptr(d, C.c_double), len(t), L.ptr(t, C.c_double),
                                                 L.ptr(out, C.c_double)))

@@ -125,7 +125,8 @@ int kmc_set_site_species(kmc_ctx* ctx, const int32_t* species, int32_t n_species
 int kmc_build_neighbors(kmc_ctx* ctx, double max_hopping_radius, kmc_nbr_stats* stats);
 
 /* Create the excitons (replaces injection_region / get_removal_domain / kubo_create_particles,
- * monte_carlo.cpp:203-251,308-316, and the particle constructor particle.h:48-52). */
+ * monte_carlo.cpp:203-251,308-316, and the particle constructor particle.h:48-52).  At most
+ * 2^31 excitons over all films. */
 int kmc_init_excitons(kmc_ctx* ctx, const kmc_inject* inject);
 
 /* n_steps calls of kubo_step(dt) (monte_carlo.cpp:319-342; particle::step particle.cpp:57-80;
@@ -426,7 +427,7 @@ int kmc_mlp_predict(kmc_ctx* ctx, int64_t n, const double* dist, const double* t
                     double* log_rate);
 
 /* A KMC_TABLE_2D_SPECIES rate table from the network: rate[S][S][nd][nt] = exp(predicted ln rate)
- * on the grids dist[nd] (m) and theta[nt] (rad). */
+ * on the grids dist[nd] (m) and theta[nt] (rad); at most 2^34 rates. */
 int kmc_mlp_rate_table(kmc_ctx* ctx, int32_t nd, const double* dist, int32_t nt, const double* theta, double* rate);
 
 /* Library version string. */

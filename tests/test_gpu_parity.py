@@ -266,6 +266,9 @@ def test_argument_errors():
             e.set_trace(n_trace, cap)
         assert ex.value.code == L.KMC_ERR_ARG
     e.set_trace(4, 1 << 10)
+    with pytest.raises(L.KmcError) as ex:  # refused before anything is allocated
+        e.init_excitons(2**31 + 1, 1, L.KMC_INJECT_UNIFORM)
+    assert ex.value.code == L.KMC_ERR_ARG and "2^31" in str(ex.value)
     e.close()
 
 

@@ -130,6 +130,21 @@ def test_rate_table_is_the_network_on_the_grid():
     np.testing.assert_allclose(np.log(tab.ravel()), pred, rtol=0, atol=1e-12)
 
 
+def test_rate_table_past_2_to_34_rates_is_refused():
+    # refused from the counts alone, before the grids are read or anything is allocated
+    import ctypes as C
+
+    e = engine_with_net(S=3, seed=3)
+    one = np.ones(1)
+    out = np.zeros(1)
+    rc = e.lib.kmc_mlp_rate_table(e.h, 1 << 20, L.ptr(one, C.c_double), 1 << 20, L.ptr(one, C.c_double),
+                                  L.ptr(out, C.c_double))
+    assert rc == L.KMC_ERR_ARG and "2^34" in e.lib.kmc_last_error(e.h).decode()
+    with pytest.raises(L.KmcError):
+        e.mlp_rate_table(np.ones(1 << 16), np.ones(1 << 16))
+    e.close()
+
+
 def mixed_film(seed=3, n_tubes=40, length=30.0, box=(60.0, 60.0, 8.0), S=4):
     f = F.straight_tubes(n_tubes, length, box, 5.0, 1.0, seed)
     tube_sp = np.random.default_rng(seed).integers(0, S, n_tubes)
