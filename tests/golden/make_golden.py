@@ -40,11 +40,39 @@ CASES = {
     "ref_wong_region": dict(tubes=10, length=30.0, box=(40, 40, 8), film_seed=11, rate="wong",
                             trim=([-1e-6, 1e-6], [2e-9, 38e-9], [-1e-6, 1e-6]), r_max=12e-9, sections=5,
                             n_exc=150, dt=2e-13, steps=30, seed=7, n_trace=16),
+    # a T-junction and a crossing, with sites at whole nanometres and a 2 nm cutoff: many sites lie
+    # exactly on cell boundaries (x - xmin = k r), where create_scatterer_buckets' truncating
+    # division and the 27-cell order decide the order of every neighbour row
+    "ref_tjunction_cells": dict(film="tjunction", rate="forster", trim=([-1e-6, 1e-6], [-1e-6, 1e-6], [-1e-6, 1e-6]),
+                                r_max=2e-9, sections=3, n_exc=120, dt=2e-14, steps=40, seed=21, n_trace=16),
 }
 
 
+def tjunction_film(n_pts=9):
+    """Six tubes of n_pts sites 1 nm apart (nm): A along x at y = z = 0; B along y from (4, 1, 0),
+    ending 1 nm from A's middle site (a T-junction); C along x at y = 4, z = 1, crossing 1 nm over
+    B; D along z at (4, 4.5); E and F along x off the grid, at (y, z) = (2.5, 2.5) and (7.5, 6)
+    starting at x = 0.5."""
+    tubes = [((0.0, 0.0, 0.0), (1.0, 0.0, 0.0)), ((4.0, 1.0, 0.0), (0.0, 1.0, 0.0)),
+             ((0.0, 4.0, 1.0), (1.0, 0.0, 0.0)), ((4.0, 4.5, 0.0), (0.0, 0.0, 1.0)),
+             ((0.5, 2.5, 2.5), (1.0, 0.0, 0.0)), ((0.5, 7.5, 6.0), (1.0, 0.0, 0.0))]
+    pos, ori, left, right = [], [], [], []
+    for t, (p0, u) in enumerate(tubes):
+        for k in range(n_pts):
+            i = t * n_pts + k
+            pos.append(tuple(p0[c] + k * u[c] for c in range(3)))
+            ori.append(u)
+            left.append(i - 1 if k > 0 else -1)
+            right.append(i + 1 if k < n_pts - 1 else -1)
+    return F.Film(np.array(pos), np.array(ori), np.array(left, np.int32), np.array(right, np.int32),
+                  np.arange(0, len(tubes) * n_pts + 1, n_pts, dtype=np.int64))
+
+
 def make_case(name, c, tmp):
-    f = F.straight_tubes(c["tubes"], c["length"], box_nm=c["box"], seed=c["film_seed"])
+    if c.get("film") == "tjunction":
+        f = tjunction_film()
+    else:
+        f = F.straight_tubes(c["tubes"], c["length"], box_nm=c["box"], seed=c["film_seed"])
     mesh = os.path.join(tmp, name, "mesh")
     F.write_mesh(f, mesh)
     mc = {

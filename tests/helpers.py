@@ -10,7 +10,7 @@ from cnt_film_monte_carlo_gb300 import film as F
 from oracle import oracle as O
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ("ref_forster_region", "ref_wong_region")
+CASES = ("ref_forster_region", "ref_wong_region", "ref_tjunction_cells")
 CONTACT_CASES = ("ref_contacts_5seg", "ref_contacts_8seg", "ref_contacts_grid", "ref_contacts_grid2")
 
 
