@@ -588,3 +588,19 @@ def test_bad_table_values_follow_the_oracle(kind, precision):
     assert e.stats()["hops"] == sim.total_hops()
     np.testing.assert_allclose(e.msd(0, steps).ravel(), om.ravel(), rtol=MSD_RTOL, atol=0)
     e.close()
+
+
+def test_empty_injection_region_is_refused():
+    # the central injection cell of this trimmed film holds no site: the reference divides by
+    # zero there (std::rand() % 0, monte_carlo.cpp:311); the engine refuses, as the oracle does
+    f = F.straight_tubes(14, 25.0, box_nm=(40, 40, 8), seed=5)
+    pos, ori, lk, rk = E.trim_sites(f.pos_m(), f.orient, f.left, f.right, [5e-9, 35e-9, -1, 1, -1, 1])
+    e = E.Engine(0)
+    e.load_arrays(np.array([0, len(lk)], np.int64), pos, ori, lk, rk)
+    e.set_table(tables.forster_2d(1e13))
+    e.build(6e-9)
+    with pytest.raises(L.KmcError) as ex:
+        e.init_excitons(96, 3, L.KMC_INJECT_REGION, 5)
+    assert ex.value.code == L.KMC_ERR_ARG and "no injection site" in str(ex.value)
+    e.init_excitons(96, 3, L.KMC_INJECT_REGION, 3)  # the 3-section region holds sites
+    e.close()

@@ -93,3 +93,103 @@ def test_live_reference_matches_oracle(tmp_path):
     msd = sim.step(5e-14, 12)
     assert np.array_equal(msd.ravel(), R["msd"])
     assert np.array_equal(sim.excitons()["pos"].ravel(), R["xpos"])
+
+
+def _golden_script():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(__file__), "golden",
+                                                                              "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+LIVE = {
+    # film, rate type, cutoff, sections, dt, steps, seed, trim (x, y limits)
+    "wong_trimmed": (("random", 14, 25.0, (40, 40, 8), 5), "wong", 6e-9, 3, 1e-13, 15, 3, ([5e-9, 35e-9], [-1, 1])),
+    "long_tubes": (("random", 6, 60.0, (30, 30, 3), 77), "forster", 12e-9, 3, 2e-14, 20, 8, ([-1, 1], [3e-9, 27e-9])),
+    "tjunction": (("tjunction",), "forster", 2e-9, 3, 3e-14, 25, 13, ([-1, 1], [-1, 1])),
+    "grid_cells": (("grid",), "wong", 3e-9, 3, 5e-14, 20, 4, ([-1, 1], [-1, 1])),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LIVE))
+def test_live_reference_matches_oracle_on_more_films(name, tmp_path):
+    """Films of other shapes against the reference run right now: random films trimmed along x or
+    y with both rate types, and two hand-built films whose sites lie on cell boundaries (a
+    T-junction with a crossing; a grid of parallel tubes).  Neighbour rows, injection and removal
+    lists, every exciton's final state and the MSD sums must be equal bit for bit."""
+    if not os.path.exists(O.REF_BIN):
+        pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
+    import json
+
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    film, rate, r_max, sections, dt, steps, seed, (xlim, ylim) = LIVE[name]
+    mg = _golden_script()
+    if film[0] == "random":
+        f = F.straight_tubes(film[1], film[2], box_nm=film[3], seed=film[4])
+    elif film[0] == "tjunction":
+        f = mg.tjunction_film()
+    else:
+        f = mg.grid_film()
+    F.write_mesh(f, str(tmp_path / "mesh"))
+    grids = {"theta [degrees]": [0, 180, 21], "zshift [m]": [1.5e-9, 10e-9, 11],
+             "axis shift 1 [m]": [-10e-9, 10e-9, 11], "axis shift 2 [m]": [-10e-9, 10e-9, 11]}
+    mc = {"mesh input directory": str(tmp_path / "mesh"), "output directory": str(tmp_path / "out"),
+          "keep old results": False, "rate type": rate, **grids, "max hopping radius [m]": r_max,
+          "trim limits": {"xlim": xlim, "ylim": ylim, "zlim": [-1, 1]}, "exciton velocity [m/s]": 2e5,
+          "monte carlo time step": dt, "number of sections for injection region": sections,
+          "maximum time for kubo simulation [seconds]": dt * steps, "number of particles for kubo simulation": 96}
+    p = tmp_path / "in.json"
+    p.write_text(json.dumps({"exciton monte carlo": mc}))
+    _, R = O.run_reference(str(p), str(tmp_path / "r.bin"), steps, seed, dump_csr=True)
+    pos, ori, lk, rk = O.trim(f.pos_m(), f.orient, f.left, f.right, [*xlim, *ylim, -1, 1])
+    assert np.array_equal(pos.ravel(), R["pos"]) and np.array_equal(lk, R["left"])
+    gamma = 1e15 if rate == "forster" else 1e13
+    sim = O.Sim(pos, ori, lk, rk, O.forster_table(gamma, *grids.values()), r_max, 2e5)
+    csr = sim.build_csr()
+    for k in ("rowptr", "col", "cum"):
+        assert np.array_equal(csr[k], R["csr_" + k]), k
+    sim.create_excitons(0, sections, 96, seed)
+    assert sim.n_inject() == len(R["inject"])
+    msd = sim.step(dt, steps)
+    e = sim.excitons()
+    assert np.array_equal(msd.ravel(), R["msd"])
+    for k, rk_ in (("site", "site"), ("pos", "xpos"), ("delta", "delta"), ("ff", "ff"), ("draws", "draws")):
+        assert np.array_equal(e[k].ravel(), R[rk_]), k
+    assert sim.total_hops() == int(R["hops"][0]) > 0
+
+
+def test_empty_injection_region_is_refused_where_the_reference_divides_by_zero(tmp_path):
+    """A film whose central injection cell holds no site: the reference draws
+    std::rand() % _inject_scats.size() with an empty list (monte_carlo.cpp:311, an integer
+    division by zero: the process dies with SIGFPE); the oracle, like the engine, refuses the
+    set-up with an error instead."""
+    if not os.path.exists(O.REF_BIN):
+        pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
+    import json
+    import signal
+    import subprocess
+
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    f = F.straight_tubes(14, 25.0, box_nm=(40, 40, 8), seed=5)
+    F.write_mesh(f, str(tmp_path / "mesh"))
+    grids = {"theta [degrees]": [0, 180, 21], "zshift [m]": [1.5e-9, 10e-9, 11],
+             "axis shift 1 [m]": [-10e-9, 10e-9, 11], "axis shift 2 [m]": [-10e-9, 10e-9, 11]}
+    mc = {"mesh input directory": str(tmp_path / "mesh"), "output directory": str(tmp_path / "out"),
+          "keep old results": False, "rate type": "wong", **grids, "max hopping radius [m]": 6e-9,
+          "trim limits": {"xlim": [5e-9, 35e-9], "ylim": [-1, 1], "zlim": [-1, 1]}, "exciton velocity [m/s]": 2e5,
+          "monte carlo time step": 1e-13, "number of sections for injection region": 5,
+          "maximum time for kubo simulation [seconds]": 1.5e-12, "number of particles for kubo simulation": 96}
+    p = tmp_path / "in.json"
+    p.write_text(json.dumps({"exciton monte carlo": mc}))
+    with pytest.raises(subprocess.CalledProcessError) as ei:
+        O.run_reference(str(p), str(tmp_path / "r.bin"), 15, 3)
+    assert ei.value.returncode == -signal.SIGFPE
+    pos, ori, lk, rk = O.trim(f.pos_m(), f.orient, f.left, f.right, [5e-9, 35e-9, -1, 1, -1, 1])
+    sim = O.Sim(pos, ori, lk, rk, O.forster_table(1e13, *grids.values()), 6e-9, 2e5)
+    with pytest.raises(RuntimeError):
+        sim.create_excitons(0, 5, 96, 3)
