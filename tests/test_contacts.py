@@ -141,3 +141,62 @@ def test_flux_gradient_diffusion_from_reference_files(name):
     fin = np.isfinite(exact) & np.isfinite(got)
     assert fin.any()
     np.testing.assert_allclose(got[fin], exact[fin], rtol=1e-5)
+
+
+LIVE_CONTACTS = {
+    # film, cutoff, segments, dt, steps, seed, (xlim, ylim)
+    "tjunction_3seg": (("tjunction",), 2.5e-9, 3, 2e-14, 12, 17, ([-1, 1], [-1, 1])),
+    "random_6seg": (("random", 16, 30.0, (50, 50, 5), 9), 8e-9, 6, 2e-14, 10, 31, ([4e-9, 46e-9], [-1, 1])),
+    "grid_5seg": (("grid",), 2e-9, 5, 3e-14, 10, 2, ([-1, 1], [-1, 1])),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LIVE_CONTACTS))
+def test_oracle_contacts_equals_the_live_reference(name, tmp_path):
+    """More films through the reference's own contacts mode, run right now: slab populations,
+    interface currents, live counts and every exciton slot equal the oracle's bit for bit."""
+    import json
+    import os
+
+    if not os.path.exists(O.REF_CONTACTS_BIN):
+        pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
+    import importlib.util
+
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(os.path.dirname(__file__), "golden", "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    film, r_max, n_seg, dt, steps, seed, (xlim, ylim) = LIVE_CONTACTS[name]
+    if film[0] == "random":
+        f = F.straight_tubes(film[1], film[2], box_nm=film[3], seed=film[4])
+    elif film[0] == "tjunction":
+        f = mg.tjunction_film()
+    else:
+        f = mg.grid_film()
+    F.write_mesh(f, str(tmp_path / "mesh"))
+    mc = {"mesh input directory": str(tmp_path / "mesh"), "output directory": str(tmp_path / "out"),
+          "keep old results": False, "rate type": "forster", "zshift [m]": [1.5e-9, 10e-9, 11],
+          "axis shift 1 [m]": [-10e-9, 10e-9, 11], "axis shift 2 [m]": [-10e-9, 10e-9, 11],
+          "theta [degrees]": [0, 180, 21], "max hopping radius [m]": r_max,
+          "trim limits": {"xlim": xlim, "ylim": ylim, "zlim": [-1, 1]}, "exciton velocity [m/s]": 2e5,
+          "monte carlo time step": dt, "number of segments": n_seg}
+    p = tmp_path / "in.json"
+    p.write_text(json.dumps({"exciton monte carlo": mc}))
+    _, R = O.run_reference_contacts(str(p), str(tmp_path / "ref.bin"), steps, seed)
+    d = {"film_pos_nm": f.pos_nm, "film_orient": f.orient, "film_left": f.left, "film_right": f.right,
+         "config": mc, "steps": steps, "seed": seed, **{"ref_" + k: v for k, v in R.items()}}
+    sim, geo, pop, cur, live, c = oracle_contacts(d)
+    assert np.array_equal(geo["area"], d["ref_area"])
+    assert tuple(geo["n_contact"]) == (len(d["ref_contact1"]), len(d["ref_contact2"]))
+    assert np.array_equal(pop.ravel(), d["ref_pop"]) and np.array_equal(cur.ravel(), d["ref_curr"])
+    assert np.array_equal(live, d["ref_n_live"]) and pop.sum() > 0
+    Rs = ref_slots(d)
+    o = sim.excitons()
+    ns = len(Rs["site"])
+    assert (o["site"][ns:] == -1).all() and np.array_equal(o["site"][:ns], Rs["site"])
+    m = Rs["live"]
+    for k in ("heading", "ff", "pos"):
+        assert np.array_equal(o[k][:ns][m], Rs[k][m]), k
+    assert np.array_equal(o["draws"][:ns], Rs["draws"]) and np.array_equal(o["hops"][:ns], Rs["hops"])
