@@ -193,3 +193,57 @@ def test_empty_injection_region_is_refused_where_the_reference_divides_by_zero(t
     sim = O.Sim(pos, ori, lk, rk, O.forster_table(1e13, *grids.values()), 6e-9, 2e5)
     with pytest.raises(RuntimeError):
         sim.create_excitons(0, 5, 96, 3)
+
+
+def test_live_reference_matches_oracle_on_random_set_ups(tmp_path_factory):
+    """Random small set-ups (film, trim, cutoff, rate type, sections, time step, seeds) through the
+    reference and the oracle: rows, injection, final states and MSD sums equal bit for bit.  A
+    set-up whose injection cell holds no site is skipped (the reference divides by zero there)."""
+    if not os.path.exists(O.REF_BIN):
+        pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    import json
+
+    from cnt_film_monte_carlo_gb300 import film as F
+
+    grids = {"theta [degrees]": [0, 180, 21], "zshift [m]": [1.5e-9, 10e-9, 11],
+             "axis shift 1 [m]": [-10e-9, 10e-9, 11], "axis shift 2 [m]": [-10e-9, 10e-9, 11]}
+
+    @hyp.settings(max_examples=60, deadline=None, database=None,
+                  suppress_health_check=[hyp.HealthCheck.filter_too_much, hyp.HealthCheck.too_slow])
+    @hyp.given(st.integers(2, 12), st.floats(5.0, 40.0), st.integers(0, 10**6), st.sampled_from(["forster", "wong"]),
+               st.floats(2e-9, 12e-9), st.sampled_from([3, 5]), st.floats(5e-15, 2e-13), st.integers(1, 12),
+               st.integers(0, 2**31 - 1), st.floats(0.0, 0.3))
+    def check(n_tubes, length, film_seed, rate, r_max, sections, dt, steps, seed, cut):
+        d = tmp_path_factory.mktemp("live")
+        f = F.straight_tubes(n_tubes, length, box_nm=(40, 40, 6), seed=film_seed)
+        F.write_mesh(f, str(d / "mesh"))
+        xlim = [cut * 40e-9, (1 - cut) * 40e-9]
+        mc = {"mesh input directory": str(d / "mesh"), "output directory": str(d / "out"),
+              "keep old results": False, "rate type": rate, **grids, "max hopping radius [m]": r_max,
+              "trim limits": {"xlim": xlim, "ylim": [-1, 1], "zlim": [-1, 1]}, "exciton velocity [m/s]": 2e5,
+              "monte carlo time step": dt, "number of sections for injection region": sections,
+              "maximum time for kubo simulation [seconds]": dt * steps,
+              "number of particles for kubo simulation": 48}
+        pos, ori, lk, rk = O.trim(f.pos_m(), f.orient, f.left, f.right, [*xlim, -1, 1, -1, 1])
+        hyp.assume(len(lk) > 0)
+        sim = O.Sim(pos, ori, lk, rk, O.forster_table(1e15 if rate == "forster" else 1e13, *grids.values()),
+                    r_max, 2e5)
+        try:
+            sim.create_excitons(0, sections, 48, seed)
+        except RuntimeError:
+            hyp.assume(False)  # no site in the injection cell
+        (d / "in.json").write_text(json.dumps({"exciton monte carlo": mc}))
+        _, R = O.run_reference(str(d / "in.json"), str(d / "r.bin"), steps, seed, dump_csr=True)
+        assert np.array_equal(pos.ravel(), R["pos"])
+        csr = sim.build_csr()
+        for k in ("rowptr", "col", "cum"):
+            assert np.array_equal(csr[k], R["csr_" + k]), k
+        msd = sim.step(dt, steps)
+        e = sim.excitons()
+        assert np.array_equal(msd.ravel(), R["msd"])
+        for k, rk_ in (("site", "site"), ("pos", "xpos"), ("delta", "delta"), ("ff", "ff"), ("draws", "draws")):
+            assert np.array_equal(e[k].ravel(), R[rk_]), k
+
+    check()
