@@ -197,8 +197,10 @@ def test_empty_injection_region_is_refused_where_the_reference_divides_by_zero(t
 
 def test_live_reference_matches_oracle_on_random_set_ups(tmp_path_factory):
     """Random small set-ups (film, trim, cutoff, rate type, sections, time step, seeds) through the
-    reference and the oracle: rows, injection, final states and MSD sums equal bit for bit.  A
-    set-up whose injection cell holds no site is skipped (the reference divides by zero there)."""
+    reference and the oracle: rows, injection, final states and MSD sums equal bit for bit.  Set-ups
+    where the reference's behaviour is undefined are skipped: an injection cell with no site (it
+    divides by zero) and a site with an empty neighbour list (set_max_rate calls back() on the
+    empty vector, scatterer.h:91; the reference process can die of it)."""
     if not os.path.exists(O.REF_BIN):
         pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
     hyp = pytest.importorskip("hypothesis")
@@ -210,7 +212,8 @@ def test_live_reference_matches_oracle_on_random_set_ups(tmp_path_factory):
     grids = {"theta [degrees]": [0, 180, 21], "zshift [m]": [1.5e-9, 10e-9, 11],
              "axis shift 1 [m]": [-10e-9, 10e-9, 11], "axis shift 2 [m]": [-10e-9, 10e-9, 11]}
 
-    @hyp.settings(max_examples=60, deadline=None, database=None,
+    # the same 60 set-ups every run: the reference's own code may meet other undefined paths
+    @hyp.settings(max_examples=60, deadline=None, database=None, derandomize=True,
                   suppress_health_check=[hyp.HealthCheck.filter_too_much, hyp.HealthCheck.too_slow])
     @hyp.given(st.integers(2, 12), st.floats(5.0, 40.0), st.integers(0, 10**6), st.sampled_from(["forster", "wong"]),
                st.floats(2e-9, 12e-9), st.sampled_from([3, 5]), st.floats(5e-15, 2e-13), st.integers(1, 12),
@@ -230,6 +233,8 @@ def test_live_reference_matches_oracle_on_random_set_ups(tmp_path_factory):
         hyp.assume(len(lk) > 0)
         sim = O.Sim(pos, ori, lk, rk, O.forster_table(1e15 if rate == "forster" else 1e13, *grids.values()),
                     r_max, 2e5)
+        csr = sim.build_csr()
+        hyp.assume(np.all(np.diff(csr["rowptr"]) > 0))  # no empty neighbour list
         try:
             sim.create_excitons(0, sections, 48, seed)
         except RuntimeError:
@@ -237,7 +242,6 @@ def test_live_reference_matches_oracle_on_random_set_ups(tmp_path_factory):
         (d / "in.json").write_text(json.dumps({"exciton monte carlo": mc}))
         _, R = O.run_reference(str(d / "in.json"), str(d / "r.bin"), steps, seed, dump_csr=True)
         assert np.array_equal(pos.ravel(), R["pos"])
-        csr = sim.build_csr()
         for k in ("rowptr", "col", "cum"):
             assert np.array_equal(csr[k], R["csr_" + k]), k
         msd = sim.step(dt, steps)
