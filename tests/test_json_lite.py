@@ -113,7 +113,7 @@ def test_random_documents_round_trip(roundtrip, tmp_path_factory):
     docs = st.recursive(scalars, lambda c: st.lists(c, max_size=5) | st.dictionaries(text_st, c, max_size=5),
                         max_leaves=25)
 
-    @hyp.settings(max_examples=150, deadline=None, database=None)
+    @hyp.settings(max_examples=150, deadline=None, database=None, derandomize=True)
     @hyp.given(docs)
     def check(value):
         text = json.dumps(value, ensure_ascii=False)
@@ -168,7 +168,7 @@ def test_arbitrary_bytes_are_read_or_refused(roundtrip, tmp_path_factory):
     texts = st.lists(pieces, max_size=40).map("".join) | st.binary(max_size=60).map(
         lambda b: b.decode("latin-1"))
 
-    @hyp.settings(max_examples=300, deadline=None, database=None)
+    @hyp.settings(max_examples=300, deadline=None, database=None, derandomize=True)
     @hyp.given(texts)
     def check(text):
         p = d / "in.json"
