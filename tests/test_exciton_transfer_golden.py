@@ -2,7 +2,8 @@
 
 tests/golden/ref_et_*.npz are outputs of src/exciton_transfer/cnt.cpp and exciton_transfer.cpp
 compiled unchanged against oracle/shim_et/armadillo (tests/golden/make_golden_exciton.py): four
-donor/acceptor pairs, two of them from the reference's input.json.  Integer results (K2-extended
+donor/acceptor pairs, two of them from the reference's input.json.  Where oracle/_ref is built,
+three more pairs of short tubes (one with no matched states) are run through the reference now.  Integer results (K2-extended
 parameters, valleys, relevant-state windows, thermally relevant states, matched pairs) must be
 equal; sums to 1e-13 relative (they agree to ~1e-15); J to 1e-12, |Q|, M and the first-order
 rate to 1e-11.  Nothing phase-dependent is compared: eigenvector phases are not a convention.
@@ -22,20 +23,25 @@ _cache = {}
 def case(name):
     if name not in _cache:
         z = np.load(os.path.join(GOLDEN, name + ".npz"))
-        d = {k: z[k] for k in z.files}
-        tubes = {}
-        for p in ("d_", "a_"):
-            if p + "ints" not in d:  # one tube for both roles
-                tubes[p] = tubes["d_"]
-                for k in list(d):
-                    if k.startswith("d_"):
-                        d["a_" + k[2:]] = d[k]
-                continue
-            n, m, cells = (int(x) for x in d[p + "ints"][:3])
-            g = X.cnt_geometry(n, m, cells)
-            tubes[p] = (g, X.exciton_dispersion(g))
-        _cache[name] = d, tubes
+        _cache[name] = prepare({k: z[k] for k in z.files})
     return _cache[name]
+
+
+def prepare(d):
+    """The reference's records of one pair (a fixture, or a dump of ref_exciton run now) and the
+    restatement's two tubes built from the same chiralities and lengths."""
+    tubes = {}
+    for p in ("d_", "a_"):
+        if p + "ints" not in d:  # one tube for both roles
+            tubes[p] = tubes["d_"]
+            for k in list(d):
+                if k.startswith("d_"):
+                    d["a_" + k[2:]] = d[k]
+            continue
+        n, m, cells = (int(x) for x in d[p + "ints"][:3])
+        g = X.cnt_geometry(n, m, cells)
+        tubes[p] = (g, X.exciton_dispersion(g))
+    return d, tubes
 
 
 def rel(a, b):
@@ -46,7 +52,10 @@ def rel(a, b):
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("p", ["d_", "a_"])
 def test_tube_geometry_and_bands(name, p):
-    d, tubes = case(name)
+    check_tube(*case(name), p)
+
+
+def check_tube(d, tubes, p):
     g, ex = tubes[p]
     n, m, cells, nu, M, Q, t1, t2 = (int(x) for x in d[p + "ints"])
     assert (g["n"], g["m"], g["n_cells"], g["Nu"], g["M"], g["Q"], g["t1"], g["t2"]) == (n, m, cells, nu, M, Q, t1, t2)
@@ -64,7 +73,10 @@ def test_tube_geometry_and_bands(name, p):
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("p", ["d_", "a_"])
 def test_screening_and_excitons(name, p):
-    d, tubes = case(name)
+    check_screening(*case(name), p)
+
+
+def check_screening(d, tubes, p):
     g, ex = tubes[p]
     assert rel(d[p + "vq"], ex["vq"]) < 1e-13
     assert rel(d[p + "eps"], ex["eps"]) < 1e-13
@@ -82,6 +94,15 @@ def test_screening_and_excitons(name, p):
 @pytest.mark.parametrize("name", CASES)
 def test_states_matrix_elements_and_rates(name):
     d, tubes = case(name)
+    check_pair(d, tubes)
+    if name in ("ref_et_42_42", "ref_et_84_84"):  # identical tubes: bright k_cm = +-1 pairs
+        (gd, _), (ga, _) = tubes["d_"], tubes["a_"]
+        q_scale = X.q_coeff(gd, ga)
+        m_scale = q_scale * np.abs(d["pair_j"]).max() / np.sqrt(X.length_m(gd) * X.length_m(ga))
+        assert d["first_order"].min() > 1e-8 * (2 * X.PI / X.HB * m_scale ** 2 * X.lorentzian(0.0))
+
+
+def check_pair(d, tubes):
     (gd, exd), (ga, exa) = tubes["d_"], tubes["a_"]
     mn = exd["A2_singlet"].min()
     ds, as_ = X.relevant_states(exd, mn), X.relevant_states(exa, mn)
@@ -96,6 +117,11 @@ def test_states_matrix_elements_and_rates(name):
     # pair's natural scale: coeff (|Q| of a bright pair is of its order), coeff |J| / L for M, and
     # (2 pi / hbar) M_scale^2 L(0) for the rate.  In ref_et_42_65 and ref_et_75_84 every matched
     # pair is dark and the reference's rates are that residue (1e-20 and 1e-49 /s).
+    if not pairs:  # no state pair within the Lorentzian: no transfer, in both codes exactly
+        assert d["pair_j"].size == 0
+        for gi, (zs, a1, a2, th) in enumerate(d["geometries"]):
+            assert X.first_order(gd, exd, ga, exa, zs, (a1, a2), th) == d["first_order"][gi] == 0.0
+        return
     q_scale = X.q_coeff(gd, ga)
     l2 = np.sqrt(X.length_m(gd) * X.length_m(ga))
     m_scale = q_scale * np.abs(d["pair_j"]).max() / l2
@@ -111,5 +137,43 @@ def test_states_matrix_elements_and_rates(name):
         r = X.first_order(gd, exd, ga, exa, zs, (a1, a2), th)
         ref = d["first_order"][gi]
         assert abs(r - ref) <= 1e-11 * max(abs(ref), rate_scale), (gi, r, ref)
-    if name in ("ref_et_42_42", "ref_et_84_84"):  # identical tubes: bright k_cm = +-1 pairs
-        assert d["first_order"].min() > 1e-8 * rate_scale
+
+
+NM = 1e-9
+LIVE = {
+    # donor (n, m, cells), acceptor (n, m, cells), geometries (z_shift, axis shift 1, axis shift 2, theta)
+    "64_64": ((6, 4, 4), (6, 4, 4), [(1.9 * NM, 0, 0, 0.3), (4 * NM, 1 * NM, 0, 1.1)]),
+    "54_64": ((5, 4, 4), (6, 4, 4), [(1.9 * NM, 0, 0, 0.0), (3 * NM, 0, 1 * NM, 0.8)]),
+    "73_73": ((7, 3, 3), (7, 3, 3), [(2.5 * NM, 0.5 * NM, -0.5 * NM, 0.2), (1.6 * NM, 0, 0, 1.5)]),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LIVE))
+def test_restatement_matches_the_live_reference_on_more_tubes(name, tmp_path):
+    """More tube pairs (short tubes, other chiralities) through the reference's exciton code run
+    right now (oracle/_ref/ref_exciton): the same comparisons as the fixtures."""
+    import importlib.util
+    import subprocess
+
+    exe = os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "ref_exciton")
+    if not os.path.exists(exe):
+        pytest.skip("oracle/_ref not built: build() compiles it where the reference sources are present")
+    spec = importlib.util.spec_from_file_location("make_golden_exciton", os.path.join(GOLDEN, "make_golden_exciton.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    donor, acceptor, geos = LIVE[name]
+    path = str(tmp_path / "ref.bin")
+    args = [exe, path, *(str(x) for x in donor + acceptor)]
+    for g in geos:
+        args += [repr(float(x)) for x in g]
+    r = subprocess.run(args, capture_output=True, text=True, env=dict(os.environ, KMC_REF_SCRATCH=str(tmp_path)),
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    d = mg.read_dump(path)
+    if donor == acceptor:
+        d = {k: v for k, v in d.items() if not k.startswith("a_")}
+    d, tubes = prepare(d)
+    for p in ("d_", "a_"):
+        check_tube(d, tubes, p)
+        check_screening(d, tubes, p)
+    check_pair(d, tubes)
